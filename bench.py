@@ -1,0 +1,348 @@
+"""Benchmark: stiffness (K) assembly throughput on the 3D Hooke workload
+"unit cube, structured 40x40x40 hex27, 3x3x3 Gauss, E=2.1e5, nu=0.3"
+(1,594,323 DoFs, 297,685,449 structural CSC entries), in GNNZ/s = structural
+nnz / assembly time with the CSC pattern prebuilt.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form fp64|fp32q]
+  python bench.py --impl reference ...   CPU restatement of the reference's
+                                          threaded direct-CSC assembly
+
+One JSON line on stdout (rank 0).  Fields follow the repository's bench
+contract: value (device-resident inputs, CUDA events on the launching
+stream), e2e (through the C-ABI from pinned host buffers: mesh upload +
+assembly + CSC copy-back), roofline of the dominant kernel, cpu_baseline,
+clocks sampled during the timed region, gpu_launches.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_CELLS = 40
+ORDER = 2
+E, NU = 2.1e5, 0.3
+WORKLOAD = "hooke3d-unit-cube-hex27-40x40x40"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="fp64", choices=["fp64", "fp32q"])
+    ap.add_argument("--n", type=int, default=N_CELLS)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.tmp = None
+
+    def __enter__(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc or not self.tmp:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.tmp.flush()
+        rows = []
+        with open(self.tmp.name) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.tmp.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, name in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(rows), "reasons": sorted(reasons)}
+
+
+# ----------------------------------------------------------------- workload
+def algorithmic(mesh, nnz):
+    """Algorithmic bytes of one assembly (structural nnz values written, node
+    coordinates and connectivity read) and FP64 operations of the element
+    kernel under the arithmetic contract (FMA = 2 flops)."""
+    npe, nip, d = mesh.npe, 27 if ORDER == 2 else (ORDER + 1) ** 3, 3
+    bytes_ = 8 * nnz + 24 * mesh.non + 4 * npe * mesh.nel
+    npairs = npe * (npe + 1) // 2
+    geo = nip * (2 * npe * d * d + 60)             # J, cofactors, det, inverse
+    grads = nip * npe * (2 * d * d + d)            # J^-T grad + weighting
+    pairs = nip * ((npairs - npe) * 2 * d * d + npe * 2 * 6)
+    combine = npairs * (3 * d * d + 6)
+    flops = mesh.nel * (geo + grads + pairs + combine)
+    return bytes_, flops
+
+
+def cpu_baseline(llf, orc, rank0=True, target_s=10.0):
+    """Oracle's threaded direct-CSC assembly (the reference's fastest CPU
+    path restated) on a slab of the same mesh: 40x40xk hex27 cells."""
+    threads = orc.num_threads()
+    k = 4
+    while True:
+        m = llf.structured_box_mesh(lz=k / N_CELLS, n=N_CELLS, order=ORDER)
+        rule = llf._lib.builtin_rule(m.family, m.order)
+        pat = orc.pattern(m.non, m.conn, 3)
+        t = orc.assemble_threaded(orc.ELASTIC, 0, 3, 3, m.xyz, m.conn, rule, [E, NU], pat,
+                                  nthreads=threads)
+        if t * 2 > target_s or k >= N_CELLS:
+            break
+        k = min(N_CELLS, max(k * 2, int(k * target_s / max(t, 1e-3) / 2)))
+    return {"value": pat.nnz / t / 1e9, "unit": "GNNZ/s", "cores": threads, "kind": "port",
+            "sample": f"40x40x{k} hex27 slab of the same mesh ({m.nel} elements, {pat.nnz} structural nnz), "
+                      f"{t:.2f} s, oracle threaded direct-CSC assembly"}, t
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import __graft_entry__ as entry
+    entry.load_oracle().build()
+    llf = entry.load_package()
+    orc = entry.load_oracle()
+    times, info = [], None
+    for i in range(args.warmup + args.steps):
+        info, t = cpu_baseline(llf, orc, target_s=4.0)
+        if i >= args.warmup:
+            times.append(info["value"])
+    v = statistics.median(times)
+    info["value"] = v
+    out = {"metric": "K-assembly throughput (structural nnz / s)", "value": v, "unit": "GNNZ/s",
+           "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic structured mesh", "config": {"workload": WORKLOAD, "form": "fp64"},
+           "cpu_baseline": info, "e2e": {"value": v, "unit": "GNNZ/s", "h2d_bytes_per_step": 0,
+                                          "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_env()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    os.environ["LLF_DEVICE"] = str(local)
+    import __graft_entry__ as entry
+    llf = entry.load_package()
+    L = llf._lib
+    form = L.FP32Q if args.form == "fp32q" else L.FP64
+
+    mesh = llf.structured_box_mesh(n=args.n, order=ORDER)
+    ctx = L.default_context()
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+    dm = L.DeviceMesh(ctx, 3, mesh.xyz, mesh.conn, mesh.family, mesh.order)
+    t0 = time.perf_counter()
+    pat = L.DevicePattern(dm, 3)
+    pattern_s = time.perf_counter() - t0
+    nnz = pat.nnz
+    Ea, nua = L.f64([E]), L.f64([NU])
+
+    def assemble():
+        h = L.C.c_void_p()
+        ctx.check(L.lib().llf_assemble_stiffness(ctx.h, dm.h, pat.h, L.SOLID, L.ptr(Ea, L.C.c_double),
+                                                 L.ptr(nua, L.C.c_double), 1, 1.0, form, L.C.byref(h)))
+        return L.DeviceMatrix(ctx, h, pat)
+
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    for _ in range(args.warmup):
+        Km = assemble()
+        del Km
+    ctx.sync()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+
+    ctx.profile_reset()
+    ctx.profile(True)
+    evs = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+            Km = assemble()
+            with torch.cuda.stream(stream):
+                b.record(stream)
+            stored = Km.nnz()
+            del Km
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        ctx.sync()
+    ctx.profile(False)
+    prof = ctx.profile_report()
+    launches = ctx.launches()
+    ms = [a.elapsed_time(b) for a, b in evs]
+    ms_step = sum(ms) / len(ms)
+    if world > 1:
+        t = torch.tensor([ms_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * nnz / (ms_step * 1e-3) / 1e9
+
+    bytes_alg, flops = algorithmic(mesh, nnz)
+    hbm_peak, peak_kind = peaks()
+    # dominant kernel by summed device time in the timed region
+    kname, kstat = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    k_ms = kstat["ms"] / max(kstat["launches"], 1)
+    per_kernel = {k: {"launches": v["launches"], "ms_per_launch": v["ms"] / max(v["launches"], 1),
+                      "share": v["ms"] / sum(x["ms"] for x in prof.values())} for k, v in prof.items()}
+    asm_ms = sum(v["ms"] for v in prof.values()) / args.steps
+    achieved = bytes_alg / (asm_ms * 1e-3) / 1e9
+
+    # FP64 rate of the dominant element kernel vs a measured DGEMM
+    fp64_peak = None
+    try:
+        x = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+        torch.matmul(x, x)
+        torch.cuda.synchronize()
+        best = 1e9
+        for _ in range(3):
+            s0 = torch.cuda.Event(enable_timing=True); s1 = torch.cuda.Event(enable_timing=True)
+            s0.record(); torch.matmul(x, x); s1.record(); torch.cuda.synchronize()
+            best = min(best, s0.elapsed_time(s1))
+        fp64_peak = 2 * 8192 ** 3 / (best * 1e-3) / 1e12
+        del x
+    except Exception:
+        pass
+    elem_ms = prof.get("k_elem_fp64", {}).get("ms", 0.0) / max(prof.get("k_elem_fp64", {}).get("launches", 1), 1)
+    fp64_achieved = flops / (elem_ms * 1e-3) / 1e12 if elem_ms > 0 else None
+
+    roofline = {"bound": "hbm", "kernel": "assembly (all kernels of one llf_assemble_stiffness)",
+                "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes": bytes_alg, "dominant_kernel": kname, "dominant_ms": k_ms,
+                "per_kernel": per_kernel,
+                "fp64": {"element_kernel_flops": flops, "achieved_tflops": fp64_achieved,
+                         "dgemm_peak_tflops_measured": fp64_peak,
+                         "frac": (fp64_achieved / fp64_peak) if (fp64_achieved and fp64_peak) else None}}
+
+    # e2e through the C-ABI from pinned host buffers
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        xyz_h = torch.from_numpy(L.f64(mesh.xyz)).pin_memory()
+        conn_h = torch.from_numpy(L.i64a(mesh.conn)).pin_memory()
+        Km = assemble()
+        nnz_s = Km.nnz()
+        del Km
+        colptr_h = torch.empty(3 * mesh.non + 1, dtype=torch.int64).pin_memory()
+        rowval_h = torch.empty(nnz_s, dtype=torch.int64).pin_memory()
+        nzval_h = torch.empty(nnz_s, dtype=torch.float64).pin_memory()
+        P = lambda t, ct: L.C.cast(t.data_ptr(), L.C.POINTER(ct))
+        e2e_steps = max(2, min(args.steps, 3))
+        ts = []
+        for i in range(1 + e2e_steps):
+            ctx.sync()
+            t0 = time.perf_counter()
+            ctx.check(L.lib().llf_mesh_update(ctx.h, dm.h, P(xyz_h, L.C.c_double), P(conn_h, L.C.c_int64)))
+            Km = assemble()
+            ctx.check(L.lib().llf_matrix_copy_csc(ctx.h, Km.h, P(colptr_h, L.C.c_int64),
+                                                  P(rowval_h, L.C.c_int64), P(nzval_h, L.C.c_double)))
+            t1 = time.perf_counter()
+            del Km
+            if i > 0:
+                ts.append(t1 - t0)
+        te = statistics.median(ts)
+        e2e = {"value": nnz / te / 1e9, "unit": "GNNZ/s", "ms_per_step": te * 1e3,
+               "h2d_bytes_per_step": xyz_h.numel() * 8 + conn_h.numel() * 8,
+               "d2h_bytes_per_step": colptr_h.numel() * 8 + 2 * nnz_s * 8}
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        try:
+            import __graft_entry__ as entry2
+            orc = entry2.load_oracle()
+            cpu, _ = cpu_baseline(llf, orc)
+        except Exception as ex:  # the baseline is reported, never required
+            cpu = {"value": None, "error": str(ex)}
+
+    if rank == 0:
+        out = {"metric": "K-assembly throughput (structural nnz / s)", "value": value, "unit": "GNNZ/s",
+               "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f64" if form == L.FP64 else "f32-quadrature/f64-accumulate",
+               "data": "synthetic structured mesh (unit cube)",
+               "config": {"workload": WORKLOAD, "elements": mesh.nel, "dofs": 3 * mesh.non,
+                          "structural_nnz": nnz, "stored_nnz": stored, "form": args.form,
+                          "pattern_build_s": pattern_s, "l2": "256 MB buffer written before every timed step",
+                          "parallelism": "replicas" if world > 1 else "single"},
+               "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+               "clocks": clk.summary()}
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,322 @@
+/*
+ * llfem_gb300.h — C-ABI of the GB300 operator-assembly + iterative-solve library.
+ *
+ * This is the drop-in boundary behind LowLevelFEM.jl's own Julia API for its
+ * assembly/solve hot path.  Every entry point is `extern "C"`, takes plain
+ * pointers and sizes, returns an int status (LLF_OK == 0, negative on error)
+ * and leaves a message readable through llf_last_error().  No entry point
+ * throws, aborts, or falls back to host computation: when the CUDA runtime or
+ * a device is missing, calls that need the GPU return LLF_ERR_CUDA.
+ *
+ * Conventions kept from the reference (LowLevelFEM.jl v1.13.31):
+ *   - node tags are dense and 1-based (src/multifield.jl:1602-1611);
+ *   - DoF numbering is interleaved, dof = (node-1)*pdim + comp (1-based,
+ *     src/general.jl:5245-5247); internally 0-based, 1-based at copy-out;
+ *   - matrices leave the library as SparseMatrixCSC{Float64,Int64} arrays:
+ *     1-based Int64 colptr (n+1) and rowval (nnz), Float64 nzval, rows sorted
+ *     within each column, exact zeros removed as dropzeros! does
+ *     (src/linear.jl:323-324);
+ *   - element node tables (connectivity) are element-major, npe entries per
+ *     element, in the element family's node order (gmsh order for the tables
+ *     the caller uploads, this library's order for its built-in tables).
+ *
+ * Objects (opaque, all device-resident):
+ *   llf_ctx      one CUDA device + one stream + last-error text; not thread
+ *                safe — use one context per host thread / Julia task.
+ *   llf_mesh     node coordinates, connectivity, node->element adjacency,
+ *                quadrature + shape tables, per-element material index.
+ *   llf_pattern  structural CSC pattern of a mesh for pdim components per
+ *                node (node-level adjacency expanded to DoFs).
+ *   llf_matrix   values on a pattern (structural nzval) plus, after
+ *                assembly, the stored (dropzeros'ed) form.
+ */
+#ifndef LLFEM_GB300_H
+#define LLFEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define LLF_OK                  0
+#define LLF_ERR_ARG            -1   /* bad argument (null pointer, size, enum)   */
+#define LLF_ERR_CUDA           -2   /* CUDA runtime error or no device           */
+#define LLF_ERR_MESH           -3   /* bad connectivity / non-positive Jacobian  */
+#define LLF_ERR_NOT_CONVERGED  -4   /* iterative solve hit maxiter               */
+#define LLF_ERR_STATE          -5   /* object used with a mismatched partner     */
+#define LLF_ERR_UNSUPPORTED    -6   /* element family/order/problem not built    */
+#define LLF_ERR_LIMIT          -7   /* a documented size limit was exceeded      */
+#define LLF_ERR_NUMERIC        -8   /* NaN/Inf in input, or singular pivot      */
+
+/* ---- element families (values equal gmsh's first-order type numbers) ---- */
+#define LLF_LINE  1
+#define LLF_TRI   2
+#define LLF_QUAD  3
+#define LLF_TET   4
+#define LLF_HEX   5
+
+/* ---- problem types (Problem.type of src/general.jl:478-632) ------------- */
+#define LLF_SOLID                  0   /* :Solid,   dim 3, pdim 3 */
+#define LLF_PLANE_STRESS           1   /* :PlaneStress, dim 2, pdim 2 */
+#define LLF_PLANE_STRAIN           2   /* :PlaneStrain, dim 2, pdim 2 */
+#define LLF_HEAT_CONDUCTION        3   /* :HeatConduction, dim 3, pdim 1 */
+#define LLF_PLANE_HEAT_CONDUCTION  4   /* :PlaneHeatConduction, dim 2, pdim 1 */
+
+/* ---- arithmetic forms ---------------------------------------------------- */
+#define LLF_FP64   0   /* plain form: every operation in IEEE FP64, fixed order */
+#define LLF_FP32Q  1   /* precision form: FP32 quadrature, FP64 accumulation    */
+
+/* ---- hyperelastic laws for the Total Lagrangian kernels ----------------- */
+#define LLF_LAW_CONSTANT_C     0   /* params: 36 values, 6x6 Voigt tangent, column-major */
+#define LLF_LAW_NEOHOOKE_COMP  1   /* params: mu, lambda; psi = mu/2(I1-3) - mu lnJ + lambda/2 (lnJ)^2 */
+#define LLF_LAW_SVK            2   /* params: mu, lambda; psi = lambda/2 tr(E)^2 + mu E:E */
+
+/* ---- preconditioners for llf_pcg ---------------------------------------- */
+#define LLF_PRECOND_NONE     0   /* IterativeSolvers Identity() (src/linear.jl:3711) */
+#define LLF_PRECOND_JACOBI   1
+#define LLF_PRECOND_BJACOBI  2   /* pdim x pdim node-block Jacobi */
+
+typedef struct llf_ctx     llf_ctx;
+typedef struct llf_mesh    llf_mesh;
+typedef struct llf_pattern llf_pattern;
+typedef struct llf_matrix  llf_matrix;
+
+/* ======================================================================== */
+/* Library / context                                                        */
+/* ======================================================================== */
+
+/* Version string of the shared library. */
+const char *llf_version(void);
+
+/* Create a context on CUDA device `device` with its own non-blocking stream.
+ * Replaces nothing in the reference (Julia has no device); the Julia shim
+ * creates one per task. */
+int llf_ctx_create(int device, llf_ctx **out);
+int llf_ctx_destroy(llf_ctx *ctx);
+
+/* Message of the last failing call on this context ("" after success).
+ * Plays the role of the reference's error("...") text (e.g. src/linear.jl:185). */
+const char *llf_last_error(const llf_ctx *ctx);
+
+/* Synchronise the context's stream (all queued work finished). */
+int llf_ctx_sync(llf_ctx *ctx);
+
+/* The stream the context launches on, as a cudaStream_t cast to void*. */
+int llf_ctx_stream(llf_ctx *ctx, void **stream);
+
+/* Tracing (no counterpart in the reference, which times with @time).
+ * Every kernel launch of the context is counted; with profiling enabled,
+ * CUDA events bracket each launch on the context stream and the report
+ * holds per-kernel launch counts and summed device milliseconds as JSON
+ * {"kernel": {"launches": n, "ms": t}, ...}.  report writes at most len
+ * bytes (NUL-terminated) and returns the full length through *needed. */
+int llf_profile_enable(llf_ctx *ctx, int on);
+int llf_profile_reset(llf_ctx *ctx);
+int llf_profile_report(llf_ctx *ctx, char *buf, int64_t len, int64_t *needed);
+int llf_launch_count(llf_ctx *ctx, int64_t *launches);
+
+/* ======================================================================== */
+/* Built-in quadrature and shape tables (host only, no GPU needed)          */
+/* ======================================================================== */
+
+/* Quadrature rule exact to degree 2*order+1 and Lagrange shape tables of one
+ * element family/order, standing in for gmsh's
+ *   getIntegrationPoints(et, "Gauss"*(2*order+1))   (src/linear.jl:235)
+ *   getBasisFunctions(et, ip, "Lagrange"/"GradLagrange") (src/linear.jl:238).
+ * Two-phase: call with null arrays to obtain *nip and *npe, then again with
+ * arrays of size xi[3*nip], w[nip], N[nip*npe], dN[3*nip*npe],
+ * node_ref[3*npe].  N[q*npe+a] = N_a(xi_q); dN[(q*npe+a)*3+j] = dN_a/dxi_j.
+ * Reference elements follow gmsh: [-1,1]^d for quads/hexes, the unit
+ * simplex for triangles/tetrahedra. */
+int llf_builtin_rule(int family, int order, int *nip, int *npe,
+                     double *xi, double *w, double *N, double *dN,
+                     double *node_ref);
+
+/* Reference gradients of the built-in basis at the element's own nodes,
+ * dNn[(k*npe+l)*3+j] = dN_l/dxi_j at node k (npe*npe*3 values) — the table
+ * ∇ evaluates at element nodes (gmsh getBasisFunctions at the element's
+ * local node coordinates, src/nabla.jl:124-126). */
+int llf_builtin_node_gradients(int family, int order, double *dNn);
+
+/* ======================================================================== */
+/* Mesh                                                                     */
+/* ======================================================================== */
+
+/* Upload a mesh: xyz[3*non] (x,y,z per node; z ignored when dim==2),
+ * conn[npe*nel] 1-based node tags, element-major.  The built-in tables of
+ * (family, order) are attached; llf_tables_upload replaces them.
+ * Replaces the gmsh queries getNodes / getElementsByType of
+ * src/linear.jl:241 and src/multifield.jl:1612-1648. */
+int llf_mesh_upload(llf_ctx *ctx, int dim, int64_t non, const double *xyz,
+                    int64_t nel, int npe, const int64_t *conn,
+                    int family, int order, llf_mesh **out);
+
+/* Overwrite the coordinates (and, if conn != NULL, the connectivity, which
+ * must describe the same adjacency) of an uploaded mesh; used when node
+ * positions move but the pattern is reused. */
+int llf_mesh_update(llf_ctx *ctx, llf_mesh *mesh, const double *xyz,
+                    const int64_t *conn);
+
+/* Per-element material index (0..nmat-1) or -1 for "not in any material
+ * group" (such elements contribute nothing, as elements outside every
+ * Material physical group do in src/linear.jl:211-232).  NULL = all 0. */
+int llf_mesh_set_materials(llf_ctx *ctx, llf_mesh *mesh,
+                           const int32_t *elem_mat);
+
+/* Replace the quadrature/shape tables with caller-supplied ones (e.g. gmsh's
+ * own getIntegrationPoints / getBasisFunctions output), same layout as
+ * llf_builtin_rule.  N may be NULL when only gradients are needed. */
+int llf_tables_upload(llf_ctx *ctx, llf_mesh *mesh, int nip, const double *w,
+                      const double *N, const double *dN);
+
+int llf_mesh_destroy(llf_ctx *ctx, llf_mesh *mesh);
+
+/* ======================================================================== */
+/* CSC pattern                                                              */
+/* ======================================================================== */
+
+/* Structural CSC pattern for pdim components per node: node adjacency
+ * through shared elements, rows sorted per column, components expanded —
+ * build_csc_pattern of src/multifield.jl:2083-2250.  *nnz_out receives the
+ * structural nnz. */
+int llf_pattern_build(llf_ctx *ctx, llf_mesh *mesh, int pdim,
+                      int64_t *nnz_out, llf_pattern **out);
+
+/* Copy the structural pattern to host arrays: colptr[n+1], rowval[nnz],
+ * both 1-based Int64. */
+int llf_pattern_copy(llf_ctx *ctx, const llf_pattern *pat, int64_t *colptr,
+                     int64_t *rowval);
+
+int llf_pattern_info(const llf_pattern *pat, int64_t *ndof, int64_t *nnz,
+                     int *pdim);
+
+int llf_pattern_destroy(llf_ctx *ctx, llf_pattern *pat);
+
+/* ======================================================================== */
+/* Assembly                                                                 */
+/* ======================================================================== */
+/* All assembly calls create a new device matrix on the pattern, fill the
+ * structural values, then apply dropzeros!.  Material arrays hold one value
+ * per material index (nmat entries). `form` is LLF_FP64 or LLF_FP32Q. */
+
+/* K = sum_e sum_q B^T D B b detJ w — stiffnessMatrix / stiffnessMatrixSolid,
+ * src/linear.jl:70-87, :154-188, :190-330.  ptype LLF_SOLID,
+ * LLF_PLANE_STRESS (b = thickness) or LLF_PLANE_STRAIN (b = 1). */
+int llf_assemble_stiffness(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
+                           int ptype, const double *E, const double *nu,
+                           int nmat, double thickness, int form,
+                           llf_matrix **out);
+
+/* M = rho b sum H^T H detJ w, consistent (lumped == 0) or row-sum lumped —
+ * massMatrix / massMatrixSolid, src/linear.jl:1843-2004. */
+int llf_assemble_mass(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
+                      int ptype, const double *rho, int nmat,
+                      double thickness, int lumped, int form,
+                      llf_matrix **out);
+
+/* K_T = sum grad N^T grad N k b detJ w — heatConductionMatrix /
+ * heatCondMatrixSolid, src/heat.jl:28-137 (b = thickness in 2D and 3D). */
+int llf_assemble_heat(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
+                      int ptype, const double *k, int nmat, double thickness,
+                      int form, llf_matrix **out);
+
+/* Total Lagrangian material tangent K_mat = sum B(F)^T C B(F) detJ0 w —
+ * materialTangentMatrix, src/nonlinear.jl:2083-2268.  Felem[9*npe*nel] holds
+ * the elementwise nodal deformation gradient, column-major 3x3 per element
+ * node (the TensorField layout of src/nonlinear.jl:2183-2199).  `law` and
+ * params[] as LLF_LAW_*; for LLF_LAW_CONSTANT_C, params is the 6x6 matrix. */
+int llf_tl_material_tangent(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
+                            const double *Felem, int law,
+                            const double *params, int nparams,
+                            llf_matrix **out);
+
+/* Geometric (initial-stress) stiffness K_geo[a i, b i] = sum grad Na^T S
+ * grad Nb detJ0 w, identity component block — initialStressMatrix,
+ * src/nonlinear.jl:2417-2595.  Exactly one of Selem (elementwise nodal PK2
+ * stress, 9*npe*nel) or Celem (elementwise nodal right Cauchy-Green tensor,
+ * with `law`) is non-NULL. */
+int llf_tl_initial_stress(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
+                          const double *Selem, const double *Celem, int law,
+                          const double *params, int nparams,
+                          llf_matrix **out);
+
+/* Internal force f_int[a i] = sum P_iJ dNa/dX_J detJ0 w, P = F S —
+ * internalForceVector, src/nonlinear.jl:2738-2910.  Exactly one of Pelem
+ * (elementwise nodal first Piola-Kirchhoff stress) or Felem (with `law`) is
+ * non-NULL.  f_int[3*non] is a host array, overwritten. */
+int llf_tl_internal_force(llf_ctx *ctx, llf_mesh *mesh, const double *Pelem,
+                          const double *Felem, int law, const double *params,
+                          int nparams, double *f_int);
+
+/* Elementwise nodal gradient of a nodal vector field, T[i,j] = du_i/dX_j,
+ * column-major 3x3 per element node (9*npe*nel) — the :vector_grad branch of
+ * ∇ / u∘∇, src/nabla.jl:77-311 and src/operators.jl:2875-2881.  u[pdim*non]
+ * interleaved; with add_identity != 0 the result is F = I + u∘∇. */
+int llf_grad_elementwise(llf_ctx *ctx, llf_mesh *mesh, const double *u,
+                         int add_identity, double *out);
+
+/* Consistent nodal load of boundary elements: f += sum H^T t Ja w over the
+ * elements of `bmesh` (a mesh of dimension dim-1 embedded in dim), with t a
+ * constant pdim-vector (t_const) or nodal values t_nodal[pdim*non_b] per
+ * boundary-mesh node (NULL to use t_const).  Ja is the line/area measure
+ * (times thickness for 2D problems) — loadVector, src/linear.jl:3088-3434,
+ * Ja at :3378-3407.  Node tags of bmesh index the volume mesh's nodes;
+ * f[pdim*non] is a host array accumulated into. */
+int llf_load_vector(llf_ctx *ctx, llf_mesh *bmesh, int problem_dim, int pdim,
+                    const double *t_const, const double *t_nodal,
+                    double thickness, double *f, int64_t ndof);
+
+/* ======================================================================== */
+/* Matrices                                                                 */
+/* ======================================================================== */
+
+/* Stored nnz after dropzeros!. */
+int llf_matrix_nnz(llf_ctx *ctx, const llf_matrix *m, int64_t *nnz);
+
+/* Copy the stored CSC to host: colptr[n+1], rowval[nnz] (1-based Int64),
+ * nzval[nnz]. Any pointer may be NULL to skip that array. */
+int llf_matrix_copy_csc(llf_ctx *ctx, const llf_matrix *m, int64_t *colptr,
+                        int64_t *rowval, double *nzval);
+
+/* Structural values (length = structural nnz of the pattern) to host. */
+int llf_matrix_copy_structural(llf_ctx *ctx, const llf_matrix *m,
+                               double *nzval);
+
+/* C = a*A + b*B on the same pattern, then dropzeros! — SystemMatrix +/-
+ * of src/operators.jl:2421-2486 (Kmat + Kgeo, K - Kext). */
+int llf_matrix_axpby(llf_ctx *ctx, double a, const llf_matrix *A, double b,
+                     const llf_matrix *B, llf_matrix **out);
+
+/* y = A x with host vectors of length n. */
+int llf_matrix_spmv(llf_ctx *ctx, const llf_matrix *m, const double *x,
+                    double *y);
+
+int llf_matrix_destroy(llf_ctx *ctx, llf_matrix *m);
+
+/* ======================================================================== */
+/* Solve                                                                    */
+/* ======================================================================== */
+
+/* Condensed Dirichlet solve by preconditioned CG — the iterative branch of
+ * solveDisplacement / solveTemperature / solveField (src/linear.jl:3711-3743,
+ * :3801-3834; src/heat.jl:1020-1084; src/poisson.jl:1432-1546):
+ *   fixed[i] != 0 marks constrained DoFs, whose prescribed values are taken
+ *   from x on entry (applyBoundaryConditions!, src/linear.jl:3505-3563);
+ *   f_kin = A[:,fixed] x[fixed]; x[free] solves
+ *   A[free,free] x[free] = b[free] - f_kin[free]
+ * with IterativeSolvers.cg's recurrence and stopping rule
+ * (||r|| <= reltol ||b_free - f_kin_free||, x0 = 0 on the free DoFs).
+ * All vectors are host arrays of length n.  *iters and *relres report the
+ * iteration count and final relative residual; LLF_ERR_NOT_CONVERGED is
+ * returned (x still holds the last iterate) when maxiter is reached. */
+int llf_pcg(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x,
+            const uint8_t *fixed, int precond, double reltol, int64_t maxiter,
+            int64_t *iters, double *relres);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LLFEM_GB300_H */

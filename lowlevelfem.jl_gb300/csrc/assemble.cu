@@ -1,0 +1,634 @@
+// Element-operator assembly into the reference's CSC layout.
+//
+// Pipeline (one call of llf_assemble_*):
+//   k_elem_fp64  one CTA per element at a time (grid-stride, persistent):
+//                element node coordinates gathered once into shared memory,
+//                the reference shape gradients staged in shared memory for
+//                the CTA's lifetime, Jacobian / inverse / physical gradients
+//                per integration point, then the upper-triangle node-pair
+//                blocks of the element matrix written to a pair buffer
+//                (elements x pairs x block);
+//   k_gather     one warp per column node: for every row node of the column
+//                the contributing elements are the intersection of the two
+//                nodes' element lists (both sorted), so every structural
+//                entry is summed over its elements in element order —
+//                the order SparseArrays.sparse combines the reference's
+//                triplets (src/linear.jl:314-323);
+//   finalize     dropzeros! (src/linear.jl:324): count, scan, compact into
+//                1-based Int64 SparseMatrixCSC arrays.
+// Every floating-point operation of the FP64 form is an explicit IEEE
+// intrinsic (__dmul_rn, __dadd_rn, __fma_rn, __drcp_rn), so no contraction
+// or reassociation can move the result away from the CPU oracle's.
+#include "common.cuh"
+
+namespace {
+
+constexpr int ELEM_THREADS = 128;
+
+struct ElemArgs {
+  const double *xyz;
+  const int32_t *conn;
+  const int32_t *emat;
+  int64_t nel;
+  int npe, nip, npairs;
+  const double *w, *N, *dN;  // device tables
+  const double *c1, *c2;     // per-material coefficients
+  double *Kp;                // nel * npairs * BS
+  double *scratch;           // per-CTA global scratch (when not in smem)
+  int64_t scratch_stride;    // doubles per CTA
+  unsigned *status;
+};
+
+__device__ __forceinline__ int pair_offset(int a, int npe) {
+  return a * npe - (a * (a - 1)) / 2;
+}
+__device__ __forceinline__ void pair_decode(int pi, int npe, int &a, int &b) {
+  int lo = 0, hi = npe - 1;
+  while (lo < hi) {  // largest a with pair_offset(a) <= pi
+    int mid = (lo + hi + 1) >> 1;
+    if (pair_offset(mid, npe) <= pi) lo = mid; else hi = mid - 1;
+  }
+  a = lo;
+  b = a + (pi - pair_offset(a, npe));
+}
+
+// Geometry at point q (contract of the oracle): returns det, fills inv
+// (row-major invJ[i][j]).
+template <int DIM>
+__device__ __forceinline__ double geom_point(const double *sX, const double *sdNq,
+                                             int npe, double *inv) {
+  double J[DIM][DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      double acc = 0.0;
+      for (int a = 0; a < npe; ++a) acc = __fma_rn(sX[a * DIM + i], sdNq[a * DIM + j], acc);
+      J[i][j] = acc;
+    }
+  double det, rdet;
+  if (DIM == 3) {
+#define M(x, y) J[(x) % DIM][(y) % DIM]
+    double c00 = __dsub_rn(__dmul_rn(M(1, 1), M(2, 2)), __dmul_rn(M(1, 2), M(2, 1)));
+    double c01 = -__dsub_rn(__dmul_rn(M(1, 0), M(2, 2)), __dmul_rn(M(1, 2), M(2, 0)));
+    double c02 = __dsub_rn(__dmul_rn(M(1, 0), M(2, 1)), __dmul_rn(M(1, 1), M(2, 0)));
+    double c10 = -__dsub_rn(__dmul_rn(M(0, 1), M(2, 2)), __dmul_rn(M(0, 2), M(2, 1)));
+    double c11 = __dsub_rn(__dmul_rn(M(0, 0), M(2, 2)), __dmul_rn(M(0, 2), M(2, 0)));
+    double c12 = -__dsub_rn(__dmul_rn(M(0, 0), M(2, 1)), __dmul_rn(M(0, 1), M(2, 0)));
+    double c20 = __dsub_rn(__dmul_rn(M(0, 1), M(1, 2)), __dmul_rn(M(0, 2), M(1, 1)));
+    double c21 = -__dsub_rn(__dmul_rn(M(0, 0), M(1, 2)), __dmul_rn(M(0, 2), M(1, 0)));
+    double c22 = __dsub_rn(__dmul_rn(M(0, 0), M(1, 1)), __dmul_rn(M(0, 1), M(1, 0)));
+#undef M
+    det = __dadd_rn(__dadd_rn(__dmul_rn(J[0][0], c00), __dmul_rn(J[0][1 % DIM], c01)),
+                    __dmul_rn(J[0][2 % DIM], c02));
+    rdet = __drcp_rn(det);
+    inv[0] = __dmul_rn(c00, rdet); inv[1] = __dmul_rn(c10, rdet); inv[2] = __dmul_rn(c20, rdet);
+    inv[3] = __dmul_rn(c01, rdet); inv[4] = __dmul_rn(c11, rdet); inv[5] = __dmul_rn(c21, rdet);
+    inv[6] = __dmul_rn(c02, rdet); inv[7] = __dmul_rn(c12, rdet); inv[8] = __dmul_rn(c22, rdet);
+  } else {
+    det = __dsub_rn(__dmul_rn(J[0][0], J[1 % DIM][1 % DIM]),
+                    __dmul_rn(J[0][1 % DIM], J[1 % DIM][0]));
+    rdet = __drcp_rn(det);
+    inv[0] = __dmul_rn(J[1 % DIM][1 % DIM], rdet);
+    inv[1] = __dmul_rn(-J[0][1 % DIM], rdet);
+    inv[2] = 0.0;
+    inv[3] = __dmul_rn(-J[1 % DIM][0], rdet);
+    inv[4] = __dmul_rn(J[0][0], rdet);
+    inv[5] = 0.0; inv[6] = 0.0; inv[7] = 0.0; inv[8] = 0.0;
+  }
+  return det;
+}
+
+// Shared-memory layout of k_elem_fp64 (doubles):
+//   sdN [nip*npe*DIM] | sw [nip] | sN [nip*npe] (mass) | sX [npe*DIM] |
+//   sWd [nip] | sInv [nip*9] | then G and S (each nip*npe*DIM) when GS_SMEM.
+template <int KIND, int DIM, bool GS_SMEM>
+__global__ void __launch_bounds__(ELEM_THREADS)
+k_elem_fp64(ElemArgs A) {
+  extern __shared__ double smem[];
+  const int npe = A.npe, nip = A.nip;
+  double *sdN = smem;
+  double *sw = sdN + (size_t)nip * npe * DIM;
+  double *sN = sw + nip;
+  double *sX = sN + (KIND == KIND_MASS ? (size_t)nip * npe : 0);
+  double *sWd = sX + (size_t)npe * DIM;
+  double *sInv = sWd + nip;
+  double *G, *S;
+  if (GS_SMEM) {
+    G = sInv + (size_t)nip * 9;
+  } else {
+    G = A.scratch + (size_t)blockIdx.x * A.scratch_stride;
+  }
+  S = G + (size_t)nip * npe * (KIND == KIND_MASS ? 1 : DIM);
+
+  for (int t = threadIdx.x; t < nip * npe * DIM; t += blockDim.x) {
+    int j = t % DIM, qa = t / DIM;
+    sdN[t] = A.dN[(size_t)qa * 3 + j];
+  }
+  for (int t = threadIdx.x; t < nip; t += blockDim.x) sw[t] = A.w[t];
+  if (KIND == KIND_MASS)
+    for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) sN[t] = A.N[t];
+  __syncthreads();
+
+  const int BS = (KIND == KIND_ELASTIC) ? DIM * DIM : 1;
+  for (int64_t e = blockIdx.x; e < A.nel; e += gridDim.x) {
+    const int mat = A.emat ? A.emat[e] : 0;
+    if (mat < 0) continue;  // uniform across the CTA
+    const double c1 = A.c1[mat];
+    const double c2 = (KIND == KIND_ELASTIC) ? A.c2[mat] : 0.0;
+    for (int t = threadIdx.x; t < npe * DIM; t += blockDim.x) {
+      int a = t / DIM, i = t % DIM;
+      sX[t] = A.xyz[(size_t)A.conn[e * npe + a] * 3 + i];
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nip; q += blockDim.x) {
+      double inv[9];
+      double det = geom_point<DIM>(sX, sdN + (size_t)q * npe * DIM, npe, inv);
+      if (!(det > 0.0)) atomicOr(A.status, ST_BAD_JACOBIAN);
+      sWd[q] = __dmul_rn(det, sw[q]);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) sInv[q * 9 + k] = inv[k];
+    }
+    __syncthreads();
+    if (KIND == KIND_MASS) {
+      for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) {
+        int q = t / npe;
+        S[t] = __dmul_rn(sWd[q], sN[t]);
+      }
+    } else {
+      for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) {
+        int q = t / npe;
+        const double *inv = sInv + q * 9;
+        const double *d = sdN + (size_t)t * DIM;
+        double wd = sWd[q];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i) {
+          double acc = 0.0;
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) acc = __fma_rn(inv[3 * j + i], d[j], acc);
+          G[(size_t)t * DIM + i] = acc;
+          S[(size_t)t * DIM + i] = __dmul_rn(wd, acc);
+        }
+      }
+    }
+    __syncthreads();
+
+    double *out = A.Kp + (size_t)e * A.npairs * BS;
+    for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
+      int a, b;
+      pair_decode(pi, npe, a, b);
+      if (KIND == KIND_ELASTIC) {
+        double O[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) O[i][j] = 0.0;
+        if (a != b) {
+          for (int q = 0; q < nip; ++q) {
+            const double *sa = S + ((size_t)q * npe + a) * DIM;
+            const double *gb = G + ((size_t)q * npe + b) * DIM;
+            double s_[DIM], g_[DIM];
+#pragma unroll
+            for (int i = 0; i < DIM; ++i) { s_[i] = sa[i]; g_[i] = gb[i]; }
+#pragma unroll
+            for (int i = 0; i < DIM; ++i)
+#pragma unroll
+              for (int j = 0; j < DIM; ++j) O[i][j] = __fma_rn(s_[i], g_[j], O[i][j]);
+          }
+        } else {
+          for (int q = 0; q < nip; ++q) {
+            const double *sa = S + ((size_t)q * npe + a) * DIM;
+            const double *ga = G + ((size_t)q * npe + a) * DIM;
+            double s_[DIM], g_[DIM];
+#pragma unroll
+            for (int i = 0; i < DIM; ++i) { s_[i] = sa[i]; g_[i] = ga[i]; }
+#pragma unroll
+            for (int i = 0; i < DIM; ++i)
+#pragma unroll
+              for (int j = i; j < DIM; ++j) O[i][j] = __fma_rn(s_[i], g_[j], O[i][j]);
+          }
+#pragma unroll
+          for (int i = 0; i < DIM; ++i)
+#pragma unroll
+            for (int j = 0; j < i; ++j) O[i][j] = O[j][i];
+        }
+        double tr = __dadd_rn(O[0][0], O[1 % DIM][1 % DIM]);
+        if (DIM == 3) tr = __dadd_rn(tr, O[2 % DIM][2 % DIM]);
+        double *o = out + (size_t)pi * BS;
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            double t = __fma_rn(c2, O[j][i], __dmul_rn(c1, O[i][j]));
+            if (i == j) t = __fma_rn(c2, tr, t);
+            o[i * DIM + j] = t;
+          }
+      } else if (KIND == KIND_HEAT) {
+        double acc = 0.0;
+        for (int q = 0; q < nip; ++q) {
+          const double *sa = S + ((size_t)q * npe + a) * DIM;
+          const double *gb = G + ((size_t)q * npe + b) * DIM;
+#pragma unroll
+          for (int i = 0; i < DIM; ++i) acc = __fma_rn(sa[i], gb[i], acc);
+        }
+        out[pi] = __dmul_rn(c1, acc);
+      } else {  // mass
+        double acc = 0.0;
+        for (int q = 0; q < nip; ++q)
+          acc = __fma_rn(S[(size_t)q * npe + a], sN[(size_t)q * npe + b], acc);
+        out[pi] = __dmul_rn(c1, acc);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// One warp per column node B; lanes over the rows (node A) of the column.
+// Sums, for every entry, the contributions of the elements containing both
+// A and B in ascending element order, starting from the first contribution.
+template <int P, bool BLOCKVAL>
+__global__ void k_gather(const int64_t *__restrict__ nptr,
+                         const int32_t *__restrict__ nadj,
+                         const int64_t *__restrict__ n2e_ptr,
+                         const int2 *__restrict__ n2e,
+                         const double *__restrict__ Kp, int npe, int npairs,
+                         int64_t non, int max_n2e, double *__restrict__ nz,
+                         unsigned *status) {
+  extern __shared__ int2 sB[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  int2 *mine = sB + (size_t)wib * max_n2e;
+  constexpr int BS = BLOCKVAL ? P * P : 1;
+  for (int64_t B = (int64_t)blockIdx.x * wpb + wib; B < non; B += (int64_t)gridDim.x * wpb) {
+    const int64_t s = n2e_ptr[B];
+    const int nb = (int)(n2e_ptr[B + 1] - s);
+    for (int k = lane; k < nb; k += 32) mine[k] = n2e[s + k];
+    __syncwarp();
+    const int64_t c0 = nptr[B];
+    const int deg = (int)(nptr[B + 1] - c0);
+    for (int t = lane; t < deg; t += 32) {
+      const int A = nadj[c0 + t];
+      int64_t ia = n2e_ptr[A];
+      const int64_t ea = n2e_ptr[A + 1];
+      int ib = 0;
+      double acc[P][P];
+      bool first = true;
+#pragma unroll
+      for (int i = 0; i < P; ++i)
+#pragma unroll
+        for (int j = 0; j < P; ++j) acc[i][j] = 0.0;
+      int2 xa = ia < ea ? n2e[ia] : make_int2(INT32_MAX, 0);
+      while (ia < ea && ib < nb) {
+        const int2 xb = mine[ib];
+        if (xa.x < xb.x) {
+          ++ia;
+          if (ia < ea) xa = n2e[ia];
+        } else if (xa.x > xb.x) {
+          ++ib;
+        } else {
+          const int e = xa.x, la = xa.y, lb = xb.y;
+          double v[P][P];
+          if (BLOCKVAL) {
+            const bool tr = la > lb;
+            const int lo = tr ? lb : la, hi = tr ? la : lb;
+            const double *blk = Kp + ((size_t)e * npairs + (size_t)(lo * npe - (lo * (lo - 1)) / 2 + (hi - lo))) * BS;
+#pragma unroll
+            for (int i = 0; i < P; ++i)
+#pragma unroll
+              for (int j = 0; j < P; ++j) v[i][j] = tr ? blk[j * P + i] : blk[i * P + j];
+          } else {
+            const int lo = la < lb ? la : lb, hi = la < lb ? lb : la;
+            double m = Kp[(size_t)e * npairs + (size_t)(lo * npe - (lo * (lo - 1)) / 2 + (hi - lo))];
+#pragma unroll
+            for (int i = 0; i < P; ++i)
+#pragma unroll
+              for (int j = 0; j < P; ++j) v[i][j] = (i == j) ? m : 0.0;
+          }
+#pragma unroll
+          for (int i = 0; i < P; ++i)
+#pragma unroll
+            for (int j = 0; j < P; ++j) acc[i][j] = first ? v[i][j] : __dadd_rn(acc[i][j], v[i][j]);
+          first = false;
+          ++ia;
+          ++ib;
+          if (ia < ea) xa = n2e[ia];
+        }
+      }
+      if (first) atomicOr(status, ST_PATTERN);
+      // row (A,i), column (B,j): colptr(B,j) = P^2 c0 + j P deg; offset P t + i
+#pragma unroll
+      for (int j = 0; j < P; ++j) {
+        double *col = nz + (size_t)P * P * c0 + (size_t)j * P * deg + (size_t)P * t;
+#pragma unroll
+        for (int i = 0; i < P; ++i) col[i] = acc[i][j];
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------- dropzeros
+__global__ void k_count_nz(const double *__restrict__ nz, const int64_t *__restrict__ colptr,
+                           int64_t ndof, int64_t *__restrict__ cnt) {
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  for (int64_t c = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5); c < ndof;
+       c += (int64_t)gridDim.x * wpb) {
+    int64_t s = colptr[c], e = colptr[c + 1];
+    int n = 0;
+    for (int64_t k = s + lane; k < e; k += 32) n += (nz[k] != 0.0);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) n += __shfl_xor_sync(0xffffffffu, n, off);
+    if (lane == 0) cnt[c] = n;
+  }
+}
+
+template <int P>
+__global__ void k_compact(const double *__restrict__ nz, const int64_t *__restrict__ colptr,
+                          const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
+                          int64_t ndof, const int64_t *__restrict__ outptr,
+                          int64_t *__restrict__ rowval_s, double *__restrict__ nzval_s) {
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  for (int64_t c = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5); c < ndof;
+       c += (int64_t)gridDim.x * wpb) {
+    const int64_t s = colptr[c], e = colptr[c + 1];
+    const int64_t B = c / P;
+    const int64_t r0 = nptr[B];
+    int64_t o = outptr[c];
+    for (int64_t k0 = s; k0 < e; k0 += 32) {
+      int64_t k = k0 + lane;
+      double v = 0.0;
+      bool keep = false;
+      if (k < e) {
+        v = nz[k];
+        keep = (v != 0.0);
+      }
+      unsigned bal = __ballot_sync(0xffffffffu, keep);
+      if (keep) {
+        int off = __popc(bal & ((1u << lane) - 1u));
+        int64_t loc = k - s;
+        int64_t row = (int64_t)P * nadj[r0 + loc / P] + loc % P;
+        rowval_s[o + off] = row + 1;
+        nzval_s[o + off] = v;
+      }
+      o += __popc(bal);
+    }
+  }
+}
+
+__global__ void k_colptr_1based(const int64_t *__restrict__ in, int64_t n,
+                                int64_t *__restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = in[i] + 1;
+}
+
+// Row sums of a symmetric matrix = column sums in row order, from 0.0
+// (sum(M, dims=2) walks columns in order; M[R,C] == M[C,R] bit for bit).
+__global__ void k_lump(const double *__restrict__ nz, const int64_t *__restrict__ colptr,
+                       int64_t ndof, double *__restrict__ diag) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ndof;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int64_t k = colptr[c]; k < colptr[c + 1]; ++k) acc = __dadd_rn(acc, nz[k]);
+    diag[c] = acc;
+  }
+}
+
+__global__ void k_diag_stored(const double *__restrict__ diag, int64_t ndof,
+                              int64_t *__restrict__ cnt) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ndof;
+       c += (int64_t)gridDim.x * blockDim.x)
+    cnt[c] = diag[c] != 0.0;
+}
+
+__global__ void k_diag_compact(const double *__restrict__ diag, int64_t ndof,
+                               const int64_t *__restrict__ outptr,
+                               int64_t *__restrict__ rowval_s, double *__restrict__ nzval_s) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ndof;
+       c += (int64_t)gridDim.x * blockDim.x)
+    if (diag[c] != 0.0) {
+      rowval_s[outptr[c]] = c + 1;
+      nzval_s[outptr[c]] = diag[c];
+    }
+}
+
+__global__ void k_axpby(double a, const double *__restrict__ x, double b,
+                        const double *__restrict__ y, double *__restrict__ z, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    z[i] = __fma_rn(b, y[i], __dmul_rn(a, x[i]));
+}
+
+inline unsigned grid_1d(int64_t n, int threads, int sms) {
+  int64_t b = (n + threads - 1) / threads;
+  int64_t cap = (int64_t)sms * 16;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+template <int KIND, int DIM, bool GS>
+int launch_elem(llf_ctx *ctx, const ElemArgs &a, size_t smem, unsigned grid) {
+  auto fn = k_elem_fp64<KIND, DIM, GS>;
+  if (smem > 48 * 1024)
+    LLF_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+  KernelScope ks(ctx, "k_elem_fp64");
+  fn<<<grid, ELEM_THREADS, smem, ctx->stream>>>(a);
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  return LLF_OK;
+}
+
+template <int KIND, int DIM>
+int run_elem(llf_ctx *ctx, ElemArgs a) {
+  const int npe = a.npe, nip = a.nip;
+  const int gsw = (KIND == KIND_MASS) ? 1 : DIM;
+  size_t base = sizeof(double) * ((size_t)nip * npe * DIM + nip +
+                                  (KIND == KIND_MASS ? (size_t)nip * npe : 0) +
+                                  (size_t)npe * DIM + nip + (size_t)nip * 9);
+  size_t gs = sizeof(double) * 2 * (size_t)nip * npe * gsw;
+  bool in_smem = base + gs <= 96 * 1024;
+  size_t smem = in_smem ? base + gs : base;
+  if (smem > 200 * 1024)
+    return llf_fail(ctx, LLF_ERR_LIMIT, "element tables exceed shared memory");
+  int per_sm = 0;
+  if (in_smem)
+    LLF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                          &per_sm, k_elem_fp64<KIND, DIM, true>, ELEM_THREADS, smem));
+  else
+    LLF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                          &per_sm, k_elem_fp64<KIND, DIM, false>, ELEM_THREADS, smem));
+  if (per_sm < 1) per_sm = 1;
+  int64_t grid = (int64_t)ctx->num_sms * per_sm;
+  if (grid > a.nel) grid = a.nel > 0 ? a.nel : 1;
+  double *scratch = nullptr;
+  if (!in_smem) {
+    a.scratch_stride = (int64_t)(gs / sizeof(double));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &scratch, (size_t)grid * a.scratch_stride));
+    a.scratch = scratch;
+  }
+  int rc = in_smem ? launch_elem<KIND, DIM, true>(ctx, a, smem, (unsigned)grid)
+                   : launch_elem<KIND, DIM, false>(ctx, a, smem, (unsigned)grid);
+  dfree(ctx, scratch);
+  return rc;
+}
+
+template <int P, bool BV>
+int run_gather(llf_ctx *ctx, llf_pattern *pat, const double *Kp, int npairs, double *nz) {
+  const int wpb = 4;
+  size_t smem = sizeof(int2) * (size_t)pat->max_n2e * wpb;
+  if (smem > 48 * 1024)
+    LLF_CUDA_TRY(ctx, cudaFuncSetAttribute(k_gather<P, BV>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+  unsigned grid = grid_1d(pat->mesh->non * 32, wpb * 32, ctx->num_sms);
+  KernelScope ks(ctx, "k_gather");
+  k_gather<P, BV><<<grid, wpb * 32, smem, ctx->stream>>>(
+      pat->d_nptr, pat->d_nadj, pat->d_n2e_ptr, pat->d_n2e, Kp, pat->mesh->npe, npairs,
+      pat->mesh->non, pat->max_n2e > 0 ? pat->max_n2e : 1, nz, ctx->d_status);
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  return LLF_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host
+int matrix_finalize(llf_ctx *ctx, llf_matrix *m) {
+  llf_pattern *pat = m->pat;
+  const int64_t n = pat->ndof;
+  cudaStream_t s = ctx->stream;
+  int64_t *cnt = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &cnt, n + 1));
+  LLF_CUDA_TRY(ctx, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (n + 1), s));
+  if (m->diagonal_only) {
+    KernelScope ks(ctx, "k_diag_stored");
+    k_diag_stored<<<grid_1d(n, 256, ctx->num_sms), 256, 0, s>>>(m->d_diag, n, cnt);
+  } else {
+    KernelScope ks(ctx, "k_count_nz");
+    k_count_nz<<<grid_1d(n * 32, 256, ctx->num_sms), 256, 0, s>>>(m->d_nz, pat->d_colptr, n, cnt);
+  }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  int64_t *ptr0 = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &ptr0, n + 1));
+  int64_t total = 0;
+  LLF_CUDA_TRY(ctx, exclusive_scan_i64(ctx, cnt, ptr0, n + 1, &total));
+  dfree(ctx, m->d_colptr_s);
+  dfree(ctx, m->d_rowval_s);
+  dfree(ctx, m->d_nzval_s);
+  m->nnz_s = total;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_colptr_s, n + 1));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_rowval_s, total));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nzval_s, total));
+  if (m->diagonal_only) {
+    KernelScope ks(ctx, "k_diag_compact");
+    k_diag_compact<<<grid_1d(n, 256, ctx->num_sms), 256, 0, s>>>(m->d_diag, n, ptr0,
+                                                                 m->d_rowval_s, m->d_nzval_s);
+  } else {
+    unsigned g = grid_1d(n * 32, 256, ctx->num_sms);
+    KernelScope ks(ctx, "k_compact");
+    switch (pat->pdim) {
+      case 1: k_compact<1><<<g, 256, 0, s>>>(m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, n, ptr0, m->d_rowval_s, m->d_nzval_s); break;
+      case 2: k_compact<2><<<g, 256, 0, s>>>(m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, n, ptr0, m->d_rowval_s, m->d_nzval_s); break;
+      case 3: k_compact<3><<<g, 256, 0, s>>>(m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, n, ptr0, m->d_rowval_s, m->d_nzval_s); break;
+      default: return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
+    }
+  }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  { KernelScope ks(ctx, "k_colptr_1based");
+  k_colptr_1based<<<grid_1d(n + 1, 256, ctx->num_sms), 256, 0, s>>>(ptr0, n + 1, m->d_colptr_s); }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  dfree(ctx, cnt);
+  dfree(ctx, ptr0);
+  return LLF_OK;
+}
+
+int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int ptype,
+                  const double *c1, const double *c2, int nmat, int form, int lumped,
+                  llf_matrix *m) {
+  (void)form;
+  const int dim = mesh->dim;
+  const int npe = mesh->npe;
+  const int npairs = npe * (npe + 1) / 2;
+  const int P = pat->pdim;
+  const int BS = (kind == KIND_ELASTIC) ? P * P : 1;
+  cudaStream_t s = ctx->stream;
+
+  double *d_c1 = nullptr, *d_c2 = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_c1, nmat));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_c2, nmat));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_c1, c1, sizeof(double) * nmat, cudaMemcpyHostToDevice, s));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_c2, c2 ? c2 : c1, sizeof(double) * nmat,
+                                    cudaMemcpyHostToDevice, s));
+  double *Kp = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &Kp, (size_t)mesh->nel * npairs * BS));
+
+  ElemArgs a{};
+  a.xyz = mesh->d_xyz;
+  a.conn = mesh->d_conn;
+  a.emat = mesh->d_emat;
+  a.nel = mesh->nel;
+  a.npe = npe;
+  a.nip = mesh->nip;
+  a.npairs = npairs;
+  a.w = mesh->d_w;
+  a.N = mesh->d_N;
+  a.dN = mesh->d_dN;
+  a.c1 = d_c1;
+  a.c2 = d_c2;
+  a.Kp = Kp;
+  a.status = ctx->d_status;
+  int rc = LLF_OK;
+  if (dim == 3) {
+    if (kind == KIND_ELASTIC) rc = run_elem<KIND_ELASTIC, 3>(ctx, a);
+    else if (kind == KIND_HEAT) rc = run_elem<KIND_HEAT, 3>(ctx, a);
+    else rc = run_elem<KIND_MASS, 3>(ctx, a);
+  } else {
+    if (kind == KIND_ELASTIC) rc = run_elem<KIND_ELASTIC, 2>(ctx, a);
+    else if (kind == KIND_HEAT) rc = run_elem<KIND_HEAT, 2>(ctx, a);
+    else rc = run_elem<KIND_MASS, 2>(ctx, a);
+  }
+  if (rc == LLF_OK) {
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nz, pat->nnz));
+    if (kind == KIND_ELASTIC) {
+      rc = (P == 3) ? run_gather<3, true>(ctx, pat, Kp, npairs, m->d_nz)
+                    : run_gather<2, true>(ctx, pat, Kp, npairs, m->d_nz);
+    } else {
+      switch (P) {
+        case 1: rc = run_gather<1, false>(ctx, pat, Kp, npairs, m->d_nz); break;
+        case 2: rc = run_gather<2, false>(ctx, pat, Kp, npairs, m->d_nz); break;
+        case 3: rc = run_gather<3, false>(ctx, pat, Kp, npairs, m->d_nz); break;
+      }
+    }
+  }
+  dfree(ctx, Kp);
+  dfree(ctx, d_c1);
+  dfree(ctx, d_c2);
+  if (rc != LLF_OK) return rc;
+  rc = llf_check_status(ctx, "assembly");
+  if (rc != LLF_OK) return rc;
+  if (kind == KIND_MASS && lumped) {
+    m->diagonal_only = true;
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_diag, pat->ndof));
+    KernelScope ks(ctx, "k_lump");
+    k_lump<<<grid_1d(pat->ndof, 128, ctx->num_sms), 128, 0, s>>>(m->d_nz, pat->d_colptr,
+                                                                 pat->ndof, m->d_diag);
+    LLF_CUDA_TRY(ctx, cudaGetLastError());
+  }
+  return matrix_finalize(ctx, m);
+}
+
+int matrix_axpby_impl(llf_ctx *ctx, double a, const llf_matrix *A, double b,
+                      const llf_matrix *B, llf_matrix *C) {
+  if (A->pat != B->pat)
+    return llf_fail(ctx, LLF_ERR_STATE, "axpby: matrices live on different patterns");
+  if (A->diagonal_only || B->diagonal_only)
+    return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "axpby: lumped (diagonal) operands");
+  C->pat = A->pat;
+  int64_t n = A->pat->nnz;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &C->d_nz, n));
+  KernelScope ks(ctx, "k_axpby");
+  k_axpby<<<grid_1d(n, 256, ctx->num_sms), 256, 0, ctx->stream>>>(a, A->d_nz, b, B->d_nz,
+                                                                  C->d_nz, n);
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  return matrix_finalize(ctx, C);
+}

@@ -1,0 +1,201 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/llfem_gb300.h"
+
+// ---------------------------------------------------------------- status
+// Bits a kernel may set in the context's device status word.  Kernels never
+// trap; the host reads the word after the operation and turns a set bit into
+// an error return.
+enum : unsigned {
+  ST_BAD_NODE = 1u << 0,      // connectivity entry outside 1..non
+  ST_BAD_JACOBIAN = 1u << 1,  // non-positive Jacobian determinant
+  ST_CAPACITY = 1u << 2,      // per-node candidate list exceeds its buffer
+  ST_NONFINITE = 1u << 3,     // NaN/Inf in an input array
+  ST_PATTERN = 1u << 4,       // an element pair found no pattern slot
+  ST_BREAKDOWN = 1u << 5,     // CG breakdown (u.Au <= 0 or not finite)
+};
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+// Per-kernel tracing: every launch site opens a KernelScope; launches are
+// always counted, and with profiling enabled a pair of CUDA events brackets
+// the launch on the context's stream (durations resolved lazily).
+struct ProfPending {
+  const char *name;
+  cudaEvent_t a, b;
+};
+struct ProfAcc {
+  double ms = 0.0;
+  long long launches = 0;
+};
+
+struct llf_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  unsigned *d_status = nullptr;   // device status word
+  unsigned *h_status = nullptr;   // pinned host mirror
+  int num_sms = 0;
+  bool profiling = false;
+  long long launches = 0;
+  std::vector<ProfPending> pending;
+  std::vector<std::pair<std::string, ProfAcc>> prof;
+};
+
+void prof_resolve(llf_ctx *ctx);
+
+struct KernelScope {
+  llf_ctx *ctx;
+  ProfPending rec{};
+  bool on = false;
+  KernelScope(llf_ctx *c, const char *name) : ctx(c) {
+    ctx->launches++;
+    if (ctx->profiling) {
+      rec.name = name;
+      if (cudaEventCreate(&rec.a) == cudaSuccess && cudaEventCreate(&rec.b) == cudaSuccess) {
+        cudaEventRecord(rec.a, ctx->stream);
+        on = true;
+      }
+    }
+  }
+  ~KernelScope() {
+    if (on) {
+      cudaEventRecord(rec.b, ctx->stream);
+      ctx->pending.push_back(rec);
+      if (ctx->pending.size() > 4096) prof_resolve(ctx);
+    }
+  }
+};
+
+struct llf_mesh {
+  int dim = 0, family = 0, order = 0, npe = 0;
+  int64_t non = 0, nel = 0;
+  double *d_xyz = nullptr;      // 3*non
+  int32_t *d_conn = nullptr;    // npe*nel, 0-based node index
+  int32_t *d_emat = nullptr;    // nel material index, -1 = skip (nullptr: all 0)
+  // tables
+  int nip = 0;
+  double *d_w = nullptr;        // nip
+  double *d_N = nullptr;        // nip*npe
+  double *d_dN = nullptr;       // nip*npe*3
+  double *d_dNn = nullptr;      // npe*npe*3 gradients at the element nodes
+  std::vector<double> h_w, h_N, h_dN;  // host copies (FP32 tables derive from these)
+  float *d_wf = nullptr, *d_Nf = nullptr, *d_dNf = nullptr;
+  int tables_version = 0;
+};
+
+struct llf_pattern {
+  llf_mesh *mesh = nullptr;
+  int pdim = 0;
+  int64_t ndof = 0;       // pdim*non
+  int64_t nnzb = 0;       // node-level blocks
+  int64_t nnz = 0;        // structural DoF-level nnz = pdim^2 * nnzb
+  // node->element adjacency (elements with material >= 0), sorted by element
+  int64_t *d_n2e_ptr = nullptr;   // non+1
+  int2 *d_n2e = nullptr;          // (element, local index)
+  int max_n2e = 0;
+  // node-level CSC
+  int64_t *d_nptr = nullptr;      // non+1
+  int32_t *d_nadj = nullptr;      // nnzb (0-based node index, sorted per column)
+  int32_t *d_diagpos = nullptr;   // non: position of the node itself in its column
+  // DoF-level colptr (0-based)
+  int64_t *d_colptr = nullptr;    // ndof+1
+};
+
+struct llf_matrix {
+  llf_pattern *pat = nullptr;
+  double *d_nz = nullptr;         // structural values (pattern->nnz)
+  bool diagonal_only = false;     // lumped mass: values live on the diagonal
+  double *d_diag = nullptr;       // ndof (diagonal_only)
+  // stored (dropzeros'ed) form, SparseMatrixCSC arrays, 1-based
+  int64_t nnz_s = 0;
+  int64_t *d_colptr_s = nullptr;  // ndof+1
+  int64_t *d_rowval_s = nullptr;  // nnz_s
+  double *d_nzval_s = nullptr;    // nnz_s
+};
+
+// ---------------------------------------------------------------- helpers
+#define LLF_CUDA_TRY(ctx, expr)                                            \
+  do {                                                                     \
+    cudaError_t _e = (expr);                                               \
+    if (_e != cudaSuccess) {                                               \
+      return llf_fail((ctx), LLF_ERR_CUDA,                                 \
+                      std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+    }                                                                      \
+  } while (0)
+
+int llf_fail(llf_ctx *ctx, int code, const std::string &msg);
+int llf_ok(llf_ctx *ctx);
+
+// Read and clear the device status word (synchronises the stream).
+int llf_check_status(llf_ctx *ctx, const char *what);
+
+template <class T>
+cudaError_t dalloc(llf_ctx *ctx, T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMallocAsync((void **)p, count * sizeof(T), ctx->stream);
+}
+template <class T>
+void dfree(llf_ctx *ctx, T *&p) {
+  if (p) cudaFreeAsync((void *)p, ctx->stream);
+  p = nullptr;
+}
+
+// ---------------------------------------------------------------- kernels
+// scan.cu
+cudaError_t exclusive_scan_i64(llf_ctx *ctx, const int64_t *in, int64_t *out,
+                               int64_t n, int64_t *total_host);
+
+// pattern.cu
+int pattern_build_impl(llf_ctx *ctx, llf_mesh *mesh, int pdim, llf_pattern *pat);
+int mesh_convert_conn(llf_ctx *ctx, llf_mesh *mesh, const int64_t *d_conn64);
+int check_finite(llf_ctx *ctx, const double *d, int64_t n);
+// node -> (element, local index) lists sorted by element (elements with emat < 0 skipped)
+int build_n2e(llf_ctx *ctx, const int32_t *conn, const int32_t *emat, int64_t nel, int npe,
+              int64_t non, int64_t **ptr, int2 **list, int *max_len);
+
+// assemble.cu
+int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
+                  int ptype, const double *c1, const double *c2, int nmat,
+                  int form, int lumped, llf_matrix *m);
+int matrix_finalize(llf_ctx *ctx, llf_matrix *m);  // dropzeros -> stored form
+int matrix_axpby_impl(llf_ctx *ctx, double a, const llf_matrix *A, double b,
+                      const llf_matrix *B, llf_matrix *C);
+
+// solve.cu
+int spmv_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_x, double *d_y);
+int pcg_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
+             const uint8_t *d_fixed, int precond, double reltol,
+             int64_t maxiter, int64_t *iters, double *relres);
+
+// tl.cu
+int tl_material_tangent_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
+                             const double *d_F, int law, const double *params,
+                             int nparams, llf_matrix *m);
+int tl_initial_stress_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
+                           const double *d_S, const double *d_C, int law,
+                           const double *params, int nparams, llf_matrix *m);
+int tl_internal_force_impl(llf_ctx *ctx, llf_mesh *mesh, const double *d_P,
+                           const double *d_F, int law, const double *params,
+                           int nparams, double *d_f);
+int grad_elementwise_impl(llf_ctx *ctx, llf_mesh *mesh, const double *d_u,
+                          int add_identity, double *d_out);
+int load_vector_impl(llf_ctx *ctx, llf_mesh *bmesh, int problem_dim, int pdim,
+                     const double *t_const, const double *d_tn,
+                     double thickness, double *d_f, int64_t ndof);
+
+// kinds of element operators
+enum { KIND_ELASTIC = 0, KIND_HEAT = 1, KIND_MASS = 2, KIND_TLMAT = 3, KIND_TLGEO = 4 };
+
+inline int ptype_dim(int ptype) {
+  return (ptype == LLF_SOLID || ptype == LLF_HEAT_CONDUCTION) ? 3 : 2;
+}

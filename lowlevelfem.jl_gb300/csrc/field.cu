@@ -1,0 +1,196 @@
+// Boundary loads (loadVector) and elementwise nodal gradients (u∘∇).
+//
+// loadVector, src/linear.jl:3088-3434: per boundary element and point,
+//   t1, t2 = columns of the boundary Jacobian (fma chains over the nodes),
+//   Ja = |t1| * b (2D edge, :3394-3395) or |t1 x t2| (3D face, :3380-3384),
+//   fe[a,i] = fma(N_a t_i, Ja w, fe[a,i]);
+// element vectors are buffered and then summed into f node by node in
+// element order, the order the reference (and the oracle) adds them.
+//
+// ∇ (:vector_grad branch), src/nabla.jl:77-311: at every element node k the
+// Jacobian and physical gradients of all shape functions are evaluated at
+// that node's reference coordinates, T[i,j] = sum_l g_l,j u_l,i (fma chain
+// over l), stored column-major per node (9 values); F = I + T on request.
+#include "common.cuh"
+
+namespace {
+
+template <int BDIM>
+__global__ void k_load_elem(const double *__restrict__ xyz, const int32_t *__restrict__ conn,
+                            int64_t nel, int npe, int nip, const double *__restrict__ w,
+                            const double *__restrict__ N, const double *__restrict__ dN, int pdim,
+                            double t0, double t1c, double t2c, const double *__restrict__ tn,
+                            double thickness, double *__restrict__ fe) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nel;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double *out = fe + (size_t)e * npe * pdim;
+    for (int k = 0; k < npe * pdim; ++k) out[k] = 0.0;
+    const int32_t *c = conn + (size_t)e * npe;
+    for (int q = 0; q < nip; ++q) {
+      double a1[3], a2[3];
+      for (int i = 0; i < 3; ++i) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int a = 0; a < npe; ++a) {
+          double xa = xyz[(size_t)c[a] * 3 + i];
+          s1 = __fma_rn(xa, dN[((size_t)q * npe + a) * 3 + 0], s1);
+          if (BDIM == 2) s2 = __fma_rn(xa, dN[((size_t)q * npe + a) * 3 + 1], s2);
+        }
+        a1[i] = s1;
+        a2[i] = s2;
+      }
+      double Ja;
+      if (BDIM == 1) {
+        Ja = __dmul_rn(__dsqrt_rn(__dadd_rn(__dmul_rn(a1[0], a1[0]), __dmul_rn(a1[1], a1[1]))), thickness);
+      } else {
+        double xy = __dsub_rn(__dmul_rn(a1[0], a2[1]), __dmul_rn(a1[1], a2[0]));
+        double yz = __dsub_rn(__dmul_rn(a1[1], a2[2]), __dmul_rn(a1[2], a2[1]));
+        double zx = __dsub_rn(__dmul_rn(a1[2], a2[0]), __dmul_rn(a1[0], a2[2]));
+        Ja = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(xy, xy), __dmul_rn(yz, yz)), __dmul_rn(zx, zx)));
+      }
+      double tq[3] = {t0, t1c, t2c};
+      if (tn) {
+        for (int i = 0; i < pdim; ++i) {
+          double acc = 0.0;
+          for (int a = 0; a < npe; ++a)
+            acc = __fma_rn(N[(size_t)q * npe + a], tn[(size_t)c[a] * pdim + i], acc);
+          tq[i] = acc;
+        }
+      }
+      const double jw = __dmul_rn(Ja, w[q]);
+      for (int a = 0; a < npe; ++a) {
+        const double Na = N[(size_t)q * npe + a];
+        for (int i = 0; i < pdim; ++i)
+          out[a * pdim + i] = __fma_rn(__dmul_rn(Na, tq[i]), jw, out[a * pdim + i]);
+      }
+    }
+  }
+}
+
+// f[node*pdim+i] += fe of every element of the node, in element order.
+__global__ void k_load_gather(const int64_t *__restrict__ ptr, const int2 *__restrict__ list,
+                              int64_t non, int npe, int pdim, const double *__restrict__ fe,
+                              double *__restrict__ f) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < non;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = ptr[v], e = ptr[v + 1];
+    if (s == e) continue;
+    for (int i = 0; i < pdim; ++i) {
+      double acc = f[v * pdim + i];
+      for (int64_t k = s; k < e; ++k) {
+        const int2 el = list[k];
+        acc = __dadd_rn(acc, fe[((size_t)el.x * npe + el.y) * pdim + i]);
+      }
+      f[v * pdim + i] = acc;
+    }
+  }
+}
+
+// One thread per (element, element node k).
+__global__ void k_grad_nodes(const double *__restrict__ xyz, const int32_t *__restrict__ conn,
+                             int64_t nel, int npe, const double *__restrict__ dNn,
+                             const double *__restrict__ u, int add_identity,
+                             double *__restrict__ out, unsigned *status) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nel * npe;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = t / npe;
+    const int k = (int)(t - e * npe);
+    const int32_t *c = conn + (size_t)e * npe;
+    const double *d = dNn + (size_t)k * npe * 3;
+    double J[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double acc = 0.0;
+        for (int a = 0; a < npe; ++a) acc = __fma_rn(xyz[(size_t)c[a] * 3 + i], d[a * 3 + j], acc);
+        J[i][j] = acc;
+      }
+    double c00 = __dsub_rn(__dmul_rn(J[1][1], J[2][2]), __dmul_rn(J[1][2], J[2][1]));
+    double c01 = -__dsub_rn(__dmul_rn(J[1][0], J[2][2]), __dmul_rn(J[1][2], J[2][0]));
+    double c02 = __dsub_rn(__dmul_rn(J[1][0], J[2][1]), __dmul_rn(J[1][1], J[2][0]));
+    double c10 = -__dsub_rn(__dmul_rn(J[0][1], J[2][2]), __dmul_rn(J[0][2], J[2][1]));
+    double c11 = __dsub_rn(__dmul_rn(J[0][0], J[2][2]), __dmul_rn(J[0][2], J[2][0]));
+    double c12 = -__dsub_rn(__dmul_rn(J[0][0], J[2][1]), __dmul_rn(J[0][1], J[2][0]));
+    double c20 = __dsub_rn(__dmul_rn(J[0][1], J[1][2]), __dmul_rn(J[0][2], J[1][1]));
+    double c21 = -__dsub_rn(__dmul_rn(J[0][0], J[1][2]), __dmul_rn(J[0][2], J[1][0]));
+    double c22 = __dsub_rn(__dmul_rn(J[0][0], J[1][1]), __dmul_rn(J[0][1], J[1][0]));
+    double det = __dadd_rn(__dadd_rn(__dmul_rn(J[0][0], c00), __dmul_rn(J[0][1], c01)),
+                           __dmul_rn(J[0][2], c02));
+    if (!(det > 0.0)) atomicOr(status, ST_BAD_JACOBIAN);
+    double r = __drcp_rn(det);
+    double inv[9] = {__dmul_rn(c00, r), __dmul_rn(c10, r), __dmul_rn(c20, r),
+                     __dmul_rn(c01, r), __dmul_rn(c11, r), __dmul_rn(c21, r),
+                     __dmul_rn(c02, r), __dmul_rn(c12, r), __dmul_rn(c22, r)};
+    double T[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // T[i][j] = du_i/dX_j
+    for (int l = 0; l < npe; ++l) {
+      double g[3];
+      for (int i = 0; i < 3; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < 3; ++j) acc = __fma_rn(inv[3 * j + i], d[l * 3 + j], acc);
+        g[i] = acc;
+      }
+      const double *ul = u + (size_t)c[l] * 3;
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) T[i][j] = __fma_rn(g[j], ul[i], T[i][j]);
+    }
+    double *o = out + (size_t)e * npe * 9 + (size_t)k * 9;
+    for (int j = 0; j < 3; ++j)
+      for (int i = 0; i < 3; ++i)
+        o[3 * j + i] = (add_identity && i == j) ? __dadd_rn(T[i][j], 1.0) : T[i][j];
+  }
+}
+
+inline unsigned grid_1d(int64_t n, int threads, int sms) {
+  int64_t b = (n + threads - 1) / threads;
+  int64_t cap = (int64_t)sms * 16;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+}  // namespace
+
+int load_vector_impl(llf_ctx *ctx, llf_mesh *bm, int problem_dim, int pdim, const double *t_const,
+                     const double *d_tn, double thickness, double *d_f, int64_t ndof) {
+  (void)problem_dim;
+  (void)ndof;
+  cudaStream_t s = ctx->stream;
+  double *fe = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &fe, (size_t)bm->nel * bm->npe * pdim));
+  double t[3] = {0, 0, 0};
+  if (t_const)
+    for (int i = 0; i < pdim; ++i) t[i] = t_const[i];
+  unsigned g = grid_1d(bm->nel, 128, ctx->num_sms);
+  {
+    KernelScope ks(ctx, "k_load_elem");
+    if (bm->dim == 1)
+      k_load_elem<1><<<g, 128, 0, s>>>(bm->d_xyz, bm->d_conn, bm->nel, bm->npe, bm->nip, bm->d_w, bm->d_N,
+                                       bm->d_dN, pdim, t[0], t[1], t[2], d_tn, thickness, fe);
+    else
+      k_load_elem<2><<<g, 128, 0, s>>>(bm->d_xyz, bm->d_conn, bm->nel, bm->npe, bm->nip, bm->d_w, bm->d_N,
+                                       bm->d_dN, pdim, t[0], t[1], t[2], d_tn, thickness, fe);
+  }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  int64_t *ptr = nullptr;
+  int2 *list = nullptr;
+  int mx = 0;
+  int rc = build_n2e(ctx, bm->d_conn, nullptr, bm->nel, bm->npe, bm->non, &ptr, &list, &mx);
+  if (rc != LLF_OK) {
+    dfree(ctx, fe);
+    return rc;
+  }
+  { KernelScope ks(ctx, "k_load_gather");
+  k_load_gather<<<grid_1d(bm->non, 128, ctx->num_sms), 128, 0, s>>>(ptr, list, bm->non, bm->npe, pdim, fe, d_f); }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  dfree(ctx, fe);
+  dfree(ctx, ptr);
+  dfree(ctx, list);
+  return llf_check_status(ctx, "loadVector");
+}
+
+int grad_elementwise_impl(llf_ctx *ctx, llf_mesh *m, const double *d_u, int add_identity,
+                          double *d_out) {
+  KernelScope ks(ctx, "k_grad_nodes");
+  k_grad_nodes<<<grid_1d(m->nel * m->npe, 128, ctx->num_sms), 128, 0, ctx->stream>>>(
+      m->d_xyz, m->d_conn, m->nel, m->npe, m->d_dNn, d_u, add_identity, d_out, ctx->d_status);
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  return llf_check_status(ctx, "grad");
+}

@@ -1,0 +1,766 @@
+/*
+ * llfem_oracle.c — CPU oracle for the operator-assembly + solve hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file restates, in plain C, the algorithms
+ * of LowLevelFEM.jl v1.13.31 that the GPU library replaces.  It is used only
+ * by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, always
+ * as the checker or the timed CPU baseline, never as the product.
+ *
+ * Parity pins: the oracle is checked against the reference's own published
+ * numbers (examples/dev/compare_LLFEM_Ferrite_dealII_Gridap/results.txt:7,
+ * test/test_validation.jl, test/test_integration.jl, test/test_dsl.jl
+ * resultants, pattern counts of examples/dev/DSL_vs_legacy*.ipynb).
+ *
+ * Arithmetic contract shared with the CUDA kernels (both compiled without
+ * floating-point contraction; every fused multiply-add is an explicit fma):
+ *   geometry at an integration point q (element nodes X[a][i]):
+ *     J[i][j]  = fma-chain over a of X[a][i] * dN[q][a][j]       (from 0.0)
+ *     cofactors c, det = (J00 c00 + J01 c01) + J02 c02 (3D) or
+ *                 J00 J11 - J01 J10 (2D);  rdet = 1/det
+ *     invJ[i][j] = c[j][i] * rdet
+ *     g[a][i]  = fma-chain over j of invJ[j][i] * dN[q][a][j]    (J^-T grad)
+ *     wdet     = det * w[q];   s[a][i] = wdet * g[a][i]
+ *   node-pair block a <= b:
+ *     O[i][j]  = fma-chain over q of s[a][i](q) * g[b][j](q)  (a == b: i <= j
+ *                computed, O[j][i] = O[i][j])
+ *     elastic  K[i][j] = fma(mub, O[j][i], lamb*O[i][j]) (+ fma(mub, tr, .)
+ *              on i == j, tr = O00 + O11 (+ O22))
+ *     heat     K = kb * (fma-chain over q, then i, of s[a][i] g[b][i])
+ *     mass     M = rb * (fma-chain over q of (wdet N[a]) * N[b]), identity
+ *              over the pdim components
+ *   the element matrix is exactly symmetric: block (b,a) = block(a,b)^T.
+ *   global: contributions to one entry are summed in element order,
+ *   left to right, starting from the first one (SparseArrays.sparse's input
+ *   order); exact zeros are then removed (dropzeros!).
+ * The element formulas are the B^T D B, H^T H and B^T B products of
+ * src/linear.jl:154-330, :1854-2004 and src/heat.jl:36-137 written in
+ * node-pair form (for isotropic Hooke D: K_ab = lambda g_a g_b^T +
+ * mu g_b g_a^T + mu (g_a . g_b) I).  Julia's BLAS summation order inside
+ * B^T D B cannot be reproduced on any other machine, so this contract fixes
+ * an order of its own; values agree with the reference to rounding.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_ELASTIC 0
+#define ORC_HEAT 1
+#define ORC_MASS 2
+
+#define PT_SOLID 0
+#define PT_PLANE_STRESS 1
+#define PT_PLANE_STRAIN 2
+#define PT_HEAT 3
+#define PT_PLANE_HEAT 4
+
+/* ------------------------------------------------------------------------ */
+/* Material constants: elastic_constants (src/general.jl:142-203) and the    */
+/* D matrices of constitutive_matrix (src/linear.jl:154-188) in Lame form.  */
+/* ------------------------------------------------------------------------ */
+void orc_lame(int ptype, double E, double nu, double thickness, double *lamb,
+              double *mub) {
+  double mu = E / (2.0 * (1.0 + nu));
+  double lam, b = 1.0;
+  if (ptype == PT_PLANE_STRESS) {
+    lam = E * nu / ((1.0 - nu) * (1.0 + nu));
+    b = thickness;
+  } else {
+    lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+  }
+  *lamb = lam * b;
+  *mub = mu * b;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Geometry at one integration point (the shared arithmetic contract).      */
+/* Returns det.                                                             */
+/* ------------------------------------------------------------------------ */
+static double orc_geom(int dim, int npe, const double *X, const double *dNq,
+                       double invJ[9]) {
+  double J[3][3] = {{0}};
+  for (int i = 0; i < dim; ++i)
+    for (int j = 0; j < dim; ++j) {
+      double acc = 0.0;
+      for (int a = 0; a < npe; ++a) acc = fma(X[3 * a + i], dNq[3 * a + j], acc);
+      J[i][j] = acc;
+    }
+  double det, rdet;
+  if (dim == 3) {
+    double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    double c01 = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]);
+    double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    double c10 = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]);
+    double c11 = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+    double c12 = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]);
+    double c20 = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    double c21 = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]);
+    double c22 = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    det = (J[0][0] * c00 + J[0][1] * c01) + J[0][2] * c02;
+    rdet = 1.0 / det;
+    /* invJ[i][j] = c[j][i] * rdet, stored row-major */
+    invJ[0] = c00 * rdet; invJ[1] = c10 * rdet; invJ[2] = c20 * rdet;
+    invJ[3] = c01 * rdet; invJ[4] = c11 * rdet; invJ[5] = c21 * rdet;
+    invJ[6] = c02 * rdet; invJ[7] = c12 * rdet; invJ[8] = c22 * rdet;
+  } else {
+    det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    rdet = 1.0 / det;
+    invJ[0] = J[1][1] * rdet;   invJ[1] = -J[0][1] * rdet; invJ[2] = 0.0;
+    invJ[3] = -J[1][0] * rdet;  invJ[4] = J[0][0] * rdet;  invJ[5] = 0.0;
+    invJ[6] = 0.0; invJ[7] = 0.0; invJ[8] = 0.0;
+  }
+  return det;
+}
+
+/* Physical gradients g[q][a][i] and weighted s = wdet*g for all points.
+ * Returns 0, or -1 on a non-positive Jacobian determinant. */
+static int orc_grads(int dim, int npe, int nip, const double *w,
+                     const double *dN, const double *X, double *g, double *s,
+                     double *wdet) {
+  for (int q = 0; q < nip; ++q) {
+    double invJ[9];
+    double det = orc_geom(dim, npe, X, dN + (size_t)q * npe * 3, invJ);
+    if (!(det > 0.0)) return -1;
+    double wd = det * w[q];
+    wdet[q] = wd;
+    for (int a = 0; a < npe; ++a) {
+      const double *d = dN + ((size_t)q * npe + a) * 3;
+      for (int i = 0; i < dim; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < dim; ++j) acc = fma(invJ[3 * j + i], d[j], acc);
+        g[((size_t)q * npe + a) * 3 + i] = acc;
+        s[((size_t)q * npe + a) * 3 + i] = wd * acc;
+      }
+    }
+  }
+  return 0;
+}
+
+/* Element matrix Ke (row-major, (pdim*npe)^2) under the arithmetic contract.
+ * kind ORC_ELASTIC: c1 = lamb, c2 = mub; ORC_HEAT: c1 = kb; ORC_MASS: c1 = rb.
+ * pdim = dim for elastic, dim for mass (vector problems) or 1, 1 for heat. */
+int orc_element_matrix(int kind, int dim, int pdim, int npe, int nip,
+                       const double *w, const double *N, const double *dN,
+                       const double *X, double c1, double c2, double *Ke) {
+  size_t nd = (size_t)pdim * npe;
+  double *g = (double *)malloc(sizeof(double) * nip * npe * 3);
+  double *s = (double *)malloc(sizeof(double) * nip * npe * 3);
+  double *wdet = (double *)malloc(sizeof(double) * nip);
+  int rc = orc_grads(dim, npe, nip, w, dN, X, g, s, wdet);
+  if (rc) {
+    free(g); free(s); free(wdet);
+    return rc;
+  }
+  memset(Ke, 0, sizeof(double) * nd * nd);
+  for (int a = 0; a < npe; ++a) {
+    for (int b = a; b < npe; ++b) {
+      double blk[9] = {0};
+      if (kind == ORC_ELASTIC) {
+        double O[3][3] = {{0}};
+        for (int i = 0; i < dim; ++i)
+          for (int j = (a == b ? i : 0); j < dim; ++j) {
+            double acc = 0.0;
+            for (int q = 0; q < nip; ++q)
+              acc = fma(s[((size_t)q * npe + a) * 3 + i],
+                        g[((size_t)q * npe + b) * 3 + j], acc);
+            O[i][j] = acc;
+            if (a == b) O[j][i] = acc;
+          }
+        double tr = O[0][0] + O[1][1];
+        if (dim == 3) tr = tr + O[2][2];
+        for (int i = 0; i < dim; ++i)
+          for (int j = 0; j < dim; ++j) {
+            double t = fma(c2, O[j][i], c1 * O[i][j]);
+            if (i == j) t = fma(c2, tr, t);
+            blk[i * pdim + j] = t;
+          }
+      } else if (kind == ORC_HEAT) {
+        double acc = 0.0;
+        for (int q = 0; q < nip; ++q)
+          for (int i = 0; i < dim; ++i)
+            acc = fma(s[((size_t)q * npe + a) * 3 + i],
+                      g[((size_t)q * npe + b) * 3 + i], acc);
+        blk[0] = c1 * acc;
+      } else { /* mass */
+        double acc = 0.0;
+        for (int q = 0; q < nip; ++q)
+          acc = fma(wdet[q] * N[(size_t)q * npe + a], N[(size_t)q * npe + b], acc);
+        double m = c1 * acc;
+        for (int i = 0; i < pdim; ++i) blk[i * pdim + i] = m;
+      }
+      for (int i = 0; i < pdim; ++i)
+        for (int j = 0; j < pdim; ++j) {
+          double v = blk[i * pdim + j];
+          Ke[((size_t)a * pdim + i) * nd + (size_t)b * pdim + j] = v;
+          Ke[((size_t)b * pdim + j) * nd + (size_t)a * pdim + i] = v;
+        }
+    }
+  }
+  free(g); free(s); free(wdet);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Structural CSC pattern: build_csc_pattern, src/multifield.jl:2083-2250.   */
+/* Node adjacency through shared elements, sorted + unique per node, then   */
+/* expanded to pdim components (rows (A-1)*pdim+i sorted inside a column).   */
+/* ------------------------------------------------------------------------ */
+static int cmp_i64(const void *x, const void *y) {
+  int64_t a = *(const int64_t *)x, b = *(const int64_t *)y;
+  return (a > b) - (a < b);
+}
+
+typedef struct {
+  int64_t n, nnz;
+  int64_t *colptr; /* 0-based, n+1 */
+  int64_t *rowval; /* 0-based      */
+  double *nzval;
+} orc_csc;
+
+/* node adjacency lists (CSR by column node), 0-based */
+static void node_adjacency(int64_t non, int64_t nel, int npe,
+                           const int32_t *conn, const int32_t *emat,
+                           int64_t **nptr_out, int64_t **nadj_out) {
+  /* node -> elements */
+  int64_t *cnt = (int64_t *)calloc(non + 1, sizeof(int64_t));
+  for (int64_t e = 0; e < nel; ++e) {
+    if (emat && emat[e] < 0) continue;
+    for (int a = 0; a < npe; ++a) cnt[conn[e * npe + a] + 1]++;
+  }
+  for (int64_t i = 0; i < non; ++i) cnt[i + 1] += cnt[i];
+  int64_t *fill = (int64_t *)malloc(sizeof(int64_t) * (non + 1));
+  memcpy(fill, cnt, sizeof(int64_t) * (non + 1));
+  int64_t *n2e = (int64_t *)malloc(sizeof(int64_t) * (cnt[non] + 1));
+  for (int64_t e = 0; e < nel; ++e) {
+    if (emat && emat[e] < 0) continue;
+    for (int a = 0; a < npe; ++a) n2e[fill[conn[e * npe + a]]++] = e;
+  }
+  /* adjacency */
+  int64_t *nptr = (int64_t *)calloc(non + 1, sizeof(int64_t));
+  int64_t cap = 0;
+  for (int64_t B = 0; B < non; ++B) {
+    int64_t m = (cnt[B + 1] - cnt[B]) * npe;
+    if (m > cap) cap = m;
+  }
+  int64_t *buf = (int64_t *)malloc(sizeof(int64_t) * (cap + 1));
+  int64_t total = 0;
+  int64_t *adj = NULL;
+  for (int pass = 0; pass < 2; ++pass) {
+    total = 0;
+    for (int64_t B = 0; B < non; ++B) {
+      int64_t m = 0;
+      for (int64_t k = cnt[B]; k < cnt[B + 1]; ++k) {
+        int64_t e = n2e[k];
+        for (int a = 0; a < npe; ++a) buf[m++] = conn[e * npe + a];
+      }
+      qsort(buf, m, sizeof(int64_t), cmp_i64);
+      int64_t u = 0;
+      for (int64_t k = 0; k < m; ++k)
+        if (k == 0 || buf[k] != buf[k - 1]) buf[u++] = buf[k];
+      if (pass == 0) {
+        nptr[B + 1] = u;
+      } else {
+        memcpy(adj + nptr[B], buf, sizeof(int64_t) * u);
+      }
+      total += u;
+    }
+    if (pass == 0) {
+      for (int64_t B = 0; B < non; ++B) nptr[B + 1] += nptr[B];
+      adj = (int64_t *)malloc(sizeof(int64_t) * (total + 1));
+    }
+  }
+  free(buf); free(n2e); free(fill); free(cnt);
+  *nptr_out = nptr;
+  *nadj_out = adj;
+}
+
+orc_csc *orc_pattern(int64_t non, int64_t nel, int npe, const int32_t *conn,
+                     const int32_t *emat, int pdim) {
+  int64_t *nptr, *adj;
+  node_adjacency(non, nel, npe, conn, emat, &nptr, &adj);
+  orc_csc *m = (orc_csc *)calloc(1, sizeof(orc_csc));
+  m->n = non * pdim;
+  m->nnz = nptr[non] * pdim * pdim;
+  m->colptr = (int64_t *)malloc(sizeof(int64_t) * (m->n + 1));
+  m->rowval = (int64_t *)malloc(sizeof(int64_t) * (m->nnz + 1));
+  m->nzval = (double *)calloc(m->nnz + 1, sizeof(double));
+  int64_t p = 0;
+  for (int64_t B = 0; B < non; ++B)
+    for (int j = 0; j < pdim; ++j) {
+      m->colptr[B * pdim + j] = p;
+      for (int64_t k = nptr[B]; k < nptr[B + 1]; ++k)
+        for (int i = 0; i < pdim; ++i) m->rowval[p++] = adj[k] * pdim + i;
+    }
+  m->colptr[m->n] = p;
+  free(nptr); free(adj);
+  return m;
+}
+
+void orc_free(orc_csc *m) {
+  if (!m) return;
+  free(m->colptr); free(m->rowval); free(m->nzval); free(m);
+}
+int64_t orc_n(const orc_csc *m) { return m->n; }
+int64_t orc_nnz(const orc_csc *m) { return m->nnz; }
+void orc_export(const orc_csc *m, int64_t *colptr, int64_t *rowval, double *nzval) {
+  if (colptr) memcpy(colptr, m->colptr, sizeof(int64_t) * (m->n + 1));
+  if (rowval) memcpy(rowval, m->rowval, sizeof(int64_t) * m->nnz);
+  if (nzval) memcpy(nzval, m->nzval, sizeof(double) * m->nnz);
+}
+
+/* ------------------------------------------------------------------------ */
+/* sparse(I, J, V, n, n) with duplicates combined left-to-right in input     */
+/* order (SparseArrays stdlib, as called at src/linear.jl:323), then         */
+/* dropzeros! (src/linear.jl:324).  Triplets are streamed element by element */
+/* in element order, so the combine order per entry is the element order.    */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  int64_t n, cap, len;
+  int64_t *I, *J;
+  double *V;
+} coo;
+
+static void coo_push(coo *c, int64_t i, int64_t j, double v) {
+  if (c->len == c->cap) {
+    c->cap = c->cap ? c->cap * 2 : 1024;
+    c->I = (int64_t *)realloc(c->I, sizeof(int64_t) * c->cap);
+    c->J = (int64_t *)realloc(c->J, sizeof(int64_t) * c->cap);
+    c->V = (double *)realloc(c->V, sizeof(double) * c->cap);
+  }
+  c->I[c->len] = i;
+  c->J[c->len] = j;
+  c->V[c->len] = v;
+  c->len++;
+}
+
+/* Returns CSC with summed duplicates (structural zeros kept). */
+static orc_csc *coo_to_csc(coo *c) {
+  int64_t n = c->n, L = c->len;
+  /* stable bucket by column */
+  int64_t *cptr = (int64_t *)calloc(n + 1, sizeof(int64_t));
+  for (int64_t k = 0; k < L; ++k) cptr[c->J[k] + 1]++;
+  for (int64_t j = 0; j < n; ++j) cptr[j + 1] += cptr[j];
+  int64_t *pos = (int64_t *)malloc(sizeof(int64_t) * (n + 1));
+  memcpy(pos, cptr, sizeof(int64_t) * (n + 1));
+  int64_t *perm = (int64_t *)malloc(sizeof(int64_t) * (L + 1));
+  for (int64_t k = 0; k < L; ++k) perm[pos[c->J[k]]++] = k;
+  /* combine duplicates per column in input order using a last-touched map */
+  int64_t *last = (int64_t *)malloc(sizeof(int64_t) * (n + 1));
+  for (int64_t i = 0; i < n; ++i) last[i] = -1;
+  orc_csc *m = (orc_csc *)calloc(1, sizeof(orc_csc));
+  m->n = n;
+  m->colptr = (int64_t *)malloc(sizeof(int64_t) * (n + 1));
+  m->rowval = (int64_t *)malloc(sizeof(int64_t) * (L + 1));
+  m->nzval = (double *)malloc(sizeof(double) * (L + 1));
+  int64_t out = 0;
+  for (int64_t j = 0; j < n; ++j) {
+    int64_t start = out;
+    m->colptr[j] = start;
+    for (int64_t t = cptr[j]; t < cptr[j + 1]; ++t) {
+      int64_t k = perm[t];
+      int64_t i = c->I[k];
+      if (last[i] >= start) {
+        m->nzval[last[i]] = m->nzval[last[i]] + c->V[k];
+      } else {
+        last[i] = out;
+        m->rowval[out] = i;
+        m->nzval[out] = c->V[k];
+        out++;
+      }
+    }
+    /* sort rows of this column (values move with rows) */
+    int64_t len = out - start;
+    for (int64_t a = 1; a < len; ++a) {
+      int64_t r = m->rowval[start + a];
+      double v = m->nzval[start + a];
+      int64_t b = a - 1;
+      while (b >= 0 && m->rowval[start + b] > r) {
+        m->rowval[start + b + 1] = m->rowval[start + b];
+        m->nzval[start + b + 1] = m->nzval[start + b];
+        --b;
+      }
+      m->rowval[start + b + 1] = r;
+      m->nzval[start + b + 1] = v;
+    }
+  }
+  m->colptr[n] = out;
+  m->nnz = out;
+  free(cptr); free(pos); free(perm); free(last);
+  return m;
+}
+
+/* dropzeros! in place */
+void orc_dropzeros(orc_csc *m) {
+  int64_t out = 0;
+  for (int64_t j = 0; j < m->n; ++j) {
+    int64_t s = m->colptr[j], e = m->colptr[j + 1];
+    m->colptr[j] = out;
+    for (int64_t k = s; k < e; ++k)
+      if (m->nzval[k] != 0.0) {
+        m->rowval[out] = m->rowval[k];
+        m->nzval[out] = m->nzval[k];
+        out++;
+      }
+  }
+  m->colptr[m->n] = out;
+  m->nnz = out;
+}
+
+/* Lumped mass: spdiagm(vec(sum(M, dims=2))) (src/linear.jl:1999-2001);
+ * row sums accumulated column by column in column order from 0.0. */
+static orc_csc *orc_lump(const orc_csc *M) {
+  int64_t n = M->n;
+  double *r = (double *)calloc(n + 1, sizeof(double));
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t k = M->colptr[j]; k < M->colptr[j + 1]; ++k)
+      r[M->rowval[k]] = r[M->rowval[k]] + M->nzval[k];
+  orc_csc *D = (orc_csc *)calloc(1, sizeof(orc_csc));
+  D->n = n;
+  D->nnz = n;
+  D->colptr = (int64_t *)malloc(sizeof(int64_t) * (n + 1));
+  D->rowval = (int64_t *)malloc(sizeof(int64_t) * (n + 1));
+  D->nzval = r;
+  for (int64_t j = 0; j <= n; ++j) D->colptr[j] = j;
+  for (int64_t j = 0; j < n; ++j) D->rowval[j] = j;
+  return D;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Assembly, restating stiffnessMatrixSolid (src/linear.jl:190-330),         */
+/* massMatrixSolid (:1854-2004) and heatCondMatrixSolid (src/heat.jl:36-137): */
+/* element loop in element order, per-element matrix, triplets with the      */
+/* transposed placement I = dof(l), J = dof(k), V = K1[k,l] (:258-259,       */
+/* :314-316), then sparse + dropzeros!.                                      */
+/*   params: per material (ELASTIC: E, nu; HEAT: k; MASS: rho), stride np.   */
+/* Returns NULL on a non-positive Jacobian (status in *err).                 */
+/* ------------------------------------------------------------------------ */
+orc_csc *orc_assemble(int kind, int ptype, int dim, int pdim, int64_t non,
+                      const double *xyz, int64_t nel, int npe,
+                      const int32_t *conn, const int32_t *emat, int nip,
+                      const double *w, const double *N, const double *dN,
+                      const double *params, int nmat, double thickness,
+                      int lumped, int *err) {
+  (void)nmat;
+  size_t nd = (size_t)pdim * npe;
+  double *Ke = (double *)malloc(sizeof(double) * nd * nd);
+  double *X = (double *)malloc(sizeof(double) * npe * 3);
+  coo c = {0};
+  c.n = non * pdim;
+  *err = 0;
+  for (int64_t e = 0; e < nel; ++e) {
+    int mat = emat ? emat[e] : 0;
+    if (mat < 0) continue;
+    double c1 = 0, c2 = 0;
+    double b = (ptype == PT_PLANE_STRESS || ptype == PT_HEAT || ptype == PT_PLANE_HEAT) ? thickness : 1.0;
+    if (kind == ORC_ELASTIC) {
+      orc_lame(ptype, params[2 * mat], params[2 * mat + 1], thickness, &c1, &c2);
+    } else if (kind == ORC_HEAT) {
+      c1 = params[mat] * b;
+    } else {
+      c1 = params[mat] * b;
+    }
+    for (int a = 0; a < npe; ++a) {
+      int64_t node = conn[e * npe + a];
+      for (int i = 0; i < 3; ++i) X[3 * a + i] = xyz[3 * node + i];
+    }
+    if (orc_element_matrix(kind, dim, pdim, npe, nip, w, N, dN, X, c1, c2, Ke)) {
+      *err = -1;
+      free(Ke); free(X); free(c.I); free(c.J); free(c.V);
+      return NULL;
+    }
+    /* column-major walk of K1: k fastest; I = nn2[l], J = nn2[k] */
+    for (size_t l = 0; l < nd; ++l)
+      for (size_t k = 0; k < nd; ++k) {
+        int64_t dl = (int64_t)conn[e * npe + l / pdim] * pdim + (int64_t)(l % pdim);
+        int64_t dk = (int64_t)conn[e * npe + k / pdim] * pdim + (int64_t)(k % pdim);
+        coo_push(&c, dl, dk, Ke[k * nd + l]);
+      }
+  }
+  orc_csc *m = coo_to_csc(&c);
+  free(c.I); free(c.J); free(c.V);
+  free(Ke); free(X);
+  if (kind == ORC_MASS && lumped) {
+    orc_csc *D = orc_lump(m);
+    orc_free(m);
+    m = D;
+  }
+  orc_dropzeros(m);
+  return m;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Threaded direct-CSC assembly, restating the reference's fastest CPU path  */
+/* (assemble_csc_worker! + reduce_csc_buffers!, src/multifield.jl:2394-2499, */
+/* :2345-2380): structural pattern reused, cyclic element chunks per worker, */
+/* one binary search per node pair (find_csc_position, :2260-2283), per-     */
+/* worker nzval buffers summed at the end.  Used as the timed CPU baseline.  */
+/* `pat` must be the structural pattern of the same mesh; nzval overwritten. */
+/* Returns elapsed seconds of the assembly (pattern excluded).               */
+/* ------------------------------------------------------------------------ */
+static int64_t find_pos(const int64_t *rowval, int64_t lo, int64_t hi, int64_t r) {
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if (rowval[mid] < r) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+double orc_assemble_csc_threaded(int kind, int ptype, int dim, int pdim,
+                                 const double *xyz, int64_t nel, int npe,
+                                 const int32_t *conn, int nip, const double *w,
+                                 const double *N, const double *dN,
+                                 const double *params, double thickness,
+                                 orc_csc *pat, int nthreads, int chunk) {
+  int64_t nnz = pat->nnz;
+  int T = nthreads > 0 ? nthreads : 1;
+#ifdef _OPENMP
+  double t0 = omp_get_wtime();
+#else
+  double t0 = 0;
+#endif
+  double **bufs = (double **)malloc(sizeof(double *) * T);
+#pragma omp parallel num_threads(T)
+  {
+#ifdef _OPENMP
+    int tid = omp_get_thread_num();
+#else
+    int tid = 0;
+#endif
+    double *nz = (double *)calloc(nnz + 1, sizeof(double));
+    bufs[tid] = nz;
+    size_t nd = (size_t)pdim * npe;
+    double *Ke = (double *)malloc(sizeof(double) * nd * nd);
+    double *X = (double *)malloc(sizeof(double) * npe * 3);
+    double c1 = 0, c2 = 0;
+    double b = (ptype == PT_PLANE_STRESS || ptype == PT_HEAT || ptype == PT_PLANE_HEAT) ? thickness : 1.0;
+    if (kind == ORC_ELASTIC) orc_lame(ptype, params[0], params[1], thickness, &c1, &c2);
+    else c1 = params[0] * b;
+    int64_t nchunks = (nel + chunk - 1) / chunk;
+    for (int64_t ch = tid; ch < nchunks; ch += T) {
+      int64_t e0 = ch * chunk, e1 = e0 + chunk < nel ? e0 + chunk : nel;
+      for (int64_t e = e0; e < e1; ++e) {
+        for (int a = 0; a < npe; ++a) {
+          int64_t node = conn[e * npe + a];
+          for (int i = 0; i < 3; ++i) X[3 * a + i] = xyz[3 * node + i];
+        }
+        orc_element_matrix(kind, dim, pdim, npe, nip, w, N, dN, X, c1, c2, Ke);
+        for (int bn = 0; bn < npe; ++bn) {
+          int64_t B = conn[e * npe + bn];
+          for (int an = 0; an < npe; ++an) {
+            int64_t A = conn[e * npe + an];
+            int64_t col0 = B * pdim;
+            int64_t p0 = find_pos(pat->rowval, pat->colptr[col0], pat->colptr[col0 + 1], A * pdim);
+            int64_t off = p0 - pat->colptr[col0];
+            for (int j = 0; j < pdim; ++j) {
+              int64_t base = pat->colptr[col0 + j] + off;
+              for (int i = 0; i < pdim; ++i)
+                nz[base + i] += Ke[((size_t)an * pdim + i) * nd + (size_t)bn * pdim + j];
+            }
+          }
+        }
+      }
+    }
+    free(Ke); free(X);
+  }
+  /* reduce worker buffers */
+#pragma omp parallel for num_threads(T) schedule(static)
+  for (int64_t k = 0; k < nnz; ++k) {
+    double s = 0.0;
+    for (int t = 0; t < T; ++t) s += bufs[t][k];
+    pat->nzval[k] = s;
+  }
+  for (int t = 0; t < T; ++t) free(bufs[t]);
+  free(bufs);
+#ifdef _OPENMP
+  return omp_get_wtime() - t0;
+#else
+  return 0.0;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* y = A x (CSC, sequential).                                               */
+/* ------------------------------------------------------------------------ */
+void orc_spmv(const orc_csc *A, const double *x, double *y) {
+  for (int64_t i = 0; i < A->n; ++i) y[i] = 0.0;
+  for (int64_t j = 0; j < A->n; ++j) {
+    double xj = x[j];
+    for (int64_t k = A->colptr[j]; k < A->colptr[j + 1]; ++k)
+      y[A->rowval[k]] += A->nzval[k] * xj;
+  }
+}
+
+static double dotp(int64_t n, const double *a, const double *b) {
+  double s = 0.0;
+  for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Condensed Dirichlet solve with IterativeSolvers.cg's recurrence           */
+/* (IterativeSolvers 0.9.4, the call at src/linear.jl:3827-3833):            */
+/*   f_kin = A[:,fixed] x[fixed]; solve A_ff x_f = b_f - f_kin_f from x_f=0; */
+/*   per iteration c = P^-1 r, rho = c.r, u = c + (rho/rho_prev) u,          */
+/*   c = A u, alpha = rho/(u.c), x += alpha u, r -= alpha c,                 */
+/*   stop when ||r|| <= reltol ||r0|| or after maxiter products.             */
+/* precond: 0 identity, 1 Jacobi (diagonal of A_ff).                         */
+/* Returns iterations; *relres = ||r||/||r0||.                               */
+/* ------------------------------------------------------------------------ */
+int64_t orc_cg(const orc_csc *A, const double *b, double *x,
+               const uint8_t *fixed, int precond, double reltol,
+               int64_t maxiter, double *relres) {
+  int64_t n = A->n;
+  double *xf = (double *)calloc(n, sizeof(double));
+  double *r = (double *)malloc(sizeof(double) * n);
+  double *c = (double *)malloc(sizeof(double) * n);
+  double *u = (double *)calloc(n, sizeof(double));
+  double *dinv = (double *)malloc(sizeof(double) * n);
+  for (int64_t i = 0; i < n; ++i) xf[i] = fixed[i] ? x[i] : 0.0;
+  orc_spmv(A, xf, c); /* f_kin */
+  for (int64_t i = 0; i < n; ++i) r[i] = fixed[i] ? 0.0 : b[i] - c[i];
+  for (int64_t j = 0; j < n; ++j) {
+    double d = 0.0;
+    for (int64_t k = A->colptr[j]; k < A->colptr[j + 1]; ++k)
+      if (A->rowval[k] == j) d = A->nzval[k];
+    dinv[j] = (precond == 1 && d != 0.0) ? 1.0 / d : 1.0;
+  }
+  for (int64_t i = 0; i < n; ++i) xf[i] = 0.0;
+  double res0 = sqrt(dotp(n, r, r)), res = res0;
+  double tol = reltol * res0;
+  double rho_prev = 1.0;
+  int64_t it = 0;
+  while (!(res <= tol) && it < maxiter) {
+    for (int64_t i = 0; i < n; ++i) c[i] = fixed[i] ? 0.0 : dinv[i] * r[i];
+    double rho = dotp(n, c, r);
+    double beta = rho / rho_prev;
+    rho_prev = rho;
+    for (int64_t i = 0; i < n; ++i) u[i] = c[i] + beta * u[i];
+    orc_spmv(A, u, c);
+    for (int64_t i = 0; i < n; ++i) if (fixed[i]) c[i] = 0.0;
+    double alpha = rho / dotp(n, u, c);
+    for (int64_t i = 0; i < n; ++i) {
+      xf[i] += alpha * u[i];
+      r[i] -= alpha * c[i];
+    }
+    res = sqrt(dotp(n, r, r));
+    ++it;
+  }
+  for (int64_t i = 0; i < n; ++i) if (!fixed[i]) x[i] = xf[i];
+  *relres = res0 > 0 ? res / res0 : 0.0;
+  free(xf); free(r); free(c); free(u); free(dinv);
+  return it;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Consistent nodal load of boundary elements, loadVector                    */
+/* (src/linear.jl:3088-3434): f1 += H^T t Ja w per point with               */
+/* Ja = |t1| b for 2D edges (:3394-3395), |t1 x t2| for 3D faces            */
+/* (:3380-3384), t1, t2 the columns of the boundary Jacobian.  Constant     */
+/* traction t[pdim] or nodal values tn[pdim*nb] interpolated with H.        */
+/* Element contributions are added into f in element order.                 */
+/* ------------------------------------------------------------------------ */
+void orc_load_vector(int problem_dim, int pdim, const double *xyz,
+                     int64_t nelb, int npeb, const int32_t *connb, int nip,
+                     const double *w, const double *N, const double *dN,
+                     const double *t, const double *tn, double thickness,
+                     double *f) {
+  int bdim = problem_dim - 1;
+  double *fe = (double *)malloc(sizeof(double) * npeb * pdim);
+  for (int64_t e = 0; e < nelb; ++e) {
+    for (int k = 0; k < npeb * pdim; ++k) fe[k] = 0.0;
+    for (int q = 0; q < nip; ++q) {
+      double t1[3] = {0, 0, 0}, t2[3] = {0, 0, 0};
+      for (int i = 0; i < 3; ++i) {
+        double a1 = 0.0, a2 = 0.0;
+        for (int a = 0; a < npeb; ++a) {
+          double xa = xyz[3 * (int64_t)connb[e * npeb + a] + i];
+          a1 = fma(xa, dN[((size_t)q * npeb + a) * 3 + 0], a1);
+          if (bdim == 2) a2 = fma(xa, dN[((size_t)q * npeb + a) * 3 + 1], a2);
+        }
+        t1[i] = a1;
+        t2[i] = a2;
+      }
+      double Ja;
+      if (bdim == 1) {
+        Ja = sqrt(t1[0] * t1[0] + t1[1] * t1[1]) * thickness;
+      } else {
+        double xy = t1[0] * t2[1] - t1[1] * t2[0];
+        double yz = t1[1] * t2[2] - t1[2] * t2[1];
+        double zx = t1[2] * t2[0] - t1[0] * t2[2];
+        Ja = sqrt(xy * xy + yz * yz + zx * zx);
+      }
+      double tq[3] = {0, 0, 0};
+      for (int i = 0; i < pdim; ++i) {
+        if (tn) {
+          double acc = 0.0;
+          for (int a = 0; a < npeb; ++a)
+            acc = fma(N[(size_t)q * npeb + a], tn[(int64_t)connb[e * npeb + a] * pdim + i], acc);
+          tq[i] = acc;
+        } else {
+          tq[i] = t[i];
+        }
+      }
+      double jw = Ja * w[q];
+      for (int a = 0; a < npeb; ++a)
+        for (int i = 0; i < pdim; ++i)
+          fe[a * pdim + i] = fma(N[(size_t)q * npeb + a] * tq[i], jw, fe[a * pdim + i]);
+    }
+    for (int a = 0; a < npeb; ++a)
+      for (int i = 0; i < pdim; ++i)
+        f[(int64_t)connb[e * npeb + a] * pdim + i] += fe[a * pdim + i];
+  }
+  free(fe);
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* Elementwise nodal gradient, the :vector_grad branch of ∇ (src/nabla.jl:   */
+/* 77-311): at every element node k, J and the physical gradients of all     */
+/* shape functions at node k's reference coordinates; T[i][j] = sum_l        */
+/* g_l[j] u_l[i] (fma chain over l), stored column-major (9 per node);       */
+/* with add_identity the deformation gradient F = I + T.                     */
+/* dNn[(k*npe+l)*3+j] = dN_l/dxi_j at node k.                               */
+/* ------------------------------------------------------------------------ */
+int orc_grad_elementwise(const double *xyz, int64_t nel, int npe, const int32_t *conn,
+                         const double *dNn, const double *u, int add_identity,
+                         double *out) {
+  double *X = (double *)malloc(sizeof(double) * npe * 3);
+  int rc = 0;
+  for (int64_t e = 0; e < nel; ++e) {
+    for (int a = 0; a < npe; ++a)
+      for (int i = 0; i < 3; ++i) X[3 * a + i] = xyz[3 * (int64_t)conn[e * npe + a] + i];
+    for (int k = 0; k < npe; ++k) {
+      const double *d = dNn + (size_t)k * npe * 3;
+      double inv[9];
+      double det = orc_geom(3, npe, X, d, inv);
+      if (!(det > 0.0)) rc = -1;
+      double T[3][3] = {{0}};
+      for (int l = 0; l < npe; ++l) {
+        double g[3];
+        for (int i = 0; i < 3; ++i) {
+          double acc = 0.0;
+          for (int j = 0; j < 3; ++j) acc = fma(inv[3 * j + i], d[l * 3 + j], acc);
+          g[i] = acc;
+        }
+        const double *ul = u + 3 * (int64_t)conn[e * npe + l];
+        for (int j = 0; j < 3; ++j)
+          for (int i = 0; i < 3; ++i) T[i][j] = fma(g[j], ul[i], T[i][j]);
+      }
+      double *o = out + (size_t)e * npe * 9 + (size_t)k * 9;
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) o[3 * j + i] = (add_identity && i == j) ? T[i][j] + 1.0 : T[i][j];
+    }
+  }
+  free(X);
+  return rc;
+}

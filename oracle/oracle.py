@@ -1,0 +1,232 @@
+"""Python access to the CPU oracle (llfem_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, as the checker or the timed CPU baseline.  The
+product (lowlevelfem.jl_gb300) never imports it.
+
+``build()`` compiles the restatement with OpenMP and without floating-point
+contraction (-ffp-contract=off): the arithmetic contract it shares with the
+CUDA kernels names every fused multiply-add explicitly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "llfem_oracle.c")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libllfem_oracle.so")
+
+ELASTIC, HEAT, MASS = 0, 1, 2
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    tmp = LIB + ".tmp"
+    subprocess.check_call(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp",
+                           "-ffp-contract=off", "-o", tmp, SRC, "-lm"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        vp, i32, i64, dbl = C.c_void_p, C.c_int, C.c_int64, C.c_double
+        Pd, Pi32, Pi64, Pu8 = (C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64),
+                               C.POINTER(C.c_uint8))
+        L.orc_pattern.restype = vp
+        L.orc_pattern.argtypes = [i64, i64, i32, Pi32, Pi32, i32]
+        L.orc_assemble.restype = vp
+        L.orc_assemble.argtypes = [i32, i32, i32, i32, i64, Pd, i64, i32, Pi32, Pi32, i32, Pd, Pd, Pd,
+                                   Pd, i32, dbl, i32, C.POINTER(i32)]
+        L.orc_assemble_csc_threaded.restype = dbl
+        L.orc_assemble_csc_threaded.argtypes = [i32, i32, i32, i32, Pd, i64, i32, Pi32, i32, Pd, Pd,
+                                                Pd, Pd, dbl, vp, i32, i32]
+        L.orc_free.argtypes = [vp]
+        L.orc_n.restype = i64
+        L.orc_n.argtypes = [vp]
+        L.orc_nnz.restype = i64
+        L.orc_nnz.argtypes = [vp]
+        L.orc_export.argtypes = [vp, Pi64, Pi64, Pd]
+        L.orc_element_matrix.restype = i32
+        L.orc_element_matrix.argtypes = [i32, i32, i32, i32, i32, Pd, Pd, Pd, Pd, dbl, dbl, Pd]
+        L.orc_cg.restype = i64
+        L.orc_cg.argtypes = [vp, Pd, Pd, Pu8, i32, dbl, i64, Pd]
+        L.orc_spmv.argtypes = [vp, Pd, Pd]
+        L.orc_lame.argtypes = [i32, dbl, dbl, dbl, Pd, Pd]
+        L.orc_load_vector.argtypes = [i32, i32, Pd, i64, i32, Pi32, i32, Pd, Pd, Pd, Pd, Pd, dbl, Pd]
+        L.orc_num_threads.restype = i32
+        L.orc_grad_elementwise.restype = i32
+        L.orc_grad_elementwise.argtypes = [Pd, i64, i32, Pi32, Pd, Pd, i32, Pd]
+        _lib = L
+    return _lib
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+class CSC:
+    """Oracle CSC matrix (0-based arrays kept in C memory, exported lazily)."""
+
+    def __init__(self, h):
+        self.h = h
+
+    @property
+    def n(self):
+        return lib().orc_n(self.h)
+
+    @property
+    def nnz(self):
+        return lib().orc_nnz(self.h)
+
+    def arrays(self):
+        n, nnz = self.n, self.nnz
+        colptr = np.zeros(n + 1, dtype=np.int64)
+        rowval = np.zeros(nnz, dtype=np.int64)
+        nzval = np.zeros(nnz)
+        lib().orc_export(self.h, _p(colptr, C.c_int64), _p(rowval, C.c_int64), _p(nzval, C.c_double))
+        return colptr, rowval, nzval
+
+    def julia(self):
+        """1-based SparseMatrixCSC arrays."""
+        c, r, v = self.arrays()
+        return c + 1, r + 1, v
+
+    def scipy(self):
+        import scipy.sparse as sp
+        c, r, v = self.arrays()
+        return sp.csc_matrix((v, r, c), shape=(self.n, self.n))
+
+    def spmv(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.n)
+        lib().orc_spmv(self.h, _p(x, C.c_double), _p(y, C.c_double))
+        return y
+
+    def cg(self, b, x0, fixed, precond=0, reltol=1.4901161193847656e-08, maxiter=None):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.ascontiguousarray(x0, dtype=np.float64).copy()
+        fx = np.ascontiguousarray(fixed, dtype=np.uint8)
+        rr = C.c_double(0.0)
+        it = lib().orc_cg(self.h, _p(b, C.c_double), _p(x, C.c_double), _p(fx, C.c_uint8), precond,
+                          reltol, self.n if maxiter is None else int(maxiter), C.byref(rr))
+        return x, it, rr.value
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().orc_free(self.h)
+        except Exception:
+            pass
+
+
+def _conn0(conn):
+    return np.ascontiguousarray(np.asarray(conn) - 1, dtype=np.int32)
+
+
+def pattern(non, conn, pdim, emat=None):
+    conn0 = _conn0(conn)
+    em = None if emat is None else np.ascontiguousarray(emat, dtype=np.int32)
+    h = lib().orc_pattern(non, conn0.shape[0], conn0.shape[1], _p(conn0, C.c_int32), _p(em, C.c_int32), pdim)
+    return CSC(h)
+
+
+def assemble(kind, ptype, dim, pdim, xyz, conn, rule, params, thickness=1.0, lumped=False, emat=None):
+    """Reference-order COO assembly + sparse + dropzeros! (see llfem_oracle.c)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    conn0 = _conn0(conn)
+    params = np.ascontiguousarray(params, dtype=np.float64).ravel()
+    em = None if emat is None else np.ascontiguousarray(emat, dtype=np.int32)
+    w = np.ascontiguousarray(rule["w"], dtype=np.float64)
+    N = np.ascontiguousarray(rule["N"], dtype=np.float64)
+    dN = np.ascontiguousarray(rule["dN"], dtype=np.float64)
+    err = C.c_int(0)
+    nmat = 1
+    h = lib().orc_assemble(kind, ptype, dim, pdim, xyz.shape[0], _p(xyz, C.c_double), conn0.shape[0],
+                           conn0.shape[1], _p(conn0, C.c_int32), _p(em, C.c_int32), len(w),
+                           _p(w, C.c_double), _p(N, C.c_double), _p(dN, C.c_double),
+                           _p(params, C.c_double), nmat, float(thickness), int(lumped), C.byref(err))
+    if not h:
+        raise ValueError("oracle: non-positive Jacobian determinant")
+    return CSC(h)
+
+
+def assemble_threaded(kind, ptype, dim, pdim, xyz, conn, rule, params, pat: CSC, thickness=1.0,
+                      nthreads=None, chunk=256):
+    """Timed CPU baseline: threaded direct-CSC assembly into `pat` (overwritten).
+    Returns seconds."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    conn0 = _conn0(conn)
+    params = np.ascontiguousarray(params, dtype=np.float64).ravel()
+    w = np.ascontiguousarray(rule["w"], dtype=np.float64)
+    N = np.ascontiguousarray(rule["N"], dtype=np.float64)
+    dN = np.ascontiguousarray(rule["dN"], dtype=np.float64)
+    T = nthreads or lib().orc_num_threads()
+    return lib().orc_assemble_csc_threaded(kind, ptype, dim, pdim, _p(xyz, C.c_double), conn0.shape[0],
+                                           conn0.shape[1], _p(conn0, C.c_int32), len(w), _p(w, C.c_double),
+                                           _p(N, C.c_double), _p(dN, C.c_double), _p(params, C.c_double),
+                                           float(thickness), pat.h, T, chunk)
+
+
+def element_matrix(kind, dim, pdim, X, rule, c1, c2=0.0):
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    npe = X.shape[0]
+    nd = pdim * npe
+    Ke = np.zeros((nd, nd))
+    w = np.ascontiguousarray(rule["w"]); N = np.ascontiguousarray(rule["N"]); dN = np.ascontiguousarray(rule["dN"])
+    rc = lib().orc_element_matrix(kind, dim, pdim, npe, len(w), _p(w, C.c_double), _p(N, C.c_double),
+                                  _p(dN, C.c_double), _p(X, C.c_double), c1, c2, _p(Ke, C.c_double))
+    if rc:
+        raise ValueError("oracle: non-positive Jacobian determinant")
+    return Ke
+
+
+def lame(ptype, E, nu, thickness=1.0):
+    a, b = C.c_double(), C.c_double()
+    lib().orc_lame(ptype, E, nu, thickness, C.byref(a), C.byref(b))
+    return a.value, b.value
+
+
+def load_vector(problem_dim, pdim, xyz, connb, rule, t=None, tn=None, thickness=1.0, f=None):
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    cb = _conn0(connb)
+    ndof = pdim * xyz.shape[0]
+    f = np.zeros(ndof) if f is None else np.ascontiguousarray(f, dtype=np.float64)
+    t = None if t is None else np.ascontiguousarray(t, dtype=np.float64)
+    tn = None if tn is None else np.ascontiguousarray(tn, dtype=np.float64)
+    w = np.ascontiguousarray(rule["w"]); N = np.ascontiguousarray(rule["N"]); dN = np.ascontiguousarray(rule["dN"])
+    lib().orc_load_vector(problem_dim, pdim, _p(xyz, C.c_double), cb.shape[0], cb.shape[1], _p(cb, C.c_int32),
+                          len(w), _p(w, C.c_double), _p(N, C.c_double), _p(dN, C.c_double), _p(t, C.c_double),
+                          _p(tn, C.c_double), float(thickness), _p(f, C.c_double))
+    return f
+
+
+def grad_elementwise(xyz, conn, rule, u, add_identity=False):
+    """Elementwise nodal gradient (nel, 9*npe) of a nodal 3-vector field."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    conn0 = _conn0(conn)
+    dNn = np.ascontiguousarray(rule["dN_nodes"], dtype=np.float64)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    out = np.zeros((conn0.shape[0], 9 * conn0.shape[1]))
+    rc = lib().orc_grad_elementwise(_p(xyz, C.c_double), conn0.shape[0], conn0.shape[1], _p(conn0, C.c_int32),
+                                    _p(dNn, C.c_double), _p(u, C.c_double), int(add_identity),
+                                    _p(out, C.c_double))
+    if rc:
+        raise ValueError("oracle: non-positive Jacobian determinant")
+    return out
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()

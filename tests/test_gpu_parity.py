@@ -1,0 +1,221 @@
+"""GPU assembly vs the CPU oracle, through the C-ABI.
+
+The FP64 form follows the same arithmetic contract as the oracle, so the
+stored CSC (colptr, rowval, nzval) must be identical bit for bit, including
+the dropzeros! pattern.  Full-size configurations are checked through
+size-independent properties.
+"""
+import numpy as np
+import pytest
+
+from helpers import PT, assert_csc_identical, make_mesh, oracle_operator
+
+pytestmark = pytest.mark.gpu
+
+SOLID_CASES = [
+    # kind, n, order, simplex, ptype
+    ("rect", 6, 1, False, "PlaneStress"),
+    ("rect", 5, 2, False, "PlaneStrain"),
+    ("rect", 3, 3, False, "PlaneStrain"),
+    ("rect", 2, 4, False, "PlaneStress"),
+    ("rect", 5, 1, True, "PlaneStrain"),
+    ("rect", 3, 2, True, "PlaneStress"),
+    ("rect", 2, 4, True, "PlaneStrain"),
+    ("box", 3, 1, False, "Solid"),
+    ("box", 3, 2, False, "Solid"),
+    ("box", 2, 3, False, "Solid"),
+    ("box", 1, 4, False, "Solid"),
+    ("box", 2, 1, True, "Solid"),
+    ("box", 2, 2, True, "Solid"),
+    ("box", 1, 3, True, "Solid"),
+    ("box", 1, 4, True, "Solid"),
+]
+
+
+def _ids(c):
+    return f"{c[0]}-n{c[1]}-p{c[2]}{'-simplex' if c[3] else ''}-{c[4]}"
+
+
+@pytest.mark.parametrize("case", SOLID_CASES, ids=_ids)
+def test_stiffness_bit_identical(llf, orc, case):
+    kind, n, order, simplex, ptype = case
+    m = make_mesh(llf, kind, n, order, simplex)
+    mat = llf.Material("body", E=2.1e5, nu=0.3)
+    p = llf.Problem([mat], type=ptype, thickness=0.7)
+    K = llf.stiffnessMatrix(p)
+    ref = oracle_operator(llf, orc, m, "stiffness", PT[ptype], mat, thickness=0.7)
+    assert_csc_identical(K.csc(), ref.julia(), f"K {_ids(case)}")
+
+
+@pytest.mark.parametrize("case", SOLID_CASES[::2], ids=_ids)
+@pytest.mark.parametrize("lumped", [False, True])
+def test_mass_bit_identical(llf, orc, case, lumped):
+    kind, n, order, simplex, ptype = case
+    m = make_mesh(llf, kind, n, order, simplex)
+    mat = llf.Material("body", rho=7.85e-9)
+    p = llf.Problem([mat], type=ptype, thickness=0.7)
+    M = llf.massMatrix(p, lumped=lumped)
+    ref = oracle_operator(llf, orc, m, "mass", PT[ptype], mat, thickness=0.7, lumped=lumped)
+    assert_csc_identical(M.csc(), ref.julia(), f"M lumped={lumped} {_ids(case)}")
+
+
+HEAT_CASES = [("rect", 6, 1, False), ("rect", 3, 3, False), ("rect", 3, 2, True),
+              ("box", 3, 1, False), ("box", 2, 2, False), ("box", 1, 4, False), ("box", 2, 2, True)]
+
+
+@pytest.mark.parametrize("case", HEAT_CASES, ids=lambda c: f"{c[0]}-n{c[1]}-p{c[2]}{'-simplex' if c[3] else ''}")
+def test_heat_bit_identical(llf, orc, case):
+    kind, n, order, simplex = case
+    m = make_mesh(llf, kind, n, order, simplex)
+    ptype = "HeatConduction" if kind == "box" else "PlaneHeatConduction"
+    mat = llf.Material("body", k=45.0)
+    p = llf.Problem([mat], type=ptype, thickness=2.0)
+    K = llf.heatConductionMatrix(p)
+    ref = oracle_operator(llf, orc, m, "heat", PT[ptype], mat, thickness=2.0)
+    assert_csc_identical(K.csc(), ref.julia(), f"KT {case}")
+
+
+def test_two_materials_and_skipped_elements(llf, orc):
+    m = llf.structured_box_mesh(n=3, order=2)
+    cx = m.xyz[m.conn - 1][:, :, 0].mean(axis=1)
+    sel_a = np.where(cx < 0.5)[0]
+    sel_b = np.where(cx >= 0.5)[0]
+    for name, sel in (("a", sel_a), ("b", sel_b)):
+        g = llf.Group(name, 3, np.unique(m.conn[sel]), m.family, m.order, m.conn[sel])
+        g.elems = sel
+        m.groups[name] = g
+    ma = llf.Material("a", E=1e5, nu=0.25)
+    mb = llf.Material("b", E=3e5, nu=0.35)
+    p = llf.Problem([ma, mb], type="Solid")
+    K = llf.stiffnessMatrix(p)
+    emat = np.where(cx < 0.5, 0, 1).astype(np.int32)
+    rule = llf._lib.builtin_rule(m.family, m.order)
+    ref = orc.assemble(orc.ELASTIC, 0, 3, 3, m.xyz, m.conn, rule, [ma.E, ma.nu, mb.E, mb.nu], emat=emat)
+    assert_csc_identical(K.csc(), ref.julia(), "two materials")
+    # a single material on half of the body: the other elements contribute nothing
+    p1 = llf.Problem([ma], type="Solid")
+    K1 = llf.stiffnessMatrix(p1)
+    em1 = np.where(cx < 0.5, 0, -1).astype(np.int32)
+    ref1 = orc.assemble(orc.ELASTIC, 0, 3, 3, m.xyz, m.conn, rule, [ma.E, ma.nu], emat=em1)
+    assert_csc_identical(K1.csc(), ref1.julia(), "half body")
+
+
+def test_pattern_copy_matches_oracle(llf, orc):
+    m = llf.structured_box_mesh(n=3, order=2)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    colptr, rowval = p.pattern().copy()
+    rc, rr, _ = orc.pattern(m.non, m.conn, 3).julia()
+    assert np.array_equal(colptr, rc) and np.array_equal(rowval, rr)
+
+
+def test_axpby_same_pattern(llf, orc):
+    llf.structured_box_mesh(n=2, order=2)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    K = llf.stiffnessMatrix(p)
+    M = llf.massMatrix(p, lumped=False)
+    S = K + M
+    D = K - K
+    assert D.nnz() == 0
+    Ks = K.dm.copy_structural()
+    Ms = M.dm.copy_structural()
+    Ss = S.dm.copy_structural()
+    assert np.array_equal(Ss, Ks + Ms)
+    c, r, v = S.csc()
+    assert np.array_equal(v, (Ks + Ms)[(Ks + Ms) != 0])
+
+
+def test_spmv_matches_scipy(llf):
+    llf.structured_box_mesh(n=4, order=2)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    K = llf.stiffnessMatrix(p)
+    x = np.random.default_rng(0).standard_normal(K.shape[0])
+    y = K * x
+    yref = K.A @ x
+    assert np.abs(y - yref).max() <= 1e-13 * np.abs(yref).max()
+
+
+def test_grad_bit_identical(llf, orc):
+    m = llf.structured_box_mesh(n=2, order=2)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    rng = np.random.default_rng(1)
+    u = llf.VectorField(rng.standard_normal((3 * m.non, 1)) * 1e-2, p)
+    F = llf.grad(u, add_identity=True)
+    rule = llf._lib.builtin_rule(m.family, m.order)
+    ref = orc.grad_elementwise(m.xyz, m.conn, rule, u.a[:, 0], add_identity=True)
+    assert np.array_equal(F.A, ref)
+    # a linear field has a constant gradient
+    A = np.array([[0.1, 0.2, -0.3], [0.05, -0.1, 0.0], [0.3, 0.0, 0.2]])
+    ul = (m.xyz @ A.T).ravel()
+    T = llf.grad(llf.VectorField(ul.reshape(-1, 1), p)).A.reshape(m.nel, m.npe, 3, 3)
+    assert np.abs(T - A.T[None, None]).max() < 1e-13   # column-major T[i,j] = A[i,j]
+
+
+def test_load_vector_bit_identical(llf, orc):
+    m = llf.structured_box_mesh(n=3, order=2)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    f = llf.loadVector(p, [llf.load("right", fx=1.0, fy=-2.0, fz=0.5)])
+    g = m.group("right")
+    ref = orc.load_vector(3, 3, m.xyz, g.conn, llf._lib.builtin_rule(g.family, g.order), t=[1.0, -2.0, 0.5])
+    assert np.array_equal(f.a[:, 0], ref)
+    assert np.allclose(f.a[:, 0].reshape(-1, 3).sum(axis=0), [1.0, -2.0, 0.5], rtol=1e-13)
+    m2 = llf.structured_rect_mesh(n=4, order=3)
+    p2 = llf.Problem([llf.Material("body")], type="PlaneStress", thickness=0.5)
+    f2 = llf.loadVector(p2, [llf.load("top", fy=-1.0)])
+    g2 = m2.group("top")
+    ref2 = orc.load_vector(2, 2, m2.xyz, g2.conn, llf._lib.builtin_rule(g2.family, g2.order), t=[0.0, -1.0],
+                           thickness=0.5)
+    assert np.array_equal(f2.a[:, 0], ref2)
+
+
+# ---------------------------------------------------------------- error paths
+def test_inverted_element_is_an_error(llf):
+    m = llf.structured_box_mesh(n=2, order=1)
+    m.conn[0] = m.conn[0][[1, 0, 3, 2, 5, 4, 7, 6]]  # mirror element 0
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    with pytest.raises(llf.LLFError, match="Jacobian"):
+        llf.stiffnessMatrix(p)
+
+
+def test_bad_node_tag_is_an_error(llf):
+    m = llf.structured_box_mesh(n=2, order=1)
+    m.conn[3, 2] = m.non + 5
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    with pytest.raises(llf.LLFError, match="node tag"):
+        p.device_mesh()
+
+
+def test_nan_coordinate_is_an_error(llf):
+    m = llf.structured_box_mesh(n=2, order=1)
+    m.xyz[4, 1] = np.nan
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    with pytest.raises(llf.LLFError, match="NaN"):
+        p.device_mesh()
+
+
+# ---------------------------------------------------------------- full size
+def test_c1_quad4_full_size_properties(llf, orc):
+    m = llf.structured_rect_mesh(lx=10.0, ly=5.0, dx=0.05, dy=0.05)
+    mat = llf.Material("body", E=2e5, nu=0.3)
+    p = llf.Problem([mat], type="PlaneStrain")
+    K = llf.stiffnessMatrix(p)
+    ref = oracle_operator(llf, orc, m, "stiffness", PT["PlaneStrain"], mat)
+    assert_csc_identical(K.csc(), ref.julia(), "C1 quad4 200x100")
+
+
+def test_c2_hex27_full_size_properties(llf):
+    m = llf.structured_box_mesh(n=40, order=2)
+    mat = llf.Material("body", E=2.1e5, nu=0.3)
+    p = llf.Problem([mat], type="Solid")
+    assert p.pattern().nnz == 297685449
+    K = llf.stiffnessMatrix(p)
+    c, r, v = K.csc()
+    n = 3 * m.non
+    assert len(c) == n + 1 and c[-1] - 1 == len(v)
+    # rigid translations are in the kernel: K t = 0
+    for comp in range(3):
+        t = np.zeros(n); t[comp::3] = 1.0
+        assert np.abs(K * t).max() <= 1e-10 * np.abs(v).max()
+    # symmetry of the stored values through y = K x vs x' K
+    x = np.random.default_rng(2).standard_normal(n)
+    z = np.random.default_rng(3).standard_normal(n)
+    assert abs(z @ (K * x) - x @ (K * z)) <= 1e-12 * np.abs(K * x).sum()
