@@ -493,6 +493,19 @@ int run_gather(llf_ctx *ctx, llf_pattern *pat, const double *Kp, int npairs, dou
 }  // namespace
 
 // ------------------------------------------------------------------ host
+int gather_pairs(llf_ctx *ctx, llf_pattern *pat, const double *Kp, int npairs, bool blockval,
+                 double *nz) {
+  switch (pat->pdim * 2 + (blockval ? 1 : 0)) {
+    case 2: return run_gather<1, false>(ctx, pat, Kp, npairs, nz);
+    case 3: return run_gather<1, true>(ctx, pat, Kp, npairs, nz);
+    case 4: return run_gather<2, false>(ctx, pat, Kp, npairs, nz);
+    case 5: return run_gather<2, true>(ctx, pat, Kp, npairs, nz);
+    case 6: return run_gather<3, false>(ctx, pat, Kp, npairs, nz);
+    case 7: return run_gather<3, true>(ctx, pat, Kp, npairs, nz);
+  }
+  return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
+}
+
 int matrix_finalize(llf_ctx *ctx, llf_matrix *m) {
   llf_pattern *pat = m->pat;
   const int64_t n = pat->ndof;

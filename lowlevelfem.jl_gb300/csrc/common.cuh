@@ -168,6 +168,13 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
                   int ptype, const double *c1, const double *c2, int nmat,
                   int form, int lumped, llf_matrix *m);
 int matrix_finalize(llf_ctx *ctx, llf_matrix *m);  // dropzeros -> stored form
+// Element-ordered gather of node-pair blocks (blockval: pdim x pdim blocks;
+// otherwise one scalar per pair placed on the component diagonal).
+int gather_pairs(llf_ctx *ctx, llf_pattern *pat, const double *Kp, int npairs, bool blockval,
+                 double *nz);
+// field.cu: f[node*pdim+i] += fe[e][a][i] of every element of the node, in element order.
+int node_gather(llf_ctx *ctx, const int32_t *conn, int64_t nel, int npe, int64_t non, int pdim,
+                const double *fe, double *f);
 int matrix_axpby_impl(llf_ctx *ctx, double a, const llf_matrix *A, double b,
                       const llf_matrix *B, llf_matrix *C);
 

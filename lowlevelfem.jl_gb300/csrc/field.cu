@@ -186,6 +186,23 @@ int load_vector_impl(llf_ctx *ctx, llf_mesh *bm, int problem_dim, int pdim, cons
   return llf_check_status(ctx, "loadVector");
 }
 
+int node_gather(llf_ctx *ctx, const int32_t *conn, int64_t nel, int npe, int64_t non, int pdim,
+                const double *fe, double *f) {
+  int64_t *ptr = nullptr;
+  int2 *list = nullptr;
+  int mx = 0;
+  int rc = build_n2e(ctx, conn, nullptr, nel, npe, non, &ptr, &list, &mx);
+  if (rc != LLF_OK) return rc;
+  {
+    KernelScope ks(ctx, "k_node_gather");
+    k_load_gather<<<grid_1d(non, 128, ctx->num_sms), 128, 0, ctx->stream>>>(ptr, list, non, npe, pdim, fe, f);
+  }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  dfree(ctx, ptr);
+  dfree(ctx, list);
+  return LLF_OK;
+}
+
 int grad_elementwise_impl(llf_ctx *ctx, llf_mesh *m, const double *d_u, int add_identity,
                           double *d_out) {
   KernelScope ks(ctx, "k_grad_nodes");

@@ -764,3 +764,334 @@ int orc_grad_elementwise(const double *xyz, int64_t nel, int npe, const int32_t 
   free(X);
   return rc;
 }
+
+/* ======================================================================== */
+/* Total Lagrangian operators (src/nonlinear.jl:2083-2910).                  */
+/* ======================================================================== */
+/* Arithmetic contract (shared with the CUDA kernels):
+ *   F(q)  = fma-chain over element nodes a of N_a(q) * Fnode_a (per entry)
+ *   C     = F^T F, C_IJ = fma-chain over k of F_kI F_kJ
+ *   Cinv  = adj(C)/det(C) with the cofactor formulas of the geometry contract
+ *   lnJ   = 0.5 * ln(det C), ln by the atanh series below
+ *   neo-Hookean psi = mu/2 (I1-3) - mu lnJ + lambda/2 lnJ^2:
+ *     S_IJ = fma(lambda lnJ, Cinv_IJ, mu (delta_IJ - Cinv_IJ))
+ *     D_ab = fma(lambda, Cinv_IJ Cinv_KL, (mu - lambda lnJ) (Cinv_IK Cinv_JL + Cinv_IL Cinv_JK))
+ *   Saint Venant-Kirchhoff psi = lambda/2 tr(E)^2 + mu E:E, E = (C - I)/2:
+ *     S_IJ = fma(lambda, trE delta_IJ, 2 mu E_IJ)
+ *     D_ab = lambda delta_IJ delta_KL + mu (delta_IK delta_JL + delta_IL delta_JK)
+ *   Voigt order (11,22,33,23,13,12), a=(I,J), b=(K,L)
+ *   (ext/LowLevelFEMTensorsExt.jl:43-50, no shear factors in D).
+ * These are the derivatives S = 2 dpsi/dC and C = 4 d2psi/dC2 that the
+ * reference takes by automatic differentiation (ext/LowLevelFEMTensorsExt.jl:
+ * 19, :37); they are checked against finite differences of psi in the tests.
+ */
+#define ORC_LAW_CONST 0
+#define ORC_LAW_NEOHOOKE 1
+#define ORC_LAW_SVK 2
+
+/* Natural logarithm: x = m 2^e with m in [sqrt(1/2), sqrt(2)),
+ * ln x = e ln2 + 2 atanh(s), s = (m-1)/(m+1), atanh by its Taylor series
+ * s + s^3/3 + ... (|s| <= 0.1716, 12 terms). */
+double orc_ln(double x) {
+  int e;
+  double m = frexp(x, &e);
+  if (m < 0.70710678118654752440) {
+    m = m * 2.0;
+    e = e - 1;
+  }
+  double s = (m - 1.0) / (m + 1.0);
+  double s2 = s * s;
+  double p = 1.0 / 25.0;
+  for (int k = 11; k >= 0; --k) p = fma(p, s2, 1.0 / (2.0 * k + 1.0));
+  return fma((double)e, 0.69314718055994530942, 2.0 * (s * p));
+}
+
+static const int VI[6] = {0, 1, 2, 1, 0, 0};
+static const int VJ[6] = {0, 1, 2, 2, 2, 1};
+
+static void sym_inverse(const double C[3][3], double Ci[3][3], double *detC) {
+  double c00 = C[1][1] * C[2][2] - C[1][2] * C[2][1];
+  double c01 = -(C[1][0] * C[2][2] - C[1][2] * C[2][0]);
+  double c02 = C[1][0] * C[2][1] - C[1][1] * C[2][0];
+  double c10 = -(C[0][1] * C[2][2] - C[0][2] * C[2][1]);
+  double c11 = C[0][0] * C[2][2] - C[0][2] * C[2][0];
+  double c12 = -(C[0][0] * C[2][1] - C[0][1] * C[2][0]);
+  double c20 = C[0][1] * C[1][2] - C[0][2] * C[1][1];
+  double c21 = -(C[0][0] * C[1][2] - C[0][2] * C[1][0]);
+  double c22 = C[0][0] * C[1][1] - C[0][1] * C[1][0];
+  double det = (C[0][0] * c00 + C[0][1] * c01) + C[0][2] * c02;
+  double r = 1.0 / det;
+  Ci[0][0] = c00 * r; Ci[0][1] = c10 * r; Ci[0][2] = c20 * r;
+  Ci[1][0] = c01 * r; Ci[1][1] = c11 * r; Ci[1][2] = c21 * r;
+  Ci[2][0] = c02 * r; Ci[2][1] = c12 * r; Ci[2][2] = c22 * r;
+  *detC = det;
+}
+
+/* PK2 stress S and Voigt tangent D (6x6 row-major) from C; returns -1 if
+ * det C <= 0. */
+int orc_law(int law, const double *prm, const double C[3][3], double S[3][3], double *D) {
+  if (law == ORC_LAW_CONST) {
+    for (int a = 0; a < 6; ++a)
+      for (int b = 0; b < 6; ++b) D[a * 6 + b] = prm[b * 6 + a]; /* params column-major */
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) S[i][j] = 0.0;
+    return 0;
+  }
+  double mu = prm[0], lam = prm[1];
+  if (law == ORC_LAW_SVK) {
+    double E[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) E[i][j] = 0.5 * (C[i][j] - (i == j ? 1.0 : 0.0));
+    double trE = (E[0][0] + E[1][1]) + E[2][2];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) S[i][j] = fma(lam, i == j ? trE : 0.0, (2.0 * mu) * E[i][j]);
+    for (int a = 0; a < 6; ++a)
+      for (int b = 0; b < 6; ++b) {
+        int I = VI[a], J = VJ[a], K = VI[b], L = VJ[b];
+        double v = lam * ((I == J && K == L) ? 1.0 : 0.0);
+        v = v + mu * ((double)((I == K && J == L) ? 1 : 0) + (double)((I == L && J == K) ? 1 : 0));
+        D[a * 6 + b] = v;
+      }
+    return 0;
+  }
+  double Ci[3][3], detC;
+  sym_inverse(C, Ci, &detC);
+  if (!(detC > 0.0)) return -1;
+  double lnJ = 0.5 * orc_ln(detC);
+  double t = lam * lnJ;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) S[i][j] = fma(t, Ci[i][j], mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]));
+  double m2 = mu - t;
+  for (int a = 0; a < 6; ++a)
+    for (int b = 0; b < 6; ++b) {
+      int I = VI[a], J = VJ[a], K = VI[b], L = VJ[b];
+      double sym = Ci[I][K] * Ci[J][L] + Ci[I][L] * Ci[J][K];
+      D[a * 6 + b] = fma(lam, Ci[I][J] * Ci[K][L], m2 * sym);
+    }
+  return 0;
+}
+
+/* 3x3 tensor at point q interpolated from the element's nodal values
+ * (column-major 3x3 per node, T[i][j] at 9a + 3j + i). */
+static void interp_tensor(int npe, const double *Nq, const double *Tn, double T[3][3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double acc = 0.0;
+      for (int a = 0; a < npe; ++a) acc = fma(Nq[a], Tn[9 * a + 3 * j + i], acc);
+      T[i][j] = acc;
+    }
+}
+
+static void right_cauchy_green(const double F[3][3], double C[3][3]) {
+  for (int I = 0; I < 3; ++I)
+    for (int J = 0; J < 3; ++J) {
+      double acc = 0.0;
+      for (int k = 0; k < 3; ++k) acc = fma(F[k][I], F[k][J], acc);
+      C[I][J] = acc;
+    }
+}
+
+/* B(F) of node a, 6x3: B[I][i] for Voigt row I and displacement component i
+ * (src/nonlinear.jl:2219-2242). */
+static void tl_B(const double F[3][3], const double g[3], double B[6][3]) {
+  for (int j = 0; j < 3; ++j) {
+    double v1 = F[j][0], v2 = F[j][1], v3 = F[j][2];
+    B[0][j] = v1 * g[0];
+    B[1][j] = v2 * g[1];
+    B[2][j] = v3 * g[2];
+    B[3][j] = v2 * g[2] + v3 * g[1];
+    B[4][j] = v1 * g[2] + v3 * g[0];
+    B[5][j] = v1 * g[1] + v2 * g[0];
+  }
+}
+
+/* Element matrices of the TL operators.  mode 0: material tangent
+ * (Felem, law); mode 1: initial stress from nodal S (Telem = S, law ignored);
+ * mode 2: initial stress from nodal C with law.  Ke row-major (3 npe)^2. */
+static int tl_element(int mode, int npe, int nip, const double *w, const double *N,
+                      const double *dN, const double *X, const double *Tn, int law,
+                      const double *prm, double *Ke) {
+  size_t nd = 3 * (size_t)npe;
+  double *g = (double *)malloc(sizeof(double) * npe * 3);
+  double *Bs = (double *)malloc(sizeof(double) * npe * 18);
+  double *Ts = (double *)malloc(sizeof(double) * npe * 18);
+  double *acc = (double *)calloc((size_t)npe * npe * 9, sizeof(double)); /* pair (a,b): 9 */
+  int rc = 0;
+  for (int q = 0; q < nip && !rc; ++q) {
+    double invJ[9];
+    double det = orc_geom(3, npe, X, dN + (size_t)q * npe * 3, invJ);
+    if (!(det > 0.0)) { rc = -1; break; }
+    double wq = det * w[q];
+    const double *Nq = N + (size_t)q * npe;
+    for (int a = 0; a < npe; ++a) {
+      const double *d = dN + ((size_t)q * npe + a) * 3;
+      for (int i = 0; i < 3; ++i) {
+        double s = 0.0;
+        for (int j = 0; j < 3; ++j) s = fma(invJ[3 * j + i], d[j], s);
+        g[3 * a + i] = s;
+      }
+    }
+    if (mode == 0) {
+      double F[3][3], C[3][3], S[3][3], D[36];
+      interp_tensor(npe, Nq, Tn, F);
+      right_cauchy_green(F, C);
+      if (orc_law(law, prm, C, S, D)) { rc = -2; break; }
+      for (int b = 0; b < npe; ++b) {
+        double B[6][3];
+        tl_B(F, g + 3 * b, B);
+        for (int I = 0; I < 6; ++I)
+          for (int j = 0; j < 3; ++j) Bs[b * 18 + I * 3 + j] = B[I][j];
+        for (int I = 0; I < 6; ++I)
+          for (int j = 0; j < 3; ++j) {
+            double s = 0.0;
+            for (int J = 0; J < 6; ++J) s = fma(D[I * 6 + J], B[J][j], s);
+            Ts[b * 18 + I * 3 + j] = s * wq;
+          }
+      }
+      for (int a = 0; a < npe; ++a)
+        for (int b = a; b < npe; ++b) {
+          double *A = acc + ((size_t)a * npe + b) * 9;
+          for (int i = 0; i < 3; ++i)
+            for (int j = (a == b ? i : 0); j < 3; ++j) {
+              double s = A[i * 3 + j];
+              for (int I = 0; I < 6; ++I) s = fma(Bs[a * 18 + I * 3 + i], Ts[b * 18 + I * 3 + j], s);
+              A[i * 3 + j] = s;
+            }
+        }
+    } else {
+      double S[3][3];
+      if (mode == 1) {
+        interp_tensor(npe, Nq, Tn, S);
+      } else {
+        double C[3][3], D[36];
+        interp_tensor(npe, Nq, Tn, C);
+        if (orc_law(law, prm, C, S, D)) { rc = -2; break; }
+      }
+      for (int a = 0; a < npe; ++a)
+        for (int b = a; b < npe; ++b) {
+          const double *ga = g + 3 * a, *gb = g + 3 * b;
+          double t[3];
+          for (int I = 0; I < 3; ++I) {
+            double s = 0.0;
+            for (int J = 0; J < 3; ++J) s = fma(S[I][J], gb[J], s);
+            t[I] = s;
+          }
+          double v = 0.0;
+          for (int I = 0; I < 3; ++I) v = fma(ga[I], t[I], v);
+          double *A = acc + ((size_t)a * npe + b) * 9;
+          A[0] = fma(v, wq, A[0]);
+        }
+    }
+  }
+  if (!rc) {
+    memset(Ke, 0, sizeof(double) * nd * nd);
+    for (int a = 0; a < npe; ++a)
+      for (int b = a; b < npe; ++b) {
+        const double *A = acc + ((size_t)a * npe + b) * 9;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            double v;
+            if (mode == 0)
+              v = (a == b && j < i) ? A[j * 3 + i] : A[i * 3 + j];
+            else
+              v = (i == j) ? A[0] : 0.0;
+            Ke[((size_t)a * 3 + i) * nd + (size_t)b * 3 + j] = v;
+            Ke[((size_t)b * 3 + j) * nd + (size_t)a * 3 + i] = v;
+          }
+      }
+  }
+  free(g); free(Bs); free(Ts); free(acc);
+  return rc;
+}
+
+/* Global TL matrix in the reference's order: element triplets (row a, col b,
+ * Ke[a,b], src/nonlinear.jl:2249-2256), sparse, dropzeros!. */
+orc_csc *orc_tl_matrix(int mode, int64_t non, const double *xyz, int64_t nel, int npe,
+                       const int32_t *conn, int nip, const double *w, const double *N,
+                       const double *dN, const double *Telem, int law, const double *prm,
+                       int *err) {
+  size_t nd = 3 * (size_t)npe;
+  double *Ke = (double *)malloc(sizeof(double) * nd * nd);
+  double *X = (double *)malloc(sizeof(double) * npe * 3);
+  coo c = {0};
+  c.n = non * 3;
+  *err = 0;
+  for (int64_t e = 0; e < nel; ++e) {
+    for (int a = 0; a < npe; ++a)
+      for (int i = 0; i < 3; ++i) X[3 * a + i] = xyz[3 * (int64_t)conn[e * npe + a] + i];
+    int rc = tl_element(mode, npe, nip, w, N, dN, X, Telem + (size_t)e * 9 * npe, law, prm, Ke);
+    if (rc) {
+      *err = rc;
+      free(Ke); free(X); free(c.I); free(c.J); free(c.V);
+      return NULL;
+    }
+    for (size_t k = 0; k < nd; ++k)
+      for (size_t l = 0; l < nd; ++l)
+        coo_push(&c, (int64_t)conn[e * npe + k / 3] * 3 + (int64_t)(k % 3),
+                 (int64_t)conn[e * npe + l / 3] * 3 + (int64_t)(l % 3), Ke[k * nd + l]);
+  }
+  orc_csc *m = coo_to_csc(&c);
+  free(c.I); free(c.J); free(c.V); free(Ke); free(X);
+  orc_dropzeros(m);
+  return m;
+}
+
+/* Internal force (src/nonlinear.jl:2738-2910): per point P = F S (energy)
+ * or P interpolated; fe[a,i] = fma(P_iJ g_aJ chain, w, fe); element vectors
+ * added into f in element order. mode 0: Telem = F with law; 1: Telem = P. */
+int orc_tl_internal_force(int mode, int64_t non, const double *xyz, int64_t nel, int npe,
+                          const int32_t *conn, int nip, const double *w, const double *N,
+                          const double *dN, const double *Telem, int law, const double *prm,
+                          double *f) {
+  double *X = (double *)malloc(sizeof(double) * npe * 3);
+  double *fe = (double *)malloc(sizeof(double) * npe * 3);
+  int rc = 0;
+  for (int64_t i = 0; i < 3 * non; ++i) f[i] = 0.0;
+  for (int64_t e = 0; e < nel && !rc; ++e) {
+    for (int a = 0; a < npe; ++a)
+      for (int i = 0; i < 3; ++i) X[3 * a + i] = xyz[3 * (int64_t)conn[e * npe + a] + i];
+    for (int k = 0; k < 3 * npe; ++k) fe[k] = 0.0;
+    const double *Tn = Telem + (size_t)e * 9 * npe;
+    for (int q = 0; q < nip; ++q) {
+      double invJ[9];
+      double det = orc_geom(3, npe, X, dN + (size_t)q * npe * 3, invJ);
+      if (!(det > 0.0)) { rc = -1; break; }
+      double wq = det * w[q];
+      const double *Nq = N + (size_t)q * npe;
+      double P[3][3];
+      if (mode == 1) {
+        interp_tensor(npe, Nq, Tn, P);
+      } else {
+        double F[3][3], C[3][3], S[3][3], D[36];
+        interp_tensor(npe, Nq, Tn, F);
+        right_cauchy_green(F, C);
+        if (orc_law(law, prm, C, S, D)) { rc = -2; break; }
+        for (int i = 0; i < 3; ++i)
+          for (int J = 0; J < 3; ++J) {
+            double s = 0.0;
+            for (int K = 0; K < 3; ++K) s = fma(F[i][K], S[K][J], s);
+            P[i][J] = s;
+          }
+      }
+      for (int a = 0; a < npe; ++a) {
+        const double *d = dN + ((size_t)q * npe + a) * 3;
+        double g[3];
+        for (int i = 0; i < 3; ++i) {
+          double s = 0.0;
+          for (int j = 0; j < 3; ++j) s = fma(invJ[3 * j + i], d[j], s);
+          g[i] = s;
+        }
+        for (int i = 0; i < 3; ++i) {
+          double v = 0.0;
+          for (int J = 0; J < 3; ++J) v = fma(P[i][J], g[J], v);
+          fe[3 * a + i] = fma(v, wq, fe[3 * a + i]);
+        }
+      }
+    }
+    if (rc) break;
+    for (int a = 0; a < npe; ++a)
+      for (int i = 0; i < 3; ++i) f[3 * (int64_t)conn[e * npe + a] + i] += fe[3 * a + i];
+  }
+  free(X); free(fe);
+  return rc;
+}

@@ -69,6 +69,14 @@ def lib():
         L.orc_num_threads.restype = i32
         L.orc_grad_elementwise.restype = i32
         L.orc_grad_elementwise.argtypes = [Pd, i64, i32, Pi32, Pd, Pd, i32, Pd]
+        L.orc_tl_matrix.restype = vp
+        L.orc_tl_matrix.argtypes = [i32, i64, Pd, i64, i32, Pi32, i32, Pd, Pd, Pd, Pd, i32, Pd, C.POINTER(i32)]
+        L.orc_tl_internal_force.restype = i32
+        L.orc_tl_internal_force.argtypes = [i32, i64, Pd, i64, i32, Pi32, i32, Pd, Pd, Pd, Pd, i32, Pd, Pd]
+        L.orc_law.restype = i32
+        L.orc_law.argtypes = [i32, Pd, Pd, Pd, Pd]
+        L.orc_ln.restype = dbl
+        L.orc_ln.argtypes = [dbl]
         _lib = L
     return _lib
 
@@ -226,6 +234,66 @@ def grad_elementwise(xyz, conn, rule, u, add_identity=False):
     if rc:
         raise ValueError("oracle: non-positive Jacobian determinant")
     return out
+
+
+LAW_CONST, LAW_NEOHOOKE, LAW_SVK = 0, 1, 2
+TL_KMAT, TL_KGEO_S, TL_KGEO_C = 0, 1, 2
+
+
+def _prm(params):
+    p = np.zeros(36)
+    v = np.asarray(params, dtype=np.float64).ravel()
+    p[: len(v)] = v
+    return p
+
+
+def tl_matrix(mode, xyz, conn, rule, Telem, law=LAW_NEOHOOKE, params=(1.0, 10.0)):
+    """Total Lagrangian material (mode 0) or initial-stress (1: nodal S, 2:
+    nodal C with law) stiffness in the reference's triplet order."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    conn0 = _conn0(conn)
+    T = np.ascontiguousarray(Telem, dtype=np.float64)
+    prm = _prm(params)
+    w = np.ascontiguousarray(rule["w"]); N = np.ascontiguousarray(rule["N"]); dN = np.ascontiguousarray(rule["dN"])
+    err = C.c_int(0)
+    h = lib().orc_tl_matrix(mode, xyz.shape[0], _p(xyz, C.c_double), conn0.shape[0], conn0.shape[1],
+                            _p(conn0, C.c_int32), len(w), _p(w, C.c_double), _p(N, C.c_double), _p(dN, C.c_double),
+                            _p(T, C.c_double), law, _p(prm, C.c_double), C.byref(err))
+    if not h:
+        raise ValueError(f"oracle TL: error {err.value}")
+    return CSC(h)
+
+
+def tl_internal_force(mode, xyz, conn, rule, Telem, law=LAW_NEOHOOKE, params=(1.0, 10.0)):
+    """mode 0: Telem = F with law; mode 1: Telem = P."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    conn0 = _conn0(conn)
+    T = np.ascontiguousarray(Telem, dtype=np.float64)
+    prm = _prm(params)
+    w = np.ascontiguousarray(rule["w"]); N = np.ascontiguousarray(rule["N"]); dN = np.ascontiguousarray(rule["dN"])
+    f = np.zeros(3 * xyz.shape[0])
+    rc = lib().orc_tl_internal_force(mode, xyz.shape[0], _p(xyz, C.c_double), conn0.shape[0], conn0.shape[1],
+                                     _p(conn0, C.c_int32), len(w), _p(w, C.c_double), _p(N, C.c_double),
+                                     _p(dN, C.c_double), _p(T, C.c_double), law, _p(prm, C.c_double),
+                                     _p(f, C.c_double))
+    if rc:
+        raise ValueError(f"oracle TL force: error {rc}")
+    return f
+
+
+def law(law_id, params, Cmat):
+    """(S, D) of a law at the right Cauchy-Green tensor Cmat."""
+    Cm = np.ascontiguousarray(Cmat, dtype=np.float64)
+    S = np.zeros((3, 3)); D = np.zeros((6, 6))
+    prm = _prm(params)
+    rc = lib().orc_law(law_id, _p(prm, C.c_double), _p(Cm, C.c_double), _p(S, C.c_double), _p(D, C.c_double))
+    if rc:
+        raise ValueError("det C <= 0")
+    return S, D
+
+
+def ln(x: float) -> float:
+    return lib().orc_ln(float(x))
 
 
 def num_threads() -> int:

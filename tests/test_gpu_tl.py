@@ -1,0 +1,112 @@
+"""GPU Total Lagrangian operators vs the oracle (bit-identical CSC / vectors)
+and the Newton-step properties of the hyperelastic configuration."""
+import numpy as np
+import pytest
+
+from helpers import assert_csc_identical
+
+pytestmark = pytest.mark.gpu
+
+CASES = [("hex8", 2, 1, False), ("hex27", 2, 2, False), ("tet10", 1, 2, True), ("hex64", 1, 3, False)]
+
+
+def _F(llf, m, p, scale, seed):
+    rng = np.random.default_rng(seed)
+    u = llf.VectorField(scale * rng.standard_normal((3 * m.non, 1)), p)
+    return llf.grad(u, add_identity=True), u
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+@pytest.mark.parametrize("law", ["NeoHookeCompressible", "StVenantKirchhoff"])
+def test_material_tangent_bit_identical(llf, orc, case, law):
+    _, n, order, simplex = case
+    m = llf.structured_box_mesh(n=n, order=order, simplex=simplex)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    F, _ = _F(llf, m, p, 0.03, 11)
+    params = {"mu": 1.0, "lambda": 10.0}
+    K = llf.materialTangentMatrix(p, F=F, energy=law, params=params)
+    rule = llf._lib.builtin_rule(m.family, m.order)
+    lid = orc.LAW_NEOHOOKE if law.startswith("Neo") else orc.LAW_SVK
+    ref = orc.tl_matrix(orc.TL_KMAT, m.xyz, m.conn, rule, F.A, lid, [1.0, 10.0])
+    assert_csc_identical(K.csc(), ref.julia(), f"Kmat {case[0]} {law}")
+
+
+def test_material_tangent_constant_C(llf, orc):
+    m = llf.structured_box_mesh(n=2, order=1)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    F, _ = _F(llf, m, p, 0.05, 3)
+    Cv = np.diag([3.0, 3.0, 3.0, 1.0, 1.0, 1.0]) + 0.5
+    K = llf.materialTangentMatrix(p, F=F, C=Cv)
+    ref = orc.tl_matrix(orc.TL_KMAT, m.xyz, m.conn, llf._lib.builtin_rule(m.family, m.order), F.A, orc.LAW_CONST,
+                        np.asarray(Cv).ravel(order="F"))
+    assert_csc_identical(K.csc(), ref.julia(), "Kmat constant C")
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_initial_stress_bit_identical(llf, orc, case):
+    _, n, order, simplex = case
+    m = llf.structured_box_mesh(n=n, order=order, simplex=simplex)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    F, _ = _F(llf, m, p, 0.03, 13)
+    rule = llf._lib.builtin_rule(m.family, m.order)
+    # C path (energy)
+    FA = F.A.reshape(m.nel, m.npe, 3, 3)          # [e, a, j, i] column-major -> F[i][j] = FA[..., j, i]
+    Fm = np.swapaxes(FA, -1, -2)
+    Cm = np.einsum("eaki,eakj->eaij", Fm, Fm)
+    Celem = np.swapaxes(Cm, -1, -2).reshape(m.nel, 9 * m.npe)
+    Kg = llf.initialStressMatrix(p, energy="NeoHookeCompressible", params={"mu": 1.0, "lambda": 10.0},
+                                 C=llf.TensorField(Celem, p))
+    ref = orc.tl_matrix(orc.TL_KGEO_C, m.xyz, m.conn, rule, Celem, orc.LAW_NEOHOOKE, [1.0, 10.0])
+    assert_csc_identical(Kg.csc(), ref.julia(), f"Kgeo(C) {case[0]}")
+    # S path (given stress field)
+    rng = np.random.default_rng(17)
+    Sn = rng.standard_normal((m.nel, m.npe, 3, 3))
+    Sn = Sn + np.swapaxes(Sn, -1, -2)
+    Selem = Sn.reshape(m.nel, 9 * m.npe)
+    Ks = llf.initialStressMatrix(p, S=llf.TensorField(Selem, p))
+    refs = orc.tl_matrix(orc.TL_KGEO_S, m.xyz, m.conn, rule, Selem)
+    assert_csc_identical(Ks.csc(), refs.julia(), f"Kgeo(S) {case[0]}")
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_internal_force_bit_identical(llf, orc, case):
+    _, n, order, simplex = case
+    m = llf.structured_box_mesh(n=n, order=order, simplex=simplex)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    F, _ = _F(llf, m, p, 0.03, 19)
+    rule = llf._lib.builtin_rule(m.family, m.order)
+    f = llf.internalForceVector(p, F=F, energy="NeoHookeCompressible", params={"mu": 1.0, "lambda": 10.0})
+    ref = orc.tl_internal_force(0, m.xyz, m.conn, rule, F.A, orc.LAW_NEOHOOKE, [1.0, 10.0])
+    assert np.array_equal(f.a[:, 0], ref)
+    P = llf.TensorField(np.random.default_rng(23).standard_normal((m.nel, 9 * m.npe)), p)
+    fp = llf.internalForceVector(p, P=P)
+    refp = orc.tl_internal_force(1, m.xyz, m.conn, rule, P.A)
+    assert np.array_equal(fp.a[:, 0], refp)
+
+
+def test_newton_step_consistency(llf):
+    """The tangent K_mat + K_geo is the derivative of f_int: a directional
+    finite difference of f_int matches K du (hex8, neo-Hookean)."""
+    m = llf.structured_box_mesh(n=3, order=1)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    prm = {"mu": 1.0, "lambda": 10.0}
+    rng = np.random.default_rng(29)
+    # affine fields: their nodal gradients interpolate exactly to the Gauss points,
+    # so f_int(u) and K_mat + K_geo describe the same discrete energy
+    u = (m.xyz @ (0.05 * rng.standard_normal((3, 3))).T).ravel()
+    du = (m.xyz @ rng.standard_normal((3, 3)).T).ravel()
+    h = 1e-6
+
+    def fint(v):
+        F = llf.grad(llf.VectorField(v.reshape(-1, 1), p), add_identity=True)
+        return llf.internalForceVector(p, F=F, energy="NeoHookeCompressible", params=prm).a[:, 0]
+
+    F = llf.grad(llf.VectorField(u.reshape(-1, 1), p), add_identity=True)
+    FA = np.swapaxes(F.A.reshape(m.nel, m.npe, 3, 3), -1, -2)
+    Cm = np.einsum("eaki,eakj->eaij", FA, FA)
+    C = llf.TensorField(np.swapaxes(Cm, -1, -2).reshape(m.nel, 9 * m.npe), p)
+    K = llf.materialTangentMatrix(p, F=F, energy="NeoHookeCompressible", params=prm) + \
+        llf.initialStressMatrix(p, energy="NeoHookeCompressible", params=prm, C=C)
+    fd = (fint(u + h * du) - fint(u - h * du)) / (2 * h)
+    Kdu = K * du
+    assert np.linalg.norm(fd - Kdu) <= 1e-6 * np.linalg.norm(Kdu)
