@@ -284,6 +284,13 @@ int llf_matrix_copy_csc(llf_ctx *ctx, const llf_matrix *m, int64_t *colptr,
 int llf_matrix_copy_structural(llf_ctx *ctx, const llf_matrix *m,
                                double *nzval);
 
+/* Device matrix from host structural values nzval[nnz of pat], in the
+ * pattern's CSC order; the stored form is then built with dropzeros!.  Lets
+ * a host-side SystemMatrix (e.g. after applyElasticSupport!) re-enter the
+ * device solve (SystemMatrix(A, model), src/general.jl:762-771). */
+int llf_matrix_from_structural(llf_ctx *ctx, llf_pattern *pat, const double *nzval,
+                               llf_matrix **out);
+
 /* C = a*A + b*B on the same pattern, then dropzeros! — SystemMatrix +/-
  * of src/operators.jl:2421-2486 (Kmat + Kgeo, K - Kext). */
 int llf_matrix_axpby(llf_ctx *ctx, double a, const llf_matrix *A, double b,

@@ -79,6 +79,7 @@ SIGNATURES = {
     "llf_matrix_copy_csc": (i32, [vp, vp, P_i64, P_i64, P_dbl]),
     "llf_matrix_copy_structural": (i32, [vp, vp, P_dbl]),
     "llf_matrix_axpby": (i32, [vp, dbl, vp, dbl, vp, PP]),
+    "llf_matrix_from_structural": (i32, [vp, vp, P_dbl, PP]),
     "llf_matrix_spmv": (i32, [vp, vp, P_dbl, P_dbl]),
     "llf_matrix_destroy": (i32, [vp, vp]),
     "llf_pcg": (i32, [vp, vp, P_dbl, P_dbl, P_u8, i32, dbl, i64, P_i64, P_dbl]),

@@ -655,6 +655,23 @@ int llf_matrix_copy_structural(llf_ctx *ctx, const llf_matrix *m, double *nzval)
   return llf_ok(ctx);
 }
 
+int llf_matrix_from_structural(llf_ctx *ctx, llf_pattern *pat, const double *nzval,
+                               llf_matrix **out) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!pat || !nzval || !out) return llf_fail(ctx, LLF_ERR_ARG, "llf_matrix_from_structural: null argument");
+  llf_matrix *m;
+  int rc;
+  if ((rc = new_matrix(ctx, pat, out, &m))) return rc;
+  cudaError_t e = dalloc(ctx, &m->d_nz, pat->nnz);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(m->d_nz, nzval, sizeof(double) * pat->nnz, cudaMemcpyHostToDevice, ctx->stream);
+  rc = (e == cudaSuccess) ? check_finite(ctx, m->d_nz, pat->nnz)
+                          : llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  if (rc == LLF_OK) rc = llf_check_status(ctx, "llf_matrix_from_structural");
+  if (rc == LLF_OK) rc = matrix_finalize(ctx, m, nullptr);
+  return finish_matrix(ctx, rc, m, out);
+}
+
 int llf_matrix_axpby(llf_ctx *ctx, double a, const llf_matrix *A, double b, const llf_matrix *B,
                      llf_matrix **out) {
   if (!ctx) return LLF_ERR_ARG;

@@ -1,21 +1,26 @@
 // Element-operator assembly into the reference's CSC layout.
 //
 // Pipeline (one call of llf_assemble_*):
-//   k_elem_fp64  one CTA per element at a time (grid-stride, persistent):
-//                element node coordinates gathered once into shared memory,
-//                the reference shape gradients staged in shared memory for
-//                the CTA's lifetime, Jacobian / inverse / physical gradients
-//                per integration point, then the upper-triangle node-pair
-//                blocks of the element matrix written to a pair buffer
-//                (elements x pairs x block);
-//   k_gather     one warp per column node: for every row node of the column
-//                the contributing elements are the intersection of the two
-//                nodes' element lists (both sorted), so every structural
-//                entry is summed over its elements in element order —
-//                the order SparseArrays.sparse combines the reference's
-//                triplets (src/linear.jl:314-323);
-//   finalize     dropzeros! (src/linear.jl:324): count, scan, compact into
-//                1-based Int64 SparseMatrixCSC arrays.
+//   k_elem_fp64   one CTA per element at a time (grid-stride, persistent):
+//                 element node coordinates gathered into shared memory, the
+//                 reference shape gradients staged in shared memory for the
+//                 CTA's lifetime (read from global memory for elements whose
+//                 tables do not fit), Jacobian / inverse / physical gradients
+//                 per integration point, then the upper-triangle node-pair
+//                 blocks of the element matrix, each written twice (block and
+//                 mirror) so the element matrix leaves the kernel whole in the
+//                 layout Kf[element][column node b][row node a][block];
+//   k_colgather   one warp per column node B: walks the elements around B in
+//                 ascending order; for each, the lanes read the element's
+//                 column b = local(B) — one contiguous run of npe blocks — and
+//                 add every block into a shared-memory accumulator of the
+//                 column (row position found by binary search in the column's
+//                 node list).  Each entry is thus summed over its elements in
+//                 element order, the order SparseArrays.sparse combines the
+//                 reference's triplets (src/linear.jl:314-323).  The column is
+//                 written out coalesced together with its non-zero count;
+//   finalize      dropzeros! (src/linear.jl:324): scan of the counts, then
+//                 compaction into 1-based Int64 SparseMatrixCSC arrays.
 // Every floating-point operation of the FP64 form is an explicit IEEE
 // intrinsic (__dmul_rn, __dadd_rn, __fma_rn, __drcp_rn), so no contraction
 // or reassociation can move the result away from the CPU oracle's.
@@ -33,8 +38,8 @@ struct ElemArgs {
   int npe, nip, npairs;
   const double *w, *N, *dN;  // device tables
   const double *c1, *c2;     // per-material coefficients
-  double *Kp;                // nel * npairs * BS
-  double *scratch;           // per-CTA global scratch (when not in smem)
+  double *Kf;                // nel * npe * npe * BS (full element matrices)
+  double *scratch;           // per-CTA global scratch for G, S (large elements)
   int64_t scratch_stride;    // doubles per CTA
   unsigned *status;
 };
@@ -52,85 +57,107 @@ __device__ __forceinline__ void pair_decode(int pi, int npe, int &a, int &b) {
   b = a + (pi - pair_offset(a, npe));
 }
 
-// Geometry at point q (contract of the oracle): returns det, fills inv
-// (row-major invJ[i][j]).
-template <int DIM>
-__device__ __forceinline__ double geom_point(const double *sX, const double *sdNq,
-                                             int npe, double *inv) {
-  double J[DIM][DIM];
+// Geometry at one point (contract of the oracle): returns det, fills inv
+// (row-major invJ[i][j]).  dNq(a, j) is the reference gradient of node a.
+template <int DIM, class Tab>
+__device__ __forceinline__ double geom_point(const double *sX, Tab dNq, int npe, double *inv) {
+  double J[3][3];
 #pragma unroll
   for (int i = 0; i < DIM; ++i)
 #pragma unroll
     for (int j = 0; j < DIM; ++j) {
       double acc = 0.0;
-      for (int a = 0; a < npe; ++a) acc = __fma_rn(sX[a * DIM + i], sdNq[a * DIM + j], acc);
+      for (int a = 0; a < npe; ++a) acc = __fma_rn(sX[a * DIM + i], dNq(a, j), acc);
       J[i][j] = acc;
     }
   double det, rdet;
   if (DIM == 3) {
-#define M(x, y) J[(x) % DIM][(y) % DIM]
-    double c00 = __dsub_rn(__dmul_rn(M(1, 1), M(2, 2)), __dmul_rn(M(1, 2), M(2, 1)));
-    double c01 = -__dsub_rn(__dmul_rn(M(1, 0), M(2, 2)), __dmul_rn(M(1, 2), M(2, 0)));
-    double c02 = __dsub_rn(__dmul_rn(M(1, 0), M(2, 1)), __dmul_rn(M(1, 1), M(2, 0)));
-    double c10 = -__dsub_rn(__dmul_rn(M(0, 1), M(2, 2)), __dmul_rn(M(0, 2), M(2, 1)));
-    double c11 = __dsub_rn(__dmul_rn(M(0, 0), M(2, 2)), __dmul_rn(M(0, 2), M(2, 0)));
-    double c12 = -__dsub_rn(__dmul_rn(M(0, 0), M(2, 1)), __dmul_rn(M(0, 1), M(2, 0)));
-    double c20 = __dsub_rn(__dmul_rn(M(0, 1), M(1, 2)), __dmul_rn(M(0, 2), M(1, 1)));
-    double c21 = -__dsub_rn(__dmul_rn(M(0, 0), M(1, 2)), __dmul_rn(M(0, 2), M(1, 0)));
-    double c22 = __dsub_rn(__dmul_rn(M(0, 0), M(1, 1)), __dmul_rn(M(0, 1), M(1, 0)));
-#undef M
-    det = __dadd_rn(__dadd_rn(__dmul_rn(J[0][0], c00), __dmul_rn(J[0][1 % DIM], c01)),
-                    __dmul_rn(J[0][2 % DIM], c02));
+    double c00 = __dsub_rn(__dmul_rn(J[1][1], J[2][2]), __dmul_rn(J[1][2], J[2][1]));
+    double c01 = -__dsub_rn(__dmul_rn(J[1][0], J[2][2]), __dmul_rn(J[1][2], J[2][0]));
+    double c02 = __dsub_rn(__dmul_rn(J[1][0], J[2][1]), __dmul_rn(J[1][1], J[2][0]));
+    double c10 = -__dsub_rn(__dmul_rn(J[0][1], J[2][2]), __dmul_rn(J[0][2], J[2][1]));
+    double c11 = __dsub_rn(__dmul_rn(J[0][0], J[2][2]), __dmul_rn(J[0][2], J[2][0]));
+    double c12 = -__dsub_rn(__dmul_rn(J[0][0], J[2][1]), __dmul_rn(J[0][1], J[2][0]));
+    double c20 = __dsub_rn(__dmul_rn(J[0][1], J[1][2]), __dmul_rn(J[0][2], J[1][1]));
+    double c21 = -__dsub_rn(__dmul_rn(J[0][0], J[1][2]), __dmul_rn(J[0][2], J[1][0]));
+    double c22 = __dsub_rn(__dmul_rn(J[0][0], J[1][1]), __dmul_rn(J[0][1], J[1][0]));
+    det = __dadd_rn(__dadd_rn(__dmul_rn(J[0][0], c00), __dmul_rn(J[0][1], c01)),
+                    __dmul_rn(J[0][2], c02));
     rdet = __drcp_rn(det);
     inv[0] = __dmul_rn(c00, rdet); inv[1] = __dmul_rn(c10, rdet); inv[2] = __dmul_rn(c20, rdet);
     inv[3] = __dmul_rn(c01, rdet); inv[4] = __dmul_rn(c11, rdet); inv[5] = __dmul_rn(c21, rdet);
     inv[6] = __dmul_rn(c02, rdet); inv[7] = __dmul_rn(c12, rdet); inv[8] = __dmul_rn(c22, rdet);
   } else {
-    det = __dsub_rn(__dmul_rn(J[0][0], J[1 % DIM][1 % DIM]),
-                    __dmul_rn(J[0][1 % DIM], J[1 % DIM][0]));
+    det = __dsub_rn(__dmul_rn(J[0][0], J[1][1]), __dmul_rn(J[0][1], J[1][0]));
     rdet = __drcp_rn(det);
-    inv[0] = __dmul_rn(J[1 % DIM][1 % DIM], rdet);
-    inv[1] = __dmul_rn(-J[0][1 % DIM], rdet);
+    inv[0] = __dmul_rn(J[1][1], rdet);
+    inv[1] = __dmul_rn(-J[0][1], rdet);
     inv[2] = 0.0;
-    inv[3] = __dmul_rn(-J[1 % DIM][0], rdet);
+    inv[3] = __dmul_rn(-J[1][0], rdet);
     inv[4] = __dmul_rn(J[0][0], rdet);
     inv[5] = 0.0; inv[6] = 0.0; inv[7] = 0.0; inv[8] = 0.0;
   }
   return det;
 }
 
+// Store block (a,b) (a <= b) of the element matrix and its mirror (b,a) in
+// the column-major-by-node layout Kf[e][col node][row node][i*P+j].
+template <int P, int BS>
+__device__ __forceinline__ void store_pair(double *Ke, int npe, int a, int b, const double *blk) {
+  double *ab = Ke + ((size_t)b * npe + a) * BS;  // rows of node a, columns of node b
+#pragma unroll
+  for (int k = 0; k < BS; ++k) ab[k] = blk[k];
+  if (a != b) {
+    double *ba = Ke + ((size_t)a * npe + b) * BS;
+    if (BS == 1) {
+      ba[0] = blk[0];
+    } else {
+#pragma unroll
+      for (int i = 0; i < P; ++i)
+#pragma unroll
+        for (int j = 0; j < P; ++j) ba[j * P + i] = blk[i * P + j];
+    }
+  }
+}
+
 // Shared-memory layout of k_elem_fp64 (doubles):
-//   sdN [nip*npe*DIM] | sw [nip] | sN [nip*npe] (mass) | sX [npe*DIM] |
-//   sWd [nip] | sInv [nip*9] | then G and S (each nip*npe*DIM) when GS_SMEM.
-template <int KIND, int DIM, bool GS_SMEM>
+//   [SMEM] sdN [nip*npe*DIM] | sw [nip] | sN [nip*npe] (mass) |
+//   sX [npe*DIM] | sWd [nip] | sInv [nip*9] | [SMEM] G, S (each nip*npe*gsw)
+// Without SMEM the tables are read from global memory (stride 3) and G, S
+// live in a per-CTA global scratch slot (L2 resident).
+template <int KIND, int DIM, bool SMEM>
 __global__ void __launch_bounds__(ELEM_THREADS)
 k_elem_fp64(ElemArgs A) {
   extern __shared__ double smem[];
   const int npe = A.npe, nip = A.nip;
+  constexpr int gsw = (KIND == KIND_MASS) ? 1 : DIM;
   double *sdN = smem;
-  double *sw = sdN + (size_t)nip * npe * DIM;
-  double *sN = sw + nip;
-  double *sX = sN + (KIND == KIND_MASS ? (size_t)nip * npe : 0);
+  double *sw = sdN + (SMEM ? (size_t)nip * npe * DIM : 0);
+  double *sN = sw + (SMEM ? nip : 0);
+  double *sX = sN + ((SMEM && KIND == KIND_MASS) ? (size_t)nip * npe : 0);
   double *sWd = sX + (size_t)npe * DIM;
   double *sInv = sWd + nip;
-  double *G, *S;
-  if (GS_SMEM) {
-    G = sInv + (size_t)nip * 9;
-  } else {
-    G = A.scratch + (size_t)blockIdx.x * A.scratch_stride;
-  }
-  S = G + (size_t)nip * npe * (KIND == KIND_MASS ? 1 : DIM);
+  double *G = SMEM ? (sInv + (size_t)nip * 9) : (A.scratch + (size_t)blockIdx.x * A.scratch_stride);
+  double *S = G + (size_t)nip * npe * gsw;
+  // table accessors
+  const int tstride = SMEM ? DIM : 3;
+  const double *tdN = SMEM ? sdN : A.dN;
+  const double *tw = SMEM ? sw : A.w;
+  const double *tN = SMEM ? sN : A.N;
 
-  for (int t = threadIdx.x; t < nip * npe * DIM; t += blockDim.x) {
-    int j = t % DIM, qa = t / DIM;
-    sdN[t] = A.dN[(size_t)qa * 3 + j];
+  if (SMEM) {
+    for (int t = threadIdx.x; t < nip * npe * DIM; t += blockDim.x) {
+      int j = t % DIM, qa = t / DIM;
+      sdN[t] = A.dN[(size_t)qa * 3 + j];
+    }
+    for (int t = threadIdx.x; t < nip; t += blockDim.x) sw[t] = A.w[t];
+    if (KIND == KIND_MASS)
+      for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) sN[t] = A.N[t];
+    __syncthreads();
   }
-  for (int t = threadIdx.x; t < nip; t += blockDim.x) sw[t] = A.w[t];
-  if (KIND == KIND_MASS)
-    for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) sN[t] = A.N[t];
-  __syncthreads();
 
-  const int BS = (KIND == KIND_ELASTIC) ? DIM * DIM : 1;
+  constexpr int BS = (KIND == KIND_ELASTIC) ? DIM * DIM : 1;
+  constexpr int P = (KIND == KIND_ELASTIC) ? DIM : 1;
   for (int64_t e = blockIdx.x; e < A.nel; e += gridDim.x) {
     const int mat = A.emat ? A.emat[e] : 0;
     if (mat < 0) continue;  // uniform across the CTA
@@ -143,24 +170,22 @@ k_elem_fp64(ElemArgs A) {
     __syncthreads();
     for (int q = threadIdx.x; q < nip; q += blockDim.x) {
       double inv[9];
-      double det = geom_point<DIM>(sX, sdN + (size_t)q * npe * DIM, npe, inv);
+      const double *dq = tdN + (size_t)q * npe * tstride;
+      double det = geom_point<DIM>(sX, [&](int a, int j) { return dq[a * tstride + j]; }, npe, inv);
       if (!(det > 0.0)) atomicOr(A.status, ST_BAD_JACOBIAN);
-      sWd[q] = __dmul_rn(det, sw[q]);
+      sWd[q] = __dmul_rn(det, tw[q]);
 #pragma unroll
       for (int k = 0; k < 9; ++k) sInv[q * 9 + k] = inv[k];
     }
     __syncthreads();
     if (KIND == KIND_MASS) {
-      for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) {
-        int q = t / npe;
-        S[t] = __dmul_rn(sWd[q], sN[t]);
-      }
+      for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) S[t] = __dmul_rn(sWd[t / npe], tN[t]);
     } else {
       for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) {
-        int q = t / npe;
+        const int q = t / npe;
         const double *inv = sInv + q * 9;
-        const double *d = sdN + (size_t)t * DIM;
-        double wd = sWd[q];
+        const double *d = tdN + (size_t)t * tstride;
+        const double wd = sWd[q];
 #pragma unroll
         for (int i = 0; i < DIM; ++i) {
           double acc = 0.0;
@@ -173,10 +198,11 @@ k_elem_fp64(ElemArgs A) {
     }
     __syncthreads();
 
-    double *out = A.Kp + (size_t)e * A.npairs * BS;
+    double *Ke = A.Kf + (size_t)e * npe * npe * BS;
     for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
       int a, b;
       pair_decode(pi, npe, a, b);
+      double blk[BS];
       if (KIND == KIND_ELASTIC) {
         double O[DIM][DIM];
 #pragma unroll
@@ -214,14 +240,13 @@ k_elem_fp64(ElemArgs A) {
         }
         double tr = __dadd_rn(O[0][0], O[1 % DIM][1 % DIM]);
         if (DIM == 3) tr = __dadd_rn(tr, O[2 % DIM][2 % DIM]);
-        double *o = out + (size_t)pi * BS;
 #pragma unroll
         for (int i = 0; i < DIM; ++i)
 #pragma unroll
           for (int j = 0; j < DIM; ++j) {
             double t = __fma_rn(c2, O[j][i], __dmul_rn(c1, O[i][j]));
             if (i == j) t = __fma_rn(c2, tr, t);
-            o[i * DIM + j] = t;
+            blk[i * DIM + j] = t;
           }
       } else if (KIND == KIND_HEAT) {
         double acc = 0.0;
@@ -231,97 +256,80 @@ k_elem_fp64(ElemArgs A) {
 #pragma unroll
           for (int i = 0; i < DIM; ++i) acc = __fma_rn(sa[i], gb[i], acc);
         }
-        out[pi] = __dmul_rn(c1, acc);
+        blk[0] = __dmul_rn(c1, acc);
       } else {  // mass
         double acc = 0.0;
         for (int q = 0; q < nip; ++q)
-          acc = __fma_rn(S[(size_t)q * npe + a], sN[(size_t)q * npe + b], acc);
-        out[pi] = __dmul_rn(c1, acc);
+          acc = __fma_rn(S[(size_t)q * npe + a], tN[(size_t)q * npe + b], acc);
+        blk[0] = __dmul_rn(c1, acc);
       }
+      store_pair<P, BS>(Ke, npe, a, b, blk);
     }
     __syncthreads();
   }
 }
 
-// One warp per column node B; lanes over the rows (node A) of the column.
-// Sums, for every entry, the contributions of the elements containing both
-// A and B in ascending element order, starting from the first contribution.
-template <int P, bool BLOCKVAL>
-__global__ void k_gather(const int64_t *__restrict__ nptr,
-                         const int32_t *__restrict__ nadj,
-                         const int64_t *__restrict__ n2e_ptr,
-                         const int2 *__restrict__ n2e,
-                         const double *__restrict__ Kp, int npe, int npairs,
-                         int64_t non, int max_n2e, double *__restrict__ nz,
-                         unsigned *status) {
-  extern __shared__ int2 sB[];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int wpb = blockDim.x >> 5;
-  int2 *mine = sB + (size_t)wib * max_n2e;
+// Column-node gather.  T = double (FP64 form) or float (precision form);
+// FP64 sums in element order in both.  Per warp: the column's row-node list
+// (deg ints) and its accumulator (deg * P * P doubles) in shared memory.
+template <int P, bool BLOCKVAL, class T>
+__global__ void k_colgather(const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
+                            const int64_t *__restrict__ n2e_ptr, const int2 *__restrict__ n2e,
+                            const int32_t *__restrict__ conn, const T *__restrict__ Kf, int npe,
+                            int64_t non, int max_deg, double *__restrict__ nz,
+                            int64_t *__restrict__ cnt, unsigned *status) {
+  extern __shared__ double cg_smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   constexpr int BS = BLOCKVAL ? P * P : 1;
+  double *acc = cg_smem + (size_t)wib * max_deg * P * P;
+  int32_t *rows = (int32_t *)(cg_smem + (size_t)wpb * max_deg * P * P) + (size_t)wib * max_deg;
   for (int64_t B = (int64_t)blockIdx.x * wpb + wib; B < non; B += (int64_t)gridDim.x * wpb) {
-    const int64_t s = n2e_ptr[B];
-    const int nb = (int)(n2e_ptr[B + 1] - s);
-    for (int k = lane; k < nb; k += 32) mine[k] = n2e[s + k];
-    __syncwarp();
     const int64_t c0 = nptr[B];
     const int deg = (int)(nptr[B + 1] - c0);
-    for (int t = lane; t < deg; t += 32) {
-      const int A = nadj[c0 + t];
-      int64_t ia = n2e_ptr[A];
-      const int64_t ea = n2e_ptr[A + 1];
-      int ib = 0;
-      double acc[P][P];
-      bool first = true;
-#pragma unroll
-      for (int i = 0; i < P; ++i)
-#pragma unroll
-        for (int j = 0; j < P; ++j) acc[i][j] = 0.0;
-      int2 xa = ia < ea ? n2e[ia] : make_int2(INT32_MAX, 0);
-      while (ia < ea && ib < nb) {
-        const int2 xb = mine[ib];
-        if (xa.x < xb.x) {
-          ++ia;
-          if (ia < ea) xa = n2e[ia];
-        } else if (xa.x > xb.x) {
-          ++ib;
-        } else {
-          const int e = xa.x, la = xa.y, lb = xb.y;
-          double v[P][P];
-          if (BLOCKVAL) {
-            const bool tr = la > lb;
-            const int lo = tr ? lb : la, hi = tr ? la : lb;
-            const double *blk = Kp + ((size_t)e * npairs + (size_t)(lo * npe - (lo * (lo - 1)) / 2 + (hi - lo))) * BS;
-#pragma unroll
-            for (int i = 0; i < P; ++i)
-#pragma unroll
-              for (int j = 0; j < P; ++j) v[i][j] = tr ? blk[j * P + i] : blk[i * P + j];
-          } else {
-            const int lo = la < lb ? la : lb, hi = la < lb ? lb : la;
-            double m = Kp[(size_t)e * npairs + (size_t)(lo * npe - (lo * (lo - 1)) / 2 + (hi - lo))];
-#pragma unroll
-            for (int i = 0; i < P; ++i)
-#pragma unroll
-              for (int j = 0; j < P; ++j) v[i][j] = (i == j) ? m : 0.0;
-          }
-#pragma unroll
-          for (int i = 0; i < P; ++i)
-#pragma unroll
-            for (int j = 0; j < P; ++j) acc[i][j] = first ? v[i][j] : __dadd_rn(acc[i][j], v[i][j]);
-          first = false;
-          ++ia;
-          ++ib;
-          if (ia < ea) xa = n2e[ia];
+    for (int t = lane; t < deg; t += 32) rows[t] = nadj[c0 + t];
+    for (int t = lane; t < deg * P * P; t += 32) acc[t] = 0.0;
+    __syncwarp();
+    const int64_t s = n2e_ptr[B], s1 = n2e_ptr[B + 1];
+    for (int64_t k = s; k < s1; ++k) {  // elements of B, ascending
+      const int2 el = n2e[k];
+      const T *col = Kf + ((size_t)el.x * npe + el.y) * npe * BS;
+      for (int a = lane; a < npe; a += 32) {
+        const int A = conn[(size_t)el.x * npe + a];
+        int lo = 0, hi = deg - 1;
+        while (lo < hi) {
+          int mid = (lo + hi) >> 1;
+          if (rows[mid] < A) lo = mid + 1; else hi = mid;
         }
-      }
-      if (first) atomicOr(status, ST_PATTERN);
-      // row (A,i), column (B,j): colptr(B,j) = P^2 c0 + j P deg; offset P t + i
+        if (rows[lo] != A) {
+          atomicOr(status, ST_PATTERN);
+          continue;
+        }
+        double *dst = acc + (size_t)lo * P * P;  // [t][j][i]
+        const T *blk = col + (size_t)a * BS;
 #pragma unroll
-      for (int j = 0; j < P; ++j) {
-        double *col = nz + (size_t)P * P * c0 + (size_t)j * P * deg + (size_t)P * t;
+        for (int i = 0; i < P; ++i)
 #pragma unroll
-        for (int i = 0; i < P; ++i) col[i] = acc[i][j];
+          for (int j = 0; j < P; ++j) {
+            double v = BLOCKVAL ? (double)blk[i * P + j] : (i == j ? (double)blk[0] : 0.0);
+            dst[j * P + i] = __dadd_rn(dst[j * P + i], v);
+          }
       }
+      __syncwarp();
+    }
+    // write column (B,j): entries (row node t, component i) at P*t + i
+#pragma unroll
+    for (int j = 0; j < P; ++j) {
+      double *out = nz + (size_t)P * P * c0 + (size_t)j * P * deg;
+      int n = 0;
+      for (int idx = lane; idx < P * deg; idx += 32) {
+        const int t = idx / P, i = idx % P;
+        const double v = acc[(size_t)t * P * P + j * P + i];
+        out[idx] = v;
+        n += (v != 0.0);
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) n += __shfl_xor_sync(0xffffffffu, n, off);
+      if (lane == 0 && cnt) cnt[B * P + j] = n;
     }
     __syncwarp();
   }
@@ -427,9 +435,9 @@ inline unsigned grid_1d(int64_t n, int threads, int sms) {
   return (unsigned)b;
 }
 
-template <int KIND, int DIM, bool GS>
+template <int KIND, int DIM, bool SM>
 int launch_elem(llf_ctx *ctx, const ElemArgs &a, size_t smem, unsigned grid) {
-  auto fn = k_elem_fp64<KIND, DIM, GS>;
+  auto fn = k_elem_fp64<KIND, DIM, SM>;
   if (smem > 48 * 1024)
     LLF_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
@@ -443,14 +451,13 @@ template <int KIND, int DIM>
 int run_elem(llf_ctx *ctx, ElemArgs a) {
   const int npe = a.npe, nip = a.nip;
   const int gsw = (KIND == KIND_MASS) ? 1 : DIM;
-  size_t base = sizeof(double) * ((size_t)nip * npe * DIM + nip +
-                                  (KIND == KIND_MASS ? (size_t)nip * npe : 0) +
-                                  (size_t)npe * DIM + nip + (size_t)nip * 9);
-  size_t gs = sizeof(double) * 2 * (size_t)nip * npe * gsw;
-  bool in_smem = base + gs <= 96 * 1024;
-  size_t smem = in_smem ? base + gs : base;
-  if (smem > 200 * 1024)
-    return llf_fail(ctx, LLF_ERR_LIMIT, "element tables exceed shared memory");
+  const size_t tables = sizeof(double) * ((size_t)nip * npe * DIM + nip +
+                                          (KIND == KIND_MASS ? (size_t)nip * npe : 0));
+  const size_t local = sizeof(double) * ((size_t)npe * DIM + nip + (size_t)nip * 9);
+  const size_t gs = sizeof(double) * 2 * (size_t)nip * npe * gsw;
+  const bool in_smem = tables + local + gs <= 96 * 1024;
+  const size_t smem = in_smem ? tables + local + gs : local;
+  if (smem > 200 * 1024) return llf_fail(ctx, LLF_ERR_LIMIT, "element exceeds shared memory");
   int per_sm = 0;
   if (in_smem)
     LLF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -473,19 +480,25 @@ int run_elem(llf_ctx *ctx, ElemArgs a) {
   return rc;
 }
 
-template <int P, bool BV>
-int run_gather(llf_ctx *ctx, llf_pattern *pat, const double *Kp, int npairs, double *nz) {
+template <int P, bool BV, class T>
+int run_colgather(llf_ctx *ctx, llf_pattern *pat, const T *Kf, double *nz, int64_t *cnt) {
   const int wpb = 4;
-  size_t smem = sizeof(int2) * (size_t)pat->max_n2e * wpb;
+  const int md = pat->max_deg > 0 ? pat->max_deg : 1;
+  size_t smem = (size_t)wpb * md * (P * P * sizeof(double) + sizeof(int32_t));
+  if (smem > 200 * 1024)
+    return llf_fail(ctx, LLF_ERR_LIMIT, "a column node has too many neighbours for the gather buffer");
+  auto fn = k_colgather<P, BV, T>;
   if (smem > 48 * 1024)
-    LLF_CUDA_TRY(ctx, cudaFuncSetAttribute(k_gather<P, BV>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem));
-  unsigned grid = grid_1d(pat->mesh->non * 32, wpb * 32, ctx->num_sms);
-  KernelScope ks(ctx, "k_gather");
-  k_gather<P, BV><<<grid, wpb * 32, smem, ctx->stream>>>(
-      pat->d_nptr, pat->d_nadj, pat->d_n2e_ptr, pat->d_n2e, Kp, pat->mesh->npe, npairs,
-      pat->mesh->non, pat->max_n2e > 0 ? pat->max_n2e : 1, nz, ctx->d_status);
+    LLF_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 1;
+  LLF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, wpb * 32, smem));
+  int64_t grid = (int64_t)ctx->num_sms * (per_sm < 1 ? 1 : per_sm);
+  int64_t need = (pat->mesh->non + wpb - 1) / wpb;
+  if (grid > need) grid = need > 0 ? need : 1;
+  KernelScope ks(ctx, "k_colgather");
+  fn<<<(unsigned)grid, wpb * 32, smem, ctx->stream>>>(pat->d_nptr, pat->d_nadj, pat->d_n2e_ptr,
+                                                      pat->d_n2e, pat->mesh->d_conn, Kf, pat->mesh->npe,
+                                                      pat->mesh->non, md, nz, cnt, ctx->d_status);
   LLF_CUDA_TRY(ctx, cudaGetLastError());
   return LLF_OK;
 }
@@ -493,38 +506,54 @@ int run_gather(llf_ctx *ctx, llf_pattern *pat, const double *Kp, int npairs, dou
 }  // namespace
 
 // ------------------------------------------------------------------ host
-int gather_pairs(llf_ctx *ctx, llf_pattern *pat, const double *Kp, int npairs, bool blockval,
-                 double *nz) {
+template <class T>
+int gather_full_t(llf_ctx *ctx, llf_pattern *pat, const T *Kf, bool blockval, double *nz,
+                  int64_t *cnt) {
   switch (pat->pdim * 2 + (blockval ? 1 : 0)) {
-    case 2: return run_gather<1, false>(ctx, pat, Kp, npairs, nz);
-    case 3: return run_gather<1, true>(ctx, pat, Kp, npairs, nz);
-    case 4: return run_gather<2, false>(ctx, pat, Kp, npairs, nz);
-    case 5: return run_gather<2, true>(ctx, pat, Kp, npairs, nz);
-    case 6: return run_gather<3, false>(ctx, pat, Kp, npairs, nz);
-    case 7: return run_gather<3, true>(ctx, pat, Kp, npairs, nz);
+    case 2: return run_colgather<1, false, T>(ctx, pat, Kf, nz, cnt);
+    case 3: return run_colgather<1, true, T>(ctx, pat, Kf, nz, cnt);
+    case 4: return run_colgather<2, false, T>(ctx, pat, Kf, nz, cnt);
+    case 5: return run_colgather<2, true, T>(ctx, pat, Kf, nz, cnt);
+    case 6: return run_colgather<3, false, T>(ctx, pat, Kf, nz, cnt);
+    case 7: return run_colgather<3, true, T>(ctx, pat, Kf, nz, cnt);
   }
   return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
 }
 
-int matrix_finalize(llf_ctx *ctx, llf_matrix *m) {
+int gather_full(llf_ctx *ctx, llf_pattern *pat, const double *Kf, bool blockval, double *nz,
+                int64_t *cnt) {
+  return gather_full_t<double>(ctx, pat, Kf, blockval, nz, cnt);
+}
+int gather_full32(llf_ctx *ctx, llf_pattern *pat, const float *Kf, bool blockval, double *nz,
+                  int64_t *cnt) {
+  return gather_full_t<float>(ctx, pat, Kf, blockval, nz, cnt);
+}
+
+int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts) {
   llf_pattern *pat = m->pat;
   const int64_t n = pat->ndof;
   cudaStream_t s = ctx->stream;
-  int64_t *cnt = nullptr;
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &cnt, n + 1));
-  LLF_CUDA_TRY(ctx, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (n + 1), s));
-  if (m->diagonal_only) {
-    KernelScope ks(ctx, "k_diag_stored");
-    k_diag_stored<<<grid_1d(n, 256, ctx->num_sms), 256, 0, s>>>(m->d_diag, n, cnt);
-  } else {
-    KernelScope ks(ctx, "k_count_nz");
-    k_count_nz<<<grid_1d(n * 32, 256, ctx->num_sms), 256, 0, s>>>(m->d_nz, pat->d_colptr, n, cnt);
+  int64_t *cnt = counts;
+  if (!cnt || m->diagonal_only) {
+    cnt = nullptr;
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &cnt, n + 1));
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (n + 1), s));
+    if (m->diagonal_only) {
+      KernelScope ks(ctx, "k_diag_stored");
+      k_diag_stored<<<grid_1d(n, 256, ctx->num_sms), 256, 0, s>>>(m->d_diag, n, cnt);
+    } else {
+      KernelScope ks(ctx, "k_count_nz");
+      k_count_nz<<<grid_1d(n * 32, 256, ctx->num_sms), 256, 0, s>>>(m->d_nz, pat->d_colptr, n, cnt);
+    }
+    LLF_CUDA_TRY(ctx, cudaGetLastError());
   }
-  LLF_CUDA_TRY(ctx, cudaGetLastError());
   int64_t *ptr0 = nullptr;
   LLF_CUDA_TRY(ctx, dalloc(ctx, &ptr0, n + 1));
   int64_t total = 0;
-  LLF_CUDA_TRY(ctx, exclusive_scan_i64(ctx, cnt, ptr0, n + 1, &total));
+  {
+    KernelScope ks(ctx, "scan");
+    LLF_CUDA_TRY(ctx, exclusive_scan_i64(ctx, cnt, ptr0, n + 1, &total));
+  }
   dfree(ctx, m->d_colptr_s);
   dfree(ctx, m->d_rowval_s);
   dfree(ctx, m->d_nzval_s);
@@ -547,10 +576,12 @@ int matrix_finalize(llf_ctx *ctx, llf_matrix *m) {
     }
   }
   LLF_CUDA_TRY(ctx, cudaGetLastError());
-  { KernelScope ks(ctx, "k_colptr_1based");
-  k_colptr_1based<<<grid_1d(n + 1, 256, ctx->num_sms), 256, 0, s>>>(ptr0, n + 1, m->d_colptr_s); }
+  {
+    KernelScope ks(ctx, "k_colptr_1based");
+    k_colptr_1based<<<grid_1d(n + 1, 256, ctx->num_sms), 256, 0, s>>>(ptr0, n + 1, m->d_colptr_s);
+  }
   LLF_CUDA_TRY(ctx, cudaGetLastError());
-  dfree(ctx, cnt);
+  if (cnt != counts) dfree(ctx, cnt);
   dfree(ctx, ptr0);
   return LLF_OK;
 }
@@ -558,76 +589,72 @@ int matrix_finalize(llf_ctx *ctx, llf_matrix *m) {
 int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int ptype,
                   const double *c1, const double *c2, int nmat, int form, int lumped,
                   llf_matrix *m) {
-  (void)form;
+  (void)ptype;
   const int dim = mesh->dim;
   const int npe = mesh->npe;
-  const int npairs = npe * (npe + 1) / 2;
   const int P = pat->pdim;
   const int BS = (kind == KIND_ELASTIC) ? P * P : 1;
   cudaStream_t s = ctx->stream;
 
   double *d_c1 = nullptr, *d_c2 = nullptr;
+  int64_t *cnt = nullptr;
   LLF_CUDA_TRY(ctx, dalloc(ctx, &d_c1, nmat));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &d_c2, nmat));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &cnt, pat->ndof + 1));
+  LLF_CUDA_TRY(ctx, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (pat->ndof + 1), s));
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_c1, c1, sizeof(double) * nmat, cudaMemcpyHostToDevice, s));
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_c2, c2 ? c2 : c1, sizeof(double) * nmat,
                                     cudaMemcpyHostToDevice, s));
-  double *Kp = nullptr;
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &Kp, (size_t)mesh->nel * npairs * BS));
-
-  ElemArgs a{};
-  a.xyz = mesh->d_xyz;
-  a.conn = mesh->d_conn;
-  a.emat = mesh->d_emat;
-  a.nel = mesh->nel;
-  a.npe = npe;
-  a.nip = mesh->nip;
-  a.npairs = npairs;
-  a.w = mesh->d_w;
-  a.N = mesh->d_N;
-  a.dN = mesh->d_dN;
-  a.c1 = d_c1;
-  a.c2 = d_c2;
-  a.Kp = Kp;
-  a.status = ctx->d_status;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nz, pat->nnz));
   int rc = LLF_OK;
-  if (dim == 3) {
-    if (kind == KIND_ELASTIC) rc = run_elem<KIND_ELASTIC, 3>(ctx, a);
-    else if (kind == KIND_HEAT) rc = run_elem<KIND_HEAT, 3>(ctx, a);
-    else rc = run_elem<KIND_MASS, 3>(ctx, a);
+  if (form == LLF_FP32Q) {
+    rc = assemble_fp32_impl(ctx, mesh, pat, kind, d_c1, d_c2, m->d_nz, cnt);
   } else {
-    if (kind == KIND_ELASTIC) rc = run_elem<KIND_ELASTIC, 2>(ctx, a);
-    else if (kind == KIND_HEAT) rc = run_elem<KIND_HEAT, 2>(ctx, a);
-    else rc = run_elem<KIND_MASS, 2>(ctx, a);
-  }
-  if (rc == LLF_OK) {
-    LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nz, pat->nnz));
-    if (kind == KIND_ELASTIC) {
-      rc = (P == 3) ? run_gather<3, true>(ctx, pat, Kp, npairs, m->d_nz)
-                    : run_gather<2, true>(ctx, pat, Kp, npairs, m->d_nz);
+    double *Kf = nullptr;
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &Kf, (size_t)mesh->nel * npe * npe * BS));
+    ElemArgs a{};
+    a.xyz = mesh->d_xyz;
+    a.conn = mesh->d_conn;
+    a.emat = mesh->d_emat;
+    a.nel = mesh->nel;
+    a.npe = npe;
+    a.nip = mesh->nip;
+    a.npairs = npe * (npe + 1) / 2;
+    a.w = mesh->d_w;
+    a.N = mesh->d_N;
+    a.dN = mesh->d_dN;
+    a.c1 = d_c1;
+    a.c2 = d_c2;
+    a.Kf = Kf;
+    a.status = ctx->d_status;
+    if (dim == 3) {
+      if (kind == KIND_ELASTIC) rc = run_elem<KIND_ELASTIC, 3>(ctx, a);
+      else if (kind == KIND_HEAT) rc = run_elem<KIND_HEAT, 3>(ctx, a);
+      else rc = run_elem<KIND_MASS, 3>(ctx, a);
     } else {
-      switch (P) {
-        case 1: rc = run_gather<1, false>(ctx, pat, Kp, npairs, m->d_nz); break;
-        case 2: rc = run_gather<2, false>(ctx, pat, Kp, npairs, m->d_nz); break;
-        case 3: rc = run_gather<3, false>(ctx, pat, Kp, npairs, m->d_nz); break;
-      }
+      if (kind == KIND_ELASTIC) rc = run_elem<KIND_ELASTIC, 2>(ctx, a);
+      else if (kind == KIND_HEAT) rc = run_elem<KIND_HEAT, 2>(ctx, a);
+      else rc = run_elem<KIND_MASS, 2>(ctx, a);
     }
+    if (rc == LLF_OK) rc = gather_full(ctx, pat, Kf, kind == KIND_ELASTIC, m->d_nz, cnt);
+    dfree(ctx, Kf);
   }
-  dfree(ctx, Kp);
   dfree(ctx, d_c1);
   dfree(ctx, d_c2);
-  if (rc != LLF_OK) return rc;
-  rc = llf_check_status(ctx, "assembly");
-  if (rc != LLF_OK) return rc;
-  if (kind == KIND_MASS && lumped) {
+  if (rc == LLF_OK) rc = llf_check_status(ctx, "assembly");
+  if (rc == LLF_OK && kind == KIND_MASS && lumped) {
     m->diagonal_only = true;
-    LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_diag, pat->ndof));
-    KernelScope ks(ctx, "k_lump");
-    k_lump<<<grid_1d(pat->ndof, 128, ctx->num_sms), 128, 0, s>>>(m->d_nz, pat->d_colptr,
-                                                                 pat->ndof, m->d_diag);
-    LLF_CUDA_TRY(ctx, cudaGetLastError());
+    cudaError_t e = dalloc(ctx, &m->d_diag, pat->ndof);
+    if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+    if (rc == LLF_OK) {
+      KernelScope ks(ctx, "k_lump");
+      k_lump<<<grid_1d(pat->ndof, 128, ctx->num_sms), 128, 0, s>>>(m->d_nz, pat->d_colptr,
+                                                                   pat->ndof, m->d_diag);
+    }
   }
-  return matrix_finalize(ctx, m);
+  if (rc == LLF_OK) rc = matrix_finalize(ctx, m, (kind == KIND_MASS && lumped) ? nullptr : cnt);
+  dfree(ctx, cnt);
+  return rc;
 }
 
 int matrix_axpby_impl(llf_ctx *ctx, double a, const llf_matrix *A, double b,
@@ -639,9 +666,11 @@ int matrix_axpby_impl(llf_ctx *ctx, double a, const llf_matrix *A, double b,
   C->pat = A->pat;
   int64_t n = A->pat->nnz;
   LLF_CUDA_TRY(ctx, dalloc(ctx, &C->d_nz, n));
-  KernelScope ks(ctx, "k_axpby");
-  k_axpby<<<grid_1d(n, 256, ctx->num_sms), 256, 0, ctx->stream>>>(a, A->d_nz, b, B->d_nz,
-                                                                  C->d_nz, n);
+  {
+    KernelScope ks(ctx, "k_axpby");
+    k_axpby<<<grid_1d(n, 256, ctx->num_sms), 256, 0, ctx->stream>>>(a, A->d_nz, b, B->d_nz,
+                                                                    C->d_nz, n);
+  }
   LLF_CUDA_TRY(ctx, cudaGetLastError());
-  return matrix_finalize(ctx, C);
+  return matrix_finalize(ctx, C, nullptr);
 }

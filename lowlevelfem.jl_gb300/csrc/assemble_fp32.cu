@@ -1,0 +1,255 @@
+// Precision form of the linear operators: element quadrature in FP32 (node
+// coordinates taken relative to the element's first node in FP64 before the
+// conversion, so large or offset meshes keep their geometric accuracy),
+// FP32 element matrices, and the global CSC accumulation in FP64 (each
+// element's FP32 contribution converted exactly to FP64 and summed in
+// element order by the same column-node gather as the FP64 form).
+// Halves the element-matrix traffic and moves the quadrature off the FP64
+// pipe.  Results agree with the FP64 form to FP32 quadrature accuracy
+// (~1e-7 relative to the largest entry); the stored (dropzeros!) pattern can
+// keep entries that cancel exactly only in FP64.
+#include "common.cuh"
+
+namespace {
+
+constexpr int E32_THREADS = 128;
+
+struct Elem32Args {
+  const double *xyz;
+  const int32_t *conn;
+  const int32_t *emat;
+  int64_t nel;
+  int npe, nip, npairs;
+  const float *w, *N, *dN;
+  const double *c1, *c2;
+  float *Kf;
+  unsigned *status;
+};
+
+__device__ __forceinline__ int poff(int a, int npe) { return a * npe - (a * (a - 1)) / 2; }
+__device__ __forceinline__ void pdec(int pi, int npe, int &a, int &b) {
+  int lo = 0, hi = npe - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (poff(mid, npe) <= pi) lo = mid; else hi = mid - 1;
+  }
+  a = lo;
+  b = a + (pi - poff(a, npe));
+}
+
+template <int P, int BS>
+__device__ __forceinline__ void store_pair32(float *Ke, int npe, int a, int b, const float *blk) {
+  float *ab = Ke + ((size_t)b * npe + a) * BS;
+#pragma unroll
+  for (int k = 0; k < BS; ++k) ab[k] = blk[k];
+  if (a != b) {
+    float *ba = Ke + ((size_t)a * npe + b) * BS;
+    if (BS == 1) {
+      ba[0] = blk[0];
+    } else {
+#pragma unroll
+      for (int i = 0; i < P; ++i)
+#pragma unroll
+        for (int j = 0; j < P; ++j) ba[j * P + i] = blk[i * P + j];
+    }
+  }
+}
+
+template <int KIND, int DIM>
+__global__ void __launch_bounds__(E32_THREADS) k_elem_fp32(Elem32Args A) {
+  extern __shared__ float sf[];
+  const int npe = A.npe, nip = A.nip;
+  constexpr int gsw = (KIND == KIND_MASS) ? 1 : DIM;
+  float *sdN = sf;                                  // nip*npe*DIM
+  float *sw = sdN + (size_t)nip * npe * DIM;        // nip
+  float *sN = sw + nip;                             // nip*npe (mass)
+  float *sX = sN + (KIND == KIND_MASS ? (size_t)nip * npe : 0);  // npe*DIM
+  float *sWd = sX + (size_t)npe * DIM;              // nip
+  float *sInv = sWd + nip;                          // nip*9
+  float *G = sInv + (size_t)nip * 9;                // nip*npe*gsw
+  float *S = G + (size_t)nip * npe * gsw;           // nip*npe*gsw
+  for (int t = threadIdx.x; t < nip * npe * DIM; t += blockDim.x)
+    sdN[t] = A.dN[(size_t)(t / DIM) * 3 + t % DIM];
+  for (int t = threadIdx.x; t < nip; t += blockDim.x) sw[t] = A.w[t];
+  if (KIND == KIND_MASS)
+    for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) sN[t] = A.N[t];
+  __syncthreads();
+  constexpr int BS = (KIND == KIND_ELASTIC) ? DIM * DIM : 1;
+  constexpr int P = (KIND == KIND_ELASTIC) ? DIM : 1;
+  for (int64_t e = blockIdx.x; e < A.nel; e += gridDim.x) {
+    const int mat = A.emat ? A.emat[e] : 0;
+    if (mat < 0) continue;
+    const float c1 = (float)A.c1[mat];
+    const float c2 = (KIND == KIND_ELASTIC) ? (float)A.c2[mat] : 0.f;
+    const int32_t *cn = A.conn + e * npe;
+    for (int t = threadIdx.x; t < npe * DIM; t += blockDim.x) {
+      int a = t / DIM, i = t % DIM;
+      sX[t] = (float)(A.xyz[(size_t)cn[a] * 3 + i] - A.xyz[(size_t)cn[0] * 3 + i]);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nip; q += blockDim.x) {
+      const float *d = sdN + (size_t)q * npe * DIM;
+      float J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+      for (int a = 0; a < npe; ++a)
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) J[i][j] = fmaf(sX[a * DIM + i], d[a * DIM + j], J[i][j]);
+      float inv[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      float det;
+      if (DIM == 3) {
+        float c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        float c01 = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]);
+        float c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        float r = 1.0f / det;
+        inv[0] = c00 * r;
+        inv[1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) * r;
+        inv[2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+        inv[3] = c01 * r;
+        inv[4] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+        inv[5] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]) * r;
+        inv[6] = c02 * r;
+        inv[7] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]) * r;
+        inv[8] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+      } else {
+        det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        float r = 1.0f / det;
+        inv[0] = J[1][1] * r; inv[1] = -J[0][1] * r;
+        inv[3] = -J[1][0] * r; inv[4] = J[0][0] * r;
+      }
+      if (!(det > 0.f)) atomicOr(A.status, ST_BAD_JACOBIAN);
+      sWd[q] = det * sw[q];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) sInv[q * 9 + k] = inv[k];
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) {
+      const int q = t / npe;
+      if (KIND == KIND_MASS) {
+        S[t] = sWd[q] * sN[t];
+      } else {
+        const float *inv = sInv + q * 9;
+        const float *d = sdN + (size_t)t * DIM;
+#pragma unroll
+        for (int i = 0; i < DIM; ++i) {
+          float acc = 0.f;
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) acc = fmaf(inv[3 * j + i], d[j], acc);
+          G[(size_t)t * DIM + i] = acc;
+          S[(size_t)t * DIM + i] = sWd[q] * acc;
+        }
+      }
+    }
+    __syncthreads();
+    float *Ke = A.Kf + (size_t)e * npe * npe * BS;
+    for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
+      int a, b;
+      pdec(pi, npe, a, b);
+      float blk[BS];
+      if (KIND == KIND_ELASTIC) {
+        float O[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) O[i][j] = 0.f;
+        for (int q = 0; q < nip; ++q) {
+          const float *sa = S + ((size_t)q * npe + a) * DIM;
+          const float *gb = G + ((size_t)q * npe + b) * DIM;
+#pragma unroll
+          for (int i = 0; i < DIM; ++i)
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) O[i][j] = fmaf(sa[i], gb[j], O[i][j]);
+        }
+        if (a == b)
+#pragma unroll
+          for (int i = 0; i < DIM; ++i)
+#pragma unroll
+            for (int j = 0; j < i; ++j) O[i][j] = O[j][i];
+        float tr = O[0][0] + O[1 % DIM][1 % DIM];
+        if (DIM == 3) tr += O[2 % DIM][2 % DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            float t = fmaf(c2, O[j][i], c1 * O[i][j]);
+            if (i == j) t = fmaf(c2, tr, t);
+            blk[i * DIM + j] = t;
+          }
+      } else if (KIND == KIND_HEAT) {
+        float acc = 0.f;
+        for (int q = 0; q < nip; ++q) {
+          const float *sa = S + ((size_t)q * npe + a) * DIM;
+          const float *gb = G + ((size_t)q * npe + b) * DIM;
+#pragma unroll
+          for (int i = 0; i < DIM; ++i) acc = fmaf(sa[i], gb[i], acc);
+        }
+        blk[0] = c1 * acc;
+      } else {
+        float acc = 0.f;
+        for (int q = 0; q < nip; ++q) acc = fmaf(S[(size_t)q * npe + a], sN[(size_t)q * npe + b], acc);
+        blk[0] = c1 * acc;
+      }
+      store_pair32<P, BS>(Ke, npe, a, b, blk);
+    }
+    __syncthreads();
+  }
+}
+
+template <int KIND, int DIM>
+int run_elem32(llf_ctx *ctx, Elem32Args a) {
+  const int npe = a.npe, nip = a.nip;
+  const int gsw = (KIND == KIND_MASS) ? 1 : DIM;
+  size_t smem = sizeof(float) * ((size_t)nip * npe * DIM + nip + (KIND == KIND_MASS ? (size_t)nip * npe : 0) +
+                                 (size_t)npe * DIM + nip + (size_t)nip * 9 + 2 * (size_t)nip * npe * gsw);
+  if (smem > 200 * 1024)
+    return llf_fail(ctx, LLF_ERR_LIMIT, "precision form: element tables exceed shared memory (use the FP64 form)");
+  auto fn = k_elem_fp32<KIND, DIM>;
+  if (smem > 48 * 1024)
+    LLF_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 1;
+  LLF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, E32_THREADS, smem));
+  int64_t grid = (int64_t)ctx->num_sms * (per_sm < 1 ? 1 : per_sm);
+  if (grid > a.nel) grid = a.nel > 0 ? a.nel : 1;
+  KernelScope ks(ctx, "k_elem_fp32");
+  fn<<<(unsigned)grid, E32_THREADS, smem, ctx->stream>>>(a);
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  return LLF_OK;
+}
+
+}  // namespace
+
+// Precision-form assembly of the structural values into nz (and the
+// per-column non-zero counts into cnt).
+int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, const double *d_c1,
+                       const double *d_c2, double *nz, int64_t *cnt) {
+  const int npe = mesh->npe, P = pat->pdim;
+  const int BS = (kind == KIND_ELASTIC) ? P * P : 1;
+  float *Kf = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &Kf, (size_t)mesh->nel * npe * npe * BS));
+  Elem32Args a{};
+  a.xyz = mesh->d_xyz;
+  a.conn = mesh->d_conn;
+  a.emat = mesh->d_emat;
+  a.nel = mesh->nel;
+  a.npe = npe;
+  a.nip = mesh->nip;
+  a.npairs = npe * (npe + 1) / 2;
+  a.w = mesh->d_wf;
+  a.N = mesh->d_Nf;
+  a.dN = mesh->d_dNf;
+  a.c1 = d_c1;
+  a.c2 = d_c2;
+  a.Kf = Kf;
+  a.status = ctx->d_status;
+  int rc;
+  if (mesh->dim == 3)
+    rc = kind == KIND_ELASTIC ? run_elem32<KIND_ELASTIC, 3>(ctx, a)
+                              : (kind == KIND_HEAT ? run_elem32<KIND_HEAT, 3>(ctx, a) : run_elem32<KIND_MASS, 3>(ctx, a));
+  else
+    rc = kind == KIND_ELASTIC ? run_elem32<KIND_ELASTIC, 2>(ctx, a)
+                              : (kind == KIND_HEAT ? run_elem32<KIND_HEAT, 2>(ctx, a) : run_elem32<KIND_MASS, 2>(ctx, a));
+  if (rc == LLF_OK) rc = gather_full32(ctx, pat, Kf, kind == KIND_ELASTIC, nz, cnt);
+  dfree(ctx, Kf);
+  return rc;
+}

@@ -106,6 +106,7 @@ struct llf_pattern {
   int64_t *d_nptr = nullptr;      // non+1
   int32_t *d_nadj = nullptr;      // nnzb (0-based node index, sorted per column)
   int32_t *d_diagpos = nullptr;   // non: position of the node itself in its column
+  int max_deg = 0;                // largest number of row nodes of a column node
   // DoF-level colptr (0-based)
   int64_t *d_colptr = nullptr;    // ndof+1
 };
@@ -167,11 +168,21 @@ int build_n2e(llf_ctx *ctx, const int32_t *conn, const int32_t *emat, int64_t ne
 int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
                   int ptype, const double *c1, const double *c2, int nmat,
                   int form, int lumped, llf_matrix *m);
-int matrix_finalize(llf_ctx *ctx, llf_matrix *m);  // dropzeros -> stored form
-// Element-ordered gather of node-pair blocks (blockval: pdim x pdim blocks;
-// otherwise one scalar per pair placed on the component diagonal).
-int gather_pairs(llf_ctx *ctx, llf_pattern *pat, const double *Kp, int npairs, bool blockval,
-                 double *nz);
+// dropzeros -> stored form; counts (non-zeros per DoF column) may come from
+// the gather, else they are counted here
+int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts);
+// assemble_fp32.cu: precision form (FP32 quadrature, FP64 accumulation) into nz
+int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
+                       const double *d_c1, const double *d_c2, double *nz, int64_t *cnt);
+// Element-ordered column-node gather of whole element matrices laid out as
+// Kf[element][column node][row node][block] (blockval: pdim x pdim blocks,
+// entry (i,j) at i*pdim+j; otherwise one scalar per node pair placed on the
+// component diagonal).  Writes the structural values and, if cnt != NULL,
+// the non-zero count of every DoF column.
+int gather_full(llf_ctx *ctx, llf_pattern *pat, const double *Kf, bool blockval, double *nz,
+                int64_t *cnt);
+int gather_full32(llf_ctx *ctx, llf_pattern *pat, const float *Kf, bool blockval, double *nz,
+                  int64_t *cnt);
 // field.cu: f[node*pdim+i] += fe[e][a][i] of every element of the node, in element order.
 int node_gather(llf_ctx *ctx, const int32_t *conn, int64_t nel, int npe, int64_t non, int pdim,
                 const double *fe, double *f);

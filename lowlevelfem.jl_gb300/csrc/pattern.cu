@@ -170,6 +170,14 @@ __global__ void k_node_adjacency(const int32_t *__restrict__ conn, int npe,
   }
 }
 
+__global__ void k_max_deg(const int64_t *__restrict__ deg, int64_t non, int *out) {
+  int m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < non;
+       i += (int64_t)gridDim.x * blockDim.x)
+    m = max(m, (int)deg[i]);
+  atomicMax(out, m);
+}
+
 __global__ void k_dof_colptr(const int64_t *__restrict__ nptr, int64_t non,
                              int p, int64_t *__restrict__ colptr) {
   int64_t B = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -280,6 +288,17 @@ int pattern_build_impl(llf_ctx *ctx, llf_mesh *mesh, int pdim, llf_pattern *pat)
                                                        pat->d_n2e, non, cap, cnt, nullptr,
                                                        nullptr, ctx->d_status);
   LLF_CUDA_TRY(ctx, cudaGetLastError());
+  {
+    int *d_md = nullptr;
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_md, 1));
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_md, 0, sizeof(int), s));
+    k_max_deg<<<grid_for(non, 256, ctx->num_sms), 256, 0, s>>>(cnt, non, d_md);
+    int md = 0;
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&md, d_md, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    dfree(ctx, d_md);
+    pat->max_deg = md;
+  }
   LLF_CUDA_TRY(ctx, dalloc(ctx, &pat->d_nptr, non + 1));
   int64_t nnzb = 0;
   LLF_CUDA_TRY(ctx, exclusive_scan_i64(ctx, cnt, pat->d_nptr, non + 1, &nnzb));

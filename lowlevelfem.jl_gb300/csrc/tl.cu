@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(TL_THREADS) k_tl_matrix(TLArgs A) {
     __syncthreads();
     for (int q = threadIdx.x; q < nip; q += blockDim.x) tl_point(A, MODE, q, sX, sT, qd + (size_t)q * QD);
     __syncthreads();
-    double *out = A.out + (size_t)e * A.npairs * BS;
+    double *Ke = A.out + (size_t)e * npe * npe * BS;  // [column node][row node][block]
     const int tile = blockDim.x * PPT;
     for (int p0 = 0; p0 < A.npairs; p0 += tile) {
       double acc[PPT][BS];
@@ -290,14 +290,20 @@ __global__ void __launch_bounds__(TL_THREADS) k_tl_matrix(TLArgs A) {
         if (pi >= A.npairs) continue;
         int a, b;
         pair_dec(pi, npe, a, b);
-        double *o = out + (size_t)pi * BS;
+        double *ab = Ke + ((size_t)b * npe + a) * BS;   // block (a,b)
+        double *ba = Ke + ((size_t)a * npe + b) * BS;   // mirror (b,a)
         if (MODE == TL_KMAT) {
 #pragma unroll
           for (int i = 0; i < 3; ++i)
 #pragma unroll
-            for (int j = 0; j < 3; ++j) o[i * 3 + j] = (a == b && j < i) ? acc[k][j * 3 + i] : acc[k][i * 3 + j];
+            for (int j = 0; j < 3; ++j) {
+              const double v = (a == b && j < i) ? acc[k][j * 3 + i] : acc[k][i * 3 + j];
+              ab[i * 3 + j] = v;
+              if (a != b) ba[j * 3 + i] = v;
+            }
         } else {
-          o[0] = acc[k][0];
+          ab[0] = acc[k][0];
+          if (a != b) ba[0] = acc[k][0];
         }
       }
     }
@@ -430,20 +436,24 @@ int tl_matrix(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int mode, const do
   if (smem > 200 * 1024) return llf_fail(ctx, LLF_ERR_LIMIT, "element too large for the TL kernels");
   const int BS = mode == TL_KMAT ? 9 : 1;
   double *Kp = nullptr;
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &Kp, (size_t)mesh->nel * a.npairs * BS));
+  int64_t *cnt = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &Kp, (size_t)mesh->nel * mesh->npe * mesh->npe * BS));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &cnt, pat->ndof + 1));
+  LLF_CUDA_TRY(ctx, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (pat->ndof + 1), ctx->stream));
   a.out = Kp;
   rc = (mode == TL_KMAT) ? launch_matrix<TL_KMAT>(ctx, a, smem)
                          : (mode == TL_KGEO_S ? launch_matrix<TL_KGEO_S>(ctx, a, smem)
                                               : launch_matrix<TL_KGEO_C>(ctx, a, smem));
   if (rc == LLF_OK) {
-    LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nz, pat->nnz));
-    rc = gather_pairs(ctx, pat, Kp, a.npairs, mode == TL_KMAT, m->d_nz);
+    cudaError_t e = dalloc(ctx, &m->d_nz, pat->nnz);
+    rc = (e == cudaSuccess) ? gather_full(ctx, pat, Kp, mode == TL_KMAT, m->d_nz, cnt)
+                            : llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
   }
   dfree(ctx, Kp);
-  if (rc) return rc;
-  rc = llf_check_status(ctx, mode == TL_KMAT ? "materialTangentMatrix" : "initialStressMatrix");
-  if (rc) return rc;
-  return matrix_finalize(ctx, m);
+  if (rc == LLF_OK) rc = llf_check_status(ctx, mode == TL_KMAT ? "materialTangentMatrix" : "initialStressMatrix");
+  if (rc == LLF_OK) rc = matrix_finalize(ctx, m, cnt);
+  dfree(ctx, cnt);
+  return rc;
 }
 
 }  // namespace

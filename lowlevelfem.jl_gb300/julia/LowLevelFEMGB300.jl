@@ -1,0 +1,267 @@
+# LowLevelFEMGB300 — drop-in GPU methods for LowLevelFEM.jl's assembly/solve
+# hot path, calling libllfem_gb300.so through ccall.
+#
+# Usage (after `using LowLevelFEM`):
+#     include("LowLevelFEMGB300.jl"); using .LowLevelFEMGB300
+#     K = LowLevelFEMGB300.stiffnessMatrix(problem)      # same result type as
+#     u = LowLevelFEMGB300.solveDisplacement(problem; load=[ld], support=[bc])
+#
+# Mesh data and quadrature/shape tables are read from gmsh exactly as
+# src/linear.jl:232-243 reads them, so the GPU integrates with gmsh's own
+# rule and node ordering (llf_tables_upload).  Every non-zero status of the
+# library becomes `error(msg)`, the reference's error behaviour.
+module LowLevelFEMGB300
+
+using LowLevelFEM
+using LowLevelFEM: gmsh, SystemMatrix, VectorField, ScalarField, BoundaryCondition, LoadCondition
+using SparseArrays
+
+const LIB = get(ENV, "LLFEM_GB300_LIB", joinpath(@__DIR__, "..", "libllfem_gb300.so"))
+
+const CTX = Ref{Ptr{Cvoid}}(C_NULL)
+
+function ctx()
+    if CTX[] == C_NULL
+        r = Ref{Ptr{Cvoid}}(C_NULL)
+        st = ccall((:llf_ctx_create, LIB), Cint, (Cint, Ref{Ptr{Cvoid}}), 0, r)
+        st == 0 || error("llf_ctx_create failed with status $st (no CUDA device?)")
+        CTX[] = r[]
+    end
+    return CTX[]
+end
+
+function check(st::Cint)
+    st == 0 && return nothing
+    msg = unsafe_string(ccall((:llf_last_error, LIB), Cstring, (Ptr{Cvoid},), ctx()))
+    error(msg)
+end
+
+const FAMILY = Dict(1 => 1, 2 => 2, 3 => 3, 4 => 4, 5 => 5, 8 => 1, 9 => 2, 10 => 3, 11 => 4, 12 => 5,
+                    26 => 1, 21 => 2, 36 => 3, 29 => 4, 92 => 5, 27 => 1, 23 => 2, 37 => 3, 35 => 4, 93 => 5)
+
+ptype(p) = p.type == :Solid ? 0 : p.type == :PlaneStress ? 1 : p.type == :PlaneStrain ? 2 :
+           p.type == :HeatConduction ? 3 : p.type == :PlaneHeatConduction ? 4 :
+           p.type == :VectorField ? (p.dim == 3 ? 0 : 2) : p.type == :ScalarField ? (p.dim == 3 ? 3 : 4) :
+           error("LowLevelFEMGB300: problem type $(p.type) is not on the accelerated path")
+
+# ---------------------------------------------------------------- mesh
+struct DevMesh
+    h::Ptr{Cvoid}
+    nel::Int
+    npe::Int
+    etype::Int
+end
+
+const MESHES = IdDict{Any,DevMesh}()
+const PATTERNS = IdDict{Any,Dict{Int,Ptr{Cvoid}}}()
+
+function device_mesh(problem)
+    haskey(MESHES, problem) && return MESHES[problem]
+    gmsh.model.setCurrent(problem.name)
+    nodeTags, coord, _ = gmsh.model.mesh.getNodes()
+    non = length(nodeTags)
+    xyz = zeros(3non)
+    for (i, t) in enumerate(nodeTags)
+        xyz[3t-2:3t] .= coord[3i-2:3i]
+    end
+    conn = Int64[]; emat = Int32[]; et0 = 0; npe = 0
+    for (imat, mat) in enumerate(problem.material)
+        for (edim, etag) in gmsh.model.getEntitiesForPhysicalName(mat.phName)
+            edim == problem.dim || continue
+            types, _, ntags = gmsh.model.mesh.getElements(edim, etag)
+            for (k, et) in enumerate(types)
+                et0 == 0 && (et0 = et)
+                et == et0 || error("LowLevelFEMGB300: one element type per problem")
+                _, _, _, npe, _, _ = gmsh.model.mesh.getElementProperties(et)
+                append!(conn, ntags[k])
+                append!(emat, fill(Int32(imat - 1), length(ntags[k]) ÷ npe))
+            end
+        end
+    end
+    _, _, order, npe, _, _ = gmsh.model.mesh.getElementProperties(et0)
+    nel = length(conn) ÷ npe
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:llf_mesh_upload, LIB), Cint,
+                (Ptr{Cvoid}, Cint, Int64, Ptr{Float64}, Int64, Cint, Ptr{Int64}, Cint, Cint, Ref{Ptr{Cvoid}}),
+                ctx(), problem.dim, non, xyz, nel, npe, conn, FAMILY[et0], order, h))
+    # gmsh's own quadrature and shape tables (src/linear.jl:235-239)
+    ip, w = gmsh.model.mesh.getIntegrationPoints(et0, "Gauss" * string(2order + 1))
+    _, N, _ = gmsh.model.mesh.getBasisFunctions(et0, ip, "Lagrange")
+    _, dN, _ = gmsh.model.mesh.getBasisFunctions(et0, ip, "GradLagrange")
+    check(ccall((:llf_tables_upload, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                ctx(), h[], length(w), w, N, dN))
+    if length(problem.material) > 1
+        check(ccall((:llf_mesh_set_materials, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Int32}), ctx(), h[], emat))
+    end
+    return MESHES[problem] = DevMesh(h[], nel, npe, et0)
+end
+
+function pattern(problem, pdim::Int=problem.pdim)
+    m = device_mesh(problem)
+    d = get!(PATTERNS, problem, Dict{Int,Ptr{Cvoid}}())
+    haskey(d, pdim) && return d[pdim]
+    nnz = Ref{Int64}(0); h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:llf_pattern_build, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ref{Int64}, Ref{Ptr{Cvoid}}),
+                ctx(), m.h, pdim, nnz, h))
+    return d[pdim] = h[]
+end
+
+# device matrix -> SparseMatrixCSC{Float64,Int64} (two-phase copy), then free
+function fetch(hm::Ptr{Cvoid}, n::Int)
+    nnz = Ref{Int64}(0)
+    check(ccall((:llf_matrix_nnz, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ref{Int64}), ctx(), hm, nnz))
+    colptr = Vector{Int64}(undef, n + 1); rowval = Vector{Int64}(undef, nnz[]); nzval = Vector{Float64}(undef, nnz[])
+    check(ccall((:llf_matrix_copy_csc, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}),
+                ctx(), hm, colptr, rowval, nzval))
+    ccall((:llf_matrix_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), hm)
+    return SparseMatrixCSC(n, n, colptr, rowval, nzval)
+end
+
+# ---------------------------------------------------------------- assembly
+function stiffnessMatrix(problem; elements=[], forceOneThread=true)
+    m = device_mesh(problem); pat = pattern(problem)
+    E = Float64[mat.E for mat in problem.material]; ν = Float64[mat.ν for mat in problem.material]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:llf_assemble_stiffness, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Cint, Float64, Cint, Ref{Ptr{Cvoid}}),
+                ctx(), m.h, pat, ptype(problem), E, ν, length(E), problem.thickness, 0, h))
+    return SystemMatrix(fetch(h[], problem.pdim * problem.non), problem)
+end
+
+function massMatrix(problem; lumped=true)
+    m = device_mesh(problem); pat = pattern(problem)
+    ρ = Float64[mat.ρ for mat in problem.material]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:llf_assemble_mass, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Float64, Cint, Cint, Ref{Ptr{Cvoid}}),
+                ctx(), m.h, pat, ptype(problem), ρ, length(ρ), problem.thickness, lumped ? 1 : 0, 0, h))
+    return SystemMatrix(fetch(h[], problem.pdim * problem.non), problem)
+end
+
+function heatConductionMatrix(problem; elements=[])
+    m = device_mesh(problem); pat = pattern(problem, 1)
+    k = Float64[mat.k for mat in problem.material]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:llf_assemble_heat, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Float64, Cint, Ref{Ptr{Cvoid}}),
+                ctx(), m.h, pat, ptype(problem), k, length(k), problem.thickness, 0, h))
+    return SystemMatrix(fetch(h[], problem.non), problem)
+end
+
+# energy: pass :NeoHookeCompressible or :StVenantKirchhoff; params = (μ=.., λ=..)
+law(energy) = energy === :NeoHookeCompressible ? 1 : energy === :StVenantKirchhoff ? 2 :
+              error("LowLevelFEMGB300: built-in laws are :NeoHookeCompressible and :StVenantKirchhoff")
+lawparams(p) = Float64[p.μ, p.λ]
+
+elementwise(T) = reduce(vcat, [vec(T.A[i][:, 1]) for i in eachindex(T.A)])
+
+function materialTangentMatrix(problem; F, C=nothing, energy=nothing, params=nothing)
+    @assert xor(C !== nothing, energy !== nothing)
+    m = device_mesh(problem); pat = pattern(problem)
+    Fe = elementwise(LowLevelFEM.nodesToElements(F))
+    lw, prm = C === nothing ? (law(energy), lawparams(params)) : (0, vec(Float64.(C)))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:llf_tl_material_tangent, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Cint, Ptr{Float64}, Cint, Ref{Ptr{Cvoid}}),
+                ctx(), m.h, pat, Fe, lw, prm, length(prm), h))
+    return SystemMatrix(fetch(h[], 3problem.non), problem)
+end
+
+function initialStressMatrix(problem; S=nothing, energy=nothing, params=nothing, C=nothing)
+    @assert xor(S !== nothing, energy !== nothing)
+    m = device_mesh(problem); pat = pattern(problem)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    if S !== nothing
+        Se = elementwise(LowLevelFEM.nodesToElements(S))
+        check(ccall((:llf_tl_initial_stress, LIB), Cint,
+                    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Cint, Ptr{Float64}, Cint, Ref{Ptr{Cvoid}}),
+                    ctx(), m.h, pat, Se, C_NULL, 0, C_NULL, 0, h))
+    else
+        Ce = elementwise(LowLevelFEM.nodesToElements(C)); prm = lawparams(params)
+        check(ccall((:llf_tl_initial_stress, LIB), Cint,
+                    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Cint, Ptr{Float64}, Cint, Ref{Ptr{Cvoid}}),
+                    ctx(), m.h, pat, C_NULL, Ce, law(energy), prm, length(prm), h))
+    end
+    return SystemMatrix(fetch(h[], 3problem.non), problem)
+end
+
+function internalForceVector(problem; P=nothing, F=nothing, energy=nothing, params=nothing)
+    @assert xor(P !== nothing, energy !== nothing)
+    m = device_mesh(problem)
+    f = zeros(3problem.non)
+    if P !== nothing
+        Pe = elementwise(LowLevelFEM.nodesToElements(P))
+        check(ccall((:llf_tl_internal_force, LIB), Cint,
+                    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Cint, Ptr{Float64}, Cint, Ptr{Float64}),
+                    ctx(), m.h, Pe, C_NULL, 0, C_NULL, 0, f))
+    else
+        Fe = elementwise(LowLevelFEM.nodesToElements(F)); prm = lawparams(params)
+        check(ccall((:llf_tl_internal_force, LIB), Cint,
+                    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Cint, Ptr{Float64}, Cint, Ptr{Float64}),
+                    ctx(), m.h, C_NULL, Fe, law(energy), prm, length(prm), f))
+    end
+    return VectorField([], reshape(f, :, 1), [0.0], [], 1, :v3D, problem)
+end
+
+# ---------------------------------------------------------------- solve
+# Condensed Dirichlet solve by PCG on the device (the iterative branch of
+# src/linear.jl:3827-3833).  K is re-uploaded from its CSC arrays through the
+# pattern of the problem; the prescribed values come from
+# applyBoundaryConditions!.
+function solveField(K::SystemMatrix, f; support=BoundaryCondition[], iterative=false,
+                    reltol=sqrt(eps()), maxiter=K.model.non * K.model.dim, preconditioner=nothing, ordering=true)
+    problem = K.model
+    n = problem.pdim * problem.non
+    u = copy(f); fill!(u.a, 0.0)
+    LowLevelFEM.applyBoundaryConditions!(u, support)
+    fixed = zeros(UInt8, n)
+    fixed[LowLevelFEM.constrainedDoFs(problem, support)] .= 1
+    hm = upload(K)
+    x = vec(u.a[:, 1]); its = Ref{Int64}(0); rr = Ref{Float64}(0.0)
+    prec = iterative ? (preconditioner === nothing ? 0 : 1) : 2
+    tol = iterative ? reltol : 1e-13
+    st = ccall((:llf_pcg, LIB), Cint,
+               (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{UInt8}, Cint, Float64, Int64, Ref{Int64}, Ref{Float64}),
+               ctx(), hm, vec(f.a[:, 1]), x, fixed, prec, tol, iterative ? maxiter : 20n, its, rr)
+    ccall((:llf_matrix_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), hm)
+    (st == 0 || (iterative && st == -4)) || check(st)
+    u.a[:, 1] .= x
+    return u
+end
+
+solveDisplacement(K::SystemMatrix, f; kw...) = solveField(K, f; kw...)
+
+function solveDisplacement(problem; load=LoadCondition[], support=BoundaryCondition[], kw...)
+    K = stiffnessMatrix(problem)
+    f = LowLevelFEM.loadVector(problem, load)
+    return solveField(K, f; support=support, kw...)
+end
+
+function solveTemperature(problem; heatFlux=LoadCondition[], temperatureConstraint=BoundaryCondition[], kw...)
+    K = heatConductionMatrix(problem)
+    q = LowLevelFEM.heatFluxVector(problem, heatFlux)
+    return solveField(K, q; support=temperatureConstraint, kw...)
+end
+
+# A host SystemMatrix re-enters the device through the structural pattern of
+# its problem: the values are scattered by row/column search on the host
+# side of Julia and uploaded as structural values.
+function upload(K::SystemMatrix)
+    problem = K.model
+    pat = pattern(problem)
+    nnz = Ref{Int64}(0); ndof = Ref{Int64}(0); pd = Ref{Cint}(0)
+    ccall((:llf_pattern_info, LIB), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}, Ref{Cint}), pat, ndof, nnz, pd)
+    colptr = Vector{Int64}(undef, ndof[] + 1); rowval = Vector{Int64}(undef, nnz[])
+    check(ccall((:llf_pattern_copy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Int64}, Ptr{Int64}), ctx(), pat, colptr, rowval))
+    S = SparseMatrixCSC(ndof[], ndof[], colptr, rowval, zeros(nnz[]))
+    A = K.A
+    for j in 1:size(A, 2), p in nzrange(A, j)
+        S[rowvals(A)[p], j] = nonzeros(A)[p]
+    end
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:llf_matrix_from_structural, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ref{Ptr{Cvoid}}),
+                ctx(), pat, nonzeros(S), h))
+    return h[]
+end
+
+end # module

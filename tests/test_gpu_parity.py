@@ -167,6 +167,30 @@ def test_load_vector_bit_identical(llf, orc):
     assert np.array_equal(f2.a[:, 0], ref2)
 
 
+PRECISION_CASES = [("rect", 5, 2, False, "PlaneStrain"), ("box", 3, 1, False, "Solid"),
+                   ("box", 3, 2, False, "Solid"), ("box", 2, 2, True, "Solid")]
+
+
+@pytest.mark.parametrize("case", PRECISION_CASES, ids=_ids)
+def test_precision_form_within_fp32_tolerance(llf, case):
+    """FP32 quadrature / FP64 accumulation: every structural value within
+    1e-6 of the column's largest FP64 value (FP32 has 6e-8 unit roundoff)."""
+    kind, n, order, simplex, ptype = case
+    make_mesh(llf, kind, n, order, simplex)
+    p = llf.Problem([llf.Material("body", E=2.1e5, nu=0.3)], type=ptype)
+    for op in ("stiffness", "mass", "heat"):
+        if op == "heat":
+            p = llf.Problem([llf.Material("body")], type="HeatConduction" if kind == "box" else "PlaneHeatConduction")
+            A64, A32 = llf.heatConductionMatrix(p), llf.heatConductionMatrix(p, precision="fp32")
+        elif op == "mass":
+            A64, A32 = llf.massMatrix(p, lumped=False), llf.massMatrix(p, lumped=False, precision="fp32")
+        else:
+            A64, A32 = llf.stiffnessMatrix(p), llf.stiffnessMatrix(p, precision="fp32")
+        v64, v32 = A64.dm.copy_structural(), A32.dm.copy_structural()
+        scale = np.abs(v64).max()
+        assert np.abs(v32 - v64).max() <= 1e-6 * scale, op
+
+
 # ---------------------------------------------------------------- error paths
 def test_inverted_element_is_an_error(llf):
     m = llf.structured_box_mesh(n=2, order=1)

@@ -68,7 +68,7 @@ def test_prescribed_nonzero_displacement(llf):
     """f_kin = K[:,fixed] u[fixed] path (src/linear.jl:3825): a prescribed
     uniform stretch gives a homogeneous field."""
     m = llf.structured_box_mesh(n=3, order=2)
-    P = llf.Problem([llf.Material("body", nu=0.0)], type="Solid")
+    P = llf.Problem([llf.Material("body", E=2e5, nu=0.0)], type="Solid")
     supp = [llf.displacementConstraint("left", ux=0.0),
             llf.displacementConstraint("right", ux=1e-3),
             llf.displacementConstraint("bottom", uy=0.0),
