@@ -95,6 +95,7 @@ def test_not_converged_reports(llf):
     sup = [llf.displacementConstraint("left", ux=0, uy=0, uz=0)]
     u = llf.solveDisplacement(K, f, support=sup, iterative=True, maxiter=3)
     assert u.iterations == 3 and u.relres > 1e-3
+    fixed = np.zeros(K.shape[0], np.uint8)
+    fixed[llf.constrainedDoFs(P, sup) - 1] = 1
     with pytest.raises(llf.LLFError, match="not converged"):
-        K.dm.pcg(f.a[:, 0], np.zeros(K.shape[0]), np.zeros(K.shape[0], np.uint8) | 0, maxiter=3,
-                 reltol=1e-12, raise_on_fail=True)
+        K.dm.pcg(f.a[:, 0], np.zeros(K.shape[0]), fixed, maxiter=3, reltol=1e-12, raise_on_fail=True)
