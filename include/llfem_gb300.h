@@ -322,6 +322,18 @@ int llf_pcg(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x,
             const uint8_t *fixed, int precond, double reltol, int64_t maxiter,
             int64_t *iters, double *relres);
 
+/* Batched form of llf_pcg for a block-diagonal matrix of nseg independent
+ * systems (for example many meshes assembled together as one mesh with one
+ * material per instance): system g owns DoFs [seg_off[g], seg_off[g+1]).
+ * Every system runs its own CG — own scalars and stopping test, exactly as a
+ * separate llf_pcg call would — inside the same kernel launches, replayed
+ * from a captured CUDA graph.  iters[nseg] and relres[nseg] are per system.
+ * Replaces a loop of solveField calls (src/poisson.jl:1432-1546). */
+int llf_pcg_batched(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x,
+                    const uint8_t *fixed, int nseg, const int64_t *seg_off,
+                    int precond, double reltol, int64_t maxiter, int64_t *iters,
+                    double *relres);
+
 #ifdef __cplusplus
 }
 #endif

@@ -10,12 +10,12 @@ module ``llfem_gb300``.
 from . import _lib
 from ._lib import LLFError, Context, default_context
 from .mesh import (Mesh, Group, structured_rect_mesh, structured_box_mesh, read_msh,
-                   current_mesh, set_current, node_lattice, LINE, TRI, QUAD, TET, HEX)
+                   current_mesh, set_current, node_lattice, concat_meshes, LINE, TRI, QUAD, TET, HEX)
 from .api import (Material, material, elastic_constants, Problem, Field, SystemMatrix, VectorField,
                   ScalarField, TensorField, BoundaryCondition, LoadCondition, displacementConstraint,
                   temperatureConstraint, load, heatFlux, constrainedDoFs, allDoFs, freeDoFs,
                   applyBoundaryConditions_, loadVector, stiffnessMatrix, massMatrix,
-                  heatConductionMatrix, solveDisplacement, solveTemperature, solveField, grad,
+                  heatConductionMatrix, solveDisplacement, solveTemperature, solveField, solveFieldBatched, grad,
                   deformationGradient, materialTangentMatrix, initialStressMatrix,
                   internalForceVector)
 

@@ -541,6 +541,34 @@ def solveField(K: SystemMatrix, f, support=(), iterative=False, reltol=SQRT_EPS,
     return _solve(K, f, list(support), iterative, reltol, maxiter, preconditioner)
 
 
+def solveFieldBatched(K: SystemMatrix, f, support=(), node_offsets=None, iterative=True, reltol=SQRT_EPS,
+                      maxiter=None, preconditioner="jacobi"):
+    """Many independent systems at once: K is the block-diagonal matrix of a
+    batch (concat_meshes), instance i owning nodes node_offsets[i]..[i+1]-1.
+    Every instance runs its own CG (own scalars and stopping rule) inside the
+    same launches; instance i's result is bit-identical to solving it alone.
+    Returns the field and per-instance iteration counts / residuals."""
+    problem = K.model
+    if node_offsets is None:
+        raise ValueError("solveFieldBatched: node_offsets required")
+    u = _field_for(problem, np.zeros(problem.pdim * problem.non))
+    applyBoundaryConditions_(u, list(support))
+    fixed = np.zeros(problem.pdim * problem.non, dtype=np.uint8)
+    cd = constrainedDoFs(problem, list(support))
+    fixed[cd - 1] = 1
+    fa = f.a[:, 0] if hasattr(f, "a") else np.asarray(f, dtype=np.float64)
+    prec = _PRECOND[preconditioner.lower() if isinstance(preconditioner, str) else preconditioner]
+    if not iterative:
+        prec, reltol = _lib.PRECOND_BJACOBI, DIRECT_RELTOL
+    seg = np.asarray(node_offsets, dtype=np.int64) * problem.pdim
+    maxiter = problem.non * problem.dim if maxiter is None else maxiter
+    x, its, rr = K.dm.pcg_batched(fa, u.a[:, 0], fixed, seg, precond=prec, reltol=reltol, maxiter=maxiter,
+                                  raise_on_fail=not iterative)
+    u.a[:, 0] = x
+    u.iterations, u.relres = its, rr
+    return u
+
+
 # --------------------------------------------------------------------------
 # Total Lagrangian
 # --------------------------------------------------------------------------

@@ -742,4 +742,38 @@ int llf_pcg(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x, const
   return rc == LLF_OK ? llf_ok(ctx) : rc;
 }
 
+int llf_pcg_batched(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x, const uint8_t *fixed,
+                    int nseg, const int64_t *seg_off, int precond, double reltol, int64_t maxiter,
+                    int64_t *iters, double *relres) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!m || !b || !x || !fixed || !seg_off || !iters || !relres || nseg < 1)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched: null argument or nseg < 1");
+  if (precond < LLF_PRECOND_NONE || precond > LLF_PRECOND_BJACOBI)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched: unknown preconditioner");
+  const int64_t n = m->pat->ndof;
+  if (seg_off[0] != 0 || seg_off[nseg] != n)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched: seg_off must run from 0 to the DoF count");
+  for (int g = 0; g < nseg; ++g)
+    if (seg_off[g + 1] < seg_off[g] || (seg_off[g] % m->pat->pdim) != 0)
+      return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched: seg_off must be non-decreasing node boundaries");
+  double *db = nullptr, *dx = nullptr;
+  uint8_t *df = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &db, n));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &dx, n));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &df, n));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(db, b, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(df, fixed, n, cudaMemcpyHostToDevice, ctx->stream));
+  int rc = pcg_batched_impl(ctx, m, db, dx, df, nseg, seg_off, precond, reltol, maxiter, iters, relres);
+  if (rc == LLF_OK || rc == LLF_ERR_NOT_CONVERGED) {
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    LLF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  dfree(ctx, db);
+  dfree(ctx, dx);
+  dfree(ctx, df);
+  cudaStreamSynchronize(ctx->stream);
+  return rc == LLF_OK ? llf_ok(ctx) : rc;
+}
+
 }  // extern "C"

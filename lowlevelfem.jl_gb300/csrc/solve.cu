@@ -1,4 +1,4 @@
-// Sparse matrix-vector product and preconditioned CG.
+// Sparse matrix-vector product and (batched) preconditioned CG.
 //
 // SpMV works on the structural node-block CSC: column c = P*B + j is the
 // contiguous run nz[colptr[c] .. colptr[c+1]) whose k-th entry sits in row
@@ -15,20 +15,29 @@
 // ||r|| <= reltol*||r0|| or after maxiter products.  Dirichlet elimination
 // (K[free,free], f_kin = K[:,fixed] u[fixed], src/linear.jl:3819-3826) is done
 // by masking: search directions and products are zeroed on fixed DoFs.
-// Scalars live on the device; every reduction is two-stage with a fixed
-// order (per-block partials, then one block), so the iteration is
-// deterministic.  The host enqueues iterations in chunks and polls a
-// device "done" flag between chunks; iterations after convergence are no-ops,
-// so the stopping iteration is exactly IterativeSolvers'.
+//
+// Batched form: the system is block diagonal with nseg independent
+// segments (instances assembled together on one pattern, e.g. many meshes
+// of one batch).  Every segment runs its own CG — own scalars, own stopping
+// test — inside the same launches.  DoFs are cut into fixed chunks that never
+// straddle a segment; every reduction is per chunk (block tree), then per
+// segment over its chunks in order, so results do not depend on the launch
+// shape or on what else is in the batch.  One CG iteration is seven
+// launches; the host captures a run of iterations into a CUDA graph once and
+// replays it, polling the count of still-active segments between replays.
+// Iterations after a segment converged are no-ops for that segment, so every
+// segment stops exactly where IterativeSolvers would.
 #include "common.cuh"
 
+#include <algorithm>
 #include <cmath>
 
 namespace {
 
 constexpr int CG_THREADS = 256;
+constexpr int CHUNK = 4096;  // DoFs per reduction chunk
 
-struct CGState {
+struct SegState {
   double rho_prev, rho, alpha, res, res0, tol;
   long long it, maxiter;
   int done, breakdown;
@@ -56,16 +65,13 @@ __device__ __forceinline__ double block_sum(double v) {
   return r;
 }
 
-template <int P, bool MASK, bool DOT>
+// y = A x for all columns (plain product, llf_matrix_spmv).
+template <int P>
 __global__ void __launch_bounds__(CG_THREADS)
 k_spmv(const double *__restrict__ nz, const int64_t *__restrict__ colptr,
        const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
-       const double *__restrict__ x, const uint8_t *__restrict__ fixed,
-       double *__restrict__ y, int64_t ndof, double *__restrict__ partial,
-       const CGState *st) {
-  if (st && st->done) return;
+       const double *__restrict__ x, double *__restrict__ y, int64_t ndof) {
   const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-  double dot = 0.0;
   for (int64_t c = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5); c < ndof;
        c += (int64_t)gridDim.x * wpb) {
     const int64_t s = colptr[c], e = colptr[c + 1];
@@ -73,19 +79,10 @@ k_spmv(const double *__restrict__ nz, const int64_t *__restrict__ colptr,
     double acc = 0.0;
     for (int64_t k = s + lane; k < e; k += 32) {
       const int64_t loc = k - s;
-      const int64_t row = (int64_t)P * nadj[r0 + loc / P] + loc % P;
-      acc = __fma_rn(nz[k], x[row], acc);
+      acc = __fma_rn(nz[k], x[(int64_t)P * nadj[r0 + loc / P] + loc % P], acc);
     }
     acc = warp_sum(acc);
-    if (MASK && fixed[c]) acc = 0.0;
-    if (lane == 0) {
-      y[c] = acc;
-      if (DOT) dot = __fma_rn(x[c], acc, dot);
-    }
-  }
-  if (DOT) {
-    double b = block_sum(dot);
-    if (threadIdx.x == 0) partial[blockIdx.x] = b;
+    if (lane == 0) y[c] = acc;
   }
 }
 
@@ -120,14 +117,13 @@ __global__ void k_precond_setup(const double *__restrict__ nz, const int64_t *__
           for (int j = 0; j < P; ++j) { D[i][j] = 0.0; D[j][i] = 0.0; }
           D[i][i] = 1.0;
         }
-      // Gauss-Jordan with partial pivoting
       double Inv[P][P];
 #pragma unroll
       for (int i = 0; i < P; ++i)
 #pragma unroll
         for (int j = 0; j < P; ++j) Inv[i][j] = (i == j) ? 1.0 : 0.0;
       bool ok = true;
-      for (int k = 0; k < P; ++k) {
+      for (int k = 0; k < P; ++k) {  // Gauss-Jordan with partial pivoting
         int piv = k;
         for (int i = k + 1; i < P; ++i)
           if (fabs(D[i][k]) > fabs(D[piv][k])) piv = i;
@@ -163,7 +159,6 @@ __global__ void k_precond_setup(const double *__restrict__ nz, const int64_t *__
   }
 }
 
-// z = Pl \ r on free DoFs (0 on fixed) and the partial sums of z.r and r.r.
 template <int P>
 __device__ __forceinline__ double apply_prec(const double *__restrict__ pinv, int mode,
                                              const double *__restrict__ r, int64_t c) {
@@ -178,128 +173,179 @@ __device__ __forceinline__ double apply_prec(const double *__restrict__ pinv, in
   return __dmul_rn(pinv[c], r[c]);
 }
 
-// r = fixed ? 0 : b - y; x = 0; u = 0; z = Pl\r; partials (z.r, r.r).
-template <int P>
+// ---------------------------------------------------------------- batched CG
+struct Seg {
+  const int64_t *cbeg, *cend;  // per chunk DoF range
+  const int32_t *cseg;         // per chunk segment
+  const int64_t *sfirst;       // per segment first chunk (nseg+1)
+  int64_t nchunks;
+  int nseg;
+  SegState *st;
+  int *active;
+};
+
+// y = fixed ? 0 : b - A x_c; r = y; x = 0; u = 0; partial r.r per chunk.
 __global__ void __launch_bounds__(CG_THREADS)
-k_cg_init(const double *__restrict__ b, const double *__restrict__ y,
-          const uint8_t *__restrict__ fixed, double *__restrict__ r, double *__restrict__ xw,
-          double *__restrict__ u, int64_t n, double *__restrict__ part_zr,
-          double *__restrict__ part_rr) {
-  double rr = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    double ri = fixed[i] ? 0.0 : __dsub_rn(b[i], y[i]);
-    r[i] = ri;
-    xw[i] = 0.0;
-    u[i] = 0.0;
-    rr = __fma_rn(ri, ri, rr);
+k_seg_init(Seg S, const double *__restrict__ b, const double *__restrict__ y,
+           const uint8_t *__restrict__ fixed, double *__restrict__ r, double *__restrict__ xw,
+           double *__restrict__ u, double *__restrict__ part) {
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    double rr = 0.0;
+    for (int64_t i = S.cbeg[ch] + threadIdx.x; i < S.cend[ch]; i += blockDim.x) {
+      double ri = fixed[i] ? 0.0 : __dsub_rn(b[i], y[i]);
+      r[i] = ri;
+      xw[i] = 0.0;
+      u[i] = 0.0;
+      rr = __fma_rn(ri, ri, rr);
+    }
+    double s = block_sum(rr);
+    if (threadIdx.x == 0) part[ch] = s;
   }
-  double s = block_sum(rr);
-  if (threadIdx.x == 0) part_rr[blockIdx.x] = s;
-  (void)part_zr;
 }
 
-template <int P>
-__global__ void __launch_bounds__(CG_THREADS)
-k_cg_prec(const double *__restrict__ pinv, int mode, const double *__restrict__ r,
-          const uint8_t *__restrict__ fixed, double *__restrict__ z, int64_t n,
-          double *__restrict__ part_zr, const CGState *st) {
-  if (st->done) return;
-  double zr = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    double zi = fixed[i] ? 0.0 : apply_prec<P>(pinv, mode, r, i);
-    z[i] = zi;
-    zr = __fma_rn(zi, r[i], zr);
-  }
-  double s = block_sum(zr);
-  if (threadIdx.x == 0) part_zr[blockIdx.x] = s;
-}
-
-__device__ __forceinline__ double sum_partials(const double *p, int n) {
+__device__ __forceinline__ double seg_total(const Seg &S, int s, const double *part) {
   double v = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) v = __dadd_rn(v, p[i]);
+  for (int64_t ch = S.sfirst[s] + threadIdx.x; ch < S.sfirst[s + 1]; ch += blockDim.x) v = __dadd_rn(v, part[ch]);
   return block_sum(v);
 }
 
-// Single block: initial residual and tolerance.
-__global__ void k_cg_start(const double *part_rr, int np, double reltol, long long maxiter,
-                           CGState *st) {
-  double rr = sum_partials(part_rr, np);
-  if (threadIdx.x == 0) {
-    st->res0 = sqrt(rr);
-    st->res = st->res0;
-    st->tol = reltol * st->res0;
-    st->rho_prev = 1.0;
-    st->rho = 0.0;
-    st->alpha = 0.0;
-    st->it = 0;
-    st->maxiter = maxiter;
-    st->breakdown = 0;
-    st->done = (st->res <= st->tol) || (maxiter <= 0);
-  }
-}
-
-// Single block: rho = z.r of this iteration.
-__global__ void k_cg_rho(const double *part_zr, int np, CGState *st) {
-  if (st->done) return;
-  double zr = sum_partials(part_zr, np);
-  if (threadIdx.x == 0) st->rho = zr;
-}
-
-// u = z + (rho/rho_prev) u
-__global__ void k_cg_dir(const double *__restrict__ z, double *__restrict__ u, int64_t n,
-                         const CGState *st) {
-  if (st->done) return;
-  const double beta = st->rho / st->rho_prev;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    u[i] = __fma_rn(beta, u[i], z[i]);
-}
-
-// Single block: alpha = rho / (u.Au)
-__global__ void k_cg_alpha(const double *part_uc, int np, CGState *st) {
-  if (st->done) return;
-  double uc = sum_partials(part_uc, np);
-  if (threadIdx.x == 0) {
-    if (!(uc > 0.0) || !isfinite(uc)) {
-      st->breakdown = 1;
-      st->done = 1;
-      st->alpha = 0.0;
-    } else {
-      st->alpha = st->rho / uc;
+__global__ void k_seg_start(Seg S, const double *part, double reltol, long long maxiter) {
+  for (int s = blockIdx.x; s < S.nseg; s += gridDim.x) {
+    double rr = seg_total(S, s, part);
+    if (threadIdx.x == 0) {
+      SegState &q = S.st[s];
+      q.res0 = sqrt(rr);
+      q.res = q.res0;
+      q.tol = reltol * q.res0;
+      q.rho_prev = 1.0;
+      q.rho = 0.0;
+      q.alpha = 0.0;
+      q.it = 0;
+      q.maxiter = maxiter;
+      q.breakdown = 0;
+      q.done = (q.res <= q.tol) || (maxiter <= 0);
+      if (!q.done) atomicAdd(S.active, 1);
     }
   }
 }
 
-// x += alpha u; r -= alpha c; partial r.r
+template <int P>
 __global__ void __launch_bounds__(CG_THREADS)
-k_cg_update(double *__restrict__ xw, double *__restrict__ r, const double *__restrict__ u,
-            const double *__restrict__ c, int64_t n, double *__restrict__ part_rr,
-            const CGState *st) {
-  if (st->done) return;
-  const double alpha = st->alpha;
-  double rr = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    xw[i] = __fma_rn(alpha, u[i], xw[i]);
-    double ri = __fma_rn(-alpha, c[i], r[i]);
-    r[i] = ri;
-    rr = __fma_rn(ri, ri, rr);
+k_seg_prec(Seg S, const double *__restrict__ pinv, int mode, const double *__restrict__ r,
+           const uint8_t *__restrict__ fixed, double *__restrict__ z, double *__restrict__ part) {
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    if (S.st[S.cseg[ch]].done) continue;
+    double zr = 0.0;
+    for (int64_t i = S.cbeg[ch] + threadIdx.x; i < S.cend[ch]; i += blockDim.x) {
+      double zi = fixed[i] ? 0.0 : apply_prec<P>(pinv, mode, r, i);
+      z[i] = zi;
+      zr = __fma_rn(zi, r[i], zr);
+    }
+    double s = block_sum(zr);
+    if (threadIdx.x == 0) part[ch] = s;
   }
-  double s = block_sum(rr);
-  if (threadIdx.x == 0) part_rr[blockIdx.x] = s;
 }
 
-// Single block: residual norm, iteration count, stopping test.
-__global__ void k_cg_finish(const double *part_rr, int np, CGState *st) {
-  if (st->done) return;
-  double rr = sum_partials(part_rr, np);
-  if (threadIdx.x == 0) {
-    st->res = sqrt(rr);
-    st->rho_prev = st->rho;
-    st->it += 1;
-    if (st->res <= st->tol || st->it >= st->maxiter) st->done = 1;
+__global__ void k_seg_rho(Seg S, const double *part) {
+  for (int s = blockIdx.x; s < S.nseg; s += gridDim.x) {
+    if (S.st[s].done) continue;
+    double v = seg_total(S, s, part);
+    if (threadIdx.x == 0) S.st[s].rho = v;
+  }
+}
+
+__global__ void k_seg_dir(Seg S, const double *__restrict__ z, double *__restrict__ u) {
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    const SegState &q = S.st[S.cseg[ch]];
+    if (q.done) continue;
+    const double beta = q.rho / q.rho_prev;
+    for (int64_t i = S.cbeg[ch] + threadIdx.x; i < S.cend[ch]; i += blockDim.x)
+      u[i] = __fma_rn(beta, u[i], z[i]);
+  }
+}
+
+// c = A u on the chunk's columns (masked) and partial u.c.
+template <int P>
+__global__ void __launch_bounds__(CG_THREADS)
+k_seg_spmv(Seg S, const double *__restrict__ nz, const int64_t *__restrict__ colptr,
+           const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
+           const double *__restrict__ u, const uint8_t *__restrict__ fixed,
+           double *__restrict__ c, double *__restrict__ part) {
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, w = threadIdx.x >> 5;
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    if (S.st[S.cseg[ch]].done) continue;
+    double dot = 0.0;
+    for (int64_t col = S.cbeg[ch] + w; col < S.cend[ch]; col += wpb) {
+      const int64_t s = colptr[col], e = colptr[col + 1];
+      const int64_t r0 = nptr[col / P];
+      double acc = 0.0;
+      for (int64_t k = s + lane; k < e; k += 32) {
+        const int64_t loc = k - s;
+        acc = __fma_rn(nz[k], u[(int64_t)P * nadj[r0 + loc / P] + loc % P], acc);
+      }
+      acc = warp_sum(acc);
+      if (fixed[col]) acc = 0.0;
+      if (lane == 0) {
+        c[col] = acc;
+        dot = __fma_rn(u[col], acc, dot);
+      }
+    }
+    double s = block_sum(dot);
+    if (threadIdx.x == 0) part[ch] = s;
+  }
+}
+
+__global__ void k_seg_alpha(Seg S, const double *part) {
+  for (int s = blockIdx.x; s < S.nseg; s += gridDim.x) {
+    if (S.st[s].done) continue;
+    double uc = seg_total(S, s, part);
+    if (threadIdx.x == 0) {
+      SegState &q = S.st[s];
+      if (!(uc > 0.0) || !isfinite(uc)) {
+        q.breakdown = 1;
+        q.done = 1;
+        q.alpha = 0.0;
+        atomicSub(S.active, 1);
+      } else {
+        q.alpha = q.rho / uc;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(CG_THREADS)
+k_seg_update(Seg S, double *__restrict__ xw, double *__restrict__ r, const double *__restrict__ u,
+             const double *__restrict__ c, double *__restrict__ part) {
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    const SegState &q = S.st[S.cseg[ch]];
+    if (q.done) continue;
+    const double alpha = q.alpha;
+    double rr = 0.0;
+    for (int64_t i = S.cbeg[ch] + threadIdx.x; i < S.cend[ch]; i += blockDim.x) {
+      xw[i] = __fma_rn(alpha, u[i], xw[i]);
+      double ri = __fma_rn(-alpha, c[i], r[i]);
+      r[i] = ri;
+      rr = __fma_rn(ri, ri, rr);
+    }
+    double s = block_sum(rr);
+    if (threadIdx.x == 0) part[ch] = s;
+  }
+}
+
+__global__ void k_seg_finish(Seg S, const double *part) {
+  for (int s = blockIdx.x; s < S.nseg; s += gridDim.x) {
+    if (S.st[s].done) continue;
+    double rr = seg_total(S, s, part);
+    if (threadIdx.x == 0) {
+      SegState &q = S.st[s];
+      q.res = sqrt(rr);
+      q.rho_prev = q.rho;
+      q.it += 1;
+      if (q.res <= q.tol || q.it >= q.maxiter) {
+        q.done = 1;
+        atomicSub(S.active, 1);
+      }
+    }
   }
 }
 
@@ -317,85 +363,144 @@ __global__ void k_keep_fixed(const double *__restrict__ x, const uint8_t *__rest
     xc[i] = fixed[i] ? x[i] : 0.0;
 }
 
-template <int P, bool MASK, bool DOT>
-void launch_spmv(llf_ctx *ctx, const llf_matrix *m, const double *x, const uint8_t *fixed,
-                 double *y, double *partial, const CGState *st, unsigned grid) {
+template <int P>
+void enqueue_iteration(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const double *pinv, int precond,
+                       double *r, double *z, double *u, double *c, double *xw, const uint8_t *fixed,
+                       double *part, unsigned gch, unsigned gseg) {
   const llf_pattern *pat = m->pat;
-  KernelScope ks(ctx, "k_spmv");
-  k_spmv<P, MASK, DOT><<<grid, CG_THREADS, 0, ctx->stream>>>(
-      m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, x, fixed, y, pat->ndof, partial, st);
+  cudaStream_t s = ctx->stream;
+  { KernelScope k(ctx, "k_seg_prec"); k_seg_prec<P><<<gch, CG_THREADS, 0, s>>>(S, pinv, precond, r, fixed, z, part); }
+  { KernelScope k(ctx, "k_seg_rho"); k_seg_rho<<<gseg, CG_THREADS, 0, s>>>(S, part); }
+  { KernelScope k(ctx, "k_seg_dir"); k_seg_dir<<<gch, CG_THREADS, 0, s>>>(S, z, u); }
+  { KernelScope k(ctx, "k_seg_spmv");
+    k_seg_spmv<P><<<gch, CG_THREADS, 0, s>>>(S, m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, u, fixed, c, part); }
+  { KernelScope k(ctx, "k_seg_alpha"); k_seg_alpha<<<gseg, CG_THREADS, 0, s>>>(S, part); }
+  { KernelScope k(ctx, "k_seg_update"); k_seg_update<<<gch, CG_THREADS, 0, s>>>(S, xw, r, u, c, part); }
+  { KernelScope k(ctx, "k_seg_finish"); k_seg_finish<<<gseg, CG_THREADS, 0, s>>>(S, part); }
 }
 
 template <int P>
-int pcg_typed(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
-              const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
-              int64_t *iters, double *relres) {
+int pcg_segments(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
+                 const uint8_t *d_fixed, int nseg, const int64_t *seg_off, int precond,
+                 double reltol, int64_t maxiter, int64_t *iters, double *relres) {
   const llf_pattern *pat = m->pat;
   const int64_t n = pat->ndof;
   cudaStream_t s = ctx->stream;
-  const unsigned grid = (unsigned)(ctx->num_sms * 4);
-  double *r, *z, *u, *c, *xw, *pinv, *part_a, *part_b;
-  CGState *st;
+  // chunks that never straddle a segment
+  std::vector<int64_t> cb, ce, sf(nseg + 1);
+  std::vector<int32_t> cs;
+  for (int g = 0; g < nseg; ++g) {
+    sf[g] = (int64_t)cb.size();
+    for (int64_t i = seg_off[g]; i < seg_off[g + 1]; i += CHUNK) {
+      cb.push_back(i);
+      ce.push_back(std::min(i + CHUNK, seg_off[g + 1]));
+      cs.push_back(g);
+    }
+  }
+  sf[nseg] = (int64_t)cb.size();
+  const int64_t nch = (int64_t)cb.size();
+  int64_t *d_cb, *d_ce, *d_sf;
+  int32_t *d_cs;
+  int *d_active;
+  SegState *d_st;
+  double *r, *z, *u, *c, *xw, *pinv, *part;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_cb, nch));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_ce, nch));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_cs, nch));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_sf, nseg + 1));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_active, 1));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_st, nseg));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &r, n));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &z, n));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &u, n));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &c, n));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &xw, n));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &pinv, precond == LLF_PRECOND_BJACOBI ? n * P : n));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &part_a, grid));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &part_b, grid));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &st, 1));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &part, nch));
+  if (nch) {
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_cb, cb.data(), sizeof(int64_t) * nch, cudaMemcpyHostToDevice, s));
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_ce, ce.data(), sizeof(int64_t) * nch, cudaMemcpyHostToDevice, s));
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_cs, cs.data(), sizeof(int32_t) * nch, cudaMemcpyHostToDevice, s));
+  }
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_sf, sf.data(), sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, s));
+  LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_active, 0, sizeof(int), s));
+  Seg S{d_cb, d_ce, d_cs, d_sf, nch, nseg, d_st, d_active};
+  const unsigned gch = (unsigned)std::max<int64_t>(1, std::min<int64_t>(nch, (int64_t)ctx->num_sms * 8));
+  const unsigned gseg = (unsigned)std::max(1, std::min(nseg, ctx->num_sms * 8));
+  const unsigned gv = (unsigned)(ctx->num_sms * 4);
 
-  { KernelScope ks_(ctx, "k_precond_setup");
-
-  k_precond_setup<P><<<(unsigned)((pat->mesh->non + 127) / 128), 128, 0, s>>>(
-      m->d_nz, pat->d_colptr, pat->d_diagpos, d_fixed, pat->mesh->non, precond, pinv); }
-  // f_kin = A x_c
-  { KernelScope ks_(ctx, "k_keep_fixed");
-  k_keep_fixed<<<grid, CG_THREADS, 0, s>>>(d_x, d_fixed, xw, n); }
-  launch_spmv<P, false, false>(ctx, m, xw, d_fixed, c, nullptr, nullptr, grid);
-  { KernelScope ks_(ctx, "k_cg_init");
-  k_cg_init<P><<<grid, CG_THREADS, 0, s>>>(d_b, c, d_fixed, r, xw, u, n, part_a, part_b); }
-  { KernelScope ks_(ctx, "k_cg_start");
-  k_cg_start<<<1, CG_THREADS, 0, s>>>(part_b, (int)grid, reltol, (long long)maxiter, st); }
+  { KernelScope k(ctx, "k_precond_setup");
+    k_precond_setup<P><<<(unsigned)((pat->mesh->non + 127) / 128), 128, 0, s>>>(
+        m->d_nz, pat->d_colptr, pat->d_diagpos, d_fixed, pat->mesh->non, precond, pinv); }
+  { KernelScope k(ctx, "k_keep_fixed"); k_keep_fixed<<<gv, CG_THREADS, 0, s>>>(d_x, d_fixed, xw, n); }
+  { KernelScope k(ctx, "k_spmv"); k_spmv<P><<<gv, CG_THREADS, 0, s>>>(m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, xw, c, n); }
+  { KernelScope k(ctx, "k_seg_init"); k_seg_init<<<gch, CG_THREADS, 0, s>>>(S, d_b, c, d_fixed, r, xw, u, part); }
+  { KernelScope k(ctx, "k_seg_start"); k_seg_start<<<gseg, CG_THREADS, 0, s>>>(S, part, reltol, (long long)maxiter); }
   LLF_CUDA_TRY(ctx, cudaGetLastError());
 
-  CGState hst{};
-  const int chunk = 16;
-  for (;;) {
-    for (int k = 0; k < chunk; ++k) {
-      { KernelScope ks_(ctx, "k_cg_prec");
-      k_cg_prec<P><<<grid, CG_THREADS, 0, s>>>(pinv, precond, r, d_fixed, z, n, part_a, st); }
-      { KernelScope ks_(ctx, "k_cg_rho");
-      k_cg_rho<<<1, CG_THREADS, 0, s>>>(part_a, (int)grid, st); }
-      { KernelScope ks_(ctx, "k_cg_dir");
-      k_cg_dir<<<grid, CG_THREADS, 0, s>>>(z, u, n, st); }
-      launch_spmv<P, true, true>(ctx, m, u, d_fixed, c, part_b, st, grid);
-      { KernelScope ks_(ctx, "k_cg_alpha");
-      k_cg_alpha<<<1, CG_THREADS, 0, s>>>(part_b, (int)grid, st); }
-      { KernelScope ks_(ctx, "k_cg_update");
-      k_cg_update<<<grid, CG_THREADS, 0, s>>>(xw, r, u, c, n, part_a, st); }
-      { KernelScope ks_(ctx, "k_cg_finish");
-      k_cg_finish<<<1, CG_THREADS, 0, s>>>(part_a, (int)grid, st); }
+  // capture a run of iterations once, replay until every segment is done
+  const int per_graph = 16;
+  cudaGraphExec_t exec = nullptr;
+  bool graph_ok = !ctx->profiling;
+  if (graph_ok) {
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const long long saved = ctx->launches;
+      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, gch, gseg);
+      ctx->launches = saved;
+      if (cudaStreamEndCapture(s, &graph) != cudaSuccess ||
+          cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+        graph_ok = false;
+      if (graph) cudaGraphDestroy(graph);
+    } else {
+      graph_ok = false;
+    }
+    cudaGetLastError();
+  }
+  int active = 1;
+  int *h_active = (int *)ctx->h_status;  // pinned word, free between status checks
+  while (active > 0) {
+    if (graph_ok) {
+      LLF_CUDA_TRY(ctx, cudaGraphLaunch(exec, s));
+      ctx->launches += 7LL * per_graph;
+    } else {
+      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, gch, gseg);
     }
     LLF_CUDA_TRY(ctx, cudaGetLastError());
-    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&hst, st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(h_active, d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
     LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
-    if (hst.done) break;
+    active = *h_active;
   }
-  { KernelScope ks_(ctx, "k_cg_merge");
-  k_cg_merge<<<grid, CG_THREADS, 0, s>>>(xw, d_fixed, d_x, n); }
+  *h_active = 0;
+  if (exec) cudaGraphExecDestroy(exec);
+  { KernelScope k(ctx, "k_cg_merge"); k_cg_merge<<<gv, CG_THREADS, 0, s>>>(xw, d_fixed, d_x, n); }
   LLF_CUDA_TRY(ctx, cudaGetLastError());
-  dfree(ctx, r); dfree(ctx, z); dfree(ctx, u); dfree(ctx, c); dfree(ctx, xw);
-  dfree(ctx, pinv); dfree(ctx, part_a); dfree(ctx, part_b); dfree(ctx, st);
-  *iters = hst.it;
-  *relres = hst.res0 > 0 ? hst.res / hst.res0 : 0.0;
-  if (hst.breakdown)
-    return llf_fail(ctx, LLF_ERR_NUMERIC, "pcg: breakdown (u.Au <= 0): matrix not positive definite on the free DoFs");
-  if (!(hst.res <= hst.tol))
-    return llf_fail(ctx, LLF_ERR_NOT_CONVERGED,
-                    "pcg: not converged after " + std::to_string(hst.it) +
-                        " iterations, relative residual " + std::to_string(*relres));
+  std::vector<SegState> hst(nseg);
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(hst.data(), d_st, sizeof(SegState) * nseg, cudaMemcpyDeviceToHost, s));
+  LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  dfree(ctx, d_cb); dfree(ctx, d_ce); dfree(ctx, d_cs); dfree(ctx, d_sf); dfree(ctx, d_active);
+  dfree(ctx, d_st); dfree(ctx, r); dfree(ctx, z); dfree(ctx, u); dfree(ctx, c); dfree(ctx, xw);
+  dfree(ctx, pinv); dfree(ctx, part);
+  int rc = LLF_OK;
+  int worst = -1;
+  for (int g = 0; g < nseg; ++g) {
+    iters[g] = hst[g].it;
+    relres[g] = hst[g].res0 > 0 ? hst[g].res / hst[g].res0 : 0.0;
+    if (hst[g].breakdown) {
+      rc = LLF_ERR_NUMERIC;
+      worst = g;
+    } else if (!(hst[g].res <= hst[g].tol) && rc == LLF_OK) {
+      rc = LLF_ERR_NOT_CONVERGED;
+      worst = g;
+    }
+  }
+  if (rc == LLF_ERR_NUMERIC)
+    return llf_fail(ctx, rc, "pcg: breakdown (u.Au <= 0) in system " + std::to_string(worst) +
+                                 ": matrix not positive definite on the free DoFs");
+  if (rc == LLF_ERR_NOT_CONVERGED)
+    return llf_fail(ctx, rc, "pcg: not converged after " + std::to_string(iters[worst]) +
+                                 " iterations (system " + std::to_string(worst) + "), relative residual " +
+                                 std::to_string(relres[worst]));
   return LLF_OK;
 }
 
@@ -408,10 +513,12 @@ int spmv_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_x, double *d_y)
     KernelScope ks(ctx, "k_diag_scale");
     k_diag_scale<<<grid, CG_THREADS, 0, ctx->stream>>>(m->d_diag, d_x, d_y, n);
   } else {
-    switch (m->pat->pdim) {
-      case 1: launch_spmv<1, false, false>(ctx, m, d_x, nullptr, d_y, nullptr, nullptr, grid); break;
-      case 2: launch_spmv<2, false, false>(ctx, m, d_x, nullptr, d_y, nullptr, nullptr, grid); break;
-      case 3: launch_spmv<3, false, false>(ctx, m, d_x, nullptr, d_y, nullptr, nullptr, grid); break;
+    KernelScope ks(ctx, "k_spmv");
+    const llf_pattern *p = m->pat;
+    switch (p->pdim) {
+      case 1: k_spmv<1><<<grid, CG_THREADS, 0, ctx->stream>>>(m->d_nz, p->d_colptr, p->d_nptr, p->d_nadj, d_x, d_y, n); break;
+      case 2: k_spmv<2><<<grid, CG_THREADS, 0, ctx->stream>>>(m->d_nz, p->d_colptr, p->d_nptr, p->d_nadj, d_x, d_y, n); break;
+      case 3: k_spmv<3><<<grid, CG_THREADS, 0, ctx->stream>>>(m->d_nz, p->d_colptr, p->d_nptr, p->d_nadj, d_x, d_y, n); break;
       default: return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
     }
   }
@@ -419,15 +526,22 @@ int spmv_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_x, double *d_y)
   return LLF_OK;
 }
 
-int pcg_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
-             const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
-             int64_t *iters, double *relres) {
+int pcg_batched_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
+                     const uint8_t *d_fixed, int nseg, const int64_t *seg_off, int precond,
+                     double reltol, int64_t maxiter, int64_t *iters, double *relres) {
   if (m->diagonal_only)
     return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pcg on a lumped (diagonal) matrix");
   switch (m->pat->pdim) {
-    case 1: return pcg_typed<1>(ctx, m, d_b, d_x, d_fixed, precond, reltol, maxiter, iters, relres);
-    case 2: return pcg_typed<2>(ctx, m, d_b, d_x, d_fixed, precond, reltol, maxiter, iters, relres);
-    case 3: return pcg_typed<3>(ctx, m, d_b, d_x, d_fixed, precond, reltol, maxiter, iters, relres);
+    case 1: return pcg_segments<1>(ctx, m, d_b, d_x, d_fixed, nseg, seg_off, precond, reltol, maxiter, iters, relres);
+    case 2: return pcg_segments<2>(ctx, m, d_b, d_x, d_fixed, nseg, seg_off, precond, reltol, maxiter, iters, relres);
+    case 3: return pcg_segments<3>(ctx, m, d_b, d_x, d_fixed, nseg, seg_off, precond, reltol, maxiter, iters, relres);
   }
   return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
+}
+
+int pcg_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
+             const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
+             int64_t *iters, double *relres) {
+  const int64_t off[2] = {0, m->pat->ndof};
+  return pcg_batched_impl(ctx, m, d_b, d_x, d_fixed, 1, off, precond, reltol, maxiter, iters, relres);
 }

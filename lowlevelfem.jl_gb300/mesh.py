@@ -65,6 +65,7 @@ class Group:
     family: int = 0
     order: int = 0
     conn: np.ndarray | None = None
+    elems: np.ndarray | None = None   # volume groups: element indices into Mesh.conn
 
 
 @dataclass
@@ -285,6 +286,38 @@ def structured_box_mesh(x0=0.0, y0=0.0, z0=0.0, lx=1.0, ly=1.0, lz=1.0, n=10,
     face("front", 2, NZ - 1)
     m = Mesh(3, fam, p, xyz, conn, groups, name="structured_box")
     return set_current(m)
+
+
+def concat_meshes(meshes, sep="#") -> tuple[Mesh, np.ndarray]:
+    """Several independent meshes of one family/order as one mesh (one
+    assembly launch, one block-diagonal matrix).  Instance i keeps its node
+    and element order; its groups are renamed "<name><sep><i>".  Returns the
+    combined mesh and node offsets (length n+1), so instance i owns nodes
+    offsets[i]..offsets[i+1]-1 (0-based)."""
+    if not meshes:
+        raise ValueError("concat_meshes: no meshes")
+    m0 = meshes[0]
+    for m in meshes:
+        if (m.dim, m.family, m.order) != (m0.dim, m0.family, m0.order):
+            raise ValueError("concat_meshes: all meshes must share dimension, family and order")
+    noff = np.zeros(len(meshes) + 1, dtype=np.int64)
+    eoff = np.zeros(len(meshes) + 1, dtype=np.int64)
+    for i, m in enumerate(meshes):
+        noff[i + 1] = noff[i] + m.non
+        eoff[i + 1] = eoff[i] + m.nel
+    xyz = np.concatenate([m.xyz for m in meshes], axis=0)
+    conn = np.concatenate([m.conn + noff[i] for i, m in enumerate(meshes)], axis=0)
+    groups = {}
+    for i, m in enumerate(meshes):
+        for name, g in m.groups.items():
+            c = None if g.conn is None else g.conn + noff[i]
+            ng = Group(f"{name}{sep}{i}", g.dim, g.nodes + noff[i], g.family, g.order, c)
+            if g.dim == m.dim:
+                ng.elems = np.arange(eoff[i], eoff[i + 1])
+            groups[ng.name] = ng
+    out = Mesh(m0.dim, m0.family, m0.order, xyz, conn, groups, name="batch")
+    set_current(out)
+    return out, noff
 
 
 # --------------------------------------------------------------------------
