@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N_CELLS)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-peak", action="store_true", help="skip the DGEMM FP64 reference rate")
+    ap.add_argument("--no-other-form", action="store_true", help="skip the second arithmetic form")
     return ap.parse_args()
 
 
@@ -207,48 +209,55 @@ def main():
     nnz = pat.nnz
     Ea, nua = L.f64([E]), L.f64([NU])
 
-    def assemble():
+    def assemble(fm=form):
         h = L.C.c_void_p()
         ctx.check(L.lib().llf_assemble_stiffness(ctx.h, dm.h, pat.h, L.SOLID, L.ptr(Ea, L.C.c_double),
-                                                 L.ptr(nua, L.C.c_double), 1, 1.0, form, L.C.byref(h)))
+                                                 L.ptr(nua, L.C.c_double), 1, 1.0, fm, L.C.byref(h)))
         return L.DeviceMatrix(ctx, h, pat)
 
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
-    for _ in range(args.warmup):
-        Km = assemble()
-        del Km
-    ctx.sync()
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
 
-    ctx.profile_reset()
-    ctx.profile(True)
-    evs = []
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(1.0)
-                a = torch.cuda.Event(enable_timing=True)
-                b = torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-            Km = assemble()
-            with torch.cuda.stream(stream):
-                b.record(stream)
-            stored = Km.nnz()
+    def measure(fm, steps, warmup):
+        """Timed assemblies of form fm: CUDA events on the library's stream,
+        L2 flushed before every step, per-kernel event tracing on."""
+        for _ in range(warmup):
+            Km = assemble(fm)
             del Km
-            evs.append((a, b))
-        torch.cuda.synchronize()
         ctx.sync()
-    ctx.profile(False)
-    prof = ctx.profile_report()
-    launches = ctx.launches()
-    ms = [a.elapsed_time(b) for a, b in evs]
-    ms_step = sum(ms) / len(ms)
-    if world > 1:
-        t = torch.tensor([ms_step], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        ctx.profile_reset()
+        ctx.profile(True)
+        evs = []
+        stored = 0
+        with ClockSampler(local) as clk:
+            for _ in range(steps):
+                with torch.cuda.stream(stream):
+                    flush.fill_(1.0)
+                    a = torch.cuda.Event(enable_timing=True)
+                    b = torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                Km = assemble(fm)
+                with torch.cuda.stream(stream):
+                    b.record(stream)
+                stored = Km.nnz()
+                del Km
+                evs.append((a, b))
+            torch.cuda.synchronize()
+            ctx.sync()
+        ctx.profile(False)
+        prof = ctx.profile_report()
+        launches = ctx.launches()
+        ms = [a.elapsed_time(b) for a, b in evs]
+        ms_step = sum(ms) / len(ms)
+        if world > 1:
+            t = torch.tensor([ms_step], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms_step = float(t.item())
+        return ms_step, prof, launches, stored, clk.summary()
+
+    ms_step, prof, launches, stored, clocks = measure(form, args.steps, args.warmup)
     value = world * nnz / (ms_step * 1e-3) / 1e9
 
     bytes_alg, flops = algorithmic(mesh, nnz)
@@ -264,6 +273,8 @@ def main():
     # FP64 rate of the dominant element kernel vs a measured DGEMM
     fp64_peak = None
     try:
+        if args.no_peak:
+            raise RuntimeError("skipped")
         x = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
         torch.matmul(x, x)
         torch.cuda.synchronize()
@@ -318,6 +329,16 @@ def main():
                "h2d_bytes_per_step": xyz_h.numel() * 8 + conn_h.numel() * 8,
                "d2h_bytes_per_step": colptr_h.numel() * 8 + 2 * nnz_s * 8}
 
+    # the other arithmetic form on the same workload (reported beside the headline)
+    other = None
+    if not args.no_other_form:
+        ofm = L.FP64 if form == L.FP32Q else L.FP32Q
+        oms, oprof, _, ostored, _ = measure(ofm, args.steps, args.warmup)
+        other = {"form": "fp64" if ofm == L.FP64 else "fp32q", "value": world * nnz / (oms * 1e-3) / 1e9,
+                 "unit": "GNNZ/s", "ms_per_step": oms, "stored_nnz": ostored,
+                 "roofline_frac": bytes_alg / (sum(v["ms"] for v in oprof.values()) / args.steps * 1e-3) / 1e9 / hbm_peak,
+                 "per_kernel_ms": {k: v["ms"] / max(v["launches"], 1) for k, v in oprof.items()}}
+
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         try:
@@ -338,7 +359,7 @@ def main():
                           "pattern_build_s": pattern_s, "l2": "256 MB buffer written before every timed step",
                           "parallelism": "replicas" if world > 1 else "single"},
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-               "clocks": clk.summary()}
+               "clocks": clocks, "other_form": other}
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -26,6 +26,8 @@
 // or reassociation can move the result away from the CPU oracle's.
 #include "common.cuh"
 
+#include <algorithm>
+
 namespace {
 
 constexpr int ELEM_THREADS = 128;
@@ -273,48 +275,92 @@ k_elem_fp64(ElemArgs A) {
 // FP64 sums in element order in both.  Per warp: the column's row-node list
 // (deg ints) and its accumulator (deg * P * P doubles) in shared memory.
 template <int P, bool BLOCKVAL, class T>
+__device__ __forceinline__ void add_block(double *acc, int t, const T *v) {
+  double *dst = acc + (size_t)t * P * P;  // [t][j][i]
+#pragma unroll
+  for (int i = 0; i < P; ++i)
+#pragma unroll
+    for (int j = 0; j < P; ++j) {
+      double x = BLOCKVAL ? (double)v[i * P + j] : (i == j ? (double)v[0] : 0.0);
+      dst[j * P + i] = __dadd_rn(dst[j * P + i], x);
+    }
+}
+
+// Per warp in shared memory: the column's row nodes (max_deg ints), its
+// accumulator (max_deg*P*P doubles), the elements of the column node
+// (max_n2e int2) and the row position of every (element, node) pair
+// (max_n2e*npe int32).  Positions are found for all elements at once
+// (independent binary searches), then the elements are accumulated in
+// ascending order with the next element's blocks prefetched into registers.
+template <int P, bool BLOCKVAL, class T>
 __global__ void k_colgather(const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
                             const int64_t *__restrict__ n2e_ptr, const int2 *__restrict__ n2e,
                             const int32_t *__restrict__ conn, const T *__restrict__ Kf, int npe,
-                            int64_t non, int max_deg, double *__restrict__ nz,
+                            int64_t non, int max_deg, int max_n2e, double *__restrict__ nz,
                             int64_t *__restrict__ cnt, unsigned *status) {
   extern __shared__ double cg_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   constexpr int BS = BLOCKVAL ? P * P : 1;
   double *acc = cg_smem + (size_t)wib * max_deg * P * P;
-  int32_t *rows = (int32_t *)(cg_smem + (size_t)wpb * max_deg * P * P) + (size_t)wib * max_deg;
+  int2 *els = (int2 *)(cg_smem + (size_t)wpb * max_deg * P * P) + (size_t)wib * max_n2e;
+  int32_t *rows = (int32_t *)((int2 *)(cg_smem + (size_t)wpb * max_deg * P * P) + (size_t)wpb * max_n2e) +
+                  (size_t)wib * (max_deg + (size_t)max_n2e * npe);
+  int32_t *tpos = rows + max_deg;
   for (int64_t B = (int64_t)blockIdx.x * wpb + wib; B < non; B += (int64_t)gridDim.x * wpb) {
     const int64_t c0 = nptr[B];
     const int deg = (int)(nptr[B + 1] - c0);
+    const int64_t s = n2e_ptr[B];
+    const int nb = (int)(n2e_ptr[B + 1] - s);
     for (int t = lane; t < deg; t += 32) rows[t] = nadj[c0 + t];
     for (int t = lane; t < deg * P * P; t += 32) acc[t] = 0.0;
+    for (int k = lane; k < nb; k += 32) els[k] = n2e[s + k];
     __syncwarp();
-    const int64_t s = n2e_ptr[B], s1 = n2e_ptr[B + 1];
-    for (int64_t k = s; k < s1; ++k) {  // elements of B, ascending
-      const int2 el = n2e[k];
-      const T *col = Kf + ((size_t)el.x * npe + el.y) * npe * BS;
-      for (int a = lane; a < npe; a += 32) {
-        const int A = conn[(size_t)el.x * npe + a];
-        int lo = 0, hi = deg - 1;
-        while (lo < hi) {
-          int mid = (lo + hi) >> 1;
-          if (rows[mid] < A) lo = mid + 1; else hi = mid;
-        }
-        if (rows[lo] != A) {
-          atomicOr(status, ST_PATTERN);
-          continue;
-        }
-        double *dst = acc + (size_t)lo * P * P;  // [t][j][i]
-        const T *blk = col + (size_t)a * BS;
-#pragma unroll
-        for (int i = 0; i < P; ++i)
-#pragma unroll
-          for (int j = 0; j < P; ++j) {
-            double v = BLOCKVAL ? (double)blk[i * P + j] : (i == j ? (double)blk[0] : 0.0);
-            dst[j * P + i] = __dadd_rn(dst[j * P + i], v);
-          }
+    for (int it = lane; it < nb * npe; it += 32) {
+      const int k = it / npe, a = it - k * npe;
+      const int A = conn[(size_t)els[k].x * npe + a];
+      int lo = 0, hi = deg - 1;
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (rows[mid] < A) lo = mid + 1; else hi = mid;
       }
-      __syncwarp();
+      if (deg == 0 || rows[lo] != A) {
+        atomicOr(status, ST_PATTERN);
+        lo = -1;
+      }
+      tpos[it] = lo;
+    }
+    __syncwarp();
+    if (npe <= 32) {
+      const bool act = lane < npe;
+      T cur[BS], nxt[BS];
+      if (nb > 0 && act) {
+        const T *v = Kf + (((size_t)els[0].x * npe + els[0].y) * npe + lane) * BS;
+#pragma unroll
+        for (int m = 0; m < BS; ++m) cur[m] = v[m];
+      }
+      for (int k = 0; k < nb; ++k) {  // elements of B, ascending
+        if (k + 1 < nb && act) {
+          const T *v = Kf + (((size_t)els[k + 1].x * npe + els[k + 1].y) * npe + lane) * BS;
+#pragma unroll
+          for (int m = 0; m < BS; ++m) nxt[m] = v[m];
+        }
+        if (act) {
+          const int t = tpos[k * npe + lane];
+          if (t >= 0) add_block<P, BLOCKVAL, T>(acc, t, cur);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int m = 0; m < BS; ++m) cur[m] = nxt[m];
+      }
+    } else {
+      for (int k = 0; k < nb; ++k) {
+        const T *col = Kf + ((size_t)els[k].x * npe + els[k].y) * npe * BS;
+        for (int a = lane; a < npe; a += 32) {
+          const int t = tpos[k * npe + a];
+          if (t >= 0) add_block<P, BLOCKVAL, T>(acc, t, col + (size_t)a * BS);
+        }
+        __syncwarp();
+      }
     }
     // write column (B,j): entries (row node t, component i) at P*t + i
 #pragma unroll
@@ -482,9 +528,14 @@ int run_elem(llf_ctx *ctx, ElemArgs a) {
 
 template <int P, bool BV, class T>
 int run_colgather(llf_ctx *ctx, llf_pattern *pat, const T *Kf, double *nz, int64_t *cnt) {
-  const int wpb = 4;
   const int md = pat->max_deg > 0 ? pat->max_deg : 1;
-  size_t smem = (size_t)wpb * md * (P * P * sizeof(double) + sizeof(int32_t));
+  const int mn = pat->max_n2e > 0 ? pat->max_n2e : 1;
+  const int npe = pat->mesh->npe;
+  const size_t per_warp = (size_t)md * P * P * sizeof(double) + (size_t)mn * sizeof(int2) +
+                          (md + (size_t)mn * npe) * sizeof(int32_t);
+  int wpb = (int)std::min<size_t>(4, (200 * 1024) / per_warp);
+  if (wpb < 1) wpb = 1;
+  size_t smem = (size_t)wpb * per_warp;
   if (smem > 200 * 1024)
     return llf_fail(ctx, LLF_ERR_LIMIT, "a column node has too many neighbours for the gather buffer");
   auto fn = k_colgather<P, BV, T>;
@@ -497,8 +548,8 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const T *Kf, double *nz, int64
   if (grid > need) grid = need > 0 ? need : 1;
   KernelScope ks(ctx, "k_colgather");
   fn<<<(unsigned)grid, wpb * 32, smem, ctx->stream>>>(pat->d_nptr, pat->d_nadj, pat->d_n2e_ptr,
-                                                      pat->d_n2e, pat->mesh->d_conn, Kf, pat->mesh->npe,
-                                                      pat->mesh->non, md, nz, cnt, ctx->d_status);
+                                                      pat->d_n2e, pat->mesh->d_conn, Kf, npe,
+                                                      pat->mesh->non, md, mn, nz, cnt, ctx->d_status);
   LLF_CUDA_TRY(ctx, cudaGetLastError());
   return LLF_OK;
 }
