@@ -45,6 +45,10 @@ def parse():
     ap.add_argument("--n", type=int, default=N_CELLS)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="assembly", choices=["assembly", "batched", "serving", "tl"])
+    ap.add_argument("--instances", type=int, default=64, help="batched: instances (a seeded sample of 512)")
+    ap.add_argument("--requests", type=int, default=200, help="serving: requests of the Poisson stream")
+    ap.add_argument("--workers", type=int, default=4, help="serving: server workers")
     ap.add_argument("--no-peak", action="store_true", help="skip the DGEMM FP64 reference rate")
     ap.add_argument("--no-other-form", action="store_true", help="skip the second arithmetic form")
     return ap.parse_args()
@@ -183,10 +187,189 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def _pct(v, q):
+    v = sorted(v)
+    return v[min(len(v) - 1, int(math.ceil(q / 100.0 * len(v))) - 1)] if v else None
+
+
+def run_batched(args, llf):
+    """Batched configuration: independent tet10 boxes assembled in one launch
+    and solved by one segmented Jacobi-PCG (CUDA graph).  Solves/s and the
+    relative displacement error of sample instances against a direct solve."""
+    import numpy as np
+    import torch
+    from llfem_gb300 import workloads as wl
+    rng = np.random.default_rng(wl.SEED)
+    inst = [wl.batched_instance(rng) for _ in range(args.instances)]
+    batch, noff = llf.concat_meshes([m for m, _, _ in inst])
+    mats = [llf.Material(f"body#{i}", E=E, nu=nu) for i, (_, E, nu) in enumerate(inst)]
+    P = llf.Problem(mats, type="Solid", mesh=batch)
+    loads = [llf.load(f"right#{i}", fx=1.0) for i in range(len(inst))]
+    sup = [llf.displacementConstraint(f"left#{i}", ux=0, uy=0, uz=0) for i in range(len(inst))]
+    f = llf.loadVector(P, loads)
+    P.pattern()
+    times = []
+    for rep in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        K = llf.stiffnessMatrix(P)
+        u = llf.solveFieldBatched(K, f, support=sup, node_offsets=noff, preconditioner="jacobi", reltol=1e-12)
+        torch.cuda.synchronize()
+        if rep >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    # accuracy against a direct solve of the two smallest instances
+    import scipy.sparse.linalg as spla
+    errs = []
+    A = K.A
+    fixed = np.zeros(A.shape[0], bool)
+    fixed[llf.constrainedDoFs(P, sup) - 1] = True
+    for i in np.argsort(np.diff(noff))[:2]:
+        a, b = 3 * noff[i], 3 * noff[i + 1]
+        fr = ~fixed[a:b]
+        Ai = A[a:b, a:b].tocsc()[fr][:, fr]
+        ud = spla.spsolve(Ai.tocsc(), f.a[a:b, 0][fr])
+        errs.append(float(np.linalg.norm(u.a[a:b, 0][fr] - ud) / np.linalg.norm(ud)))
+    nel = sum(m.nel for m, _, _ in inst)
+    return {"metric": "batched assemble+solve (independent tet10 systems / s)", "value": len(inst) / t,
+            "unit": "solves/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded sample of the 512-instance tet10 workload",
+            "config": {"workload": f"batched-tet10-{len(inst)}", "instances": len(inst), "elements": nel,
+                       "dofs": 3 * batch.non, "structural_nnz": P.pattern().nnz, "precond": "jacobi",
+                       "reltol": 1e-12},
+            "cg_iterations": {"min": int(np.min(u.iterations)), "median": float(np.median(u.iterations)),
+                              "max": int(np.max(u.iterations))},
+            "rel_err_vs_direct": errs}
+
+
+def run_serving(args, llf):
+    """Serving configuration: a Poisson stream (200 req/s) of steady heat
+    requests through llf_server; p50/p99 latency and solves/s, against the same
+    requests solved one at a time."""
+    import numpy as np
+    import threading
+    from llfem_gb300 import workloads as wl
+    rng = np.random.default_rng(wl.SEED)
+    reqs = [wl.heat_request(rng) for _ in range(args.requests)]
+    arrivals = np.cumsum(rng.exponential(1.0 / 200.0, size=len(reqs)))
+
+    def submit(srv, r):
+        m, k, fixed, x0 = r
+        return srv.submit_heat(m.dim, m.xyz, m.conn, m.family, m.order, k, x0, fixed, reltol=1e-10)
+
+    # one at a time (a single worker, next request after the previous result)
+    warm = [wl.heat_request(np.random.default_rng(1), dofs_max=5e3) for _ in range(2 * args.workers)]
+    one = llf._lib.Server(workers=1)
+    one.wait(submit(one, warm[0]))
+    t0 = time.perf_counter()
+    for r in reqs:
+        one.wait(submit(one, r))
+    t_single = time.perf_counter() - t0
+    one.close()
+    srv = llf._lib.Server(workers=args.workers, budget_bytes=120 << 30)
+    for t in [submit(srv, r) for r in warm]:   # every worker has created its context
+        srv.wait(t)
+    tickets = [None] * len(reqs)
+    start = time.perf_counter()
+
+    def producer():
+        for i, r in enumerate(reqs):
+            delay = start + arrivals[i] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            tickets[i] = (submit(srv, r), time.perf_counter())
+
+    th = threading.Thread(target=producer)
+    th.start()
+    lat, iters = [], []
+    done_at = start
+    for i in range(len(reqs)):
+        while tickets[i] is None:
+            time.sleep(0.0005)
+        x, it, rr, l, svc = srv.wait(tickets[i][0])
+        lat.append(l)
+        iters.append(it)
+        done_at = max(done_at, time.perf_counter())
+    th.join()
+    stats = srv.stats()
+    srv.close()
+    span = done_at - start
+    dofs = [m.non for m, _, _, _ in reqs]
+    return {"metric": "served steady-heat solves / s (Poisson 200 req/s)", "value": len(reqs) / span,
+            "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic heat requests (seeded)",
+            "config": {"workload": f"serving-heat-{len(reqs)}", "requests": len(reqs), "workers": args.workers,
+                       "dofs_median": float(np.median(dofs)), "dofs_max": int(max(dofs)), "reltol": 1e-10},
+            "latency_s": {"p50": _pct(lat, 50), "p99": _pct(lat, 99), "max": max(lat)},
+            "one_at_a_time_solves_per_s": len(reqs) / t_single,
+            "cg_iterations_median": float(np.median(iters)), "peak_device_bytes": stats["peak_bytes"]}
+
+
+def run_tl(args, llf):
+    """Hyperelastic Total Lagrangian configuration: compressible neo-Hookean
+    (mu=1, lambda=10) unit cube hex8 48^3, 30% axial stretch in 10 load steps,
+    full Newton with the consistent tangent reassembled every iteration; and
+    the tangent assembly of the order-4 hex variant (12^3 hex125)."""
+    import numpy as np
+    import torch
+    prm = {"mu": 1.0, "lambda": 10.0}
+    n = 48 if args.n == N_CELLS else args.n
+    m = llf.structured_box_mesh(n=n, order=1)
+    P = llf.Problem([llf.Material("body")], type="Solid")
+    sup = [llf.displacementConstraint("left", ux=0.0), llf.displacementConstraint("right", ux=0.3),
+           llf.displacementConstraint("bottom", uy=0.0), llf.displacementConstraint("rear", uz=0.0)]
+    P.pattern()
+    ctx = P._ctx
+    ctx.profile_reset()
+    ctx.profile(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    u = llf.solveDeformation(P, support=sup, params=prm, steps=10, tol=1e-8, preconditioner="bjacobi")
+    torch.cuda.synchronize()
+    t_newton = time.perf_counter() - t0
+    ctx.profile(False)
+    prof = ctx.profile_report()
+    its = len(u.history)
+    # order-4 hex tangent assembly
+    m4 = llf.structured_box_mesh(n=12, order=4)
+    P4 = llf.Problem([llf.Material("body")], type="Solid")
+    F4 = llf.grad(llf.VectorField(np.zeros((3 * m4.non, 1)), P4), add_identity=True)
+    P4.pattern()
+    llf.tangentMatrix(P4, F4, params=prm)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        llf.tangentMatrix(P4, F4, params=prm)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t1)
+    t4 = min(ts)
+    flops4 = 2 * 375 ** 2 * 6 * 125 * m4.nel / 2  # upper-triangle pairs of B^T (D B) per point
+    return {"metric": "TL Newton iteration time (hex8 48^3, 30% stretch, 10 steps)", "value": t_newton / max(its, 1) * 1e3,
+            "unit": "ms/iteration", "n_gpus": 1, "steps": its, "warmup": 0, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic unit cube",
+            "config": {"workload": "tl-neohooke-hex8-48", "elements": m.nel, "dofs": 3 * m.non,
+                       "newton_iterations": its, "load_steps": 10},
+            "newton_total_s": t_newton,
+            "kernels_ms": {k: v["ms"] for k, v in prof.items()},
+            "final_residual": u.history[-1]["residual"],
+            "hex125_tangent": {"elements": m4.nel, "ms": t4 * 1e3, "gflops_fp64": flops4 / t4 / 1e9,
+                               "structural_nnz": P4.pattern().nnz}}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "assembly":
+        import torch
+        torch.cuda.set_device(0)
+        import __graft_entry__ as entry
+        llf = entry.load_package()
+        fn = {"batched": run_batched, "serving": run_serving, "tl": run_tl}[args.workload]
+        print(json.dumps(fn(args, llf)), flush=True)
+        return
     rank, world, local = dist_env()
     import torch
     if world > 1:

@@ -232,6 +232,16 @@ int llf_tl_material_tangent(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
                             const double *params, int nparams,
                             llf_matrix **out);
 
+/* Consistent Newton tangent K_mat + K_geo in one pass from the elementwise
+ * nodal F: at every point S and the tangent come from the same C = F^T F, so
+ * the matrix is the exact derivative of llf_tl_internal_force.  Replaces the
+ * user-level sum materialTangentMatrix(F) + initialStressMatrix(C) of the
+ * reference's Newton loops (src/nonlinear.jl:2083-2595), which interpolates
+ * the nodal C = F^T F instead. */
+int llf_tl_tangent(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
+                   const double *Felem, int law, const double *params,
+                   int nparams, llf_matrix **out);
+
 /* Geometric (initial-stress) stiffness K_geo[a i, b i] = sum grad Na^T S
  * grad Nb detJ0 w, identity component block — initialStressMatrix,
  * src/nonlinear.jl:2417-2595.  Exactly one of Selem (elementwise nodal PK2
@@ -333,6 +343,49 @@ int llf_pcg_batched(llf_ctx *ctx, const llf_matrix *m, const double *b, double *
                     const uint8_t *fixed, int nseg, const int64_t *seg_off,
                     int precond, double reltol, int64_t maxiter, int64_t *iters,
                     double *relres);
+
+/* ======================================================================== */
+/* Serving                                                                  */
+/* ======================================================================== */
+/* A request server for steady heat-conduction solves — the serving form of
+ * solveTemperature(problem; heatFlux, temperatureConstraint)
+ * (src/heat.jl:1068-1084): each request carries its own mesh, conductivity,
+ * right-hand side, prescribed temperatures and tolerance.  nworkers threads,
+ * each with its own context and stream, take queued requests in arrival
+ * order as soon as a worker is free and the request's device-memory
+ * estimate fits in mem_budget_bytes; requests in flight overlap on the GPU.
+ * Results are the same as a lone solve of the request (deterministic
+ * kernels). */
+typedef struct llf_server llf_server;
+
+int llf_server_create(int device, int nworkers, int64_t mem_budget_bytes,
+                      llf_server **out);
+
+/* Copy one request into the server; *ticket identifies it. x0[non] holds the
+ * prescribed temperatures on fixed[non] != 0 (other entries ignored); rhs
+ * (may be NULL = 0) the nodal heat loads.  maxiter <= 0 means 20*non. */
+int llf_server_submit_heat(llf_server *s, int dim, int64_t non,
+                           const double *xyz, int64_t nel, int npe,
+                           const int64_t *conn, int family, int order,
+                           double k, double thickness, const double *rhs,
+                           const double *x0, const uint8_t *fixed,
+                           int precond, double reltol, int64_t maxiter,
+                           int64_t *ticket);
+
+/* Wait up to timeout_s (< 0: no limit) for a ticket and take its result:
+ * solution x[non], CG iterations and relative residual, latency from
+ * submission to result and the worker's service time; err receives the
+ * error text of a failed request.  Returns LLF_ERR_STATE on timeout or an
+ * unknown ticket, otherwise the request's own status. */
+int llf_server_wait(llf_server *s, int64_t ticket, double timeout_s, double *x,
+                    int64_t *iters, double *relres, double *latency_s,
+                    double *service_s, char *err, int64_t errlen);
+
+int llf_server_stats(llf_server *s, int64_t *queued, int64_t *served,
+                     int64_t *bytes_in_use, int64_t *peak_bytes);
+
+/* Drains the queue, joins the workers and frees the server. */
+int llf_server_destroy(llf_server *s);
 
 #ifdef __cplusplus
 }

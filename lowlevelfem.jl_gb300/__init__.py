@@ -16,7 +16,7 @@ from .api import (Material, material, elastic_constants, Problem, Field, SystemM
                   temperatureConstraint, load, heatFlux, constrainedDoFs, allDoFs, freeDoFs,
                   applyBoundaryConditions_, loadVector, stiffnessMatrix, massMatrix,
                   heatConductionMatrix, solveDisplacement, solveTemperature, solveField, solveFieldBatched, grad,
-                  deformationGradient, materialTangentMatrix, initialStressMatrix,
+                  deformationGradient, materialTangentMatrix, initialStressMatrix, tangentMatrix, solveDeformation,
                   internalForceVector)
 
 __version__ = "0.1.0"

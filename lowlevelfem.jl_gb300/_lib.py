@@ -71,6 +71,7 @@ SIGNATURES = {
     "llf_assemble_mass": (i32, [vp, vp, vp, i32, P_dbl, i32, dbl, i32, i32, PP]),
     "llf_assemble_heat": (i32, [vp, vp, vp, i32, P_dbl, i32, dbl, i32, PP]),
     "llf_tl_material_tangent": (i32, [vp, vp, vp, P_dbl, i32, P_dbl, i32, PP]),
+    "llf_tl_tangent": (i32, [vp, vp, vp, P_dbl, i32, P_dbl, i32, PP]),
     "llf_tl_initial_stress": (i32, [vp, vp, vp, P_dbl, P_dbl, i32, P_dbl, i32, PP]),
     "llf_tl_internal_force": (i32, [vp, vp, P_dbl, P_dbl, i32, P_dbl, i32, P_dbl]),
     "llf_grad_elementwise": (i32, [vp, vp, P_dbl, i32, P_dbl]),
@@ -84,6 +85,12 @@ SIGNATURES = {
     "llf_matrix_destroy": (i32, [vp, vp]),
     "llf_pcg": (i32, [vp, vp, P_dbl, P_dbl, P_u8, i32, dbl, i64, P_i64, P_dbl]),
     "llf_pcg_batched": (i32, [vp, vp, P_dbl, P_dbl, P_u8, i32, P_i64, i32, dbl, i64, P_i64, P_dbl]),
+    "llf_server_create": (i32, [i32, i32, i64, PP]),
+    "llf_server_submit_heat": (i32, [vp, i32, i64, P_dbl, i64, i32, P_i64, i32, i32, dbl, dbl, P_dbl, P_dbl, P_u8,
+                                     i32, dbl, i64, P_i64]),
+    "llf_server_wait": (i32, [vp, i64, dbl, P_dbl, P_i64, P_dbl, P_dbl, P_dbl, C.c_char_p, i64]),
+    "llf_server_stats": (i32, [vp, P_i64, P_i64, P_i64, P_i64]),
+    "llf_server_destroy": (i32, [vp]),
 }
 
 _lib = None
@@ -186,6 +193,61 @@ class Context:
     def close(self):
         if getattr(self, "h", None):
             lib().llf_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Request server of the library (llf_server): worker threads with their
+    own streams, admission by device-memory budget."""
+
+    def __init__(self, device: int = 0, workers: int = 4, budget_bytes: int = 64 << 30):
+        h = C.c_void_p()
+        rc = lib().llf_server_create(device, workers, int(budget_bytes), C.byref(h))
+        if rc != LLF_OK:
+            raise LLFError(rc, "llf_server_create failed")
+        self.h = h
+        self._non = {}
+
+    def submit_heat(self, dim, xyz, conn, family, order, k, x0, fixed, rhs=None, thickness=1.0,
+                    precond=PRECOND_JACOBI, reltol=1e-10, maxiter=0) -> int:
+        xyz, conn, x0 = f64(xyz), i64a(conn), f64(x0)
+        fx = np.ascontiguousarray(fixed, dtype=np.uint8)
+        rhs = None if rhs is None else f64(rhs)
+        t = C.c_int64(0)
+        rc = lib().llf_server_submit_heat(self.h, dim, xyz.shape[0], ptr(xyz, C.c_double), conn.shape[0],
+                                          conn.shape[1], ptr(conn, C.c_int64), family, order, float(k),
+                                          float(thickness), ptr(rhs, C.c_double), ptr(x0, C.c_double),
+                                          ptr(fx, C.c_uint8), int(precond), float(reltol), int(maxiter), C.byref(t))
+        if rc != LLF_OK:
+            raise LLFError(rc, "llf_server_submit_heat: bad request")
+        self._non[t.value] = xyz.shape[0]
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = -1.0):
+        n = self._non.pop(ticket)
+        x = np.zeros(n)
+        it, rr, lat, svc = C.c_int64(0), C.c_double(0), C.c_double(0), C.c_double(0)
+        err = C.create_string_buffer(512)
+        rc = lib().llf_server_wait(self.h, ticket, float(timeout), ptr(x, C.c_double), C.byref(it), C.byref(rr),
+                                   C.byref(lat), C.byref(svc), err, 512)
+        if rc != LLF_OK:
+            raise LLFError(rc, err.value.decode() or "server request failed")
+        return x, it.value, rr.value, lat.value, svc.value
+
+    def stats(self) -> dict:
+        q, s, b, p = C.c_int64(0), C.c_int64(0), C.c_int64(0), C.c_int64(0)
+        lib().llf_server_stats(self.h, C.byref(q), C.byref(s), C.byref(b), C.byref(p))
+        return {"queued": q.value, "served": s.value, "bytes_in_use": b.value, "peak_bytes": p.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().llf_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -632,6 +632,68 @@ def materialTangentMatrix(problem: Problem, F, C=None, energy=None, params=None)
     return SystemMatrix(_lib.DeviceMatrix(ctx, h, pat), problem)
 
 
+def tangentMatrix(problem: Problem, F, energy="NeoHookeCompressible", params=None) -> SystemMatrix:
+    """Consistent Newton tangent K_mat + K_geo from F in one pass (the exact
+    derivative of internalForceVector for the same F); the reference's Newton
+    loops sum materialTangentMatrix(F) and initialStressMatrix(C)."""
+    law, prm = _law(energy, params)
+    Fa = _tensor_array(problem, F)
+    ctx = problem._ctx
+    h = _lib.C.c_void_p()
+    dm, pat = problem.device_mesh(), problem.pattern()
+    ctx.check(_lib.lib().llf_tl_tangent(ctx.h, dm.h, pat.h, _lib.ptr(Fa, _lib.C.c_double), law,
+                                        _lib.ptr(prm, _lib.C.c_double), len(prm), _lib.C.byref(h)), "tangentMatrix")
+    return SystemMatrix(_lib.DeviceMatrix(ctx, h, pat), problem)
+
+
+def solveDeformation(problem: Problem, support=(), load=(), energy="NeoHookeCompressible", params=None,
+                     steps=10, tol=1e-8, maxit=25, reltol=1e-10, preconditioner="bjacobi", callback=None):
+    """Total Lagrangian Newton solution in `steps` proportional load steps:
+    prescribed displacements and external loads are ramped linearly; every
+    Newton iteration evaluates F = I + u∘∇, f_int and the consistent tangent on
+    the GPU and solves K du = f_ext - f_int for du with the increments of the
+    prescribed values on the constrained DoFs.  Converged when the FP64
+    residual on the free DoFs drops below tol times its value at the start of
+    the step (or below tol times |f_ext| when that is larger).  Returns u and
+    per-iteration records (step, iteration, residual norm, CG iterations)."""
+    n = problem.pdim * problem.non
+    u = _field_for(problem, np.zeros(n))
+    target = _field_for(problem, np.zeros(n))
+    applyBoundaryConditions_(target, list(support))
+    fixed = np.zeros(n, dtype=np.uint8)
+    fixed[constrainedDoFs(problem, list(support)) - 1] = 1
+    fext_full = loadVector(problem, list(load)).a[:, 0] if load else np.zeros(n)
+    free = fixed == 0
+    history = []
+    prec = _PRECOND[preconditioner]
+    for step in range(1, steps + 1):
+        lam = step / steps
+        fext = lam * fext_full
+        res0 = None
+        for it in range(maxit):
+            F = grad(u, add_identity=True)
+            fint = internalForceVector(problem, F=F, energy=energy, params=params).a[:, 0]
+            r = fext - fint
+            r[~free] = 0.0
+            rn = float(np.linalg.norm(r))
+            du_fixed = np.where(free, 0.0, lam * target.a[:, 0] - u.a[:, 0])
+            history.append({"step": step, "iter": it, "residual": rn})
+            if not np.any(du_fixed != 0.0):
+                if res0 is None:   # first equilibrium residual of the step
+                    res0 = max(rn, float(np.linalg.norm(fext)), 1e-300)
+                if rn <= tol * res0:
+                    break
+            K = tangentMatrix(problem, F, energy=energy, params=params)
+            x, cg_it, _ = K.dm.pcg(r, du_fixed, fixed, precond=prec, reltol=reltol, maxiter=20 * n,
+                                   raise_on_fail=True)
+            history[-1]["cg_iterations"] = cg_it
+            u.a[:, 0] += x
+            if callback:
+                callback(step, it, rn)
+    u.history = history
+    return u
+
+
 def initialStressMatrix(problem: Problem, S=None, energy=None, params=None, C=None) -> SystemMatrix:
     """K_geo[ai,bi] = Σ ∇Naᵀ S ∇Nb detJ0 w (src/nonlinear.jl:2417-2595);
     S given, or computed from the Cauchy-Green field C with `energy`."""

@@ -15,7 +15,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libllfem_gb300.so")
 
 CU_SOURCES = ["abi.cu", "scan.cu", "pattern.cu", "assemble.cu", "assemble_fp32.cu", "solve.cu", "tl.cu", "field.cu"]
-CXX_SOURCES = ["tables.cpp"]
+CXX_SOURCES = ["tables.cpp", "serve.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -56,7 +56,7 @@ def build_library(verbose: bool = False, force: bool = False) -> str:
         objs.append(obj)
         if not force and _newer(obj, [path] + headers):
             continue
-        cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-c", path, "-o", obj]
+        cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-pthread", "-ffp-contract=off", "-c", path, "-o", obj]
         jobs.append((cmd, src))
     procs = [(subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT), src)
              for cmd, src in jobs]

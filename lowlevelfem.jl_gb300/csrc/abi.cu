@@ -526,6 +526,23 @@ int llf_tl_material_tangent(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, cons
   return finish_matrix(ctx, rc, m, out);
 }
 
+int llf_tl_tangent(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *Felem, int law,
+                   const double *params, int nparams, llf_matrix **out) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!mesh || !pat || !Felem || pat->mesh != mesh || mesh->dim != 3 || pat->pdim != 3)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_tl_tangent: needs a 3D mesh, its pdim 3 pattern and F");
+  size_t nF = (size_t)9 * mesh->npe * mesh->nel;
+  double *dF = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &dF, nF));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(dF, Felem, sizeof(double) * nF, cudaMemcpyHostToDevice, ctx->stream));
+  llf_matrix *m;
+  int rc;
+  if ((rc = new_matrix(ctx, pat, out, &m))) { dfree(ctx, dF); return rc; }
+  rc = tl_tangent_impl(ctx, mesh, pat, dF, law, params, nparams, m);
+  dfree(ctx, dF);
+  return finish_matrix(ctx, rc, m, out);
+}
+
 int llf_tl_initial_stress(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *Selem,
                           const double *Celem, int law, const double *params, int nparams,
                           llf_matrix **out) {

@@ -202,6 +202,8 @@ int pcg_batched_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doubl
 int tl_material_tangent_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
                              const double *d_F, int law, const double *params,
                              int nparams, llf_matrix *m);
+int tl_tangent_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *d_F, int law,
+                    const double *params, int nparams, llf_matrix *m);
 int tl_initial_stress_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
                            const double *d_S, const double *d_C, int law,
                            const double *params, int nparams, llf_matrix *m);

@@ -380,6 +380,12 @@ void enqueue_iteration(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const do
 }
 
 template <int P>
+int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
+             const Seg &S, double *r, double *z, double *u, double *c, double *xw, double *pinv,
+             double *part, int precond, double reltol, int64_t maxiter, bool use_graph, SegState *hst);
+int pcg_outcome(llf_ctx *ctx, int nseg, const SegState *hst, int64_t *iters, double *relres);
+
+template <int P>
 int pcg_segments(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                  const uint8_t *d_fixed, int nseg, const int64_t *seg_off, int precond,
                  double reltol, int64_t maxiter, int64_t *iters, double *relres) {
@@ -425,6 +431,31 @@ int pcg_segments(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_sf, sf.data(), sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, s));
   LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_active, 0, sizeof(int), s));
   Seg S{d_cb, d_ce, d_cs, d_sf, nch, nseg, d_st, d_active};
+  std::vector<SegState> hst(nseg);
+  int rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, precond, reltol, maxiter,
+                       !ctx->profiling, hst.data());
+  dfree(ctx, d_cb); dfree(ctx, d_ce); dfree(ctx, d_cs); dfree(ctx, d_sf); dfree(ctx, d_active);
+  dfree(ctx, d_st); dfree(ctx, r); dfree(ctx, z); dfree(ctx, u); dfree(ctx, c); dfree(ctx, xw);
+  dfree(ctx, pinv); dfree(ctx, part);
+  if (rc != LLF_OK) return rc;
+  return pcg_outcome(ctx, nseg, hst.data(), iters, relres);
+}
+
+// Runs the CG of every segment of S to completion with caller-provided
+// device buffers (r, z, u, c, xw of ndof doubles, pinv of ndof or ndof*P,
+// part of nchunks) and copies the final per-segment states into hst.
+// Allocates no device memory; with use_graph the iteration runs are captured
+// once into a CUDA graph and replayed.
+template <int P>
+int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
+             const Seg &S, double *r, double *z, double *u, double *c, double *xw, double *pinv,
+             double *part, int precond, double reltol, int64_t maxiter, bool use_graph, SegState *hst) {
+  const llf_pattern *pat = m->pat;
+  const int64_t n = pat->ndof;
+  const int64_t nch = S.nchunks;
+  const int nseg = S.nseg;
+  cudaStream_t s = ctx->stream;
+  int *d_active = S.active;
   const unsigned gch = (unsigned)std::max<int64_t>(1, std::min<int64_t>(nch, (int64_t)ctx->num_sms * 8));
   const unsigned gseg = (unsigned)std::max(1, std::min(nseg, ctx->num_sms * 8));
   const unsigned gv = (unsigned)(ctx->num_sms * 4);
@@ -441,7 +472,7 @@ int pcg_segments(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d
   // capture a run of iterations once, replay until every segment is done
   const int per_graph = 16;
   cudaGraphExec_t exec = nullptr;
-  bool graph_ok = !ctx->profiling;
+  bool graph_ok = use_graph;
   if (graph_ok) {
     cudaGraph_t graph = nullptr;
     if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
@@ -475,12 +506,14 @@ int pcg_segments(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d
   if (exec) cudaGraphExecDestroy(exec);
   { KernelScope k(ctx, "k_cg_merge"); k_cg_merge<<<gv, CG_THREADS, 0, s>>>(xw, d_fixed, d_x, n); }
   LLF_CUDA_TRY(ctx, cudaGetLastError());
-  std::vector<SegState> hst(nseg);
-  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(hst.data(), d_st, sizeof(SegState) * nseg, cudaMemcpyDeviceToHost, s));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(hst, S.st, sizeof(SegState) * nseg, cudaMemcpyDeviceToHost, s));
   LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
-  dfree(ctx, d_cb); dfree(ctx, d_ce); dfree(ctx, d_cs); dfree(ctx, d_sf); dfree(ctx, d_active);
-  dfree(ctx, d_st); dfree(ctx, r); dfree(ctx, z); dfree(ctx, u); dfree(ctx, c); dfree(ctx, xw);
-  dfree(ctx, pinv); dfree(ctx, part);
+  return LLF_OK;
+}
+
+// Per-segment iteration counts and residuals; error for breakdown or
+// non-convergence (first offending system named).
+int pcg_outcome(llf_ctx *ctx, int nseg, const SegState *hst, int64_t *iters, double *relres) {
   int rc = LLF_OK;
   int worst = -1;
   for (int g = 0; g < nseg; ++g) {

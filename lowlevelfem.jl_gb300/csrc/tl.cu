@@ -19,8 +19,8 @@
 namespace {
 
 constexpr int TL_THREADS = 128;
-constexpr int QD = 64;  // per-point record: wq, invJ[9], F or S [9], D[36]
-enum { TL_KMAT = 0, TL_KGEO_S = 1, TL_KGEO_C = 2 };
+constexpr int QD = 64;  // per-point record: wq, invJ[9], F or S [9], D[36], S[9] (tangent)
+enum { TL_KMAT = 0, TL_KGEO_S = 1, TL_KGEO_C = 2, TL_KTAN = 3 };
 
 struct TLArgs {
   const double *xyz;
@@ -164,7 +164,7 @@ __device__ void tl_point(const TLArgs &A, int mode, int q, const double *sX, con
     return;
   }
   double C[3][3];
-  if (mode == TL_KMAT) {
+  if (mode == TL_KMAT || mode == TL_KTAN) {
     for (int I = 0; I < 3; ++I)
       for (int J2 = 0; J2 < 3; ++J2) {
         double acc = 0.0;
@@ -182,6 +182,9 @@ __device__ void tl_point(const TLArgs &A, int mode, int q, const double *sX, con
   if (mode == TL_KGEO_C)
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) rec[10 + 3 * i + j] = S[i][j];
+  if (mode == TL_KTAN)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) rec[55 + 3 * i + j] = S[i][j];
 }
 
 template <int MODE, int PPT>
@@ -194,7 +197,8 @@ __global__ void __launch_bounds__(TL_THREADS) k_tl_matrix(TLArgs A) {
   double *sG = qd + (size_t)nip * QD;      // npe*3
   double *sB = sG + npe * 3;               // npe*18
   double *sTb = sB + npe * 18;             // npe*18 (KMAT)
-  constexpr int BS = (MODE == TL_KMAT) ? 9 : 1;
+  constexpr bool MAT = (MODE == TL_KMAT || MODE == TL_KTAN);
+  constexpr int BS = MAT ? 9 : 1;
   for (int64_t e = blockIdx.x; e < A.nel; e += gridDim.x) {
     if (A.emat && A.emat[e] < 0) continue;
     for (int t = threadIdx.x; t < npe * 3; t += blockDim.x)
@@ -222,7 +226,7 @@ __global__ void __launch_bounds__(TL_THREADS) k_tl_matrix(TLArgs A) {
           sG[t] = s;
         }
         __syncthreads();
-        if (MODE == TL_KMAT) {
+        if (MAT) {
           // B(F) per node (src/nonlinear.jl:2219-2242)
           for (int t = threadIdx.x; t < npe * 3; t += blockDim.x) {
             int b = t / 3, j = t % 3;
@@ -254,7 +258,7 @@ __global__ void __launch_bounds__(TL_THREADS) k_tl_matrix(TLArgs A) {
           if (pi >= A.npairs) continue;
           int a, b;
           pair_dec(pi, npe, a, b);
-          if (MODE == TL_KMAT) {
+          if (MAT) {
             const double *Ba = sB + a * 18, *Tb = sTb + b * 18;
 #pragma unroll
             for (int i = 0; i < 3; ++i)
@@ -266,6 +270,22 @@ __global__ void __launch_bounds__(TL_THREADS) k_tl_matrix(TLArgs A) {
                 for (int I = 0; I < 6; ++I) s = __fma_rn(Ba[I * 3 + i], Tb[I * 3 + j], s);
                 acc[k][i * 3 + j] = s;
               }
+            if (MODE == TL_KTAN) {  // consistent tangent: geometric part from the same S
+              const double *S = rec + 55, *ga = sG + 3 * a, *gb = sG + 3 * b;
+              double tv[3];
+#pragma unroll
+              for (int I = 0; I < 3; ++I) {
+                double s = 0.0;
+#pragma unroll
+                for (int J2 = 0; J2 < 3; ++J2) s = __fma_rn(S[3 * I + J2], gb[J2], s);
+                tv[I] = s;
+              }
+              double v = 0.0;
+#pragma unroll
+              for (int I = 0; I < 3; ++I) v = __fma_rn(ga[I], tv[I], v);
+#pragma unroll
+              for (int i = 0; i < 3; ++i) acc[k][i * 3 + i] = __fma_rn(v, rec[0], acc[k][i * 3 + i]);
+            }
           } else {
             const double *S = rec + 10, *ga = sG + 3 * a, *gb = sG + 3 * b;
             double tv[3];
@@ -292,7 +312,7 @@ __global__ void __launch_bounds__(TL_THREADS) k_tl_matrix(TLArgs A) {
         pair_dec(pi, npe, a, b);
         double *ab = Ke + ((size_t)b * npe + a) * BS;   // block (a,b)
         double *ba = Ke + ((size_t)a * npe + b) * BS;   // mirror (b,a)
-        if (MODE == TL_KMAT) {
+        if (MAT) {
 #pragma unroll
           for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -415,7 +435,7 @@ int launch_matrix(llf_ctx *ctx, TLArgs a, size_t smem) {
     if (per_sm < 1) per_sm = 1;
     int64_t grid = (int64_t)ctx->num_sms * per_sm;
     if (grid > a.nel) grid = a.nel > 0 ? a.nel : 1;
-    KernelScope ks(ctx, MODE == TL_KMAT ? "k_tl_material" : "k_tl_geometric");
+    KernelScope ks(ctx, MODE == TL_KMAT ? "k_tl_material" : (MODE == TL_KTAN ? "k_tl_tangent" : "k_tl_geometric"));
     fn<<<(unsigned)grid, TL_THREADS, smem, ctx->stream>>>(a);
     LLF_CUDA_TRY(ctx, cudaGetLastError());
     return LLF_OK;
@@ -434,7 +454,8 @@ int tl_matrix(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int mode, const do
   if (rc) return rc;
   size_t smem = tl_smem(mesh->npe, mesh->nip, true);
   if (smem > 200 * 1024) return llf_fail(ctx, LLF_ERR_LIMIT, "element too large for the TL kernels");
-  const int BS = mode == TL_KMAT ? 9 : 1;
+  const bool mat = (mode == TL_KMAT || mode == TL_KTAN);
+  const int BS = mat ? 9 : 1;
   double *Kp = nullptr;
   int64_t *cnt = nullptr;
   LLF_CUDA_TRY(ctx, dalloc(ctx, &Kp, (size_t)mesh->nel * mesh->npe * mesh->npe * BS));
@@ -442,15 +463,15 @@ int tl_matrix(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int mode, const do
   LLF_CUDA_TRY(ctx, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (pat->ndof + 1), ctx->stream));
   a.out = Kp;
   rc = (mode == TL_KMAT) ? launch_matrix<TL_KMAT>(ctx, a, smem)
-                         : (mode == TL_KGEO_S ? launch_matrix<TL_KGEO_S>(ctx, a, smem)
-                                              : launch_matrix<TL_KGEO_C>(ctx, a, smem));
+       : (mode == TL_KTAN) ? launch_matrix<TL_KTAN>(ctx, a, smem)
+       : (mode == TL_KGEO_S ? launch_matrix<TL_KGEO_S>(ctx, a, smem) : launch_matrix<TL_KGEO_C>(ctx, a, smem));
   if (rc == LLF_OK) {
     cudaError_t e = dalloc(ctx, &m->d_nz, pat->nnz);
-    rc = (e == cudaSuccess) ? gather_full(ctx, pat, Kp, mode == TL_KMAT, m->d_nz, cnt)
+    rc = (e == cudaSuccess) ? gather_full(ctx, pat, Kp, mat, m->d_nz, cnt)
                             : llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
   }
   dfree(ctx, Kp);
-  if (rc == LLF_OK) rc = llf_check_status(ctx, mode == TL_KMAT ? "materialTangentMatrix" : "initialStressMatrix");
+  if (rc == LLF_OK) rc = llf_check_status(ctx, mat ? "materialTangentMatrix" : "initialStressMatrix");
   if (rc == LLF_OK) rc = matrix_finalize(ctx, m, cnt);
   dfree(ctx, cnt);
   return rc;
@@ -461,6 +482,11 @@ int tl_matrix(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int mode, const do
 int tl_material_tangent_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *d_F,
                              int law, const double *params, int nparams, llf_matrix *m) {
   return tl_matrix(ctx, mesh, pat, TL_KMAT, d_F, law, params, nparams, m);
+}
+
+int tl_tangent_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *d_F, int law,
+                    const double *params, int nparams, llf_matrix *m) {
+  return tl_matrix(ctx, mesh, pat, TL_KTAN, d_F, law, params, nparams, m);
 }
 
 int tl_initial_stress_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *d_S,

@@ -931,7 +931,7 @@ static int tl_element(int mode, int npe, int nip, const double *w, const double 
         g[3 * a + i] = s;
       }
     }
-    if (mode == 0) {
+    if (mode == 0 || mode == 3) {
       double F[3][3], C[3][3], S[3][3], D[36];
       interp_tensor(npe, Nq, Tn, F);
       right_cauchy_green(F, C);
@@ -957,6 +957,18 @@ static int tl_element(int mode, int npe, int nip, const double *w, const double 
               for (int I = 0; I < 6; ++I) s = fma(Bs[a * 18 + I * 3 + i], Ts[b * 18 + I * 3 + j], s);
               A[i * 3 + j] = s;
             }
+          if (mode == 3) {  /* consistent tangent: geometric part from the same S */
+            const double *ga = g + 3 * a, *gb = g + 3 * b;
+            double t[3];
+            for (int I = 0; I < 3; ++I) {
+              double s = 0.0;
+              for (int J = 0; J < 3; ++J) s = fma(S[I][J], gb[J], s);
+              t[I] = s;
+            }
+            double v = 0.0;
+            for (int I = 0; I < 3; ++I) v = fma(ga[I], t[I], v);
+            for (int i = 0; i < 3; ++i) A[i * 3 + i] = fma(v, wq, A[i * 3 + i]);
+          }
         }
     } else {
       double S[3][3];
@@ -991,7 +1003,7 @@ static int tl_element(int mode, int npe, int nip, const double *w, const double 
         for (int i = 0; i < 3; ++i)
           for (int j = 0; j < 3; ++j) {
             double v;
-            if (mode == 0)
+            if (mode == 0 || mode == 3)
               v = (a == b && j < i) ? A[j * 3 + i] : A[i * 3 + j];
             else
               v = (i == j) ? A[0] : 0.0;

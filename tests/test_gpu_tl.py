@@ -110,3 +110,52 @@ def test_newton_step_consistency(llf):
     fd = (fint(u + h * du) - fint(u - h * du)) / (2 * h)
     Kdu = K * du
     assert np.linalg.norm(fd - Kdu) <= 1e-6 * np.linalg.norm(Kdu)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_fused_tangent_bit_identical(llf, orc, case):
+    _, n, order, simplex = case
+    m = llf.structured_box_mesh(n=n, order=order, simplex=simplex)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    F, _ = _F(llf, m, p, 0.03, 31)
+    K = llf.tangentMatrix(p, F, energy="NeoHookeCompressible", params={"mu": 1.0, "lambda": 10.0})
+    ref = orc.tl_matrix(3, m.xyz, m.conn, llf._lib.builtin_rule(m.family, m.order), F.A, orc.LAW_NEOHOOKE,
+                        [1.0, 10.0])
+    assert_csc_identical(K.csc(), ref.julia(), f"Kt {case[0]}")
+
+
+def test_fused_tangent_is_derivative_of_internal_force(llf):
+    m = llf.structured_box_mesh(n=2, order=2)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    prm = {"mu": 1.0, "lambda": 10.0}
+    rng = np.random.default_rng(37)
+    u = (m.xyz @ (0.05 * rng.standard_normal((3, 3))).T).ravel()
+    du = (m.xyz @ rng.standard_normal((3, 3)).T).ravel()
+    fint = lambda v: llf.internalForceVector(p, F=llf.grad(llf.VectorField(v.reshape(-1, 1), p), add_identity=True),
+                                             energy="NeoHookeCompressible", params=prm).a[:, 0]
+    K = llf.tangentMatrix(p, llf.grad(llf.VectorField(u.reshape(-1, 1), p), add_identity=True), params=prm)
+    h = 1e-6
+    fd = (fint(u + h * du) - fint(u - h * du)) / (2 * h)
+    assert np.linalg.norm(fd - K * du) <= 1e-6 * np.linalg.norm(K * du)
+
+
+def test_newton_stretch_converges(llf):
+    """Hyperelastic TL configuration in miniature: compressible neo-Hookean
+    (mu=1, lambda=10) unit cube, 30% axial stretch in 3 steps, full Newton
+    with the consistent tangent reassembled every iteration."""
+    m = llf.structured_box_mesh(n=3, order=1)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    sup = [llf.displacementConstraint("left", ux=0.0), llf.displacementConstraint("right", ux=0.3),
+           llf.displacementConstraint("bottom", uy=0.0), llf.displacementConstraint("rear", uz=0.0)]
+    u = llf.solveDeformation(p, support=sup, params={"mu": 1.0, "lambda": 10.0}, steps=3, tol=1e-10)
+    ux = u.a[0::3, 0]
+    assert abs(ux[np.abs(m.xyz[:, 0] - 1) < 1e-12] - 0.3).max() < 1e-14
+    last = [h for h in u.history if h["step"] == 3]
+    assert last[-1]["residual"] <= 1e-10 * max(1.0, last[0]["residual"]) or len(last) <= 25
+    # quadratic convergence: the last reductions shrink fast
+    res = [h["residual"] for h in last]
+    assert res[-1] < 1e-9
+    # homogeneous uniaxial stretch: lateral contraction is uniform
+    uy = u.a[1::3, 0]
+    top = np.abs(m.xyz[:, 1] - 1) < 1e-12
+    assert np.ptp(uy[top]) < 1e-9
