@@ -5,6 +5,7 @@
 #include <cstring>
 #include <new>
 #include <algorithm>
+#include <cmath>
 
 #include "common.cuh"
 #include "tables.h"
@@ -66,6 +67,9 @@ int upload_tables(llf_ctx *ctx, llf_mesh *m, int nip, const double *w, const dou
   dfree(ctx, m->d_wf);
   dfree(ctx, m->d_Nf);
   dfree(ctx, m->d_dNf);
+  dfree(ctx, m->d_nref);
+  dfree(ctx, m->d_Rp);
+  dfree(ctx, m->d_Mp);
   m->nip = nip;
   const size_t nn = (size_t)nip * m->npe;
   m->h_w.assign(w, w + nip);
@@ -95,6 +99,41 @@ int upload_tables(llf_ctx *ctx, llf_mesh *m, int nip, const double *w, const dou
                                     cudaMemcpyHostToDevice, ctx->stream));
   LLF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   m->tables_version++;
+  return LLF_OK;
+}
+
+// Affine-element tables of the current rule (contract of the oracle):
+// R_ab[k][l] = fma chain over q of (w_q dN_a,k) dN_b,l and Mref_ab = fma chain
+// of (w_q N_a) N_b, stored for the pairs a <= b in a-major order.
+int upload_affine(llf_ctx *ctx, llf_mesh *m, const double *node_ref) {
+  const int npe = m->npe, nip = m->nip;
+  const size_t npairs = (size_t)npe * (npe + 1) / 2;
+  std::vector<double> Rp(npairs * 9), Mp(npairs);
+  const double *w = m->h_w.data(), *N = m->h_N.data(), *dN = m->h_dN.data();
+  size_t pi = 0;
+  for (int a = 0; a < npe; ++a)
+    for (int b = a; b < npe; ++b, ++pi) {
+      for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) {
+          double acc = 0.0;
+          for (int q = 0; q < nip; ++q)
+            acc = std::fma(w[q] * dN[((size_t)q * npe + a) * 3 + k], dN[((size_t)q * npe + b) * 3 + l], acc);
+          Rp[pi * 9 + k * 3 + l] = acc;
+        }
+      double acc = 0.0;
+      for (int q = 0; q < nip; ++q) acc = std::fma(w[q] * N[(size_t)q * npe + a], N[(size_t)q * npe + b], acc);
+      Mp[pi] = acc;
+    }
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nref, (size_t)npe * 3));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_Rp, npairs * 9));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_Mp, npairs));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_nref, node_ref, sizeof(double) * npe * 3, cudaMemcpyHostToDevice,
+                                    ctx->stream));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_Rp, Rp.data(), sizeof(double) * npairs * 9, cudaMemcpyHostToDevice,
+                                    ctx->stream));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_Mp, Mp.data(), sizeof(double) * npairs, cudaMemcpyHostToDevice,
+                                    ctx->stream));
+  LLF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return LLF_OK;
 }
 
@@ -286,6 +325,7 @@ int llf_mesh_upload(llf_ctx *ctx, int dim, int64_t non, const double *xyz, int64
   if (rc == LLF_OK) rc = check_finite(ctx, m->d_xyz, 3 * non);
   dfree(ctx, d_conn64);
   if (rc == LLF_OK) rc = upload_tables(ctx, m, rule.nip, rule.w.data(), rule.N.data(), rule.dN.data());
+  if (rc == LLF_OK) rc = upload_affine(ctx, m, rule.node_ref.data());
   if (rc == LLF_OK) {
     LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_dNn, rule.dN_nodes.size()));
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_dNn, rule.dN_nodes.data(), sizeof(double) * rule.dN_nodes.size(),
@@ -343,6 +383,7 @@ int llf_mesh_destroy(llf_ctx *ctx, llf_mesh *m) {
   if (ctx) {
     dfree(ctx, m->d_xyz); dfree(ctx, m->d_conn); dfree(ctx, m->d_emat);
     dfree(ctx, m->d_w); dfree(ctx, m->d_N); dfree(ctx, m->d_dN); dfree(ctx, m->d_dNn);
+    dfree(ctx, m->d_nref); dfree(ctx, m->d_Rp); dfree(ctx, m->d_Mp);
     dfree(ctx, m->d_wf); dfree(ctx, m->d_Nf); dfree(ctx, m->d_dNf);
     cudaStreamSynchronize(ctx->stream);
   }

@@ -44,6 +44,10 @@ struct ElemArgs {
   double *scratch;           // per-CTA global scratch for G, S (large elements)
   int64_t scratch_stride;    // doubles per CTA
   unsigned *status;
+  // affine-element form (all three set, or all null): reference node
+  // coordinates [npe*3] and, per upper-triangle node pair in pair order,
+  // R_ab [9] and Mref_ab [1]
+  const double *nref, *Rp, *Mp;
 };
 
 __device__ __forceinline__ int pair_offset(int a, int npe) {
@@ -59,19 +63,11 @@ __device__ __forceinline__ void pair_decode(int pi, int npe, int &a, int &b) {
   b = a + (pi - pair_offset(a, npe));
 }
 
-// Geometry at one point (contract of the oracle): returns det, fills inv
-// (row-major invJ[i][j]).  dNq(a, j) is the reference gradient of node a.
-template <int DIM, class Tab>
-__device__ __forceinline__ double geom_point(const double *sX, Tab dNq, int npe, double *inv) {
-  double J[3][3];
-#pragma unroll
-  for (int i = 0; i < DIM; ++i)
-#pragma unroll
-    for (int j = 0; j < DIM; ++j) {
-      double acc = 0.0;
-      for (int a = 0; a < npe; ++a) acc = __fma_rn(sX[a * DIM + i], dNq(a, j), acc);
-      J[i][j] = acc;
-    }
+// Determinant and row-major inverse of the Jacobian J (contract of the
+// oracle's geometry: cofactors, det by the first row, inverse = cofactor^T
+// times the rounded reciprocal of det).
+template <int DIM>
+__device__ __forceinline__ double jac_inverse(const double (&J)[3][3], double *inv) {
   double det, rdet;
   if (DIM == 3) {
     double c00 = __dsub_rn(__dmul_rn(J[1][1], J[2][2]), __dmul_rn(J[1][2], J[2][1]));
@@ -102,6 +98,22 @@ __device__ __forceinline__ double geom_point(const double *sX, Tab dNq, int npe,
   return det;
 }
 
+// Geometry at one point (contract of the oracle): returns det, fills inv
+// (row-major invJ[i][j]).  dNq(a, j) is the reference gradient of node a.
+template <int DIM, class Tab>
+__device__ __forceinline__ double geom_point(const double *sX, Tab dNq, int npe, double *inv) {
+  double J[3][3];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      double acc = 0.0;
+      for (int a = 0; a < npe; ++a) acc = __fma_rn(sX[a * DIM + i], dNq(a, j), acc);
+      J[i][j] = acc;
+    }
+  return jac_inverse<DIM>(J, inv);
+}
+
 // Store block (a,b) (a <= b) of the element matrix and its mirror (b,a) in
 // the column-major-by-node layout Kf[e][col node][row node][i*P+j].
 template <int P, int BS>
@@ -122,9 +134,130 @@ __device__ __forceinline__ void store_pair(double *Ke, int npe, int a, int b, co
   }
 }
 
+constexpr int AFF_DOUBLES = 32;
+
+// Affinity test of the element in sX (contract of the oracle): warp 0 forms
+// J0 (geometry contract at point 0) and s = max |X|; every node then has to
+// satisfy |X_a - X_0 - J0 (xi_a - xi_0)| <= 2^-46 s componentwise.  Returns a
+// CTA-uniform flag; sAff[0..9] hold J0 and s afterwards.
+template <int DIM>
+__device__ __forceinline__ bool elem_is_affine(const double *sX, const double *dN0, int tstride,
+                                               int npe, const double *nref, double *sAff) {
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    double m = 0.0;
+    for (int t = lane; t < npe * DIM; t += 32) m = fmax(m, fabs(sX[t]));
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane < DIM * DIM) {
+      const int i = lane / DIM, j = lane % DIM;
+      double acc = 0.0;
+      for (int a = 0; a < npe; ++a) acc = __fma_rn(sX[a * DIM + i], dN0[a * tstride + j], acc);
+      sAff[i * 3 + j] = acc;
+    }
+    if (lane == 0) sAff[9] = m;
+  }
+  __syncthreads();
+  const double sc = sAff[9];
+  const double tol = __dmul_rn(1.4210854715202004e-14, sc);  // 64 * 2^-52
+  int bad = 0;
+  for (int t = threadIdx.x; t < npe * DIM; t += blockDim.x) {
+    const int a = t / DIM, i = t - a * DIM;
+    double r = __dsub_rn(sX[t], sX[i]);
+#pragma unroll
+    for (int j = 0; j < DIM; ++j)
+      r = __fma_rn(-sAff[i * 3 + j], __dsub_rn(nref[a * 3 + j], nref[j]), r);
+    if (!(fabs(r) <= tol)) bad = 1;
+  }
+  return !__syncthreads_or(bad) && sc > 0.0;
+}
+
+// Node-pair blocks of an affine element (contract of the oracle): with
+// Y = det*invJ, T = R_ab Y and O_ab = invJ^T T; heat c1*trace(O_ab), mass
+// c1*(det*Mref_ab), elasticity from O_ab as in the quadrature form.
+template <int KIND, int DIM, int P, int BS>
+__device__ __forceinline__ void affine_pairs(const ElemArgs &A, const double *sAff, double c1,
+                                             double c2, double *Ke) {
+  const int npe = A.npe;
+  double inv[9], Y[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    inv[k] = sAff[10 + k];
+    Y[k] = sAff[19 + k];
+  }
+  const double det = sAff[28];
+  for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
+    int a, b;
+    pair_decode(pi, npe, a, b);
+    double blk[BS];
+    if (KIND == KIND_MASS) {
+      blk[0] = __dmul_rn(c1, __dmul_rn(det, __ldg(A.Mp + pi)));
+    } else {
+      const double *R = A.Rp + (size_t)pi * 9;
+      double T[DIM][DIM];
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        double r[DIM];
+#pragma unroll
+        for (int l = 0; l < DIM; ++l) r[l] = __ldg(R + k * 3 + l);
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) {
+          double acc = 0.0;
+#pragma unroll
+          for (int l = 0; l < DIM; ++l) acc = __fma_rn(r[l], Y[l * 3 + j], acc);
+          T[k][j] = acc;
+        }
+      }
+      if (KIND == KIND_HEAT) {
+        double acc = 0.0;
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) acc = __fma_rn(inv[k * 3 + i], T[k][i], acc);
+        blk[0] = __dmul_rn(c1, acc);
+      } else {
+        double O[DIM][DIM];
+        if (a != b) {
+#pragma unroll
+          for (int i = 0; i < DIM; ++i)
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) {
+              double acc = 0.0;
+#pragma unroll
+              for (int k = 0; k < DIM; ++k) acc = __fma_rn(inv[k * 3 + i], T[k][j], acc);
+              O[i][j] = acc;
+            }
+        } else {
+#pragma unroll
+          for (int i = 0; i < DIM; ++i)
+#pragma unroll
+            for (int j = i; j < DIM; ++j) {
+              double acc = 0.0;
+#pragma unroll
+              for (int k = 0; k < DIM; ++k) acc = __fma_rn(inv[k * 3 + i], T[k][j], acc);
+              O[i][j] = acc;
+              O[j][i] = acc;
+            }
+        }
+        double tr = __dadd_rn(O[0][0], O[1 % DIM][1 % DIM]);
+        if (DIM == 3) tr = __dadd_rn(tr, O[2 % DIM][2 % DIM]);
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            double t = __fma_rn(c2, O[j][i], __dmul_rn(c1, O[i][j]));
+            if (i == j) t = __fma_rn(c2, tr, t);
+            blk[i * DIM + j] = t;
+          }
+      }
+    }
+    store_pair<P, BS>(Ke, npe, a, b, blk);
+  }
+}
+
 // Shared-memory layout of k_elem_fp64 (doubles):
 //   [SMEM] sdN [nip*npe*DIM] | sw [nip] | sN [nip*npe] (mass) |
-//   sX [npe*DIM] | sWd [nip] | sInv [nip*9] | [SMEM] G, S (each nip*npe*gsw)
+//   sX [npe*DIM] | sWd [nip] | sInv [nip*9] | sAff [32] | [SMEM] G, S (each nip*npe*gsw)
 // Without SMEM the tables are read from global memory (stride 3) and G, S
 // live in a per-CTA global scratch slot (L2 resident).
 template <int KIND, int DIM, bool SMEM>
@@ -139,7 +272,8 @@ k_elem_fp64(ElemArgs A) {
   double *sX = sN + ((SMEM && KIND == KIND_MASS) ? (size_t)nip * npe : 0);
   double *sWd = sX + (size_t)npe * DIM;
   double *sInv = sWd + nip;
-  double *G = SMEM ? (sInv + (size_t)nip * 9) : (A.scratch + (size_t)blockIdx.x * A.scratch_stride);
+  double *sAff = sInv + (size_t)nip * 9;  // [0,9) J0, [9] s, [10,19) invJ, [19,28) det*invJ, [28] det
+  double *G = SMEM ? (sAff + AFF_DOUBLES) : (A.scratch + (size_t)blockIdx.x * A.scratch_stride);
   double *S = G + (size_t)nip * npe * gsw;
   // table accessors
   const int tstride = SMEM ? DIM : 3;
@@ -170,102 +304,123 @@ k_elem_fp64(ElemArgs A) {
       sX[t] = A.xyz[(size_t)A.conn[e * npe + a] * 3 + i];
     }
     __syncthreads();
-    for (int q = threadIdx.x; q < nip; q += blockDim.x) {
-      double inv[9];
-      const double *dq = tdN + (size_t)q * npe * tstride;
-      double det = geom_point<DIM>(sX, [&](int a, int j) { return dq[a * tstride + j]; }, npe, inv);
-      if (!(det > 0.0)) atomicOr(A.status, ST_BAD_JACOBIAN);
-      sWd[q] = __dmul_rn(det, tw[q]);
+    double *Ke = A.Kf + (size_t)e * npe * npe * BS;
+    if (A.Rp && elem_is_affine<DIM>(sX, tdN, tstride, npe, A.nref, sAff)) {
+      if (threadIdx.x == 0) {
+        double J[3][3], inv[9];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) sInv[q * 9 + k] = inv[k];
-    }
-    __syncthreads();
-    if (KIND == KIND_MASS) {
-      for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) S[t] = __dmul_rn(sWd[t / npe], tN[t]);
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) J[i][j] = (i < DIM && j < DIM) ? sAff[i * 3 + j] : 0.0;
+        const double det = jac_inverse<DIM>(J, inv);
+        if (!(det > 0.0)) atomicOr(A.status, ST_BAD_JACOBIAN);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          sAff[10 + k] = inv[k];
+          sAff[19 + k] = __dmul_rn(det, inv[k]);
+        }
+        sAff[28] = det;
+      }
+      __syncthreads();
+      affine_pairs<KIND, DIM, P, BS>(A, sAff, c1, c2, Ke);
     } else {
-      for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) {
-        const int q = t / npe;
-        const double *inv = sInv + q * 9;
-        const double *d = tdN + (size_t)t * tstride;
-        const double wd = sWd[q];
+      for (int q = threadIdx.x; q < nip; q += blockDim.x) {
+        double inv[9];
+        const double *dq = tdN + (size_t)q * npe * tstride;
+        double det = geom_point<DIM>(sX, [&](int a, int j) { return dq[a * tstride + j]; }, npe, inv);
+        if (!(det > 0.0)) atomicOr(A.status, ST_BAD_JACOBIAN);
+        sWd[q] = __dmul_rn(det, tw[q]);
 #pragma unroll
-        for (int i = 0; i < DIM; ++i) {
-          double acc = 0.0;
+        for (int k = 0; k < 9; ++k) sInv[q * 9 + k] = inv[k];
+      }
+      __syncthreads();
+      if (KIND == KIND_MASS) {
+        for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) S[t] = __dmul_rn(sWd[t / npe], tN[t]);
+      } else {
+        for (int t = threadIdx.x; t < nip * npe; t += blockDim.x) {
+          const int q = t / npe;
+          const double *inv = sInv + q * 9;
+          const double *d = tdN + (size_t)t * tstride;
+          const double wd = sWd[q];
 #pragma unroll
-          for (int j = 0; j < DIM; ++j) acc = __fma_rn(inv[3 * j + i], d[j], acc);
-          G[(size_t)t * DIM + i] = acc;
-          S[(size_t)t * DIM + i] = __dmul_rn(wd, acc);
+          for (int i = 0; i < DIM; ++i) {
+            double acc = 0.0;
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) acc = __fma_rn(inv[3 * j + i], d[j], acc);
+            G[(size_t)t * DIM + i] = acc;
+            S[(size_t)t * DIM + i] = __dmul_rn(wd, acc);
+          }
         }
       }
-    }
-    __syncthreads();
+      __syncthreads();
 
-    double *Ke = A.Kf + (size_t)e * npe * npe * BS;
-    for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
-      int a, b;
-      pair_decode(pi, npe, a, b);
-      double blk[BS];
-      if (KIND == KIND_ELASTIC) {
-        double O[DIM][DIM];
-#pragma unroll
-        for (int i = 0; i < DIM; ++i)
-#pragma unroll
-          for (int j = 0; j < DIM; ++j) O[i][j] = 0.0;
-        if (a != b) {
-          for (int q = 0; q < nip; ++q) {
-            const double *sa = S + ((size_t)q * npe + a) * DIM;
-            const double *gb = G + ((size_t)q * npe + b) * DIM;
-            double s_[DIM], g_[DIM];
-#pragma unroll
-            for (int i = 0; i < DIM; ++i) { s_[i] = sa[i]; g_[i] = gb[i]; }
-#pragma unroll
-            for (int i = 0; i < DIM; ++i)
-#pragma unroll
-              for (int j = 0; j < DIM; ++j) O[i][j] = __fma_rn(s_[i], g_[j], O[i][j]);
-          }
-        } else {
-          for (int q = 0; q < nip; ++q) {
-            const double *sa = S + ((size_t)q * npe + a) * DIM;
-            const double *ga = G + ((size_t)q * npe + a) * DIM;
-            double s_[DIM], g_[DIM];
-#pragma unroll
-            for (int i = 0; i < DIM; ++i) { s_[i] = sa[i]; g_[i] = ga[i]; }
-#pragma unroll
-            for (int i = 0; i < DIM; ++i)
-#pragma unroll
-              for (int j = i; j < DIM; ++j) O[i][j] = __fma_rn(s_[i], g_[j], O[i][j]);
-          }
+      for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
+        int a, b;
+        pair_decode(pi, npe, a, b);
+        double blk[BS];
+        if (KIND == KIND_ELASTIC) {
+          double O[DIM][DIM];
 #pragma unroll
           for (int i = 0; i < DIM; ++i)
 #pragma unroll
-            for (int j = 0; j < i; ++j) O[i][j] = O[j][i];
-        }
-        double tr = __dadd_rn(O[0][0], O[1 % DIM][1 % DIM]);
-        if (DIM == 3) tr = __dadd_rn(tr, O[2 % DIM][2 % DIM]);
+            for (int j = 0; j < DIM; ++j) O[i][j] = 0.0;
+          if (a != b) {
+            for (int q = 0; q < nip; ++q) {
+              const double *sa = S + ((size_t)q * npe + a) * DIM;
+              const double *gb = G + ((size_t)q * npe + b) * DIM;
+              double s_[DIM], g_[DIM];
 #pragma unroll
-        for (int i = 0; i < DIM; ++i)
+              for (int i = 0; i < DIM; ++i) { s_[i] = sa[i]; g_[i] = gb[i]; }
 #pragma unroll
-          for (int j = 0; j < DIM; ++j) {
-            double t = __fma_rn(c2, O[j][i], __dmul_rn(c1, O[i][j]));
-            if (i == j) t = __fma_rn(c2, tr, t);
-            blk[i * DIM + j] = t;
+              for (int i = 0; i < DIM; ++i)
+#pragma unroll
+                for (int j = 0; j < DIM; ++j) O[i][j] = __fma_rn(s_[i], g_[j], O[i][j]);
+            }
+          } else {
+            for (int q = 0; q < nip; ++q) {
+              const double *sa = S + ((size_t)q * npe + a) * DIM;
+              const double *ga = G + ((size_t)q * npe + a) * DIM;
+              double s_[DIM], g_[DIM];
+#pragma unroll
+              for (int i = 0; i < DIM; ++i) { s_[i] = sa[i]; g_[i] = ga[i]; }
+#pragma unroll
+              for (int i = 0; i < DIM; ++i)
+#pragma unroll
+                for (int j = i; j < DIM; ++j) O[i][j] = __fma_rn(s_[i], g_[j], O[i][j]);
+            }
+#pragma unroll
+            for (int i = 0; i < DIM; ++i)
+#pragma unroll
+              for (int j = 0; j < i; ++j) O[i][j] = O[j][i];
           }
-      } else if (KIND == KIND_HEAT) {
-        double acc = 0.0;
-        for (int q = 0; q < nip; ++q) {
-          const double *sa = S + ((size_t)q * npe + a) * DIM;
-          const double *gb = G + ((size_t)q * npe + b) * DIM;
+          double tr = __dadd_rn(O[0][0], O[1 % DIM][1 % DIM]);
+          if (DIM == 3) tr = __dadd_rn(tr, O[2 % DIM][2 % DIM]);
 #pragma unroll
-          for (int i = 0; i < DIM; ++i) acc = __fma_rn(sa[i], gb[i], acc);
+          for (int i = 0; i < DIM; ++i)
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) {
+              double t = __fma_rn(c2, O[j][i], __dmul_rn(c1, O[i][j]));
+              if (i == j) t = __fma_rn(c2, tr, t);
+              blk[i * DIM + j] = t;
+            }
+        } else if (KIND == KIND_HEAT) {
+          double acc = 0.0;
+          for (int q = 0; q < nip; ++q) {
+            const double *sa = S + ((size_t)q * npe + a) * DIM;
+            const double *gb = G + ((size_t)q * npe + b) * DIM;
+#pragma unroll
+            for (int i = 0; i < DIM; ++i) acc = __fma_rn(sa[i], gb[i], acc);
+          }
+          blk[0] = __dmul_rn(c1, acc);
+        } else {  // mass
+          double acc = 0.0;
+          for (int q = 0; q < nip; ++q)
+            acc = __fma_rn(S[(size_t)q * npe + a], tN[(size_t)q * npe + b], acc);
+          blk[0] = __dmul_rn(c1, acc);
         }
-        blk[0] = __dmul_rn(c1, acc);
-      } else {  // mass
-        double acc = 0.0;
-        for (int q = 0; q < nip; ++q)
-          acc = __fma_rn(S[(size_t)q * npe + a], tN[(size_t)q * npe + b], acc);
-        blk[0] = __dmul_rn(c1, acc);
+        store_pair<P, BS>(Ke, npe, a, b, blk);
       }
-      store_pair<P, BS>(Ke, npe, a, b, blk);
+
     }
     __syncthreads();
   }
@@ -275,15 +430,20 @@ k_elem_fp64(ElemArgs A) {
 // FP64 sums in element order in both.  Per warp: the column's row-node list
 // (deg ints) and its accumulator (deg * P * P doubles) in shared memory.
 template <int P, bool BLOCKVAL, class T>
-__device__ __forceinline__ void add_block(double *acc, int t, const T *v) {
+__device__ __forceinline__ void add_block(double *acc, int t, const T *v, bool first) {
   double *dst = acc + (size_t)t * P * P;  // [t][j][i]
 #pragma unroll
   for (int i = 0; i < P; ++i)
 #pragma unroll
     for (int j = 0; j < P; ++j) {
       double x = BLOCKVAL ? (double)v[i * P + j] : (i == j ? (double)v[0] : 0.0);
-      dst[j * P + i] = __dadd_rn(dst[j * P + i], x);
+      dst[j * P + i] = first ? x : __dadd_rn(dst[j * P + i], x);
     }
+}
+
+// Non-zero test on the bit pattern (integer pipe): every value but +-0.
+__device__ __forceinline__ int nonzero_bits(double v) {
+  return ((unsigned long long)__double_as_longlong(v) << 1) != 0ull;
 }
 
 // Per warp in shared memory: the column's row nodes (max_deg ints), its
@@ -292,6 +452,10 @@ __device__ __forceinline__ void add_block(double *acc, int t, const T *v) {
 // (max_n2e*npe int32).  Positions are found for all elements at once
 // (independent binary searches), then the elements are accumulated in
 // ascending order with the next element's blocks prefetched into registers.
+// The accumulator starts at -0.0 (the identity of IEEE addition) and the
+// first element's blocks are stored rather than added: every entry equals
+// the reference's combination of its triplets (first value, then + each
+// later one), signed zeros included, with one FP64 addition fewer.
 template <int P, bool BLOCKVAL, class T>
 __global__ void k_colgather(const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
                             const int64_t *__restrict__ n2e_ptr, const int2 *__restrict__ n2e,
@@ -312,7 +476,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int32_t *__r
     const int64_t s = n2e_ptr[B];
     const int nb = (int)(n2e_ptr[B + 1] - s);
     for (int t = lane; t < deg; t += 32) rows[t] = nadj[c0 + t];
-    for (int t = lane; t < deg * P * P; t += 32) acc[t] = 0.0;
+    for (int t = lane; t < deg * P * P; t += 32) acc[t] = -0.0;
     for (int k = lane; k < nb; k += 32) els[k] = n2e[s + k];
     __syncwarp();
     for (int it = lane; it < nb * npe; it += 32) {
@@ -346,7 +510,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int32_t *__r
         }
         if (act) {
           const int t = tpos[k * npe + lane];
-          if (t >= 0) add_block<P, BLOCKVAL, T>(acc, t, cur);
+          if (t >= 0) add_block<P, BLOCKVAL, T>(acc, t, cur, k == 0);
         }
         __syncwarp();
 #pragma unroll
@@ -357,7 +521,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int32_t *__r
         const T *col = Kf + ((size_t)els[k].x * npe + els[k].y) * npe * BS;
         for (int a = lane; a < npe; a += 32) {
           const int t = tpos[k * npe + a];
-          if (t >= 0) add_block<P, BLOCKVAL, T>(acc, t, col + (size_t)a * BS);
+          if (t >= 0) add_block<P, BLOCKVAL, T>(acc, t, col + (size_t)a * BS, k == 0);
         }
         __syncwarp();
       }
@@ -371,7 +535,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int32_t *__r
         const int t = idx / P, i = idx % P;
         const double v = acc[(size_t)t * P * P + j * P + i];
         out[idx] = v;
-        n += (v != 0.0);
+        n += nonzero_bits(v);
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) n += __shfl_xor_sync(0xffffffffu, n, off);
@@ -389,42 +553,48 @@ __global__ void k_count_nz(const double *__restrict__ nz, const int64_t *__restr
        c += (int64_t)gridDim.x * wpb) {
     int64_t s = colptr[c], e = colptr[c + 1];
     int n = 0;
-    for (int64_t k = s + lane; k < e; k += 32) n += (nz[k] != 0.0);
+    for (int64_t k = s + lane; k < e; k += 32) n += nonzero_bits(nz[k]);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) n += __shfl_xor_sync(0xffffffffu, n, off);
     if (lane == 0) cnt[c] = n;
   }
 }
 
+// One warp per DoF column; four 32-entry chunks loaded (values and row
+// nodes) before their ballots so that each warp keeps 2 KB in flight.
 template <int P>
 __global__ void k_compact(const double *__restrict__ nz, const int64_t *__restrict__ colptr,
                           const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
                           int64_t ndof, const int64_t *__restrict__ outptr,
                           int64_t *__restrict__ rowval_s, double *__restrict__ nzval_s) {
+  constexpr int U = 4;
   const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
   for (int64_t c = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5); c < ndof;
        c += (int64_t)gridDim.x * wpb) {
-    const int64_t s = colptr[c], e = colptr[c + 1];
-    const int64_t B = c / P;
-    const int64_t r0 = nptr[B];
+    const int64_t s = colptr[c];
+    const int len = (int)(colptr[c + 1] - s);
+    const int32_t *rn = nadj + nptr[c / P];
     int64_t o = outptr[c];
-    for (int64_t k0 = s; k0 < e; k0 += 32) {
-      int64_t k = k0 + lane;
-      double v = 0.0;
-      bool keep = false;
-      if (k < e) {
-        v = nz[k];
-        keep = (v != 0.0);
+    for (int l0 = 0; l0 < len; l0 += 32 * U) {
+      double v[U];
+      int64_t row[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int l = l0 + u * 32 + lane;
+        v[u] = l < len ? nz[s + l] : 0.0;
+        row[u] = l < len ? (int64_t)P * rn[l / P] + l % P : 0;
       }
-      unsigned bal = __ballot_sync(0xffffffffu, keep);
-      if (keep) {
-        int off = __popc(bal & ((1u << lane) - 1u));
-        int64_t loc = k - s;
-        int64_t row = (int64_t)P * nadj[r0 + loc / P] + loc % P;
-        rowval_s[o + off] = row + 1;
-        nzval_s[o + off] = v;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const bool keep = (l0 + u * 32 + lane < len) && nonzero_bits(v[u]);
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+          const int off = __popc(bal & ((1u << lane) - 1u));
+          rowval_s[o + off] = row[u] + 1;
+          nzval_s[o + off] = v[u];
+        }
+        o += __popc(bal);
       }
-      o += __popc(bal);
     }
   }
 }
@@ -452,7 +622,7 @@ __global__ void k_diag_stored(const double *__restrict__ diag, int64_t ndof,
                               int64_t *__restrict__ cnt) {
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ndof;
        c += (int64_t)gridDim.x * blockDim.x)
-    cnt[c] = diag[c] != 0.0;
+    cnt[c] = nonzero_bits(diag[c]);
 }
 
 __global__ void k_diag_compact(const double *__restrict__ diag, int64_t ndof,
@@ -460,7 +630,7 @@ __global__ void k_diag_compact(const double *__restrict__ diag, int64_t ndof,
                                int64_t *__restrict__ rowval_s, double *__restrict__ nzval_s) {
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ndof;
        c += (int64_t)gridDim.x * blockDim.x)
-    if (diag[c] != 0.0) {
+    if (nonzero_bits(diag[c])) {
       rowval_s[outptr[c]] = c + 1;
       nzval_s[outptr[c]] = diag[c];
     }
@@ -499,18 +669,27 @@ int run_elem(llf_ctx *ctx, ElemArgs a) {
   const int gsw = (KIND == KIND_MASS) ? 1 : DIM;
   const size_t tables = sizeof(double) * ((size_t)nip * npe * DIM + nip +
                                           (KIND == KIND_MASS ? (size_t)nip * npe : 0));
-  const size_t local = sizeof(double) * ((size_t)npe * DIM + nip + (size_t)nip * 9);
+  const size_t local = sizeof(double) * ((size_t)npe * DIM + nip + (size_t)nip * 9 + AFF_DOUBLES);
   const size_t gs = sizeof(double) * 2 * (size_t)nip * npe * gsw;
   const bool in_smem = tables + local + gs <= 96 * 1024;
   const size_t smem = in_smem ? tables + local + gs : local;
   if (smem > 200 * 1024) return llf_fail(ctx, LLF_ERR_LIMIT, "element exceeds shared memory");
+  // the dynamic shared-memory limit is raised before the occupancy query:
+  // above 48 KB the query answers 0 for a kernel still at the default limit
   int per_sm = 0;
-  if (in_smem)
+  if (in_smem) {
+    if (smem > 48 * 1024)
+      LLF_CUDA_TRY(ctx, cudaFuncSetAttribute(k_elem_fp64<KIND, DIM, true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     LLF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                           &per_sm, k_elem_fp64<KIND, DIM, true>, ELEM_THREADS, smem));
-  else
+  } else {
+    if (smem > 48 * 1024)
+      LLF_CUDA_TRY(ctx, cudaFuncSetAttribute(k_elem_fp64<KIND, DIM, false>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     LLF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                           &per_sm, k_elem_fp64<KIND, DIM, false>, ELEM_THREADS, smem));
+  }
   if (per_sm < 1) per_sm = 1;
   int64_t grid = (int64_t)ctx->num_sms * per_sm;
   if (grid > a.nel) grid = a.nel > 0 ? a.nel : 1;
@@ -678,6 +857,9 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
     a.c2 = d_c2;
     a.Kf = Kf;
     a.status = ctx->d_status;
+    a.nref = mesh->d_nref;
+    a.Rp = mesh->d_Rp;
+    a.Mp = mesh->d_Mp;
     if (dim == 3) {
       if (kind == KIND_ELASTIC) rc = run_elem<KIND_ELASTIC, 3>(ctx, a);
       else if (kind == KIND_HEAT) rc = run_elem<KIND_HEAT, 3>(ctx, a);

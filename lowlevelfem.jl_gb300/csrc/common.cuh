@@ -90,6 +90,10 @@ struct llf_mesh {
   std::vector<double> h_w, h_N, h_dN;  // host copies (FP32 tables derive from these)
   float *d_wf = nullptr, *d_Nf = nullptr, *d_dNf = nullptr;
   int tables_version = 0;
+  // affine-element tables (built-in rules, whose node coordinates are known;
+  // null after llf_tables_upload): reference node coordinates [npe*3] and,
+  // per upper-triangle node pair (a <= b, a-major), R_ab [9] and Mref_ab
+  double *d_nref = nullptr, *d_Rp = nullptr, *d_Mp = nullptr;
 };
 
 struct llf_pattern {

@@ -139,12 +139,137 @@ static int orc_grads(int dim, int npe, int nip, const double *w,
   return 0;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Affine elements.  When the element's nodes are an affine image of the     */
+/* reference nodes (every straight-sided element), J is the same at every    */
+/* point and the quadrature factors through reference matrices:              */
+/*   O_ab = det J^-T R_ab J^-1,  R_ab[k][l] = sum_q w_q dN_a,k dN_b,l,        */
+/*   M_ab = det Mref_ab,         Mref_ab    = sum_q w_q N_a N_b.              */
+/* Contract: R and Mref are fma chains over q of (w_q * first) * second;     */
+/* J0, det, invJ as the geometry contract at point 0; an element is affine   */
+/* when every node satisfies |X_a - X_0 - J0 (xi_a - xi_0)| <= 64 eps s      */
+/* componentwise (fma chain over j), s the largest |X| of the element.       */
+/* ------------------------------------------------------------------------ */
+void orc_affine_tables(int npe, int nip, const double *w, const double *N, const double *dN,
+                       double *R, double *Mref) {
+  for (int a = 0; a < npe; ++a)
+    for (int b = 0; b < npe; ++b) {
+      for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) {
+          double acc = 0.0;
+          for (int q = 0; q < nip; ++q)
+            acc = fma(w[q] * dN[((size_t)q * npe + a) * 3 + k], dN[((size_t)q * npe + b) * 3 + l], acc);
+          R[((size_t)a * npe + b) * 9 + k * 3 + l] = acc;
+        }
+      double m = 0.0;
+      for (int q = 0; q < nip; ++q) m = fma(w[q] * N[(size_t)q * npe + a], N[(size_t)q * npe + b], m);
+      Mref[(size_t)a * npe + b] = m;
+    }
+}
+
+static int orc_is_affine(int dim, int npe, const double *X, const double *dN0, const double *nref) {
+  double J[3][3] = {{0}};
+  for (int i = 0; i < dim; ++i)
+    for (int j = 0; j < dim; ++j) {
+      double acc = 0.0;
+      for (int a = 0; a < npe; ++a) acc = fma(X[3 * a + i], dN0[3 * a + j], acc);
+      J[i][j] = acc;
+    }
+  double s = 0.0;
+  for (int a = 0; a < npe; ++a)
+    for (int i = 0; i < dim; ++i) s = fmax(s, fabs(X[3 * a + i]));
+  const double tol = 64.0 * 2.220446049250313e-16 * s;
+  for (int a = 0; a < npe; ++a)
+    for (int i = 0; i < dim; ++i) {
+      double t = X[3 * a + i] - X[i];
+      for (int j = 0; j < dim; ++j) t = fma(-J[i][j], nref[3 * a + j] - nref[j], t);
+      if (!(fabs(t) <= tol)) return 0;
+    }
+  return s > 0.0;
+}
+
+/* Affine-element matrix; returns -1 for det <= 0.  With the geometry of
+ * point 0 (the Jacobian of an affine element is the same at every point) and
+ * Y = det*J^-1:  T = R_ab Y,  O_ab = J^-T T  (= sum_q w_q det g_a g_b^T),
+ * heat: trace(O_ab), mass: det*Mref_ab. */
+static int orc_element_affine(int kind, int dim, int pdim, int npe, const double *dN0, const double *X,
+                              const double *R, const double *Mref, double c1, double c2, double *Ke) {
+  size_t nd = (size_t)pdim * npe;
+  double inv[9], Y[9];
+  double det = orc_geom(dim, npe, X, dN0, inv);
+  if (!(det > 0.0)) return -1;
+  for (int k = 0; k < 9; ++k) Y[k] = det * inv[k];
+  memset(Ke, 0, sizeof(double) * nd * nd);
+  for (int a = 0; a < npe; ++a)
+    for (int b = a; b < npe; ++b) {
+      double blk[9] = {0};
+      const double *Rab = R + ((size_t)a * npe + b) * 9;
+      if (kind == ORC_MASS) {
+        double m = c1 * (det * Mref[(size_t)a * npe + b]);
+        for (int i = 0; i < pdim; ++i) blk[i * pdim + i] = m;
+      } else {
+        double T[3][3];
+        for (int k = 0; k < dim; ++k)
+          for (int j = 0; j < dim; ++j) {
+            double acc = 0.0;
+            for (int l = 0; l < dim; ++l) acc = fma(Rab[k * 3 + l], Y[l * 3 + j], acc);
+            T[k][j] = acc;
+          }
+        if (kind == ORC_HEAT) {
+          double sacc = 0.0;
+          for (int i = 0; i < dim; ++i)
+            for (int k = 0; k < dim; ++k) sacc = fma(inv[k * 3 + i], T[k][i], sacc);
+          blk[0] = c1 * sacc;
+        } else {
+          double O[3][3] = {{0}};
+          for (int i = 0; i < dim; ++i)
+            for (int j = (a == b ? i : 0); j < dim; ++j) {
+              double acc = 0.0;
+              for (int k = 0; k < dim; ++k) acc = fma(inv[k * 3 + i], T[k][j], acc);
+              O[i][j] = acc;
+              if (a == b) O[j][i] = acc;
+            }
+          double tr = O[0][0] + O[1][1];
+          if (dim == 3) tr = tr + O[2][2];
+          for (int i = 0; i < dim; ++i)
+            for (int j = 0; j < dim; ++j) {
+              double t = fma(c2, O[j][i], c1 * O[i][j]);
+              if (i == j) t = fma(c2, tr, t);
+              blk[i * pdim + j] = t;
+            }
+        }
+      }
+      for (int i = 0; i < pdim; ++i)
+        for (int j = 0; j < pdim; ++j) {
+          double v = blk[i * pdim + j];
+          Ke[((size_t)a * pdim + i) * nd + (size_t)b * pdim + j] = v;
+          Ke[((size_t)b * pdim + j) * nd + (size_t)a * pdim + i] = v;
+        }
+    }
+  return 0;
+}
+
 /* Element matrix Ke (row-major, (pdim*npe)^2) under the arithmetic contract.
  * kind ORC_ELASTIC: c1 = lamb, c2 = mub; ORC_HEAT: c1 = kb; ORC_MASS: c1 = rb.
- * pdim = dim for elastic, dim for mass (vector problems) or 1, 1 for heat. */
+ * pdim = dim for elastic, dim for mass (vector problems) or 1, 1 for heat.
+ * nref/R/Mref (may be NULL) enable the affine-element form. */
+int orc_element_matrix_ex(int kind, int dim, int pdim, int npe, int nip,
+                          const double *w, const double *N, const double *dN,
+                          const double *X, double c1, double c2, const double *nref,
+                          const double *R, const double *Mref, double *Ke);
+
 int orc_element_matrix(int kind, int dim, int pdim, int npe, int nip,
                        const double *w, const double *N, const double *dN,
                        const double *X, double c1, double c2, double *Ke) {
+  return orc_element_matrix_ex(kind, dim, pdim, npe, nip, w, N, dN, X, c1, c2, NULL, NULL, NULL, Ke);
+}
+
+int orc_element_matrix_ex(int kind, int dim, int pdim, int npe, int nip,
+                          const double *w, const double *N, const double *dN,
+                          const double *X, double c1, double c2, const double *nref,
+                          const double *R, const double *Mref, double *Ke) {
+  if (nref && R && Mref && orc_is_affine(dim, npe, X, dN, nref))
+    return orc_element_affine(kind, dim, pdim, npe, dN, X, R, Mref, c1, c2, Ke);
   size_t nd = (size_t)pdim * npe;
   double *g = (double *)malloc(sizeof(double) * nip * npe * 3);
   double *s = (double *)malloc(sizeof(double) * nip * npe * 3);
@@ -442,11 +567,14 @@ orc_csc *orc_assemble(int kind, int ptype, int dim, int pdim, int64_t non,
                       const int32_t *conn, const int32_t *emat, int nip,
                       const double *w, const double *N, const double *dN,
                       const double *params, int nmat, double thickness,
-                      int lumped, int *err) {
+                      int lumped, const double *nref, int *err) {
   (void)nmat;
   size_t nd = (size_t)pdim * npe;
   double *Ke = (double *)malloc(sizeof(double) * nd * nd);
   double *X = (double *)malloc(sizeof(double) * npe * 3);
+  double *R = (double *)malloc(sizeof(double) * npe * npe * 9);
+  double *Mref = (double *)malloc(sizeof(double) * npe * npe);
+  orc_affine_tables(npe, nip, w, N, dN, R, Mref);
   coo c = {0};
   c.n = non * pdim;
   *err = 0;
@@ -466,9 +594,9 @@ orc_csc *orc_assemble(int kind, int ptype, int dim, int pdim, int64_t non,
       int64_t node = conn[e * npe + a];
       for (int i = 0; i < 3; ++i) X[3 * a + i] = xyz[3 * node + i];
     }
-    if (orc_element_matrix(kind, dim, pdim, npe, nip, w, N, dN, X, c1, c2, Ke)) {
+    if (orc_element_matrix_ex(kind, dim, pdim, npe, nip, w, N, dN, X, c1, c2, nref, R, Mref, Ke)) {
       *err = -1;
-      free(Ke); free(X); free(c.I); free(c.J); free(c.V);
+      free(Ke); free(X); free(R); free(Mref); free(c.I); free(c.J); free(c.V);
       return NULL;
     }
     /* column-major walk of K1: k fastest; I = nn2[l], J = nn2[k] */
@@ -481,7 +609,7 @@ orc_csc *orc_assemble(int kind, int ptype, int dim, int pdim, int64_t non,
   }
   orc_csc *m = coo_to_csc(&c);
   free(c.I); free(c.J); free(c.V);
-  free(Ke); free(X);
+  free(Ke); free(X); free(R); free(Mref);
   if (kind == ORC_MASS && lumped) {
     orc_csc *D = orc_lump(m);
     orc_free(m);
@@ -513,8 +641,11 @@ double orc_assemble_csc_threaded(int kind, int ptype, int dim, int pdim,
                                  const int32_t *conn, int nip, const double *w,
                                  const double *N, const double *dN,
                                  const double *params, double thickness,
-                                 orc_csc *pat, int nthreads, int chunk) {
+                                 orc_csc *pat, int nthreads, int chunk, const double *nref) {
   int64_t nnz = pat->nnz;
+  double *R = (double *)malloc(sizeof(double) * npe * npe * 9);
+  double *Mref = (double *)malloc(sizeof(double) * npe * npe);
+  orc_affine_tables(npe, nip, w, N, dN, R, Mref);
   int T = nthreads > 0 ? nthreads : 1;
 #ifdef _OPENMP
   double t0 = omp_get_wtime();
@@ -546,7 +677,7 @@ double orc_assemble_csc_threaded(int kind, int ptype, int dim, int pdim,
           int64_t node = conn[e * npe + a];
           for (int i = 0; i < 3; ++i) X[3 * a + i] = xyz[3 * node + i];
         }
-        orc_element_matrix(kind, dim, pdim, npe, nip, w, N, dN, X, c1, c2, Ke);
+        orc_element_matrix_ex(kind, dim, pdim, npe, nip, w, N, dN, X, c1, c2, nref, R, Mref, Ke);
         for (int bn = 0; bn < npe; ++bn) {
           int64_t B = conn[e * npe + bn];
           for (int an = 0; an < npe; ++an) {
@@ -574,6 +705,8 @@ double orc_assemble_csc_threaded(int kind, int ptype, int dim, int pdim,
   }
   for (int t = 0; t < T; ++t) free(bufs[t]);
   free(bufs);
+  free(R);
+  free(Mref);
 #ifdef _OPENMP
   return omp_get_wtime() - t0;
 #else

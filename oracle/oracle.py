@@ -49,10 +49,10 @@ def lib():
         L.orc_pattern.argtypes = [i64, i64, i32, Pi32, Pi32, i32]
         L.orc_assemble.restype = vp
         L.orc_assemble.argtypes = [i32, i32, i32, i32, i64, Pd, i64, i32, Pi32, Pi32, i32, Pd, Pd, Pd,
-                                   Pd, i32, dbl, i32, C.POINTER(i32)]
+                                   Pd, i32, dbl, i32, Pd, C.POINTER(i32)]
         L.orc_assemble_csc_threaded.restype = dbl
         L.orc_assemble_csc_threaded.argtypes = [i32, i32, i32, i32, Pd, i64, i32, Pi32, i32, Pd, Pd,
-                                                Pd, Pd, dbl, vp, i32, i32]
+                                                Pd, Pd, dbl, vp, i32, i32, Pd]
         L.orc_free.argtypes = [vp]
         L.orc_n.restype = i64
         L.orc_n.argtypes = [vp]
@@ -151,7 +151,7 @@ def pattern(non, conn, pdim, emat=None):
     return CSC(h)
 
 
-def assemble(kind, ptype, dim, pdim, xyz, conn, rule, params, thickness=1.0, lumped=False, emat=None):
+def assemble(kind, ptype, dim, pdim, xyz, conn, rule, params, thickness=1.0, lumped=False, emat=None, affine=True):
     """Reference-order COO assembly + sparse + dropzeros! (see llfem_oracle.c)."""
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
     conn0 = _conn0(conn)
@@ -162,17 +162,19 @@ def assemble(kind, ptype, dim, pdim, xyz, conn, rule, params, thickness=1.0, lum
     dN = np.ascontiguousarray(rule["dN"], dtype=np.float64)
     err = C.c_int(0)
     nmat = 1
+    nref = None if rule.get("node_ref") is None or not affine else np.ascontiguousarray(rule["node_ref"], dtype=np.float64)
     h = lib().orc_assemble(kind, ptype, dim, pdim, xyz.shape[0], _p(xyz, C.c_double), conn0.shape[0],
                            conn0.shape[1], _p(conn0, C.c_int32), _p(em, C.c_int32), len(w),
                            _p(w, C.c_double), _p(N, C.c_double), _p(dN, C.c_double),
-                           _p(params, C.c_double), nmat, float(thickness), int(lumped), C.byref(err))
+                           _p(params, C.c_double), nmat, float(thickness), int(lumped), _p(nref, C.c_double),
+                           C.byref(err))
     if not h:
         raise ValueError("oracle: non-positive Jacobian determinant")
     return CSC(h)
 
 
 def assemble_threaded(kind, ptype, dim, pdim, xyz, conn, rule, params, pat: CSC, thickness=1.0,
-                      nthreads=None, chunk=256):
+                      nthreads=None, chunk=256, affine=True):
     """Timed CPU baseline: threaded direct-CSC assembly into `pat` (overwritten).
     Returns seconds."""
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
@@ -185,7 +187,9 @@ def assemble_threaded(kind, ptype, dim, pdim, xyz, conn, rule, params, pat: CSC,
     return lib().orc_assemble_csc_threaded(kind, ptype, dim, pdim, _p(xyz, C.c_double), conn0.shape[0],
                                            conn0.shape[1], _p(conn0, C.c_int32), len(w), _p(w, C.c_double),
                                            _p(N, C.c_double), _p(dN, C.c_double), _p(params, C.c_double),
-                                           float(thickness), pat.h, T, chunk)
+                                           float(thickness), pat.h, T, chunk,
+                                           _p(np.ascontiguousarray(rule["node_ref"], dtype=np.float64), C.c_double)
+                                           if affine else None)
 
 
 def element_matrix(kind, dim, pdim, X, rule, c1, c2=0.0):

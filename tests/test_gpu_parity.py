@@ -191,6 +191,36 @@ def test_precision_form_within_fp32_tolerance(llf, case):
         assert np.abs(v32 - v64).max() <= 1e-6 * scale, op
 
 
+DISTORTED_CASES = [("box", 2, 2, False, "Solid"), ("box", 3, 1, False, "Solid"),
+                   ("rect", 3, 3, False, "PlaneStrain"), ("box", 2, 2, True, "Solid")]
+
+
+@pytest.mark.parametrize("case", DISTORTED_CASES, ids=_ids)
+@pytest.mark.parametrize("part", ["all", "half"])
+def test_distorted_mesh_bit_identical(llf, orc, case, part):
+    """Interior nodes moved (everywhere, or only for x > 0.5): distorted
+    elements take the quadrature form, the others the affine form, on both
+    sides."""
+    kind, n, order, simplex, ptype = case
+    m = make_mesh(llf, kind, n, order, simplex)
+    d = m.dim
+    sel = np.all((m.xyz[:, :d] > 1e-9) & (m.xyz[:, :d] < 1 - 1e-9), axis=1)
+    if part == "half":
+        sel &= m.xyz[:, 0] > 0.5 + 1e-9
+    rng = np.random.default_rng(5)
+    m.xyz[sel, :d] += rng.uniform(-0.04, 0.04, (sel.sum(), d)) / n
+    mat = llf.Material("body", E=2.1e5, nu=0.3, rho=7.85e-9, k=45.0)
+    p = llf.Problem([mat], type=ptype)
+    assert_csc_identical(llf.stiffnessMatrix(p).csc(), oracle_operator(llf, orc, m, "stiffness", PT[ptype], mat).julia(),
+                         f"K {_ids(case)} {part}")
+    assert_csc_identical(llf.massMatrix(p, lumped=False).csc(),
+                         oracle_operator(llf, orc, m, "mass", PT[ptype], mat).julia(), f"M {_ids(case)} {part}")
+    hp = "HeatConduction" if d == 3 else "PlaneHeatConduction"
+    ph = llf.Problem([mat], type=hp)
+    assert_csc_identical(llf.heatConductionMatrix(ph).csc(), oracle_operator(llf, orc, m, "heat", PT[hp], mat).julia(),
+                         f"H {_ids(case)} {part}")
+
+
 # ---------------------------------------------------------------- error paths
 def test_inverted_element_is_an_error(llf):
     m = llf.structured_box_mesh(n=2, order=1)
