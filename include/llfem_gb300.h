@@ -332,6 +332,37 @@ int llf_pcg(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x,
             const uint8_t *fixed, int precond, double reltol, int64_t maxiter,
             int64_t *iters, double *relres);
 
+/* Largest system (DoFs) llf_pcg_noalloc accepts. */
+#define LLF_NOALLOC_MAX_DOFS 131072
+
+/* Allocation-free variant of llf_pcg (no counterpart in the reference).
+ *
+ * For callers that cannot allocate device memory once they are running:
+ * code inside a host framework that has already reserved the GPU's memory
+ * for its own pool, real-time or control loops that forbid allocation (and
+ * its latency and fragmentation) after start-up, and solvers embedded in a
+ * process whose device-memory budget is fixed in advance.  Such a caller
+ * passes device pointers it already owns — right-hand side d_b, the initial
+ * and prescribed values d_x (overwritten with the solution) and the mask
+ * d_fixed, each of the matrix's DoF count — and the call allocates nothing:
+ * no cudaMalloc, cudaMallocAsync or cudaFree, no library allocator.  The CG
+ * work vectors live in one fixed array compiled into the library
+ * (about 8.4 MB for LLF_NOALLOC_MAX_DOFS = 131072 unknowns), which every GPU
+ * that loads the library holds until the process exits.
+ *
+ * Same algorithm and results as llf_pcg (IterativeSolvers.cg recurrence and
+ * stopping rule, Dirichlet masking); systems above LLF_NOALLOC_MAX_DOFS are
+ * rejected with LLF_ERR_LIMIT.  The first call on a device looks up the
+ * array's device address for that device (make that first call before any
+ * stream capture).  All calls share the one array and it keeps the previous
+ * call's contents; each call clears on its own stream what has to start at
+ * zero (the count of unconverged systems) and writes every other work
+ * vector before reading it.  Calls whose work overlaps on the GPU (two
+ * contexts or threads at once) race on the array: serialise them. */
+int llf_pcg_noalloc(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
+                    const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
+                    int64_t *iters, double *relres);
+
 /* Batched form of llf_pcg for a block-diagonal matrix of nseg independent
  * systems (for example many meshes assembled together as one mesh with one
  * material per instance): system g owns DoFs [seg_off[g], seg_off[g+1]).

@@ -85,6 +85,7 @@ SIGNATURES = {
     "llf_matrix_destroy": (i32, [vp, vp]),
     "llf_pcg": (i32, [vp, vp, P_dbl, P_dbl, P_u8, i32, dbl, i64, P_i64, P_dbl]),
     "llf_pcg_batched": (i32, [vp, vp, P_dbl, P_dbl, P_u8, i32, P_i64, i32, dbl, i64, P_i64, P_dbl]),
+    "llf_pcg_noalloc": (i32, [vp, vp, vp, vp, vp, i32, dbl, i64, P_i64, P_dbl]),
     "llf_server_create": (i32, [i32, i32, i64, PP]),
     "llf_server_submit_heat": (i32, [vp, i32, i64, P_dbl, i64, i32, P_i64, i32, i32, dbl, dbl, P_dbl, P_dbl, P_u8,
                                      i32, dbl, i64, P_i64]),

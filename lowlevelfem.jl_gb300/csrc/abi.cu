@@ -800,6 +800,22 @@ int llf_pcg(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x, const
   return rc == LLF_OK ? llf_ok(ctx) : rc;
 }
 
+int llf_pcg_noalloc(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
+                    const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
+                    int64_t *iters, double *relres) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!m || !d_b || !d_x || !d_fixed)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_noalloc: null argument");
+  if (precond < LLF_PRECOND_NONE || precond > LLF_PRECOND_BJACOBI)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_noalloc: unknown preconditioner");
+  int64_t it = 0;
+  double rr = 0.0;
+  int rc = pcg_noalloc_impl(ctx, m, d_b, d_x, d_fixed, precond, reltol, maxiter, &it, &rr);
+  if (iters) *iters = it;
+  if (relres) *relres = rr;
+  return rc == LLF_OK ? llf_ok(ctx) : rc;
+}
+
 int llf_pcg_batched(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x, const uint8_t *fixed,
                     int nseg, const int64_t *seg_off, int precond, double reltol, int64_t maxiter,
                     int64_t *iters, double *relres) {

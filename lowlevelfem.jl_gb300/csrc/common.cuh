@@ -198,6 +198,9 @@ int spmv_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_x, double *d_y)
 int pcg_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
              const uint8_t *d_fixed, int precond, double reltol,
              int64_t maxiter, int64_t *iters, double *relres);
+int pcg_noalloc_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
+                     const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
+                     int64_t *iters, double *relres);
 int pcg_batched_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                      const uint8_t *d_fixed, int nseg, const int64_t *seg_off, int precond,
                      double reltol, int64_t maxiter, int64_t *iters, double *relres);

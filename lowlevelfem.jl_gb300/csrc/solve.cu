@@ -31,6 +31,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 namespace {
 
@@ -537,7 +538,118 @@ int pcg_outcome(llf_ctx *ctx, int nseg, const SegState *hst, int64_t *iters, dou
   return LLF_OK;
 }
 
+// ---------------------------------------------------------------- no-alloc PCG
+// Fixed device scratch for llf_pcg_noalloc: every work vector of one CG of
+// at most LLF_NOALLOC_MAX_DOFS unknowns, the chunk descriptors of a single
+// system and its state word.  Each GPU that loads the library holds this
+// array until the process exits.  Regions are 256-byte aligned.
+constexpr int64_t NA_N = LLF_NOALLOC_MAX_DOFS;
+constexpr int64_t NA_CH = (NA_N + CHUNK - 1) / CHUNK;
+constexpr size_t na_round(size_t b) { return (b + 255) / 256 * 256; }
+constexpr size_t NA_VEC = na_round(sizeof(double) * NA_N);
+constexpr size_t NA_OFF_PINV = 5 * NA_VEC;                       // r, z, u, c, xw
+constexpr size_t NA_OFF_PART = NA_OFF_PINV + 3 * NA_VEC;         // pinv (up to 3 per DoF)
+constexpr size_t NA_OFF_CB = NA_OFF_PART + na_round(sizeof(double) * NA_CH);
+constexpr size_t NA_OFF_CE = NA_OFF_CB + na_round(sizeof(int64_t) * NA_CH);
+constexpr size_t NA_OFF_SF = NA_OFF_CE + na_round(sizeof(int64_t) * NA_CH);
+constexpr size_t NA_OFF_CS = NA_OFF_SF + na_round(sizeof(int64_t) * 2);
+constexpr size_t NA_OFF_ST = NA_OFF_CS + na_round(sizeof(int32_t) * NA_CH);
+constexpr size_t NA_OFF_ACT = NA_OFF_ST + na_round(sizeof(SegState));
+constexpr size_t NA_BYTES = NA_OFF_ACT + 256;
+
 }  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+namespace {
+
+// Uniform chunks of one system of n DoFs (chunk count nch <= NA_CH).
+__global__ void k_na_chunks(int64_t *cb, int64_t *ce, int32_t *cs, int64_t *sf, int64_t n, int64_t nch) {
+  for (int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ch < nch;
+       ch += (int64_t)gridDim.x * blockDim.x) {
+    cb[ch] = ch * CHUNK;
+    ce[ch] = (ch + 1) * CHUNK < n ? (ch + 1) * CHUNK : n;
+    cs[ch] = 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sf[0] = 0;
+    sf[1] = nch;
+  }
+}
+
+// Device address of the scratch array, looked up once per device with that
+// device current (host code must not use the symbol itself as an address).
+std::mutex g_na_mutex;
+unsigned char *g_na_ptr[128] = {nullptr};
+
+int noalloc_scratch(llf_ctx *ctx, unsigned char **out) {
+  if (ctx->device < 0 || ctx->device >= 128) return llf_fail(ctx, LLF_ERR_ARG, "device index");
+  std::lock_guard<std::mutex> lock(g_na_mutex);
+  if (!g_na_ptr[ctx->device]) {
+    LLF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return llf_fail(ctx, LLF_ERR_CUDA, std::string("llf_pcg_noalloc: cudaGetSymbolAddress of the scratch array failed: ") +
+                                             cudaGetErrorString(e));
+    g_na_ptr[ctx->device] = (unsigned char *)p;
+  }
+  *out = g_na_ptr[ctx->device];
+  return LLF_OK;
+}
+
+template <int P>
+int pcg_noalloc_typed(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
+                      const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
+                      int64_t *iters, double *relres) {
+  const int64_t n = m->pat->ndof;
+  unsigned char *base = nullptr;
+  int rc = noalloc_scratch(ctx, &base);
+  if (rc != LLF_OK) return rc;
+  double *r = (double *)(base + 0 * NA_VEC), *z = (double *)(base + 1 * NA_VEC);
+  double *u = (double *)(base + 2 * NA_VEC), *c = (double *)(base + 3 * NA_VEC);
+  double *xw = (double *)(base + 4 * NA_VEC), *pinv = (double *)(base + NA_OFF_PINV);
+  double *part = (double *)(base + NA_OFF_PART);
+  int64_t *cb = (int64_t *)(base + NA_OFF_CB), *ce = (int64_t *)(base + NA_OFF_CE);
+  int64_t *sf = (int64_t *)(base + NA_OFF_SF);
+  int32_t *cs = (int32_t *)(base + NA_OFF_CS);
+  SegState *st = (SegState *)(base + NA_OFF_ST);
+  int *active = (int *)(base + NA_OFF_ACT);
+  const int64_t nch = (n + CHUNK - 1) / CHUNK;
+  // the array keeps the previous call's contents: the active-system counter
+  // must start at zero; every other region is written before it is read
+  LLF_CUDA_TRY(ctx, cudaMemsetAsync(active, 0, sizeof(int), ctx->stream));
+  k_na_chunks<<<1, 64, 0, ctx->stream>>>(cb, ce, cs, sf, n, nch);
+  ctx->launches++;
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  Seg S{cb, ce, cs, sf, nch, 1, st, active};
+  SegState hst[1];
+  rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, precond, reltol, maxiter,
+                   false, hst);
+  if (rc != LLF_OK) return rc;
+  return pcg_outcome(ctx, 1, hst, iters, relres);
+}
+
+}  // namespace
+
+int pcg_noalloc_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
+                     const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
+                     int64_t *iters, double *relres) {
+  if (m->diagonal_only)
+    return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "llf_pcg_noalloc: lumped (diagonal) matrix");
+  const int64_t n = m->pat->ndof;
+  if (n > LLF_NOALLOC_MAX_DOFS)
+    return llf_fail(ctx, LLF_ERR_LIMIT, "llf_pcg_noalloc: the system has " + std::to_string(n) +
+                                            " unknowns; the fixed scratch array holds at most " +
+                                            std::to_string((long long)LLF_NOALLOC_MAX_DOFS) +
+                                            " (use llf_pcg for larger systems)");
+  switch (m->pat->pdim) {
+    case 1: return pcg_noalloc_typed<1>(ctx, m, d_b, d_x, d_fixed, precond, reltol, maxiter, iters, relres);
+    case 2: return pcg_noalloc_typed<2>(ctx, m, d_b, d_x, d_fixed, precond, reltol, maxiter, iters, relres);
+    case 3: return pcg_noalloc_typed<3>(ctx, m, d_b, d_x, d_fixed, precond, reltol, maxiter, iters, relres);
+  }
+  return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
+}
 
 int spmv_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_x, double *d_y) {
   const int64_t n = m->pat->ndof;
