@@ -132,15 +132,20 @@ class ClockSampler:
 def algorithmic(mesh, nnz):
     """Algorithmic bytes of one assembly (structural nnz values written, node
     coordinates and connectivity read) and FP64 operations of the element
-    kernel under the arithmetic contract (FMA = 2 flops)."""
-    npe, nip, d = mesh.npe, 27 if ORDER == 2 else (ORDER + 1) ** 3, 3
+    kernel under the arithmetic contract (FMA = 2 flops).  Every element of
+    the structured mesh passes the affinity test, so the count is the affine
+    form's: affinity test, Jacobian inverse and per-element coefficients,
+    then per node pair Ksym = W S (ns x ns FMA), Kanti = U A (na x na FMA,
+    a != b) and the 2 na additions that form the two off-diagonal halves."""
+    npe, d = mesh.npe, 3
+    ns, na = (6, 3) if d == 3 else (3, 1)
     bytes_ = 8 * nnz + 24 * mesh.non + 4 * npe * mesh.nel
     npairs = npe * (npe + 1) // 2
-    geo = nip * (2 * npe * d * d + 60)             # J, cofactors, det, inverse
-    grads = nip * npe * (2 * d * d + d)            # J^-T grad + weighting
-    pairs = nip * ((npairs - npe) * 2 * d * d + npe * 2 * 6)
-    combine = npairs * (3 * d * d + 6)
-    flops = mesh.nel * (geo + grads + pairs + combine)
+    test = 2 * d * d * npe + npe * d * (1 + 3 * d)
+    inverse = 42
+    coeffs = 3 * ns * ns + (2 + 1) * ns * ns + d * ns * 2 + 5 * na * na + ns + 1
+    pairs = (npairs - npe) * (2 * ns * ns + 2 * na * na + 2 * na) + npe * 2 * ns * ns
+    flops = mesh.nel * (test + inverse + coeffs + pairs)
     return bytes_, flops
 
 

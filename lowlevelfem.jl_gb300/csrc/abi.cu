@@ -70,6 +70,8 @@ int upload_tables(llf_ctx *ctx, llf_mesh *m, int nip, const double *w, const dou
   dfree(ctx, m->d_nref);
   dfree(ctx, m->d_Rp);
   dfree(ctx, m->d_Mp);
+  dfree(ctx, m->d_Rpf);
+  dfree(ctx, m->d_Mpf);
   m->nip = nip;
   const size_t nn = (size_t)nip * m->npe;
   m->h_w.assign(w, w + nip);
@@ -104,22 +106,39 @@ int upload_tables(llf_ctx *ctx, llf_mesh *m, int nip, const double *w, const dou
 
 // Affine-element tables of the current rule (contract of the oracle):
 // R_ab[k][l] = fma chain over q of (w_q dN_a,k) dN_b,l and Mref_ab = fma chain
-// of (w_q N_a) N_b, stored for the pairs a <= b in a-major order.
+// of (w_q N_a) N_b.  Stored for the pairs a <= b in a-major order: 9 values
+// per pair, the symmetric components S_kl = (R_kl + R_lk) * 0.5 (k <= l;
+// 3D 00 11 22 01 02 12, 2D 00 11 01) first, the antisymmetric components
+// A_kl = (R_kl - R_lk) * 0.5 (off-diagonal, same order) from index 6.
 int upload_affine(llf_ctx *ctx, llf_mesh *m, const double *node_ref) {
+  static const int sym3[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  static const int sym2[3][2] = {{0, 0}, {1, 1}, {0, 1}};
+  const int dim = m->dim;
+  const int ns = dim == 3 ? 6 : 3, na = dim == 3 ? 3 : 1;
+  const int(*sym)[2] = dim == 3 ? sym3 : sym2;
   const int npe = m->npe, nip = m->nip;
   const size_t npairs = (size_t)npe * (npe + 1) / 2;
-  std::vector<double> Rp(npairs * 9), Mp(npairs);
+  std::vector<double> Rp(npairs * 9, 0.0), Mp(npairs);
   const double *w = m->h_w.data(), *N = m->h_N.data(), *dN = m->h_dN.data();
   size_t pi = 0;
   for (int a = 0; a < npe; ++a)
     for (int b = a; b < npe; ++b, ++pi) {
+      double R[9];
       for (int k = 0; k < 3; ++k)
         for (int l = 0; l < 3; ++l) {
           double acc = 0.0;
           for (int q = 0; q < nip; ++q)
             acc = std::fma(w[q] * dN[((size_t)q * npe + a) * 3 + k], dN[((size_t)q * npe + b) * 3 + l], acc);
-          Rp[pi * 9 + k * 3 + l] = acc;
+          R[k * 3 + l] = acc;
         }
+      for (int n = 0; n < ns; ++n) {
+        const int k = sym[n][0], l = sym[n][1];
+        Rp[pi * 9 + n] = k == l ? R[k * 3 + k] : (R[k * 3 + l] + R[l * 3 + k]) * 0.5;
+      }
+      for (int n = 0; n < na; ++n) {
+        const int k = sym[dim + n][0], l = sym[dim + n][1];
+        Rp[pi * 9 + 6 + n] = (R[k * 3 + l] - R[l * 3 + k]) * 0.5;
+      }
       double acc = 0.0;
       for (int q = 0; q < nip; ++q) acc = std::fma(w[q] * N[(size_t)q * npe + a], N[(size_t)q * npe + b], acc);
       Mp[pi] = acc;
@@ -132,6 +151,13 @@ int upload_affine(llf_ctx *ctx, llf_mesh *m, const double *node_ref) {
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_Rp, Rp.data(), sizeof(double) * npairs * 9, cudaMemcpyHostToDevice,
                                     ctx->stream));
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_Mp, Mp.data(), sizeof(double) * npairs, cudaMemcpyHostToDevice,
+                                    ctx->stream));
+  std::vector<float> Rpf(Rp.begin(), Rp.end()), Mpf(Mp.begin(), Mp.end());
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_Rpf, npairs * 9));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_Mpf, npairs));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_Rpf, Rpf.data(), sizeof(float) * npairs * 9, cudaMemcpyHostToDevice,
+                                    ctx->stream));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_Mpf, Mpf.data(), sizeof(float) * npairs, cudaMemcpyHostToDevice,
                                     ctx->stream));
   LLF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return LLF_OK;
@@ -349,9 +375,11 @@ int llf_mesh_update(llf_ctx *ctx, llf_mesh *m, const double *xyz, const int64_t 
     LLF_CUDA_TRY(ctx, dalloc(ctx, &d_conn64, (size_t)m->npe * m->nel));
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_conn64, conn, sizeof(int64_t) * m->npe * m->nel,
                                       cudaMemcpyHostToDevice, ctx->stream));
-    int rc = mesh_convert_conn(ctx, m, d_conn64);
+    bool changed = false;
+    int rc = mesh_update_conn(ctx, m, d_conn64, &changed);
     dfree(ctx, d_conn64);
     if (rc != LLF_OK) return rc;
+    if (changed) m->conn_version++;  // patterns built before no longer match
   }
   int rc = check_finite(ctx, m->d_xyz, 3 * m->non);
   if (rc != LLF_OK) return rc;
@@ -384,6 +412,7 @@ int llf_mesh_destroy(llf_ctx *ctx, llf_mesh *m) {
     dfree(ctx, m->d_xyz); dfree(ctx, m->d_conn); dfree(ctx, m->d_emat);
     dfree(ctx, m->d_w); dfree(ctx, m->d_N); dfree(ctx, m->d_dN); dfree(ctx, m->d_dNn);
     dfree(ctx, m->d_nref); dfree(ctx, m->d_Rp); dfree(ctx, m->d_Mp);
+    dfree(ctx, m->d_Rpf); dfree(ctx, m->d_Mpf);
     dfree(ctx, m->d_wf); dfree(ctx, m->d_Nf); dfree(ctx, m->d_dNf);
     cudaStreamSynchronize(ctx->stream);
   }
@@ -468,6 +497,7 @@ int llf_pattern_destroy(llf_ctx *ctx, llf_pattern *p) {
   if (ctx) {
     dfree(ctx, p->d_n2e_ptr); dfree(ctx, p->d_n2e); dfree(ctx, p->d_nptr);
     dfree(ctx, p->d_nadj); dfree(ctx, p->d_diagpos); dfree(ctx, p->d_colptr);
+    dfree(ctx, p->d_pos);
     cudaStreamSynchronize(ctx->stream);
   }
   delete p;

@@ -25,6 +25,7 @@
 // intrinsic (__dmul_rn, __dadd_rn, __fma_rn, __drcp_rn), so no contraction
 // or reassociation can move the result away from the CPU oracle's.
 #include "common.cuh"
+#include "affine.cuh"
 
 #include <algorithm>
 
@@ -40,14 +41,16 @@ struct ElemArgs {
   int npe, nip, npairs;
   const double *w, *N, *dN;  // device tables
   const double *c1, *c2;     // per-material coefficients
-  double *Kf;                // nel * npe * npe * BS (full element matrices)
+  double *Kf;                // nel * npe * colstride (full element matrices)
+  int64_t colstride;         // doubles per element-matrix column (16-byte multiple)
   double *scratch;           // per-CTA global scratch for G, S (large elements)
   int64_t scratch_stride;    // doubles per CTA
   unsigned *status;
-  // affine-element form (all three set, or all null): reference node
-  // coordinates [npe*3] and, per upper-triangle node pair in pair order,
-  // R_ab [9] and Mref_ab [1]
-  const double *nref, *Rp, *Mp;
+  // affine-element form: per-element flag and invJ/det (k_affine_geometry;
+  // aflag null = none), and per upper-triangle node pair in pair order the
+  // symmetric [0,NS) and antisymmetric [6,6+NA) parts of R_ab, and Mref_ab
+  const uint8_t *aflag;
+  const double *ageo, *Rp, *Mp;
 };
 
 __device__ __forceinline__ int pair_offset(int a, int npe) {
@@ -61,41 +64,6 @@ __device__ __forceinline__ void pair_decode(int pi, int npe, int &a, int &b) {
   }
   a = lo;
   b = a + (pi - pair_offset(a, npe));
-}
-
-// Determinant and row-major inverse of the Jacobian J (contract of the
-// oracle's geometry: cofactors, det by the first row, inverse = cofactor^T
-// times the rounded reciprocal of det).
-template <int DIM>
-__device__ __forceinline__ double jac_inverse(const double (&J)[3][3], double *inv) {
-  double det, rdet;
-  if (DIM == 3) {
-    double c00 = __dsub_rn(__dmul_rn(J[1][1], J[2][2]), __dmul_rn(J[1][2], J[2][1]));
-    double c01 = -__dsub_rn(__dmul_rn(J[1][0], J[2][2]), __dmul_rn(J[1][2], J[2][0]));
-    double c02 = __dsub_rn(__dmul_rn(J[1][0], J[2][1]), __dmul_rn(J[1][1], J[2][0]));
-    double c10 = -__dsub_rn(__dmul_rn(J[0][1], J[2][2]), __dmul_rn(J[0][2], J[2][1]));
-    double c11 = __dsub_rn(__dmul_rn(J[0][0], J[2][2]), __dmul_rn(J[0][2], J[2][0]));
-    double c12 = -__dsub_rn(__dmul_rn(J[0][0], J[2][1]), __dmul_rn(J[0][1], J[2][0]));
-    double c20 = __dsub_rn(__dmul_rn(J[0][1], J[1][2]), __dmul_rn(J[0][2], J[1][1]));
-    double c21 = -__dsub_rn(__dmul_rn(J[0][0], J[1][2]), __dmul_rn(J[0][2], J[1][0]));
-    double c22 = __dsub_rn(__dmul_rn(J[0][0], J[1][1]), __dmul_rn(J[0][1], J[1][0]));
-    det = __dadd_rn(__dadd_rn(__dmul_rn(J[0][0], c00), __dmul_rn(J[0][1], c01)),
-                    __dmul_rn(J[0][2], c02));
-    rdet = __drcp_rn(det);
-    inv[0] = __dmul_rn(c00, rdet); inv[1] = __dmul_rn(c10, rdet); inv[2] = __dmul_rn(c20, rdet);
-    inv[3] = __dmul_rn(c01, rdet); inv[4] = __dmul_rn(c11, rdet); inv[5] = __dmul_rn(c21, rdet);
-    inv[6] = __dmul_rn(c02, rdet); inv[7] = __dmul_rn(c12, rdet); inv[8] = __dmul_rn(c22, rdet);
-  } else {
-    det = __dsub_rn(__dmul_rn(J[0][0], J[1][1]), __dmul_rn(J[0][1], J[1][0]));
-    rdet = __drcp_rn(det);
-    inv[0] = __dmul_rn(J[1][1], rdet);
-    inv[1] = __dmul_rn(-J[0][1], rdet);
-    inv[2] = 0.0;
-    inv[3] = __dmul_rn(-J[1][0], rdet);
-    inv[4] = __dmul_rn(J[0][0], rdet);
-    inv[5] = 0.0; inv[6] = 0.0; inv[7] = 0.0; inv[8] = 0.0;
-  }
-  return det;
 }
 
 // Geometry at one point (contract of the oracle): returns det, fills inv
@@ -117,12 +85,12 @@ __device__ __forceinline__ double geom_point(const double *sX, Tab dNq, int npe,
 // Store block (a,b) (a <= b) of the element matrix and its mirror (b,a) in
 // the column-major-by-node layout Kf[e][col node][row node][i*P+j].
 template <int P, int BS>
-__device__ __forceinline__ void store_pair(double *Ke, int npe, int a, int b, const double *blk) {
-  double *ab = Ke + ((size_t)b * npe + a) * BS;  // rows of node a, columns of node b
+__device__ __forceinline__ void store_pair(double *Ke, int64_t cs, int a, int b, const double *blk) {
+  double *ab = Ke + (size_t)b * cs + (size_t)a * BS;  // rows of node a, columns of node b
 #pragma unroll
   for (int k = 0; k < BS; ++k) ab[k] = blk[k];
   if (a != b) {
-    double *ba = Ke + ((size_t)a * npe + b) * BS;
+    double *ba = Ke + (size_t)a * cs + (size_t)b * BS;
     if (BS == 1) {
       ba[0] = blk[0];
     } else {
@@ -134,124 +102,84 @@ __device__ __forceinline__ void store_pair(double *Ke, int npe, int a, int b, co
   }
 }
 
-constexpr int AFF_DOUBLES = 32;
-
-// Affinity test of the element in sX (contract of the oracle): warp 0 forms
-// J0 (geometry contract at point 0) and s = max |X|; every node then has to
-// satisfy |X_a - X_0 - J0 (xi_a - xi_0)| <= 2^-46 s componentwise.  Returns a
-// CTA-uniform flag; sAff[0..9] hold J0 and s afterwards.
-template <int DIM>
-__device__ __forceinline__ bool elem_is_affine(const double *sX, const double *dN0, int tstride,
-                                               int npe, const double *nref, double *sAff) {
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
-    double m = 0.0;
-    for (int t = lane; t < npe * DIM; t += 32) m = fmax(m, fabs(sX[t]));
-#pragma unroll
-    for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (lane < DIM * DIM) {
-      const int i = lane / DIM, j = lane % DIM;
-      double acc = 0.0;
-      for (int a = 0; a < npe; ++a) acc = __fma_rn(sX[a * DIM + i], dN0[a * tstride + j], acc);
-      sAff[i * 3 + j] = acc;
-    }
-    if (lane == 0) sAff[9] = m;
-  }
-  __syncthreads();
-  const double sc = sAff[9];
-  const double tol = __dmul_rn(1.4210854715202004e-14, sc);  // 64 * 2^-52
-  int bad = 0;
-  for (int t = threadIdx.x; t < npe * DIM; t += blockDim.x) {
-    const int a = t / DIM, i = t - a * DIM;
-    double r = __dsub_rn(sX[t], sX[i]);
-#pragma unroll
-    for (int j = 0; j < DIM; ++j)
-      r = __fma_rn(-sAff[i * 3 + j], __dsub_rn(nref[a * 3 + j], nref[j]), r);
-    if (!(fabs(r) <= tol)) bad = 1;
-  }
-  return !__syncthreads_or(bad) && sc > 0.0;
-}
-
-// Node-pair blocks of an affine element (contract of the oracle): with
-// Y = det*invJ, T = R_ab Y and O_ab = invJ^T T; heat c1*trace(O_ab), mass
-// c1*(det*Mref_ab), elasticity from O_ab as in the quadrature form.
+// Node-pair blocks of an affine element (contract of the oracle): per pair
+// the symmetric part S (NS values) and antisymmetric part A (NA values) of
+// R_ab; elasticity Ksym = W S, Kanti = U A (a != b), heat (c1 trV) . S, mass
+// (c1 det) Mref_ab.
 template <int KIND, int DIM, int P, int BS>
-__device__ __forceinline__ void affine_pairs(const ElemArgs &A, const double *sAff, double c1,
-                                             double c2, double *Ke) {
+__device__ __forceinline__ void affine_pairs(const ElemArgs &A, const double *sAff, double *Ke) {
+  constexpr int NS = DIM == 3 ? 6 : 3, NA = DIM == 3 ? 3 : 1;
   const int npe = A.npe;
-  double inv[9], Y[9];
+  if (KIND == KIND_MASS) {
+    const double cm = sAff[AF_M];
+    for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
+      int a, b;
+      pair_decode(pi, npe, a, b);
+      double blk[BS];
+      blk[0] = __dmul_rn(cm, __ldg(A.Mp + pi));
+      store_pair<P, BS>(Ke, A.colstride, a, b, blk);
+    }
+  } else if (KIND == KIND_HEAT) {
+    double Q[NS];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) {
-    inv[k] = sAff[10 + k];
-    Y[k] = sAff[19 + k];
-  }
-  const double det = sAff[28];
-  for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
-    int a, b;
-    pair_decode(pi, npe, a, b);
-    double blk[BS];
-    if (KIND == KIND_MASS) {
-      blk[0] = __dmul_rn(c1, __dmul_rn(det, __ldg(A.Mp + pi)));
-    } else {
-      const double *R = A.Rp + (size_t)pi * 9;
-      double T[DIM][DIM];
+    for (int n = 0; n < NS; ++n) Q[n] = sAff[AF_Q + n];
+    for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
+      int a, b;
+      pair_decode(pi, npe, a, b);
+      const double *sp = A.Rp + (size_t)pi * 9;
+      double acc = 0.0;
 #pragma unroll
-      for (int k = 0; k < DIM; ++k) {
-        double r[DIM];
+      for (int n = 0; n < NS; ++n) acc = __fma_rn(Q[n], __ldg(sp + n), acc);
+      double blk[BS];
+      blk[0] = acc;
+      store_pair<P, BS>(Ke, A.colstride, a, b, blk);
+    }
+  } else {
+    double W[NS * NS], U[NA * NA];
 #pragma unroll
-        for (int l = 0; l < DIM; ++l) r[l] = __ldg(R + k * 3 + l);
+    for (int t = 0; t < NS * NS; ++t) W[t] = sAff[AF_W + t];
 #pragma unroll
-        for (int j = 0; j < DIM; ++j) {
-          double acc = 0.0;
+    for (int t = 0; t < NA * NA; ++t) U[t] = sAff[AF_U + t];
+    for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
+      int a, b;
+      pair_decode(pi, npe, a, b);
+      const double *sp = A.Rp + (size_t)pi * 9;
+      double sv[NS], av[NA];
 #pragma unroll
-          for (int l = 0; l < DIM; ++l) acc = __fma_rn(r[l], Y[l * 3 + j], acc);
-          T[k][j] = acc;
-        }
-      }
-      if (KIND == KIND_HEAT) {
+      for (int n = 0; n < NS; ++n) sv[n] = __ldg(sp + n);
+#pragma unroll
+      for (int n = 0; n < NA; ++n) av[n] = __ldg(sp + 6 + n);
+      double ks[NS];
+#pragma unroll
+      for (int m = 0; m < NS; ++m) {
         double acc = 0.0;
 #pragma unroll
-        for (int i = 0; i < DIM; ++i)
-#pragma unroll
-          for (int k = 0; k < DIM; ++k) acc = __fma_rn(inv[k * 3 + i], T[k][i], acc);
-        blk[0] = __dmul_rn(c1, acc);
-      } else {
-        double O[DIM][DIM];
-        if (a != b) {
-#pragma unroll
-          for (int i = 0; i < DIM; ++i)
-#pragma unroll
-            for (int j = 0; j < DIM; ++j) {
-              double acc = 0.0;
-#pragma unroll
-              for (int k = 0; k < DIM; ++k) acc = __fma_rn(inv[k * 3 + i], T[k][j], acc);
-              O[i][j] = acc;
-            }
-        } else {
-#pragma unroll
-          for (int i = 0; i < DIM; ++i)
-#pragma unroll
-            for (int j = i; j < DIM; ++j) {
-              double acc = 0.0;
-#pragma unroll
-              for (int k = 0; k < DIM; ++k) acc = __fma_rn(inv[k * 3 + i], T[k][j], acc);
-              O[i][j] = acc;
-              O[j][i] = acc;
-            }
-        }
-        double tr = __dadd_rn(O[0][0], O[1 % DIM][1 % DIM]);
-        if (DIM == 3) tr = __dadd_rn(tr, O[2 % DIM][2 % DIM]);
-#pragma unroll
-        for (int i = 0; i < DIM; ++i)
-#pragma unroll
-          for (int j = 0; j < DIM; ++j) {
-            double t = __fma_rn(c2, O[j][i], __dmul_rn(c1, O[i][j]));
-            if (i == j) t = __fma_rn(c2, tr, t);
-            blk[i * DIM + j] = t;
-          }
+        for (int n = 0; n < NS; ++n) acc = __fma_rn(W[m * NS + n], sv[n], acc);
+        ks[m] = acc;
       }
+      double blk[BS];
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) blk[i * DIM + i] = ks[i];
+      if (a != b) {
+#pragma unroll
+        for (int m = 0; m < NA; ++m) {
+          double acc = 0.0;
+#pragma unroll
+          for (int n = 0; n < NA; ++n) acc = __fma_rn(U[m * NA + n], av[n], acc);
+          const int i = sym_k<DIM>(DIM + m), j = sym_l<DIM>(DIM + m);
+          blk[i * DIM + j] = __dadd_rn(ks[DIM + m], acc);
+          blk[j * DIM + i] = __dsub_rn(ks[DIM + m], acc);
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < NA; ++m) {
+          const int i = sym_k<DIM>(DIM + m), j = sym_l<DIM>(DIM + m);
+          blk[i * DIM + j] = ks[DIM + m];
+          blk[j * DIM + i] = ks[DIM + m];
+        }
+      }
+      store_pair<P, BS>(Ke, A.colstride, a, b, blk);
     }
-    store_pair<P, BS>(Ke, npe, a, b, blk);
   }
 }
 
@@ -272,7 +200,7 @@ k_elem_fp64(ElemArgs A) {
   double *sX = sN + ((SMEM && KIND == KIND_MASS) ? (size_t)nip * npe : 0);
   double *sWd = sX + (size_t)npe * DIM;
   double *sInv = sWd + nip;
-  double *sAff = sInv + (size_t)nip * 9;  // [0,9) J0, [9] s, [10,19) invJ, [19,28) det*invJ, [28] det
+  double *sAff = sInv + (size_t)nip * 9;  // affine-form scratch (AF_* offsets)
   double *G = SMEM ? (sAff + AFF_DOUBLES) : (A.scratch + (size_t)blockIdx.x * A.scratch_stride);
   double *S = G + (size_t)nip * npe * gsw;
   // table accessors
@@ -299,31 +227,17 @@ k_elem_fp64(ElemArgs A) {
     if (mat < 0) continue;  // uniform across the CTA
     const double c1 = A.c1[mat];
     const double c2 = (KIND == KIND_ELASTIC) ? A.c2[mat] : 0.0;
-    for (int t = threadIdx.x; t < npe * DIM; t += blockDim.x) {
-      int a = t / DIM, i = t % DIM;
-      sX[t] = A.xyz[(size_t)A.conn[e * npe + a] * 3 + i];
-    }
-    __syncthreads();
-    double *Ke = A.Kf + (size_t)e * npe * npe * BS;
-    if (A.Rp && elem_is_affine<DIM>(sX, tdN, tstride, npe, A.nref, sAff)) {
-      if (threadIdx.x == 0) {
-        double J[3][3], inv[9];
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-          for (int j = 0; j < 3; ++j) J[i][j] = (i < DIM && j < DIM) ? sAff[i * 3 + j] : 0.0;
-        const double det = jac_inverse<DIM>(J, inv);
-        if (!(det > 0.0)) atomicOr(A.status, ST_BAD_JACOBIAN);
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-          sAff[10 + k] = inv[k];
-          sAff[19 + k] = __dmul_rn(det, inv[k]);
-        }
-        sAff[28] = det;
+    double *Ke = A.Kf + (size_t)e * npe * A.colstride;
+    if (A.aflag && A.aflag[e]) {  // uniform across the CTA
+      if (threadIdx.x < 32) affine_stage<DIM>(A.ageo + (size_t)e * 10, c1, c2, sAff, A.status);
+      __syncthreads();
+      affine_pairs<KIND, DIM, P, BS>(A, sAff, Ke);
+    } else {
+      for (int t = threadIdx.x; t < npe * DIM; t += blockDim.x) {
+        int a = t / DIM, i = t % DIM;
+        sX[t] = A.xyz[(size_t)A.conn[e * npe + a] * 3 + i];
       }
       __syncthreads();
-      affine_pairs<KIND, DIM, P, BS>(A, sAff, c1, c2, Ke);
-    } else {
       for (int q = threadIdx.x; q < nip; q += blockDim.x) {
         double inv[9];
         const double *dq = tdN + (size_t)q * npe * tstride;
@@ -418,7 +332,7 @@ k_elem_fp64(ElemArgs A) {
             acc = __fma_rn(S[(size_t)q * npe + a], tN[(size_t)q * npe + b], acc);
           blk[0] = __dmul_rn(c1, acc);
         }
-        store_pair<P, BS>(Ke, npe, a, b, blk);
+        store_pair<P, BS>(Ke, A.colstride, a, b, blk);
       }
 
     }
@@ -429,15 +343,36 @@ k_elem_fp64(ElemArgs A) {
 // Column-node gather.  T = double (FP64 form) or float (precision form);
 // FP64 sums in element order in both.  Per warp: the column's row-node list
 // (deg ints) and its accumulator (deg * P * P doubles) in shared memory.
-template <int P, bool BLOCKVAL, class T>
-__device__ __forceinline__ void add_block(double *acc, int t, const T *v, bool first) {
+// Exact FP32 -> FP64 widening on the integer pipe (sign, exponent rebias,
+// mantissa shift; subnormals normalised by their leading-zero count; Inf and
+// NaN keep their payload): the precision form's gather widens every element
+// value, and GB300's FP64 pipe is kept for the additions.
+__device__ __forceinline__ double widen(double x) { return x; }
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  unsigned long long bits;
+  if (e != 0u) {
+    const unsigned long long ed = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
+    bits = (ed << 52) | ((unsigned long long)m << 29);
+  } else if (m != 0u) {
+    const int p = 31 - __clz((int)m);
+    bits = ((unsigned long long)(p + 874) << 52) | (((unsigned long long)m << (52 - p)) & 0xfffffffffffffull);
+  } else {
+    bits = 0ull;
+  }
+  return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) | bits));
+}
+
+template <int P, bool BLOCKVAL, bool FIRST, class T>
+__device__ __forceinline__ void add_block(double *acc, int t, const T *v) {
   double *dst = acc + (size_t)t * P * P;  // [t][j][i]
 #pragma unroll
   for (int i = 0; i < P; ++i)
 #pragma unroll
     for (int j = 0; j < P; ++j) {
-      double x = BLOCKVAL ? (double)v[i * P + j] : (i == j ? (double)v[0] : 0.0);
-      dst[j * P + i] = first ? x : __dadd_rn(dst[j * P + i], x);
+      double x = BLOCKVAL ? widen(v[i * P + j]) : (i == j ? widen(v[0]) : 0.0);
+      dst[j * P + i] = FIRST ? x : __dadd_rn(dst[j * P + i], x);
     }
 }
 
@@ -446,87 +381,76 @@ __device__ __forceinline__ int nonzero_bits(double v) {
   return ((unsigned long long)__double_as_longlong(v) << 1) != 0ull;
 }
 
-// Per warp in shared memory: the column's row nodes (max_deg ints), its
-// accumulator (max_deg*P*P doubles), the elements of the column node
-// (max_n2e int2) and the row position of every (element, node) pair
-// (max_n2e*npe int32).  Positions are found for all elements at once
-// (independent binary searches), then the elements are accumulated in
-// ascending order with the next element's blocks prefetched into registers.
-// The accumulator starts at -0.0 (the identity of IEEE addition) and the
-// first element's blocks are stored rather than added: every entry equals
-// the reference's combination of its triplets (first value, then + each
-// later one), signed zeros included, with one FP64 addition fewer.
+// Column-node gather.  One warp per column node B: its accumulator
+// (deg*P*P doubles) lives in shared memory, starting at -0.0 (the identity
+// of IEEE addition).  The elements of B are walked in ascending order; lane
+// a reads block (a, b) of the element's column b = local(B) (one contiguous
+// run of npe blocks, 16-byte padded) and the block's row position from the
+// pattern's element-to-column map, both prefetched one element ahead, and
+// adds the block into the accumulator.  The first element's blocks are
+// stored rather than added: every entry equals the reference's combination
+// of its triplets (first value, then + each later one), signed zeros
+// included, with one FP64 addition fewer.  The column is written out
+// coalesced with its non-zero count: column (B,j) holds the entries (row
+// node t, component i) at P*t + i.
 template <int P, bool BLOCKVAL, class T>
-__global__ void k_colgather(const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
-                            const int64_t *__restrict__ n2e_ptr, const int2 *__restrict__ n2e,
-                            const int32_t *__restrict__ conn, const T *__restrict__ Kf, int npe,
-                            int64_t non, int max_deg, int max_n2e, double *__restrict__ nz,
-                            int64_t *__restrict__ cnt, unsigned *status) {
+__global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__restrict__ n2e_ptr,
+                            const int2 *__restrict__ n2e, const uint16_t *__restrict__ pos,
+                            const T *__restrict__ Kf, int64_t cs, int npe, int64_t non, int max_deg,
+                            double *__restrict__ nz, int64_t *__restrict__ cnt) {
   extern __shared__ double cg_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   constexpr int BS = BLOCKVAL ? P * P : 1;
   double *acc = cg_smem + (size_t)wib * max_deg * P * P;
-  int2 *els = (int2 *)(cg_smem + (size_t)wpb * max_deg * P * P) + (size_t)wib * max_n2e;
-  int32_t *rows = (int32_t *)((int2 *)(cg_smem + (size_t)wpb * max_deg * P * P) + (size_t)wpb * max_n2e) +
-                  (size_t)wib * (max_deg + (size_t)max_n2e * npe);
-  int32_t *tpos = rows + max_deg;
   for (int64_t B = (int64_t)blockIdx.x * wpb + wib; B < non; B += (int64_t)gridDim.x * wpb) {
     const int64_t c0 = nptr[B];
     const int deg = (int)(nptr[B + 1] - c0);
     const int64_t s = n2e_ptr[B];
     const int nb = (int)(n2e_ptr[B + 1] - s);
-    for (int t = lane; t < deg; t += 32) rows[t] = nadj[c0 + t];
     for (int t = lane; t < deg * P * P; t += 32) acc[t] = -0.0;
-    for (int k = lane; k < nb; k += 32) els[k] = n2e[s + k];
-    __syncwarp();
-    for (int it = lane; it < nb * npe; it += 32) {
-      const int k = it / npe, a = it - k * npe;
-      const int A = conn[(size_t)els[k].x * npe + a];
-      int lo = 0, hi = deg - 1;
-      while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (rows[mid] < A) lo = mid + 1; else hi = mid;
-      }
-      if (deg == 0 || rows[lo] != A) {
-        atomicOr(status, ST_PATTERN);
-        lo = -1;
-      }
-      tpos[it] = lo;
-    }
     __syncwarp();
     if (npe <= 32) {
       const bool act = lane < npe;
       T cur[BS], nxt[BS];
+      unsigned tc = 0xffffu, tn = 0xffffu;
       if (nb > 0 && act) {
-        const T *v = Kf + (((size_t)els[0].x * npe + els[0].y) * npe + lane) * BS;
+        const int2 el = n2e[s];
+        const T *v = Kf + ((size_t)el.x * npe + el.y) * cs + (size_t)lane * BS;
 #pragma unroll
         for (int m = 0; m < BS; ++m) cur[m] = v[m];
+        tc = pos[s * npe + lane];
       }
       for (int k = 0; k < nb; ++k) {  // elements of B, ascending
         if (k + 1 < nb && act) {
-          const T *v = Kf + (((size_t)els[k + 1].x * npe + els[k + 1].y) * npe + lane) * BS;
+          const int2 el = n2e[s + k + 1];
+          const T *v = Kf + ((size_t)el.x * npe + el.y) * cs + (size_t)lane * BS;
 #pragma unroll
           for (int m = 0; m < BS; ++m) nxt[m] = v[m];
+          tn = pos[(s + k + 1) * npe + lane];
         }
-        if (act) {
-          const int t = tpos[k * npe + lane];
-          if (t >= 0) add_block<P, BLOCKVAL, T>(acc, t, cur, k == 0);
+        if (act && tc != 0xffffu) {
+          if (k == 0) add_block<P, BLOCKVAL, true>(acc, (int)tc, cur);  // k is warp-uniform
+          else add_block<P, BLOCKVAL, false>(acc, (int)tc, cur);
         }
         __syncwarp();
 #pragma unroll
         for (int m = 0; m < BS; ++m) cur[m] = nxt[m];
+        tc = tn;
       }
     } else {
       for (int k = 0; k < nb; ++k) {
-        const T *col = Kf + ((size_t)els[k].x * npe + els[k].y) * npe * BS;
+        const int2 el = n2e[s + k];
+        const T *col = Kf + ((size_t)el.x * npe + el.y) * cs;
         for (int a = lane; a < npe; a += 32) {
-          const int t = tpos[k * npe + a];
-          if (t >= 0) add_block<P, BLOCKVAL, T>(acc, t, col + (size_t)a * BS, k == 0);
+          const unsigned t = pos[(s + k) * npe + a];
+          if (t != 0xffffu) {
+            if (k == 0) add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BS);
+            else add_block<P, BLOCKVAL, false>(acc, (int)t, col + (size_t)a * BS);
+          }
         }
         __syncwarp();
       }
     }
-    // write column (B,j): entries (row node t, component i) at P*t + i
 #pragma unroll
     for (int j = 0; j < P; ++j) {
       double *out = nz + (size_t)P * P * c0 + (size_t)j * P * deg;
@@ -706,12 +630,12 @@ int run_elem(llf_ctx *ctx, ElemArgs a) {
 }
 
 template <int P, bool BV, class T>
-int run_colgather(llf_ctx *ctx, llf_pattern *pat, const T *Kf, double *nz, int64_t *cnt) {
+int run_colgather(llf_ctx *ctx, llf_pattern *pat, const T *Kf, int64_t cs, double *nz, int64_t *cnt) {
+  if (pat->conn_version != pat->mesh->conn_version)
+    return llf_fail(ctx, LLF_ERR_STATE, "the mesh connectivity changed after the pattern was built; rebuild it");
   const int md = pat->max_deg > 0 ? pat->max_deg : 1;
-  const int mn = pat->max_n2e > 0 ? pat->max_n2e : 1;
   const int npe = pat->mesh->npe;
-  const size_t per_warp = (size_t)md * P * P * sizeof(double) + (size_t)mn * sizeof(int2) +
-                          (md + (size_t)mn * npe) * sizeof(int32_t);
+  const size_t per_warp = (size_t)md * P * P * sizeof(double);
   int wpb = (int)std::min<size_t>(4, (200 * 1024) / per_warp);
   if (wpb < 1) wpb = 1;
   size_t smem = (size_t)wpb * per_warp;
@@ -726,9 +650,8 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const T *Kf, double *nz, int64
   int64_t need = (pat->mesh->non + wpb - 1) / wpb;
   if (grid > need) grid = need > 0 ? need : 1;
   KernelScope ks(ctx, "k_colgather");
-  fn<<<(unsigned)grid, wpb * 32, smem, ctx->stream>>>(pat->d_nptr, pat->d_nadj, pat->d_n2e_ptr,
-                                                      pat->d_n2e, pat->mesh->d_conn, Kf, npe,
-                                                      pat->mesh->non, md, mn, nz, cnt, ctx->d_status);
+  fn<<<(unsigned)grid, wpb * 32, smem, ctx->stream>>>(pat->d_nptr, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, Kf,
+                                                      cs, npe, pat->mesh->non, md, nz, cnt);
   LLF_CUDA_TRY(ctx, cudaGetLastError());
   return LLF_OK;
 }
@@ -737,26 +660,26 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const T *Kf, double *nz, int64
 
 // ------------------------------------------------------------------ host
 template <class T>
-int gather_full_t(llf_ctx *ctx, llf_pattern *pat, const T *Kf, bool blockval, double *nz,
+int gather_full_t(llf_ctx *ctx, llf_pattern *pat, const T *Kf, int64_t cs, bool blockval, double *nz,
                   int64_t *cnt) {
   switch (pat->pdim * 2 + (blockval ? 1 : 0)) {
-    case 2: return run_colgather<1, false, T>(ctx, pat, Kf, nz, cnt);
-    case 3: return run_colgather<1, true, T>(ctx, pat, Kf, nz, cnt);
-    case 4: return run_colgather<2, false, T>(ctx, pat, Kf, nz, cnt);
-    case 5: return run_colgather<2, true, T>(ctx, pat, Kf, nz, cnt);
-    case 6: return run_colgather<3, false, T>(ctx, pat, Kf, nz, cnt);
-    case 7: return run_colgather<3, true, T>(ctx, pat, Kf, nz, cnt);
+    case 2: return run_colgather<1, false, T>(ctx, pat, Kf, cs, nz, cnt);
+    case 3: return run_colgather<1, true, T>(ctx, pat, Kf, cs, nz, cnt);
+    case 4: return run_colgather<2, false, T>(ctx, pat, Kf, cs, nz, cnt);
+    case 5: return run_colgather<2, true, T>(ctx, pat, Kf, cs, nz, cnt);
+    case 6: return run_colgather<3, false, T>(ctx, pat, Kf, cs, nz, cnt);
+    case 7: return run_colgather<3, true, T>(ctx, pat, Kf, cs, nz, cnt);
   }
   return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
 }
 
-int gather_full(llf_ctx *ctx, llf_pattern *pat, const double *Kf, bool blockval, double *nz,
-                int64_t *cnt) {
-  return gather_full_t<double>(ctx, pat, Kf, blockval, nz, cnt);
+int gather_full(llf_ctx *ctx, llf_pattern *pat, const double *Kf, int64_t colstride, bool blockval,
+                double *nz, int64_t *cnt) {
+  return gather_full_t<double>(ctx, pat, Kf, colstride, blockval, nz, cnt);
 }
-int gather_full32(llf_ctx *ctx, llf_pattern *pat, const float *Kf, bool blockval, double *nz,
-                  int64_t *cnt) {
-  return gather_full_t<float>(ctx, pat, Kf, blockval, nz, cnt);
+int gather_full32(llf_ctx *ctx, llf_pattern *pat, const float *Kf, int64_t colstride, bool blockval,
+                  double *nz, int64_t *cnt) {
+  return gather_full_t<float>(ctx, pat, Kf, colstride, blockval, nz, cnt);
 }
 
 int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts) {
@@ -836,12 +759,29 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_c2, c2 ? c2 : c1, sizeof(double) * nmat,
                                     cudaMemcpyHostToDevice, s));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nz, pat->nnz));
+  // affine geometry of every element (built-in tables only)
+  uint8_t *aflag = nullptr;
+  double *ageo = nullptr;
+  if (mesh->d_Rp) {
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &aflag, mesh->nel));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &ageo, (size_t)mesh->nel * 10));
+    KernelScope ks(ctx, "k_affine_geometry");
+    const unsigned g = grid_1d(mesh->nel, 128, ctx->num_sms);
+    if (dim == 3)
+      k_affine_geometry<3><<<g, 128, 0, s>>>(mesh->d_xyz, mesh->d_conn, mesh->d_emat, mesh->nel, npe,
+                                             mesh->d_dN, mesh->d_nref, ageo, aflag);
+    else
+      k_affine_geometry<2><<<g, 128, 0, s>>>(mesh->d_xyz, mesh->d_conn, mesh->d_emat, mesh->nel, npe,
+                                             mesh->d_dN, mesh->d_nref, ageo, aflag);
+    LLF_CUDA_TRY(ctx, cudaGetLastError());
+  }
   int rc = LLF_OK;
   if (form == LLF_FP32Q) {
-    rc = assemble_fp32_impl(ctx, mesh, pat, kind, d_c1, d_c2, m->d_nz, cnt);
+    rc = assemble_fp32_impl(ctx, mesh, pat, kind, d_c1, d_c2, aflag, ageo, m->d_nz, cnt);
   } else {
     double *Kf = nullptr;
-    LLF_CUDA_TRY(ctx, dalloc(ctx, &Kf, (size_t)mesh->nel * npe * npe * BS));
+    const int64_t cs = kf_colstride(npe, BS, (int)sizeof(double));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &Kf, (size_t)mesh->nel * npe * cs));
     ElemArgs a{};
     a.xyz = mesh->d_xyz;
     a.conn = mesh->d_conn;
@@ -856,8 +796,10 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
     a.c1 = d_c1;
     a.c2 = d_c2;
     a.Kf = Kf;
+    a.colstride = cs;
     a.status = ctx->d_status;
-    a.nref = mesh->d_nref;
+    a.aflag = aflag;
+    a.ageo = ageo;
     a.Rp = mesh->d_Rp;
     a.Mp = mesh->d_Mp;
     if (dim == 3) {
@@ -869,11 +811,13 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
       else if (kind == KIND_HEAT) rc = run_elem<KIND_HEAT, 2>(ctx, a);
       else rc = run_elem<KIND_MASS, 2>(ctx, a);
     }
-    if (rc == LLF_OK) rc = gather_full(ctx, pat, Kf, kind == KIND_ELASTIC, m->d_nz, cnt);
+    if (rc == LLF_OK) rc = gather_full(ctx, pat, Kf, cs, kind == KIND_ELASTIC, m->d_nz, cnt);
     dfree(ctx, Kf);
   }
   dfree(ctx, d_c1);
   dfree(ctx, d_c2);
+  dfree(ctx, aflag);
+  dfree(ctx, ageo);
   if (rc == LLF_OK) rc = llf_check_status(ctx, "assembly");
   if (rc == LLF_OK && kind == KIND_MASS && lumped) {
     m->diagonal_only = true;

@@ -9,6 +9,7 @@
 // (~1e-7 relative to the largest entry); the stored (dropzeros!) pattern can
 // keep entries that cancel exactly only in FP64.
 #include "common.cuh"
+#include "affine.cuh"
 
 namespace {
 
@@ -23,7 +24,13 @@ struct Elem32Args {
   const float *w, *N, *dN;
   const double *c1, *c2;
   float *Kf;
+  int64_t colstride;  // floats per element-matrix column (16-byte multiple)
   unsigned *status;
+  // affine-element form: per-element flag and FP64 invJ/det (aflag null =
+  // none) and the per-pair tables of the FP64 form rounded to FP32
+  const uint8_t *aflag;
+  const double *ageo;
+  const float *Rp, *Mp;
 };
 
 __device__ __forceinline__ int poff(int a, int npe) { return a * npe - (a * (a - 1)) / 2; }
@@ -38,12 +45,12 @@ __device__ __forceinline__ void pdec(int pi, int npe, int &a, int &b) {
 }
 
 template <int P, int BS>
-__device__ __forceinline__ void store_pair32(float *Ke, int npe, int a, int b, const float *blk) {
-  float *ab = Ke + ((size_t)b * npe + a) * BS;
+__device__ __forceinline__ void store_pair32(float *Ke, int64_t cs, int a, int b, const float *blk) {
+  float *ab = Ke + (size_t)b * cs + (size_t)a * BS;
 #pragma unroll
   for (int k = 0; k < BS; ++k) ab[k] = blk[k];
   if (a != b) {
-    float *ba = Ke + ((size_t)a * npe + b) * BS;
+    float *ba = Ke + (size_t)a * cs + (size_t)b * BS;
     if (BS == 1) {
       ba[0] = blk[0];
     } else {
@@ -55,11 +62,85 @@ __device__ __forceinline__ void store_pair32(float *Ke, int npe, int a, int b, c
   }
 }
 
+// Node-pair blocks of an affine element in FP32: the FP64 form's per-element
+// coefficients (from the FP64 invJ and det) rounded to FP32, then
+// Ksym = W S, Kanti = U A per pair as in the FP64 form.
+template <int KIND, int DIM, int P, int BS>
+__device__ __forceinline__ void affine_pairs32(const Elem32Args &A, const double *sAff, float *Ke) {
+  constexpr int NS = DIM == 3 ? 6 : 3, NA = DIM == 3 ? 3 : 1;
+  const int npe = A.npe;
+  if (KIND == KIND_MASS) {
+    const float cm = (float)sAff[AF_M];
+    for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
+      int a, b;
+      pdec(pi, npe, a, b);
+      float blk[BS];
+      blk[0] = cm * __ldg(A.Mp + pi);
+      store_pair32<P, BS>(Ke, A.colstride, a, b, blk);
+    }
+  } else if (KIND == KIND_HEAT) {
+    float Q[NS];
+#pragma unroll
+    for (int n = 0; n < NS; ++n) Q[n] = (float)sAff[AF_Q + n];
+    for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
+      int a, b;
+      pdec(pi, npe, a, b);
+      const float *sp = A.Rp + (size_t)pi * 9;
+      float acc = 0.f;
+#pragma unroll
+      for (int n = 0; n < NS; ++n) acc = fmaf(Q[n], __ldg(sp + n), acc);
+      float blk[BS];
+      blk[0] = acc;
+      store_pair32<P, BS>(Ke, A.colstride, a, b, blk);
+    }
+  } else {
+    float W[NS * NS], U[NA * NA];
+#pragma unroll
+    for (int t = 0; t < NS * NS; ++t) W[t] = (float)sAff[AF_W + t];
+#pragma unroll
+    for (int t = 0; t < NA * NA; ++t) U[t] = (float)sAff[AF_U + t];
+    for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
+      int a, b;
+      pdec(pi, npe, a, b);
+      const float *sp = A.Rp + (size_t)pi * 9;
+      float sv[NS], av[NA];
+#pragma unroll
+      for (int n = 0; n < NS; ++n) sv[n] = __ldg(sp + n);
+#pragma unroll
+      for (int n = 0; n < NA; ++n) av[n] = __ldg(sp + 6 + n);
+      float ks[NS];
+#pragma unroll
+      for (int m = 0; m < NS; ++m) {
+        float acc = 0.f;
+#pragma unroll
+        for (int n = 0; n < NS; ++n) acc = fmaf(W[m * NS + n], sv[n], acc);
+        ks[m] = acc;
+      }
+      float blk[BS];
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) blk[i * DIM + i] = ks[i];
+#pragma unroll
+      for (int m = 0; m < NA; ++m) {
+        float acc = 0.f;
+        if (a != b)
+#pragma unroll
+          for (int n = 0; n < NA; ++n) acc = fmaf(U[m * NA + n], av[n], acc);
+        const int i = sym_k<DIM>(DIM + m), j = sym_l<DIM>(DIM + m);
+        blk[i * DIM + j] = ks[DIM + m] + acc;
+        blk[j * DIM + i] = ks[DIM + m] - acc;
+      }
+      store_pair32<P, BS>(Ke, A.colstride, a, b, blk);
+    }
+  }
+}
+
 template <int KIND, int DIM>
 __global__ void __launch_bounds__(E32_THREADS) k_elem_fp32(Elem32Args A) {
-  extern __shared__ float sf[];
+  extern __shared__ double sd64[];
   const int npe = A.npe, nip = A.nip;
   constexpr int gsw = (KIND == KIND_MASS) ? 1 : DIM;
+  double *sAff = sd64;                              // AFF_DOUBLES (affine form)
+  float *sf = (float *)(sAff + AFF_DOUBLES);
   float *sdN = sf;                                  // nip*npe*DIM
   float *sw = sdN + (size_t)nip * npe * DIM;        // nip
   float *sN = sw + nip;                             // nip*npe (mass)
@@ -82,6 +163,16 @@ __global__ void __launch_bounds__(E32_THREADS) k_elem_fp32(Elem32Args A) {
     const float c1 = (float)A.c1[mat];
     const float c2 = (KIND == KIND_ELASTIC) ? (float)A.c2[mat] : 0.f;
     const int32_t *cn = A.conn + e * npe;
+    float *Ke = A.Kf + (size_t)e * npe * A.colstride;
+    if (A.aflag && A.aflag[e]) {  // uniform across the CTA
+      if (threadIdx.x < 32)
+        affine_stage<DIM>(A.ageo + (size_t)e * 10, A.c1[mat], KIND == KIND_ELASTIC ? A.c2[mat] : 0.0, sAff,
+                          A.status);
+      __syncthreads();
+      affine_pairs32<KIND, DIM, P, BS>(A, sAff, Ke);
+      __syncthreads();
+      continue;
+    }
     for (int t = threadIdx.x; t < npe * DIM; t += blockDim.x) {
       int a = t / DIM, i = t % DIM;
       sX[t] = (float)(A.xyz[(size_t)cn[a] * 3 + i] - A.xyz[(size_t)cn[0] * 3 + i]);
@@ -142,7 +233,6 @@ __global__ void __launch_bounds__(E32_THREADS) k_elem_fp32(Elem32Args A) {
       }
     }
     __syncthreads();
-    float *Ke = A.Kf + (size_t)e * npe * npe * BS;
     for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
       int a, b;
       pdec(pi, npe, a, b);
@@ -190,7 +280,7 @@ __global__ void __launch_bounds__(E32_THREADS) k_elem_fp32(Elem32Args A) {
         for (int q = 0; q < nip; ++q) acc = fmaf(S[(size_t)q * npe + a], sN[(size_t)q * npe + b], acc);
         blk[0] = c1 * acc;
       }
-      store_pair32<P, BS>(Ke, npe, a, b, blk);
+      store_pair32<P, BS>(Ke, A.colstride, a, b, blk);
     }
     __syncthreads();
   }
@@ -200,7 +290,8 @@ template <int KIND, int DIM>
 int run_elem32(llf_ctx *ctx, Elem32Args a) {
   const int npe = a.npe, nip = a.nip;
   const int gsw = (KIND == KIND_MASS) ? 1 : DIM;
-  size_t smem = sizeof(float) * ((size_t)nip * npe * DIM + nip + (KIND == KIND_MASS ? (size_t)nip * npe : 0) +
+  size_t smem = sizeof(double) * AFF_DOUBLES +
+                sizeof(float) * ((size_t)nip * npe * DIM + nip + (KIND == KIND_MASS ? (size_t)nip * npe : 0) +
                                  (size_t)npe * DIM + nip + (size_t)nip * 9 + 2 * (size_t)nip * npe * gsw);
   if (smem > 200 * 1024)
     return llf_fail(ctx, LLF_ERR_LIMIT, "precision form: element tables exceed shared memory (use the FP64 form)");
@@ -222,11 +313,13 @@ int run_elem32(llf_ctx *ctx, Elem32Args a) {
 // Precision-form assembly of the structural values into nz (and the
 // per-column non-zero counts into cnt).
 int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, const double *d_c1,
-                       const double *d_c2, double *nz, int64_t *cnt) {
+                       const double *d_c2, const uint8_t *aflag, const double *ageo, double *nz,
+                       int64_t *cnt) {
   const int npe = mesh->npe, P = pat->pdim;
   const int BS = (kind == KIND_ELASTIC) ? P * P : 1;
   float *Kf = nullptr;
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &Kf, (size_t)mesh->nel * npe * npe * BS));
+  const int64_t cs = kf_colstride(npe, BS, (int)sizeof(float));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &Kf, (size_t)mesh->nel * npe * cs));
   Elem32Args a{};
   a.xyz = mesh->d_xyz;
   a.conn = mesh->d_conn;
@@ -241,7 +334,12 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
   a.c1 = d_c1;
   a.c2 = d_c2;
   a.Kf = Kf;
+  a.colstride = cs;
   a.status = ctx->d_status;
+  a.aflag = aflag;
+  a.ageo = ageo;
+  a.Rp = mesh->d_Rpf;
+  a.Mp = mesh->d_Mpf;
   int rc;
   if (mesh->dim == 3)
     rc = kind == KIND_ELASTIC ? run_elem32<KIND_ELASTIC, 3>(ctx, a)
@@ -249,7 +347,7 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
   else
     rc = kind == KIND_ELASTIC ? run_elem32<KIND_ELASTIC, 2>(ctx, a)
                               : (kind == KIND_HEAT ? run_elem32<KIND_HEAT, 2>(ctx, a) : run_elem32<KIND_MASS, 2>(ctx, a));
-  if (rc == LLF_OK) rc = gather_full32(ctx, pat, Kf, kind == KIND_ELASTIC, nz, cnt);
+  if (rc == LLF_OK) rc = gather_full32(ctx, pat, Kf, cs, kind == KIND_ELASTIC, nz, cnt);
   dfree(ctx, Kf);
   return rc;
 }

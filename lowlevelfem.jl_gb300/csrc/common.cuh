@@ -90,10 +90,12 @@ struct llf_mesh {
   std::vector<double> h_w, h_N, h_dN;  // host copies (FP32 tables derive from these)
   float *d_wf = nullptr, *d_Nf = nullptr, *d_dNf = nullptr;
   int tables_version = 0;
+  int conn_version = 0;           // bumped when llf_mesh_update changes the connectivity
   // affine-element tables (built-in rules, whose node coordinates are known;
   // null after llf_tables_upload): reference node coordinates [npe*3] and,
   // per upper-triangle node pair (a <= b, a-major), R_ab [9] and Mref_ab
   double *d_nref = nullptr, *d_Rp = nullptr, *d_Mp = nullptr;
+  float *d_Rpf = nullptr, *d_Mpf = nullptr;  // the same tables rounded to FP32
 };
 
 struct llf_pattern {
@@ -113,6 +115,11 @@ struct llf_pattern {
   int max_deg = 0;                // largest number of row nodes of a column node
   // DoF-level colptr (0-based)
   int64_t *d_colptr = nullptr;    // ndof+1
+  // element-to-column map: for column node B, element k of its list and local
+  // node a, the position of node conn[e][a] in B's row-node list,
+  // d_pos[(n2e_ptr[B] + k) * npe + a] (0xffff: not in the pattern)
+  uint16_t *d_pos = nullptr;
+  int conn_version = 0;           // mesh connectivity the pattern was built from
 };
 
 struct llf_matrix {
@@ -163,6 +170,9 @@ cudaError_t exclusive_scan_i64(llf_ctx *ctx, const int64_t *in, int64_t *out,
 // pattern.cu
 int pattern_build_impl(llf_ctx *ctx, llf_mesh *mesh, int pdim, llf_pattern *pat);
 int mesh_convert_conn(llf_ctx *ctx, llf_mesh *mesh, const int64_t *d_conn64);
+// Replace the connectivity by d_conn64 (1-based); *changed tells whether any
+// entry differs from the current one.
+int mesh_update_conn(llf_ctx *ctx, llf_mesh *mesh, const int64_t *d_conn64, bool *changed);
 int check_finite(llf_ctx *ctx, const double *d, int64_t n);
 // node -> (element, local index) lists sorted by element (elements with emat < 0 skipped)
 int build_n2e(llf_ctx *ctx, const int32_t *conn, const int32_t *emat, int64_t nel, int npe,
@@ -176,17 +186,26 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
 // the gather, else they are counted here
 int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts);
 // assemble_fp32.cu: precision form (FP32 quadrature, FP64 accumulation) into nz
+// aflag/ageo: per-element affine flag and invJ/det (null: quadrature form only)
 int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
-                       const double *d_c1, const double *d_c2, double *nz, int64_t *cnt);
+                       const double *d_c1, const double *d_c2, const uint8_t *aflag,
+                       const double *ageo, double *nz, int64_t *cnt);
 // Element-ordered column-node gather of whole element matrices laid out as
 // Kf[element][column node][row node][block] (blockval: pdim x pdim blocks,
 // entry (i,j) at i*pdim+j; otherwise one scalar per node pair placed on the
-// component diagonal).  Writes the structural values and, if cnt != NULL,
-// the non-zero count of every DoF column.
-int gather_full(llf_ctx *ctx, llf_pattern *pat, const double *Kf, bool blockval, double *nz,
-                int64_t *cnt);
-int gather_full32(llf_ctx *ctx, llf_pattern *pat, const float *Kf, bool blockval, double *nz,
-                  int64_t *cnt);
+// component diagonal).  Column (e, b) starts at Kf + (e*npe + b)*colstride
+// (colstride >= npe*block size, in elements).  Writes the structural values
+// and, if cnt != NULL, the non-zero count of every DoF column.
+int gather_full(llf_ctx *ctx, llf_pattern *pat, const double *Kf, int64_t colstride, bool blockval,
+                double *nz, int64_t *cnt);
+int gather_full32(llf_ctx *ctx, llf_pattern *pat, const float *Kf, int64_t colstride, bool blockval,
+                  double *nz, int64_t *cnt);
+// Element-matrix column stride (elements of `tsize` bytes) padded to 16 bytes,
+// so that every column can be fetched by one bulk copy.
+inline int64_t kf_colstride(int npe, int bs, int tsize) {
+  const int64_t bytes = ((int64_t)npe * bs * tsize + 15) / 16 * 16;
+  return bytes / tsize;
+}
 // field.cu: f[node*pdim+i] += fe[e][a][i] of every element of the node, in element order.
 int node_gather(llf_ctx *ctx, const int32_t *conn, int64_t nel, int npe, int64_t non, int pdim,
                 const double *fe, double *f);

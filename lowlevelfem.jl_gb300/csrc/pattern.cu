@@ -208,6 +208,48 @@ int mesh_convert_conn(llf_ctx *ctx, llf_mesh *mesh, const int64_t *d_conn64) {
   return LLF_OK;
 }
 
+// 1-based tags -> 0-based node indices into out, flagging entries that
+// differ from cur.
+__global__ void k_conn_update(const int64_t *__restrict__ in, const int32_t *__restrict__ cur,
+                              int32_t *__restrict__ out, int64_t count, int64_t non, int *differs,
+                              unsigned *status) {
+  int d = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = in[i];
+    int32_t v = 0;
+    if (t < 1 || t > non) atomicOr(status, ST_BAD_NODE);
+    else v = (int32_t)(t - 1);
+    out[i] = v;
+    d |= (v != cur[i]);
+  }
+  if (__syncthreads_or(d) && threadIdx.x == 0) atomicOr(differs, 1);
+}
+
+int mesh_update_conn(llf_ctx *ctx, llf_mesh *mesh, const int64_t *d_conn64, bool *changed) {
+  const int64_t count = mesh->nel * mesh->npe;
+  int32_t *fresh = nullptr;
+  int *d_diff = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &fresh, count));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_diff, 1));
+  LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_diff, 0, sizeof(int), ctx->stream));
+  k_conn_update<<<grid_for(count, 256, ctx->num_sms), 256, 0, ctx->stream>>>(
+      d_conn64, mesh->d_conn, fresh, count, mesh->non, d_diff, ctx->d_status);
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  int h = 0;
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&h, d_diff, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  LLF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  dfree(ctx, d_diff);
+  *changed = h != 0;
+  if (*changed) {
+    dfree(ctx, mesh->d_conn);
+    mesh->d_conn = fresh;
+  } else {
+    dfree(ctx, fresh);
+  }
+  return LLF_OK;
+}
+
 int check_finite(llf_ctx *ctx, const double *d, int64_t n) {
   if (n <= 0) return LLF_OK;
   k_check_finite<<<grid_for(n, 256, ctx->num_sms), 256, 0, ctx->stream>>>(d, n, ctx->d_status);
@@ -244,6 +286,38 @@ int build_n2e(llf_ctx *ctx, const int32_t *conn, const int32_t *emat, int64_t ne
   *list_out = list;
   *max_len = hmax;
   return LLF_OK;
+}
+
+// Element-to-column map, one warp per column node: for every (element of
+// the node's list, local node) pair, the row node's position in the column,
+// by binary search in the sorted row-node list.
+__global__ void k_row_positions(const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
+                                const int64_t *__restrict__ n2e_ptr, const int2 *__restrict__ n2e,
+                                const int32_t *__restrict__ conn, int npe, int64_t non,
+                                uint16_t *__restrict__ pos, unsigned *status) {
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  for (int64_t B = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5); B < non; B += (int64_t)gridDim.x * wpb) {
+    const int64_t c0 = nptr[B];
+    const int deg = (int)(nptr[B + 1] - c0);
+    const int64_t s = n2e_ptr[B];
+    const int64_t m = (n2e_ptr[B + 1] - s) * npe;
+    for (int64_t it = lane; it < m; it += 32) {
+      const int64_t k = it / npe;
+      const int a = (int)(it - k * npe);
+      const int A = conn[(size_t)n2e[s + k].x * npe + a];
+      int lo = 0, hi = deg - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (nadj[c0 + mid] < A) lo = mid + 1; else hi = mid;
+      }
+      uint16_t p = (uint16_t)lo;
+      if (deg == 0 || nadj[c0 + lo] != A) {
+        atomicOr(status, ST_PATTERN);
+        p = 0xffff;
+      }
+      pos[s * npe + it] = p;
+    }
+  }
 }
 
 int pattern_build_impl(llf_ctx *ctx, llf_mesh *mesh, int pdim, llf_pattern *pat) {
@@ -319,5 +393,19 @@ int pattern_build_impl(llf_ctx *ctx, llf_mesh *mesh, int pdim, llf_pattern *pat)
   k_dof_colptr<<<grid_for(non, 256, ctx->num_sms), 256, 0, s>>>(pat->d_nptr, non, pdim,
                                                                 pat->d_colptr);
   LLF_CUDA_TRY(ctx, cudaGetLastError());
+
+  // 4. element-to-column map (positions fit 16 bits)
+  if (pat->max_deg > 0xfffe)
+    return llf_fail(ctx, LLF_ERR_LIMIT, "pattern: a column node has more than 65534 row nodes");
+  int64_t n2e_total = 0;
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&n2e_total, pat->d_n2e_ptr + non, sizeof(int64_t),
+                                    cudaMemcpyDeviceToHost, s));
+  LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &pat->d_pos, (size_t)n2e_total * npe));
+  k_row_positions<<<grid_for(non * 32, 256, ctx->num_sms), 256, 0, s>>>(
+      pat->d_nptr, pat->d_nadj, pat->d_n2e_ptr, pat->d_n2e, mesh->d_conn, npe, non, pat->d_pos,
+      ctx->d_status);
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  pat->conn_version = mesh->conn_version;
   return llf_check_status(ctx, "llf_pattern_build");
 }

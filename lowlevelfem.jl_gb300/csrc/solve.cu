@@ -36,7 +36,7 @@
 namespace {
 
 constexpr int CG_THREADS = 256;
-constexpr int CHUNK = 4096;  // DoFs per reduction chunk
+constexpr int CHUNK = 768;  // DoFs per reduction chunk (a multiple of every pdim: chunks hold whole nodes)
 
 struct SegState {
   double rho_prev, rho, alpha, res, res0, tol;
@@ -265,30 +265,47 @@ __global__ void k_seg_dir(Seg S, const double *__restrict__ z, double *__restric
   }
 }
 
-// c = A u on the chunk's columns (masked) and partial u.c.
+// c = A u on the chunk's columns (masked) and partial u.c.  One warp per
+// node column B (chunks start and end on node boundaries): lanes take the
+// column's row nodes, read each row node's P values of u once and apply the
+// P x P block of all P DoF columns of B.
 template <int P>
 __global__ void __launch_bounds__(CG_THREADS)
-k_seg_spmv(Seg S, const double *__restrict__ nz, const int64_t *__restrict__ colptr,
-           const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
-           const double *__restrict__ u, const uint8_t *__restrict__ fixed,
-           double *__restrict__ c, double *__restrict__ part) {
+k_seg_spmv(Seg S, const double *__restrict__ nz, const int64_t *__restrict__ nptr,
+           const int32_t *__restrict__ nadj, const double *__restrict__ u,
+           const uint8_t *__restrict__ fixed, double *__restrict__ c, double *__restrict__ part) {
   const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, w = threadIdx.x >> 5;
   for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
     if (S.st[S.cseg[ch]].done) continue;
     double dot = 0.0;
-    for (int64_t col = S.cbeg[ch] + w; col < S.cend[ch]; col += wpb) {
-      const int64_t s = colptr[col], e = colptr[col + 1];
-      const int64_t r0 = nptr[col / P];
-      double acc = 0.0;
-      for (int64_t k = s + lane; k < e; k += 32) {
-        const int64_t loc = k - s;
-        acc = __fma_rn(nz[k], u[(int64_t)P * nadj[r0 + loc / P] + loc % P], acc);
+    const int64_t B1 = S.cend[ch] / P;
+    for (int64_t B = S.cbeg[ch] / P + w; B < B1; B += wpb) {
+      const int64_t r0 = nptr[B];
+      const int deg = (int)(nptr[B + 1] - r0);
+      const double *col = nz + (int64_t)P * P * r0;  // column (B,j): col[(j*deg + t)*P + i]
+      double acc[P];
+#pragma unroll
+      for (int j = 0; j < P; ++j) acc[j] = 0.0;
+      for (int t = lane; t < deg; t += 32) {
+        const int64_t A = nadj[r0 + t];
+        double xa[P];
+#pragma unroll
+        for (int i = 0; i < P; ++i) xa[i] = u[P * A + i];
+#pragma unroll
+        for (int j = 0; j < P; ++j)
+#pragma unroll
+          for (int i = 0; i < P; ++i) acc[j] = __fma_rn(col[((size_t)j * deg + t) * P + i], xa[i], acc[j]);
       }
-      acc = warp_sum(acc);
-      if (fixed[col]) acc = 0.0;
+#pragma unroll
+      for (int j = 0; j < P; ++j) acc[j] = warp_sum(acc[j]);
       if (lane == 0) {
-        c[col] = acc;
-        dot = __fma_rn(u[col], acc, dot);
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+          const int64_t d = P * B + j;
+          const double v = fixed[d] ? 0.0 : acc[j];
+          c[d] = v;
+          dot = __fma_rn(u[d], v, dot);
+        }
       }
     }
     double s = block_sum(dot);
@@ -374,7 +391,7 @@ void enqueue_iteration(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const do
   { KernelScope k(ctx, "k_seg_rho"); k_seg_rho<<<gseg, CG_THREADS, 0, s>>>(S, part); }
   { KernelScope k(ctx, "k_seg_dir"); k_seg_dir<<<gch, CG_THREADS, 0, s>>>(S, z, u); }
   { KernelScope k(ctx, "k_seg_spmv");
-    k_seg_spmv<P><<<gch, CG_THREADS, 0, s>>>(S, m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, u, fixed, c, part); }
+    k_seg_spmv<P><<<gch, CG_THREADS, 0, s>>>(S, m->d_nz, pat->d_nptr, pat->d_nadj, u, fixed, c, part); }
   { KernelScope k(ctx, "k_seg_alpha"); k_seg_alpha<<<gseg, CG_THREADS, 0, s>>>(S, part); }
   { KernelScope k(ctx, "k_seg_update"); k_seg_update<<<gch, CG_THREADS, 0, s>>>(S, xw, r, u, c, part); }
   { KernelScope k(ctx, "k_seg_finish"); k_seg_finish<<<gseg, CG_THREADS, 0, s>>>(S, part); }

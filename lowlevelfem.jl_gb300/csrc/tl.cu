@@ -467,7 +467,7 @@ int tl_matrix(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int mode, const do
        : (mode == TL_KGEO_S ? launch_matrix<TL_KGEO_S>(ctx, a, smem) : launch_matrix<TL_KGEO_C>(ctx, a, smem));
   if (rc == LLF_OK) {
     cudaError_t e = dalloc(ctx, &m->d_nz, pat->nnz);
-    rc = (e == cudaSuccess) ? gather_full(ctx, pat, Kp, mat, m->d_nz, cnt)
+    rc = (e == cudaSuccess) ? gather_full(ctx, pat, Kp, (int64_t)mesh->npe * BS, mat, m->d_nz, cnt)
                             : llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
   }
   dfree(ctx, Kp);

@@ -188,55 +188,95 @@ static int orc_is_affine(int dim, int npe, const double *X, const double *dN0, c
   return s > 0.0;
 }
 
-/* Affine-element matrix; returns -1 for det <= 0.  With the geometry of
- * point 0 (the Jacobian of an affine element is the same at every point) and
- * Y = det*J^-1:  T = R_ab Y,  O_ab = J^-T T  (= sum_q w_q det g_a g_b^T),
- * heat: trace(O_ab), mass: det*Mref_ab. */
+/* Affine-element matrix; returns -1 for det <= 0.
+ * R_ab splits into its symmetric part S (components n = (k,l), k <= l, in the
+ * order 00 11 22 01 02 12; 2D: 00 11 01; S_kl = (R_kl + R_lk) * 0.5) and its
+ * antisymmetric part A (01 02 12; 2D: 01; A_kl = (R_kl - R_lk) * 0.5).  With
+ * O = det J^-T R J^-1 = Os + Oa, the element's coefficients
+ *   V[m][n] = det * inv_ki inv_kj                      (k == l)
+ *           = det * fma(inv_ki, inv_lj, inv_li inv_kj)  (k <  l)   m = (i,j)
+ *   U[m][n] = cm * (det * fma(inv_ki, inv_lj, -(inv_li inv_kj)))
+ * (inv_ki = invJ[k][i]) map S and A to Os and Oa, and the Lame combination
+ * K = c1 O + c2 O^T + c2 tr(O) I becomes, with cp = c1 + c2, cm = c1 - c2,
+ *   Ksym = W S,  W[m][n] = fma(c2, trV[n], cp*V[m][n]) (m diagonal) or cp*V[m][n],
+ *   Kanti = U A,  K_ii = Ksym_ii,  K_ij = Ksym_ij + Kanti_ij,  K_ji = Ksym_ij - Kanti_ij
+ * (a == b: A = 0, K_ij = K_ji = Ksym_ij); heat: (c1 trV) . S; mass: (c1 det) Mref.
+ * Products with W, U, c1 trV are fma chains over n from 0.0. */
+static const int ORC_SYM3[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+static const int ORC_SYM2[3][2] = {{0, 0}, {1, 1}, {0, 1}};
+
+void orc_affine_split(int dim, const double *Rab, double *sv, double *av) {
+  const int ns = dim == 3 ? 6 : 3, na = dim == 3 ? 3 : 1;
+  const int(*sym)[2] = dim == 3 ? ORC_SYM3 : ORC_SYM2;
+  for (int n = 0; n < ns; ++n) {
+    int k = sym[n][0], l = sym[n][1];
+    sv[n] = k == l ? Rab[k * 3 + k] : (Rab[k * 3 + l] + Rab[l * 3 + k]) * 0.5;
+  }
+  for (int n = 0; n < na; ++n) {
+    int k = sym[dim + n][0], l = sym[dim + n][1];
+    av[n] = (Rab[k * 3 + l] - Rab[l * 3 + k]) * 0.5;
+  }
+}
+
 static int orc_element_affine(int kind, int dim, int pdim, int npe, const double *dN0, const double *X,
                               const double *R, const double *Mref, double c1, double c2, double *Ke) {
   size_t nd = (size_t)pdim * npe;
-  double inv[9], Y[9];
+  double inv[9];
   double det = orc_geom(dim, npe, X, dN0, inv);
   if (!(det > 0.0)) return -1;
-  for (int k = 0; k < 9; ++k) Y[k] = det * inv[k];
+  const int ns = dim == 3 ? 6 : 3, na = dim == 3 ? 3 : 1;
+  const int(*sym)[2] = dim == 3 ? ORC_SYM3 : ORC_SYM2;
+  double V[6][6], trV[6], W[6][6], U[3][3], Qh[6];
+  for (int m = 0; m < ns; ++m)
+    for (int n = 0; n < ns; ++n) {
+      int i = sym[m][0], j = sym[m][1], k = sym[n][0], l = sym[n][1];
+      V[m][n] = k == l ? det * (inv[k * 3 + i] * inv[k * 3 + j])
+                       : det * fma(inv[k * 3 + i], inv[l * 3 + j], inv[l * 3 + i] * inv[k * 3 + j]);
+    }
+  for (int n = 0; n < ns; ++n) trV[n] = dim == 3 ? (V[0][n] + V[1][n]) + V[2][n] : V[0][n] + V[1][n];
+  const double cp = c1 + c2, cm = c1 - c2;
+  for (int m = 0; m < ns; ++m)
+    for (int n = 0; n < ns; ++n) W[m][n] = m < dim ? fma(c2, trV[n], cp * V[m][n]) : cp * V[m][n];
+  for (int m = 0; m < na; ++m)
+    for (int n = 0; n < na; ++n) {
+      int i = sym[dim + m][0], j = sym[dim + m][1], k = sym[dim + n][0], l = sym[dim + n][1];
+      U[m][n] = cm * (det * fma(inv[k * 3 + i], inv[l * 3 + j], -(inv[l * 3 + i] * inv[k * 3 + j])));
+    }
+  for (int n = 0; n < ns; ++n) Qh[n] = c1 * trV[n];
+  const double cmass = c1 * det;
   memset(Ke, 0, sizeof(double) * nd * nd);
   for (int a = 0; a < npe; ++a)
     for (int b = a; b < npe; ++b) {
       double blk[9] = {0};
-      const double *Rab = R + ((size_t)a * npe + b) * 9;
       if (kind == ORC_MASS) {
-        double m = c1 * (det * Mref[(size_t)a * npe + b]);
-        for (int i = 0; i < pdim; ++i) blk[i * pdim + i] = m;
+        double mv = cmass * Mref[(size_t)a * npe + b];
+        for (int i = 0; i < pdim; ++i) blk[i * pdim + i] = mv;
       } else {
-        double T[3][3];
-        for (int k = 0; k < dim; ++k)
-          for (int j = 0; j < dim; ++j) {
-            double acc = 0.0;
-            for (int l = 0; l < dim; ++l) acc = fma(Rab[k * 3 + l], Y[l * 3 + j], acc);
-            T[k][j] = acc;
-          }
+        double sv[6], av[3];
+        orc_affine_split(dim, R + ((size_t)a * npe + b) * 9, sv, av);
         if (kind == ORC_HEAT) {
-          double sacc = 0.0;
-          for (int i = 0; i < dim; ++i)
-            for (int k = 0; k < dim; ++k) sacc = fma(inv[k * 3 + i], T[k][i], sacc);
-          blk[0] = c1 * sacc;
+          double acc = 0.0;
+          for (int n = 0; n < ns; ++n) acc = fma(Qh[n], sv[n], acc);
+          blk[0] = acc;
         } else {
-          double O[3][3] = {{0}};
-          for (int i = 0; i < dim; ++i)
-            for (int j = (a == b ? i : 0); j < dim; ++j) {
+          double ks[6], ka[3] = {0.0, 0.0, 0.0};
+          for (int m = 0; m < ns; ++m) {
+            double acc = 0.0;
+            for (int n = 0; n < ns; ++n) acc = fma(W[m][n], sv[n], acc);
+            ks[m] = acc;
+          }
+          if (a != b)
+            for (int m = 0; m < na; ++m) {
               double acc = 0.0;
-              for (int k = 0; k < dim; ++k) acc = fma(inv[k * 3 + i], T[k][j], acc);
-              O[i][j] = acc;
-              if (a == b) O[j][i] = acc;
+              for (int n = 0; n < na; ++n) acc = fma(U[m][n], av[n], acc);
+              ka[m] = acc;
             }
-          double tr = O[0][0] + O[1][1];
-          if (dim == 3) tr = tr + O[2][2];
-          for (int i = 0; i < dim; ++i)
-            for (int j = 0; j < dim; ++j) {
-              double t = fma(c2, O[j][i], c1 * O[i][j]);
-              if (i == j) t = fma(c2, tr, t);
-              blk[i * pdim + j] = t;
-            }
+          for (int i = 0; i < dim; ++i) blk[i * pdim + i] = ks[i];
+          for (int m = 0; m < na; ++m) {
+            int i = sym[dim + m][0], j = sym[dim + m][1];
+            blk[i * pdim + j] = a != b ? ks[dim + m] + ka[m] : ks[dim + m];
+            blk[j * pdim + i] = a != b ? ks[dim + m] - ka[m] : ks[dim + m];
+          }
         }
       }
       for (int i = 0; i < pdim; ++i)

@@ -273,3 +273,38 @@ def test_c2_hex27_full_size_properties(llf):
     x = np.random.default_rng(2).standard_normal(n)
     z = np.random.default_rng(3).standard_normal(n)
     assert abs(z @ (K * x) - x @ (K * z)) <= 1e-12 * np.abs(K * x).sum()
+
+
+def test_connectivity_change_requires_new_pattern(llf, orc):
+    """The pattern carries an element-to-column map: re-uploading the same
+    connectivity keeps it valid; a changed connectivity makes assembly fail
+    with LLF_ERR_STATE until a new pattern is built."""
+    L = llf._lib
+    m = llf.structured_box_mesh(n=2, order=2)
+    ctx = L.Context(0)
+    dm = L.DeviceMesh(ctx, m.dim, m.xyz, m.conn, m.family, m.order)
+    pat = L.DevicePattern(dm, 3)
+    E, nu = np.array([2.1e5]), np.array([0.3])
+
+    def assemble(p):
+        h = L.C.c_void_p()
+        rc = L.lib().llf_assemble_stiffness(ctx.h, dm.h, p.h, 0, L.ptr(E, L.C.c_double), L.ptr(nu, L.C.c_double),
+                                            1, 1.0, 0, L.C.byref(h))
+        return rc, (L.DeviceMatrix(ctx, h, p) if rc == 0 else None)
+
+    rc, K0 = assemble(pat)
+    assert rc == 0
+    dm.update(m.xyz, m.conn)                       # same connectivity: pattern still valid
+    rc, K1 = assemble(pat)
+    assert rc == 0
+    assert all(np.array_equal(a, b) for a, b in zip(K0.copy_csc(), K1.copy_csc()))
+    conn2 = np.asarray(m.conn).copy()
+    conn2[[0, 1]] = conn2[[1, 0]]                  # same elements, another element order
+    dm.update(m.xyz, conn2)
+    rc, _ = assemble(pat)
+    assert rc == -5 and "pattern" in L.lib().llf_last_error(ctx.h).decode()
+    pat2 = L.DevicePattern(dm, 3)
+    rc, K2 = assemble(pat2)
+    assert rc == 0
+    ref = orc.assemble(orc.ELASTIC, 0, 3, 3, m.xyz, conn2, L.builtin_rule(m.family, m.order), [2.1e5, 0.3])
+    assert_csc_identical(K2.copy_csc(), ref.julia(), "K after connectivity change")
