@@ -33,6 +33,11 @@ N_CELLS = 40
 ORDER = 2
 E, NU = 2.1e5, 0.3
 WORKLOAD = "hooke3d-unit-cube-hex27-40x40x40"
+# ncu DRAM bytes (read + write) of one FP64 assembly of hex27 16^3 (19,320,201
+# structural nnz): k_affine_geometry 1.3 MB, k_elem_fp64 165.0 MB,
+# k_colgather 338.2 MB, k_compact 417.5 MB
+NNZ_16CUBE = 19320201
+DRAM_BYTES_16CUBE = (1.324032 + 6.096128 + 158.8992 + 224.209664 + 114.00704 + 165.33248 + 252.210688) * 1e6
 
 
 def parse():
@@ -478,9 +483,17 @@ def main():
     elem_ms = prof.get("k_elem_fp64", {}).get("ms", 0.0) / max(prof.get("k_elem_fp64", {}).get("launches", 1), 1)
     fp64_achieved = flops / (elem_ms * 1e-3) / 1e12 if elem_ms > 0 else None
 
+    # DRAM traffic of one FP64 assembly from ncu captures of its kernels on
+    # hex27 16^3 (profiles/k_*_hex27_16cube.md), scaled by structural nnz
+    traffic = None
+    if form == L.FP64 and ORDER == 2:
+        traffic = DRAM_BYTES_16CUBE * nnz / NNZ_16CUBE
     roofline = {"bound": "hbm", "kernel": "assembly (all kernels of one llf_assemble_stiffness)",
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "peak_source": peak_kind, "traffic": None,
+                "peak_source": peak_kind, "traffic": traffic,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_affine_geometry, "
+                                  "k_elem_fp64, k_colgather, k_compact on hex27 16^3, scaled by structural nnz"
+                                  if traffic else None,
                 "algorithmic_bytes": bytes_alg, "dominant_kernel": kname, "dominant_ms": k_ms,
                 "per_kernel": per_kernel,
                 "fp64": {"element_kernel_flops": flops, "achieved_tflops": fp64_achieved,
