@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--workers", type=int, default=4, help="serving: server workers")
     ap.add_argument("--no-peak", action="store_true", help="skip the DGEMM FP64 reference rate")
     ap.add_argument("--no-other-form", action="store_true", help="skip the second arithmetic form")
+    ap.add_argument("--precond", default=None, choices=["jacobi", "bjacobi", "ic0"],
+                    help="batched / tl: CG preconditioner (default: ic0 for batched, bjacobi for tl)")
     return ap.parse_args()
 
 
@@ -218,12 +220,13 @@ def run_batched(args, llf):
     sup = [llf.displacementConstraint(f"left#{i}", ux=0, uy=0, uz=0) for i in range(len(inst))]
     f = llf.loadVector(P, loads)
     P.pattern()
+    prec = args.precond or "ic0"
     times = []
     for rep in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         K = llf.stiffnessMatrix(P)
-        u = llf.solveFieldBatched(K, f, support=sup, node_offsets=noff, preconditioner="jacobi", reltol=1e-12)
+        u = llf.solveFieldBatched(K, f, support=sup, node_offsets=noff, preconditioner=prec, reltol=1e-12)
         torch.cuda.synchronize()
         if rep >= args.warmup:
             times.append(time.perf_counter() - t0)
@@ -246,7 +249,7 @@ def run_batched(args, llf):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded sample of the 512-instance tet10 workload",
             "config": {"workload": f"batched-tet10-{len(inst)}", "instances": len(inst), "elements": nel,
-                       "dofs": 3 * batch.non, "structural_nnz": P.pattern().nnz, "precond": "jacobi",
+                       "dofs": 3 * batch.non, "structural_nnz": P.pattern().nnz, "precond": prec,
                        "reltol": 1e-12},
             "cg_iterations": {"min": int(np.min(u.iterations)), "median": float(np.median(u.iterations)),
                               "max": int(np.max(u.iterations))},
@@ -335,7 +338,7 @@ def run_tl(args, llf):
     ctx.profile(True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    u = llf.solveDeformation(P, support=sup, params=prm, steps=10, tol=1e-8, preconditioner="bjacobi")
+    u = llf.solveDeformation(P, support=sup, params=prm, steps=10, tol=1e-8, preconditioner=args.precond or "bjacobi")
     torch.cuda.synchronize()
     t_newton = time.perf_counter() - t0
     ctx.profile(False)
@@ -360,6 +363,7 @@ def run_tl(args, llf):
             "unit": "ms/iteration", "n_gpus": 1, "steps": its, "warmup": 0, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic unit cube",
             "config": {"workload": "tl-neohooke-hex8-48", "elements": m.nel, "dofs": 3 * m.non,
+                       "precond": args.precond or "bjacobi",
                        "newton_iterations": its, "load_steps": 10},
             "newton_total_s": t_newton,
             "kernels_ms": {k: v["ms"] for k, v in prof.items()},

@@ -77,6 +77,7 @@ extern "C" {
 #define LLF_PRECOND_NONE     0   /* IterativeSolvers Identity() (src/linear.jl:3711) */
 #define LLF_PRECOND_JACOBI   1
 #define LLF_PRECOND_BJACOBI  2   /* pdim x pdim node-block Jacobi */
+#define LLF_PRECOND_IC0      3   /* node-block IC(0) in multicolour order (llf_pcg, llf_pcg_batched) */
 
 typedef struct llf_ctx     llf_ctx;
 typedef struct llf_mesh    llf_mesh;

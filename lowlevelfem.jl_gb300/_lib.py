@@ -25,7 +25,7 @@ LINE, TRI, QUAD, TET, HEX = 1, 2, 3, 4, 5
 SOLID, PLANE_STRESS, PLANE_STRAIN, HEAT_CONDUCTION, PLANE_HEAT_CONDUCTION = 0, 1, 2, 3, 4
 FP64, FP32Q = 0, 1
 LAW_CONSTANT_C, LAW_NEOHOOKE_COMP, LAW_SVK = 0, 1, 2
-PRECOND_NONE, PRECOND_JACOBI, PRECOND_BJACOBI = 0, 1, 2
+PRECOND_NONE, PRECOND_JACOBI, PRECOND_BJACOBI, PRECOND_IC0 = 0, 1, 2, 3
 
 
 class LLFError(RuntimeError):

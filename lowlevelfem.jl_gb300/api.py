@@ -468,7 +468,7 @@ def loadVector(problem: Problem, loads) -> VectorField | ScalarField:
 # --------------------------------------------------------------------------
 _PRECOND = {"identity": _lib.PRECOND_NONE, "none": _lib.PRECOND_NONE, None: _lib.PRECOND_NONE,
             "jacobi": _lib.PRECOND_JACOBI, "bjacobi": _lib.PRECOND_BJACOBI,
-            "blockjacobi": _lib.PRECOND_BJACOBI}
+            "blockjacobi": _lib.PRECOND_BJACOBI, "ic0": _lib.PRECOND_IC0, "ichol": _lib.PRECOND_IC0}
 
 # tolerance used when the caller asks for the reference's direct solve
 DIRECT_RELTOL = 1e-13

@@ -498,6 +498,7 @@ int llf_pattern_destroy(llf_ctx *ctx, llf_pattern *p) {
     dfree(ctx, p->d_n2e_ptr); dfree(ctx, p->d_n2e); dfree(ctx, p->d_nptr);
     dfree(ctx, p->d_nadj); dfree(ctx, p->d_diagpos); dfree(ctx, p->d_colptr);
     dfree(ctx, p->d_pos);
+    ic0_coloring_free(ctx, p);
     cudaStreamSynchronize(ctx->stream);
   }
   delete p;
@@ -803,7 +804,7 @@ int llf_pcg(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x, const
             int precond, double reltol, int64_t maxiter, int64_t *iters, double *relres) {
   if (!ctx) return LLF_ERR_ARG;
   if (!m || !b || !x || !fixed) return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg: null argument");
-  if (precond < LLF_PRECOND_NONE || precond > LLF_PRECOND_BJACOBI)
+  if (precond < LLF_PRECOND_NONE || precond > LLF_PRECOND_IC0)
     return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg: unknown preconditioner");
   const int64_t n = m->pat->ndof;
   double *db = nullptr, *dx = nullptr;
@@ -852,7 +853,7 @@ int llf_pcg_batched(llf_ctx *ctx, const llf_matrix *m, const double *b, double *
   if (!ctx) return LLF_ERR_ARG;
   if (!m || !b || !x || !fixed || !seg_off || !iters || !relres || nseg < 1)
     return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched: null argument or nseg < 1");
-  if (precond < LLF_PRECOND_NONE || precond > LLF_PRECOND_BJACOBI)
+  if (precond < LLF_PRECOND_NONE || precond > LLF_PRECOND_IC0)
     return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched: unknown preconditioner");
   const int64_t n = m->pat->ndof;
   if (seg_off[0] != 0 || seg_off[nseg] != n)

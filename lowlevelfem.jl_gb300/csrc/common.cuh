@@ -120,6 +120,7 @@ struct llf_pattern {
   // d_pos[(n2e_ptr[B] + k) * npe + a] (0xffff: not in the pattern)
   uint16_t *d_pos = nullptr;
   int conn_version = 0;           // mesh connectivity the pattern was built from
+  void *ic_coloring = nullptr;    // node colouring of the IC(0) preconditioner (ic0.cu), on first use
 };
 
 struct llf_matrix {
@@ -223,6 +224,31 @@ int pcg_noalloc_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doubl
 int pcg_batched_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                      const uint8_t *d_fixed, int nseg, const int64_t *seg_off, int precond,
                      double reltol, int64_t maxiter, int64_t *iters, double *relres);
+
+// ic0.cu: multicolour node-block IC(0)
+struct Ic0Factor {
+  int ncolors = 0;
+  std::vector<int64_t> color_ptr;   // host: colour c = nodes [color_ptr[c], color_ptr[c+1]) of d_nodes
+  const int16_t *d_color = nullptr; // per node (owned by the pattern)
+  const int32_t *d_nodes = nullptr; // nodes sorted by colour (owned by the pattern)
+  double *Lrow = nullptr;           // L_jk with node j's list  (nnzb * P * P), FP64, during the factorisation
+  double *Lcol = nullptr;           // L_jk with node k's list  (nnzb * P * P)
+  double *Ldinv = nullptr;          // L_jj^-1 per node          (non * P * P)
+  double shift = 0.0;               // diagonal shift the factorisation needed
+  // FP32 factor for the solves: node j's earlier neighbours fk[fptr[j]..] with
+  // blocks Lf (L_jk), later neighbours bk[bptr[j]..] with blocks Lb (L_kj),
+  // and L_jj^-1 (Ldf); the index arrays belong to the pattern's colouring
+  const int64_t *fptr = nullptr, *bptr = nullptr;
+  const int32_t *fk = nullptr, *bk = nullptr;
+  float *Lf = nullptr, *Lb = nullptr, *Ldf = nullptr;
+};
+// seg_nodes: first node of each independent system (+ node count), d_node_seg:
+// system of every node; a system's colouring and factor do not depend on the
+// others, so a batched system preconditions exactly as it would alone.
+int ic0_factor(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixed, const std::vector<int64_t> &seg_nodes,
+               const int32_t *d_node_seg, Ic0Factor *f);
+void ic0_release(llf_ctx *ctx, Ic0Factor *f);
+void ic0_coloring_free(llf_ctx *ctx, llf_pattern *pat);
 
 // tl.cu
 int tl_material_tangent_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,

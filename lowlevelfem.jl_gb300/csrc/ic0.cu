@@ -1,0 +1,543 @@
+// Multicolour node-block incomplete Cholesky, IC(0), for the PCG (the
+// preconditioner the reference leaves to the caller's `preconditioner=`
+// keyword of solveDisplacement / solveField, src/linear.jl:3711-3743 and
+// src/poisson.jl:1432-1546).
+//
+// Ordering.  The node graph of the pattern is coloured once per pattern
+// (Jones-Plassmann rounds with hashed priorities, first-fit colours: nodes
+// coloured in one round are pairwise non-adjacent), and the unknowns are
+// ordered colour by colour.  Within a colour no two nodes are coupled, so
+// every step of the factorisation and of both triangular solves is
+// parallel over the nodes of one colour.
+//
+// Factor.  L is block lower triangular (p x p blocks on the node pattern,
+// zero fill):  for node j of colour c and each neighbour i of an earlier
+// colour (colour by colour),
+//     L_ji = (A'_ji - sum_k L_jk L_ik^T) L_ii^-T,   k earlier than i, k ~ i, k ~ j
+//     L_jj = chol(A'_jj - sum_k L_jk L_jk^T)
+// where A' is A with the fixed DoFs' rows and columns replaced by identity.
+// L_ji is kept twice: with node j's row list (forward solve) and with node
+// i's list (backward solve).  A non-positive pivot sets a flag; the host
+// then refactors A + alpha diag(A) with growing alpha.
+//
+// Apply.  z = (L L^T)^-1 r: forward colour sweep y_j = L_jj^-1 (r_j -
+// sum L_jk y_k), backward sweep z_i = L_ii^-T (y_i - sum L_ji^T z_j).  The
+// factor is computed in FP64 and applied in FP32 (blocks packed per node in
+// forward and backward neighbour lists, eight lanes per node, fixed tree
+// reductions, so the result is deterministic): the preconditioner only
+// steers the CG directions, whose residuals stay FP64.
+#include "common.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace {
+
+constexpr int IC_THREADS = 256;
+constexpr int MAX_COLORS = 256;
+
+__device__ __forceinline__ uint32_t jp_hash(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+// One Jones-Plassmann round: an uncoloured node whose priority (hash of its
+// index within its system, then that index) is the largest among its
+// uncoloured neighbours takes the smallest colour none of its coloured
+// neighbours has.  Priorities relative to the system's first node make the
+// colouring of a system the same alone and inside a batch.  Reads cin,
+// writes cout (a copy of cin plus this round's colours); counts the nodes
+// left uncoloured.
+__global__ void k_jp_round(const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj, int64_t non,
+                           const int32_t *__restrict__ node_seg, const int64_t *__restrict__ seg_nbeg,
+                           const int16_t *__restrict__ cin, int16_t *__restrict__ cout, int *remaining,
+                           unsigned *status) {
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  for (int64_t B = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5); B < non; B += (int64_t)gridDim.x * wpb) {
+    const int16_t cb = cin[B];
+    if (cb >= 0) {
+      if (lane == 0) cout[B] = cb;
+      continue;
+    }
+    const int64_t base = seg_nbeg[node_seg[B]];
+    const uint32_t lb = (uint32_t)(B - base), hb = jp_hash(lb);
+    const int64_t c0 = nptr[B];
+    const int deg = (int)(nptr[B + 1] - c0);
+    bool beaten = false;
+    uint32_t used[MAX_COLORS / 32];
+#pragma unroll
+    for (int w = 0; w < MAX_COLORS / 32; ++w) used[w] = 0u;
+    for (int t = lane; t < deg; t += 32) {
+      const int32_t A = nadj[c0 + t];
+      if (A == B) continue;
+      const int16_t ca = cin[A];
+      if (ca >= 0) {
+        used[ca >> 5] |= 1u << (ca & 31);
+      } else {
+        const uint32_t la = (uint32_t)(A - base), ha = jp_hash(la);  // A is in B's system
+        if (ha > hb || (ha == hb && la > lb)) beaten = true;
+      }
+    }
+    beaten = __any_sync(0xffffffffu, beaten);
+    if (beaten) {
+      if (lane == 0) {
+        cout[B] = -1;
+        atomicAdd(remaining, 1);
+      }
+      continue;
+    }
+#pragma unroll
+    for (int w = 0; w < MAX_COLORS / 32; ++w)
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) used[w] |= __shfl_xor_sync(0xffffffffu, used[w], off);
+    if (lane == 0) {
+      int c = -1;
+      for (int w = 0; w < MAX_COLORS / 32 && c < 0; ++w)
+        if (~used[w]) c = w * 32 + __ffs(~used[w]) - 1;
+      if (c < 0) {
+        atomicOr(status, ST_CAPACITY);
+        c = MAX_COLORS - 1;
+      }
+      cout[B] = (int16_t)c;
+    }
+  }
+}
+
+__device__ __forceinline__ int bsearch_row(const int32_t *__restrict__ rows, int deg, int32_t key) {
+  int lo = 0, hi = deg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (rows[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  return (deg > 0 && rows[lo] == key) ? lo : -1;
+}
+
+// A' entry (row DoF (jr), column DoF (ic)) from the structural values: the
+// column (i, cc) of node i holds the row node j at position t of i's list.
+template <int P>
+__device__ __forceinline__ double a_prime(const double *__restrict__ nz, int64_t ci0, int degi, int ti, int r,
+                                          int cc, int64_t j, int64_t i, const uint8_t *__restrict__ fixed) {
+  const bool fj = fixed[P * j + r], fi = fixed[P * i + cc];
+  if (fj || fi) return (j == i && r == cc) ? 1.0 : 0.0;
+  return nz[(size_t)P * P * ci0 + (size_t)cc * P * degi + (size_t)P * ti + r];
+}
+
+// Factorisation of the nodes of one colour (warp per node).
+template <int P>
+__global__ void __launch_bounds__(IC_THREADS)
+k_ic0_factor(const int32_t *__restrict__ nodes, int count, int color_c, const int64_t *__restrict__ nptr,
+             const int32_t *__restrict__ nadj, const int32_t *__restrict__ diagpos,
+             const int16_t *__restrict__ color, const double *__restrict__ nz,
+             const uint8_t *__restrict__ fixed, double shift, double *__restrict__ Lrow,
+             double *__restrict__ Lcol, double *__restrict__ Ldinv, int *fail) {
+  constexpr int PP = P * P;
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  for (int w = blockIdx.x * wpb + (threadIdx.x >> 5); w < count; w += gridDim.x * wpb) {
+    const int64_t j = nodes[w];
+    const int64_t c0 = nptr[j];
+    const int deg = (int)(nptr[j + 1] - c0);
+    const int32_t *rj = nadj + c0;
+    // off-diagonal blocks of row j, one earlier colour at a time
+    for (int cp = 0; cp < color_c; ++cp) {
+      for (int t = lane; t < deg; t += 32) {
+        const int64_t i = rj[t];
+        if (color[i] != cp) continue;
+        const int64_t ci0 = nptr[i];
+        const int degi = (int)(nptr[i + 1] - ci0);
+        const int32_t *ri = nadj + ci0;
+        double S[P][P];
+#pragma unroll
+        for (int a = 0; a < P; ++a)
+#pragma unroll
+          for (int b = 0; b < P; ++b) S[a][b] = 0.0;
+        for (int u = 0; u < deg; ++u) {
+          const int32_t k = rj[u];
+          if (color[k] >= cp) continue;
+          const int pk = bsearch_row(ri, degi, k);
+          if (pk < 0) continue;
+          const double *Ljk = Lrow + (size_t)(c0 + u) * PP;
+          const double *Lik = Lrow + (size_t)(ci0 + pk) * PP;
+#pragma unroll
+          for (int a = 0; a < P; ++a)
+#pragma unroll
+            for (int b = 0; b < P; ++b)
+#pragma unroll
+              for (int m = 0; m < P; ++m) S[a][b] = __fma_rn(Ljk[a * P + m], Lik[b * P + m], S[a][b]);
+        }
+        const int tj = bsearch_row(ri, degi, (int32_t)j);  // j in i's list
+        if (tj < 0) {  // the node pattern is symmetric; a miss means corrupt input
+          atomicOr((unsigned *)fail, 2u);
+          continue;
+        }
+        double Bm[P][P];
+#pragma unroll
+        for (int a = 0; a < P; ++a)
+#pragma unroll
+          for (int b = 0; b < P; ++b)
+            Bm[a][b] = __dsub_rn(a_prime<P>(nz, ci0, degi, tj, a, b, j, i, fixed), S[a][b]);
+        const double *Di = Ldinv + (size_t)i * PP;  // L_ii^-1, lower
+        double X[P][P];
+#pragma unroll
+        for (int a = 0; a < P; ++a)
+#pragma unroll
+          for (int b = 0; b < P; ++b) {
+            double acc = 0.0;
+#pragma unroll
+            for (int m = 0; m < P; ++m) acc = __fma_rn(Bm[a][m], Di[b * P + m], acc);
+            X[a][b] = acc;
+          }
+        double *lr = Lrow + (size_t)(c0 + t) * PP;
+        double *lc = Lcol + (size_t)(ci0 + tj) * PP;
+#pragma unroll
+        for (int a = 0; a < P; ++a)
+#pragma unroll
+          for (int b = 0; b < P; ++b) {
+            lr[a * P + b] = X[a][b];
+            lc[a * P + b] = X[a][b];
+          }
+      }
+      __syncwarp();
+    }
+    // diagonal block
+    double D[P][P];
+#pragma unroll
+    for (int a = 0; a < P; ++a)
+#pragma unroll
+      for (int b = 0; b < P; ++b) D[a][b] = 0.0;
+    for (int t = lane; t < deg; t += 32) {
+      const int32_t k = rj[t];
+      if (color[k] >= color_c) continue;
+      const double *Ljk = Lrow + (size_t)(c0 + t) * PP;
+#pragma unroll
+      for (int a = 0; a < P; ++a)
+#pragma unroll
+        for (int b = 0; b < P; ++b)
+#pragma unroll
+          for (int m = 0; m < P; ++m) D[a][b] = __fma_rn(Ljk[a * P + m], Ljk[b * P + m], D[a][b]);
+    }
+#pragma unroll
+    for (int a = 0; a < P; ++a)
+#pragma unroll
+      for (int b = 0; b < P; ++b)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) D[a][b] = __dadd_rn(D[a][b], __shfl_xor_sync(0xffffffffu, D[a][b], off));
+    if (lane == 0) {
+      const int dp = diagpos[j];
+      double Aj[P][P];
+#pragma unroll
+      for (int a = 0; a < P; ++a)
+#pragma unroll
+        for (int b = 0; b < P; ++b) {
+          double v = dp >= 0 ? a_prime<P>(nz, c0, deg, dp, a, b, j, j, fixed) : (a == b ? 1.0 : 0.0);
+          if (a == b) v = __dmul_rn(v, 1.0 + shift);
+          Aj[a][b] = __dsub_rn(v, D[a][b]);
+        }
+      // Cholesky Aj = L L^T, then L^-1 (both lower)
+      double L[P][P], Li[P][P];
+      bool ok = true;
+#pragma unroll
+      for (int a = 0; a < P; ++a)
+#pragma unroll
+        for (int b = 0; b < P; ++b) { L[a][b] = 0.0; Li[a][b] = 0.0; }
+#pragma unroll
+      for (int b = 0; b < P; ++b) {
+        double d = Aj[b][b];
+#pragma unroll
+        for (int m = 0; m < b; ++m) d = __fma_rn(-L[b][m], L[b][m], d);
+        if (!(d > 0.0)) { ok = false; d = 1.0; }
+        const double lb = __dsqrt_rn(d);
+        L[b][b] = lb;
+        const double rl = __drcp_rn(lb);
+#pragma unroll
+        for (int a = b + 1; a < P; ++a) {
+          double v = Aj[a][b];
+#pragma unroll
+          for (int m = 0; m < b; ++m) v = __fma_rn(-L[a][m], L[b][m], v);
+          L[a][b] = __dmul_rn(v, rl);
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < P; ++b) {
+        Li[b][b] = __drcp_rn(L[b][b]);
+#pragma unroll
+        for (int a = b + 1; a < P; ++a) {
+          double v = 0.0;
+#pragma unroll
+          for (int m = b; m < a; ++m) v = __fma_rn(L[a][m], Li[m][b], v);
+          Li[a][b] = __dmul_rn(-v, __drcp_rn(L[a][a]));
+        }
+      }
+      if (!ok) atomicOr((unsigned *)fail, 1u);
+      double *ld = Ldinv + (size_t)j * PP;
+#pragma unroll
+      for (int a = 0; a < P; ++a)
+#pragma unroll
+        for (int b = 0; b < P; ++b) ld[a * P + b] = Li[a][b];
+    }
+    __syncwarp();
+  }
+}
+
+// Earlier / later neighbour counts of every node (thread per node).
+__global__ void k_ic0_count(const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
+                            const int16_t *__restrict__ color, int64_t non, int64_t *__restrict__ fcnt,
+                            int64_t *__restrict__ bcnt) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < non; j += (int64_t)gridDim.x * blockDim.x) {
+    const int16_t cj = color[j];
+    int64_t f = 0, b = 0;
+    for (int64_t q = nptr[j]; q < nptr[j + 1]; ++q) {
+      const int16_t ck = color[nadj[q]];
+      f += ck < cj;
+      b += ck > cj;
+    }
+    fcnt[j] = f;
+    bcnt[j] = b;
+  }
+}
+
+// Packed neighbour lists: for node j its earlier neighbours (forward solve)
+// and later neighbours (backward solve), each with the position of the
+// block in the node's adjacency list.
+__global__ void k_ic0_lists(const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
+                            const int16_t *__restrict__ color, int64_t non, const int64_t *__restrict__ fptr,
+                            const int64_t *__restrict__ bptr, int32_t *__restrict__ fk, int32_t *__restrict__ fsrc,
+                            int32_t *__restrict__ bk, int32_t *__restrict__ bsrc) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < non; j += (int64_t)gridDim.x * blockDim.x) {
+    const int16_t cj = color[j];
+    int64_t f = fptr[j], b = bptr[j];
+    for (int64_t q = nptr[j]; q < nptr[j + 1]; ++q) {
+      const int32_t k = nadj[q];
+      const int16_t ck = color[k];
+      if (ck < cj) {
+        fk[f] = k;
+        fsrc[f++] = (int32_t)q;
+      } else if (ck > cj) {
+        bk[b] = k;
+        bsrc[b++] = (int32_t)q;
+      }
+    }
+  }
+}
+
+// FP32 copies of the factor in packed order (blocks of L with the forward
+// and backward lists, and L_jj^-1).
+__global__ void k_ic0_pack(const double *__restrict__ src, const int32_t *__restrict__ idx, int64_t count, int pp,
+                           float *__restrict__ dst) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < count * pp;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = t / pp;
+    const int e = (int)(t - q * pp);
+    dst[t] = (float)src[(idx ? (int64_t)idx[q] : q) * pp + e];
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+struct IcColoring {
+  std::vector<int64_t> seg_nodes;  // first node of every system the colouring was made for (+ end)
+  int ncolors = 0;
+  std::vector<int64_t> ptr;      // colour c: nodes [ptr[c], ptr[c+1]) of d_nodes
+  int16_t *d_color = nullptr;    // non
+  int32_t *d_nodes = nullptr;    // non, sorted by (colour, index)
+  // packed neighbour lists: earlier (f) and later (b) neighbours of every node
+  int64_t *d_fptr = nullptr, *d_bptr = nullptr;     // non + 1
+  int32_t *d_fk = nullptr, *d_fsrc = nullptr;       // neighbour, position in the adjacency
+  int32_t *d_bk = nullptr, *d_bsrc = nullptr;
+  int64_t nf = 0, nb = 0;
+};
+
+void ic0_coloring_free(llf_ctx *ctx, llf_pattern *pat) {
+  if (!pat->ic_coloring) return;
+  IcColoring *cl = (IcColoring *)pat->ic_coloring;
+  dfree(ctx, cl->d_color);
+  dfree(ctx, cl->d_nodes);
+  dfree(ctx, cl->d_fptr); dfree(ctx, cl->d_bptr);
+  dfree(ctx, cl->d_fk); dfree(ctx, cl->d_fsrc);
+  dfree(ctx, cl->d_bk); dfree(ctx, cl->d_bsrc);
+  delete cl;
+  pat->ic_coloring = nullptr;
+}
+
+static int ic0_coloring(llf_ctx *ctx, llf_pattern *pat, const std::vector<int64_t> &seg_nodes,
+                        const int32_t *d_node_seg, IcColoring **out) {
+  if (pat->ic_coloring) {
+    if (((IcColoring *)pat->ic_coloring)->seg_nodes == seg_nodes) {
+      *out = (IcColoring *)pat->ic_coloring;
+      return LLF_OK;
+    }
+    ic0_coloring_free(ctx, pat);
+  }
+  const int64_t non = pat->mesh->non;
+  cudaStream_t s = ctx->stream;
+  int16_t *ca = nullptr, *cb = nullptr;
+  int *d_rem = nullptr;
+  int64_t *d_nbeg = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &ca, non));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &cb, non));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_rem, 1));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_nbeg, seg_nodes.size()));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_nbeg, seg_nodes.data(), sizeof(int64_t) * seg_nodes.size(),
+                                    cudaMemcpyHostToDevice, s));
+  LLF_CUDA_TRY(ctx, cudaMemsetAsync(ca, 0xff, sizeof(int16_t) * non, s));
+  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((non + 7) / 8, (int64_t)ctx->num_sms * 16));
+  int remaining = 1, rounds = 0;
+  while (remaining > 0) {
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_rem, 0, sizeof(int), s));
+    {
+      KernelScope ks(ctx, "k_jp_round");
+      k_jp_round<<<grid, IC_THREADS, 0, s>>>(pat->d_nptr, pat->d_nadj, non, d_node_seg, d_nbeg, ca, cb, d_rem,
+                                             ctx->d_status);
+    }
+    LLF_CUDA_TRY(ctx, cudaGetLastError());
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&remaining, d_rem, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    std::swap(ca, cb);
+    if (++rounds > 100000) {
+      remaining = -1;
+      break;
+    }
+  }
+  dfree(ctx, cb);
+  dfree(ctx, d_rem);
+  dfree(ctx, d_nbeg);
+  int rc = llf_check_status(ctx, "IC(0) colouring");
+  if (rc == LLF_OK && remaining < 0) rc = llf_fail(ctx, LLF_ERR_LIMIT, "IC(0) colouring did not finish");
+  if (rc != LLF_OK) {
+    dfree(ctx, ca);
+    return rc == LLF_ERR_LIMIT ? rc : llf_fail(ctx, LLF_ERR_LIMIT, "IC(0): more than 256 colours needed");
+  }
+  std::vector<int16_t> h(non);
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), ca, sizeof(int16_t) * non, cudaMemcpyDeviceToHost, s));
+  LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  IcColoring *cl = new IcColoring;
+  cl->seg_nodes = seg_nodes;
+  for (int64_t i = 0; i < non; ++i) cl->ncolors = std::max(cl->ncolors, (int)h[i] + 1);
+  cl->ptr.assign(cl->ncolors + 1, 0);
+  for (int64_t i = 0; i < non; ++i) cl->ptr[h[i] + 1]++;
+  for (int c = 0; c < cl->ncolors; ++c) cl->ptr[c + 1] += cl->ptr[c];
+  std::vector<int32_t> nodes(non);
+  std::vector<int64_t> fill(cl->ptr.begin(), cl->ptr.end() - 1);
+  for (int64_t i = 0; i < non; ++i) nodes[fill[h[i]]++] = (int32_t)i;
+  cl->d_color = ca;
+  cudaError_t e = dalloc(ctx, &cl->d_nodes, non);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(cl->d_nodes, nodes.data(), sizeof(int32_t) * non, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    dfree(ctx, cl->d_color);
+    dfree(ctx, cl->d_nodes);
+    delete cl;
+    return llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  }
+  pat->ic_coloring = cl;
+  // packed forward / backward neighbour lists
+  if (pat->nnzb >= (int64_t)1 << 31) return llf_fail(ctx, LLF_ERR_LIMIT, "IC(0): more than 2^31 node blocks");
+  int64_t *fcnt = nullptr, *bcnt = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &fcnt, non + 1));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &bcnt, non + 1));
+  LLF_CUDA_TRY(ctx, cudaMemsetAsync(fcnt + non, 0, sizeof(int64_t), s));
+  LLF_CUDA_TRY(ctx, cudaMemsetAsync(bcnt + non, 0, sizeof(int64_t), s));
+  const unsigned gt = (unsigned)std::max<int64_t>(1, std::min<int64_t>((non + 127) / 128, (int64_t)ctx->num_sms * 16));
+  k_ic0_count<<<gt, 128, 0, s>>>(pat->d_nptr, pat->d_nadj, cl->d_color, non, fcnt, bcnt);
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_fptr, non + 1));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_bptr, non + 1));
+  LLF_CUDA_TRY(ctx, exclusive_scan_i64(ctx, fcnt, cl->d_fptr, non + 1, &cl->nf));
+  LLF_CUDA_TRY(ctx, exclusive_scan_i64(ctx, bcnt, cl->d_bptr, non + 1, &cl->nb));
+  dfree(ctx, fcnt);
+  dfree(ctx, bcnt);
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_fk, cl->nf));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_fsrc, cl->nf));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_bk, cl->nb));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_bsrc, cl->nb));
+  k_ic0_lists<<<gt, 128, 0, s>>>(pat->d_nptr, pat->d_nadj, cl->d_color, non, cl->d_fptr, cl->d_bptr, cl->d_fk,
+                                 cl->d_fsrc, cl->d_bk, cl->d_bsrc);
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  *out = cl;
+  return LLF_OK;
+}
+
+template <int P>
+static int ic0_factor_t(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixed,
+                        const std::vector<int64_t> &seg_nodes, const int32_t *d_node_seg, Ic0Factor *f) {
+  const llf_pattern *pat = m->pat;
+  const int64_t non = pat->mesh->non;
+  cudaStream_t s = ctx->stream;
+  IcColoring *cl = nullptr;
+  int rc = ic0_coloring(ctx, (llf_pattern *)pat, seg_nodes, d_node_seg, &cl);
+  if (rc != LLF_OK) return rc;
+  f->ncolors = cl->ncolors;
+  f->color_ptr = cl->ptr;
+  f->d_color = cl->d_color;
+  f->d_nodes = cl->d_nodes;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &f->Lrow, (size_t)pat->nnzb * P * P));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &f->Lcol, (size_t)pat->nnzb * P * P));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &f->Ldinv, (size_t)non * P * P));
+  int *d_fail = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_fail, 1));
+  const double shifts[] = {0.0, 1e-4, 1e-3, 1e-2, 1e-1, 1.0};
+  int fail = 1;
+  for (double shift : shifts) {
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_fail, 0, sizeof(int), s));
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(f->Lrow, 0, sizeof(double) * pat->nnzb * P * P, s));
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(f->Lcol, 0, sizeof(double) * pat->nnzb * P * P, s));
+    for (int c = 0; c < cl->ncolors; ++c) {
+      const int count = (int)(cl->ptr[c + 1] - cl->ptr[c]);
+      if (count == 0) continue;
+      const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((count + 7) / 8, (int64_t)ctx->num_sms * 16));
+      KernelScope ks(ctx, "k_ic0_factor");
+      k_ic0_factor<P><<<grid, IC_THREADS, 0, s>>>(cl->d_nodes + cl->ptr[c], count, c, pat->d_nptr, pat->d_nadj,
+                                                  pat->d_diagpos, cl->d_color, m->d_nz, d_fixed, shift, f->Lrow,
+                                                  f->Lcol, f->Ldinv, d_fail);
+    }
+    LLF_CUDA_TRY(ctx, cudaGetLastError());
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&fail, d_fail, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    f->shift = shift;
+    if (!fail || (fail & 2)) break;
+  }
+  dfree(ctx, d_fail);
+  if (fail & 2) return llf_fail(ctx, LLF_ERR_STATE, "IC(0): the node pattern is not symmetric");
+  if (fail) return llf_fail(ctx, LLF_ERR_NUMERIC, "IC(0): non-positive pivot even with a diagonal shift of 1");
+  // FP32 copies in packed order for the triangular solves; the FP64 factor goes
+  f->fptr = cl->d_fptr; f->fk = cl->d_fk;
+  f->bptr = cl->d_bptr; f->bk = cl->d_bk;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &f->Lf, (size_t)cl->nf * P * P));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &f->Lb, (size_t)cl->nb * P * P));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &f->Ldf, (size_t)non * P * P));
+  const unsigned gp = (unsigned)(ctx->num_sms * 16);
+  {
+    KernelScope ks(ctx, "k_ic0_pack");
+    k_ic0_pack<<<gp, 256, 0, s>>>(f->Lrow, cl->d_fsrc, cl->nf, P * P, f->Lf);
+    k_ic0_pack<<<gp, 256, 0, s>>>(f->Lcol, cl->d_bsrc, cl->nb, P * P, f->Lb);
+    k_ic0_pack<<<gp, 256, 0, s>>>(f->Ldinv, nullptr, non, P * P, f->Ldf);
+  }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  dfree(ctx, f->Lrow);
+  dfree(ctx, f->Lcol);
+  dfree(ctx, f->Ldinv);
+  return LLF_OK;
+}
+
+int ic0_factor(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixed, const std::vector<int64_t> &seg_nodes,
+               const int32_t *d_node_seg, Ic0Factor *f) {
+  switch (m->pat->pdim) {
+    case 1: return ic0_factor_t<1>(ctx, m, d_fixed, seg_nodes, d_node_seg, f);
+    case 2: return ic0_factor_t<2>(ctx, m, d_fixed, seg_nodes, d_node_seg, f);
+    case 3: return ic0_factor_t<3>(ctx, m, d_fixed, seg_nodes, d_node_seg, f);
+  }
+  return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
+}
+
+void ic0_release(llf_ctx *ctx, Ic0Factor *f) {
+  dfree(ctx, f->Lrow);
+  dfree(ctx, f->Lcol);
+  dfree(ctx, f->Ldinv);
+  dfree(ctx, f->Lf);
+  dfree(ctx, f->Lb);
+  dfree(ctx, f->Ldf);
+}

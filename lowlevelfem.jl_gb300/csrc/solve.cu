@@ -381,13 +381,174 @@ __global__ void k_keep_fixed(const double *__restrict__ x, const uint8_t *__rest
     xc[i] = fixed[i] ? x[i] : 0.0;
 }
 
+// IC(0) application z = (L L^T)^-1 r in FP32, one colour per launch, eight
+// lanes per node over the node's packed neighbour list; nodes of converged
+// systems are skipped.  y and z share one FP32 vector (the backward sweep
+// overwrites y_i by z_i once every later z_j is known).
+constexpr int IC_G = 8;  // lanes per node
+
+template <int P>
+__global__ void __launch_bounds__(CG_THREADS)
+k_ic0_forward(const int32_t *__restrict__ nodes, int count, const int64_t *__restrict__ fptr,
+              const int32_t *__restrict__ fk, const float *__restrict__ Lf, const float *__restrict__ Ldf,
+              const int32_t *__restrict__ node_seg, const SegState *__restrict__ st,
+              const double *__restrict__ r, float *__restrict__ y) {
+  constexpr int PP = P * P;
+  const int lane = threadIdx.x & 31, gl = lane & (IC_G - 1);
+  const int per_warp = 32 / IC_G;
+  const int wg = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * per_warp;
+  const int stride = gridDim.x * (blockDim.x >> 5) * per_warp;
+  for (int base = wg; base < count; base += stride) {
+    const int idx = base + (lane / IC_G);
+    int64_t j = -1;
+    if (idx < count) {
+      j = nodes[idx];
+      if (st[node_seg[j]].done) j = -1;
+    }
+    float acc[P];
+#pragma unroll
+    for (int a = 0; a < P; ++a) acc[a] = 0.f;
+    if (j >= 0)
+      for (int64_t q = fptr[j] + gl; q < fptr[j + 1]; q += IC_G) {
+        const int64_t k = fk[q];
+        const float *L = Lf + q * PP;
+#pragma unroll
+        for (int a = 0; a < P; ++a)
+#pragma unroll
+          for (int m = 0; m < P; ++m) acc[a] = fmaf(L[a * P + m], y[P * k + m], acc[a]);
+      }
+#pragma unroll
+    for (int a = 0; a < P; ++a)
+#pragma unroll
+      for (int off = IC_G / 2; off > 0; off >>= 1) acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], off);
+    if (j >= 0 && gl == 0) {
+      const float *D = Ldf + j * PP;
+      float v[P];
+#pragma unroll
+      for (int a = 0; a < P; ++a) v[a] = (float)r[P * j + a] - acc[a];
+#pragma unroll
+      for (int a = 0; a < P; ++a) {
+        float s = 0.f;
+#pragma unroll
+        for (int m = 0; m <= a; ++m) s = fmaf(D[a * P + m], v[m], s);
+        y[P * j + a] = s;
+      }
+    }
+  }
+}
+
+template <int P>
+__global__ void __launch_bounds__(CG_THREADS)
+k_ic0_backward(const int32_t *__restrict__ nodes, int count, const int64_t *__restrict__ bptr,
+               const int32_t *__restrict__ bk, const float *__restrict__ Lb, const float *__restrict__ Ldf,
+               const int32_t *__restrict__ node_seg, const SegState *__restrict__ st, float *__restrict__ z) {
+  constexpr int PP = P * P;
+  const int lane = threadIdx.x & 31, gl = lane & (IC_G - 1);
+  const int per_warp = 32 / IC_G;
+  const int wg = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * per_warp;
+  const int stride = gridDim.x * (blockDim.x >> 5) * per_warp;
+  for (int base = wg; base < count; base += stride) {
+    const int idx = base + (lane / IC_G);
+    int64_t i = -1;
+    if (idx < count) {
+      i = nodes[idx];
+      if (st[node_seg[i]].done) i = -1;
+    }
+    float acc[P];
+#pragma unroll
+    for (int b = 0; b < P; ++b) acc[b] = 0.f;
+    if (i >= 0)
+      for (int64_t q = bptr[i] + gl; q < bptr[i + 1]; q += IC_G) {
+        const int64_t jn = bk[q];
+        const float *L = Lb + q * PP;  // L_{jn,i}
+#pragma unroll
+        for (int b = 0; b < P; ++b)
+#pragma unroll
+          for (int a = 0; a < P; ++a) acc[b] = fmaf(L[a * P + b], z[P * jn + a], acc[b]);
+      }
+#pragma unroll
+    for (int b = 0; b < P; ++b)
+#pragma unroll
+      for (int off = IC_G / 2; off > 0; off >>= 1) acc[b] += __shfl_xor_sync(0xffffffffu, acc[b], off);
+    if (i >= 0 && gl == 0) {
+      const float *D = Ldf + i * PP;
+      float v[P];
+#pragma unroll
+      for (int b = 0; b < P; ++b) v[b] = z[P * i + b] - acc[b];
+#pragma unroll
+      for (int b = 0; b < P; ++b) {
+        float s = 0.f;
+#pragma unroll
+        for (int m = b; m < P; ++m) s = fmaf(D[m * P + b], v[m], s);
+        z[P * i + b] = s;
+      }
+    }
+  }
+}
+
+// z = (double) zf and the partial z.r per chunk (after an IC(0) application).
+__global__ void __launch_bounds__(CG_THREADS)
+k_seg_zr(Seg S, const float *__restrict__ zf, const double *__restrict__ r, double *__restrict__ z,
+         double *__restrict__ part) {
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    if (S.st[S.cseg[ch]].done) continue;
+    double zr = 0.0;
+    for (int64_t i = S.cbeg[ch] + threadIdx.x; i < S.cend[ch]; i += blockDim.x) {
+      const double zi = (double)zf[i];
+      z[i] = zi;
+      zr = __fma_rn(zi, r[i], zr);
+    }
+    double s = block_sum(zr);
+    if (threadIdx.x == 0) part[ch] = s;
+  }
+}
+
+// IC(0) state of one solve: the factor and the node -> system map.
+struct IcApply {
+  const Ic0Factor *f = nullptr;
+  const int32_t *node_seg = nullptr;
+  float *zf = nullptr;  // FP32 work vector (ndof)
+};
+
+template <int P>
+void enqueue_ic0(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const IcApply &ic, const double *r, double *z,
+                 double *part, unsigned gch) {
+  const Ic0Factor &f = *ic.f;
+  cudaStream_t s = ctx->stream;
+  (void)m;
+  auto grid = [&](int count) {
+    const int64_t warps = (count + 32 / IC_G - 1) / (32 / IC_G);
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)ctx->num_sms * 16));
+  };
+  for (int c = 0; c < f.ncolors; ++c) {
+    const int count = (int)(f.color_ptr[c + 1] - f.color_ptr[c]);
+    if (!count) continue;
+    KernelScope k(ctx, "k_ic0_forward");
+    k_ic0_forward<P><<<grid(count), CG_THREADS, 0, s>>>(f.d_nodes + f.color_ptr[c], count, f.fptr, f.fk, f.Lf,
+                                                        f.Ldf, ic.node_seg, S.st, r, ic.zf);
+  }
+  for (int c = f.ncolors - 1; c >= 0; --c) {
+    const int count = (int)(f.color_ptr[c + 1] - f.color_ptr[c]);
+    if (!count) continue;
+    KernelScope k(ctx, "k_ic0_backward");
+    k_ic0_backward<P><<<grid(count), CG_THREADS, 0, s>>>(f.d_nodes + f.color_ptr[c], count, f.bptr, f.bk, f.Lb,
+                                                         f.Ldf, ic.node_seg, S.st, ic.zf);
+  }
+  { KernelScope k(ctx, "k_seg_zr"); k_seg_zr<<<gch, CG_THREADS, 0, s>>>(S, ic.zf, r, z, part); }
+}
+
 template <int P>
 void enqueue_iteration(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const double *pinv, int precond,
                        double *r, double *z, double *u, double *c, double *xw, const uint8_t *fixed,
-                       double *part, unsigned gch, unsigned gseg) {
+                       double *part, unsigned gch, unsigned gseg, const IcApply &ic) {
   const llf_pattern *pat = m->pat;
   cudaStream_t s = ctx->stream;
-  { KernelScope k(ctx, "k_seg_prec"); k_seg_prec<P><<<gch, CG_THREADS, 0, s>>>(S, pinv, precond, r, fixed, z, part); }
+  if (precond == LLF_PRECOND_IC0) {
+    enqueue_ic0<P>(ctx, S, m, ic, r, z, part, gch);
+  } else {
+    KernelScope k(ctx, "k_seg_prec");
+    k_seg_prec<P><<<gch, CG_THREADS, 0, s>>>(S, pinv, precond, r, fixed, z, part);
+  }
   { KernelScope k(ctx, "k_seg_rho"); k_seg_rho<<<gseg, CG_THREADS, 0, s>>>(S, part); }
   { KernelScope k(ctx, "k_seg_dir"); k_seg_dir<<<gch, CG_THREADS, 0, s>>>(S, z, u); }
   { KernelScope k(ctx, "k_seg_spmv");
@@ -400,7 +561,8 @@ void enqueue_iteration(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const do
 template <int P>
 int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
              const Seg &S, double *r, double *z, double *u, double *c, double *xw, double *pinv,
-             double *part, int precond, double reltol, int64_t maxiter, bool use_graph, SegState *hst);
+             double *part, int precond, double reltol, int64_t maxiter, bool use_graph, SegState *hst,
+             const IcApply &ic = IcApply());
 int pcg_outcome(llf_ctx *ctx, int nseg, const SegState *hst, int64_t *iters, double *relres);
 
 template <int P>
@@ -450,8 +612,36 @@ int pcg_segments(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d
   LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_active, 0, sizeof(int), s));
   Seg S{d_cb, d_ce, d_cs, d_sf, nch, nseg, d_st, d_active};
   std::vector<SegState> hst(nseg);
-  int rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, precond, reltol, maxiter,
-                       !ctx->profiling, hst.data());
+  // IC(0): factor of A with the fixed DoFs as identity rows, node -> system map
+  Ic0Factor icf;
+  IcApply ic;
+  int32_t *d_node_seg = nullptr;
+  int rc = LLF_OK;
+  if (precond == LLF_PRECOND_IC0) {
+    const int64_t non = pat->mesh->non;
+    std::vector<int32_t> ns(non, 0);
+    std::vector<int64_t> seg_nodes(nseg + 1);
+    for (int g = 0; g < nseg; ++g) {
+      seg_nodes[g] = seg_off[g] / P;
+      for (int64_t b = seg_off[g] / P; b < seg_off[g + 1] / P; ++b) ns[b] = g;
+    }
+    seg_nodes[nseg] = non;
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_node_seg, non));
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_node_seg, ns.data(), sizeof(int32_t) * non, cudaMemcpyHostToDevice, s));
+    rc = ic0_factor(ctx, m, d_fixed, seg_nodes, d_node_seg, &icf);
+    if (rc == LLF_OK && dalloc(ctx, &ic.zf, n) != cudaSuccess)
+      rc = llf_fail(ctx, LLF_ERR_CUDA, "pcg: out of device memory for the IC(0) work vector");
+    ic.f = &icf;
+    ic.node_seg = d_node_seg;
+  }
+  if (rc == LLF_OK)
+    rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, precond, reltol, maxiter,
+                     !ctx->profiling, hst.data(), ic);
+  if (precond == LLF_PRECOND_IC0) {
+    ic0_release(ctx, &icf);
+    dfree(ctx, d_node_seg);
+    dfree(ctx, ic.zf);
+  }
   dfree(ctx, d_cb); dfree(ctx, d_ce); dfree(ctx, d_cs); dfree(ctx, d_sf); dfree(ctx, d_active);
   dfree(ctx, d_st); dfree(ctx, r); dfree(ctx, z); dfree(ctx, u); dfree(ctx, c); dfree(ctx, xw);
   dfree(ctx, pinv); dfree(ctx, part);
@@ -467,7 +657,8 @@ int pcg_segments(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d
 template <int P>
 int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
              const Seg &S, double *r, double *z, double *u, double *c, double *xw, double *pinv,
-             double *part, int precond, double reltol, int64_t maxiter, bool use_graph, SegState *hst) {
+             double *part, int precond, double reltol, int64_t maxiter, bool use_graph, SegState *hst,
+             const IcApply &ic) {
   const llf_pattern *pat = m->pat;
   const int64_t n = pat->ndof;
   const int64_t nch = S.nchunks;
@@ -478,9 +669,11 @@ int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, 
   const unsigned gseg = (unsigned)std::max(1, std::min(nseg, ctx->num_sms * 8));
   const unsigned gv = (unsigned)(ctx->num_sms * 4);
 
-  { KernelScope k(ctx, "k_precond_setup");
+  if (precond != LLF_PRECOND_IC0) {
+    KernelScope k(ctx, "k_precond_setup");
     k_precond_setup<P><<<(unsigned)((pat->mesh->non + 127) / 128), 128, 0, s>>>(
-        m->d_nz, pat->d_colptr, pat->d_diagpos, d_fixed, pat->mesh->non, precond, pinv); }
+        m->d_nz, pat->d_colptr, pat->d_diagpos, d_fixed, pat->mesh->non, precond, pinv);
+  }
   { KernelScope k(ctx, "k_keep_fixed"); k_keep_fixed<<<gv, CG_THREADS, 0, s>>>(d_x, d_fixed, xw, n); }
   { KernelScope k(ctx, "k_spmv"); k_spmv<P><<<gv, CG_THREADS, 0, s>>>(m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, xw, c, n); }
   { KernelScope k(ctx, "k_seg_init"); k_seg_init<<<gch, CG_THREADS, 0, s>>>(S, d_b, c, d_fixed, r, xw, u, part); }
@@ -489,13 +682,15 @@ int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, 
 
   // capture a run of iterations once, replay until every segment is done
   const int per_graph = 16;
+  long long launches_per_graph = 0;
   cudaGraphExec_t exec = nullptr;
   bool graph_ok = use_graph;
   if (graph_ok) {
     cudaGraph_t graph = nullptr;
     if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       const long long saved = ctx->launches;
-      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, gch, gseg);
+      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, gch, gseg, ic);
+      launches_per_graph = ctx->launches - saved;
       ctx->launches = saved;
       if (cudaStreamEndCapture(s, &graph) != cudaSuccess ||
           cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
@@ -511,9 +706,9 @@ int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, 
   while (active > 0) {
     if (graph_ok) {
       LLF_CUDA_TRY(ctx, cudaGraphLaunch(exec, s));
-      ctx->launches += 7LL * per_graph;
+      ctx->launches += launches_per_graph;
     } else {
-      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, gch, gseg);
+      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, gch, gseg, ic);
     }
     LLF_CUDA_TRY(ctx, cudaGetLastError());
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(h_active, d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
