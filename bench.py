@@ -359,6 +359,25 @@ def run_tl(args, llf):
         ts.append(time.perf_counter() - t1)
     t4 = min(ts)
     flops4 = 2 * 375 ** 2 * 6 * 125 * m4.nel / 2  # upper-triangle pairs of B^T (D B) per point
+    # the same tangent on the tensor cores (tcgen05, split TF32): per element one
+    # GEMM 375 x 375 x (15 rows x 125 points), three split products
+    ktc = llf.tangentMatrix(P4, F4, params=prm, precision="tf32x3")
+    torch.cuda.synchronize()
+    ctx.profile(True)
+    ctx.profile_reset()
+    ts = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        ktc = llf.tangentMatrix(P4, F4, params=prm, precision="tf32x3")
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t1)
+    ctx.profile(False)
+    prof_tc = {k: v["ms"] / max(v["launches"], 1) for k, v in ctx.profile_report().items()}
+    t4tc = min(ts)
+    k64 = llf.tangentMatrix(P4, F4, params=prm).dm.copy_structural()
+    dtc = float(np.abs(ktc.dm.copy_structural() - k64).max() / np.abs(k64).max())
+    gemm4 = 2 * 375 ** 2 * (15 * 125) * m4.nel
+    tc_ms = prof_tc.get("k_tl_tangent_tc", 0.0)
     return {"metric": "TL Newton iteration time (hex8 48^3, 30% stretch, 10 steps)", "value": t_newton / max(its, 1) * 1e3,
             "unit": "ms/iteration", "n_gpus": 1, "steps": its, "warmup": 0, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic unit cube",
@@ -369,7 +388,12 @@ def run_tl(args, llf):
             "kernels_ms": {k: v["ms"] for k, v in prof.items()},
             "final_residual": u.history[-1]["residual"],
             "hex125_tangent": {"elements": m4.nel, "ms": t4 * 1e3, "gflops_fp64": flops4 / t4 / 1e9,
-                               "structural_nnz": P4.pattern().nnz}}
+                               "structural_nnz": P4.pattern().nnz,
+                               "tensor_core_form": {"ms": t4tc * 1e3, "kernels_ms": prof_tc,
+                                                    "gemm_flops": gemm4,
+                                                    "tensor_tflops_per_split": gemm4 / (tc_ms * 1e-3) / 1e12 if tc_ms else None,
+                                                    "tensor_tflops_issued": 3 * gemm4 / (tc_ms * 1e-3) / 1e12 if tc_ms else None,
+                                                    "max_rel_diff_vs_fp64": dtc}}}
 
 
 def main():

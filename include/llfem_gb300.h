@@ -67,6 +67,9 @@ extern "C" {
 /* ---- arithmetic forms ---------------------------------------------------- */
 #define LLF_FP64   0   /* plain form: every operation in IEEE FP64, fixed order */
 #define LLF_FP32Q  1   /* precision form: FP32 quadrature, FP64 accumulation    */
+#define LLF_TF32X3 2   /* tensor-core form: element contraction on the tensor
+                          cores with split TF32 operands (hi*hi + hi*lo + lo*hi),
+                          FP32 accumulation, FP64 global accumulation */
 
 /* ---- hyperelastic laws for the Total Lagrangian kernels ----------------- */
 #define LLF_LAW_CONSTANT_C     0   /* params: 36 values, 6x6 Voigt tangent, column-major */
@@ -242,6 +245,18 @@ int llf_tl_material_tangent(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
 int llf_tl_tangent(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
                    const double *Felem, int law, const double *params,
                    int nparams, llf_matrix **out);
+
+/* llf_tl_tangent with a choice of arithmetic: LLF_FP64 (the call above) or
+ * LLF_TF32X3 — the element matrices as one dense GEMM per element,
+ * [B; G]^T diag(w D, w S (x) I) [B; G] with 15 rows per point, on the
+ * tensor cores (tcgen05, split TF32 products, FP32 accumulation in tensor
+ * memory), then summed in FP64.  Meant for high-order elements (order >= 3),
+ * where the contraction is dense.  The tile operands are formed in FP32 and
+ * summed in FP32, so values agree with the FP64 form to about 1e-5 of the
+ * largest entry for a well-conditioned F (less as det F approaches 0). */
+int llf_tl_tangent_form(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
+                        const double *Felem, int law, const double *params,
+                        int nparams, int form, llf_matrix **out);
 
 /* Geometric (initial-stress) stiffness K_geo[a i, b i] = sum grad Na^T S
  * grad Nb detJ0 w, identity component block — initialStressMatrix,

@@ -72,6 +72,7 @@ SIGNATURES = {
     "llf_assemble_heat": (i32, [vp, vp, vp, i32, P_dbl, i32, dbl, i32, PP]),
     "llf_tl_material_tangent": (i32, [vp, vp, vp, P_dbl, i32, P_dbl, i32, PP]),
     "llf_tl_tangent": (i32, [vp, vp, vp, P_dbl, i32, P_dbl, i32, PP]),
+    "llf_tl_tangent_form": (i32, [vp, vp, vp, P_dbl, i32, P_dbl, i32, i32, PP]),
     "llf_tl_initial_stress": (i32, [vp, vp, vp, P_dbl, P_dbl, i32, P_dbl, i32, PP]),
     "llf_tl_internal_force": (i32, [vp, vp, P_dbl, P_dbl, i32, P_dbl, i32, P_dbl]),
     "llf_grad_elementwise": (i32, [vp, vp, P_dbl, i32, P_dbl]),

@@ -632,17 +632,21 @@ def materialTangentMatrix(problem: Problem, F, C=None, energy=None, params=None)
     return SystemMatrix(_lib.DeviceMatrix(ctx, h, pat), problem)
 
 
-def tangentMatrix(problem: Problem, F, energy="NeoHookeCompressible", params=None) -> SystemMatrix:
+def tangentMatrix(problem: Problem, F, energy="NeoHookeCompressible", params=None, precision="fp64") -> SystemMatrix:
     """Consistent Newton tangent K_mat + K_geo from F in one pass (the exact
     derivative of internalForceVector for the same F); the reference's Newton
-    loops sum materialTangentMatrix(F) and initialStressMatrix(C)."""
+    loops sum materialTangentMatrix(F) and initialStressMatrix(C).
+    precision="tf32x3": the element contraction on the tensor cores (split
+    TF32 products, FP32 accumulation; for high-order elements)."""
     law, prm = _law(energy, params)
     Fa = _tensor_array(problem, F)
     ctx = problem._ctx
     h = _lib.C.c_void_p()
     dm, pat = problem.device_mesh(), problem.pattern()
-    ctx.check(_lib.lib().llf_tl_tangent(ctx.h, dm.h, pat.h, _lib.ptr(Fa, _lib.C.c_double), law,
-                                        _lib.ptr(prm, _lib.C.c_double), len(prm), _lib.C.byref(h)), "tangentMatrix")
+    form = {"fp64": 0, "tf32x3": 2}[precision]
+    ctx.check(_lib.lib().llf_tl_tangent_form(ctx.h, dm.h, pat.h, _lib.ptr(Fa, _lib.C.c_double), law,
+                                             _lib.ptr(prm, _lib.C.c_double), len(prm), form, _lib.C.byref(h)),
+              "tangentMatrix")
     return SystemMatrix(_lib.DeviceMatrix(ctx, h, pat), problem)
 
 

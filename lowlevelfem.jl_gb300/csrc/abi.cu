@@ -54,6 +54,7 @@ int llf_check_status(llf_ctx *ctx, const char *what) {
   if (st & ST_NONFINITE) return llf_fail(ctx, LLF_ERR_NUMERIC, w + ": NaN or Inf in an input array");
   if (st & ST_PATTERN) return llf_fail(ctx, LLF_ERR_STATE, w + ": pattern entry without a contributing element (mesh and pattern disagree)");
   if (st & ST_BREAKDOWN) return llf_fail(ctx, LLF_ERR_NUMERIC, w + ": breakdown");
+  if (st & ST_TIMEOUT) return llf_fail(ctx, LLF_ERR_CUDA, w + ": a bounded wait on the tensor cores timed out");
   return llf_fail(ctx, LLF_ERR_CUDA, w + ": unknown device status");
 }
 
@@ -611,6 +612,25 @@ int llf_tl_tangent(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double 
   int rc;
   if ((rc = new_matrix(ctx, pat, out, &m))) { dfree(ctx, dF); return rc; }
   rc = tl_tangent_impl(ctx, mesh, pat, dF, law, params, nparams, m);
+  dfree(ctx, dF);
+  return finish_matrix(ctx, rc, m, out);
+}
+
+int llf_tl_tangent_form(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *Felem, int law,
+                        const double *params, int nparams, int form, llf_matrix **out) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (form == LLF_FP64) return llf_tl_tangent(ctx, mesh, pat, Felem, law, params, nparams, out);
+  if (form != LLF_TF32X3) return llf_fail(ctx, LLF_ERR_ARG, "llf_tl_tangent_form: form must be LLF_FP64 or LLF_TF32X3");
+  if (!mesh || !pat || !Felem || pat->mesh != mesh || mesh->dim != 3 || pat->pdim != 3)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_tl_tangent_form: needs a 3D mesh, its pdim 3 pattern and F");
+  size_t nF = (size_t)9 * mesh->npe * mesh->nel;
+  double *dF = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &dF, nF));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(dF, Felem, sizeof(double) * nF, cudaMemcpyHostToDevice, ctx->stream));
+  llf_matrix *m;
+  int rc;
+  if ((rc = new_matrix(ctx, pat, out, &m))) { dfree(ctx, dF); return rc; }
+  rc = tl_tangent_tc_impl(ctx, mesh, pat, dF, law, params, nparams, m);
   dfree(ctx, dF);
   return finish_matrix(ctx, rc, m, out);
 }

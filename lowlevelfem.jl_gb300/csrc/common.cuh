@@ -18,6 +18,7 @@ enum : unsigned {
   ST_NONFINITE = 1u << 3,     // NaN/Inf in an input array
   ST_PATTERN = 1u << 4,       // an element pair found no pattern slot
   ST_BREAKDOWN = 1u << 5,     // CG breakdown (u.Au <= 0 or not finite)
+  ST_TIMEOUT = 1u << 6,       // a bounded wait on the tensor cores gave up
 };
 
 struct DevBuf {
@@ -256,6 +257,8 @@ int tl_material_tangent_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
                              int nparams, llf_matrix *m);
 int tl_tangent_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *d_F, int law,
                     const double *params, int nparams, llf_matrix *m);
+int tl_tangent_tc_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *d_F, int law,
+                       const double *params, int nparams, llf_matrix *m);
 int tl_initial_stress_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
                            const double *d_S, const double *d_C, int law,
                            const double *params, int nparams, llf_matrix *m);

@@ -390,6 +390,285 @@ __global__ void __launch_bounds__(TL_THREADS) k_tl_force(TLArgs A) {
   }
 }
 
+// ------------------------------------------------------------ tensor-core form
+// Consistent tangent on the 5th-generation tensor cores (tcgen05), for
+// high-order elements where the element contraction is dense.  Per point q
+// the tangent is [B_q; G_q]^T diag(w D_q, w S_q (x) I) [B_q; G_q], with B_q
+// the 6 x 3npe matrix B(F) and G_q the 9 x 3npe displacement-gradient
+// operator, so the whole element matrix is one GEMM over K = 15 rows per
+// point.  One CTA computes a 128 x 192 tile of one element matrix:
+//   - the point records (w, J^-1, F, D, S, FP64 as in the FP64 form) come
+//     from k_tl_records;
+//   - per k-block of 2 points (2 x 15 rows, padded to 32) the threads build
+//     the A (= [B; G] rows of the tile) and B (= weighted [D B; S G]) tiles
+//     in shared memory in the K-major core-matrix layout (8 rows x 16 bytes),
+//     each split into TF32 hi and lo parts;
+//   - one thread issues tcgen05.mma kind::tf32 (M 128, N 192, K 8) for the
+//     three split products hi*hi + hi*lo + lo*hi into an FP32 accumulator in
+//     tensor memory and commits to the stage's mbarrier (two stages, the
+//     next k-block is built while the tensor cores run);
+//   - the epilogue reads the accumulator with tcgen05.ld and writes the
+//     element matrix (FP32) in the gather's layout.
+// Every mbarrier wait is bounded (2 s): a timeout sets ST_TIMEOUT, the CTA
+// skips its epilogue and releases its tensor memory.
+constexpr int TC_M = 128, TC_N = 192, TC_KB = 32, TC_PTS = 2, TC_THREADS = 128, TC_PREC = 63;
+constexpr int TC_TILE_A = TC_M * TC_KB, TC_TILE_B = TC_N * TC_KB;  // floats
+constexpr size_t TC_STAGE = (size_t)2 * (TC_TILE_A + TC_TILE_B);   // floats per stage (hi + lo)
+
+struct TcArgs {
+  const double *recs;  // nel * nip * QD point records
+  const double *dN;    // nip * npe * 3
+  const int32_t *emat;
+  int64_t nel;
+  int npe, nip, n, nstrip, nhalf;
+  float *Kf;           // nel * npe * cs
+  int64_t cs;
+  unsigned *status;
+};
+
+__device__ __forceinline__ uint32_t tc_saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor, K-major, no swizzle: core matrices of
+// 8 rows x 16 bytes, LBO = distance of K-adjacent core matrices (128 B),
+// SBO = distance of 8-row groups (TC_KB / 4 core matrices of 128 B).
+__device__ __forceinline__ uint64_t tc_desc(const float *p) {
+  const uint64_t lbo = 128, sbo = (TC_KB / 4) * 128;
+  return (uint64_t)((tc_saddr(p) & 0x3FFFF) >> 4) | ((lbo >> 4) << 16) | ((sbo >> 4) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ int tc_off(int row, int k) {
+  return ((row >> 3) * (TC_KB / 4) + (k >> 2)) * 32 + (row & 7) * 4 + (k & 3);
+}
+
+__device__ __forceinline__ float tc_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void tc_put(float *hi, float *lo, int row, int k, float v) {
+  const float h = tc_tf32(v);
+  hi[tc_off(row, k)] = h;
+  lo[tc_off(row, k)] = v - h;
+}
+
+__device__ __forceinline__ uint64_t tc_now() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait on an mbarrier phase (2 s); false on timeout.
+__device__ __forceinline__ bool tc_wait(uint64_t *bar, unsigned parity) {
+  const uint64_t t0 = tc_now();
+  for (;;) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok) : "r"(tc_saddr(bar)), "r"(parity) : "memory");
+    if (ok) return true;
+    if (tc_now() - t0 > 2000000000ull) return false;
+  }
+}
+
+// Point records for the tensor-core form (one CTA per element).
+__global__ void __launch_bounds__(TL_THREADS) k_tl_records(TLArgs A, double *recs) {
+  extern __shared__ double sm[];
+  const int npe = A.npe, nip = A.nip;
+  double *sX = sm, *sT = sX + npe * 3;
+  for (int64_t e = blockIdx.x; e < A.nel; e += gridDim.x) {
+    if (A.emat && A.emat[e] < 0) continue;
+    for (int t = threadIdx.x; t < npe * 3; t += blockDim.x)
+      sX[t] = A.xyz[(size_t)A.conn[e * npe + t / 3] * 3 + t % 3];
+    for (int t = threadIdx.x; t < npe * 9; t += blockDim.x) sT[t] = A.T[(size_t)e * npe * 9 + t];
+    __syncthreads();
+    for (int q = threadIdx.x; q < nip; q += blockDim.x)
+      tl_point(A, TL_KTAN, q, sX, sT, recs + ((size_t)e * nip + q) * QD);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
+  extern __shared__ __align__(1024) float tsm[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int per_e = A.nstrip * A.nhalf;
+  const int64_t e = blockIdx.x / per_e;
+  const int rr = (int)(blockIdx.x - e * per_e);
+  const int row0 = (rr / A.nhalf) * TC_M, col0 = (rr % A.nhalf) * TC_N;
+  if (e >= A.nel || (A.emat && A.emat[e] < 0)) return;  // uniform across the CTA
+  const int npe = A.npe, nip = A.nip, n = A.n;
+  float *pts = tsm + 2 * TC_STAGE;                        // TC_PTS * TC_PREC
+  float *sg = pts + TC_PTS * 64;                          // TC_PTS * npe * 3
+  uint64_t *bar = (uint64_t *)(sg + ((TC_PTS * npe * 3 + 1) & ~1));
+  uint32_t *tslot = (uint32_t *)(bar + 2);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_saddr(tslot)), "r"(256u)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_saddr(bar)), "r"(1u) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_saddr(bar + 1)), "r"(1u) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
+                         ((uint32_t)(TC_M >> 4) << 24);
+  const int nkb = (nip + TC_PTS - 1) / TC_PTS;
+  bool ok = true;
+  for (int kb = 0; kb < nkb && ok; ++kb) {
+    const int st = kb & 1;
+    float *Ahi = tsm + st * TC_STAGE, *Alo = Ahi + TC_TILE_A, *Bhi = Alo + TC_TILE_A, *Blo = Bhi + TC_TILE_B;
+    if (kb >= 2) {
+      const bool w = tc_wait(bar + st, (unsigned)((kb - 2) >> 1) & 1u);
+      if (!__syncthreads_and(w)) {
+        ok = false;
+        break;
+      }
+    }
+    const int q0 = kb * TC_PTS;
+    // point data: F[9], w*D[36], w*S[9], J^-1[9] (FP32)
+    for (int t = tid; t < TC_PTS * TC_PREC; t += TC_THREADS) {
+      const int ql = t / TC_PREC, f = t - ql * TC_PREC, q = q0 + ql;
+      float v = 0.f;
+      if (q < nip) {
+        const double *rec = A.recs + ((size_t)e * nip + q) * QD;
+        if (f < 9) v = (float)rec[10 + f];
+        else if (f < 45) v = (float)(rec[0] * rec[19 + (f - 9)]);
+        else if (f < 54) v = (float)(rec[0] * rec[55 + (f - 45)]);
+        else v = (float)rec[1 + (f - 54)];
+      }
+      pts[ql * 64 + f] = v;
+    }
+    __syncthreads();
+    // physical gradients of every node at both points
+    for (int t = tid; t < TC_PTS * npe * 3; t += TC_THREADS) {
+      const int ql = t / (npe * 3), a = (t / 3) % npe, I = t % 3, q = q0 + ql;
+      float g = 0.f;
+      if (q < nip) {
+        const double *d = A.dN + ((size_t)q * npe + a) * 3;
+        const float *iv = pts + ql * 64 + 54;
+#pragma unroll
+        for (int J = 0; J < 3; ++J) g = fmaf(iv[3 * J + I], (float)d[J], g);
+      }
+      sg[t] = g;
+    }
+    __syncthreads();
+    // A tile: rows of the strip, K = (point, 16 rows: B(F) 6, grad 9, pad 1)
+    for (int t = tid; t < TC_M * TC_PTS; t += TC_THREADS) {
+      const int i = t / TC_PTS, ql = t - (t / TC_PTS) * TC_PTS, gi = row0 + i, q = q0 + ql;
+      float v[16];
+#pragma unroll
+      for (int r = 0; r < 16; ++r) v[r] = 0.f;
+      if (gi < n && q < nip) {
+        const int a = gi / 3, ci = gi - 3 * (gi / 3);
+        const float *F = pts + ql * 64, *g = sg + (ql * npe + a) * 3;
+        const float v1 = F[3 * ci], v2 = F[3 * ci + 1], v3 = F[3 * ci + 2];
+        v[0] = v1 * g[0];
+        v[1] = v2 * g[1];
+        v[2] = v3 * g[2];
+        v[3] = fmaf(v2, g[2], v3 * g[1]);
+        v[4] = fmaf(v1, g[2], v3 * g[0]);
+        v[5] = fmaf(v1, g[1], v2 * g[0]);
+#pragma unroll
+        for (int I = 0; I < 3; ++I) v[6 + 3 * I + ci] = g[I];
+      }
+#pragma unroll
+      for (int r = 0; r < 16; ++r) tc_put(Ahi, Alo, i, ql * 16 + r, v[r]);
+    }
+    // B tile: columns of the half, weighted by w D and w S
+    for (int t = tid; t < TC_N * TC_PTS; t += TC_THREADS) {
+      const int j = t / TC_PTS, ql = t - (t / TC_PTS) * TC_PTS, gj = col0 + j, q = q0 + ql;
+      float v[16];
+#pragma unroll
+      for (int r = 0; r < 16; ++r) v[r] = 0.f;
+      if (gj < n && q < nip) {
+        const int b = gj / 3, cj = gj - 3 * (gj / 3);
+        const float *P = pts + ql * 64, *g = sg + (ql * npe + b) * 3;
+        const float v1 = P[3 * cj], v2 = P[3 * cj + 1], v3 = P[3 * cj + 2];
+        float Bv[6];
+        Bv[0] = v1 * g[0];
+        Bv[1] = v2 * g[1];
+        Bv[2] = v3 * g[2];
+        Bv[3] = fmaf(v2, g[2], v3 * g[1]);
+        Bv[4] = fmaf(v1, g[2], v3 * g[0]);
+        Bv[5] = fmaf(v1, g[1], v2 * g[0]);
+        const float *wD = P + 9, *wS = P + 45;
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+          float s = 0.f;
+#pragma unroll
+          for (int r2 = 0; r2 < 6; ++r2) s = fmaf(wD[r * 6 + r2], Bv[r2], s);
+          v[r] = s;
+        }
+#pragma unroll
+        for (int I = 0; I < 3; ++I) {
+          float s = 0.f;
+#pragma unroll
+          for (int J = 0; J < 3; ++J) s = fmaf(wS[3 * I + J], g[J], s);
+          v[6 + 3 * I + cj] = s;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < 16; ++r) tc_put(Bhi, Blo, j, ql * 16 + r, v[r]);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int kk = 0; kk < TC_KB / 8; ++kk)
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+          const float *Ax = (p == 2 ? Alo : Ahi) + kk * 64, *Bx = (p == 1 ? Blo : Bhi) + kk * 64;
+          const uint32_t acc = (kb | kk | p) != 0;
+          asm volatile("{\n\t.reg .pred pa;\n\tsetp.ne.b32 pa, %4, 0;\n\t"
+                       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, pa;\n\t}"
+                       ::"r"(tmem), "l"(tc_desc(Ax)), "l"(tc_desc(Bx)), "r"(idesc), "r"(acc)
+                       : "memory");
+        }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       tc_saddr(bar + st))
+                   : "memory");
+    }
+  }
+  // the last commit covers every earlier MMA of this thread
+  const bool fin = ok ? tc_wait(bar + ((nkb - 1) & 1), (unsigned)((nkb - 1) >> 1) & 1u) : false;
+  ok = __syncthreads_and(fin);
+  if (!ok && tid == 0) atomicOr(A.status, ST_TIMEOUT);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    const int gi = row0 + warp * 32 + lane;
+    const int a = gi / 3, ci = gi - 3 * (gi / 3);
+    for (int c0 = 0; c0 < TC_N; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t addr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                   : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                     "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                     "=r"(r[15])
+                   : "r"(addr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (gi < n)
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int gj = col0 + c0 + u;
+          if (gj < n) {
+            const int b = gj / 3, cj = gj - 3 * (gj / 3);
+            A.Kf[((size_t)e * npe + b) * A.cs + a * 9 + ci * 3 + cj] = __uint_as_float(r[u]);
+          }
+        }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256u) : "memory");
+}
+
 size_t tl_smem(int npe, int nip, bool matrix) {
   size_t d = (size_t)npe * 3 + (size_t)npe * 9 + (size_t)nip * QD;
   if (matrix) d += (size_t)npe * 3 + (size_t)npe * 18 * 2;
@@ -487,6 +766,73 @@ int tl_material_tangent_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, con
 int tl_tangent_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *d_F, int law,
                     const double *params, int nparams, llf_matrix *m) {
   return tl_matrix(ctx, mesh, pat, TL_KTAN, d_F, law, params, nparams, m);
+}
+
+// Tensor-core form of the consistent tangent (k_tl_records + k_tl_tangent_tc,
+// then the FP32 element matrices summed in FP64 by the gather).
+int tl_tangent_tc_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *d_F, int law,
+                       const double *params, int nparams, llf_matrix *m) {
+  if (mesh->dim != 3 || pat->pdim != 3)
+    return llf_fail(ctx, LLF_ERR_ARG, "Total Lagrangian operators need dim == 3 and pdim == 3");
+  TLArgs a{};
+  int rc = fill_args(ctx, mesh, d_F, law, params, nparams, a);
+  if (rc) return rc;
+  const int npe = mesh->npe, nip = mesh->nip, n = 3 * npe;
+  cudaStream_t s = ctx->stream;
+  double *recs = nullptr;
+  float *Kf = nullptr;
+  int64_t *cnt = nullptr;
+  const int64_t cs = kf_colstride(npe, 9, (int)sizeof(float));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &recs, (size_t)mesh->nel * nip * QD));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &Kf, (size_t)mesh->nel * npe * cs));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &cnt, pat->ndof + 1));
+  LLF_CUDA_TRY(ctx, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (pat->ndof + 1), s));
+  {
+    const size_t smem = sizeof(double) * (size_t)npe * 12;
+    const unsigned grid = (unsigned)std::min<int64_t>(std::max<int64_t>(mesh->nel, 1), (int64_t)ctx->num_sms * 8);
+    KernelScope ks(ctx, "k_tl_records");
+    k_tl_records<<<grid, TL_THREADS, smem, s>>>(a, recs);
+    LLF_CUDA_TRY(ctx, cudaGetLastError());
+  }
+  TcArgs t{};
+  t.recs = recs;
+  t.dN = mesh->d_dN;
+  t.emat = mesh->d_emat;
+  t.nel = mesh->nel;
+  t.npe = npe;
+  t.nip = nip;
+  t.n = n;
+  t.nstrip = (n + TC_M - 1) / TC_M;
+  t.nhalf = (n + TC_N - 1) / TC_N;
+  t.Kf = Kf;
+  t.cs = cs;
+  t.status = ctx->d_status;
+  const size_t smem = sizeof(float) * (2 * TC_STAGE + TC_PTS * 64 + (((size_t)TC_PTS * npe * 3 + 1) & ~(size_t)1)) +
+                      2 * sizeof(uint64_t) + 16;
+  if (smem > 220 * 1024) rc = llf_fail(ctx, LLF_ERR_LIMIT, "tensor-core tangent: element too large");
+  const int64_t ctas = mesh->nel * t.nstrip * t.nhalf;
+  if (rc == LLF_OK && ctas >= ((int64_t)1 << 31)) rc = llf_fail(ctx, LLF_ERR_LIMIT, "tensor-core tangent: too many tiles");
+  if (rc == LLF_OK && ctas > 0) {
+    cudaError_t e = cudaFuncSetAttribute(k_tl_tangent_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+    if (rc == LLF_OK) {
+      KernelScope ks(ctx, "k_tl_tangent_tc");
+      k_tl_tangent_tc<<<(unsigned)ctas, TC_THREADS, smem, s>>>(t);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+    }
+  }
+  if (rc == LLF_OK) {
+    cudaError_t e = dalloc(ctx, &m->d_nz, pat->nnz);
+    rc = (e == cudaSuccess) ? gather_full32(ctx, pat, Kf, cs, true, m->d_nz, cnt)
+                            : llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  }
+  dfree(ctx, recs);
+  dfree(ctx, Kf);
+  if (rc == LLF_OK) rc = llf_check_status(ctx, "tangent (tensor-core form)");
+  if (rc == LLF_OK) rc = matrix_finalize(ctx, m, cnt);
+  dfree(ctx, cnt);
+  return rc;
 }
 
 int tl_initial_stress_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *d_S,

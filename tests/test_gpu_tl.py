@@ -159,3 +159,34 @@ def test_newton_stretch_converges(llf):
     uy = u.a[1::3, 0]
     top = np.abs(m.xyz[:, 1] - 1) < 1e-12
     assert np.ptp(uy[top]) < 1e-9
+
+
+TC_CASES = [("hex27", 2, 2, False), ("hex64", 2, 3, False), ("hex125", 1, 4, False), ("tet20", 1, 3, True)]
+
+
+def _smooth_F(llf, m, p):
+    """F = I + grad u of a smooth, moderate deformation (stretch, shear and a
+    bending mode): well-conditioned, as in a Newton step of a physical load."""
+    x, y, z = m.xyz[:, 0], m.xyz[:, 1], m.xyz[:, 2]
+    u = np.stack([0.10 * x + 0.03 * y * z, -0.02 * y + 0.05 * np.sin(np.pi * x), 0.04 * z * x], axis=1)
+    return llf.grad(llf.VectorField(u.reshape(-1, 1), p), add_identity=True)
+
+
+@pytest.mark.parametrize("case", TC_CASES, ids=[c[0] for c in TC_CASES])
+def test_tensor_core_tangent_within_tf32x3_tolerance(llf, case):
+    """Tensor-core form (tcgen05, split TF32 products, FP32 accumulation):
+    every structural value within 5e-5 of the largest FP64 value for a
+    well-conditioned deformation (tile operands formed in FP32, FP32 sums over
+    15 rows x nip points in tensor memory)."""
+    _, n, order, simplex = case
+    m = llf.structured_box_mesh(n=n, order=order, simplex=simplex)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    F = _smooth_F(llf, m, p)
+    prm = {"mu": 1.0, "lambda": 10.0}
+    K64 = llf.tangentMatrix(p, F, energy="NeoHookeCompressible", params=prm)
+    Ktc = llf.tangentMatrix(p, F, energy="NeoHookeCompressible", params=prm, precision="tf32x3")
+    a, b = K64.dm.copy_structural(), Ktc.dm.copy_structural()
+    scale = np.abs(a).max()
+    err = np.abs(a - b).max() / scale
+    assert err <= 5e-5, err
+    assert err > 0.0  # the tensor-core path really ran (TF32 splits are not bit-exact)
