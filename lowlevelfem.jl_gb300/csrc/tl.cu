@@ -397,8 +397,9 @@ __global__ void __launch_bounds__(TL_THREADS) k_tl_force(TLArgs A) {
 // the 6 x 3npe matrix B(F) and G_q the 9 x 3npe displacement-gradient
 // operator, so the whole element matrix is one GEMM over K = 15 rows per
 // point.  One CTA computes a 128 x 192 tile of one element matrix:
-//   - the point records (w, J^-1, F, D, S, FP64 as in the FP64 form) come
-//     from k_tl_records;
+//   - the point data (F, w D, w S, physical gradients; FP64 as in the FP64
+//     form, rounded to FP32) come from k_tl_points_tc, two points per
+//     k-block, fetched by cp.async.bulk one k-block ahead;
 //   - per k-block of 2 points (2 x 15 rows, padded to 32) the threads build
 //     the A (= [B; G] rows of the tile) and B (= weighted [D B; S G]) tiles
 //     in shared memory in the K-major core-matrix layout (8 rows x 16 bytes),
@@ -411,13 +412,12 @@ __global__ void __launch_bounds__(TL_THREADS) k_tl_force(TLArgs A) {
 //     element matrix (FP32) in the gather's layout.
 // Every mbarrier wait is bounded (2 s): a timeout sets ST_TIMEOUT, the CTA
 // skips its epilogue and releases its tensor memory.
-constexpr int TC_M = 128, TC_N = 192, TC_KB = 32, TC_PTS = 2, TC_THREADS = 128, TC_PREC = 63;
+constexpr int TC_M = 128, TC_N = 192, TC_KB = 32, TC_PTS = 2, TC_THREADS = 256;
 constexpr int TC_TILE_A = TC_M * TC_KB, TC_TILE_B = TC_N * TC_KB;  // floats
 constexpr size_t TC_STAGE = (size_t)2 * (TC_TILE_A + TC_TILE_B);   // floats per stage (hi + lo)
 
 struct TcArgs {
-  const double *recs;  // nel * nip * QD point records
-  const double *dN;    // nip * npe * 3
+  const float *pd;     // nel * nip * tc_pstride(npe) packed point data (k_tl_points_tc)
   const int32_t *emat;
   int64_t nel;
   int npe, nip, n, nstrip, nhalf;
@@ -471,23 +471,55 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, unsigned parity) {
   }
 }
 
-// Point records for the tensor-core form (one CTA per element).
-__global__ void __launch_bounds__(TL_THREADS) k_tl_records(TLArgs A, double *recs) {
+// Packed FP32 point data of the tensor-core form, one CTA per element: for
+// every point q a run of tc_pstride(npe) floats (16-byte multiple)
+//   [0,9) F | [9,45) w D | [45,54) w S | [54,56) 0 | [56, 56+3 npe) grad N_a
+// computed in FP64 (the FP64 form's point record and gradients) and rounded.
+__host__ __device__ __forceinline__ int tc_pstride(int npe) { return (56 + 3 * npe + 3) & ~3; }
+
+__global__ void __launch_bounds__(TL_THREADS) k_tl_points_tc(TLArgs A, float *pd) {
   extern __shared__ double sm[];
-  const int npe = A.npe, nip = A.nip;
-  double *sX = sm, *sT = sX + npe * 3;
+  const int npe = A.npe, nip = A.nip, ps = tc_pstride(npe);
+  double *sX = sm, *sT = sX + npe * 3, *rec = sT + npe * 9;  // rec: nip * QD
   for (int64_t e = blockIdx.x; e < A.nel; e += gridDim.x) {
     if (A.emat && A.emat[e] < 0) continue;
     for (int t = threadIdx.x; t < npe * 3; t += blockDim.x)
       sX[t] = A.xyz[(size_t)A.conn[e * npe + t / 3] * 3 + t % 3];
     for (int t = threadIdx.x; t < npe * 9; t += blockDim.x) sT[t] = A.T[(size_t)e * npe * 9 + t];
     __syncthreads();
-    for (int q = threadIdx.x; q < nip; q += blockDim.x)
-      tl_point(A, TL_KTAN, q, sX, sT, recs + ((size_t)e * nip + q) * QD);
+    for (int q = threadIdx.x; q < nip; q += blockDim.x) tl_point(A, TL_KTAN, q, sX, sT, rec + (size_t)q * QD);
+    __syncthreads();
+    float *out = pd + (size_t)e * nip * ps;
+    for (int t = threadIdx.x; t < nip * ps; t += blockDim.x) {
+      const int q = t / ps, f = t - q * ps;
+      const double *r = rec + (size_t)q * QD;
+      double v = 0.0;
+      if (f < 9) v = r[10 + f];
+      else if (f < 45) v = __dmul_rn(r[0], r[19 + (f - 9)]);
+      else if (f < 54) v = __dmul_rn(r[0], r[55 + (f - 45)]);
+      else if (f >= 56 && f < 56 + 3 * npe) {
+        const int a = (f - 56) / 3, I = (f - 56) % 3;
+        const double *d = A.dN + ((size_t)q * npe + a) * 3;
+        double g = 0.0;
+        for (int J = 0; J < 3; ++J) g = __fma_rn(r[1 + 3 * J + I], d[J], g);
+        v = g;
+      }
+      out[t] = (float)v;
+    }
     __syncthreads();
   }
 }
 
+__device__ __forceinline__ void tc_bulk(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc_saddr(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(tc_saddr(dst)), "l"(src), "r"(bytes), "r"(tc_saddr(bar))
+               : "memory");
+}
+
+// Shared memory: 2 stages x (A hi, A lo, B hi, B lo) | 2 point-data buffers
+// (TC_PTS points each, fetched by cp.async.bulk one k-block ahead) |
+// mbarriers: MMA completion x2, point data x2 | tensor-memory address.
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
   extern __shared__ __align__(1024) float tsm[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -496,20 +528,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
   const int rr = (int)(blockIdx.x - e * per_e);
   const int row0 = (rr / A.nhalf) * TC_M, col0 = (rr % A.nhalf) * TC_N;
   if (e >= A.nel || (A.emat && A.emat[e] < 0)) return;  // uniform across the CTA
-  const int npe = A.npe, nip = A.nip, n = A.n;
-  float *pts = tsm + 2 * TC_STAGE;                        // TC_PTS * TC_PREC
-  float *sg = pts + TC_PTS * 64;                          // TC_PTS * npe * 3
-  uint64_t *bar = (uint64_t *)(sg + ((TC_PTS * npe * 3 + 1) & ~1));
-  uint32_t *tslot = (uint32_t *)(bar + 2);
+  const int npe = A.npe, nip = A.nip, n = A.n, ps = tc_pstride(npe);
+  float *pbuf = tsm + 2 * TC_STAGE;                      // 2 x TC_PTS * ps
+  uint64_t *bar = (uint64_t *)(pbuf + 2 * TC_PTS * ps);  // [0,2) MMA, [2,4) point data
+  uint32_t *tslot = (uint32_t *)(bar + 4);
+  const float *pd = A.pd + (size_t)e * nip * ps;
+  const int nkb = (nip + TC_PTS - 1) / TC_PTS;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_saddr(tslot)), "r"(256u)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_saddr(bar)), "r"(1u) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_saddr(bar + 1)), "r"(1u) : "memory");
+    for (int b = 0; b < 4; ++b)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_saddr(bar + b)), "r"(1u) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    const int np = nip < TC_PTS ? nip : TC_PTS;
+    tc_bulk(pbuf, pd, (unsigned)(np * ps * sizeof(float)), bar + 2);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -517,46 +552,31 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
   const uint32_t tmem = *tslot;
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
                          ((uint32_t)(TC_M >> 4) << 24);
-  const int nkb = (nip + TC_PTS - 1) / TC_PTS;
   bool ok = true;
-  for (int kb = 0; kb < nkb && ok; ++kb) {
+  int fetched = 1;  // point-data copies issued (k-blocks 0 .. fetched-1)
+  for (int kb = 0; kb < nkb; ++kb) {
     const int st = kb & 1;
     float *Ahi = tsm + st * TC_STAGE, *Alo = Ahi + TC_TILE_A, *Bhi = Alo + TC_TILE_A, *Blo = Bhi + TC_TILE_B;
-    if (kb >= 2) {
-      const bool w = tc_wait(bar + st, (unsigned)((kb - 2) >> 1) & 1u);
-      if (!__syncthreads_and(w)) {
-        ok = false;
-        break;
+    // tiles of this stage free (MMAs of k-block kb - 2 done) and point data of kb landed
+    bool w = kb < 2 || tc_wait(bar + st, (unsigned)((kb - 2) >> 1) & 1u);
+    w = w && tc_wait(bar + 2 + st, (unsigned)(kb >> 1) & 1u);
+    if (!__syncthreads_and(w)) {
+      ok = false;
+      break;
+    }
+    // prefetch the next k-block's point data into the other buffer (its last
+    // reader, the tile build of kb - 1, finished before the barrier above)
+    if (kb + 1 < nkb) {
+      if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const int q1 = (kb + 1) * TC_PTS, np = (nip - q1) < TC_PTS ? (nip - q1) : TC_PTS;
+        tc_bulk(pbuf + ((kb + 1) & 1) * TC_PTS * ps, pd + (size_t)q1 * ps, (unsigned)(np * ps * sizeof(float)),
+                bar + 2 + ((kb + 1) & 1));
       }
+      ++fetched;
     }
     const int q0 = kb * TC_PTS;
-    // point data: F[9], w*D[36], w*S[9], J^-1[9] (FP32)
-    for (int t = tid; t < TC_PTS * TC_PREC; t += TC_THREADS) {
-      const int ql = t / TC_PREC, f = t - ql * TC_PREC, q = q0 + ql;
-      float v = 0.f;
-      if (q < nip) {
-        const double *rec = A.recs + ((size_t)e * nip + q) * QD;
-        if (f < 9) v = (float)rec[10 + f];
-        else if (f < 45) v = (float)(rec[0] * rec[19 + (f - 9)]);
-        else if (f < 54) v = (float)(rec[0] * rec[55 + (f - 45)]);
-        else v = (float)rec[1 + (f - 54)];
-      }
-      pts[ql * 64 + f] = v;
-    }
-    __syncthreads();
-    // physical gradients of every node at both points
-    for (int t = tid; t < TC_PTS * npe * 3; t += TC_THREADS) {
-      const int ql = t / (npe * 3), a = (t / 3) % npe, I = t % 3, q = q0 + ql;
-      float g = 0.f;
-      if (q < nip) {
-        const double *d = A.dN + ((size_t)q * npe + a) * 3;
-        const float *iv = pts + ql * 64 + 54;
-#pragma unroll
-        for (int J = 0; J < 3; ++J) g = fmaf(iv[3 * J + I], (float)d[J], g);
-      }
-      sg[t] = g;
-    }
-    __syncthreads();
+    const float *pb = pbuf + st * TC_PTS * ps;
     // A tile: rows of the strip, K = (point, 16 rows: B(F) 6, grad 9, pad 1)
     for (int t = tid; t < TC_M * TC_PTS; t += TC_THREADS) {
       const int i = t / TC_PTS, ql = t - (t / TC_PTS) * TC_PTS, gi = row0 + i, q = q0 + ql;
@@ -565,8 +585,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
       for (int r = 0; r < 16; ++r) v[r] = 0.f;
       if (gi < n && q < nip) {
         const int a = gi / 3, ci = gi - 3 * (gi / 3);
-        const float *F = pts + ql * 64, *g = sg + (ql * npe + a) * 3;
-        const float v1 = F[3 * ci], v2 = F[3 * ci + 1], v3 = F[3 * ci + 2];
+        const float *P = pb + ql * ps, *g = P + 56 + 3 * a;
+        const float v1 = P[3 * ci], v2 = P[3 * ci + 1], v3 = P[3 * ci + 2];
         v[0] = v1 * g[0];
         v[1] = v2 * g[1];
         v[2] = v3 * g[2];
@@ -574,7 +594,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
         v[4] = fmaf(v1, g[2], v3 * g[0]);
         v[5] = fmaf(v1, g[1], v2 * g[0]);
 #pragma unroll
-        for (int I = 0; I < 3; ++I) v[6 + 3 * I + ci] = g[I];
+        for (int I = 0; I < 3; ++I)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) v[6 + 3 * I + c] = (c == ci) ? g[I] : 0.f;
       }
 #pragma unroll
       for (int r = 0; r < 16; ++r) tc_put(Ahi, Alo, i, ql * 16 + r, v[r]);
@@ -587,7 +609,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
       for (int r = 0; r < 16; ++r) v[r] = 0.f;
       if (gj < n && q < nip) {
         const int b = gj / 3, cj = gj - 3 * (gj / 3);
-        const float *P = pts + ql * 64, *g = sg + (ql * npe + b) * 3;
+        const float *P = pb + ql * ps, *g = P + 56 + 3 * b;
         const float v1 = P[3 * cj], v2 = P[3 * cj + 1], v3 = P[3 * cj + 2];
         float Bv[6];
         Bv[0] = v1 * g[0];
@@ -599,17 +621,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
         const float *wD = P + 9, *wS = P + 45;
 #pragma unroll
         for (int r = 0; r < 6; ++r) {
-          float s = 0.f;
+          float sacc = 0.f;
 #pragma unroll
-          for (int r2 = 0; r2 < 6; ++r2) s = fmaf(wD[r * 6 + r2], Bv[r2], s);
-          v[r] = s;
+          for (int r2 = 0; r2 < 6; ++r2) sacc = fmaf(wD[r * 6 + r2], Bv[r2], sacc);
+          v[r] = sacc;
         }
 #pragma unroll
         for (int I = 0; I < 3; ++I) {
-          float s = 0.f;
+          float sacc = 0.f;
 #pragma unroll
-          for (int J = 0; J < 3; ++J) s = fmaf(wS[3 * I + J], g[J], s);
-          v[6 + 3 * I + cj] = s;
+          for (int J = 0; J < 3; ++J) sacc = fmaf(wS[3 * I + J], g[J], sacc);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) v[6 + 3 * I + c] = (c == cj) ? sacc : 0.f;
         }
       }
 #pragma unroll
@@ -641,11 +664,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
   if (!ok && tid == 0) atomicOr(A.status, ST_TIMEOUT);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
-    const int gi = row0 + warp * 32 + lane;
+    // warps w and w + 4 read the same 32 TMEM lanes, different column halves
+    const int lanes = (warp & 3) * 32, cbeg = (warp >> 2) * (TC_N / 2);
+    const int gi = row0 + lanes + lane;
     const int a = gi / 3, ci = gi - 3 * (gi / 3);
-    for (int c0 = 0; c0 < TC_N; c0 += 16) {
+    for (int c0 = cbeg; c0 < cbeg + TC_N / 2; c0 += 16) {
       uint32_t r[16];
-      const uint32_t addr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      const uint32_t addr = tmem + ((uint32_t)lanes << 16) + (uint32_t)c0;
       asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
@@ -662,6 +687,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
           }
         }
     }
+  } else {
+    // drain this CTA's point-data copies (bounded) before it exits: copy k of
+    // buffer k & 1 is that buffer's (k >> 1)-th phase
+    for (int k = 0; k < fetched; ++k) tc_wait(bar + 2 + (k & 1), (unsigned)(k >> 1) & 1u);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -768,7 +797,7 @@ int tl_tangent_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double
   return tl_matrix(ctx, mesh, pat, TL_KTAN, d_F, law, params, nparams, m);
 }
 
-// Tensor-core form of the consistent tangent (k_tl_records + k_tl_tangent_tc,
+// Tensor-core form of the consistent tangent (k_tl_points_tc + k_tl_tangent_tc,
 // then the FP32 element matrices summed in FP64 by the gather).
 int tl_tangent_tc_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *d_F, int law,
                        const double *params, int nparams, llf_matrix *m) {
@@ -779,24 +808,32 @@ int tl_tangent_tc_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const dou
   if (rc) return rc;
   const int npe = mesh->npe, nip = mesh->nip, n = 3 * npe;
   cudaStream_t s = ctx->stream;
-  double *recs = nullptr;
+  float *pd = nullptr;
   float *Kf = nullptr;
   int64_t *cnt = nullptr;
+  const int ps = tc_pstride(npe);
   const int64_t cs = kf_colstride(npe, 9, (int)sizeof(float));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &recs, (size_t)mesh->nel * nip * QD));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &pd, (size_t)mesh->nel * nip * ps));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &Kf, (size_t)mesh->nel * npe * cs));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &cnt, pat->ndof + 1));
   LLF_CUDA_TRY(ctx, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (pat->ndof + 1), s));
   {
-    const size_t smem = sizeof(double) * (size_t)npe * 12;
-    const unsigned grid = (unsigned)std::min<int64_t>(std::max<int64_t>(mesh->nel, 1), (int64_t)ctx->num_sms * 8);
-    KernelScope ks(ctx, "k_tl_records");
-    k_tl_records<<<grid, TL_THREADS, smem, s>>>(a, recs);
-    LLF_CUDA_TRY(ctx, cudaGetLastError());
+    const size_t smem = sizeof(double) * ((size_t)npe * 12 + (size_t)nip * QD);
+    if (smem > 200 * 1024) rc = llf_fail(ctx, LLF_ERR_LIMIT, "tensor-core tangent: element too large");
+    if (rc == LLF_OK && smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k_tl_points_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (rc == LLF_OK) {
+      const unsigned grid = (unsigned)std::min<int64_t>(std::max<int64_t>(mesh->nel, 1), (int64_t)ctx->num_sms * 4);
+      KernelScope ks(ctx, "k_tl_points_tc");
+      k_tl_points_tc<<<grid, TL_THREADS, smem, s>>>(a, pd);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+    }
   }
   TcArgs t{};
-  t.recs = recs;
-  t.dN = mesh->d_dN;
+  t.pd = pd;
   t.emat = mesh->d_emat;
   t.nel = mesh->nel;
   t.npe = npe;
@@ -807,9 +844,8 @@ int tl_tangent_tc_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const dou
   t.Kf = Kf;
   t.cs = cs;
   t.status = ctx->d_status;
-  const size_t smem = sizeof(float) * (2 * TC_STAGE + TC_PTS * 64 + (((size_t)TC_PTS * npe * 3 + 1) & ~(size_t)1)) +
-                      2 * sizeof(uint64_t) + 16;
-  if (smem > 220 * 1024) rc = llf_fail(ctx, LLF_ERR_LIMIT, "tensor-core tangent: element too large");
+  const size_t smem = sizeof(float) * (2 * TC_STAGE + 2 * (size_t)TC_PTS * ps) + 4 * sizeof(uint64_t) + 16;
+  if (rc == LLF_OK && smem > 220 * 1024) rc = llf_fail(ctx, LLF_ERR_LIMIT, "tensor-core tangent: element too large");
   const int64_t ctas = mesh->nel * t.nstrip * t.nhalf;
   if (rc == LLF_OK && ctas >= ((int64_t)1 << 31)) rc = llf_fail(ctx, LLF_ERR_LIMIT, "tensor-core tangent: too many tiles");
   if (rc == LLF_OK && ctas > 0) {
@@ -827,7 +863,7 @@ int tl_tangent_tc_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const dou
     rc = (e == cudaSuccess) ? gather_full32(ctx, pat, Kf, cs, true, m->d_nz, cnt)
                             : llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
   }
-  dfree(ctx, recs);
+  dfree(ctx, pd);
   dfree(ctx, Kf);
   if (rc == LLF_OK) rc = llf_check_status(ctx, "tangent (tensor-core form)");
   if (rc == LLF_OK) rc = matrix_finalize(ctx, m, cnt);
