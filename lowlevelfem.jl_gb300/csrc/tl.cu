@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(TL_THREADS) k_tl_force(TLArgs A) {
 //     element matrix (FP32) in the gather's layout.
 // Every mbarrier wait is bounded (2 s): a timeout sets ST_TIMEOUT, the CTA
 // skips its epilogue and releases its tensor memory.
-constexpr int TC_M = 128, TC_N = 192, TC_KB = 32, TC_PTS = 2, TC_THREADS = 256;
+constexpr int TC_M = 128, TC_N = 192, TC_KB = 32, TC_PTS = 2, TC_THREADS = 512;
 constexpr int TC_TILE_A = TC_M * TC_KB, TC_TILE_B = TC_N * TC_KB;  // floats
 constexpr size_t TC_STAGE = (size_t)2 * (TC_TILE_A + TC_TILE_B);   // floats per stage (hi + lo)
 
@@ -446,10 +446,24 @@ __device__ __forceinline__ float tc_tf32(float x) {
   return __uint_as_float(r);
 }
 
-__device__ __forceinline__ void tc_put(float *hi, float *lo, int row, int k, float v) {
-  const float h = tc_tf32(v);
-  hi[tc_off(row, k)] = h;
-  lo[tc_off(row, k)] = v - h;
+// Row `row`, columns k0 .. k0+15 (k0 a multiple of 4) of a tile: TF32 hi and
+// lo parts, one 16-byte store per 4 columns (a core-matrix row).
+__device__ __forceinline__ void tc_put16(float *hi, float *lo, int row, int k0, const float *v) {
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float4 h, l;
+    h.x = tc_tf32(v[4 * c]);
+    h.y = tc_tf32(v[4 * c + 1]);
+    h.z = tc_tf32(v[4 * c + 2]);
+    h.w = tc_tf32(v[4 * c + 3]);
+    l.x = v[4 * c] - h.x;
+    l.y = v[4 * c + 1] - h.y;
+    l.z = v[4 * c + 2] - h.z;
+    l.w = v[4 * c + 3] - h.w;
+    const int o = tc_off(row, k0 + 4 * c);
+    *reinterpret_cast<float4 *>(hi + o) = h;
+    *reinterpret_cast<float4 *>(lo + o) = l;
+  }
 }
 
 __device__ __forceinline__ uint64_t tc_now() {
@@ -519,6 +533,7 @@ __device__ __forceinline__ void tc_bulk(void *dst, const void *src, unsigned byt
 
 // Shared memory: 2 stages x (A hi, A lo, B hi, B lo) | 2 point-data buffers
 // (TC_PTS points each, fetched by cp.async.bulk one k-block ahead) |
+// (TC_N / (TC_THREADS / 128) must be a multiple of 16)
 // mbarriers: MMA completion x2, point data x2 | tensor-memory address.
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
   extern __shared__ __align__(1024) float tsm[];
@@ -579,7 +594,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
     const float *pb = pbuf + st * TC_PTS * ps;
     // A tile: rows of the strip, K = (point, 16 rows: B(F) 6, grad 9, pad 1)
     for (int t = tid; t < TC_M * TC_PTS; t += TC_THREADS) {
-      const int i = t / TC_PTS, ql = t - (t / TC_PTS) * TC_PTS, gi = row0 + i, q = q0 + ql;
+      const int ql = t / TC_M, i = t - ql * TC_M, gi = row0 + i, q = q0 + ql;
       float v[16];
 #pragma unroll
       for (int r = 0; r < 16; ++r) v[r] = 0.f;
@@ -598,12 +613,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) v[6 + 3 * I + c] = (c == ci) ? g[I] : 0.f;
       }
-#pragma unroll
-      for (int r = 0; r < 16; ++r) tc_put(Ahi, Alo, i, ql * 16 + r, v[r]);
+      tc_put16(Ahi, Alo, i, ql * 16, v);
     }
     // B tile: columns of the half, weighted by w D and w S
     for (int t = tid; t < TC_N * TC_PTS; t += TC_THREADS) {
-      const int j = t / TC_PTS, ql = t - (t / TC_PTS) * TC_PTS, gj = col0 + j, q = q0 + ql;
+      const int ql = t / TC_N, j = t - ql * TC_N, gj = col0 + j, q = q0 + ql;
       float v[16];
 #pragma unroll
       for (int r = 0; r < 16; ++r) v[r] = 0.f;
@@ -635,8 +649,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
           for (int c = 0; c < 3; ++c) v[6 + 3 * I + c] = (c == cj) ? sacc : 0.f;
         }
       }
-#pragma unroll
-      for (int r = 0; r < 16; ++r) tc_put(Bhi, Blo, j, ql * 16 + r, v[r]);
+      tc_put16(Bhi, Blo, j, ql * 16, v);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
@@ -664,11 +677,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
   if (!ok && tid == 0) atomicOr(A.status, ST_TIMEOUT);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
-    // warps w and w + 4 read the same 32 TMEM lanes, different column halves
-    const int lanes = (warp & 3) * 32, cbeg = (warp >> 2) * (TC_N / 2);
+    // warp w reads TMEM lanes 32 (w % 4) .. +31 (the lanes its position in a
+    // warpgroup may access) and one of TC_THREADS / 128 column ranges
+    constexpr int NCR = TC_THREADS / 128, CW = TC_N / NCR;
+    const int lanes = (warp & 3) * 32, cbeg = (warp >> 2) * CW;
     const int gi = row0 + lanes + lane;
     const int a = gi / 3, ci = gi - 3 * (gi / 3);
-    for (int c0 = cbeg; c0 < cbeg + TC_N / 2; c0 += 16) {
+    for (int c0 = cbeg; c0 < cbeg + CW; c0 += 16) {
       uint32_t r[16];
       const uint32_t addr = tmem + ((uint32_t)lanes << 16) + (uint32_t)c0;
       asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
