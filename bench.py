@@ -56,8 +56,9 @@ def parse():
     ap.add_argument("--workers", type=int, default=4, help="serving: server workers")
     ap.add_argument("--no-peak", action="store_true", help="skip the DGEMM FP64 reference rate")
     ap.add_argument("--no-other-form", action="store_true", help="skip the second arithmetic form")
-    ap.add_argument("--precond", default=None, choices=["jacobi", "bjacobi", "ic0"],
-                    help="batched / tl: CG preconditioner (default: ic0 for batched, bjacobi for tl)")
+    ap.add_argument("--precond", default=None, choices=["jacobi", "bjacobi", "ic0", "auto"],
+                    help="CG preconditioner (defaults: ic0 for batched, bjacobi for tl, auto for serving: "
+                         "IC(0) from 50,000 nodes, Jacobi below)")
     return ap.parse_args()
 
 
@@ -267,9 +268,17 @@ def run_serving(args, llf):
     reqs = [wl.heat_request(rng) for _ in range(args.requests)]
     arrivals = np.cumsum(rng.exponential(1.0 / 200.0, size=len(reqs)))
 
+    def precond(m):
+        mode = args.precond or "auto"
+        if mode == "auto":  # IC(0) where the CG dominates, Jacobi where launches do
+            return llf._lib.PRECOND_IC0 if m.non >= 50000 else llf._lib.PRECOND_JACOBI
+        return {"jacobi": llf._lib.PRECOND_JACOBI, "bjacobi": llf._lib.PRECOND_BJACOBI,
+                "ic0": llf._lib.PRECOND_IC0}[mode]
+
     def submit(srv, r):
         m, k, fixed, x0 = r
-        return srv.submit_heat(m.dim, m.xyz, m.conn, m.family, m.order, k, x0, fixed, reltol=1e-10)
+        return srv.submit_heat(m.dim, m.xyz, m.conn, m.family, m.order, k, x0, fixed, reltol=1e-10,
+                               precond=precond(m))
 
     # one at a time (a single worker, next request after the previous result)
     warm = [wl.heat_request(np.random.default_rng(1), dofs_max=5e3) for _ in range(2 * args.workers)]
@@ -313,7 +322,8 @@ def run_serving(args, llf):
             "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic heat requests (seeded)",
             "config": {"workload": f"serving-heat-{len(reqs)}", "requests": len(reqs), "workers": args.workers,
-                       "dofs_median": float(np.median(dofs)), "dofs_max": int(max(dofs)), "reltol": 1e-10},
+                       "dofs_median": float(np.median(dofs)), "dofs_max": int(max(dofs)), "reltol": 1e-10,
+                       "precond": args.precond or "auto"},
             "latency_s": {"p50": _pct(lat, 50), "p99": _pct(lat, 99), "max": max(lat)},
             "one_at_a_time_solves_per_s": len(reqs) / t_single,
             "cg_iterations_median": float(np.median(iters)), "peak_device_bytes": stats["peak_bytes"]}
