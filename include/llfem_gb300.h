@@ -226,6 +226,21 @@ int llf_assemble_heat(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
                       int ptype, const double *k, int nmat, double thickness,
                       int form, llf_matrix **out);
 
+/* Boundary support matrix C = sum H^T diag(k) H Ja w over the elements of
+ * `bmesh` (dimension dim-1, node tags of the pattern's volume mesh), Ja as in
+ * llf_load_vector — elasticSupportMatrix, src/linear.jl:2859-3005 (k = kx,
+ * ky, kz), and heatConvectionMatrix, src/heat.jl:562-567 (pdim 1, k = h).
+ * Exactly one of k_elem[pdim*nel_b] (one constant per boundary element) and
+ * k_elem_nodal[pdim*npe*nel_b] (values at every element's nodes,
+ * interpolated at the points) is non-NULL.  Several support groups go in one
+ * call as one element list in group order, which sums them in the order of
+ * the reference's single sparse() call.  The matrix lives on the volume
+ * pattern, so it adds to the stiffness or conduction matrix with
+ * llf_matrix_axpby. */
+int llf_assemble_support(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bmesh,
+                         const double *k_elem, const double *k_elem_nodal,
+                         double thickness, llf_matrix **out);
+
 /* Total Lagrangian material tangent K_mat = sum B(F)^T C B(F) detJ0 w —
  * materialTangentMatrix, src/nonlinear.jl:2083-2268.  Felem[9*npe*nel] holds
  * the elementwise nodal deformation gradient, column-major 3x3 per element

@@ -13,9 +13,11 @@ from .mesh import (Mesh, Group, structured_rect_mesh, structured_box_mesh, read_
                    current_mesh, set_current, node_lattice, concat_meshes, LINE, TRI, QUAD, TET, HEX)
 from .api import (Material, material, elastic_constants, Problem, Field, SystemMatrix, VectorField,
                   ScalarField, TensorField, BoundaryCondition, LoadCondition, displacementConstraint,
-                  temperatureConstraint, load, heatFlux, constrainedDoFs, allDoFs, freeDoFs,
-                  applyBoundaryConditions_, loadVector, stiffnessMatrix, massMatrix,
-                  heatConductionMatrix, solveDisplacement, solveTemperature, solveField, solveFieldBatched, grad,
+                  temperatureConstraint, load, heatFlux, elasticSupport, heatConvection, constrainedDoFs,
+                  allDoFs, freeDoFs, applyBoundaryConditions_, loadVector, stiffnessMatrix, massMatrix,
+                  heatConductionMatrix, heatCapacityMatrix, elasticSupportMatrix, heatConvectionMatrix,
+                  heatConvectionVector, applyElasticSupport_, applyHeatConvection_, solveDisplacement,
+                  solveTemperature, solveField, solveFieldBatched, grad,
                   deformationGradient, materialTangentMatrix, initialStressMatrix, tangentMatrix, solveDeformation,
                   internalForceVector)
 

@@ -177,11 +177,18 @@ class Problem:
             self._dpat[p] = _lib.DevicePattern(self.device_mesh(), p)
         return self._dpat[p]
 
-    def boundary_mesh(self, name: str) -> _lib.DeviceMesh:
-        if name not in self._bmesh:
-            g = self.mesh.group(name)
-            self._bmesh[name] = _lib.DeviceMesh(self._ctx, self.dim, self.mesh.xyz, g.conn, g.family, g.order)
-        return self._bmesh[name]
+    def boundary_mesh(self, name) -> _lib.DeviceMesh:
+        """Device mesh of a boundary group, or of several groups of one element
+        type (a tuple of names) as one element list in the given order."""
+        key = name if isinstance(name, str) else tuple(name)
+        if key not in self._bmesh:
+            gs = [self.mesh.group(n) for n in ((key,) if isinstance(key, str) else key)]
+            g = gs[0]
+            if any(x.family != g.family or x.order != g.order for x in gs):
+                raise ValueError("boundary_mesh: the groups hold different element types")
+            conn = np.concatenate([x.conn for x in gs], axis=0)
+            self._bmesh[key] = _lib.DeviceMesh(self._ctx, self.dim, self.mesh.xyz, conn, g.family, g.order)
+        return self._bmesh[key]
 
 
 Field = Problem
@@ -313,6 +320,21 @@ def massMatrix(problem: Problem, lumped=True, precision="fp64") -> SystemMatrix:
     return SystemMatrix(_lib.DeviceMatrix(ctx, h, pat), problem)
 
 
+def heatCapacityMatrix(problem: Problem, elements=(), lumped=False, precision="fp64") -> SystemMatrix:
+    """C = c ρ Σ HᵀH detJ w (b = 1 in 2D and 3D), consistent or row-sum lumped
+    (src/heat.jl:257-376): the mass kernels on the scalar pattern with c ρ."""
+    if problem.type not in ("HeatConduction", "PlaneHeatConduction"):
+        raise ValueError(f"heatCapacityMatrix: dimension is {problem.dim}, problem type is {problem.type}.")
+    ctx = problem._ctx
+    crho = np.array([m.c * m.rho for m in problem.material])
+    h = _lib.C.c_void_p()
+    dm, pat = problem.device_mesh(), problem.pattern()
+    ctx.check(_lib.lib().llf_assemble_mass(ctx.h, dm.h, pat.h, problem.ptype, _lib.ptr(crho, _lib.C.c_double),
+                                           len(crho), problem.thickness, int(bool(lumped)), _form(precision),
+                                           _lib.C.byref(h)), "heatCapacityMatrix")
+    return SystemMatrix(_lib.DeviceMatrix(ctx, h, pat), problem)
+
+
 def heatConductionMatrix(problem: Problem, elements=(), precision="fp64") -> SystemMatrix:
     """K_T = Σ ∇Nᵀ∇N k b detJ w (src/heat.jl:28-137)."""
     if problem.type not in ("HeatConduction", "PlaneHeatConduction"):
@@ -357,6 +379,21 @@ def load(name, fx=None, fy=None, fz=None):
 
 def heatFlux(name, qn=None):
     return LoadCondition(name, qn=qn)
+
+
+def elasticSupport(name, kx=None, ky=None, kz=None):
+    """elasticSupport(name; kx, ky, kz) (src/general.jl:4281-4285)."""
+    if kx is None and ky is None and kz is None:
+        raise ValueError("elasticSupport: at least one of kx, ky, kz, p must be specified.")
+    return BoundaryCondition(name, kx=kx, ky=ky, kz=kz)
+
+
+def heatConvection(name, h=None, Tinf=None):
+    """heatConvection(name; h, T∞) (src/general.jl:4384-4388); the ambient
+    temperature is stored under the reference's key "T∞"."""
+    if h is None or Tinf is None:
+        raise ValueError("heatSource: h and T∞ must be specified.")
+    return BoundaryCondition(name, h=h, **{"T∞": Tinf})
 
 
 def _component(problem: Problem, key: str):
@@ -463,6 +500,106 @@ def loadVector(problem: Problem, loads) -> VectorField | ScalarField:
     return _field_for(problem, f)
 
 
+def _support_matrix(problem: Problem, conds, keys, what) -> SystemMatrix:
+    """Σ over the conditions' boundary groups of Hᵀ diag(k) H Ja w on the
+    volume pattern.  Consecutive conditions on groups of one element type go
+    to the device as one element list in condition order, which sums every
+    entry in the order of the reference's single sparse() call; runs of
+    different element types are added afterwards.  Constant values are used
+    as they are; when a run holds a function value, every group of the run is
+    sampled at its nodes and interpolated at the points."""
+    ctx, pat = problem._ctx, problem.pattern()
+    conds = list(conds)
+    if not conds:
+        raise ValueError(f"{what}: no conditions given")
+    runs = []
+    for bc in conds:
+        g = problem.mesh.group(bc.phName)
+        if g.dim != problem.dim - 1:
+            raise NotImplementedError(f"{what}: only boundary groups of dimension {problem.dim - 1} are "
+                                      f"accelerated (group {bc.phName!r} has dimension {g.dim})")
+        if runs and (runs[-1][-1][1].family, runs[-1][-1][1].order) == (g.family, g.order):
+            runs[-1].append((bc, g))
+        else:
+            runs.append([(bc, g)])
+    total = None
+    for run in runs:
+        vals = [[bc.values.get(k, 0.0) for k in keys] for bc, _ in run]
+        nodal = any(not np.isscalar(v) for vs in vals for v in vs)
+        parts = []
+        for (bc, g), vs in zip(run, vals):
+            if nodal:
+                kn = np.zeros((problem.non, len(keys)))
+                for c, v in enumerate(vs):
+                    kn[g.nodes - 1, c] = _values_at(problem, g.nodes, v)
+                parts.append(kn[g.conn - 1])
+            else:
+                parts.append(np.tile(np.array([float(v) for v in vs]), (g.conn.shape[0], 1)))
+        karr = np.ascontiguousarray(np.concatenate(parts, axis=0), dtype=np.float64)
+        bm = problem.boundary_mesh(tuple(bc.phName for bc, _ in run))
+        h = _lib.C.c_void_p()
+        ke, ken = (None, karr) if nodal else (karr, None)
+        ctx.check(_lib.lib().llf_assemble_support(ctx.h, pat.h, bm.h, _lib.ptr(ke, _lib.C.c_double),
+                                                  _lib.ptr(ken, _lib.C.c_double),
+                                                  problem.thickness if problem.dim == 2 else 1.0,
+                                                  _lib.C.byref(h)), what)
+        C = SystemMatrix(_lib.DeviceMatrix(ctx, h, pat), problem)
+        total = C if total is None else total + C
+    return total
+
+
+def elasticSupportMatrix(problem: Problem, elSupports) -> SystemMatrix:
+    """C = Σ Hᵀ diag(kx, ky, kz) H Ja w over the supports' boundary groups
+    (src/linear.jl:2859-3005): elastic (Winkler) supports, added to K."""
+    if not isinstance(elSupports, (list, tuple)):
+        raise TypeError("elasticSupportMatrix: elastic supports are not arranged in a vector. Put them in [...]")
+    return _support_matrix(problem, elSupports, ["kx", "ky", "kz"][: problem.pdim], "elasticSupportMatrix")
+
+
+def heatConvectionMatrix(problem: Problem, heatConvection) -> SystemMatrix:
+    """C = Σ Hᵀ h H Ja w over the convection groups (src/heat.jl:562-567)."""
+    if not isinstance(heatConvection, (list, tuple)):
+        raise TypeError("heatConvection: heat convections are not arranged in a vector. Put them in [...]")
+    if problem.pdim != 1:
+        raise ValueError("heatConvectionMatrix: the problem must be a heat conduction problem")
+    return _support_matrix(problem, heatConvection, ["h"], "heatConvectionMatrix")
+
+
+def heatConvectionVector(problem: Problem, heatConvection) -> ScalarField:
+    """q = Σ Hᵀ (h T∞) Ja w over the convection groups (src/heat.jl:667-673,
+    loadVector's h/T∞ branch src/linear.jl:3281-3285)."""
+    if not isinstance(heatConvection, (list, tuple)):
+        raise TypeError("heatConvectionVector: heat convections are not arranged in a vector. Put them in [...]")
+    loads = []
+    for bc in heatConvection:
+        h, T = bc.values.get("h"), bc.values.get("T∞")
+        if callable(h):
+            raise ValueError("heatConvectionVector: h cannot be a function.")
+        if h is None or T is None:
+            raise ValueError("heatConvectionVector: h and T∞ must be specified.")
+        qn = (lambda *x, T=T, h=h: float(T(*x)) * h) if callable(T) else float(T) * float(h)
+        loads.append(LoadCondition(bc.phName, qn=qn))
+    return loadVector(problem, loads)
+
+
+def applyElasticSupport_(K: SystemMatrix, elSupports) -> SystemMatrix:
+    """applyElasticSupport!(K, elSupports) (src/linear.jl:3648-3660): K += C.
+    Returns the updated matrix (the device matrix is replaced in place)."""
+    C = elasticSupportMatrix(K.model, list(elSupports))
+    K.dm, K._csc = K.dm.axpby(1.0, 1.0, C.dm), None
+    return K
+
+
+def applyHeatConvection_(K: SystemMatrix, q, heatConvection):
+    """applyHeatConvection!(K, q, heatConv) (src/heat.jl:969-981): K += C and
+    q += the convection vector."""
+    problem = K.model
+    C = heatConvectionMatrix(problem, list(heatConvection))
+    K.dm, K._csc = K.dm.axpby(1.0, 1.0, C.dm), None
+    q.a += heatConvectionVector(problem, list(heatConvection)).a
+    return None
+
+
 # --------------------------------------------------------------------------
 # Solves
 # --------------------------------------------------------------------------
@@ -509,6 +646,8 @@ def solveDisplacement(problem_or_K, f=None, load=(), support=(), elasticSupport=
     else:
         problem = problem_or_K
         K = stiffnessMatrix(problem)
+        if elasticSupport:
+            applyElasticSupport_(K, elasticSupport)
         f = loadVector(problem, list(load))
     pr = K.model
     maxiter = pr.non * pr.dim if maxiter is None else maxiter
@@ -517,16 +656,16 @@ def solveDisplacement(problem_or_K, f=None, load=(), support=(), elasticSupport=
 
 def solveTemperature(problem_or_K, q=None, heatFlux=(), temperatureConstraint=(), heatConvection=(),
                      iterative=False, reltol=SQRT_EPS, maxiter=None, preconditioner="identity"):
-    """solveTemperature(problem; heatFlux, temperatureConstraint) or
+    """solveTemperature(problem; heatFlux, temperatureConstraint, heatConvection) or
     solveTemperature(K, q; temperatureConstraint) (src/heat.jl:1020-1084)."""
-    if heatConvection:
-        raise NotImplementedError("heatConvection is outside the accelerated path")
     if isinstance(problem_or_K, SystemMatrix):
         K = problem_or_K
     else:
         problem = problem_or_K
         K = heatConductionMatrix(problem)
         q = loadVector(problem, list(heatFlux))
+        if heatConvection:
+            applyHeatConvection_(K, q, heatConvection)
     pr = K.model
     maxiter = pr.non * pr.dim if maxiter is None else maxiter
     return _solve(K, q, list(temperatureConstraint), iterative, reltol, maxiter, preconditioner)

@@ -563,6 +563,32 @@ int llf_assemble_mass(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int ptype,
   return finish_matrix(ctx, rc, m, out);
 }
 
+int llf_assemble_support(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bmesh, const double *k_elem,
+                         const double *k_elem_nodal, double thickness, llf_matrix **out) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!pat || !bmesh || !out || (!k_elem == !k_elem_nodal))
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_assemble_support: give exactly one of k_elem and k_elem_nodal");
+  if (bmesh->non != pat->mesh->non || bmesh->dim != pat->mesh->dim - 1)
+    return llf_fail(ctx, LLF_ERR_ARG,
+                    "llf_assemble_support: the boundary mesh must have dimension dim-1 on the volume mesh's nodes");
+  if (pat->conn_version != pat->mesh->conn_version)
+    return llf_fail(ctx, LLF_ERR_STATE, "the mesh connectivity changed after the pattern was built; rebuild it");
+  const size_t n = (size_t)std::max<int64_t>(bmesh->nel, 1) * pat->pdim * (k_elem_nodal ? bmesh->npe : 1);
+  double *dk = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &dk, n));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(dk, k_elem ? k_elem : k_elem_nodal,
+                                    sizeof(double) * (size_t)bmesh->nel * pat->pdim * (k_elem_nodal ? bmesh->npe : 1),
+                                    cudaMemcpyHostToDevice, ctx->stream));
+  llf_matrix *m;
+  int rc = new_matrix(ctx, pat, out, &m);
+  if (rc == LLF_OK) {
+    rc = support_impl(ctx, pat, bmesh, k_elem ? dk : nullptr, k_elem_nodal ? dk : nullptr, thickness, m);
+    rc = finish_matrix(ctx, rc, m, out);
+  }
+  dfree(ctx, dk);
+  return rc;
+}
+
 int llf_assemble_heat(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int ptype,
                       const double *k, int nmat, double thickness, int form,
                       llf_matrix **out) {

@@ -629,12 +629,14 @@ int run_elem(llf_ctx *ctx, ElemArgs a) {
   return rc;
 }
 
+// Gather over explicit node -> element lists and element-to-column map (the
+// pattern's own, or those of another element set on the same nodes).
 template <int P, bool BV, class T>
-int run_colgather(llf_ctx *ctx, llf_pattern *pat, const T *Kf, int64_t cs, double *nz, int64_t *cnt) {
+int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,
+                  int npe, const T *Kf, int64_t cs, double *nz, int64_t *cnt) {
   if (pat->conn_version != pat->mesh->conn_version)
     return llf_fail(ctx, LLF_ERR_STATE, "the mesh connectivity changed after the pattern was built; rebuild it");
   const int md = pat->max_deg > 0 ? pat->max_deg : 1;
-  const int npe = pat->mesh->npe;
   const size_t per_warp = (size_t)md * P * P * sizeof(double);
   int wpb = (int)std::min<size_t>(4, (200 * 1024) / per_warp);
   if (wpb < 1) wpb = 1;
@@ -650,8 +652,8 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const T *Kf, int64_t cs, doubl
   int64_t need = (pat->mesh->non + wpb - 1) / wpb;
   if (grid > need) grid = need > 0 ? need : 1;
   KernelScope ks(ctx, "k_colgather");
-  fn<<<(unsigned)grid, wpb * 32, smem, ctx->stream>>>(pat->d_nptr, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, Kf,
-                                                      cs, npe, pat->mesh->non, md, nz, cnt);
+  fn<<<(unsigned)grid, wpb * 32, smem, ctx->stream>>>(pat->d_nptr, n2e_ptr, n2e, pos, Kf, cs, npe, pat->mesh->non, md,
+                                                      nz, cnt);
   LLF_CUDA_TRY(ctx, cudaGetLastError());
   return LLF_OK;
 }
@@ -660,26 +662,32 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const T *Kf, int64_t cs, doubl
 
 // ------------------------------------------------------------------ host
 template <class T>
-int gather_full_t(llf_ctx *ctx, llf_pattern *pat, const T *Kf, int64_t cs, bool blockval, double *nz,
-                  int64_t *cnt) {
+int gather_full_t(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,
+                  int npe, const T *Kf, int64_t cs, bool blockval, double *nz, int64_t *cnt) {
   switch (pat->pdim * 2 + (blockval ? 1 : 0)) {
-    case 2: return run_colgather<1, false, T>(ctx, pat, Kf, cs, nz, cnt);
-    case 3: return run_colgather<1, true, T>(ctx, pat, Kf, cs, nz, cnt);
-    case 4: return run_colgather<2, false, T>(ctx, pat, Kf, cs, nz, cnt);
-    case 5: return run_colgather<2, true, T>(ctx, pat, Kf, cs, nz, cnt);
-    case 6: return run_colgather<3, false, T>(ctx, pat, Kf, cs, nz, cnt);
-    case 7: return run_colgather<3, true, T>(ctx, pat, Kf, cs, nz, cnt);
+    case 2: return run_colgather<1, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, nz, cnt);
+    case 3: return run_colgather<1, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, nz, cnt);
+    case 4: return run_colgather<2, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, nz, cnt);
+    case 5: return run_colgather<2, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, nz, cnt);
+    case 6: return run_colgather<3, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, nz, cnt);
+    case 7: return run_colgather<3, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, nz, cnt);
   }
   return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
 }
 
 int gather_full(llf_ctx *ctx, llf_pattern *pat, const double *Kf, int64_t colstride, bool blockval,
                 double *nz, int64_t *cnt) {
-  return gather_full_t<double>(ctx, pat, Kf, colstride, blockval, nz, cnt);
+  return gather_full_t<double>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, colstride,
+                               blockval, nz, cnt);
 }
 int gather_full32(llf_ctx *ctx, llf_pattern *pat, const float *Kf, int64_t colstride, bool blockval,
                   double *nz, int64_t *cnt) {
-  return gather_full_t<float>(ctx, pat, Kf, colstride, blockval, nz, cnt);
+  return gather_full_t<float>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, colstride,
+                              blockval, nz, cnt);
+}
+int gather_full_ext(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,
+                    int npe, const double *Kf, int64_t colstride, bool blockval, double *nz, int64_t *cnt) {
+  return gather_full_t<double>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, colstride, blockval, nz, cnt);
 }
 
 int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts) {

@@ -202,6 +202,17 @@ int gather_full(llf_ctx *ctx, llf_pattern *pat, const double *Kf, int64_t colstr
                 double *nz, int64_t *cnt);
 int gather_full32(llf_ctx *ctx, llf_pattern *pat, const float *Kf, int64_t colstride, bool blockval,
                   double *nz, int64_t *cnt);
+// The same gather for another element set on the pattern's nodes (e.g.
+// boundary faces): its node -> element lists, element-to-column map and npe.
+int gather_full_ext(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,
+                    int npe, const double *Kf, int64_t colstride, bool blockval, double *nz, int64_t *cnt);
+// Element-to-column map of an element set (conn, npe, node lists) into the
+// pattern's node CSC; *pos allocated (n2e_total * npe entries).
+int row_positions(llf_ctx *ctx, const llf_pattern *pat, const int32_t *conn, int npe, const int64_t *n2e_ptr,
+                  const int2 *n2e, int64_t n2e_total, uint16_t **pos);
+// elasticSupportMatrix / heatConvectionMatrix on the volume pattern (field.cu)
+int support_impl(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bmesh, const double *d_ke, const double *d_ken,
+                 double thickness, llf_matrix *m);
 // Element-matrix column stride (elements of `tsize` bytes) padded to 16 bytes,
 // so that every column can be fetched by one bulk copy.
 inline int64_t kf_colstride(int npe, int bs, int tsize) {

@@ -7,11 +7,22 @@
 // element vectors are buffered and then summed into f node by node in
 // element order, the order the reference (and the oracle) adds them.
 //
+// elasticSupportMatrix / heatConvectionMatrix, src/linear.jl:2859-3005 and
+// src/heat.jl:562-567: C = sum over boundary elements and points of
+// H^T diag(k) H Ja w with Ja as in the load vector.  One thread per boundary
+// element accumulates, for node pairs a <= b and component i, the fma chain
+// over the points of ((N_a Ja w) k_i) N_b into the diagonal of block (a,b) of
+// a full element matrix in the assembly's column-major-by-node layout; the
+// pattern's column gather then sums the element matrices in element order
+// into the volume pattern and dropzeros! compacts it.
+//
 // ∇ (:vector_grad branch), src/nabla.jl:77-311: at every element node k the
 // Jacobian and physical gradients of all shape functions are evaluated at
 // that node's reference coordinates, T[i,j] = sum_l g_l,j u_l,i (fma chain
 // over l), stored column-major per node (9 values); F = I + T on request.
 #include "common.cuh"
+
+#include <algorithm>
 
 namespace {
 
@@ -63,6 +74,75 @@ __global__ void k_load_elem(const double *__restrict__ xyz, const int32_t *__res
           out[a * pdim + i] = __fma_rn(__dmul_rn(Na, tq[i]), jw, out[a * pdim + i]);
       }
     }
+  }
+}
+
+// Ja of boundary point q (contract of the load vector): |t1| * b for a 2D
+// edge, |t1 x t2| for a 3D face; t1, t2 fma chains over the nodes.
+template <int BDIM>
+__device__ __forceinline__ double boundary_ja(const double *__restrict__ xyz, const int32_t *c, int npe, int q,
+                                              const double *__restrict__ dN, double thickness) {
+  double a1[3], a2[3];
+  for (int i = 0; i < 3; ++i) {
+    double s1 = 0.0, s2 = 0.0;
+    for (int a = 0; a < npe; ++a) {
+      double xa = xyz[(size_t)c[a] * 3 + i];
+      s1 = __fma_rn(xa, dN[((size_t)q * npe + a) * 3 + 0], s1);
+      if (BDIM == 2) s2 = __fma_rn(xa, dN[((size_t)q * npe + a) * 3 + 1], s2);
+    }
+    a1[i] = s1;
+    a2[i] = s2;
+  }
+  if (BDIM == 1)
+    return __dmul_rn(__dsqrt_rn(__dadd_rn(__dmul_rn(a1[0], a1[0]), __dmul_rn(a1[1], a1[1]))), thickness);
+  double xy = __dsub_rn(__dmul_rn(a1[0], a2[1]), __dmul_rn(a1[1], a2[0]));
+  double yz = __dsub_rn(__dmul_rn(a1[1], a2[2]), __dmul_rn(a1[2], a2[1]));
+  double zx = __dsub_rn(__dmul_rn(a1[2], a2[0]), __dmul_rn(a1[0], a2[2]));
+  return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(xy, xy), __dmul_rn(yz, yz)), __dmul_rn(zx, zx)));
+}
+
+// Boundary support element matrices: Kf[e][col node b][row node a][i*P+j],
+// cs doubles per column; stiffness per element ke[P*e+i], or element-node
+// values ken[(npe*e+a)*P+i] interpolated at the points.
+template <int BDIM>
+__global__ void k_support_elem(const double *__restrict__ xyz, const int32_t *__restrict__ conn, int64_t nel,
+                               int npe, int nip, const double *__restrict__ w, const double *__restrict__ N,
+                               const double *__restrict__ dN, int P, const double *__restrict__ ke,
+                               const double *__restrict__ ken, double thickness, double *__restrict__ Kf,
+                               int64_t cs) {
+  const int BS = P * P;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nel;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double *Ke = Kf + (size_t)e * npe * cs;
+    for (int b = 0; b < npe; ++b)
+      for (int m = 0; m < npe * BS; ++m) Ke[(size_t)b * cs + m] = 0.0;
+    const int32_t *c = conn + (size_t)e * npe;
+    for (int q = 0; q < nip; ++q) {
+      const double jw = __dmul_rn(boundary_ja<BDIM>(xyz, c, npe, q, dN, thickness), w[q]);
+      double kq[3] = {0.0, 0.0, 0.0};
+      for (int i = 0; i < P; ++i) {
+        if (ken) {
+          double acc = 0.0;
+          for (int a = 0; a < npe; ++a)
+            acc = __fma_rn(N[(size_t)q * npe + a], ken[((size_t)e * npe + a) * P + i], acc);
+          kq[i] = acc;
+        } else {
+          kq[i] = ke[(size_t)e * P + i];
+        }
+      }
+      for (int a = 0; a < npe; ++a) {
+        const double naj = __dmul_rn(N[(size_t)q * npe + a], jw);
+        for (int b = a; b < npe; ++b) {
+          const double Nb = N[(size_t)q * npe + b];
+          double *blk = Ke + (size_t)b * cs + (size_t)a * BS;
+          for (int i = 0; i < P; ++i) blk[i * P + i] = __fma_rn(__dmul_rn(naj, kq[i]), Nb, blk[i * P + i]);
+        }
+      }
+    }
+    for (int a = 0; a < npe; ++a)
+      for (int b = a + 1; b < npe; ++b)
+        for (int i = 0; i < P; ++i)
+          Ke[(size_t)a * cs + (size_t)b * BS + i * P + i] = Ke[(size_t)b * cs + (size_t)a * BS + i * P + i];
   }
 }
 
@@ -184,6 +264,49 @@ int load_vector_impl(llf_ctx *ctx, llf_mesh *bm, int problem_dim, int pdim, cons
   dfree(ctx, ptr);
   dfree(ctx, list);
   return llf_check_status(ctx, "loadVector");
+}
+
+int support_impl(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bm, const double *d_ke, const double *d_ken,
+                 double thickness, llf_matrix *m) {
+  cudaStream_t s = ctx->stream;
+  const int P = pat->pdim, npe = bm->npe;
+  const int64_t cs = kf_colstride(npe, P * P, (int)sizeof(double));
+  const int64_t non = pat->mesh->non;
+  double *Kf = nullptr;
+  int64_t *ptr = nullptr, *cnt = nullptr;
+  int2 *list = nullptr;
+  uint16_t *pos = nullptr;
+  int mx = 0, rc = LLF_OK;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &Kf, (size_t)std::max<int64_t>(bm->nel, 1) * npe * cs));
+  {
+    KernelScope ks(ctx, "k_support_elem");
+    const unsigned g = grid_1d(bm->nel, 128, ctx->num_sms);
+    if (bm->dim == 1)
+      k_support_elem<1><<<g, 128, 0, s>>>(bm->d_xyz, bm->d_conn, bm->nel, npe, bm->nip, bm->d_w, bm->d_N, bm->d_dN,
+                                          P, d_ke, d_ken, thickness, Kf, cs);
+    else
+      k_support_elem<2><<<g, 128, 0, s>>>(bm->d_xyz, bm->d_conn, bm->nel, npe, bm->nip, bm->d_w, bm->d_N, bm->d_dN,
+                                          P, d_ke, d_ken, thickness, Kf, cs);
+  }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  rc = build_n2e(ctx, bm->d_conn, nullptr, bm->nel, npe, non, &ptr, &list, &mx);
+  if (rc == LLF_OK) rc = row_positions(ctx, pat, bm->d_conn, npe, ptr, list, bm->nel * npe, &pos);
+  if (rc == LLF_OK) rc = llf_check_status(ctx, "elasticSupportMatrix: a boundary element pair outside the volume pattern");
+  if (rc == LLF_OK) {
+    cudaError_t e = dalloc(ctx, &cnt, pat->ndof + 1);
+    if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (pat->ndof + 1), s);
+    if (e == cudaSuccess) e = dalloc(ctx, &m->d_nz, pat->nnz);
+    if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (rc == LLF_OK) rc = gather_full_ext(ctx, pat, ptr, list, pos, npe, Kf, cs, true, m->d_nz, cnt);
+  dfree(ctx, Kf);
+  dfree(ctx, ptr);
+  dfree(ctx, list);
+  dfree(ctx, pos);
+  if (rc == LLF_OK) rc = llf_check_status(ctx, "elasticSupportMatrix");
+  if (rc == LLF_OK) rc = matrix_finalize(ctx, m, cnt);
+  dfree(ctx, cnt);
+  return rc;
 }
 
 int node_gather(llf_ctx *ctx, const int32_t *conn, int64_t nel, int npe, int64_t non, int pdim,

@@ -320,6 +320,17 @@ __global__ void k_row_positions(const int64_t *__restrict__ nptr, const int32_t 
   }
 }
 
+int row_positions(llf_ctx *ctx, const llf_pattern *pat, const int32_t *conn, int npe, const int64_t *n2e_ptr,
+                  const int2 *n2e, int64_t n2e_total, uint16_t **pos) {
+  *pos = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, pos, (size_t)n2e_total * npe));
+  const int64_t non = pat->mesh->non;
+  k_row_positions<<<grid_for(non * 32, 256, ctx->num_sms), 256, 0, ctx->stream>>>(
+      pat->d_nptr, pat->d_nadj, n2e_ptr, n2e, conn, npe, non, *pos, ctx->d_status);
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  return LLF_OK;
+}
+
 int pattern_build_impl(llf_ctx *ctx, llf_mesh *mesh, int pdim, llf_pattern *pat) {
   const int64_t non = mesh->non, nel = mesh->nel;
   const int npe = mesh->npe;

@@ -148,6 +148,76 @@ function heatConductionMatrix(problem; elements=[])
     return SystemMatrix(fetch(h[], problem.non), problem)
 end
 
+function heatCapacityMatrix(problem; elements=[], lumped=false)
+    m = device_mesh(problem); pat = pattern(problem, 1)
+    cρ = Float64[mat.c * mat.ρ for mat in problem.material]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:llf_assemble_mass, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Float64, Cint, Cint, Ref{Ptr{Cvoid}}),
+                ctx(), m.h, pat, ptype(problem), cρ, length(cρ), 1.0, lumped ? 1 : 0, 0, h))
+    return SystemMatrix(fetch(h[], problem.non), problem)
+end
+
+# Boundary elements of the conditions' physical groups, in condition order,
+# with gmsh's own tables for their element type (src/linear.jl:2896-2907).
+function boundary_mesh(problem, conds)
+    gmsh.model.setCurrent(problem.name)
+    nodeTags, coord, _ = gmsh.model.mesh.getNodes()
+    non = length(nodeTags)
+    xyz = zeros(3non)
+    for (i, t) in enumerate(nodeTags)
+        xyz[3t-2:3t] .= coord[3i-2:3i]
+    end
+    conn = Int64[]; owner = Int[]; et0 = 0; npe = 0
+    for (c, bc) in enumerate(conds)
+        for (edim, etag) in gmsh.model.getEntitiesForPhysicalName(bc.phName)
+            edim == problem.dim - 1 || error("LowLevelFEMGB300: supports on groups of dimension $(problem.dim - 1) only")
+            types, _, ntags = gmsh.model.mesh.getElements(edim, etag)
+            for (k, et) in enumerate(types)
+                et0 == 0 && (et0 = et)
+                et == et0 || error("LowLevelFEMGB300: one boundary element type per call")
+                _, _, _, npe, _, _ = gmsh.model.mesh.getElementProperties(et)
+                append!(conn, ntags[k]); append!(owner, fill(c, length(ntags[k]) ÷ npe))
+            end
+        end
+    end
+    _, _, order, npe, _, _ = gmsh.model.mesh.getElementProperties(et0)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:llf_mesh_upload, LIB), Cint,
+                (Ptr{Cvoid}, Cint, Int64, Ptr{Float64}, Int64, Cint, Ptr{Int64}, Cint, Cint, Ref{Ptr{Cvoid}}),
+                ctx(), problem.dim, non, xyz, length(owner), npe, conn, FAMILY[et0], order, h))
+    ip, w = gmsh.model.mesh.getIntegrationPoints(et0, "Gauss" * string(2order + 1))
+    _, N, _ = gmsh.model.mesh.getBasisFunctions(et0, ip, "Lagrange")
+    _, dN, _ = gmsh.model.mesh.getBasisFunctions(et0, ip, "GradLagrange")
+    check(ccall((:llf_tables_upload, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                ctx(), h[], length(w), w, N, dN))
+    return h[], owner
+end
+
+# elasticSupportMatrix (src/linear.jl:2859-3005) with constant kx, ky, kz (or
+# h for heat convection, src/heat.jl:562-567), one value set per condition.
+function support_matrix(problem, conds, keys)
+    pat = pattern(problem)
+    bm, owner = boundary_mesh(problem, conds)
+    pd = problem.pdim
+    ke = zeros(pd * length(owner))
+    for (e, c) in enumerate(owner), i in 1:pd
+        v = get(conds[c].values, keys[i], 0)
+        v isa Function && error("LowLevelFEMGB300: function-valued supports go through the Python mirror")
+        ke[pd*(e-1)+i] = v
+    end
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:llf_assemble_support, LIB), Cint,
+               (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Float64, Ref{Ptr{Cvoid}}),
+               ctx(), pat, bm, ke, C_NULL, problem.dim == 2 ? problem.thickness : 1.0, h)
+    ccall((:llf_mesh_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), bm)
+    check(st)
+    return SystemMatrix(fetch(h[], pd * problem.non), problem)
+end
+
+elasticSupportMatrix(problem, elSupports) = support_matrix(problem, elSupports, (:kx, :ky, :kz))
+heatConvectionMatrix(problem, heatConvection) = support_matrix(problem, heatConvection, (:h,))
+
 # energy: pass :NeoHookeCompressible or :StVenantKirchhoff; params = (μ=.., λ=..)
 law(energy) = energy === :NeoHookeCompressible ? 1 : energy === :StVenantKirchhoff ? 2 :
               error("LowLevelFEMGB300: built-in laws are :NeoHookeCompressible and :StVenantKirchhoff")

@@ -627,8 +627,9 @@ orc_csc *orc_assemble(int kind, int ptype, int dim, int pdim, int64_t non,
       orc_lame(ptype, params[2 * mat], params[2 * mat + 1], thickness, &c1, &c2);
     } else if (kind == ORC_HEAT) {
       c1 = params[mat] * b;
-    } else {
-      c1 = params[mat] * b;
+    } else {  /* massMatrixSolid: b = thickness for plane stress only (src/linear.jl:1873-1879);
+                 heatCapacityMatrix: b = 1 (src/heat.jl:275-283) */
+      c1 = params[mat] * (ptype == PT_PLANE_STRESS ? thickness : 1.0);
     }
     for (int a = 0; a < npe; ++a) {
       int64_t node = conn[e * npe + a];
@@ -708,7 +709,8 @@ double orc_assemble_csc_threaded(int kind, int ptype, int dim, int pdim,
     double c1 = 0, c2 = 0;
     double b = (ptype == PT_PLANE_STRESS || ptype == PT_HEAT || ptype == PT_PLANE_HEAT) ? thickness : 1.0;
     if (kind == ORC_ELASTIC) orc_lame(ptype, params[0], params[1], thickness, &c1, &c2);
-    else c1 = params[0] * b;
+    else if (kind == ORC_HEAT) c1 = params[0] * b;
+    else c1 = params[0] * (ptype == PT_PLANE_STRESS ? thickness : 1.0);
     int64_t nchunks = (nel + chunk - 1) / chunk;
     for (int64_t ch = tid; ch < nchunks; ch += T) {
       int64_t e0 = ch * chunk, e1 = e0 + chunk < nel ? e0 + chunk : nel;
@@ -835,6 +837,94 @@ int64_t orc_cg(const orc_csc *A, const double *b, double *x,
 /* traction t[pdim] or nodal values tn[pdim*nb] interpolated with H.        */
 /* Element contributions are added into f in element order.                 */
 /* ------------------------------------------------------------------------ */
+/* elasticSupportMatrix / heatConvectionMatrix (src/linear.jl:2859-3005,
+ * src/heat.jl:562-567): C = sum over boundary elements and points of
+ * H^T diag(k) H Ja w, Ja as in the load vector.  The stiffness k_i at a
+ * point of element e is the element's constant ke[pdim*e+i] or, with ken,
+ * its element-node values ken[(npe*e+a)*pdim+i] interpolated with H (fma
+ * chain over the nodes).  Several support groups are one element list in
+ * group order (the reference collects all groups' triplets before its single
+ * sparse() call).  Contract: jw = Ja * w_q;
+ * for node pairs a <= b and component i, the fma chain over q of
+ * ((N_a * jw) * k_i) * N_b is the diagonal entry i of block (a,b), mirrored
+ * to (b,a); triplets in the reference's transposed order, sparse
+ * (duplicates in input order), dropzeros!. */
+orc_csc *orc_support_matrix(int problem_dim, int pdim, int64_t non, const double *xyz, int64_t nelb, int npeb,
+                            const int32_t *connb, int nip, const double *w, const double *N, const double *dN,
+                            const double *ke, const double *ken, double thickness) {
+  int bdim = problem_dim - 1;
+  size_t nd = (size_t)pdim * npeb;
+  /* acc[(a*npeb+b)*pdim+i]: diagonal entry i of block (a,b), a <= b */
+  double *acc = (double *)malloc(sizeof(double) * npeb * npeb * pdim);
+  double *Ke = (double *)malloc(sizeof(double) * nd * nd);
+  coo c = {0};
+  c.n = non * pdim;
+  for (int64_t e = 0; e < nelb; ++e) {
+    const int32_t *ce = connb + e * npeb;
+    for (int k = 0; k < npeb * npeb * pdim; ++k) acc[k] = 0.0;
+    for (int q = 0; q < nip; ++q) {
+      double t1[3] = {0, 0, 0}, t2[3] = {0, 0, 0};
+      for (int i = 0; i < 3; ++i) {
+        double a1 = 0.0, a2 = 0.0;
+        for (int a = 0; a < npeb; ++a) {
+          double xa = xyz[3 * (int64_t)ce[a] + i];
+          a1 = fma(xa, dN[((size_t)q * npeb + a) * 3 + 0], a1);
+          if (bdim == 2) a2 = fma(xa, dN[((size_t)q * npeb + a) * 3 + 1], a2);
+        }
+        t1[i] = a1;
+        t2[i] = a2;
+      }
+      double Ja;
+      if (bdim == 1) {
+        Ja = sqrt(t1[0] * t1[0] + t1[1] * t1[1]) * thickness;
+      } else {
+        double xy = t1[0] * t2[1] - t1[1] * t2[0];
+        double yz = t1[1] * t2[2] - t1[2] * t2[1];
+        double zx = t1[2] * t2[0] - t1[0] * t2[2];
+        Ja = sqrt(xy * xy + yz * yz + zx * zx);
+      }
+      double jw = Ja * w[q];
+      double kq[3] = {0, 0, 0};
+      for (int i = 0; i < pdim; ++i) {
+        if (ken) {
+          double s = 0.0;
+          for (int a = 0; a < npeb; ++a) s = fma(N[(size_t)q * npeb + a], ken[(e * npeb + a) * pdim + i], s);
+          kq[i] = s;
+        } else {
+          kq[i] = ke[e * pdim + i];
+        }
+      }
+      for (int a = 0; a < npeb; ++a) {
+        double naj = N[(size_t)q * npeb + a] * jw;
+        for (int b = a; b < npeb; ++b)
+          for (int i = 0; i < pdim; ++i) {
+            double *t = &acc[((size_t)a * npeb + b) * pdim + i];
+            *t = fma(naj * kq[i], N[(size_t)q * npeb + b], *t);
+          }
+      }
+    }
+    memset(Ke, 0, sizeof(double) * nd * nd);
+    for (int a = 0; a < npeb; ++a)
+      for (int b = a; b < npeb; ++b)
+        for (int i = 0; i < pdim; ++i) {
+          double v = acc[((size_t)a * npeb + b) * pdim + i];
+          Ke[((size_t)a * pdim + i) * nd + (size_t)b * pdim + i] = v;
+          Ke[((size_t)b * pdim + i) * nd + (size_t)a * pdim + i] = v;
+        }
+    for (size_t l = 0; l < nd; ++l)
+      for (size_t k = 0; k < nd; ++k) {
+        int64_t dl = (int64_t)ce[l / pdim] * pdim + (int64_t)(l % pdim);
+        int64_t dk = (int64_t)ce[k / pdim] * pdim + (int64_t)(k % pdim);
+        coo_push(&c, dl, dk, Ke[k * nd + l]);
+      }
+  }
+  orc_csc *out = coo_to_csc(&c);
+  free(c.I); free(c.J); free(c.V);
+  free(acc); free(Ke);
+  orc_dropzeros(out);
+  return out;
+}
+
 void orc_load_vector(int problem_dim, int pdim, const double *xyz,
                      int64_t nelb, int npeb, const int32_t *connb, int nip,
                      const double *w, const double *N, const double *dN,

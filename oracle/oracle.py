@@ -67,6 +67,8 @@ def lib():
         L.orc_lame.argtypes = [i32, dbl, dbl, dbl, Pd, Pd]
         L.orc_load_vector.argtypes = [i32, i32, Pd, i64, i32, Pi32, i32, Pd, Pd, Pd, Pd, Pd, dbl, Pd]
         L.orc_num_threads.restype = i32
+        L.orc_support_matrix.restype = vp
+        L.orc_support_matrix.argtypes = [i32, i32, i64, Pd, i64, i32, Pi32, i32, Pd, Pd, Pd, Pd, Pd, dbl]
         L.orc_grad_elementwise.restype = i32
         L.orc_grad_elementwise.argtypes = [Pd, i64, i32, Pi32, Pd, Pd, i32, Pd]
         L.orc_tl_matrix.restype = vp
@@ -302,3 +304,27 @@ def ln(x: float) -> float:
 
 def num_threads() -> int:
     return lib().orc_num_threads()
+
+
+def support_matrix(problem_dim, pdim, non, xyz, bconn, rule, k, thickness=1.0, kn=None):
+    """elasticSupportMatrix / heatConvectionMatrix over the boundary elements
+    bconn (1-based node tags of the volume mesh, all groups in group order).
+    k: pdim constants for every element, or a (nel, pdim) array of
+    per-element constants; kn (optional, replaces k): nodal values
+    kn[non*pdim], taken at every element's nodes and interpolated."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    c0 = _conn0(bconn)
+    nel, npe = c0.shape
+    k = np.asarray(k, dtype=np.float64)
+    ke = np.ascontiguousarray(np.broadcast_to(k.reshape(-1, pdim) if k.ndim == 2 else k[:pdim], (nel, pdim)))
+    ken = None
+    if kn is not None:
+        kn = np.asarray(kn, dtype=np.float64).reshape(-1, pdim)
+        ken = np.ascontiguousarray(kn[c0.astype(np.int64)].reshape(nel, npe, pdim))
+    w = np.ascontiguousarray(rule["w"], dtype=np.float64)
+    N = np.ascontiguousarray(rule["N"], dtype=np.float64)
+    dN = np.ascontiguousarray(rule["dN"], dtype=np.float64)
+    h = lib().orc_support_matrix(problem_dim, pdim, non, _p(xyz, C.c_double), nel, npe,
+                                 _p(c0, C.c_int32), len(w), _p(w, C.c_double), _p(N, C.c_double),
+                                 _p(dN, C.c_double), _p(ke, C.c_double), _p(ken, C.c_double), float(thickness))
+    return CSC(h)

@@ -308,3 +308,19 @@ def test_connectivity_change_requires_new_pattern(llf, orc):
     assert rc == 0
     ref = orc.assemble(orc.ELASTIC, 0, 3, 3, m.xyz, conn2, L.builtin_rule(m.family, m.order), [2.1e5, 0.3])
     assert_csc_identical(K2.copy_csc(), ref.julia(), "K after connectivity change")
+
+
+@pytest.mark.parametrize("case", [("box", 3, 2, False), ("rect", 4, 3, True), ("box", 2, 1, True)],
+                         ids=["hex27", "tri10", "tet4"])
+@pytest.mark.parametrize("lumped", [False, True])
+def test_heat_capacity_bit_identical(llf, orc, case, lumped):
+    """heatCapacityMatrix (src/heat.jl:257-376): c rho sum H^T H detJ w with b = 1."""
+    kind, n, order, simplex = case
+    m = make_mesh(llf, kind, n, order, simplex)
+    mat = llf.Material("body", rho=7.85e-9, c=4.2e8)
+    pt = "HeatConduction" if m.dim == 3 else "PlaneHeatConduction"
+    p = llf.Problem([mat], type=pt, thickness=0.7)
+    C = llf.heatCapacityMatrix(p, lumped=lumped)
+    rule = llf._lib.builtin_rule(m.family, m.order)
+    ref = orc.assemble(orc.MASS, PT[pt], m.dim, 1, m.xyz, m.conn, rule, [mat.c * mat.rho], 0.7, lumped)
+    assert_csc_identical(C.csc(), ref.julia(), f"C {kind} {order} lumped={lumped}")

@@ -102,3 +102,25 @@ def test_heat_constant_nullspace(llf, orc):
     mat = llf.Material("body")
     K = oracle_operator(llf, orc, m, "heat", 3, mat).scipy()
     assert np.abs(K @ np.ones(K.shape[0])).max() <= 1e-12 * abs(K).max()
+
+
+@pytest.mark.parametrize("simplex", [False, True])
+def test_support_totals(llf, orc, simplex):
+    """elasticSupportMatrix: symmetric, diagonal blocks only, and each
+    component's entries sum to k_i times the supported area (2 x 3 face)."""
+    m = llf.structured_box_mesh(lx=2.0, ly=1.0, lz=3.0, n=2, order=2, simplex=simplex)
+    g = m.group("bottom")
+    rule = llf._lib.builtin_rule(g.family, g.order)
+    k = [3.0, 5.0, 11.0]
+    C = orc.support_matrix(3, 3, m.xyz.shape[0], m.xyz, g.conn, rule, k).scipy().tocoo()
+    assert np.all(C.row % 3 == C.col % 3)
+    for i in range(3):
+        s = C.data[C.row % 3 == i].sum()
+        assert abs(s - k[i] * 6.0) < 1e-12 * k[i] * 6.0
+    D = C.tocsc()
+    assert abs(D - D.T).max() == 0.0
+    m2 = llf.structured_rect_mesh(lx=2.0, n=4, order=3)
+    g2 = m2.group("top")
+    C2 = orc.support_matrix(2, 1, m2.xyz.shape[0], m2.xyz, g2.conn, llf._lib.builtin_rule(g2.family, g2.order),
+                            [4.0], 0.5).scipy()
+    assert abs(C2.sum() - 4.0 * 2.0 * 0.5) < 1e-13 * 4.0
