@@ -226,6 +226,20 @@ int llf_assemble_heat(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
                       int ptype, const double *k, int nmat, double thickness,
                       int form, llf_matrix **out);
 
+/* Follower-load tangent of traction loads on faces of a 3D body —
+ * externalTangentFollower, src/nonlinear.jl:3053-3258: per face point, with
+ * F_q interpolated from F_nodal[9*non] (column-major 3x3 per node), tg = F_q t
+ * and g = grad N_b on the face (Jacobian [t1 t2 n], n the unit normal),
+ *   K[(a,i),(b,j)] += N_a (Jgp F^-T ((F^-1[:,j].g) tg - (F^-1[:,j].tg) g
+ *                     + (g.F^-1 tg) e_j))_i |t1 x t2| w,
+ * triplets in element order, sparse, dropzeros!.  Traction per boundary
+ * element t_elem[3*nel_b] or at its nodes t_elem_nodal[3*npe*nel_b]
+ * (exactly one non-NULL).  The matrix is unsymmetric and lives on the
+ * volume pattern. */
+int llf_follower_tangent(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bmesh,
+                         const double *F_nodal, const double *t_elem,
+                         const double *t_elem_nodal, llf_matrix **out);
+
 /* Boundary support matrix C = sum H^T diag(k) H Ja w over the elements of
  * `bmesh` (dimension dim-1, node tags of the pattern's volume mesh), Ja as in
  * llf_load_vector — elasticSupportMatrix, src/linear.jl:2859-3005 (k = kx,
@@ -308,6 +322,21 @@ int llf_grad_elementwise(llf_ctx *ctx, llf_mesh *mesh, const double *u,
 int llf_load_vector(llf_ctx *ctx, llf_mesh *bmesh, int problem_dim, int pdim,
                     const double *t_const, const double *t_nodal,
                     double thickness, double *f, int64_t ndof);
+
+/* Follower traction loads of a 3D body — loadVector(problem, loads; F),
+ * src/linear.jl:3333-3372: the traction at a face point is F_q t (F_q
+ * interpolated from F_nodal[9*non], column-major 3x3 per node), integrated
+ * on the reference face.  t_const[3] or t_nodal[3*non]; f[3*non] host,
+ * accumulated into. */
+int llf_load_vector_follower(llf_ctx *ctx, llf_mesh *bmesh, const double *F_nodal,
+                             const double *t_const, const double *t_nodal,
+                             double *f, int64_t ndof);
+
+/* elementsToNodes, src/general.jl:5519-5640: nodal[ncomp*non] = the mean of
+ * the element-node values elem_values[ncomp*npe*nel] of every node (summed
+ * in element order, times 1/count); nodes in no element get 0. */
+int llf_elements_to_nodes(llf_ctx *ctx, llf_mesh *mesh, int ncomp,
+                          const double *elem_values, double *nodal);
 
 /* ======================================================================== */
 /* Matrices                                                                 */

@@ -16,7 +16,8 @@ from .api import (Material, material, elastic_constants, Problem, Field, SystemM
                   temperatureConstraint, load, heatFlux, elasticSupport, heatConvection, constrainedDoFs,
                   allDoFs, freeDoFs, applyBoundaryConditions_, loadVector, stiffnessMatrix, massMatrix,
                   heatConductionMatrix, heatCapacityMatrix, elasticSupportMatrix, heatConvectionMatrix,
-                  heatConvectionVector, applyElasticSupport_, applyHeatConvection_, solveDisplacement,
+                  heatConvectionVector, applyElasticSupport_, applyHeatConvection_, externalTangentFollower,
+                  elementsToNodes, isElementwise, solveDisplacement,
                   solveTemperature, solveField, solveFieldBatched, grad,
                   deformationGradient, materialTangentMatrix, initialStressMatrix, tangentMatrix, solveDeformation,
                   internalForceVector)

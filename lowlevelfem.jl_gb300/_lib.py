@@ -71,6 +71,9 @@ SIGNATURES = {
     "llf_assemble_mass": (i32, [vp, vp, vp, i32, P_dbl, i32, dbl, i32, i32, PP]),
     "llf_assemble_heat": (i32, [vp, vp, vp, i32, P_dbl, i32, dbl, i32, PP]),
     "llf_assemble_support": (i32, [vp, vp, vp, P_dbl, P_dbl, dbl, PP]),
+    "llf_follower_tangent": (i32, [vp, vp, vp, P_dbl, P_dbl, P_dbl, PP]),
+    "llf_load_vector_follower": (i32, [vp, vp, P_dbl, P_dbl, P_dbl, P_dbl, i64]),
+    "llf_elements_to_nodes": (i32, [vp, vp, i32, P_dbl, P_dbl]),
     "llf_tl_material_tangent": (i32, [vp, vp, vp, P_dbl, i32, P_dbl, i32, PP]),
     "llf_tl_tangent": (i32, [vp, vp, vp, P_dbl, i32, P_dbl, i32, PP]),
     "llf_tl_tangent_form": (i32, [vp, vp, vp, P_dbl, i32, P_dbl, i32, i32, PP]),

@@ -223,11 +223,18 @@ class ScalarField:
 
 @dataclass
 class TensorField:
-    """Elementwise nodal tensor field: A[e] holds 9*npe values (column-major
-    3x3 per element node), the layout of src/nabla.jl:190-208."""
-    A: np.ndarray                 # (nel, 9*npe)
+    """Tensor field, elementwise (A[e] holds 9*npe values, column-major 3x3
+    per element node, the layout of src/nabla.jl:190-208) or nodal (a holds
+    9 values per node, the same order)."""
+    A: np.ndarray | None          # (nel, 9*npe), or None for a nodal field
     model: Problem
     type: str = "tensor"
+    a: np.ndarray | None = None   # (9*non, 1) for a nodal field
+
+
+def isElementwise(T) -> bool:
+    """isElementwise (src/general.jl): the field holds element-node values."""
+    return getattr(T, "A", None) is not None
 
 
 def _field_for(problem: Problem, a: np.ndarray):
@@ -464,14 +471,21 @@ def applyBoundaryConditions_(u, supports):
     return u
 
 
-def loadVector(problem: Problem, loads) -> VectorField | ScalarField:
+def loadVector(problem: Problem, loads, F=None) -> VectorField | ScalarField:
     """Consistent nodal loads of LoadConditions on boundary groups
     (src/linear.jl:3088-3434).  Constant values are integrated exactly;
     function values are sampled at the group's nodes and interpolated with the
-    shape functions."""
+    shape functions.  With F (the deformation gradient, nodal or elementwise)
+    the tractions on faces of a 3D body are follower loads F t
+    (src/linear.jl:3333-3372)."""
     ndof = problem.pdim * problem.non
     f = np.zeros(ndof)
     ctx = problem._ctx
+    Fn = None
+    if F is not None:
+        if problem.dim != 3 or problem.pdim != 3:
+            raise ValueError("loadVector: follower loads need a 3D vector problem")
+        Fn = _nodal_F(problem, F)
     for ld in loads:
         g = problem.mesh.group(ld.phName)
         keys = ["qn"] if problem.pdim == 1 else ["fx", "fy", "fz"][: problem.pdim]
@@ -479,6 +493,8 @@ def loadVector(problem: Problem, loads) -> VectorField | ScalarField:
             keys = ["q"]
         vals = [ld.values.get(k, 0.0) for k in keys]
         if g.dim == 0:
+            if Fn is not None:
+                raise NotImplementedError("loadVector: follower loads on point groups are not accelerated")
             for n in g.nodes:
                 for c, v in enumerate(vals):
                     f[(n - 1) * problem.pdim + c] += float(v(*problem.mesh.xyz[n - 1]) if callable(v) else v)
@@ -493,11 +509,106 @@ def loadVector(problem: Problem, loads) -> VectorField | ScalarField:
             tn = np.zeros(ndof)
             for c, v in enumerate(vals):
                 tn[(g.nodes - 1) * problem.pdim + c] = _values_at(problem, g.nodes, v)
+        if Fn is not None:
+            ctx.check(_lib.lib().llf_load_vector_follower(ctx.h, bm.h, _lib.ptr(Fn, _lib.C.c_double),
+                                                          _lib.ptr(tconst, _lib.C.c_double),
+                                                          _lib.ptr(tn, _lib.C.c_double),
+                                                          _lib.ptr(f, _lib.C.c_double), ndof), "loadVector")
+            continue
         ctx.check(_lib.lib().llf_load_vector(ctx.h, bm.h, problem.dim, problem.pdim,
                                              _lib.ptr(tconst, _lib.C.c_double), _lib.ptr(tn, _lib.C.c_double),
                                              problem.thickness if problem.dim == 2 else 1.0,
                                              _lib.ptr(f, _lib.C.c_double), ndof), "loadVector")
     return _field_for(problem, f)
+
+
+def elementsToNodes(T: TensorField) -> TensorField:
+    """elementsToNodes (src/general.jl:5519-5640): the mean of the
+    element-node values at every node, summed in element order."""
+    if not isElementwise(T):
+        return T
+    problem = T.model
+    A = _tensor_array(problem, T)
+    out = np.zeros(9 * problem.non)
+    ctx = problem._ctx
+    ctx.check(_lib.lib().llf_elements_to_nodes(ctx.h, problem.device_mesh().h, 9, _lib.ptr(A, _lib.C.c_double),
+                                               _lib.ptr(out, _lib.C.c_double)), "elementsToNodes")
+    return TensorField(None, problem, a=out.reshape(-1, 1))
+
+
+def _nodal_F(problem: Problem, F) -> np.ndarray:
+    """F as 9 values per node (column-major 3x3), from a nodal or an
+    elementwise TensorField or a (non, 9) array."""
+    if isinstance(F, TensorField):
+        F = elementsToNodes(F).a
+    F = np.ascontiguousarray(np.asarray(F, dtype=np.float64).reshape(-1))
+    if F.size != 9 * problem.non:
+        raise ValueError(f"F must hold 9 values per node ({9 * problem.non}), got {F.size}")
+    return F
+
+
+def _boundary_runs(problem: Problem, conds, what):
+    """Consecutive conditions whose groups share the element type, each
+    group of dimension dim-1."""
+    runs = []
+    for bc in conds:
+        g = problem.mesh.group(bc.phName)
+        if g.dim != problem.dim - 1:
+            raise NotImplementedError(f"{what}: only boundary groups of dimension {problem.dim - 1} are "
+                                      f"accelerated (group {bc.phName!r} has dimension {g.dim})")
+        if runs and (runs[-1][-1][1].family, runs[-1][-1][1].order) == (g.family, g.order):
+            runs[-1].append((bc, g))
+        else:
+            runs.append([(bc, g)])
+    return runs
+
+
+def _element_values(problem: Problem, run, keys):
+    """Per-element constants (nel, len(keys)) of a run, or, when one value is
+    a function or a field, the values at every element's nodes
+    (nel, npe, len(keys)).  Returns (constants, element-node values)."""
+    vals = [[bc.values.get(k, 0.0) for k in keys] for bc, _ in run]
+    nodal = any(not np.isscalar(v) for vs in vals for v in vs)
+    parts = []
+    for (bc, g), vs in zip(run, vals):
+        if nodal:
+            kn = np.zeros((problem.non, len(keys)))
+            for c, v in enumerate(vs):
+                kn[g.nodes - 1, c] = _values_at(problem, g.nodes, v)
+            parts.append(kn[g.conn - 1])
+        else:
+            parts.append(np.tile(np.array([float(v) for v in vs]), (g.conn.shape[0], 1)))
+    karr = np.ascontiguousarray(np.concatenate(parts, axis=0), dtype=np.float64)
+    return (None, karr) if nodal else (karr, None)
+
+
+def externalTangentFollower(problem: Problem, loads, F) -> SystemMatrix:
+    """Tangent of follower traction loads fx, fy, fz on faces of a 3D body
+    (src/nonlinear.jl:3053-3258), K_ext; the Newton matrix is
+    K_mat + K_geo - K_ext.  F: the deformation gradient, nodal or
+    elementwise (averaged to the nodes).  The loads' groups of one element
+    type go in one call in load order."""
+    if problem.dim != 3 or problem.pdim != 3:
+        raise ValueError("externalTangentFollower: dim == 3 && pdim == 3 is required")
+    loads = list(loads)
+    for ld in loads:
+        if "p" in ld.values:
+            raise NotImplementedError("externalTangentFollower: pressure follower loads are not accelerated")
+    Fn = _nodal_F(problem, F)
+    ctx, pat = problem._ctx, problem.pattern()
+    total = None
+    for run in _boundary_runs(problem, loads, "externalTangentFollower"):
+        te, ten = _element_values(problem, run, ["fx", "fy", "fz"])
+        bm = problem.boundary_mesh(tuple(bc.phName for bc, _ in run))
+        h = _lib.C.c_void_p()
+        ctx.check(_lib.lib().llf_follower_tangent(ctx.h, pat.h, bm.h, _lib.ptr(Fn, _lib.C.c_double),
+                                                  _lib.ptr(te, _lib.C.c_double), _lib.ptr(ten, _lib.C.c_double),
+                                                  _lib.C.byref(h)), "externalTangentFollower")
+        K = SystemMatrix(_lib.DeviceMatrix(ctx, h, pat), problem)
+        total = K if total is None else total + K
+    if total is None:
+        raise ValueError("externalTangentFollower: no loads given")
+    return total
 
 
 def _support_matrix(problem: Problem, conds, keys, what) -> SystemMatrix:
@@ -512,33 +623,11 @@ def _support_matrix(problem: Problem, conds, keys, what) -> SystemMatrix:
     conds = list(conds)
     if not conds:
         raise ValueError(f"{what}: no conditions given")
-    runs = []
-    for bc in conds:
-        g = problem.mesh.group(bc.phName)
-        if g.dim != problem.dim - 1:
-            raise NotImplementedError(f"{what}: only boundary groups of dimension {problem.dim - 1} are "
-                                      f"accelerated (group {bc.phName!r} has dimension {g.dim})")
-        if runs and (runs[-1][-1][1].family, runs[-1][-1][1].order) == (g.family, g.order):
-            runs[-1].append((bc, g))
-        else:
-            runs.append([(bc, g)])
     total = None
-    for run in runs:
-        vals = [[bc.values.get(k, 0.0) for k in keys] for bc, _ in run]
-        nodal = any(not np.isscalar(v) for vs in vals for v in vs)
-        parts = []
-        for (bc, g), vs in zip(run, vals):
-            if nodal:
-                kn = np.zeros((problem.non, len(keys)))
-                for c, v in enumerate(vs):
-                    kn[g.nodes - 1, c] = _values_at(problem, g.nodes, v)
-                parts.append(kn[g.conn - 1])
-            else:
-                parts.append(np.tile(np.array([float(v) for v in vs]), (g.conn.shape[0], 1)))
-        karr = np.ascontiguousarray(np.concatenate(parts, axis=0), dtype=np.float64)
+    for run in _boundary_runs(problem, conds, what):
+        ke, ken = _element_values(problem, run, keys)
         bm = problem.boundary_mesh(tuple(bc.phName for bc, _ in run))
         h = _lib.C.c_void_p()
-        ke, ken = (None, karr) if nodal else (karr, None)
         ctx.check(_lib.lib().llf_assemble_support(ctx.h, pat.h, bm.h, _lib.ptr(ke, _lib.C.c_double),
                                                   _lib.ptr(ken, _lib.C.c_double),
                                                   problem.thickness if problem.dim == 2 else 1.0,
@@ -733,6 +822,12 @@ def _law(energy, params, C=None):
 
 
 def _tensor_array(problem: Problem, T) -> np.ndarray:
+    """Elementwise (nel, 9*npe) values of a tensor field; a nodal field is
+    taken at every element's nodes (nodesToElements, src/general.jl:5671)."""
+    if isinstance(T, TensorField) and T.A is None:
+        m = problem.mesh
+        return np.ascontiguousarray(np.asarray(T.a, dtype=np.float64).reshape(-1, 9)[m.conn - 1]
+                                    .reshape(m.nel, 9 * m.npe))
     A = T.A if isinstance(T, TensorField) else np.asarray(T)
     A = np.ascontiguousarray(A, dtype=np.float64)
     if A.shape != (problem.mesh.nel, 9 * problem.mesh.npe):

@@ -746,13 +746,92 @@ int llf_load_vector(llf_ctx *ctx, llf_mesh *bmesh, int problem_dim, int pdim, co
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(dtn, t_nodal, sizeof(double) * ndof, cudaMemcpyHostToDevice,
                                       ctx->stream));
   }
-  int rc = load_vector_impl(ctx, bmesh, problem_dim, pdim, t_const, dtn, thickness, df, ndof);
+  int rc = load_vector_impl(ctx, bmesh, problem_dim, pdim, t_const, dtn, thickness, nullptr, df, ndof);
   if (rc == LLF_OK) {
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(f, df, sizeof(double) * ndof, cudaMemcpyDeviceToHost, ctx->stream));
     LLF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   }
   dfree(ctx, df);
   dfree(ctx, dtn);
+  return rc == LLF_OK ? llf_ok(ctx) : rc;
+}
+
+int llf_load_vector_follower(llf_ctx *ctx, llf_mesh *bmesh, const double *F_nodal, const double *t_const,
+                             const double *t_nodal, double *f, int64_t ndof) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!bmesh || !f || !F_nodal || (!t_const && !t_nodal) || bmesh->dim != 2)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_load_vector_follower: needs F, a traction and a face mesh of a 3D body");
+  if (ndof != 3 * bmesh->non) return llf_fail(ctx, LLF_ERR_ARG, "llf_load_vector_follower: ndof must be 3 * non");
+  double *df = nullptr, *dtn = nullptr, *dF = nullptr;
+  int rc = LLF_OK;
+  cudaError_t e = dalloc(ctx, &df, ndof);
+  if (e == cudaSuccess) e = dalloc(ctx, &dF, (size_t)9 * bmesh->non);
+  if (e == cudaSuccess && t_nodal) e = dalloc(ctx, &dtn, ndof);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(df, f, sizeof(double) * ndof, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dF, F_nodal, sizeof(double) * 9 * bmesh->non, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess && t_nodal)
+    e = cudaMemcpyAsync(dtn, t_nodal, sizeof(double) * ndof, cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  if (rc == LLF_OK) rc = load_vector_impl(ctx, bmesh, 3, 3, t_const, dtn, 1.0, dF, df, ndof);
+  if (rc == LLF_OK) {
+    e = cudaMemcpyAsync(f, df, sizeof(double) * ndof, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  }
+  dfree(ctx, df);
+  dfree(ctx, dtn);
+  dfree(ctx, dF);
+  return rc == LLF_OK ? llf_ok(ctx) : rc;
+}
+
+int llf_follower_tangent(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bmesh, const double *F_nodal,
+                         const double *t_elem, const double *t_elem_nodal, llf_matrix **out) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!pat || !bmesh || !out || !F_nodal || (!t_elem == !t_elem_nodal))
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_follower_tangent: needs F and exactly one of t_elem, t_elem_nodal");
+  if (pat->pdim != 3 || pat->mesh->dim != 3 || bmesh->dim != 2 || bmesh->non != pat->mesh->non)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_follower_tangent: a pdim 3 pattern of a 3D mesh and a face mesh on its nodes");
+  if (pat->conn_version != pat->mesh->conn_version)
+    return llf_fail(ctx, LLF_ERR_STATE, "the mesh connectivity changed after the pattern was built; rebuild it");
+  const size_t nt = (size_t)bmesh->nel * 3 * (t_elem_nodal ? bmesh->npe : 1);
+  double *dF = nullptr, *dt = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &dF, (size_t)9 * bmesh->non));
+  cudaError_t e = dalloc(ctx, &dt, std::max<size_t>(nt, 1));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dF, F_nodal, sizeof(double) * 9 * bmesh->non, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dt, t_elem ? t_elem : t_elem_nodal, sizeof(double) * nt, cudaMemcpyHostToDevice, ctx->stream);
+  int rc = e == cudaSuccess ? LLF_OK : llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  llf_matrix *m = nullptr;
+  if (rc == LLF_OK) rc = new_matrix(ctx, pat, out, &m);
+  if (rc == LLF_OK) {
+    rc = follower_tangent_impl(ctx, pat, bmesh, dF, t_elem ? dt : nullptr, t_elem_nodal ? dt : nullptr, m);
+    rc = finish_matrix(ctx, rc, m, out);
+  }
+  dfree(ctx, dF);
+  dfree(ctx, dt);
+  return rc;
+}
+
+int llf_elements_to_nodes(llf_ctx *ctx, llf_mesh *mesh, int ncomp, const double *elem_values, double *nodal) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!mesh || !elem_values || !nodal || ncomp < 1)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_elements_to_nodes: bad arguments");
+  const size_t ne = (size_t)mesh->nel * mesh->npe * ncomp, nn = (size_t)mesh->non * ncomp;
+  double *dE = nullptr, *dN = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &dE, std::max<size_t>(ne, 1)));
+  cudaError_t e = dalloc(ctx, &dN, nn);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dE, elem_values, sizeof(double) * ne, cudaMemcpyHostToDevice, ctx->stream);
+  int rc = e == cudaSuccess ? LLF_OK : llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  if (rc == LLF_OK) rc = elements_to_nodes_impl(ctx, mesh, ncomp, dE, dN);
+  if (rc == LLF_OK) {
+    e = cudaMemcpyAsync(nodal, dN, sizeof(double) * nn, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  }
+  dfree(ctx, dE);
+  dfree(ctx, dN);
   return rc == LLF_OK ? llf_ok(ctx) : rc;
 }
 

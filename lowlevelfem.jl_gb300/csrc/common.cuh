@@ -280,7 +280,12 @@ int grad_elementwise_impl(llf_ctx *ctx, llf_mesh *mesh, const double *d_u,
                           int add_identity, double *d_out);
 int load_vector_impl(llf_ctx *ctx, llf_mesh *bmesh, int problem_dim, int pdim,
                      const double *t_const, const double *d_tn,
-                     double thickness, double *d_f, int64_t ndof);
+                     double thickness, const double *d_Fn, double *d_f, int64_t ndof);
+// externalTangentFollower on the volume pattern (field.cu)
+int follower_tangent_impl(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bmesh, const double *d_Fn,
+                          const double *d_te, const double *d_ten, llf_matrix *m);
+// elementsToNodes of ncomp values per element node (field.cu)
+int elements_to_nodes_impl(llf_ctx *ctx, llf_mesh *mesh, int ncomp, const double *d_ev, double *d_nv);
 
 // kinds of element operators
 enum { KIND_ELASTIC = 0, KIND_HEAT = 1, KIND_MASS = 2, KIND_TLMAT = 3, KIND_TLGEO = 4 };

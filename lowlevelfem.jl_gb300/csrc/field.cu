@@ -21,17 +21,33 @@
 // that node's reference coordinates, T[i,j] = sum_l g_l,j u_l,i (fma chain
 // over l), stored column-major per node (9 values); F = I + T on request.
 #include "common.cuh"
+#include "affine.cuh"
 
 #include <algorithm>
+#include <string>
 
 namespace {
+
+// F at a face point: Fq[i][j] = fma chain over the nodes of N_a F_a[i][j],
+// F nodal (9 per node, column-major 3x3).
+template <int BDIM>
+__device__ __forceinline__ void face_F(const double *__restrict__ Fn, const int32_t *c, int npe,
+                                       const double *__restrict__ Nq, double (&Fq)[3][3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double acc = 0.0;
+      for (int a = 0; a < npe; ++a) acc = __fma_rn(Nq[a], Fn[(size_t)c[a] * 9 + 3 * j + i], acc);
+      Fq[i][j] = acc;
+    }
+}
 
 template <int BDIM>
 __global__ void k_load_elem(const double *__restrict__ xyz, const int32_t *__restrict__ conn,
                             int64_t nel, int npe, int nip, const double *__restrict__ w,
                             const double *__restrict__ N, const double *__restrict__ dN, int pdim,
                             double t0, double t1c, double t2c, const double *__restrict__ tn,
-                            double thickness, double *__restrict__ fe) {
+                            double thickness, const double *__restrict__ Fn, unsigned *status,
+                            double *__restrict__ fe) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nel;
        e += (int64_t)gridDim.x * blockDim.x) {
     double *out = fe + (size_t)e * npe * pdim;
@@ -66,6 +82,18 @@ __global__ void k_load_elem(const double *__restrict__ xyz, const int32_t *__res
             acc = __fma_rn(N[(size_t)q * npe + a], tn[(size_t)c[a] * pdim + i], acc);
           tq[i] = acc;
         }
+      }
+      if (BDIM == 2 && Fn) {  // follower traction F_q t_q (3D faces)
+        double Fq[3][3], Fi[9];
+        face_F<BDIM>(Fn, c, npe, N + (size_t)q * npe, Fq);
+        if (!(jac_inverse<3>(Fq, Fi) > 0.0)) atomicOr(status, ST_BAD_JACOBIAN);
+        double tg[3];
+        for (int i = 0; i < 3; ++i) {
+          double acc = 0.0;
+          for (int j = 0; j < 3; ++j) acc = __fma_rn(Fq[i][j], tq[j], acc);
+          tg[i] = acc;
+        }
+        for (int i = 0; i < 3; ++i) tq[i] = tg[i];
       }
       const double jw = __dmul_rn(Ja, w[q]);
       for (int a = 0; a < npe; ++a) {
@@ -143,6 +171,124 @@ __global__ void k_support_elem(const double *__restrict__ xyz, const int32_t *__
       for (int b = a + 1; b < npe; ++b)
         for (int i = 0; i < P; ++i)
           Ke[(size_t)a * cs + (size_t)b * BS + i * P + i] = Ke[(size_t)b * cs + (size_t)a * BS + i * P + i];
+  }
+}
+
+// externalTangentFollower element matrices (3D faces, P = 3), full and
+// unsymmetric: Kf[e][col node b][row node a][ia*3+jb].  Contract of the
+// oracle: face Jacobian [t1 t2 n], n = (t1 x t2)/|t1 x t2|, surface
+// gradients g_b = Jm^-T (dN/du, dN/dv, 0); per column (b, jb)
+// u = alpha tg - s g + c e_jb, dt0 = Jgp Finv^T u, Ke += (N_a jw) dt0.
+__global__ void k_follower_elem(const double *__restrict__ xyz, const int32_t *__restrict__ conn, int64_t nel,
+                                int npe, int nip, const double *__restrict__ w, const double *__restrict__ N,
+                                const double *__restrict__ dN, const double *__restrict__ Fn,
+                                const double *__restrict__ te, const double *__restrict__ ten,
+                                double *__restrict__ Kf, int64_t cs, unsigned *status) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nel;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double *Ke = Kf + (size_t)e * npe * cs;
+    for (int b = 0; b < npe; ++b)
+      for (int m = 0; m < npe * 9; ++m) Ke[(size_t)b * cs + m] = 0.0;
+    const int32_t *c = conn + (size_t)e * npe;
+    for (int q = 0; q < nip; ++q) {
+      const double *Nq = N + (size_t)q * npe;
+      double t1[3], t2[3];
+      for (int i = 0; i < 3; ++i) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int a = 0; a < npe; ++a) {
+          const double xa = xyz[(size_t)c[a] * 3 + i];
+          s1 = __fma_rn(xa, dN[((size_t)q * npe + a) * 3 + 0], s1);
+          s2 = __fma_rn(xa, dN[((size_t)q * npe + a) * 3 + 1], s2);
+        }
+        t1[i] = s1;
+        t2[i] = s2;
+      }
+      const double xy = __dsub_rn(__dmul_rn(t1[0], t2[1]), __dmul_rn(t1[1], t2[0]));
+      const double yz = __dsub_rn(__dmul_rn(t1[1], t2[2]), __dmul_rn(t1[2], t2[1]));
+      const double zx = __dsub_rn(__dmul_rn(t1[2], t2[0]), __dmul_rn(t1[0], t2[2]));
+      const double da = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(xy, xy), __dmul_rn(yz, yz)), __dmul_rn(zx, zx)));
+      const double nrm[3] = {__ddiv_rn(yz, da), __ddiv_rn(zx, da), __ddiv_rn(xy, da)};
+      double Jm[3][3], Ji[9], Fq[3][3], Fi[9];
+      for (int i = 0; i < 3; ++i) {
+        Jm[i][0] = t1[i];
+        Jm[i][1] = t2[i];
+        Jm[i][2] = nrm[i];
+      }
+      jac_inverse<3>(Jm, Ji);
+      face_F<2>(Fn, c, npe, Nq, Fq);
+      const double Jgp = jac_inverse<3>(Fq, Fi);
+      if (!(Jgp > 0.0)) atomicOr(status, ST_BAD_JACOBIAN);
+      double tq[3], tg[3], tl[3];
+      for (int i = 0; i < 3; ++i) {
+        if (ten) {
+          double acc = 0.0;
+          for (int a = 0; a < npe; ++a) acc = __fma_rn(Nq[a], ten[((size_t)e * npe + a) * 3 + i], acc);
+          tq[i] = acc;
+        } else {
+          tq[i] = te[(size_t)e * 3 + i];
+        }
+      }
+      for (int i = 0; i < 3; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < 3; ++j) acc = __fma_rn(Fq[i][j], tq[j], acc);
+        tg[i] = acc;
+      }
+      for (int i = 0; i < 3; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < 3; ++j) acc = __fma_rn(Fi[3 * i + j], tg[j], acc);
+        tl[i] = acc;
+      }
+      const double jw = __dmul_rn(da, w[q]);
+      for (int b = 0; b < npe; ++b) {
+        const double *d = dN + ((size_t)q * npe + b) * 3;
+        double g[3];
+        for (int i = 0; i < 3; ++i) g[i] = __fma_rn(Ji[3 + i], d[1], __dmul_rn(Ji[i], d[0]));
+        double cdot = 0.0;
+        for (int i = 0; i < 3; ++i) cdot = __fma_rn(g[i], tl[i], cdot);
+        for (int jb = 0; jb < 3; ++jb) {
+          double alpha = 0.0, sdot = 0.0;
+          for (int i = 0; i < 3; ++i) {
+            alpha = __fma_rn(Fi[3 * i + jb], g[i], alpha);
+            sdot = __fma_rn(Fi[3 * i + jb], tg[i], sdot);
+          }
+          double u[3];
+          for (int i = 0; i < 3; ++i) u[i] = __dsub_rn(__dmul_rn(alpha, tg[i]), __dmul_rn(sdot, g[i]));
+          u[jb] = __dadd_rn(u[jb], cdot);
+          double dt0[3];
+          for (int i = 0; i < 3; ++i) {
+            double acc = 0.0;
+            for (int k = 0; k < 3; ++k) acc = __fma_rn(Fi[3 * k + i], u[k], acc);
+            dt0[i] = __dmul_rn(Jgp, acc);
+          }
+          double *col = Ke + (size_t)b * cs;
+          for (int a = 0; a < npe; ++a) {
+            const double nj = __dmul_rn(Nq[a], jw);
+            for (int ia = 0; ia < 3; ++ia) {
+              double *t = col + (size_t)a * 9 + ia * 3 + jb;
+              *t = __fma_rn(nj, dt0[ia], *t);
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+// elementsToNodes: nodal value = (sum of the element-node values of the
+// node in element order, from +0) * rcp(count).
+__global__ void k_elements_to_nodes(const int64_t *__restrict__ ptr, const int2 *__restrict__ list, int64_t non,
+                                    int npe, int ncomp, const double *__restrict__ ev, double *__restrict__ nv) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < non * ncomp;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t v = t / ncomp;
+    const int i = (int)(t - v * ncomp);
+    const int64_t s = ptr[v], e = ptr[v + 1];
+    double acc = 0.0;
+    for (int64_t k = s; k < e; ++k) {
+      const int2 el = list[k];
+      acc = __dadd_rn(acc, ev[((size_t)el.x * npe + el.y) * ncomp + i]);
+    }
+    nv[t] = (e > s) ? __dmul_rn(acc, __drcp_rn((double)(e - s))) : 0.0;
   }
 }
 
@@ -229,7 +375,7 @@ inline unsigned grid_1d(int64_t n, int threads, int sms) {
 }  // namespace
 
 int load_vector_impl(llf_ctx *ctx, llf_mesh *bm, int problem_dim, int pdim, const double *t_const,
-                     const double *d_tn, double thickness, double *d_f, int64_t ndof) {
+                     const double *d_tn, double thickness, const double *d_Fn, double *d_f, int64_t ndof) {
   (void)problem_dim;
   (void)ndof;
   cudaStream_t s = ctx->stream;
@@ -243,10 +389,12 @@ int load_vector_impl(llf_ctx *ctx, llf_mesh *bm, int problem_dim, int pdim, cons
     KernelScope ks(ctx, "k_load_elem");
     if (bm->dim == 1)
       k_load_elem<1><<<g, 128, 0, s>>>(bm->d_xyz, bm->d_conn, bm->nel, bm->npe, bm->nip, bm->d_w, bm->d_N,
-                                       bm->d_dN, pdim, t[0], t[1], t[2], d_tn, thickness, fe);
+                                       bm->d_dN, pdim, t[0], t[1], t[2], d_tn, thickness, nullptr, ctx->d_status,
+                                       fe);
     else
       k_load_elem<2><<<g, 128, 0, s>>>(bm->d_xyz, bm->d_conn, bm->nel, bm->npe, bm->nip, bm->d_w, bm->d_N,
-                                       bm->d_dN, pdim, t[0], t[1], t[2], d_tn, thickness, fe);
+                                       bm->d_dN, pdim, t[0], t[1], t[2], d_tn, thickness, d_Fn, ctx->d_status,
+                                       fe);
   }
   LLF_CUDA_TRY(ctx, cudaGetLastError());
   int64_t *ptr = nullptr;
@@ -266,47 +414,97 @@ int load_vector_impl(llf_ctx *ctx, llf_mesh *bm, int problem_dim, int pdim, cons
   return llf_check_status(ctx, "loadVector");
 }
 
-int support_impl(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bm, const double *d_ke, const double *d_ken,
-                 double thickness, llf_matrix *m) {
-  cudaStream_t s = ctx->stream;
-  const int P = pat->pdim, npe = bm->npe;
-  const int64_t cs = kf_colstride(npe, P * P, (int)sizeof(double));
-  const int64_t non = pat->mesh->non;
-  double *Kf = nullptr;
+// Gather the element matrices Kf (cs doubles per column) of the boundary
+// mesh bm into the volume pattern (element order per entry), dropzeros!, and
+// free Kf.
+static int boundary_matrix_finish(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bm, double *Kf, int64_t cs,
+                                  const char *what, llf_matrix *m) {
   int64_t *ptr = nullptr, *cnt = nullptr;
   int2 *list = nullptr;
   uint16_t *pos = nullptr;
-  int mx = 0, rc = LLF_OK;
+  int mx = 0;
+  int rc = llf_check_status(ctx, what);
+  if (rc == LLF_OK) rc = build_n2e(ctx, bm->d_conn, nullptr, bm->nel, bm->npe, pat->mesh->non, &ptr, &list, &mx);
+  if (rc == LLF_OK) rc = row_positions(ctx, pat, bm->d_conn, bm->npe, ptr, list, bm->nel * bm->npe, &pos);
+  if (rc == LLF_OK)
+    rc = llf_check_status(ctx, (std::string(what) + ": a boundary element pair outside the volume pattern").c_str());
+  if (rc == LLF_OK) {
+    cudaError_t e = dalloc(ctx, &cnt, pat->ndof + 1);
+    if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (pat->ndof + 1), ctx->stream);
+    if (e == cudaSuccess) e = dalloc(ctx, &m->d_nz, pat->nnz);
+    if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (rc == LLF_OK) rc = gather_full_ext(ctx, pat, ptr, list, pos, bm->npe, Kf, cs, true, m->d_nz, cnt);
+  dfree(ctx, Kf);
+  dfree(ctx, ptr);
+  dfree(ctx, list);
+  dfree(ctx, pos);
+  if (rc == LLF_OK) rc = llf_check_status(ctx, what);
+  if (rc == LLF_OK) rc = matrix_finalize(ctx, m, cnt);
+  dfree(ctx, cnt);
+  return rc;
+}
+
+int support_impl(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bm, const double *d_ke, const double *d_ken,
+                 double thickness, llf_matrix *m) {
+  const int P = pat->pdim, npe = bm->npe;
+  const int64_t cs = kf_colstride(npe, P * P, (int)sizeof(double));
+  double *Kf = nullptr;
   LLF_CUDA_TRY(ctx, dalloc(ctx, &Kf, (size_t)std::max<int64_t>(bm->nel, 1) * npe * cs));
   {
     KernelScope ks(ctx, "k_support_elem");
     const unsigned g = grid_1d(bm->nel, 128, ctx->num_sms);
     if (bm->dim == 1)
-      k_support_elem<1><<<g, 128, 0, s>>>(bm->d_xyz, bm->d_conn, bm->nel, npe, bm->nip, bm->d_w, bm->d_N, bm->d_dN,
-                                          P, d_ke, d_ken, thickness, Kf, cs);
+      k_support_elem<1><<<g, 128, 0, ctx->stream>>>(bm->d_xyz, bm->d_conn, bm->nel, npe, bm->nip, bm->d_w, bm->d_N,
+                                                    bm->d_dN, P, d_ke, d_ken, thickness, Kf, cs);
     else
-      k_support_elem<2><<<g, 128, 0, s>>>(bm->d_xyz, bm->d_conn, bm->nel, npe, bm->nip, bm->d_w, bm->d_N, bm->d_dN,
-                                          P, d_ke, d_ken, thickness, Kf, cs);
+      k_support_elem<2><<<g, 128, 0, ctx->stream>>>(bm->d_xyz, bm->d_conn, bm->nel, npe, bm->nip, bm->d_w, bm->d_N,
+                                                    bm->d_dN, P, d_ke, d_ken, thickness, Kf, cs);
   }
-  LLF_CUDA_TRY(ctx, cudaGetLastError());
-  rc = build_n2e(ctx, bm->d_conn, nullptr, bm->nel, npe, non, &ptr, &list, &mx);
-  if (rc == LLF_OK) rc = row_positions(ctx, pat, bm->d_conn, npe, ptr, list, bm->nel * npe, &pos);
-  if (rc == LLF_OK) rc = llf_check_status(ctx, "elasticSupportMatrix: a boundary element pair outside the volume pattern");
-  if (rc == LLF_OK) {
-    cudaError_t e = dalloc(ctx, &cnt, pat->ndof + 1);
-    if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (pat->ndof + 1), s);
-    if (e == cudaSuccess) e = dalloc(ctx, &m->d_nz, pat->nnz);
-    if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    dfree(ctx, Kf);
+    return llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
   }
-  if (rc == LLF_OK) rc = gather_full_ext(ctx, pat, ptr, list, pos, npe, Kf, cs, true, m->d_nz, cnt);
-  dfree(ctx, Kf);
+  return boundary_matrix_finish(ctx, pat, bm, Kf, cs, "elasticSupportMatrix", m);
+}
+
+int follower_tangent_impl(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bm, const double *d_Fn, const double *d_te,
+                          const double *d_ten, llf_matrix *m) {
+  const int npe = bm->npe;
+  const int64_t cs = kf_colstride(npe, 9, (int)sizeof(double));
+  double *Kf = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &Kf, (size_t)std::max<int64_t>(bm->nel, 1) * npe * cs));
+  {
+    KernelScope ks(ctx, "k_follower_elem");
+    k_follower_elem<<<grid_1d(bm->nel, 128, ctx->num_sms), 128, 0, ctx->stream>>>(
+        bm->d_xyz, bm->d_conn, bm->nel, npe, bm->nip, bm->d_w, bm->d_N, bm->d_dN, d_Fn, d_te, d_ten, Kf, cs,
+        ctx->d_status);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    dfree(ctx, Kf);
+    return llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  }
+  return boundary_matrix_finish(ctx, pat, bm, Kf, cs, "externalTangentFollower", m);
+}
+
+int elements_to_nodes_impl(llf_ctx *ctx, llf_mesh *mesh, int ncomp, const double *d_ev, double *d_nv) {
+  int64_t *ptr = nullptr;
+  int2 *list = nullptr;
+  int mx = 0;
+  int rc = build_n2e(ctx, mesh->d_conn, nullptr, mesh->nel, mesh->npe, mesh->non, &ptr, &list, &mx);
+  if (rc != LLF_OK) return rc;
+  {
+    KernelScope ks(ctx, "k_elements_to_nodes");
+    k_elements_to_nodes<<<grid_1d(mesh->non * ncomp, 128, ctx->num_sms), 128, 0, ctx->stream>>>(
+        ptr, list, mesh->non, mesh->npe, ncomp, d_ev, d_nv);
+  }
+  cudaError_t e = cudaGetLastError();
   dfree(ctx, ptr);
   dfree(ctx, list);
-  dfree(ctx, pos);
-  if (rc == LLF_OK) rc = llf_check_status(ctx, "elasticSupportMatrix");
-  if (rc == LLF_OK) rc = matrix_finalize(ctx, m, cnt);
-  dfree(ctx, cnt);
-  return rc;
+  if (e != cudaSuccess) return llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  return LLF_OK;
 }
 
 int node_gather(llf_ctx *ctx, const int32_t *conn, int64_t nel, int npe, int64_t non, int pdim,

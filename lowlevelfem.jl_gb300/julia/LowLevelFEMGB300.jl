@@ -218,6 +218,27 @@ end
 elasticSupportMatrix(problem, elSupports) = support_matrix(problem, elSupports, (:kx, :ky, :kz))
 heatConvectionMatrix(problem, heatConvection) = support_matrix(problem, heatConvection, (:h,))
 
+# externalTangentFollower (src/nonlinear.jl:3053-3258) with constant fx, fy,
+# fz per load; F nodal (9 per node) after elementsToNodes.
+function externalTangentFollower(problem, loads; F)
+    pat = pattern(problem)
+    Fn = vec(LowLevelFEM.elementsToNodes(F).a[:, 1])
+    bm, owner = boundary_mesh(problem, loads)
+    te = zeros(3 * length(owner))
+    for (e, c) in enumerate(owner), (i, k) in enumerate((:fx, :fy, :fz))
+        v = get(loads[c].values, k, 0)
+        v isa Number || error("LowLevelFEMGB300: function-valued follower loads go through the Python mirror")
+        te[3*(e-1)+i] = v
+    end
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:llf_follower_tangent, LIB), Cint,
+               (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ref{Ptr{Cvoid}}),
+               ctx(), pat, bm, Fn, te, C_NULL, h)
+    ccall((:llf_mesh_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), bm)
+    check(st)
+    return SystemMatrix(fetch(h[], 3problem.non), problem)
+end
+
 # energy: pass :NeoHookeCompressible or :StVenantKirchhoff; params = (μ=.., λ=..)
 law(energy) = energy === :NeoHookeCompressible ? 1 : energy === :StVenantKirchhoff ? 2 :
               error("LowLevelFEMGB300: built-in laws are :NeoHookeCompressible and :StVenantKirchhoff")

@@ -79,6 +79,8 @@ void orc_lame(int ptype, double E, double nu, double thickness, double *lamb,
 /* Geometry at one integration point (the shared arithmetic contract).      */
 /* Returns det.                                                             */
 /* ------------------------------------------------------------------------ */
+static double orc_inv3(const double J[3][3], double invJ[9]);
+
 static double orc_geom(int dim, int npe, const double *X, const double *dNq,
                        double invJ[9]) {
   double J[3][3] = {{0}};
@@ -88,8 +90,19 @@ static double orc_geom(int dim, int npe, const double *X, const double *dNq,
       for (int a = 0; a < npe; ++a) acc = fma(X[3 * a + i], dNq[3 * a + j], acc);
       J[i][j] = acc;
     }
+  if (dim == 3) return orc_inv3(J, invJ);
+  double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+  double rdet = 1.0 / det;
+  invJ[0] = J[1][1] * rdet;   invJ[1] = -J[0][1] * rdet; invJ[2] = 0.0;
+  invJ[3] = -J[1][0] * rdet;  invJ[4] = J[0][0] * rdet;  invJ[5] = 0.0;
+  invJ[6] = 0.0; invJ[7] = 0.0; invJ[8] = 0.0;
+  return det;
+}
+
+/* 3x3 inverse by cofactors, invJ row-major; returns det. */
+static double orc_inv3(const double J[3][3], double invJ[9]) {
   double det, rdet;
-  if (dim == 3) {
+  {
     double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
     double c01 = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]);
     double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
@@ -105,12 +118,6 @@ static double orc_geom(int dim, int npe, const double *X, const double *dNq,
     invJ[0] = c00 * rdet; invJ[1] = c10 * rdet; invJ[2] = c20 * rdet;
     invJ[3] = c01 * rdet; invJ[4] = c11 * rdet; invJ[5] = c21 * rdet;
     invJ[6] = c02 * rdet; invJ[7] = c12 * rdet; invJ[8] = c22 * rdet;
-  } else {
-    det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-    rdet = 1.0 / det;
-    invJ[0] = J[1][1] * rdet;   invJ[1] = -J[0][1] * rdet; invJ[2] = 0.0;
-    invJ[3] = -J[1][0] * rdet;  invJ[4] = J[0][0] * rdet;  invJ[5] = 0.0;
-    invJ[6] = 0.0; invJ[7] = 0.0; invJ[8] = 0.0;
   }
   return det;
 }
@@ -923,6 +930,203 @@ orc_csc *orc_support_matrix(int problem_dim, int pdim, int64_t non, const double
   free(acc); free(Ke);
   orc_dropzeros(out);
   return out;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Follower loads on boundary faces of a 3D body, F given at the nodes      */
+/* (Fn[9*node], column-major 3x3).  Shared contract at a face point q:       */
+/*   t1, t2 = fma chains over the nodes of x_a dN_a/du, x_a dN_a/dv;         */
+/*   cr = t1 x t2 as (yz, zx, xy), da = sqrt(|cr|^2) (the load vector's Ja); */
+/*   F_q[i][j] = fma chain over the nodes of N_a F_a[i][j];                  */
+/*   t_q = per-element constant te[3e+i], or fma chain of N_a ten[..];       */
+/*   tg = F_q t_q (fma chain over j).                                        */
+/* ------------------------------------------------------------------------ */
+static void orc_face_point(const double *xyz, const int32_t *ce, int npe, int q, const double *N,
+                           const double *dN, const double *Fn, double t1[3], double t2[3], double *da,
+                           double Fq[3][3]) {
+  for (int i = 0; i < 3; ++i) {
+    double a1 = 0.0, a2 = 0.0;
+    for (int a = 0; a < npe; ++a) {
+      double xa = xyz[3 * (int64_t)ce[a] + i];
+      a1 = fma(xa, dN[((size_t)q * npe + a) * 3 + 0], a1);
+      a2 = fma(xa, dN[((size_t)q * npe + a) * 3 + 1], a2);
+    }
+    t1[i] = a1;
+    t2[i] = a2;
+  }
+  double xy = t1[0] * t2[1] - t1[1] * t2[0];
+  double yz = t1[1] * t2[2] - t1[2] * t2[1];
+  double zx = t1[2] * t2[0] - t1[0] * t2[2];
+  *da = sqrt(xy * xy + yz * yz + zx * zx);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double acc = 0.0;
+      for (int a = 0; a < npe; ++a) acc = fma(N[(size_t)q * npe + a], Fn[9 * (int64_t)ce[a] + 3 * j + i], acc);
+      Fq[i][j] = acc;
+    }
+}
+
+static void orc_face_traction(int64_t e, const int32_t *ce, int npe, int q, const double *N, const double *te,
+                              const double *ten, double tq[3]) {
+  (void)ce;
+  for (int i = 0; i < 3; ++i) {
+    if (ten) {
+      double acc = 0.0;
+      for (int a = 0; a < npe; ++a) acc = fma(N[(size_t)q * npe + a], ten[(e * npe + a) * 3 + i], acc);
+      tq[i] = acc;
+    } else {
+      tq[i] = te[3 * e + i];
+    }
+  }
+}
+
+/* loadVector(problem, loads; F) (src/linear.jl:3088-3434, follower branch
+ * :3333-3372): the traction at a point is F_q t_q, integrated on the
+ * reference face, f[3*node+i] += fma(N_a tg_i, da w).  Element vectors are
+ * added into f in element order.  Returns 0, or -1 when det F_q <= 0. */
+int orc_load_vector_follower(const double *xyz, int64_t nelb, int npeb, const int32_t *connb, int nip,
+                             const double *w, const double *N, const double *dN, const double *Fn,
+                             const double *te, const double *ten, double *f) {
+  double *fe = (double *)malloc(sizeof(double) * npeb * 3);
+  int rc = 0;
+  for (int64_t e = 0; e < nelb; ++e) {
+    const int32_t *ce = connb + e * npeb;
+    for (int k = 0; k < npeb * 3; ++k) fe[k] = 0.0;
+    for (int q = 0; q < nip; ++q) {
+      double t1[3], t2[3], da, Fq[3][3], Fi[9], tq[3], tg[3];
+      orc_face_point(xyz, ce, npeb, q, N, dN, Fn, t1, t2, &da, Fq);
+      if (!(orc_inv3(Fq, Fi) > 0.0)) rc = -1;
+      orc_face_traction(e, ce, npeb, q, N, te, ten, tq);
+      for (int i = 0; i < 3; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < 3; ++j) acc = fma(Fq[i][j], tq[j], acc);
+        tg[i] = acc;
+      }
+      double jw = da * w[q];
+      for (int a = 0; a < npeb; ++a) {
+        double Na = N[(size_t)q * npeb + a];
+        for (int i = 0; i < 3; ++i) fe[a * 3 + i] = fma(Na * tg[i], jw, fe[a * 3 + i]);
+      }
+    }
+    for (int a = 0; a < npeb; ++a)
+      for (int i = 0; i < 3; ++i) f[3 * (int64_t)ce[a] + i] += fe[a * 3 + i];
+  }
+  free(fe);
+  return rc;
+}
+
+/* externalTangentFollower (src/nonlinear.jl:3053-3258): per face point,
+ * the face Jacobian Jm = [t1 t2 n] with n = cr / da (gmsh's completion of a
+ * surface Jacobian), jw = da w, grad N_b = Jm^-T (dN_b/du, dN_b/dv, 0) (fma
+ * chains), Finv = F_q^-1 and Jgp = det F_q by cofactors, tg = F_q t_q,
+ * tl = Finv tg.  For column (b, jb), with g = grad N_b and f = Finv[:,jb]:
+ *   u = alpha tg - s g + c e_jb,  alpha = f.g, s = f.tg, c = g.tl
+ *   dt0 = Jgp (Finv^T u)  (each dot product an fma chain in index order)
+ *   Ke[(a,ia),(b,jb)] = fma(N_a jw, dt0_ia, Ke)
+ * which is the reference's Jgp F^-T (alpha I - g f^T) tg + Jgp F^-T e_jb c.
+ * Triplets (row (a,ia), column (b,jb), Ke) in element order, sparse,
+ * dropzeros!.  *status = -1 when det F_q <= 0 somewhere. */
+orc_csc *orc_follower_tangent(int64_t non, const double *xyz, int64_t nelb, int npeb, const int32_t *connb,
+                              int nip, const double *w, const double *N, const double *dN, const double *Fn,
+                              const double *te, const double *ten, int *status) {
+  size_t nd = (size_t)3 * npeb;
+  double *Ke = (double *)malloc(sizeof(double) * nd * nd);
+  coo c = {0};
+  c.n = non * 3;
+  *status = 0;
+  for (int64_t e = 0; e < nelb; ++e) {
+    const int32_t *ce = connb + e * npeb;
+    for (size_t k = 0; k < nd * nd; ++k) Ke[k] = 0.0;
+    for (int q = 0; q < nip; ++q) {
+      double t1[3], t2[3], da, Fq[3][3], Fi[9], tq[3], tg[3], tl[3], Jm[3][3], Ji[9];
+      orc_face_point(xyz, ce, npeb, q, N, dN, Fn, t1, t2, &da, Fq);
+      double xy = t1[0] * t2[1] - t1[1] * t2[0];
+      double yz = t1[1] * t2[2] - t1[2] * t2[1];
+      double zx = t1[2] * t2[0] - t1[0] * t2[2];
+      double nrm[3] = {yz / da, zx / da, xy / da};
+      for (int i = 0; i < 3; ++i) {
+        Jm[i][0] = t1[i];
+        Jm[i][1] = t2[i];
+        Jm[i][2] = nrm[i];
+      }
+      orc_inv3(Jm, Ji);
+      double Jgp = orc_inv3(Fq, Fi);
+      if (!(Jgp > 0.0)) *status = -1;
+      orc_face_traction(e, ce, npeb, q, N, te, ten, tq);
+      for (int i = 0; i < 3; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < 3; ++j) acc = fma(Fq[i][j], tq[j], acc);
+        tg[i] = acc;
+      }
+      for (int i = 0; i < 3; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < 3; ++j) acc = fma(Fi[3 * i + j], tg[j], acc);
+        tl[i] = acc;
+      }
+      double jw = da * w[q];
+      for (int b = 0; b < npeb; ++b) {
+        const double *d = dN + ((size_t)q * npeb + b) * 3;
+        double g[3];
+        for (int i = 0; i < 3; ++i) g[i] = fma(Ji[3 + i], d[1], Ji[i] * d[0]);
+        double cdot = 0.0;
+        for (int i = 0; i < 3; ++i) cdot = fma(g[i], tl[i], cdot);
+        for (int jb = 0; jb < 3; ++jb) {
+          double alpha = 0.0, sdot = 0.0;
+          for (int i = 0; i < 3; ++i) {
+            alpha = fma(Fi[3 * i + jb], g[i], alpha);
+            sdot = fma(Fi[3 * i + jb], tg[i], sdot);
+          }
+          double u[3];
+          for (int i = 0; i < 3; ++i) u[i] = alpha * tg[i] - sdot * g[i];
+          u[jb] += cdot;
+          double dt0[3];
+          for (int i = 0; i < 3; ++i) {
+            double acc = 0.0;
+            for (int k = 0; k < 3; ++k) acc = fma(Fi[3 * k + i], u[k], acc);
+            dt0[i] = Jgp * acc;
+          }
+          for (int a = 0; a < npeb; ++a) {
+            double nj = N[(size_t)q * npeb + a] * jw;
+            for (int ia = 0; ia < 3; ++ia) {
+              double *t = &Ke[((size_t)a * 3 + ia) * nd + (size_t)b * 3 + jb];
+              *t = fma(nj, dt0[ia], *t);
+            }
+          }
+        }
+      }
+    }
+    for (size_t r = 0; r < nd; ++r)
+      for (size_t k = 0; k < nd; ++k) {
+        int64_t dr = (int64_t)ce[r / 3] * 3 + (int64_t)(r % 3);
+        int64_t dk = (int64_t)ce[k / 3] * 3 + (int64_t)(k % 3);
+        coo_push(&c, dr, dk, Ke[r * nd + k]);
+      }
+  }
+  orc_csc *out = coo_to_csc(&c);
+  free(c.I); free(c.J); free(c.V);
+  free(Ke);
+  orc_dropzeros(out);
+  return out;
+}
+
+/* elementsToNodes (src/general.jl:5519-5640): nodal value = (sum of the
+ * element-node values in element order) * (1 / count). */
+void orc_elements_to_nodes(int64_t non, int64_t nel, int npe, const int32_t *conn, int ncomp, const double *ev,
+                           double *nv) {
+  int64_t *cnt = (int64_t *)calloc((size_t)non, sizeof(int64_t));
+  for (int64_t k = 0; k < non * ncomp; ++k) nv[k] = 0.0;
+  for (int64_t e = 0; e < nel; ++e)
+    for (int a = 0; a < npe; ++a) {
+      int64_t v = conn[e * npe + a];
+      cnt[v] += 1;
+      for (int i = 0; i < ncomp; ++i) nv[v * ncomp + i] += ev[(e * npe + a) * ncomp + i];
+    }
+  for (int64_t v = 0; v < non; ++v) {
+    if (!cnt[v]) continue;
+    double fct = 1.0 / (double)cnt[v];
+    for (int i = 0; i < ncomp; ++i) nv[v * ncomp + i] *= fct;
+  }
+  free(cnt);
 }
 
 void orc_load_vector(int problem_dim, int pdim, const double *xyz,

@@ -69,6 +69,11 @@ def lib():
         L.orc_num_threads.restype = i32
         L.orc_support_matrix.restype = vp
         L.orc_support_matrix.argtypes = [i32, i32, i64, Pd, i64, i32, Pi32, i32, Pd, Pd, Pd, Pd, Pd, dbl]
+        L.orc_load_vector_follower.restype = i32
+        L.orc_load_vector_follower.argtypes = [Pd, i64, i32, Pi32, i32, Pd, Pd, Pd, Pd, Pd, Pd, Pd]
+        L.orc_follower_tangent.restype = vp
+        L.orc_follower_tangent.argtypes = [i64, Pd, i64, i32, Pi32, i32, Pd, Pd, Pd, Pd, Pd, Pd, C.POINTER(i32)]
+        L.orc_elements_to_nodes.argtypes = [i64, i64, i32, Pi32, i32, Pd, Pd]
         L.orc_grad_elementwise.restype = i32
         L.orc_grad_elementwise.argtypes = [Pd, i64, i32, Pi32, Pd, Pd, i32, Pd]
         L.orc_tl_matrix.restype = vp
@@ -225,6 +230,57 @@ def load_vector(problem_dim, pdim, xyz, connb, rule, t=None, tn=None, thickness=
                           len(w), _p(w, C.c_double), _p(N, C.c_double), _p(dN, C.c_double), _p(t, C.c_double),
                           _p(tn, C.c_double), float(thickness), _p(f, C.c_double))
     return f
+
+
+def _face_traction(cb, t, tn):
+    """(per-element constants, element-node values) of a face traction: t is
+    3 constants or a (nel, 3) array; tn (replaces t) nodal values (non, 3)."""
+    nel, npe = cb.shape
+    if tn is not None:
+        tn = np.asarray(tn, dtype=np.float64).reshape(-1, 3)
+        return None, np.ascontiguousarray(tn[cb.astype(np.int64)].reshape(nel, npe, 3))
+    t = np.asarray(t, dtype=np.float64)
+    return np.ascontiguousarray(np.broadcast_to(t.reshape(-1, 3) if t.ndim == 2 else t[:3], (nel, 3))), None
+
+
+def load_vector_follower(xyz, connb, rule, Fn, t=None, tn=None, f=None):
+    """Follower traction F t on 3D boundary faces, F nodal (non, 9)
+    column-major.  Returns (f, status)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    cb = _conn0(connb)
+    f = np.zeros(3 * xyz.shape[0]) if f is None else np.ascontiguousarray(f, dtype=np.float64)
+    Fn = np.ascontiguousarray(Fn, dtype=np.float64)
+    te, ten = _face_traction(cb, t, tn)
+    w = np.ascontiguousarray(rule["w"]); N = np.ascontiguousarray(rule["N"]); dN = np.ascontiguousarray(rule["dN"])
+    rc = lib().orc_load_vector_follower(_p(xyz, C.c_double), cb.shape[0], cb.shape[1], _p(cb, C.c_int32), len(w),
+                                        _p(w, C.c_double), _p(N, C.c_double), _p(dN, C.c_double),
+                                        _p(Fn, C.c_double), _p(te, C.c_double), _p(ten, C.c_double),
+                                        _p(f, C.c_double))
+    return f, rc
+
+
+def follower_tangent(xyz, connb, rule, Fn, t=None, tn=None):
+    """externalTangentFollower over 3D boundary faces; returns (CSC, status)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    cb = _conn0(connb)
+    Fn = np.ascontiguousarray(Fn, dtype=np.float64)
+    te, ten = _face_traction(cb, t, tn)
+    w = np.ascontiguousarray(rule["w"]); N = np.ascontiguousarray(rule["N"]); dN = np.ascontiguousarray(rule["dN"])
+    st = C.c_int32(0)
+    h = lib().orc_follower_tangent(xyz.shape[0], _p(xyz, C.c_double), cb.shape[0], cb.shape[1], _p(cb, C.c_int32),
+                                   len(w), _p(w, C.c_double), _p(N, C.c_double), _p(dN, C.c_double),
+                                   _p(Fn, C.c_double), _p(te, C.c_double), _p(ten, C.c_double), C.byref(st))
+    return CSC(h), st.value
+
+
+def elements_to_nodes(non, conn, ev, ncomp):
+    """elementsToNodes: ev (nel, npe*ncomp) -> nodal (non, ncomp)."""
+    c0 = _conn0(conn)
+    ev = np.ascontiguousarray(ev, dtype=np.float64)
+    out = np.zeros((non, ncomp))
+    lib().orc_elements_to_nodes(non, c0.shape[0], c0.shape[1], _p(c0, C.c_int32), ncomp, _p(ev, C.c_double),
+                                _p(out, C.c_double))
+    return out
 
 
 def grad_elementwise(xyz, conn, rule, u, add_identity=False):
