@@ -71,6 +71,11 @@ extern "C" {
                           cores with split TF32 operands (hi*hi + hi*lo + lo*hi),
                           FP32 accumulation, FP64 global accumulation */
 
+/* ---- weak-form DSL bilinear forms (src/multifield.jl:4385-4931) -------- */
+#define LLF_FORM_SYMGRAD_D_SYMGRAD 0  /* ∫(SymGrad(P)⋅D⋅SymGrad(P)), isotropic D: c1 = lambda, c2 = mu */
+#define LLF_FORM_GRAD_K_GRAD       1  /* ∫(Grad(P)⋅k⋅Grad(P)), scalar P: c1 = k */
+#define LLF_FORM_ID_C_ID           2  /* ∫(Id(P)⋅c⋅Id(P)): c1 = c */
+
 /* ---- hyperelastic laws for the Total Lagrangian kernels ----------------- */
 #define LLF_LAW_CONSTANT_C     0   /* params: 36 values, 6x6 Voigt tangent, column-major */
 #define LLF_LAW_NEOHOOKE_COMP  1   /* params: mu, lambda; psi = mu/2(I1-3) - mu lnJ + lambda/2 (lnJ)^2 */
@@ -239,6 +244,22 @@ int llf_assemble_heat(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
 int llf_follower_tangent(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bmesh,
                          const double *F_nodal, const double *t_elem,
                          const double *t_elem_nodal, llf_matrix **out);
+
+/* Weak-form DSL bilinear term ∫(a(P)⋅coef⋅b(P); csc_matrix) —
+ * src/multifield.jl:5280-5346 with assemble_operator, :2630-.  The three
+ * forms above run on the assembly kernels with the coefficients as given
+ * (b = 1; per material index, nmat entries).  accumulate NULL: a new matrix
+ * with dropzeros!.  accumulate = a matrix on the same pattern (csc_matrix):
+ * the assembly adds into its values in element order, keeps the full
+ * structural pattern, and the result is returned in *out (accumulate itself
+ * is left unchanged). */
+int llf_assemble_form(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int form_kind,
+                      const double *c1, const double *c2, int nmat,
+                      const llf_matrix *accumulate, int form, llf_matrix **out);
+
+/* build_csc_pattern, src/multifield.jl:2083-2250: a matrix on the pattern
+ * holding structural zeros, whose stored form keeps every entry. */
+int llf_matrix_zero_pattern(llf_ctx *ctx, llf_pattern *pat, llf_matrix **out);
 
 /* Boundary support matrix C = sum H^T diag(k) H Ja w over the elements of
  * `bmesh` (dimension dim-1, node tags of the pattern's volume mesh), Ja as in

@@ -22,4 +22,6 @@ from .api import (Material, material, elastic_constants, Problem, Field, SystemM
                   deformationGradient, materialTangentMatrix, initialStressMatrix, tangentMatrix, solveDeformation,
                   internalForceVector)
 
+from .dsl import OpApplied, BilinearTerm, Grad, SymGrad, Id, integrate, build_csc_pattern
+
 __version__ = "0.1.0"

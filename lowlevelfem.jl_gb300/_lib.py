@@ -24,6 +24,7 @@ ERRORS = {
 LINE, TRI, QUAD, TET, HEX = 1, 2, 3, 4, 5
 SOLID, PLANE_STRESS, PLANE_STRAIN, HEAT_CONDUCTION, PLANE_HEAT_CONDUCTION = 0, 1, 2, 3, 4
 FP64, FP32Q = 0, 1
+FORM_SYMGRAD, FORM_GRAD, FORM_ID = 0, 1, 2
 LAW_CONSTANT_C, LAW_NEOHOOKE_COMP, LAW_SVK = 0, 1, 2
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_BJACOBI, PRECOND_IC0 = 0, 1, 2, 3
 
@@ -71,6 +72,8 @@ SIGNATURES = {
     "llf_assemble_mass": (i32, [vp, vp, vp, i32, P_dbl, i32, dbl, i32, i32, PP]),
     "llf_assemble_heat": (i32, [vp, vp, vp, i32, P_dbl, i32, dbl, i32, PP]),
     "llf_assemble_support": (i32, [vp, vp, vp, P_dbl, P_dbl, dbl, PP]),
+    "llf_assemble_form": (i32, [vp, vp, vp, i32, P_dbl, P_dbl, i32, vp, i32, PP]),
+    "llf_matrix_zero_pattern": (i32, [vp, vp, PP]),
     "llf_follower_tangent": (i32, [vp, vp, vp, P_dbl, P_dbl, P_dbl, PP]),
     "llf_load_vector_follower": (i32, [vp, vp, P_dbl, P_dbl, P_dbl, P_dbl, i64]),
     "llf_elements_to_nodes": (i32, [vp, vp, i32, P_dbl, P_dbl]),

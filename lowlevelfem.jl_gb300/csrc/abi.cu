@@ -589,6 +589,49 @@ int llf_assemble_support(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bmesh, const 
   return rc;
 }
 
+int llf_assemble_form(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int form_kind, const double *c1,
+                      const double *c2, int nmat, const llf_matrix *accumulate, int form, llf_matrix **out) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!mesh || !pat || !out || !c1 || nmat < 1) return llf_fail(ctx, LLF_ERR_ARG, "llf_assemble_form: null argument");
+  if (pat->mesh != mesh) return llf_fail(ctx, LLF_ERR_STATE, "llf_assemble_form: the pattern belongs to another mesh");
+  if (form != LLF_FP64 && form != LLF_FP32Q) return llf_fail(ctx, LLF_ERR_ARG, "llf_assemble_form: form");
+  int kind;
+  if (form_kind == LLF_FORM_SYMGRAD_D_SYMGRAD) {
+    if (pat->pdim != mesh->dim || !c2)
+      return llf_fail(ctx, LLF_ERR_ARG, "∫(SymGrad⋅D⋅SymGrad): a vector field with pdim == dim and lambda, mu");
+    kind = KIND_ELASTIC;
+  } else if (form_kind == LLF_FORM_GRAD_K_GRAD) {
+    if (pat->pdim != 1) return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "∫(Grad⋅k⋅Grad): only scalar fields are accelerated");
+    kind = KIND_HEAT;
+  } else if (form_kind == LLF_FORM_ID_C_ID) {
+    kind = KIND_MASS;
+  } else {
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_assemble_form: form_kind");
+  }
+  if (accumulate && (accumulate->pat != pat || accumulate->diagonal_only || !accumulate->d_nz))
+    return llf_fail(ctx, LLF_ERR_STATE, "llf_assemble_form: csc_matrix must be a full matrix on the same pattern");
+  llf_matrix *m;
+  int rc;
+  if ((rc = new_matrix(ctx, pat, out, &m))) return rc;
+  m->keep_pattern = accumulate != nullptr;
+  rc = assemble_impl(ctx, mesh, pat, kind, mesh->dim == 3 ? LLF_SOLID : LLF_PLANE_STRAIN, c1, c2, nmat, form, 0, m,
+                     accumulate ? accumulate->d_nz : nullptr);
+  return finish_matrix(ctx, rc, m, out);
+}
+
+int llf_matrix_zero_pattern(llf_ctx *ctx, llf_pattern *pat, llf_matrix **out) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!pat || !out) return llf_fail(ctx, LLF_ERR_ARG, "llf_matrix_zero_pattern: null argument");
+  llf_matrix *m;
+  int rc;
+  if ((rc = new_matrix(ctx, pat, out, &m))) return rc;
+  m->keep_pattern = true;
+  cudaError_t e = dalloc(ctx, &m->d_nz, pat->nnz);
+  if (e == cudaSuccess) e = cudaMemsetAsync(m->d_nz, 0, sizeof(double) * pat->nnz, ctx->stream);
+  rc = e == cudaSuccess ? matrix_finalize(ctx, m, nullptr) : llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+  return finish_matrix(ctx, rc, m, out);
+}
+
 int llf_assemble_heat(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int ptype,
                       const double *k, int nmat, double thickness, int form,
                       llf_matrix **out) {

@@ -397,7 +397,8 @@ template <int P, bool BLOCKVAL, class T>
 __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__restrict__ n2e_ptr,
                             const int2 *__restrict__ n2e, const uint16_t *__restrict__ pos,
                             const T *__restrict__ Kf, int64_t cs, int npe, int64_t non, int max_deg,
-                            double *__restrict__ nz, int64_t *__restrict__ cnt) {
+                            const double *__restrict__ init, double *__restrict__ nz,
+                            int64_t *__restrict__ cnt) {
   extern __shared__ double cg_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   constexpr int BS = BLOCKVAL ? P * P : 1;
@@ -407,7 +408,16 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
     const int deg = (int)(nptr[B + 1] - c0);
     const int64_t s = n2e_ptr[B];
     const int nb = (int)(n2e_ptr[B + 1] - s);
-    for (int t = lane; t < deg * P * P; t += 32) acc[t] = -0.0;
+    if (init) {  // accumulate into existing structural values (same layout as the output)
+      const double *src = init + (size_t)P * P * c0;
+      for (int idx = lane; idx < deg * P * P; idx += 32) {
+        const int j = idx / (P * deg), r = idx - j * P * deg;
+        acc[(size_t)(r / P) * P * P + j * P + r % P] = src[idx];
+      }
+    } else {
+      for (int t = lane; t < deg * P * P; t += 32) acc[t] = -0.0;
+    }
+    const bool store_first = init == nullptr;
     __syncwarp();
     if (npe <= 32) {
       const bool act = lane < npe;
@@ -429,7 +439,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
           tn = pos[(s + k + 1) * npe + lane];
         }
         if (act && tc != 0xffffu) {
-          if (k == 0) add_block<P, BLOCKVAL, true>(acc, (int)tc, cur);  // k is warp-uniform
+          if (k == 0 && store_first) add_block<P, BLOCKVAL, true>(acc, (int)tc, cur);  // warp-uniform
           else add_block<P, BLOCKVAL, false>(acc, (int)tc, cur);
         }
         __syncwarp();
@@ -444,7 +454,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
         for (int a = lane; a < npe; a += 32) {
           const unsigned t = pos[(s + k) * npe + a];
           if (t != 0xffffu) {
-            if (k == 0) add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BS);
+            if (k == 0 && store_first) add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BS);
             else add_block<P, BLOCKVAL, false>(acc, (int)t, col + (size_t)a * BS);
           }
         }
@@ -470,6 +480,12 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
 }
 
 // ---------------------------------------------------------------- dropzeros
+// Structural entry count of every column (a matrix that keeps its pattern).
+__global__ void k_count_struct(const int64_t *__restrict__ colptr, int64_t ndof, int64_t *__restrict__ cnt) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ndof; c += (int64_t)gridDim.x * blockDim.x)
+    cnt[c] = colptr[c + 1] - colptr[c];
+}
+
 __global__ void k_count_nz(const double *__restrict__ nz, const int64_t *__restrict__ colptr,
                            int64_t ndof, int64_t *__restrict__ cnt) {
   const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
@@ -486,7 +502,7 @@ __global__ void k_count_nz(const double *__restrict__ nz, const int64_t *__restr
 
 // One warp per DoF column; four 32-entry chunks loaded (values and row
 // nodes) before their ballots so that each warp keeps 2 KB in flight.
-template <int P>
+template <int P, bool KEEP>
 __global__ void k_compact(const double *__restrict__ nz, const int64_t *__restrict__ colptr,
                           const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
                           int64_t ndof, const int64_t *__restrict__ outptr,
@@ -510,7 +526,7 @@ __global__ void k_compact(const double *__restrict__ nz, const int64_t *__restri
       }
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const bool keep = (l0 + u * 32 + lane < len) && nonzero_bits(v[u]);
+        const bool keep = (l0 + u * 32 + lane < len) && (KEEP || nonzero_bits(v[u]));
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
         if (keep) {
           const int off = __popc(bal & ((1u << lane) - 1u));
@@ -633,7 +649,7 @@ int run_elem(llf_ctx *ctx, ElemArgs a) {
 // pattern's own, or those of another element set on the same nodes).
 template <int P, bool BV, class T>
 int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,
-                  int npe, const T *Kf, int64_t cs, double *nz, int64_t *cnt) {
+                  int npe, const T *Kf, int64_t cs, const double *init, double *nz, int64_t *cnt) {
   if (pat->conn_version != pat->mesh->conn_version)
     return llf_fail(ctx, LLF_ERR_STATE, "the mesh connectivity changed after the pattern was built; rebuild it");
   const int md = pat->max_deg > 0 ? pat->max_deg : 1;
@@ -653,7 +669,7 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const 
   if (grid > need) grid = need > 0 ? need : 1;
   KernelScope ks(ctx, "k_colgather");
   fn<<<(unsigned)grid, wpb * 32, smem, ctx->stream>>>(pat->d_nptr, n2e_ptr, n2e, pos, Kf, cs, npe, pat->mesh->non, md,
-                                                      nz, cnt);
+                                                      init, nz, cnt);
   LLF_CUDA_TRY(ctx, cudaGetLastError());
   return LLF_OK;
 }
@@ -663,31 +679,31 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const 
 // ------------------------------------------------------------------ host
 template <class T>
 int gather_full_t(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,
-                  int npe, const T *Kf, int64_t cs, bool blockval, double *nz, int64_t *cnt) {
+                  int npe, const T *Kf, int64_t cs, bool blockval, const double *init, double *nz, int64_t *cnt) {
   switch (pat->pdim * 2 + (blockval ? 1 : 0)) {
-    case 2: return run_colgather<1, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, nz, cnt);
-    case 3: return run_colgather<1, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, nz, cnt);
-    case 4: return run_colgather<2, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, nz, cnt);
-    case 5: return run_colgather<2, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, nz, cnt);
-    case 6: return run_colgather<3, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, nz, cnt);
-    case 7: return run_colgather<3, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, nz, cnt);
+    case 2: return run_colgather<1, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt);
+    case 3: return run_colgather<1, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt);
+    case 4: return run_colgather<2, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt);
+    case 5: return run_colgather<2, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt);
+    case 6: return run_colgather<3, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt);
+    case 7: return run_colgather<3, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt);
   }
   return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
 }
 
 int gather_full(llf_ctx *ctx, llf_pattern *pat, const double *Kf, int64_t colstride, bool blockval,
-                double *nz, int64_t *cnt) {
+                double *nz, int64_t *cnt, const double *init) {
   return gather_full_t<double>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, colstride,
-                               blockval, nz, cnt);
+                               blockval, init, nz, cnt);
 }
 int gather_full32(llf_ctx *ctx, llf_pattern *pat, const float *Kf, int64_t colstride, bool blockval,
-                  double *nz, int64_t *cnt) {
+                  double *nz, int64_t *cnt, const double *init) {
   return gather_full_t<float>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, colstride,
-                              blockval, nz, cnt);
+                              blockval, init, nz, cnt);
 }
 int gather_full_ext(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,
                     int npe, const double *Kf, int64_t colstride, bool blockval, double *nz, int64_t *cnt) {
-  return gather_full_t<double>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, colstride, blockval, nz, cnt);
+  return gather_full_t<double>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, colstride, blockval, nullptr, nz, cnt);
 }
 
 int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts) {
@@ -695,11 +711,15 @@ int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts) {
   const int64_t n = pat->ndof;
   cudaStream_t s = ctx->stream;
   int64_t *cnt = counts;
-  if (!cnt || m->diagonal_only) {
+  const bool keep = m->keep_pattern && !m->diagonal_only;
+  if (!cnt || m->diagonal_only || keep) {
     cnt = nullptr;
     LLF_CUDA_TRY(ctx, dalloc(ctx, &cnt, n + 1));
     LLF_CUDA_TRY(ctx, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (n + 1), s));
-    if (m->diagonal_only) {
+    if (keep) {
+      KernelScope ks(ctx, "k_count_struct");
+      k_count_struct<<<grid_1d(n, 256, ctx->num_sms), 256, 0, s>>>(pat->d_colptr, n, cnt);
+    } else if (m->diagonal_only) {
       KernelScope ks(ctx, "k_diag_stored");
       k_diag_stored<<<grid_1d(n, 256, ctx->num_sms), 256, 0, s>>>(m->d_diag, n, cnt);
     } else {
@@ -730,9 +750,13 @@ int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts) {
     unsigned g = grid_1d(n * 32, 256, ctx->num_sms);
     KernelScope ks(ctx, "k_compact");
     switch (pat->pdim) {
-      case 1: k_compact<1><<<g, 256, 0, s>>>(m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, n, ptr0, m->d_rowval_s, m->d_nzval_s); break;
-      case 2: k_compact<2><<<g, 256, 0, s>>>(m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, n, ptr0, m->d_rowval_s, m->d_nzval_s); break;
-      case 3: k_compact<3><<<g, 256, 0, s>>>(m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, n, ptr0, m->d_rowval_s, m->d_nzval_s); break;
+#define LLF_COMPACT(PP, KK) \
+  k_compact<PP, KK><<<g, 256, 0, s>>>(m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, n, ptr0, m->d_rowval_s, \
+                                      m->d_nzval_s)
+      case 1: if (keep) LLF_COMPACT(1, true); else LLF_COMPACT(1, false); break;
+      case 2: if (keep) LLF_COMPACT(2, true); else LLF_COMPACT(2, false); break;
+      case 3: if (keep) LLF_COMPACT(3, true); else LLF_COMPACT(3, false); break;
+#undef LLF_COMPACT
       default: return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
     }
   }
@@ -749,7 +773,7 @@ int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts) {
 
 int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int ptype,
                   const double *c1, const double *c2, int nmat, int form, int lumped,
-                  llf_matrix *m) {
+                  llf_matrix *m, const double *init) {
   (void)ptype;
   const int dim = mesh->dim;
   const int npe = mesh->npe;
@@ -785,7 +809,7 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
   }
   int rc = LLF_OK;
   if (form == LLF_FP32Q) {
-    rc = assemble_fp32_impl(ctx, mesh, pat, kind, d_c1, d_c2, aflag, ageo, m->d_nz, cnt);
+    rc = assemble_fp32_impl(ctx, mesh, pat, kind, d_c1, d_c2, aflag, ageo, m->d_nz, cnt, init);
   } else {
     double *Kf = nullptr;
     const int64_t cs = kf_colstride(npe, BS, (int)sizeof(double));
@@ -819,7 +843,7 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
       else if (kind == KIND_HEAT) rc = run_elem<KIND_HEAT, 2>(ctx, a);
       else rc = run_elem<KIND_MASS, 2>(ctx, a);
     }
-    if (rc == LLF_OK) rc = gather_full(ctx, pat, Kf, cs, kind == KIND_ELASTIC, m->d_nz, cnt);
+    if (rc == LLF_OK) rc = gather_full(ctx, pat, Kf, cs, kind == KIND_ELASTIC, m->d_nz, cnt, init);
     dfree(ctx, Kf);
   }
   dfree(ctx, d_c1);

@@ -314,7 +314,7 @@ int run_elem32(llf_ctx *ctx, Elem32Args a) {
 // per-column non-zero counts into cnt).
 int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, const double *d_c1,
                        const double *d_c2, const uint8_t *aflag, const double *ageo, double *nz,
-                       int64_t *cnt) {
+                       int64_t *cnt, const double *init) {
   const int npe = mesh->npe, P = pat->pdim;
   const int BS = (kind == KIND_ELASTIC) ? P * P : 1;
   float *Kf = nullptr;
@@ -347,7 +347,7 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
   else
     rc = kind == KIND_ELASTIC ? run_elem32<KIND_ELASTIC, 2>(ctx, a)
                               : (kind == KIND_HEAT ? run_elem32<KIND_HEAT, 2>(ctx, a) : run_elem32<KIND_MASS, 2>(ctx, a));
-  if (rc == LLF_OK) rc = gather_full32(ctx, pat, Kf, cs, kind == KIND_ELASTIC, nz, cnt);
+  if (rc == LLF_OK) rc = gather_full32(ctx, pat, Kf, cs, kind == KIND_ELASTIC, nz, cnt, init);
   dfree(ctx, Kf);
   return rc;
 }

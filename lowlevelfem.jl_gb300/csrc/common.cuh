@@ -128,6 +128,7 @@ struct llf_matrix {
   llf_pattern *pat = nullptr;
   double *d_nz = nullptr;         // structural values (pattern->nnz)
   bool diagonal_only = false;     // lumped mass: values live on the diagonal
+  bool keep_pattern = false;      // stored form keeps every structural entry (no dropzeros!)
   double *d_diag = nullptr;       // ndof (diagonal_only)
   // stored (dropzeros'ed) form, SparseMatrixCSC arrays, 1-based
   int64_t nnz_s = 0;
@@ -181,9 +182,11 @@ int build_n2e(llf_ctx *ctx, const int32_t *conn, const int32_t *emat, int64_t ne
               int64_t non, int64_t **ptr, int2 **list, int *max_len);
 
 // assemble.cu
+// init (device, structural values of the pattern, or null): the assembly adds
+// into these values instead of starting from zero (the DSL's csc_matrix).
 int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
                   int ptype, const double *c1, const double *c2, int nmat,
-                  int form, int lumped, llf_matrix *m);
+                  int form, int lumped, llf_matrix *m, const double *init = nullptr);
 // dropzeros -> stored form; counts (non-zeros per DoF column) may come from
 // the gather, else they are counted here
 int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts);
@@ -191,7 +194,7 @@ int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts);
 // aflag/ageo: per-element affine flag and invJ/det (null: quadrature form only)
 int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
                        const double *d_c1, const double *d_c2, const uint8_t *aflag,
-                       const double *ageo, double *nz, int64_t *cnt);
+                       const double *ageo, double *nz, int64_t *cnt, const double *init = nullptr);
 // Element-ordered column-node gather of whole element matrices laid out as
 // Kf[element][column node][row node][block] (blockval: pdim x pdim blocks,
 // entry (i,j) at i*pdim+j; otherwise one scalar per node pair placed on the
@@ -199,9 +202,9 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
 // (colstride >= npe*block size, in elements).  Writes the structural values
 // and, if cnt != NULL, the non-zero count of every DoF column.
 int gather_full(llf_ctx *ctx, llf_pattern *pat, const double *Kf, int64_t colstride, bool blockval,
-                double *nz, int64_t *cnt);
+                double *nz, int64_t *cnt, const double *init = nullptr);
 int gather_full32(llf_ctx *ctx, llf_pattern *pat, const float *Kf, int64_t colstride, bool blockval,
-                  double *nz, int64_t *cnt);
+                  double *nz, int64_t *cnt, const double *init = nullptr);
 // The same gather for another element set on the pattern's nodes (e.g.
 // boundary faces): its node -> element lists, element-to-column map and npe.
 int gather_full_ext(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,

@@ -56,6 +56,9 @@
 #define PT_PLANE_STRAIN 2
 #define PT_HEAT 3
 #define PT_PLANE_HEAT 4
+/* DSL forms (src/multifield.jl): coefficients given as they are (ELASTIC:
+ * lambda, mu; HEAT: k; MASS: c), b = 1 */
+#define PT_LAME (-1)
 
 /* ------------------------------------------------------------------------ */
 /* Material constants: elastic_constants (src/general.jl:142-203) and the    */
@@ -609,12 +612,17 @@ static orc_csc *orc_lump(const orc_csc *M) {
 /*   params: per material (ELASTIC: E, nu; HEAT: k; MASS: rho), stride np.   */
 /* Returns NULL on a non-positive Jacobian (status in *err).                 */
 /* ------------------------------------------------------------------------ */
-orc_csc *orc_assemble(int kind, int ptype, int dim, int pdim, int64_t non,
-                      const double *xyz, int64_t nel, int npe,
-                      const int32_t *conn, const int32_t *emat, int nip,
-                      const double *w, const double *N, const double *dN,
-                      const double *params, int nmat, double thickness,
-                      int lumped, const double *nref, int *err) {
+/* With init (a CSC of the full structural pattern, 0-based arrays icp,
+ * irv, values inz) its entries go first as triplets and no zeros are
+ * dropped: the DSL's ∫(...; csc_matrix=K), which adds into K.nzval in
+ * element order and keeps K's pattern (src/multifield.jl:5280-5346). */
+orc_csc *orc_assemble_ex(int kind, int ptype, int dim, int pdim, int64_t non,
+                         const double *xyz, int64_t nel, int npe,
+                         const int32_t *conn, const int32_t *emat, int nip,
+                         const double *w, const double *N, const double *dN,
+                         const double *params, int nmat, double thickness,
+                         int lumped, const double *nref, const int64_t *icp,
+                         const int64_t *irv, const double *inz, int *err) {
   (void)nmat;
   size_t nd = (size_t)pdim * npe;
   double *Ke = (double *)malloc(sizeof(double) * nd * nd);
@@ -625,12 +633,18 @@ orc_csc *orc_assemble(int kind, int ptype, int dim, int pdim, int64_t non,
   coo c = {0};
   c.n = non * pdim;
   *err = 0;
+  if (icp)
+    for (int64_t j = 0; j < non * pdim; ++j)
+      for (int64_t k = icp[j]; k < icp[j + 1]; ++k) coo_push(&c, irv[k], j, inz[k]);
   for (int64_t e = 0; e < nel; ++e) {
     int mat = emat ? emat[e] : 0;
     if (mat < 0) continue;
     double c1 = 0, c2 = 0;
     double b = (ptype == PT_PLANE_STRESS || ptype == PT_HEAT || ptype == PT_PLANE_HEAT) ? thickness : 1.0;
-    if (kind == ORC_ELASTIC) {
+    if (kind == ORC_ELASTIC && ptype == PT_LAME) {
+      c1 = params[2 * mat];
+      c2 = params[2 * mat + 1];
+    } else if (kind == ORC_ELASTIC) {
       orc_lame(ptype, params[2 * mat], params[2 * mat + 1], thickness, &c1, &c2);
     } else if (kind == ORC_HEAT) {
       c1 = params[mat] * b;
@@ -663,8 +677,18 @@ orc_csc *orc_assemble(int kind, int ptype, int dim, int pdim, int64_t non,
     orc_free(m);
     m = D;
   }
-  orc_dropzeros(m);
+  if (!icp) orc_dropzeros(m);
   return m;
+}
+
+orc_csc *orc_assemble(int kind, int ptype, int dim, int pdim, int64_t non,
+                      const double *xyz, int64_t nel, int npe,
+                      const int32_t *conn, const int32_t *emat, int nip,
+                      const double *w, const double *N, const double *dN,
+                      const double *params, int nmat, double thickness,
+                      int lumped, const double *nref, int *err) {
+  return orc_assemble_ex(kind, ptype, dim, pdim, non, xyz, nel, npe, conn, emat, nip, w, N, dN, params, nmat,
+                         thickness, lumped, nref, NULL, NULL, NULL, err);
 }
 
 /* ------------------------------------------------------------------------ */

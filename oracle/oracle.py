@@ -69,6 +69,9 @@ def lib():
         L.orc_num_threads.restype = i32
         L.orc_support_matrix.restype = vp
         L.orc_support_matrix.argtypes = [i32, i32, i64, Pd, i64, i32, Pi32, i32, Pd, Pd, Pd, Pd, Pd, dbl]
+        L.orc_assemble_ex.restype = vp
+        L.orc_assemble_ex.argtypes = [i32, i32, i32, i32, i64, Pd, i64, i32, Pi32, Pi32, i32, Pd, Pd, Pd, Pd, i32,
+                                      dbl, i32, Pd, Pi64, Pi64, Pd, C.POINTER(C.c_int)]
         L.orc_load_vector_follower.restype = i32
         L.orc_load_vector_follower.argtypes = [Pd, i64, i32, Pi32, i32, Pd, Pd, Pd, Pd, Pd, Pd, Pd]
         L.orc_follower_tangent.restype = vp
@@ -158,8 +161,14 @@ def pattern(non, conn, pdim, emat=None):
     return CSC(h)
 
 
-def assemble(kind, ptype, dim, pdim, xyz, conn, rule, params, thickness=1.0, lumped=False, emat=None, affine=True):
-    """Reference-order COO assembly + sparse + dropzeros! (see llfem_oracle.c)."""
+PT_LAME = -1   # DSL forms: params are the coefficients themselves (lambda, mu / k / c), b = 1
+
+
+def assemble(kind, ptype, dim, pdim, xyz, conn, rule, params, thickness=1.0, lumped=False, emat=None, affine=True,
+             init=None):
+    """Reference-order COO assembly + sparse + dropzeros! (see llfem_oracle.c).
+    init: (colptr, rowval, nzval) 0-based arrays of a matrix with the full
+    structural pattern, whose values the assembly adds into (no dropzeros!)."""
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
     conn0 = _conn0(conn)
     params = np.ascontiguousarray(params, dtype=np.float64).ravel()
@@ -170,11 +179,14 @@ def assemble(kind, ptype, dim, pdim, xyz, conn, rule, params, thickness=1.0, lum
     err = C.c_int(0)
     nmat = 1
     nref = None if rule.get("node_ref") is None or not affine else np.ascontiguousarray(rule["node_ref"], dtype=np.float64)
-    h = lib().orc_assemble(kind, ptype, dim, pdim, xyz.shape[0], _p(xyz, C.c_double), conn0.shape[0],
-                           conn0.shape[1], _p(conn0, C.c_int32), _p(em, C.c_int32), len(w),
-                           _p(w, C.c_double), _p(N, C.c_double), _p(dN, C.c_double),
-                           _p(params, C.c_double), nmat, float(thickness), int(lumped), _p(nref, C.c_double),
-                           C.byref(err))
+    icp = irv = inz = None
+    if init is not None:
+        icp, irv, inz = (np.ascontiguousarray(a, dtype=t) for a, t in zip(init, (np.int64, np.int64, np.float64)))
+    h = lib().orc_assemble_ex(kind, ptype, dim, pdim, xyz.shape[0], _p(xyz, C.c_double), conn0.shape[0],
+                              conn0.shape[1], _p(conn0, C.c_int32), _p(em, C.c_int32), len(w),
+                              _p(w, C.c_double), _p(N, C.c_double), _p(dN, C.c_double),
+                              _p(params, C.c_double), nmat, float(thickness), int(lumped), _p(nref, C.c_double),
+                              _p(icp, C.c_int64), _p(irv, C.c_int64), _p(inz, C.c_double), C.byref(err))
     if not h:
         raise ValueError("oracle: non-positive Jacobian determinant")
     return CSC(h)
