@@ -546,27 +546,48 @@ def main():
         Km = assemble()
         nnz_s = Km.nnz()
         del Km
+        # capacity = structural nnz, as a caller sizes them before the call
         colptr_h = torch.empty(3 * mesh.non + 1, dtype=torch.int64).pin_memory()
-        rowval_h = torch.empty(nnz_s, dtype=torch.int64).pin_memory()
-        nzval_h = torch.empty(nnz_s, dtype=torch.float64).pin_memory()
+        rowval_h = torch.empty(pat.nnz, dtype=torch.int64).pin_memory()
+        nzval_h = torch.empty(pat.nnz, dtype=torch.float64).pin_memory()
         P = lambda t, ct: L.C.cast(t.data_ptr(), L.C.POINTER(ct))
         e2e_steps = max(2, min(args.steps, 3))
-        ts = []
-        for i in range(1 + e2e_steps):
-            ctx.sync()
-            t0 = time.perf_counter()
-            ctx.check(L.lib().llf_mesh_update(ctx.h, dm.h, P(xyz_h, L.C.c_double), P(conn_h, L.C.c_int64)))
+        got = L.C.c_int64(0)
+
+        def to_host_fused():
+            # one call: assembly with each column slab copied out behind the next
+            ctx.check(L.lib().llf_assemble_stiffness_csc(
+                ctx.h, dm.h, pat.h, L.SOLID, L.ptr(Ea, L.C.c_double), L.ptr(nua, L.C.c_double), 1, 1.0, form,
+                pat.nnz, P(colptr_h, L.C.c_int64), P(rowval_h, L.C.c_int64), P(nzval_h, L.C.c_double),
+                L.C.byref(got)))
+
+        def to_host_two_calls():
             Km = assemble()
             ctx.check(L.lib().llf_matrix_copy_csc(ctx.h, Km.h, P(colptr_h, L.C.c_int64),
                                                   P(rowval_h, L.C.c_int64), P(nzval_h, L.C.c_double)))
-            t1 = time.perf_counter()
             del Km
-            if i > 0:
-                ts.append(t1 - t0)
-        te = statistics.median(ts)
+
+        def time_e2e(fn):
+            ts = []
+            for i in range(1 + e2e_steps):
+                ctx.sync()
+                t0 = time.perf_counter()
+                ctx.check(L.lib().llf_mesh_update(ctx.h, dm.h, P(xyz_h, L.C.c_double), P(conn_h, L.C.c_int64)))
+                fn()
+                t1 = time.perf_counter()
+                if i > 0:
+                    ts.append(t1 - t0)
+            return statistics.median(ts)
+
+        te = time_e2e(to_host_fused)
+        assert got.value == nnz_s
+        te2 = time_e2e(to_host_two_calls)
         e2e = {"value": nnz / te / 1e9, "unit": "GNNZ/s", "ms_per_step": te * 1e3,
                "h2d_bytes_per_step": xyz_h.numel() * 8 + conn_h.numel() * 8,
-               "d2h_bytes_per_step": colptr_h.numel() * 8 + 2 * nnz_s * 8}
+               "d2h_bytes_per_step": colptr_h.numel() * 8 + 2 * nnz_s * 8,
+               "call": "llf_mesh_update + llf_assemble_stiffness_csc (pinned host arrays)",
+               "two_call_ms_per_step": te2 * 1e3,
+               "two_call": "llf_mesh_update + llf_assemble_stiffness + llf_matrix_copy_csc"}
 
     # the other arithmetic form on the same workload (reported beside the headline)
     other = None

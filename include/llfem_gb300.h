@@ -218,6 +218,21 @@ int llf_assemble_stiffness(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
                            int nmat, double thickness, int form,
                            llf_matrix **out);
 
+/* stiffnessMatrix straight into the host arrays of a
+ * SparseMatrixCSC{Float64,Int64} — the same result, bit for bit, as
+ * llf_assemble_stiffness followed by llf_matrix_copy_csc, in one call whose
+ * device-to-host copy of each column slab overlaps the gather and
+ * compaction of the next (the copy is the largest cost of the pair).
+ * rowval and nzval hold `capacity` entries, at least the pattern's
+ * structural nnz (llf_pattern_info); *nnz receives the stored count (the
+ * Julia side resize!s the arrays to it).  colptr[ndof+1].  Page-locked host
+ * arrays let the copies run asynchronously. */
+int llf_assemble_stiffness_csc(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
+                               int ptype, const double *E, const double *nu,
+                               int nmat, double thickness, int form,
+                               int64_t capacity, int64_t *colptr,
+                               int64_t *rowval, double *nzval, int64_t *nnz);
+
 /* M = rho b sum H^T H detJ w, consistent (lumped == 0) or row-sum lumped —
  * massMatrix / massMatrixSolid, src/linear.jl:1843-2004. */
 int llf_assemble_mass(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,

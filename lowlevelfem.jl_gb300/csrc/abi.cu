@@ -545,6 +545,27 @@ int llf_assemble_stiffness(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int p
   return finish_matrix(ctx, rc, m, out);
 }
 
+int llf_assemble_stiffness_csc(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int ptype, const double *E,
+                               const double *nu, int nmat, double thickness, int form, int64_t capacity,
+                               int64_t *colptr, int64_t *rowval, double *nzval, int64_t *nnz) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!valid_ptype(ptype) || ptype == LLF_HEAT_CONDUCTION || ptype == LLF_PLANE_HEAT_CONDUCTION)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_assemble_stiffness_csc: ptype must be SOLID, PLANE_STRESS or PLANE_STRAIN");
+  int rc = pattern_dim_check(ctx, mesh, pat, ptype);
+  if (rc) return rc;
+  if (pat->pdim != mesh->dim) return llf_fail(ctx, LLF_ERR_STATE, "stiffness needs a pattern with pdim == dim");
+  if (!E || !nu || nmat < 1) return llf_fail(ctx, LLF_ERR_ARG, "material arrays");
+  if (form != LLF_FP64 && form != LLF_FP32Q) return llf_fail(ctx, LLF_ERR_ARG, "form");
+  if (!colptr || !rowval || !nzval || !nnz) return llf_fail(ctx, LLF_ERR_ARG, "llf_assemble_stiffness_csc: null output");
+  if (capacity < pat->nnz)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_assemble_stiffness_csc: capacity must be at least the structural nnz");
+  std::vector<double> c1(nmat), c2(nmat);
+  for (int i = 0; i < nmat; ++i) lame(ptype, E[i], nu[i], thickness, &c1[i], &c2[i]);
+  rc = assemble_to_host_impl(ctx, mesh, pat, KIND_ELASTIC, c1.data(), c2.data(), nmat, form, capacity, colptr,
+                             rowval, nzval, nnz);
+  return rc == LLF_OK ? llf_ok(ctx) : rc;
+}
+
 int llf_assemble_mass(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int ptype,
                       const double *rho, int nmat, double thickness, int lumped, int form,
                       llf_matrix **out) {

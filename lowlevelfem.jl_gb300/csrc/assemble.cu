@@ -649,7 +649,11 @@ int run_elem(llf_ctx *ctx, ElemArgs a) {
 // pattern's own, or those of another element set on the same nodes).
 template <int P, bool BV, class T>
 int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,
-                  int npe, const T *Kf, int64_t cs, const double *init, double *nz, int64_t *cnt) {
+                  int npe, const T *Kf, int64_t cs, const double *init, double *nz, int64_t *cnt,
+                  int64_t B0 = 0, int64_t nB = -1) {
+  // column nodes [B0, B0 + nB): the node-indexed arrays are offset, the
+  // offsets they hold (into n2e, pos, nz) stay absolute
+  if (nB < 0) nB = pat->mesh->non - B0;
   if (pat->conn_version != pat->mesh->conn_version)
     return llf_fail(ctx, LLF_ERR_STATE, "the mesh connectivity changed after the pattern was built; rebuild it");
   const int md = pat->max_deg > 0 ? pat->max_deg : 1;
@@ -665,11 +669,11 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const 
   int per_sm = 1;
   LLF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, wpb * 32, smem));
   int64_t grid = (int64_t)ctx->num_sms * (per_sm < 1 ? 1 : per_sm);
-  int64_t need = (pat->mesh->non + wpb - 1) / wpb;
+  int64_t need = (nB + wpb - 1) / wpb;
   if (grid > need) grid = need > 0 ? need : 1;
   KernelScope ks(ctx, "k_colgather");
-  fn<<<(unsigned)grid, wpb * 32, smem, ctx->stream>>>(pat->d_nptr, n2e_ptr, n2e, pos, Kf, cs, npe, pat->mesh->non, md,
-                                                      init, nz, cnt);
+  fn<<<(unsigned)grid, wpb * 32, smem, ctx->stream>>>(pat->d_nptr + B0, n2e_ptr + B0, n2e, pos, Kf, cs, npe, nB, md,
+                                                      init, nz, cnt ? cnt + B0 * P : nullptr);
   LLF_CUDA_TRY(ctx, cudaGetLastError());
   return LLF_OK;
 }
@@ -773,7 +777,7 @@ int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts) {
 
 int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int ptype,
                   const double *c1, const double *c2, int nmat, int form, int lumped,
-                  llf_matrix *m, const double *init) {
+                  llf_matrix *m, const double *init, GatherSink *sink) {
   (void)ptype;
   const int dim = mesh->dim;
   const int npe = mesh->npe;
@@ -790,7 +794,7 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_c1, c1, sizeof(double) * nmat, cudaMemcpyHostToDevice, s));
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_c2, c2 ? c2 : c1, sizeof(double) * nmat,
                                     cudaMemcpyHostToDevice, s));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nz, pat->nnz));
+  if (!sink) LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nz, pat->nnz));
   // affine geometry of every element (built-in tables only)
   uint8_t *aflag = nullptr;
   double *ageo = nullptr;
@@ -809,7 +813,7 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
   }
   int rc = LLF_OK;
   if (form == LLF_FP32Q) {
-    rc = assemble_fp32_impl(ctx, mesh, pat, kind, d_c1, d_c2, aflag, ageo, m->d_nz, cnt, init);
+    rc = assemble_fp32_impl(ctx, mesh, pat, kind, d_c1, d_c2, aflag, ageo, m->d_nz, cnt, init, sink);
   } else {
     double *Kf = nullptr;
     const int64_t cs = kf_colstride(npe, BS, (int)sizeof(double));
@@ -834,16 +838,31 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
     a.ageo = ageo;
     a.Rp = mesh->d_Rp;
     a.Mp = mesh->d_Mp;
-    if (dim == 3) {
-      if (kind == KIND_ELASTIC) rc = run_elem<KIND_ELASTIC, 3>(ctx, a);
-      else if (kind == KIND_HEAT) rc = run_elem<KIND_HEAT, 3>(ctx, a);
-      else rc = run_elem<KIND_MASS, 3>(ctx, a);
+    // element range [e0, e1): the element-indexed arrays are offset
+    auto elems = [&](int64_t e0, int64_t e1) -> int {
+      ElemArgs b = a;
+      b.conn = a.conn + e0 * npe;
+      b.emat = a.emat ? a.emat + e0 : nullptr;
+      b.nel = e1 - e0;
+      b.Kf = a.Kf + e0 * npe * cs;
+      b.aflag = a.aflag ? a.aflag + e0 : nullptr;
+      b.ageo = a.ageo ? a.ageo + e0 * 10 : nullptr;
+      if (b.nel <= 0) return LLF_OK;
+      if (dim == 3) {
+        if (kind == KIND_ELASTIC) return run_elem<KIND_ELASTIC, 3>(ctx, b);
+        if (kind == KIND_HEAT) return run_elem<KIND_HEAT, 3>(ctx, b);
+        return run_elem<KIND_MASS, 3>(ctx, b);
+      }
+      if (kind == KIND_ELASTIC) return run_elem<KIND_ELASTIC, 2>(ctx, b);
+      if (kind == KIND_HEAT) return run_elem<KIND_HEAT, 2>(ctx, b);
+      return run_elem<KIND_MASS, 2>(ctx, b);
+    };
+    if (sink) {
+      rc = sink->gather(ctx, pat, Kf, cs, kind == KIND_ELASTIC, elems);
     } else {
-      if (kind == KIND_ELASTIC) rc = run_elem<KIND_ELASTIC, 2>(ctx, a);
-      else if (kind == KIND_HEAT) rc = run_elem<KIND_HEAT, 2>(ctx, a);
-      else rc = run_elem<KIND_MASS, 2>(ctx, a);
+      rc = elems(0, mesh->nel);
+      if (rc == LLF_OK) rc = gather_full(ctx, pat, Kf, cs, kind == KIND_ELASTIC, m->d_nz, cnt, init);
     }
-    if (rc == LLF_OK) rc = gather_full(ctx, pat, Kf, cs, kind == KIND_ELASTIC, m->d_nz, cnt, init);
     dfree(ctx, Kf);
   }
   dfree(ctx, d_c1);
@@ -851,6 +870,10 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
   dfree(ctx, aflag);
   dfree(ctx, ageo);
   if (rc == LLF_OK) rc = llf_check_status(ctx, "assembly");
+  if (sink) {
+    dfree(ctx, cnt);
+    return rc;
+  }
   if (rc == LLF_OK && kind == KIND_MASS && lumped) {
     m->diagonal_only = true;
     cudaError_t e = dalloc(ctx, &m->d_diag, pat->ndof);
@@ -882,4 +905,218 @@ int matrix_axpby_impl(llf_ctx *ctx, double a, const llf_matrix *A, double b,
   }
   LLF_CUDA_TRY(ctx, cudaGetLastError());
   return matrix_finalize(ctx, C, nullptr);
+}
+
+// ---------------------------------------------------------------- to host
+// Assembly straight into host SparseMatrixCSC arrays.  After the element
+// kernel the columns are processed in NSLAB node slabs on the compute
+// stream: gather (structural values and non-zero counts), scan of the
+// counts continued from the previous slab's end (a device-side carry),
+// compaction and the 1-based column pointers.  Each slab's end offset is
+// copied to pinned host memory behind an event; the host waits for slab s
+// only, then copies its compacted rows and values to the caller's arrays
+// on a second stream while the GPU works on the slabs after it, so the
+// device-to-host copy (the largest cost of the whole call) overlaps all but
+// the first slab of the gather and compaction.  The result is the one
+// llf_assemble_stiffness + llf_matrix_copy_csc give, bit for bit.
+namespace {
+
+__global__ void k_slab_carry(int64_t *__restrict__ outptr, int64_t n, int64_t *__restrict__ carry, int s,
+                             const int64_t *__restrict__ slab_total) {
+  const int64_t c0 = carry[s];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    outptr[i] += c0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) carry[s + 1] = c0 + *slab_total;
+}
+
+// d_max[k] = 1 + the largest element index in the lists of the nodes of
+// slab k (B[k] <= node < B[k+1]); lists are sorted, so the last entry.
+__global__ void k_slab_last_elem(const int64_t *__restrict__ n2e_ptr, const int2 *__restrict__ n2e, int64_t non,
+                                 const int64_t *__restrict__ B, int nslab, int64_t *__restrict__ d_max) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < non; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = n2e_ptr[v + 1];
+    if (e == n2e_ptr[v]) continue;
+    int k = 0;
+    while (k + 1 < nslab && v >= B[k + 1]) ++k;
+    atomicMax((unsigned long long *)&d_max[k], (unsigned long long)(n2e[e - 1].x + 1));
+  }
+}
+
+__global__ void k_colptr_last(const int64_t *__restrict__ carry, int s, int64_t *__restrict__ colptr_last) {
+  *colptr_last = carry[s] + 1;
+}
+
+struct HostSlabSink : GatherSink {
+  static constexpr int NSLAB = 16;
+  int64_t capacity = 0;
+  int64_t *h_colptr = nullptr, *h_rowval = nullptr;
+  double *h_nzval = nullptr;
+  int64_t nnz = 0;
+
+  template <class T>
+  int run(llf_ctx *ctx, llf_pattern *pat, const T *Kf, int64_t cs, bool blockval, const ElemLauncher &elems) {
+    const int P = pat->pdim;
+    const int64_t non = pat->mesh->non, ndof = pat->ndof;
+    cudaStream_t s = ctx->stream;
+    double *nz = nullptr, *nzval = nullptr;
+    int64_t *cnt = nullptr, *outptr = nullptr, *rowval = nullptr, *colptr = nullptr, *carry = nullptr,
+            *totals = nullptr, *h_end = nullptr;
+    cudaStream_t cp = nullptr;
+    cudaEvent_t ev[NSLAB] = {}, done[NSLAB] = {};
+    int rc = LLF_OK;
+    cudaError_t e = dalloc(ctx, &nz, pat->nnz);
+    if (e == cudaSuccess) e = dalloc(ctx, &cnt, ndof + 1);
+    if (e == cudaSuccess) e = dalloc(ctx, &outptr, ndof + 1);
+    if (e == cudaSuccess) e = dalloc(ctx, &colptr, ndof + 1);
+    if (e == cudaSuccess) e = dalloc(ctx, &rowval, pat->nnz);
+    if (e == cudaSuccess) e = dalloc(ctx, &nzval, pat->nnz);
+    if (e == cudaSuccess) e = dalloc(ctx, &carry, NSLAB + 1);
+    if (e == cudaSuccess) e = dalloc(ctx, &totals, NSLAB);
+    if (e == cudaSuccess) e = cudaMemsetAsync(carry, 0, sizeof(int64_t) * (NSLAB + 1), s);
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&h_end, sizeof(int64_t) * (NSLAB + 1));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cp, cudaStreamNonBlocking);
+    for (int k = 0; k < NSLAB && e == cudaSuccess; ++k) {
+      e = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+    // 1. all slabs on the compute stream, each after the elements it needs
+    int64_t B[NSLAB + 1];
+    for (int k = 0; k <= NSLAB; ++k) B[k] = non * k / NSLAB;
+    if (rc == LLF_OK) rc = slab_elements(ctx, pat, B);
+    int64_t e_done = 0;
+    for (int k = 0; k < NSLAB && rc == LLF_OK; ++k) {
+      const int64_t B0 = B[k], nB = B[k + 1] - B[k], c0 = B0 * P, nc = nB * P;
+      const int64_t e_need = pat->slab_elem_end[k];
+      if (e_need > e_done) {
+        rc = elems(e_done, e_need);
+        if (rc != LLF_OK) break;
+        e_done = e_need;
+      }
+      if (nB > 0) {
+        switch (P * 2 + (blockval ? 1 : 0)) {
+          case 2: rc = run_colgather<1, false, T>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, cs, nullptr, nz, cnt, B0, nB); break;
+          case 3: rc = run_colgather<1, true, T>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, cs, nullptr, nz, cnt, B0, nB); break;
+          case 4: rc = run_colgather<2, false, T>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, cs, nullptr, nz, cnt, B0, nB); break;
+          case 5: rc = run_colgather<2, true, T>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, cs, nullptr, nz, cnt, B0, nB); break;
+          case 6: rc = run_colgather<3, false, T>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, cs, nullptr, nz, cnt, B0, nB); break;
+          case 7: rc = run_colgather<3, true, T>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, cs, nullptr, nz, cnt, B0, nB); break;
+          default: rc = llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
+        }
+        if (rc != LLF_OK) break;
+        {
+          KernelScope ks(ctx, "scan");
+          e = exclusive_scan_i64_dev(ctx, cnt + c0, outptr + c0, nc, totals + k);
+        }
+        if (e != cudaSuccess) { rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e)); break; }
+      } else {
+        cudaMemsetAsync(totals + k, 0, sizeof(int64_t), s);
+      }
+      k_slab_carry<<<grid_1d(std::max<int64_t>(nc, 1), 256, ctx->num_sms), 256, 0, s>>>(outptr + c0, nc, carry, k,
+                                                                                       totals + k);
+      if (nc > 0) {
+        const unsigned g = grid_1d(nc * 32, 256, ctx->num_sms);
+        KernelScope ks(ctx, "k_compact");
+#define LLF_SLAB_COMPACT(PP) \
+  k_compact<PP, false><<<g, 256, 0, s>>>(nz, pat->d_colptr + c0, pat->d_nptr + B0, pat->d_nadj, nc, outptr + c0, \
+                                          rowval, nzval)
+        if (P == 1) LLF_SLAB_COMPACT(1); else if (P == 2) LLF_SLAB_COMPACT(2); else LLF_SLAB_COMPACT(3);
+#undef LLF_SLAB_COMPACT
+        k_colptr_1based<<<grid_1d(nc, 256, ctx->num_sms), 256, 0, s>>>(outptr + c0, nc, colptr + c0);
+      }
+      if (k == NSLAB - 1) k_colptr_last<<<1, 1, 0, s>>>(carry, NSLAB, colptr + ndof);
+      cudaMemcpyAsync(h_end + k + 1, carry + k + 1, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+      cudaEventRecord(ev[k], s);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) { rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e)); break; }
+    }
+    // 2. each slab to the host as soon as it is compacted
+    h_end[0] = 0;
+    for (int k = 0; k < NSLAB && rc == LLF_OK; ++k) {
+      e = cudaEventSynchronize(ev[k]);
+      if (e != cudaSuccess) { rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e)); break; }
+      const int64_t o0 = h_end[k], o1 = h_end[k + 1];
+      if (o1 > capacity) { rc = llf_fail(ctx, LLF_ERR_LIMIT, "llf_assemble_stiffness_csc: capacity too small"); break; }
+      const int64_t c0 = B[k] * P, nc = (B[k + 1] - B[k]) * P + (k == NSLAB - 1 ? 1 : 0);
+      e = cudaStreamWaitEvent(cp, ev[k], 0);
+      if (e == cudaSuccess && nc > 0)
+        e = cudaMemcpyAsync(h_colptr + c0, colptr + c0, sizeof(int64_t) * nc, cudaMemcpyDeviceToHost, cp);
+      if (e == cudaSuccess && o1 > o0)
+        e = cudaMemcpyAsync(h_rowval + o0, rowval + o0, sizeof(int64_t) * (o1 - o0), cudaMemcpyDeviceToHost, cp);
+      if (e == cudaSuccess && o1 > o0)
+        e = cudaMemcpyAsync(h_nzval + o0, nzval + o0, sizeof(double) * (o1 - o0), cudaMemcpyDeviceToHost, cp);
+      if (e == cudaSuccess) e = cudaEventRecord(done[k], cp);
+      if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (cp) {
+      cudaError_t e2 = cudaStreamSynchronize(cp);
+      if (rc == LLF_OK && e2 != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e2));
+    }
+    // the buffers are freed on the compute stream after the copies that read them
+    for (int k = 0; k < NSLAB; ++k)
+      if (done[k]) cudaStreamWaitEvent(s, done[k], 0);
+    if (rc == LLF_OK) nnz = h_end[NSLAB];
+    dfree(ctx, nz);
+    dfree(ctx, cnt);
+    dfree(ctx, outptr);
+    dfree(ctx, colptr);
+    dfree(ctx, rowval);
+    dfree(ctx, nzval);
+    dfree(ctx, carry);
+    dfree(ctx, totals);
+    cudaStreamSynchronize(s);
+    for (int k = 0; k < NSLAB; ++k) {
+      if (ev[k]) cudaEventDestroy(ev[k]);
+      if (done[k]) cudaEventDestroy(done[k]);
+    }
+    if (cp) cudaStreamDestroy(cp);
+    if (h_end) cudaFreeHost(h_end);
+    return rc;
+  }
+  // pat->slab_elem_end for the node slabs B (once per pattern): prefix
+  // maximum over the slabs of the last element in each node's list.
+  static int slab_elements(llf_ctx *ctx, llf_pattern *pat, const int64_t *B) {
+    if ((int)pat->slab_elem_end.size() == NSLAB) return LLF_OK;
+    int64_t *d_B = nullptr, *d_max = nullptr;
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_B, NSLAB + 1));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_max, NSLAB));
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_B, B, sizeof(int64_t) * (NSLAB + 1), cudaMemcpyHostToDevice, ctx->stream));
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_max, 0, sizeof(int64_t) * NSLAB, ctx->stream));
+    k_slab_last_elem<<<grid_1d(pat->mesh->non, 256, ctx->num_sms), 256, 0, ctx->stream>>>(
+        pat->d_n2e_ptr, pat->d_n2e, pat->mesh->non, d_B, NSLAB, d_max);
+    std::vector<int64_t> h(NSLAB);
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), d_max, sizeof(int64_t) * NSLAB, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+    LLF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    dfree(ctx, d_B);
+    dfree(ctx, d_max);
+    for (int k = 1; k < NSLAB; ++k) h[k] = std::max(h[k], h[k - 1]);
+    pat->slab_elem_end = h;
+    return LLF_OK;
+  }
+  int gather(llf_ctx *ctx, llf_pattern *pat, const double *Kf, int64_t cs, bool blockval,
+             const ElemLauncher &elems) override {
+    return run<double>(ctx, pat, Kf, cs, blockval, elems);
+  }
+  int gather(llf_ctx *ctx, llf_pattern *pat, const float *Kf, int64_t cs, bool blockval,
+             const ElemLauncher &elems) override {
+    return run<float>(ctx, pat, Kf, cs, blockval, elems);
+  }
+};
+
+}  // namespace
+
+int assemble_to_host_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, const double *c1,
+                          const double *c2, int nmat, int form, int64_t capacity, int64_t *colptr,
+                          int64_t *rowval, double *nzval, int64_t *nnz) {
+  HostSlabSink sink;
+  sink.capacity = capacity;
+  sink.h_colptr = colptr;
+  sink.h_rowval = rowval;
+  sink.h_nzval = nzval;
+  llf_matrix scratch;
+  scratch.pat = pat;
+  int rc = assemble_impl(ctx, mesh, pat, kind, LLF_SOLID, c1, c2, nmat, form, 0, &scratch, nullptr, &sink);
+  if (rc == LLF_OK) *nnz = sink.nnz;
+  return rc;
 }

@@ -314,7 +314,7 @@ int run_elem32(llf_ctx *ctx, Elem32Args a) {
 // per-column non-zero counts into cnt).
 int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, const double *d_c1,
                        const double *d_c2, const uint8_t *aflag, const double *ageo, double *nz,
-                       int64_t *cnt, const double *init) {
+                       int64_t *cnt, const double *init, GatherSink *sink) {
   const int npe = mesh->npe, P = pat->pdim;
   const int BS = (kind == KIND_ELASTIC) ? P * P : 1;
   float *Kf = nullptr;
@@ -340,14 +340,29 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
   a.ageo = ageo;
   a.Rp = mesh->d_Rpf;
   a.Mp = mesh->d_Mpf;
+  // element range [e0, e1): the element-indexed arrays are offset
+  auto elems = [&](int64_t e0, int64_t e1) -> int {
+    Elem32Args b = a;
+    b.conn = a.conn + e0 * npe;
+    b.emat = a.emat ? a.emat + e0 : nullptr;
+    b.nel = e1 - e0;
+    b.Kf = a.Kf + e0 * npe * cs;
+    b.aflag = a.aflag ? a.aflag + e0 : nullptr;
+    b.ageo = a.ageo ? a.ageo + e0 * 10 : nullptr;
+    if (b.nel <= 0) return LLF_OK;
+    if (mesh->dim == 3)
+      return kind == KIND_ELASTIC ? run_elem32<KIND_ELASTIC, 3>(ctx, b)
+                                  : (kind == KIND_HEAT ? run_elem32<KIND_HEAT, 3>(ctx, b) : run_elem32<KIND_MASS, 3>(ctx, b));
+    return kind == KIND_ELASTIC ? run_elem32<KIND_ELASTIC, 2>(ctx, b)
+                                : (kind == KIND_HEAT ? run_elem32<KIND_HEAT, 2>(ctx, b) : run_elem32<KIND_MASS, 2>(ctx, b));
+  };
   int rc;
-  if (mesh->dim == 3)
-    rc = kind == KIND_ELASTIC ? run_elem32<KIND_ELASTIC, 3>(ctx, a)
-                              : (kind == KIND_HEAT ? run_elem32<KIND_HEAT, 3>(ctx, a) : run_elem32<KIND_MASS, 3>(ctx, a));
-  else
-    rc = kind == KIND_ELASTIC ? run_elem32<KIND_ELASTIC, 2>(ctx, a)
-                              : (kind == KIND_HEAT ? run_elem32<KIND_HEAT, 2>(ctx, a) : run_elem32<KIND_MASS, 2>(ctx, a));
-  if (rc == LLF_OK) rc = gather_full32(ctx, pat, Kf, cs, kind == KIND_ELASTIC, nz, cnt, init);
+  if (sink) {
+    rc = sink->gather(ctx, pat, Kf, cs, kind == KIND_ELASTIC, elems);
+  } else {
+    rc = elems(0, mesh->nel);
+    if (rc == LLF_OK) rc = gather_full32(ctx, pat, Kf, cs, kind == KIND_ELASTIC, nz, cnt, init);
+  }
   dfree(ctx, Kf);
   return rc;
 }

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -122,6 +123,9 @@ struct llf_pattern {
   uint16_t *d_pos = nullptr;
   int conn_version = 0;           // mesh connectivity the pattern was built from
   void *ic_coloring = nullptr;    // node colouring of the IC(0) preconditioner (ic0.cu), on first use
+  // per column slab of the to-host assembly: one past the largest element
+  // index that a node of this or an earlier slab touches (assemble.cu)
+  std::vector<int64_t> slab_elem_end;
 };
 
 struct llf_matrix {
@@ -170,6 +174,8 @@ void dfree(llf_ctx *ctx, T *&p) {
 cudaError_t exclusive_scan_i64(llf_ctx *ctx, const int64_t *in, int64_t *out,
                                int64_t n, int64_t *total_host);
 
+cudaError_t exclusive_scan_i64_dev(llf_ctx *ctx, const int64_t *in, int64_t *out, int64_t n, int64_t *d_total);
+
 // pattern.cu
 int pattern_build_impl(llf_ctx *ctx, llf_mesh *mesh, int pdim, llf_pattern *pat);
 int mesh_convert_conn(llf_ctx *ctx, llf_mesh *mesh, const int64_t *d_conn64);
@@ -182,11 +188,31 @@ int build_n2e(llf_ctx *ctx, const int32_t *conn, const int32_t *emat, int64_t ne
               int64_t non, int64_t **ptr, int2 **list, int *max_len);
 
 // assemble.cu
+// Receives the complete element matrices of an assembly in place of the
+// whole-pattern gather (FP64 or FP32 element matrices, cs values per column).
+// elems(e0, e1) launches the element kernel on elements [e0, e1); the sink
+// calls it so that each element range is ready before the slabs that use it.
+using ElemLauncher = std::function<int(int64_t, int64_t)>;
+struct GatherSink {
+  virtual int gather(llf_ctx *ctx, llf_pattern *pat, const double *Kf, int64_t cs, bool blockval,
+                     const ElemLauncher &elems) = 0;
+  virtual int gather(llf_ctx *ctx, llf_pattern *pat, const float *Kf, int64_t cs, bool blockval,
+                     const ElemLauncher &elems) = 0;
+  virtual ~GatherSink() {}
+};
 // init (device, structural values of the pattern, or null): the assembly adds
 // into these values instead of starting from zero (the DSL's csc_matrix).
+// sink (or null): takes the element matrices; m is then neither gathered
+// nor finalised.
 int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
                   int ptype, const double *c1, const double *c2, int nmat,
-                  int form, int lumped, llf_matrix *m, const double *init = nullptr);
+                  int form, int lumped, llf_matrix *m, const double *init = nullptr,
+                  GatherSink *sink = nullptr);
+// stiffness straight to host CSC arrays, column slabs copied out while the
+// next slab is gathered and compacted (assemble.cu)
+int assemble_to_host_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, const double *c1,
+                          const double *c2, int nmat, int form, int64_t capacity, int64_t *colptr,
+                          int64_t *rowval, double *nzval, int64_t *nnz);
 // dropzeros -> stored form; counts (non-zeros per DoF column) may come from
 // the gather, else they are counted here
 int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts);
@@ -194,7 +220,8 @@ int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts);
 // aflag/ageo: per-element affine flag and invJ/det (null: quadrature form only)
 int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
                        const double *d_c1, const double *d_c2, const uint8_t *aflag,
-                       const double *ageo, double *nz, int64_t *cnt, const double *init = nullptr);
+                       const double *ageo, double *nz, int64_t *cnt, const double *init = nullptr,
+                       GatherSink *sink = nullptr);
 // Element-ordered column-node gather of whole element matrices laid out as
 // Kf[element][column node][row node][block] (blockval: pdim x pdim blocks,
 // entry (i,j) at i*pdim+j; otherwise one scalar per node pair placed on the

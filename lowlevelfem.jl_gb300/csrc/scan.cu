@@ -86,6 +86,15 @@ cudaError_t scan_rec(cudaStream_t s, const int64_t *in, int64_t *out, int64_t n,
 
 }  // namespace
 
+// out[i] = sum_{k<i} in[k]; *d_total (device) receives the sum of all n
+// inputs; nothing synchronises.
+cudaError_t exclusive_scan_i64_dev(llf_ctx *ctx, const int64_t *in, int64_t *out, int64_t n, int64_t *d_total) {
+  cudaError_t e = cudaMemsetAsync(d_total, 0, sizeof(int64_t), ctx->stream);
+  if (e != cudaSuccess) return e;
+  if (n > 0) return scan_rec(ctx->stream, in, out, n, d_total);
+  return cudaGetLastError();
+}
+
 // out[i] = sum_{k<i} in[k]; *total_host (if non-null) receives the sum of all
 // n inputs (synchronising the stream).  in may equal out.
 cudaError_t exclusive_scan_i64(llf_ctx *ctx, const int64_t *in, int64_t *out,

@@ -118,14 +118,24 @@ function fetch(hm::Ptr{Cvoid}, n::Int)
 end
 
 # ---------------------------------------------------------------- assembly
+# One call straight into the SparseMatrixCSC arrays: rowval/nzval sized by the
+# structural nnz, filled while the assembly runs, then resize!d to the
+# stored count.
 function stiffnessMatrix(problem; elements=[], forceOneThread=true)
     m = device_mesh(problem); pat = pattern(problem)
     E = Float64[mat.E for mat in problem.material]; ν = Float64[mat.ν for mat in problem.material]
-    h = Ref{Ptr{Cvoid}}(C_NULL)
-    check(ccall((:llf_assemble_stiffness, LIB), Cint,
-                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Cint, Float64, Cint, Ref{Ptr{Cvoid}}),
-                ctx(), m.h, pat, ptype(problem), E, ν, length(E), problem.thickness, 0, h))
-    return SystemMatrix(fetch(h[], problem.pdim * problem.non), problem)
+    n = problem.pdim * problem.non
+    snnz = Ref{Int64}(0); ndof = Ref{Int64}(0); pd = Ref{Cint}(0)
+    ccall((:llf_pattern_info, LIB), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}, Ref{Cint}), pat, ndof, snnz, pd)
+    colptr = Vector{Int64}(undef, n + 1); rowval = Vector{Int64}(undef, snnz[]); nzval = Vector{Float64}(undef, snnz[])
+    nnz = Ref{Int64}(0)
+    check(ccall((:llf_assemble_stiffness_csc, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Cint, Float64, Cint, Int64,
+                 Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Ref{Int64}),
+                ctx(), m.h, pat, ptype(problem), E, ν, length(E), problem.thickness, 0, snnz[],
+                colptr, rowval, nzval, nnz))
+    resize!(rowval, nnz[]); resize!(nzval, nnz[])
+    return SystemMatrix(SparseMatrixCSC(n, n, colptr, rowval, nzval), problem)
 end
 
 function massMatrix(problem; lumped=true)
