@@ -33,6 +33,11 @@ N_CELLS = 40
 ORDER = 2
 E, NU = 2.1e5, 0.3
 WORKLOAD = "hooke3d-unit-cube-hex27-40x40x40"
+
+
+def workload_name(n):
+    """The workload label for n cells per edge (the headline case is 40)."""
+    return f"hooke3d-unit-cube-hex27-{n}x{n}x{n}"
 # ncu DRAM bytes (read + write) of one FP64 assembly of hex27 16^3 (19,320,201
 # structural nnz): k_affine_geometry 1.3 MB, k_elem_fp64 165.0 MB,
 # k_colgather 338.2 MB, k_compact 417.5 MB
@@ -614,7 +619,7 @@ def main():
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f64" if form == L.FP64 else "f32-quadrature/f64-accumulate",
                "data": "synthetic structured mesh (unit cube)",
-               "config": {"workload": WORKLOAD, "elements": mesh.nel, "dofs": 3 * mesh.non,
+               "config": {"workload": workload_name(args.n), "elements": mesh.nel, "dofs": 3 * mesh.non,
                           "structural_nnz": nnz, "stored_nnz": stored, "form": args.form,
                           "pattern_build_s": pattern_s, "l2": "256 MB buffer written before every timed step",
                           "parallelism": "replicas" if world > 1 else "single"},

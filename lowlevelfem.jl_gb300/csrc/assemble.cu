@@ -387,12 +387,16 @@ __device__ __forceinline__ int nonzero_bits(double v) {
 // a reads block (a, b) of the element's column b = local(B) (one contiguous
 // run of npe blocks, 16-byte padded) and the block's row position from the
 // pattern's element-to-column map, both prefetched one element ahead, and
-// adds the block into the accumulator.  The first element's blocks are
-// stored rather than added: every entry equals the reference's combination
-// of its triplets (first value, then + each later one), signed zeros
-// included, with one FP64 addition fewer.  The column is written out
-// coalesced with its non-zero count: column (B,j) holds the entries (row
-// node t, component i) at P*t + i.
+// adds the block into the accumulator.  A byte per row position records
+// whether the position has a value yet: the first block that reaches a
+// position is stored, later ones are added, and positions that no element
+// reaches are written as -0.0 (the identity of IEEE addition).  Every entry
+// thus equals the reference's combination of its triplets (first value,
+// then + each later one), signed zeros included, with one FP64 addition per
+// contribution after the first only.  With init (values to accumulate into)
+// the accumulator starts from them and every block is added.  The column is
+// written out coalesced with its non-zero count: column (B,j) holds the
+// entries (row node t, component i) at P*t + i.
 template <int P, bool BLOCKVAL, class T>
 __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__restrict__ n2e_ptr,
                             const int2 *__restrict__ n2e, const uint16_t *__restrict__ pos,
@@ -403,6 +407,8 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   constexpr int BS = BLOCKVAL ? P * P : 1;
   double *acc = cg_smem + (size_t)wib * max_deg * P * P;
+  unsigned char *has = reinterpret_cast<unsigned char *>(cg_smem + (size_t)wpb * max_deg * P * P) +
+                       (size_t)wib * ((max_deg + 7) & ~7);
   for (int64_t B = (int64_t)blockIdx.x * wpb + wib; B < non; B += (int64_t)gridDim.x * wpb) {
     const int64_t c0 = nptr[B];
     const int deg = (int)(nptr[B + 1] - c0);
@@ -415,7 +421,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
         acc[(size_t)(r / P) * P * P + j * P + r % P] = src[idx];
       }
     } else {
-      for (int t = lane; t < deg * P * P; t += 32) acc[t] = -0.0;
+      for (int t = lane; t < deg; t += 32) has[t] = 0;
     }
     const bool store_first = init == nullptr;
     __syncwarp();
@@ -438,9 +444,13 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
           for (int m = 0; m < BS; ++m) nxt[m] = v[m];
           tn = pos[(s + k + 1) * npe + lane];
         }
-        if (act && tc != 0xffffu) {
-          if (k == 0 && store_first) add_block<P, BLOCKVAL, true>(acc, (int)tc, cur);  // warp-uniform
-          else add_block<P, BLOCKVAL, false>(acc, (int)tc, cur);
+        if (act && tc != 0xffffu) {  // the lanes of one element hold distinct positions
+          if (store_first && !has[tc]) {
+            add_block<P, BLOCKVAL, true>(acc, (int)tc, cur);
+            has[tc] = 1;
+          } else {
+            add_block<P, BLOCKVAL, false>(acc, (int)tc, cur);
+          }
         }
         __syncwarp();
 #pragma unroll
@@ -454,8 +464,12 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
         for (int a = lane; a < npe; a += 32) {
           const unsigned t = pos[(s + k) * npe + a];
           if (t != 0xffffu) {
-            if (k == 0 && store_first) add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BS);
-            else add_block<P, BLOCKVAL, false>(acc, (int)t, col + (size_t)a * BS);
+            if (store_first && !has[t]) {
+              add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BS);
+              has[t] = 1;
+            } else {
+              add_block<P, BLOCKVAL, false>(acc, (int)t, col + (size_t)a * BS);
+            }
           }
         }
         __syncwarp();
@@ -467,7 +481,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
       int n = 0;
       for (int idx = lane; idx < P * deg; idx += 32) {
         const int t = idx / P, i = idx % P;
-        const double v = acc[(size_t)t * P * P + j * P + i];
+        const double v = (!store_first || has[t]) ? acc[(size_t)t * P * P + j * P + i] : -0.0;
         out[idx] = v;
         n += nonzero_bits(v);
       }
@@ -657,7 +671,7 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const 
   if (pat->conn_version != pat->mesh->conn_version)
     return llf_fail(ctx, LLF_ERR_STATE, "the mesh connectivity changed after the pattern was built; rebuild it");
   const int md = pat->max_deg > 0 ? pat->max_deg : 1;
-  const size_t per_warp = (size_t)md * P * P * sizeof(double);
+  const size_t per_warp = (size_t)md * P * P * sizeof(double) + (size_t)((md + 7) & ~7);
   int wpb = (int)std::min<size_t>(4, (200 * 1024) / per_warp);
   if (wpb < 1) wpb = 1;
   size_t smem = (size_t)wpb * per_warp;
