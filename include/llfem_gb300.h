@@ -398,7 +398,9 @@ int llf_matrix_from_structural(llf_ctx *ctx, llf_pattern *pat, const double *nzv
                                llf_matrix **out);
 
 /* C = a*A + b*B on the same pattern, then dropzeros! — SystemMatrix +/-
- * of src/operators.jl:2421-2486 (Kmat + Kgeo, K - Kext). */
+ * of src/operators.jl:2421-2486 (Kmat + Kgeo, K - Kext).  A lumped
+ * (diagonal) operand adds on the diagonal; two lumped operands give a
+ * lumped result. */
 int llf_matrix_axpby(llf_ctx *ctx, double a, const llf_matrix *A, double b,
                      const llf_matrix *B, llf_matrix **out);
 
@@ -427,6 +429,25 @@ int llf_matrix_destroy(llf_ctx *ctx, llf_matrix *m);
 int llf_pcg(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x,
             const uint8_t *fixed, int precond, double reltol, int64_t maxiter,
             int64_t *iters, double *relres);
+
+/* Transient heat conduction by the theta-method — FDM(K, C, q, bc, T0, n,
+ * dt; ϑ), src/heat.jl:1466-1616.  K (conduction, with any convection added)
+ * and C (capacity, consistent or lumped) on the same pattern.  q[ndof*q_steps]
+ * (q_steps 1 or nsteps, column-major), T[ndof*nsteps] host: on entry column
+ * 0 is the initial state and the fixed entries of every column hold the
+ * prescribed values (applyBoundaryConditions!); on return every column holds
+ * the state at t = i*dt.  theta == 0 with a lumped C takes the reference's
+ * explicit update; otherwise every step solves
+ *   (C + ϑ dt K)_ff T_f^{n+1} = ((C - (1-ϑ) dt K) T^n + dt q^{n+ϑ})_f
+ *                               - (C + ϑ dt K)_fc T_c^{n+1}
+ * by PCG to reltol (the reference uses one LU factorisation), starting from
+ * T^n, with the preconditioner built once.  *iters_total sums the PCG
+ * iterations.  A non-positive diag(C) on a free DoF is an error, as in the
+ * reference. */
+int llf_heat_fdm(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C,
+                 const double *q, int q_steps, double *T, const uint8_t *fixed,
+                 int64_t nsteps, double dt, double theta, int precond,
+                 double reltol, int64_t maxiter, int64_t *iters_total);
 
 /* Largest system (DoFs) llf_pcg_noalloc accepts. */
 #define LLF_NOALLOC_MAX_DOFS 131072

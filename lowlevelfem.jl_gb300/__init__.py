@@ -18,7 +18,7 @@ from .api import (Material, material, elastic_constants, Problem, Field, SystemM
                   heatConductionMatrix, heatCapacityMatrix, elasticSupportMatrix, heatConvectionMatrix,
                   heatConvectionVector, applyElasticSupport_, applyHeatConvection_, externalTangentFollower,
                   elementsToNodes, isElementwise, solveDisplacement,
-                  solveTemperature, solveField, solveFieldBatched, grad,
+                  solveTemperature, solveField, solveFieldBatched, FDM, grad,
                   deformationGradient, materialTangentMatrix, initialStressMatrix, tangentMatrix, solveDeformation,
                   internalForceVector)
 

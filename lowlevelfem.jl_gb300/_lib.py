@@ -72,6 +72,7 @@ SIGNATURES = {
     "llf_assemble_mass": (i32, [vp, vp, vp, i32, P_dbl, i32, dbl, i32, i32, PP]),
     "llf_assemble_heat": (i32, [vp, vp, vp, i32, P_dbl, i32, dbl, i32, PP]),
     "llf_assemble_support": (i32, [vp, vp, vp, P_dbl, P_dbl, dbl, PP]),
+    "llf_heat_fdm": (i32, [vp, vp, vp, P_dbl, i32, P_dbl, P_u8, i64, dbl, dbl, i32, dbl, i64, P_i64]),
     "llf_assemble_stiffness_csc": (i32, [vp, vp, vp, i32, P_dbl, P_dbl, i32, dbl, i32, i64, P_i64, P_i64, P_dbl,
                                          P_i64]),
     "llf_assemble_form": (i32, [vp, vp, vp, i32, P_dbl, P_dbl, i32, vp, i32, PP]),

@@ -760,6 +760,50 @@ def solveTemperature(problem_or_K, q=None, heatFlux=(), temperatureConstraint=()
     return _solve(K, q, list(temperatureConstraint), iterative, reltol, maxiter, preconditioner)
 
 
+def FDM(K: SystemMatrix, C: SystemMatrix, q, bc, TT0, n: int, dt: float, theta: float = 0.5,
+        preconditioner="bjacobi", reltol=DIRECT_RELTOL, maxiter=None):
+    """Transient heat conduction by the theta-method, FDM(K, C, q, bc, TT0,
+    n, Δt; ϑ) (src/heat.jl:1466-1616): n states T(0), T(Δt), ... with
+    (C + ϑΔtK) T^{n+1} = (C − (1−ϑ)ΔtK) T^n + Δt q^{n+ϑ} on the free DoFs, or
+    the explicit update for ϑ = 0 with a lumped C.  The whole time loop runs
+    on the device: the reference's LU back-substitutions become PCG solves to
+    `reltol` with the preconditioner built once.  Returns a field whose `a`
+    holds the n states as columns and `t` the times."""
+    problem = K.model
+    if C.model is not problem or q.model is not problem or TT0.model is not problem:
+        raise ValueError("FDM: K, C, q and TT0 must belong to the same model.")
+    if n < 2:
+        raise ValueError("FDM: n must be at least 2.")
+    if not dt > 0:
+        raise ValueError("FDM: Δt must be positive.")
+    if not 0.0 <= theta <= 1.0:
+        raise ValueError("FDM: ϑ must be between 0 and 1.")
+    ndof = problem.pdim * problem.non
+    qa = np.asarray(q.a, dtype=np.float64).reshape(ndof, -1)
+    if qa.shape[1] not in (1, n):
+        raise ValueError("FDM: number of time steps in q must be 1 or n.")
+    T = np.zeros((n, ndof))                       # row i = the state at step i
+    T[0] = np.asarray(TT0.a, dtype=np.float64).reshape(ndof, -1)[:, 0]
+    u = _field_for(problem, np.zeros(ndof))
+    applyBoundaryConditions_(u, list(bc))
+    fixed = np.zeros(ndof, dtype=np.uint8)
+    cd = constrainedDoFs(problem, list(bc))
+    fixed[cd - 1] = 1
+    T[:, cd - 1] = u.a[cd - 1, 0]                # prescribed in every step, the initial one included
+    qt = np.ascontiguousarray(qa.T)
+    prec = _PRECOND[preconditioner.lower() if isinstance(preconditioner, str) else preconditioner]
+    maxiter = 20 * ndof if maxiter is None else maxiter
+    it = _lib.C.c_int64(0)
+    ctx = problem._ctx
+    ctx.check(_lib.lib().llf_heat_fdm(ctx.h, K.dm.h, C.dm.h, _lib.ptr(qt, _lib.C.c_double), qt.shape[0],
+                                      _lib.ptr(T, _lib.C.c_double), _lib.ptr(fixed, _lib.C.c_uint8), n, float(dt),
+                                      float(theta), prec, float(reltol), int(maxiter), _lib.C.byref(it)), "FDM")
+    out = _field_for(problem, np.ascontiguousarray(T.T))
+    out.t = np.arange(n) * float(dt)
+    out.iterations = it.value
+    return out
+
+
 def solveField(K: SystemMatrix, f, support=(), iterative=False, reltol=SQRT_EPS, maxiter=None,
                preconditioner="identity", ordering=True):
     """solveField(K, f; support, iterative, reltol, maxiter, preconditioner)

@@ -1020,6 +1020,42 @@ int llf_pcg(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x, const
   return rc == LLF_OK ? llf_ok(ctx) : rc;
 }
 
+int llf_heat_fdm(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C, const double *q, int q_steps, double *T,
+                 const uint8_t *fixed, int64_t nsteps, double dt, double theta, int precond, double reltol,
+                 int64_t maxiter, int64_t *iters_total) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!K || !C || !q || !T || !fixed) return llf_fail(ctx, LLF_ERR_ARG, "FDM: null argument");
+  if (K->pat != C->pat) return llf_fail(ctx, LLF_ERR_STATE, "FDM: K and C must belong to the same model.");
+  if (K->diagonal_only) return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "FDM: K must be a full matrix");
+  if (nsteps < 2) return llf_fail(ctx, LLF_ERR_ARG, "FDM: n must be at least 2.");
+  if (q_steps != 1 && q_steps != nsteps) return llf_fail(ctx, LLF_ERR_ARG, "FDM: number of time steps in q must be 1 or n.");
+  if (!(dt > 0)) return llf_fail(ctx, LLF_ERR_ARG, "FDM: Δt must be positive.");
+  if (!(theta >= 0.0 && theta <= 1.0)) return llf_fail(ctx, LLF_ERR_ARG, "FDM: ϑ must be between 0 and 1.");
+  if (precond < LLF_PRECOND_NONE || precond > LLF_PRECOND_IC0)
+    return llf_fail(ctx, LLF_ERR_ARG, "FDM: unknown preconditioner");
+  const int64_t n = K->pat->ndof;
+  double *dq = nullptr, *dT = nullptr;
+  uint8_t *df = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &dq, n * q_steps));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &dT, n * nsteps));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &df, n));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(dq, q, sizeof(double) * n * q_steps, cudaMemcpyHostToDevice, ctx->stream));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(dT, T, sizeof(double) * n * nsteps, cudaMemcpyHostToDevice, ctx->stream));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(df, fixed, n, cudaMemcpyHostToDevice, ctx->stream));
+  int64_t it = 0;
+  int rc = heat_fdm_impl(ctx, K, C, dq, q_steps, dT, df, nsteps, dt, theta, precond, reltol, maxiter, &it);
+  if (iters_total) *iters_total = it;
+  if (rc == LLF_OK) {
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(T, dT, sizeof(double) * n * nsteps, cudaMemcpyDeviceToHost, ctx->stream));
+    LLF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  dfree(ctx, dq);
+  dfree(ctx, dT);
+  dfree(ctx, df);
+  cudaStreamSynchronize(ctx->stream);
+  return rc == LLF_OK ? llf_ok(ctx) : rc;
+}
+
 int llf_pcg_noalloc(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                     const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
                     int64_t *iters, double *relres) {

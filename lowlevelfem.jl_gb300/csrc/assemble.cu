@@ -903,13 +903,51 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
   return rc;
 }
 
+namespace {
+// Structural values of a*X + b*D for a lumped (diagonal) D: off the
+// diagonal a*x, on it fma(b, d, a*x) — the full-full formula with zeros off
+// the diagonal of D.
+__global__ void k_axpby_diag(double a, const double *__restrict__ x, double b, const double *__restrict__ d,
+                             const int64_t *__restrict__ colptr, const int32_t *__restrict__ diagpos, int P,
+                             int64_t ndof, double *__restrict__ z) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ndof; c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t B = c / P;
+    const int j = (int)(c - B * P);
+    const int64_t k = colptr[c] + (int64_t)P * diagpos[B] + j;
+    z[k] = __fma_rn(b, d[c], __dmul_rn(a, x[k]));
+  }
+}
+
+__global__ void k_scale(double a, const double *__restrict__ x, double *__restrict__ z, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    z[i] = __dmul_rn(a, x[i]);
+}
+}  // namespace
+
 int matrix_axpby_impl(llf_ctx *ctx, double a, const llf_matrix *A, double b,
                       const llf_matrix *B, llf_matrix *C) {
   if (A->pat != B->pat)
     return llf_fail(ctx, LLF_ERR_STATE, "axpby: matrices live on different patterns");
-  if (A->diagonal_only || B->diagonal_only)
-    return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "axpby: lumped (diagonal) operands");
   C->pat = A->pat;
+  if (A->diagonal_only && B->diagonal_only) {  // both lumped: a lumped result
+    const int64_t n = A->pat->ndof;
+    C->diagonal_only = true;
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &C->d_diag, n));
+    k_axpby<<<grid_1d(n, 256, ctx->num_sms), 256, 0, ctx->stream>>>(a, A->d_diag, b, B->d_diag, C->d_diag, n);
+    LLF_CUDA_TRY(ctx, cudaGetLastError());
+    return matrix_finalize(ctx, C, nullptr);
+  }
+  if (A->diagonal_only || B->diagonal_only) {  // one lumped operand
+    const llf_matrix *F = A->diagonal_only ? B : A, *D = A->diagonal_only ? A : B;
+    const double af = A->diagonal_only ? b : a, bd = A->diagonal_only ? a : b;
+    const llf_pattern *p = A->pat;
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &C->d_nz, p->nnz));
+    k_scale<<<grid_1d(p->nnz, 256, ctx->num_sms), 256, 0, ctx->stream>>>(af, F->d_nz, C->d_nz, p->nnz);
+    k_axpby_diag<<<grid_1d(p->ndof, 256, ctx->num_sms), 256, 0, ctx->stream>>>(
+        af, F->d_nz, bd, D->d_diag, p->d_colptr, p->d_diagpos, p->pdim, p->ndof, C->d_nz);
+    LLF_CUDA_TRY(ctx, cudaGetLastError());
+    return matrix_finalize(ctx, C, nullptr);
+  }
   int64_t n = A->pat->nnz;
   LLF_CUDA_TRY(ctx, dalloc(ctx, &C->d_nz, n));
   {

@@ -263,6 +263,9 @@ int pcg_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
 int pcg_noalloc_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                      const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
                      int64_t *iters, double *relres);
+int heat_fdm_impl(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C, const double *d_q, int nq, double *d_T,
+                  const uint8_t *d_fixed, int64_t nsteps, double dt, double theta, int precond, double reltol,
+                  int64_t maxiter, int64_t *iters_total);
 int pcg_batched_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                      const uint8_t *d_fixed, int nseg, const int64_t *seg_off, int precond,
                      double reltol, int64_t maxiter, int64_t *iters, double *relres);

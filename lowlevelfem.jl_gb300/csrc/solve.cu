@@ -565,88 +565,117 @@ int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, 
              const IcApply &ic = IcApply());
 int pcg_outcome(llf_ctx *ctx, int nseg, const SegState *hst, int64_t *iters, double *relres);
 
+// Buffers, chunking and preconditioner of the segmented PCG for one matrix
+// and one set of fixed DoFs, built once and reused by every solve with them
+// (the theta-method's time steps solve with the same matrix each step).
+template <int P>
+struct PcgPlan {
+  std::vector<int64_t> cb, ce, sf;
+  std::vector<int32_t> cs;
+  int64_t *d_cb = nullptr, *d_ce = nullptr, *d_sf = nullptr;
+  int32_t *d_cs = nullptr;
+  int *d_active = nullptr;
+  SegState *d_st = nullptr;
+  double *r = nullptr, *z = nullptr, *u = nullptr, *c = nullptr, *xw = nullptr, *pinv = nullptr, *part = nullptr;
+  Ic0Factor icf;
+  IcApply ic;
+  int32_t *d_node_seg = nullptr;
+  int precond = 0, nseg = 0;
+  Seg S{};
+  std::vector<SegState> hst;
+
+  int create(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixed, int nseg_, const int64_t *seg_off,
+             int precond_) {
+    precond = precond_;
+    nseg = nseg_;
+    const llf_pattern *pat = m->pat;
+    const int64_t n = pat->ndof;
+    cudaStream_t s = ctx->stream;
+    // chunks that never straddle a segment
+    sf.assign(nseg + 1, 0);
+    for (int g = 0; g < nseg; ++g) {
+      sf[g] = (int64_t)cb.size();
+      for (int64_t i = seg_off[g]; i < seg_off[g + 1]; i += CHUNK) {
+        cb.push_back(i);
+        ce.push_back(std::min(i + CHUNK, seg_off[g + 1]));
+        cs.push_back(g);
+      }
+    }
+    sf[nseg] = (int64_t)cb.size();
+    const int64_t nch = (int64_t)cb.size();
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_cb, nch));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_ce, nch));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_cs, nch));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_sf, nseg + 1));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_active, 1));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_st, nseg));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &r, n));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &z, n));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &u, n));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &c, n));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &xw, n));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &pinv, precond == LLF_PRECOND_BJACOBI ? n * P : n));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &part, nch));
+    if (nch) {
+      LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_cb, cb.data(), sizeof(int64_t) * nch, cudaMemcpyHostToDevice, s));
+      LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_ce, ce.data(), sizeof(int64_t) * nch, cudaMemcpyHostToDevice, s));
+      LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_cs, cs.data(), sizeof(int32_t) * nch, cudaMemcpyHostToDevice, s));
+    }
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_sf, sf.data(), sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, s));
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_active, 0, sizeof(int), s));
+    S = Seg{d_cb, d_ce, d_cs, d_sf, nch, nseg, d_st, d_active};
+    hst.assign(nseg, SegState{});
+    // IC(0): factor of A with the fixed DoFs as identity rows, node -> system map
+    if (precond == LLF_PRECOND_IC0) {
+      const int64_t non = pat->mesh->non;
+      std::vector<int32_t> ns(non, 0);
+      std::vector<int64_t> seg_nodes(nseg + 1);
+      for (int g = 0; g < nseg; ++g) {
+        seg_nodes[g] = seg_off[g] / P;
+        for (int64_t b = seg_off[g] / P; b < seg_off[g + 1] / P; ++b) ns[b] = g;
+      }
+      seg_nodes[nseg] = non;
+      LLF_CUDA_TRY(ctx, dalloc(ctx, &d_node_seg, non));
+      LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_node_seg, ns.data(), sizeof(int32_t) * non, cudaMemcpyHostToDevice, s));
+      int rc = ic0_factor(ctx, m, d_fixed, seg_nodes, d_node_seg, &icf);
+      if (rc != LLF_OK) return rc;
+      if (dalloc(ctx, &ic.zf, n) != cudaSuccess)
+        return llf_fail(ctx, LLF_ERR_CUDA, "pcg: out of device memory for the IC(0) work vector");
+      ic.f = &icf;
+      ic.node_seg = d_node_seg;
+    }
+    return LLF_OK;
+  }
+
+  int solve(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
+            double reltol, int64_t maxiter, int64_t *iters, double *relres) {
+    int rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, precond, reltol, maxiter,
+                         !ctx->profiling, hst.data(), ic);
+    if (rc != LLF_OK) return rc;
+    return pcg_outcome(ctx, nseg, hst.data(), iters, relres);
+  }
+
+  void destroy(llf_ctx *ctx) {
+    if (precond == LLF_PRECOND_IC0) {
+      ic0_release(ctx, &icf);
+      dfree(ctx, d_node_seg);
+      dfree(ctx, ic.zf);
+    }
+    dfree(ctx, d_cb); dfree(ctx, d_ce); dfree(ctx, d_cs); dfree(ctx, d_sf); dfree(ctx, d_active);
+    dfree(ctx, d_st); dfree(ctx, r); dfree(ctx, z); dfree(ctx, u); dfree(ctx, c); dfree(ctx, xw);
+    dfree(ctx, pinv); dfree(ctx, part);
+  }
+};
+
 template <int P>
 int pcg_segments(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                  const uint8_t *d_fixed, int nseg, const int64_t *seg_off, int precond,
                  double reltol, int64_t maxiter, int64_t *iters, double *relres) {
-  const llf_pattern *pat = m->pat;
-  const int64_t n = pat->ndof;
-  cudaStream_t s = ctx->stream;
-  // chunks that never straddle a segment
-  std::vector<int64_t> cb, ce, sf(nseg + 1);
-  std::vector<int32_t> cs;
-  for (int g = 0; g < nseg; ++g) {
-    sf[g] = (int64_t)cb.size();
-    for (int64_t i = seg_off[g]; i < seg_off[g + 1]; i += CHUNK) {
-      cb.push_back(i);
-      ce.push_back(std::min(i + CHUNK, seg_off[g + 1]));
-      cs.push_back(g);
-    }
-  }
-  sf[nseg] = (int64_t)cb.size();
-  const int64_t nch = (int64_t)cb.size();
-  int64_t *d_cb, *d_ce, *d_sf;
-  int32_t *d_cs;
-  int *d_active;
-  SegState *d_st;
-  double *r, *z, *u, *c, *xw, *pinv, *part;
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_cb, nch));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_ce, nch));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_cs, nch));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_sf, nseg + 1));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_active, 1));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_st, nseg));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &r, n));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &z, n));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &u, n));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &c, n));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &xw, n));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &pinv, precond == LLF_PRECOND_BJACOBI ? n * P : n));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &part, nch));
-  if (nch) {
-    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_cb, cb.data(), sizeof(int64_t) * nch, cudaMemcpyHostToDevice, s));
-    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_ce, ce.data(), sizeof(int64_t) * nch, cudaMemcpyHostToDevice, s));
-    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_cs, cs.data(), sizeof(int32_t) * nch, cudaMemcpyHostToDevice, s));
-  }
-  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_sf, sf.data(), sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, s));
-  LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_active, 0, sizeof(int), s));
-  Seg S{d_cb, d_ce, d_cs, d_sf, nch, nseg, d_st, d_active};
-  std::vector<SegState> hst(nseg);
-  // IC(0): factor of A with the fixed DoFs as identity rows, node -> system map
-  Ic0Factor icf;
-  IcApply ic;
-  int32_t *d_node_seg = nullptr;
-  int rc = LLF_OK;
-  if (precond == LLF_PRECOND_IC0) {
-    const int64_t non = pat->mesh->non;
-    std::vector<int32_t> ns(non, 0);
-    std::vector<int64_t> seg_nodes(nseg + 1);
-    for (int g = 0; g < nseg; ++g) {
-      seg_nodes[g] = seg_off[g] / P;
-      for (int64_t b = seg_off[g] / P; b < seg_off[g + 1] / P; ++b) ns[b] = g;
-    }
-    seg_nodes[nseg] = non;
-    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_node_seg, non));
-    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_node_seg, ns.data(), sizeof(int32_t) * non, cudaMemcpyHostToDevice, s));
-    rc = ic0_factor(ctx, m, d_fixed, seg_nodes, d_node_seg, &icf);
-    if (rc == LLF_OK && dalloc(ctx, &ic.zf, n) != cudaSuccess)
-      rc = llf_fail(ctx, LLF_ERR_CUDA, "pcg: out of device memory for the IC(0) work vector");
-    ic.f = &icf;
-    ic.node_seg = d_node_seg;
-  }
-  if (rc == LLF_OK)
-    rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, precond, reltol, maxiter,
-                     !ctx->profiling, hst.data(), ic);
-  if (precond == LLF_PRECOND_IC0) {
-    ic0_release(ctx, &icf);
-    dfree(ctx, d_node_seg);
-    dfree(ctx, ic.zf);
-  }
-  dfree(ctx, d_cb); dfree(ctx, d_ce); dfree(ctx, d_cs); dfree(ctx, d_sf); dfree(ctx, d_active);
-  dfree(ctx, d_st); dfree(ctx, r); dfree(ctx, z); dfree(ctx, u); dfree(ctx, c); dfree(ctx, xw);
-  dfree(ctx, pinv); dfree(ctx, part);
-  if (rc != LLF_OK) return rc;
-  return pcg_outcome(ctx, nseg, hst.data(), iters, relres);
+  PcgPlan<P> plan;
+  int rc = plan.create(ctx, m, d_fixed, nseg, seg_off, precond);
+  if (rc == LLF_OK) rc = plan.solve(ctx, m, d_b, d_x, d_fixed, reltol, maxiter, iters, relres);
+  plan.destroy(ctx);
+  return rc;
 }
 
 // Runs the CG of every segment of S to completion with caller-provided
@@ -901,4 +930,152 @@ int pcg_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
              int64_t *iters, double *relres) {
   const int64_t off[2] = {0, m->pat->ndof};
   return pcg_batched_impl(ctx, m, d_b, d_x, d_fixed, 1, off, precond, reltol, maxiter, iters, relres);
+}
+
+// ---------------------------------------------------------------- FDM
+// Transient heat by the theta-method — FDM, src/heat.jl:1466-1616.  T holds
+// nsteps columns of ndof values on the device: column 0 the initial state,
+// the fixed entries of every column the prescribed values.
+//  * theta == 0 with a lumped (diagonal) C: the reference's explicit branch,
+//    T1_f = T0_f + (1/c_f) (dt (q^n - K T^n)_f), fixed entries kept;
+//  * otherwise (C + theta dt K) T^{n+1} = (C - (1-theta) dt K) T^n
+//    + dt q^{n+theta} on the free DoFs, with q^{n+theta} = q when q holds one
+//    column and (1-theta) q^n + theta q^{n+1} otherwise; the fixed-DoF
+//    couplings (-A_fc Tc^{n+1} + B_fc Tc^n) come from the masked PCG, which
+//    solves A_ff x_f = b_f - A_fc x_c with b = B T^n + dt q^{n+theta}.  The
+//    reference factorises A once (lu) and back-substitutes each step; here
+//    the PCG plan (buffers, chunking, IC(0) factor) is built once and each
+//    step starts from the previous state.
+namespace {
+
+__global__ void k_fdm_explicit(const double *__restrict__ T0, const double *__restrict__ y,
+                               const double *__restrict__ q, const double *__restrict__ cdiag,
+                               const uint8_t *__restrict__ fixed, double dt, int64_t n, double *__restrict__ T1) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (!fixed[i])
+      T1[i] = __dadd_rn(T0[i], __dmul_rn(__drcp_rn(cdiag[i]), __dmul_rn(dt, __dsub_rn(q[i], y[i]))));
+}
+
+__global__ void k_fdm_rhs(const double *__restrict__ y, const double *__restrict__ q0,
+                          const double *__restrict__ q1, double theta, double dt, int64_t n,
+                          double *__restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double qt = q1 ? __fma_rn(theta, q1[i], __dmul_rn(1.0 - theta, q0[i])) : q0[i];
+    b[i] = __fma_rn(dt, qt, y[i]);
+  }
+}
+
+__global__ void k_fdm_start(const double *__restrict__ Tprev, const uint8_t *__restrict__ fixed, int64_t n,
+                            double *__restrict__ Tnext) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (!fixed[i]) Tnext[i] = Tprev[i];
+}
+
+__global__ void k_diag_of(const double *__restrict__ nz, const int64_t *__restrict__ colptr,
+                          const int32_t *__restrict__ diagpos, int P, int64_t n, double *__restrict__ d) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t B = c / P;
+    const int j = (int)(c - B * P);
+    d[c] = nz[colptr[c] + (int64_t)P * diagpos[B] + j];
+  }
+}
+
+__global__ void k_fdm_check_diag(const double *__restrict__ d, const uint8_t *__restrict__ fixed, int64_t n,
+                                 int *bad) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (!fixed[i] && !(d[i] > 0.0)) atomicAdd(bad, 1);
+}
+
+void free_matrix_arrays(llf_ctx *ctx, llf_matrix *m) {
+  dfree(ctx, m->d_nz); dfree(ctx, m->d_diag); dfree(ctx, m->d_colptr_s);
+  dfree(ctx, m->d_rowval_s); dfree(ctx, m->d_nzval_s);
+}
+
+template <int P>
+int fdm_typed(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C, const double *d_q, int nq, double *d_T,
+              const uint8_t *d_fixed, int64_t nsteps, double dt, double theta, int precond, double reltol,
+              int64_t maxiter, int64_t *iters_total) {
+  const llf_pattern *pat = K->pat;
+  const int64_t n = pat->ndof;
+  cudaStream_t s = ctx->stream;
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * 16));
+  double *cd = nullptr, *y = nullptr, *b = nullptr;
+  int rc = LLF_OK;
+  *iters_total = 0;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &cd, n));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &y, n));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &b, n));
+  // diag(C_ff) > 0 (the reference's check on the free DoFs)
+  if (C->diagonal_only)
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(cd, C->d_diag, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  else
+    k_diag_of<<<g, 256, 0, s>>>(C->d_nz, pat->d_colptr, pat->d_diagpos, P, n, cd);
+  {
+    int *d_bad = nullptr, h_bad = 0;
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_bad, 1));
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_bad, 0, sizeof(int), s));
+    k_fdm_check_diag<<<g, 256, 0, s>>>(cd, d_fixed, n, d_bad);
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&h_bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    dfree(ctx, d_bad);
+    if (h_bad) rc = llf_fail(ctx, LLF_ERR_NUMERIC, "FDM: non-positive diagonal entry detected in Cff on free DOFs.");
+  }
+  if (rc == LLF_OK && theta == 0.0 && C->diagonal_only) {
+    for (int64_t i = 1; i < nsteps && rc == LLF_OK; ++i) {
+      const double *T0 = d_T + (i - 1) * n;
+      rc = spmv_impl(ctx, K, T0, y);
+      if (rc != LLF_OK) break;
+      KernelScope ks(ctx, "k_fdm_explicit");
+      k_fdm_explicit<<<g, 256, 0, s>>>(T0, y, d_q + (nq == 1 ? 0 : (i - 1) * n), cd, d_fixed, dt, n, d_T + i * n);
+    }
+  } else if (rc == LLF_OK) {
+    llf_matrix A, Bm;
+    A.pat = Bm.pat = K->pat;
+    rc = matrix_axpby_impl(ctx, 1.0, C, theta * dt, K, &A);
+    if (rc == LLF_OK) rc = matrix_axpby_impl(ctx, 1.0, C, -((1.0 - theta) * dt), K, &Bm);
+    PcgPlan<P> plan;
+    const int64_t off[2] = {0, n};
+    bool planned = false;
+    if (rc == LLF_OK) {
+      rc = plan.create(ctx, &A, d_fixed, 1, off, precond);
+      planned = true;
+    }
+    for (int64_t i = 1; i < nsteps && rc == LLF_OK; ++i) {
+      const double *T0 = d_T + (i - 1) * n;
+      double *T1 = d_T + i * n;
+      rc = spmv_impl(ctx, &Bm, T0, y);
+      if (rc != LLF_OK) break;
+      {
+        KernelScope ks(ctx, "k_fdm_rhs");
+        k_fdm_rhs<<<g, 256, 0, s>>>(y, d_q + (nq == 1 ? 0 : (i - 1) * n), nq == 1 ? nullptr : d_q + i * n, theta,
+                                    dt, n, b);
+        k_fdm_start<<<g, 256, 0, s>>>(T0, d_fixed, n, T1);
+      }
+      int64_t it = 0;
+      double rr = 0.0;
+      rc = plan.solve(ctx, &A, b, T1, d_fixed, reltol, maxiter, &it, &rr);
+      *iters_total += it;
+    }
+    if (planned) plan.destroy(ctx);
+    free_matrix_arrays(ctx, &A);
+    free_matrix_arrays(ctx, &Bm);
+  }
+  dfree(ctx, cd);
+  dfree(ctx, y);
+  dfree(ctx, b);
+  if (rc == LLF_OK) LLF_CUDA_TRY(ctx, cudaGetLastError());
+  return rc;
+}
+
+}  // namespace
+
+int heat_fdm_impl(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C, const double *d_q, int nq, double *d_T,
+                  const uint8_t *d_fixed, int64_t nsteps, double dt, double theta, int precond, double reltol,
+                  int64_t maxiter, int64_t *iters_total) {
+  switch (K->pat->pdim) {
+    case 1: return fdm_typed<1>(ctx, K, C, d_q, nq, d_T, d_fixed, nsteps, dt, theta, precond, reltol, maxiter, iters_total);
+    case 2: return fdm_typed<2>(ctx, K, C, d_q, nq, d_T, d_fixed, nsteps, dt, theta, precond, reltol, maxiter, iters_total);
+    case 3: return fdm_typed<3>(ctx, K, C, d_q, nq, d_T, d_fixed, nsteps, dt, theta, precond, reltol, maxiter, iters_total);
+  }
+  return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
 }

@@ -396,3 +396,48 @@ def support_matrix(problem_dim, pdim, non, xyz, bconn, rule, k, thickness=1.0, k
                                  _p(c0, C.c_int32), len(w), _p(w, C.c_double), _p(N, C.c_double),
                                  _p(dN, C.c_double), _p(ke, C.c_double), _p(ken, C.c_double), float(thickness))
     return CSC(h)
+
+
+def fdm(K, C, q, fixed, T, dt, theta):
+    """FDM (src/heat.jl:1466-1616) restated with scipy: K, C scipy sparse (C
+    may be diagonal), q (ndof, 1 or n), fixed bool mask, T (n, ndof) with row
+    0 the initial state and the fixed entries of every row prescribed; fills
+    the free entries of rows 1.. .  Explicit branch when theta == 0 and
+    C_ff is diagonal, else one LU of C_ff + theta dt K_ff."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    n = T.shape[0]
+    free = np.flatnonzero(~fixed)
+    fix = np.flatnonzero(fixed)
+    K = sp.csc_matrix(K)
+    C = sp.csc_matrix(C)
+    Kff, Cff = K[free][:, free], C[free][:, free]
+    Kfc, Cfc = K[free][:, fix], C[free][:, fix]
+    q = np.asarray(q).reshape(K.shape[0], -1)
+    qf = lambda i: q[free, 0 if q.shape[1] == 1 else i]
+    d = Cff.diagonal()
+    if not np.all(d > 0):
+        raise ValueError("FDM: non-positive diagonal entry detected in Cff on free DOFs.")
+    T0 = T[0, free].copy()
+    if theta == 0 and (Cff - sp.diags(d)).count_nonzero() == 0:
+        invd = 1.0 / d
+        for i in range(1, n):
+            Tc_n, Tc_np1 = T[i - 1, fix], T[i, fix]
+            r = qf(i - 1) - Kff @ T0 - Kfc @ Tc_n
+            T1 = T0 + invd * (dt * r - Cfc @ (Tc_np1 - Tc_n))
+            T[i, free] = T1
+            T0 = T1
+        return T
+    A = (Cff + theta * dt * Kff).tocsc()
+    B = Cff - (1 - theta) * dt * Kff
+    Afc = Cfc + theta * dt * Kfc
+    Bfc = Cfc - (1 - theta) * dt * Kfc
+    lu = spla.splu(A)
+    for i in range(1, n):
+        Tc_n, Tc_np1 = T[i - 1, fix], T[i, fix]
+        qth = qf(0) if q.shape[1] == 1 else (1 - theta) * qf(i - 1) + theta * qf(i)
+        rhs = B @ T0 + dt * qth - Afc @ Tc_np1 + Bfc @ Tc_n
+        T1 = lu.solve(rhs)
+        T[i, free] = T1
+        T0 = T1
+    return T
