@@ -153,10 +153,13 @@ int upload_affine(llf_ctx *ctx, llf_mesh *m, const double *node_ref) {
                                     ctx->stream));
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_Mp, Mp.data(), sizeof(double) * npairs, cudaMemcpyHostToDevice,
                                     ctx->stream));
-  std::vector<float> Rpf(Rp.begin(), Rp.end()), Mpf(Mp.begin(), Mp.end());
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_Rpf, npairs * 9));
+  // FP32 copy at 12 floats per pair (16-byte rows for the precision form's loads)
+  std::vector<float> Rpf((size_t)npairs * 12, 0.f), Mpf(Mp.begin(), Mp.end());
+  for (size_t pi = 0; pi < (size_t)npairs; ++pi)
+    for (int k = 0; k < 9; ++k) Rpf[pi * 12 + k] = (float)Rp[pi * 9 + k];
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_Rpf, npairs * 12));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_Mpf, npairs));
-  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_Rpf, Rpf.data(), sizeof(float) * npairs * 9, cudaMemcpyHostToDevice,
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_Rpf, Rpf.data(), sizeof(float) * npairs * 12, cudaMemcpyHostToDevice,
                                     ctx->stream));
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_Mpf, Mpf.data(), sizeof(float) * npairs, cudaMemcpyHostToDevice,
                                     ctx->stream));

@@ -157,6 +157,55 @@ __device__ __forceinline__ void affine_coefficients(double *sAff, double c1, dou
   if (lane == 0) sAff[AF_M] = __dmul_rn(c1, det);
 }
 
+// The same coefficients by one thread, rounded to FP32 for the precision
+// form: every value is formed by exactly the operations of
+// affine_coefficients.  out: elastic W[NS*NS] then U[NA*NA]; heat
+// (c1 trV)[NS]; mass c1*det.
+template <int KIND, int DIM>
+__device__ __forceinline__ void affine_coefficients32(const double *geo_e, double c1, double c2, float *out) {
+  constexpr int NS = DIM == 3 ? 6 : 3, NA = DIM == 3 ? 3 : 1;
+  const double *inv = geo_e;
+  const double det = geo_e[9];
+  if (KIND == KIND_MASS) {
+    out[0] = (float)__dmul_rn(c1, det);
+    return;
+  }
+  const double cp = __dadd_rn(c1, c2), cm = __dsub_rn(c1, c2);
+#pragma unroll
+  for (int n = 0; n < NS; ++n) {
+    const int k = sym_k<DIM>(n), l = sym_l<DIM>(n);
+    double V[NS];
+#pragma unroll
+    for (int m = 0; m < NS; ++m) {
+      const int i = sym_k<DIM>(m), j = sym_l<DIM>(m);
+      V[m] = k == l ? __dmul_rn(det, __dmul_rn(inv[k * 3 + i], inv[k * 3 + j]))
+                    : __dmul_rn(det, __fma_rn(inv[k * 3 + i], inv[l * 3 + j],
+                                              __dmul_rn(inv[l * 3 + i], inv[k * 3 + j])));
+    }
+    double tr = __dadd_rn(V[0], V[1]);
+    if (DIM == 3) tr = __dadd_rn(tr, V[2]);
+    if (KIND == KIND_HEAT) {
+      out[n] = (float)__dmul_rn(c1, tr);
+    } else {
+#pragma unroll
+      for (int m = 0; m < NS; ++m) {
+        const double v = __dmul_rn(cp, V[m]);
+        out[m * NS + n] = (float)(m < DIM ? __fma_rn(c2, tr, v) : v);
+      }
+    }
+  }
+  if (KIND == KIND_ELASTIC) {
+#pragma unroll
+    for (int t = 0; t < NA * NA; ++t) {
+      const int m = t / NA, n = t - m * NA;
+      const int i = sym_k<DIM>(DIM + m), j = sym_l<DIM>(DIM + m);
+      const int k = sym_k<DIM>(DIM + n), l = sym_l<DIM>(DIM + n);
+      out[NS * NS + t] = (float)__dmul_rn(cm, __dmul_rn(det, __fma_rn(inv[k * 3 + i], inv[l * 3 + j],
+                                                                     -__dmul_rn(inv[l * 3 + i], inv[k * 3 + j]))));
+    }
+  }
+}
+
 template <int DIM>
 __device__ __forceinline__ void affine_stage(const double *geo_e, double c1, double c2, double *sAff,
                                              unsigned *status) {

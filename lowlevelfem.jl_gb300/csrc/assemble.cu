@@ -406,6 +406,8 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
   extern __shared__ double cg_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   constexpr int BS = BLOCKVAL ? P * P : 1;
+  constexpr int BSTR = kf_bstride(P, BLOCKVAL, (int)sizeof(T));  // stored block stride
+  constexpr bool VEC = sizeof(T) == 4 && BSTR % 4 == 0;           // 16-byte block loads
   double *acc = cg_smem + (size_t)wib * max_deg * P * P;
   unsigned char *has = reinterpret_cast<unsigned char *>(cg_smem + (size_t)wpb * max_deg * P * P) +
                        (size_t)wib * ((max_deg + 7) & ~7);
@@ -427,21 +429,29 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
     __syncwarp();
     if (npe <= 32) {
       const bool act = lane < npe;
-      T cur[BS], nxt[BS];
+      T cur[BSTR], nxt[BSTR];
       unsigned tc = 0xffffu, tn = 0xffffu;
+      auto load_block = [&](const T *v, T *dst) {
+        if constexpr (VEC) {
+#pragma unroll
+          for (int m = 0; m < BSTR; m += 4) {
+            const float4 f = __ldg(reinterpret_cast<const float4 *>(v + m));
+            dst[m] = f.x; dst[m + 1] = f.y; dst[m + 2] = f.z; dst[m + 3] = f.w;
+          }
+        } else {
+#pragma unroll
+          for (int m = 0; m < BS; ++m) dst[m] = v[m];
+        }
+      };
       if (nb > 0 && act) {
         const int2 el = n2e[s];
-        const T *v = Kf + ((size_t)el.x * npe + el.y) * cs + (size_t)lane * BS;
-#pragma unroll
-        for (int m = 0; m < BS; ++m) cur[m] = v[m];
+        load_block(Kf + ((size_t)el.x * npe + el.y) * cs + (size_t)lane * BSTR, cur);
         tc = pos[s * npe + lane];
       }
       for (int k = 0; k < nb; ++k) {  // elements of B, ascending
         if (k + 1 < nb && act) {
           const int2 el = n2e[s + k + 1];
-          const T *v = Kf + ((size_t)el.x * npe + el.y) * cs + (size_t)lane * BS;
-#pragma unroll
-          for (int m = 0; m < BS; ++m) nxt[m] = v[m];
+          load_block(Kf + ((size_t)el.x * npe + el.y) * cs + (size_t)lane * BSTR, nxt);
           tn = pos[(s + k + 1) * npe + lane];
         }
         if (act && tc != 0xffffu) {  // the lanes of one element hold distinct positions
@@ -454,7 +464,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
         }
         __syncwarp();
 #pragma unroll
-        for (int m = 0; m < BS; ++m) cur[m] = nxt[m];
+        for (int m = 0; m < BSTR; ++m) cur[m] = nxt[m];
         tc = tn;
       }
     } else {
@@ -465,10 +475,10 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
           const unsigned t = pos[(s + k) * npe + a];
           if (t != 0xffffu) {
             if (store_first && !has[t]) {
-              add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BS);
+              add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BSTR);
               has[t] = 1;
             } else {
-              add_block<P, BLOCKVAL, false>(acc, (int)t, col + (size_t)a * BS);
+              add_block<P, BLOCKVAL, false>(acc, (int)t, col + (size_t)a * BSTR);
             }
           }
         }

@@ -11,6 +11,8 @@
 #include "common.cuh"
 #include "affine.cuh"
 
+#include <algorithm>
+
 namespace {
 
 constexpr int E32_THREADS = 128;
@@ -31,7 +33,37 @@ struct Elem32Args {
   const uint8_t *aflag;
   const double *ageo;
   const float *Rp, *Mp;
+  // per affine element its FP32 coefficients (k_affine_coeff32), CW floats
+  const float *coef;
 };
+
+constexpr int CW = 48;  // coefficient floats per element (W 36 + U 9, padded)
+constexpr int RPF_STRIDE = 12;  // floats per pair in the FP32 R table (sym 6, anti 3, pad 3)
+
+// Twelve consecutive floats from a 16-byte aligned address.
+__device__ __forceinline__ void load12(const float *p, float *r) {
+#pragma unroll
+  for (int t = 0; t < 12; t += 4) {
+    const float4 f = __ldg(reinterpret_cast<const float4 *>(p + t));
+    r[t] = f.x; r[t + 1] = f.y; r[t + 2] = f.z; r[t + 3] = f.w;
+  }
+}
+
+// One thread per affine element: the FP64 form's coefficients rounded to
+// FP32 (affine_coefficients32), and the determinant check of the staged form.
+template <int KIND, int DIM>
+__global__ void k_affine_coeff32(const double *__restrict__ ageo, const uint8_t *__restrict__ aflag,
+                                 const int32_t *__restrict__ emat, const double *__restrict__ c1,
+                                 const double *__restrict__ c2, int64_t nel, float *__restrict__ coef,
+                                 unsigned *status) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nel; e += (int64_t)gridDim.x * blockDim.x) {
+    const int mat = emat ? emat[e] : 0;
+    if (mat < 0 || !aflag[e]) continue;
+    const double *g = ageo + (size_t)e * 10;
+    if (!(g[9] > 0.0)) atomicOr(status, ST_BAD_JACOBIAN);
+    affine_coefficients32<KIND, DIM>(g, c1[mat], KIND == KIND_ELASTIC ? c2[mat] : 0.0, coef + (size_t)e * CW);
+  }
+}
 
 __device__ __forceinline__ int poff(int a, int npe) { return a * npe - (a * (a - 1)) / 2; }
 __device__ __forceinline__ void pdec(int pi, int npe, int &a, int &b) {
@@ -44,33 +76,50 @@ __device__ __forceinline__ void pdec(int pi, int npe, int &a, int &b) {
   b = a + (pi - poff(a, npe));
 }
 
+// Block (a,b) and its mirror (b,a) at the padded block stride
+// kf_bstride(P, BS > 1, 4); blocks of 4 and 12 floats go out as 16-byte
+// stores (the column stride is a 16-byte multiple).
 template <int P, int BS>
 __device__ __forceinline__ void store_pair32(float *Ke, int64_t cs, int a, int b, const float *blk) {
-  float *ab = Ke + (size_t)b * cs + (size_t)a * BS;
+  constexpr int BSTR = kf_bstride(P, BS > 1, 4);
+  float *ab = Ke + (size_t)b * cs + (size_t)a * BSTR;
+  if constexpr (BSTR % 4 == 0) {
+    float t[BSTR];
 #pragma unroll
-  for (int k = 0; k < BS; ++k) ab[k] = blk[k];
-  if (a != b) {
-    float *ba = Ke + (size_t)a * cs + (size_t)b * BS;
-    if (BS == 1) {
-      ba[0] = blk[0];
-    } else {
+    for (int k = 0; k < BSTR; ++k) t[k] = k < BS ? blk[k] : 0.f;
+#pragma unroll
+    for (int k = 0; k < BSTR; k += 4)
+      *reinterpret_cast<float4 *>(ab + k) = make_float4(t[k], t[k + 1], t[k + 2], t[k + 3]);
+    if (a != b) {
+      float *ba = Ke + (size_t)a * cs + (size_t)b * BSTR;
 #pragma unroll
       for (int i = 0; i < P; ++i)
 #pragma unroll
-        for (int j = 0; j < P; ++j) ba[j * P + i] = blk[i * P + j];
+        for (int j = 0; j < P; ++j) t[j * P + i] = blk[i * P + j];
+#pragma unroll
+      for (int k = 0; k < BSTR; k += 4)
+        *reinterpret_cast<float4 *>(ba + k) = make_float4(t[k], t[k + 1], t[k + 2], t[k + 3]);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < BS; ++k) ab[k] = blk[k];
+    if (a != b) {
+      float *ba = Ke + (size_t)a * cs + (size_t)b * BSTR;
+      ba[0] = blk[0];
     }
   }
 }
 
 // Node-pair blocks of an affine element in FP32: the FP64 form's per-element
-// coefficients (from the FP64 invJ and det) rounded to FP32, then
-// Ksym = W S, Kanti = U A per pair as in the FP64 form.
+// coefficients (from the FP64 invJ and det) rounded to FP32, read from the
+// element's coefficient row cf, then Ksym = W S, Kanti = U A per pair as in
+// the FP64 form.  No shared memory and no barrier: each thread's pairs only.
 template <int KIND, int DIM, int P, int BS>
-__device__ __forceinline__ void affine_pairs32(const Elem32Args &A, const double *sAff, float *Ke) {
+__device__ __forceinline__ void affine_pairs32(const Elem32Args &A, const float *__restrict__ cf, float *Ke) {
   constexpr int NS = DIM == 3 ? 6 : 3, NA = DIM == 3 ? 3 : 1;
   const int npe = A.npe;
   if (KIND == KIND_MASS) {
-    const float cm = (float)sAff[AF_M];
+    const float cm = __ldg(cf);
     for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
       int a, b;
       pdec(pi, npe, a, b);
@@ -81,33 +130,41 @@ __device__ __forceinline__ void affine_pairs32(const Elem32Args &A, const double
   } else if (KIND == KIND_HEAT) {
     float Q[NS];
 #pragma unroll
-    for (int n = 0; n < NS; ++n) Q[n] = (float)sAff[AF_Q + n];
+    for (int n = 0; n < NS; ++n) Q[n] = __ldg(cf + n);
     for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
       int a, b;
       pdec(pi, npe, a, b);
-      const float *sp = A.Rp + (size_t)pi * 9;
+      float r[12];
+      load12(A.Rp + (size_t)pi * RPF_STRIDE, r);
       float acc = 0.f;
 #pragma unroll
-      for (int n = 0; n < NS; ++n) acc = fmaf(Q[n], __ldg(sp + n), acc);
+      for (int n = 0; n < NS; ++n) acc = fmaf(Q[n], r[n], acc);
       float blk[BS];
       blk[0] = acc;
       store_pair32<P, BS>(Ke, A.colstride, a, b, blk);
     }
   } else {
+    float c[CW];
+#pragma unroll
+    for (int t = 0; t < CW; t += 4) {
+      const float4 f = __ldg(reinterpret_cast<const float4 *>(cf + t));
+      c[t] = f.x; c[t + 1] = f.y; c[t + 2] = f.z; c[t + 3] = f.w;
+    }
     float W[NS * NS], U[NA * NA];
 #pragma unroll
-    for (int t = 0; t < NS * NS; ++t) W[t] = (float)sAff[AF_W + t];
+    for (int t = 0; t < NS * NS; ++t) W[t] = c[t];
 #pragma unroll
-    for (int t = 0; t < NA * NA; ++t) U[t] = (float)sAff[AF_U + t];
+    for (int t = 0; t < NA * NA; ++t) U[t] = c[NS * NS + t];
     for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
       int a, b;
       pdec(pi, npe, a, b);
-      const float *sp = A.Rp + (size_t)pi * 9;
+      float r[12];
+      load12(A.Rp + (size_t)pi * RPF_STRIDE, r);
       float sv[NS], av[NA];
 #pragma unroll
-      for (int n = 0; n < NS; ++n) sv[n] = __ldg(sp + n);
+      for (int n = 0; n < NS; ++n) sv[n] = r[n];
 #pragma unroll
-      for (int n = 0; n < NA; ++n) av[n] = __ldg(sp + 6 + n);
+      for (int n = 0; n < NA; ++n) av[n] = r[6 + n];
       float ks[NS];
 #pragma unroll
       for (int m = 0; m < NS; ++m) {
@@ -164,13 +221,8 @@ __global__ void __launch_bounds__(E32_THREADS) k_elem_fp32(Elem32Args A) {
     const float c2 = (KIND == KIND_ELASTIC) ? (float)A.c2[mat] : 0.f;
     const int32_t *cn = A.conn + e * npe;
     float *Ke = A.Kf + (size_t)e * npe * A.colstride;
-    if (A.aflag && A.aflag[e]) {  // uniform across the CTA
-      if (threadIdx.x < 32)
-        affine_stage<DIM>(A.ageo + (size_t)e * 10, A.c1[mat], KIND == KIND_ELASTIC ? A.c2[mat] : 0.0, sAff,
-                          A.status);
-      __syncthreads();
-      affine_pairs32<KIND, DIM, P, BS>(A, sAff, Ke);
-      __syncthreads();
+    if (A.aflag && A.aflag[e]) {  // uniform across the CTA; no shared state
+      affine_pairs32<KIND, DIM, P, BS>(A, A.coef + (size_t)e * CW, Ke);
       continue;
     }
     for (int t = threadIdx.x; t < npe * DIM; t += blockDim.x) {
@@ -316,9 +368,8 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
                        const double *d_c2, const uint8_t *aflag, const double *ageo, double *nz,
                        int64_t *cnt, const double *init, GatherSink *sink) {
   const int npe = mesh->npe, P = pat->pdim;
-  const int BS = (kind == KIND_ELASTIC) ? P * P : 1;
   float *Kf = nullptr;
-  const int64_t cs = kf_colstride(npe, BS, (int)sizeof(float));
+  const int64_t cs = kf_colstride(npe, kf_bstride(P, kind == KIND_ELASTIC, (int)sizeof(float)), (int)sizeof(float));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &Kf, (size_t)mesh->nel * npe * cs));
   Elem32Args a{};
   a.xyz = mesh->d_xyz;
@@ -340,6 +391,27 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
   a.ageo = ageo;
   a.Rp = mesh->d_Rpf;
   a.Mp = mesh->d_Mpf;
+  float *coef = nullptr;
+  if (aflag) {  // FP32 coefficients of every affine element, one thread each
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &coef, (size_t)std::max<int64_t>(mesh->nel, 1) * CW));
+    const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((mesh->nel + 127) / 128, (int64_t)ctx->num_sms * 16));
+    KernelScope ks(ctx, "k_affine_coeff32");
+#define LLF_COEF32(KK, DD) \
+  k_affine_coeff32<KK, DD><<<g, 128, 0, ctx->stream>>>(ageo, aflag, mesh->d_emat, d_c1, d_c2, mesh->nel, coef, \
+                                                         ctx->d_status)
+    if (mesh->dim == 3) {
+      if (kind == KIND_ELASTIC) LLF_COEF32(KIND_ELASTIC, 3);
+      else if (kind == KIND_HEAT) LLF_COEF32(KIND_HEAT, 3);
+      else LLF_COEF32(KIND_MASS, 3);
+    } else {
+      if (kind == KIND_ELASTIC) LLF_COEF32(KIND_ELASTIC, 2);
+      else if (kind == KIND_HEAT) LLF_COEF32(KIND_HEAT, 2);
+      else LLF_COEF32(KIND_MASS, 2);
+    }
+#undef LLF_COEF32
+    LLF_CUDA_TRY(ctx, cudaGetLastError());
+  }
+  a.coef = coef;
   // element range [e0, e1): the element-indexed arrays are offset
   auto elems = [&](int64_t e0, int64_t e1) -> int {
     Elem32Args b = a;
@@ -349,6 +421,7 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
     b.Kf = a.Kf + e0 * npe * cs;
     b.aflag = a.aflag ? a.aflag + e0 : nullptr;
     b.ageo = a.ageo ? a.ageo + e0 * 10 : nullptr;
+    b.coef = a.coef ? a.coef + e0 * CW : nullptr;
     if (b.nel <= 0) return LLF_OK;
     if (mesh->dim == 3)
       return kind == KIND_ELASTIC ? run_elem32<KIND_ELASTIC, 3>(ctx, b)
@@ -363,6 +436,7 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
     rc = elems(0, mesh->nel);
     if (rc == LLF_OK) rc = gather_full32(ctx, pat, Kf, cs, kind == KIND_ELASTIC, nz, cnt, init);
   }
+  dfree(ctx, coef);
   dfree(ctx, Kf);
   return rc;
 }

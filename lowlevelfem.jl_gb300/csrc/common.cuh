@@ -243,6 +243,11 @@ int row_positions(llf_ctx *ctx, const llf_pattern *pat, const int32_t *conn, int
 // elasticSupportMatrix / heatConvectionMatrix on the volume pattern (field.cu)
 int support_impl(llf_ctx *ctx, llf_pattern *pat, llf_mesh *bmesh, const double *d_ke, const double *d_ken,
                  double thickness, llf_matrix *m);
+// Element-matrix block stride (values per node block): an FP32 3x3 block is
+// padded to 12 floats so that it is three 16-byte stores and loads.
+__host__ __device__ constexpr int kf_bstride(int P, bool blockval, int tsize) {
+  return !blockval ? 1 : (tsize == 4 && P == 3 ? 12 : P * P);
+}
 // Element-matrix column stride (elements of `tsize` bytes) padded to 16 bytes,
 // so that every column can be fetched by one bulk copy.
 inline int64_t kf_colstride(int npe, int bs, int tsize) {

@@ -698,7 +698,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tl_tangent_tc(TcArgs A) {
           const int gj = col0 + c0 + u;
           if (gj < n) {
             const int b = gj / 3, cj = gj - 3 * (gj / 3);
-            A.Kf[((size_t)e * npe + b) * A.cs + a * 9 + ci * 3 + cj] = __uint_as_float(r[u]);
+            A.Kf[((size_t)e * npe + b) * A.cs + a * kf_bstride(3, true, 4) + ci * 3 + cj] = __uint_as_float(r[u]);
           }
         }
     }
@@ -827,7 +827,7 @@ int tl_tangent_tc_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const dou
   float *Kf = nullptr;
   int64_t *cnt = nullptr;
   const int ps = tc_pstride(npe);
-  const int64_t cs = kf_colstride(npe, 9, (int)sizeof(float));
+  const int64_t cs = kf_colstride(npe, kf_bstride(3, true, (int)sizeof(float)), (int)sizeof(float));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &pd, (size_t)mesh->nel * nip * ps));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &Kf, (size_t)mesh->nel * npe * cs));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &cnt, pat->ndof + 1));
