@@ -35,6 +35,7 @@ struct Elem32Args {
   const float *Rp, *Mp;
   // per affine element its FP32 coefficients (k_affine_coeff32), CW floats
   const float *coef;
+  int affine_elsewhere;  // affine elements are left to k_affine_fp32
 };
 
 constexpr int CW = 48;  // coefficient floats per element (W 36 + U 9, padded)
@@ -114,17 +115,45 @@ __device__ __forceinline__ void store_pair32(float *Ke, int64_t cs, int a, int b
 // coefficients (from the FP64 invJ and det) rounded to FP32, read from the
 // element's coefficient row cf, then Ksym = W S, Kanti = U A per pair as in
 // the FP64 form.  No shared memory and no barrier: each thread's pairs only.
-template <int KIND, int DIM, int P, int BS>
-__device__ __forceinline__ void affine_pairs32(const Elem32Args &A, const float *__restrict__ cf, float *Ke) {
+// R rows (RPF_STRIDE floats per pair, 16-byte aligned) from global memory
+// or from a shared-memory copy; (a, b) decoded from the pair index, or read
+// from a shared table packed as a | b << 16.
+struct GlobalPairs {
+  const float *R, *M;
+  int npe;
+  __device__ void row(int pi, float *r) const { load12(R + (size_t)pi * RPF_STRIDE, r); }
+  __device__ float mass(int pi) const { return __ldg(M + pi); }
+  __device__ void ab(int pi, int &a, int &b) const { pdec(pi, npe, a, b); }
+};
+struct SharedPairs {
+  const float *R, *M;
+  const uint32_t *AB;
+  __device__ void row(int pi, float *r) const {
+#pragma unroll
+    for (int t = 0; t < RPF_STRIDE; t += 4) {
+      const float4 f = *reinterpret_cast<const float4 *>(R + (size_t)pi * RPF_STRIDE + t);
+      r[t] = f.x; r[t + 1] = f.y; r[t + 2] = f.z; r[t + 3] = f.w;
+    }
+  }
+  __device__ float mass(int pi) const { return M[pi]; }
+  __device__ void ab(int pi, int &a, int &b) const {
+    const uint32_t v = AB[pi];
+    a = (int)(v & 0xffffu);
+    b = (int)(v >> 16);
+  }
+};
+
+template <int KIND, int DIM, int P, int BS, class Pairs>
+__device__ __forceinline__ void affine_pairs32(const Elem32Args &A, const Pairs &T, const float *__restrict__ cf,
+                                               float *Ke) {
   constexpr int NS = DIM == 3 ? 6 : 3, NA = DIM == 3 ? 3 : 1;
-  const int npe = A.npe;
   if (KIND == KIND_MASS) {
     const float cm = __ldg(cf);
     for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
       int a, b;
-      pdec(pi, npe, a, b);
+      T.ab(pi, a, b);
       float blk[BS];
-      blk[0] = cm * __ldg(A.Mp + pi);
+      blk[0] = cm * T.mass(pi);
       store_pair32<P, BS>(Ke, A.colstride, a, b, blk);
     }
   } else if (KIND == KIND_HEAT) {
@@ -133,9 +162,9 @@ __device__ __forceinline__ void affine_pairs32(const Elem32Args &A, const float 
     for (int n = 0; n < NS; ++n) Q[n] = __ldg(cf + n);
     for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
       int a, b;
-      pdec(pi, npe, a, b);
-      float r[12];
-      load12(A.Rp + (size_t)pi * RPF_STRIDE, r);
+      T.ab(pi, a, b);
+      float r[RPF_STRIDE];
+      T.row(pi, r);
       float acc = 0.f;
 #pragma unroll
       for (int n = 0; n < NS; ++n) acc = fmaf(Q[n], r[n], acc);
@@ -157,9 +186,9 @@ __device__ __forceinline__ void affine_pairs32(const Elem32Args &A, const float 
     for (int t = 0; t < NA * NA; ++t) U[t] = c[NS * NS + t];
     for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
       int a, b;
-      pdec(pi, npe, a, b);
-      float r[12];
-      load12(A.Rp + (size_t)pi * RPF_STRIDE, r);
+      T.ab(pi, a, b);
+      float r[RPF_STRIDE];
+      T.row(pi, r);
       float sv[NS], av[NA];
 #pragma unroll
       for (int n = 0; n < NS; ++n) sv[n] = r[n];
@@ -222,7 +251,8 @@ __global__ void __launch_bounds__(E32_THREADS) k_elem_fp32(Elem32Args A) {
     const int32_t *cn = A.conn + e * npe;
     float *Ke = A.Kf + (size_t)e * npe * A.colstride;
     if (A.aflag && A.aflag[e]) {  // uniform across the CTA; no shared state
-      affine_pairs32<KIND, DIM, P, BS>(A, A.coef + (size_t)e * CW, Ke);
+      if (!A.affine_elsewhere)
+        affine_pairs32<KIND, DIM, P, BS>(A, GlobalPairs{A.Rp, A.Mp, npe}, A.coef + (size_t)e * CW, Ke);
       continue;
     }
     for (int t = threadIdx.x; t < npe * DIM; t += blockDim.x) {
@@ -338,6 +368,139 @@ __global__ void __launch_bounds__(E32_THREADS) k_elem_fp32(Elem32Args A) {
   }
 }
 
+// Every block (a, b) of an affine element, column by column: unit u is
+// column b = u / npe, row a = u % npe, so the lanes of a warp write one
+// contiguous run of a column and every block is written once.  The block is
+// the pair (min, max)'s, transposed when a > b — the values of
+// affine_pairs32 and its mirror, bit for bit.
+template <int KIND, int DIM, int P, int BS>
+__device__ __forceinline__ void affine_units32(const Elem32Args &A, const SharedPairs &T, const float *__restrict__ cf,
+                                               float *Ke) {
+  constexpr int NS = DIM == 3 ? 6 : 3, NA = DIM == 3 ? 3 : 1;
+  constexpr int BSTR = kf_bstride(P, BS > 1, 4);
+  const int npe = A.npe, nu = npe * npe;
+  float c[CW];
+  if (KIND == KIND_ELASTIC) {
+#pragma unroll
+    for (int t = 0; t < CW; t += 4) {
+      const float4 f = __ldg(reinterpret_cast<const float4 *>(cf + t));
+      c[t] = f.x; c[t + 1] = f.y; c[t + 2] = f.z; c[t + 3] = f.w;
+    }
+  } else {
+#pragma unroll
+    for (int t = 0; t < 8; t += 4) {
+      const float4 f = __ldg(reinterpret_cast<const float4 *>(cf + t));
+      c[t] = f.x; c[t + 1] = f.y; c[t + 2] = f.z; c[t + 3] = f.w;
+    }
+  }
+  for (int u = threadIdx.x; u < nu; u += blockDim.x) {
+    const int b = u / npe, a = u - b * npe;
+    const int lo = a < b ? a : b, hi = a < b ? b : a;
+    const int pi = lo * npe - (lo * (lo - 1)) / 2 + (hi - lo);
+    float *dst = Ke + (size_t)b * A.colstride + (size_t)a * BSTR;
+    if (KIND == KIND_MASS) {
+      dst[0] = c[0] * T.mass(pi);
+    } else if (KIND == KIND_HEAT) {
+      float r[RPF_STRIDE];
+      T.row(pi, r);
+      float acc = 0.f;
+#pragma unroll
+      for (int n = 0; n < NS; ++n) acc = fmaf(c[n], r[n], acc);
+      dst[0] = acc;
+    } else {
+      float r[RPF_STRIDE];
+      T.row(pi, r);
+      float ks[NS];
+#pragma unroll
+      for (int m = 0; m < NS; ++m) {
+        float acc = 0.f;
+#pragma unroll
+        for (int n = 0; n < NS; ++n) acc = fmaf(c[m * NS + n], r[n], acc);
+        ks[m] = acc;
+      }
+      float blk[BSTR];
+#pragma unroll
+      for (int k = BS; k < BSTR; ++k) blk[k] = 0.f;
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) blk[i * DIM + i] = ks[i];
+#pragma unroll
+      for (int m = 0; m < NA; ++m) {
+        float acc = 0.f;
+        if (lo != hi)
+#pragma unroll
+          for (int n = 0; n < NA; ++n) acc = fmaf(c[NS * NS + m * NA + n], r[6 + n], acc);
+        const int i = sym_k<DIM>(DIM + m), j = sym_l<DIM>(DIM + m);
+        // block (lo, hi) holds ks + acc at (i, j) and ks - acc at (j, i); (hi, lo) its transpose
+        blk[i * DIM + j] = a <= b ? ks[DIM + m] + acc : ks[DIM + m] - acc;
+        blk[j * DIM + i] = a <= b ? ks[DIM + m] - acc : ks[DIM + m] + acc;
+      }
+      if constexpr (BSTR % 4 == 0) {
+#pragma unroll
+        for (int k = 0; k < BSTR; k += 4)
+          *reinterpret_cast<float4 *>(dst + k) = make_float4(blk[k], blk[k + 1], blk[k + 2], blk[k + 3]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < BS; ++k) dst[k] = blk[k];
+      }
+    }
+  }
+}
+
+// Affine elements only: the pair tables (R rows or reference mass, and the
+// packed (a, b) of every pair) are copied into shared memory once per CTA
+// and stay there; per element a thread reads the element's coefficient row
+// and forms its pairs with no further global loads and no barrier.
+template <int KIND, int DIM>
+__global__ void __launch_bounds__(E32_THREADS) k_affine_fp32(Elem32Args A) {
+  extern __shared__ float4 af_smem[];
+  constexpr int BS = (KIND == KIND_ELASTIC) ? DIM * DIM : 1;
+  constexpr int P = (KIND == KIND_ELASTIC) ? DIM : 1;
+  const int np = A.npairs;
+  float *sR = reinterpret_cast<float *>(af_smem);                       // np * RPF_STRIDE (elastic, heat)
+  float *sM = sR + (KIND == KIND_MASS ? 0 : (size_t)np * RPF_STRIDE);   // np (mass)
+  uint32_t *sAB = reinterpret_cast<uint32_t *>(sM + (KIND == KIND_MASS ? np : 0));
+  if (KIND == KIND_MASS) {
+    for (int t = threadIdx.x; t < np; t += blockDim.x) sM[t] = A.Mp[t];
+  } else {
+    for (int t = threadIdx.x; t < np * RPF_STRIDE / 4; t += blockDim.x)
+      reinterpret_cast<float4 *>(sR)[t] = __ldg(reinterpret_cast<const float4 *>(A.Rp) + t);
+  }
+  for (int pi = threadIdx.x; pi < np; pi += blockDim.x) {
+    int a, b;
+    pdec(pi, A.npe, a, b);
+    sAB[pi] = (uint32_t)a | ((uint32_t)b << 16);
+  }
+  __syncthreads();
+  const SharedPairs T{sR, sM, sAB};
+  for (int64_t e = blockIdx.x; e < A.nel; e += gridDim.x) {
+    if (!A.aflag[e] || (A.emat && A.emat[e] < 0)) continue;
+    affine_units32<KIND, DIM, P, BS>(A, T, A.coef + (size_t)e * CW, A.Kf + (size_t)e * A.npe * A.colstride);
+  }
+}
+
+// Shared memory of k_affine_fp32 for npairs pairs.
+template <int KIND>
+size_t affine_fp32_smem(int npairs) {
+  return (KIND == KIND_MASS ? sizeof(float) * npairs : sizeof(float) * (size_t)npairs * RPF_STRIDE) +
+         sizeof(uint32_t) * npairs;
+}
+
+template <int KIND, int DIM>
+int run_affine32(llf_ctx *ctx, const Elem32Args &a) {
+  const size_t smem = affine_fp32_smem<KIND>(a.npairs);
+  auto fn = k_affine_fp32<KIND, DIM>;
+  if (smem > 48 * 1024)
+    LLF_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 1;
+  LLF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, E32_THREADS, smem));
+  int64_t grid = (int64_t)ctx->num_sms * (per_sm < 1 ? 1 : per_sm);
+  if (grid > a.nel) grid = a.nel > 0 ? a.nel : 1;
+  KernelScope ks(ctx, "k_affine_fp32");
+  fn<<<(unsigned)grid, E32_THREADS, smem, ctx->stream>>>(a);
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  return LLF_OK;
+}
+
 template <int KIND, int DIM>
 int run_elem32(llf_ctx *ctx, Elem32Args a) {
   const int npe = a.npe, nip = a.nip;
@@ -412,6 +575,11 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
     LLF_CUDA_TRY(ctx, cudaGetLastError());
   }
   a.coef = coef;
+  // the affine kernel keeps the pair tables in shared memory; beyond 96 KB
+  // (high orders) the general kernel reads them from global memory instead
+  const size_t af_smem = kind == KIND_MASS ? affine_fp32_smem<KIND_MASS>(a.npairs)
+                                           : affine_fp32_smem<KIND_ELASTIC>(a.npairs);
+  a.affine_elsewhere = (aflag && af_smem <= 96 * 1024) ? 1 : 0;
   // element range [e0, e1): the element-indexed arrays are offset
   auto elems = [&](int64_t e0, int64_t e1) -> int {
     Elem32Args b = a;
@@ -423,6 +591,16 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
     b.ageo = a.ageo ? a.ageo + e0 * 10 : nullptr;
     b.coef = a.coef ? a.coef + e0 * CW : nullptr;
     if (b.nel <= 0) return LLF_OK;
+    int r = LLF_OK;
+    if (b.affine_elsewhere) {
+      if (mesh->dim == 3)
+        r = kind == KIND_ELASTIC ? run_affine32<KIND_ELASTIC, 3>(ctx, b)
+                                 : (kind == KIND_HEAT ? run_affine32<KIND_HEAT, 3>(ctx, b) : run_affine32<KIND_MASS, 3>(ctx, b));
+      else
+        r = kind == KIND_ELASTIC ? run_affine32<KIND_ELASTIC, 2>(ctx, b)
+                                 : (kind == KIND_HEAT ? run_affine32<KIND_HEAT, 2>(ctx, b) : run_affine32<KIND_MASS, 2>(ctx, b));
+      if (r != LLF_OK) return r;
+    }
     if (mesh->dim == 3)
       return kind == KIND_ELASTIC ? run_elem32<KIND_ELASTIC, 3>(ctx, b)
                                   : (kind == KIND_HEAT ? run_elem32<KIND_HEAT, 3>(ctx, b) : run_elem32<KIND_MASS, 3>(ctx, b));
