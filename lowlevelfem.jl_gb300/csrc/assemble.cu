@@ -351,6 +351,10 @@ __device__ __forceinline__ double widen(double x) { return x; }
 __device__ __forceinline__ double widen(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  if (e - 1u < 254u) {  // normal: in 32-bit halves, exponent + (1023 - 127), mantissa << 29
+    const unsigned hi = (u & 0x80000000u) | (((u & 0x7fffffffu) >> 3) + 0x38000000u);
+    return __hiloint2double((int)hi, (int)(u << 29));
+  }
   unsigned long long bits;
   if (e != 0u) {
     const unsigned long long ed = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
