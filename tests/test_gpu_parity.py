@@ -324,3 +324,23 @@ def test_heat_capacity_bit_identical(llf, orc, case, lumped):
     rule = llf._lib.builtin_rule(m.family, m.order)
     ref = orc.assemble(orc.MASS, PT[pt], m.dim, 1, m.xyz, m.conn, rule, [mat.c * mat.rho], 0.7, lumped)
     assert_csc_identical(C.csc(), ref.julia(), f"C {kind} {order} lumped={lumped}")
+
+
+@pytest.mark.parametrize("case", [("box", 17, 1, False), ("box", 9, 2, True), ("rect", 70, 2, False)],
+                         ids=["hex8-4913", "tet10-4374", "quad9-4900"])
+def test_larger_meshes_bit_identical(llf, orc, case):
+    """Meshes of several thousand elements (many gather CTAs and grid-stride
+    passes per kernel) against the oracle."""
+    kind, n, order, simplex = case
+    m = make_mesh(llf, kind, n, order, simplex)
+    assert m.nel >= 4096
+    pt = "Solid" if m.dim == 3 else "PlaneStrain"
+    mat = llf.Material("body", E=2.1e5, nu=0.3, k=45.0)
+    p = llf.Problem([mat], type=pt)
+    K = llf.stiffnessMatrix(p)
+    ref = oracle_operator(llf, orc, m, "stiffness", PT[pt], mat)
+    assert_csc_identical(K.csc(), ref.julia(), f"stiffness {kind} n{n} p{order}")
+    ph = llf.Problem([mat], type="HeatConduction" if m.dim == 3 else "PlaneHeatConduction")
+    H = llf.heatConductionMatrix(ph)
+    refh = oracle_operator(llf, orc, m, "heat", PT[ph.type], mat)
+    assert_csc_identical(H.csc(), refh.julia(), f"conduction {kind} n{n} p{order}")

@@ -28,8 +28,9 @@ def _to_host(llf, p, form, capacity=None):
 
 @pytest.mark.parametrize("case", [("box", 3, 2, False, "Solid"), ("box", 4, 2, True, "Solid"),
                                   ("rect", 20, 1, False, "PlaneStrain"), ("rect", 1, 1, False, "PlaneStress"),
-                                  ("box", 6, 1, False, "Solid")],
-                         ids=["hex27", "tet10", "quad4", "one-quad", "hex8"])
+                                  ("box", 6, 1, False, "Solid"), ("box", 17, 1, False, "Solid"),
+                                  ("box", 9, 2, True, "Solid")],
+                         ids=["hex27", "tet10", "quad4", "one-quad", "hex8", "hex8-4913", "tet10-4374"])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_to_host_equals_assemble_then_copy(llf, case, precision):
     kind, n, order, simplex, pt = case
