@@ -66,24 +66,74 @@ __device__ __forceinline__ double block_sum(double v) {
   return r;
 }
 
-// y = A x for all columns (plain product, llf_matrix_spmv).
+// Products of the P columns of node B by x, summed over SPMV_G lanes: the
+// node's columns are P contiguous runs of deg*P values (entry (t, i) of
+// column j at (j*deg + t)*P + i); group lane g takes positions g, g+G, ...
+// of all P columns at once, the x value of a position being shared by the
+// P columns.  On GB300 the FP64 pipe, not HBM, bounds this product (one DFMA
+// per stored value), so a warp serves 32/G nodes and the reduction is
+// log2(G) shuffle-adds per column shared by those nodes.  After the call
+// every lane of the group holds the P sums.
+constexpr int SPMV_G = 4;
+
+template <int P>
+__device__ __forceinline__ void node_columns(const double *__restrict__ nz, const int64_t *__restrict__ nptr,
+                                             const int32_t *__restrict__ nadj, const double *__restrict__ x,
+                                             int64_t B, bool valid, int g, double (&acc)[P]) {
+#pragma unroll
+  for (int j = 0; j < P; ++j) acc[j] = 0.0;
+  if (valid) {
+    const int64_t r0 = nptr[B];
+    const int n = (int)(nptr[B + 1] - r0) * P;  // entries per column
+    const double *col = nz + (int64_t)P * r0 * P;
+    int k = g;
+    for (; k + SPMV_G < n; k += 2 * SPMV_G) {
+      const int k2 = k + SPMV_G;
+      double v[P], v2[P];
+#pragma unroll
+      for (int j = 0; j < P; ++j) {
+        v[j] = col[(int64_t)j * n + k];
+        v2[j] = col[(int64_t)j * n + k2];
+      }
+      const double xa = x[(int64_t)P * nadj[r0 + k / P] + k % P];
+      const double xb = x[(int64_t)P * nadj[r0 + k2 / P] + k2 % P];
+#pragma unroll
+      for (int j = 0; j < P; ++j) acc[j] = __fma_rn(v2[j], xb, __fma_rn(v[j], xa, acc[j]));
+    }
+    if (k < n) {
+      const double xa = x[(int64_t)P * nadj[r0 + k / P] + k % P];
+#pragma unroll
+      for (int j = 0; j < P; ++j) acc[j] = __fma_rn(col[(int64_t)j * n + k], xa, acc[j]);
+    }
+  }
+#pragma unroll
+  for (int off = SPMV_G / 2; off > 0; off >>= 1)
+#pragma unroll
+    for (int j = 0; j < P; ++j) acc[j] = __dadd_rn(acc[j], __shfl_xor_sync(0xffffffffu, acc[j], off));
+}
+
+// y = A x for all columns (plain product, llf_matrix_spmv), SPMV_G lanes per
+// column node.
 template <int P>
 __global__ void __launch_bounds__(CG_THREADS)
 k_spmv(const double *__restrict__ nz, const int64_t *__restrict__ colptr,
        const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
        const double *__restrict__ x, double *__restrict__ y, int64_t ndof) {
-  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-  for (int64_t c = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5); c < ndof;
-       c += (int64_t)gridDim.x * wpb) {
-    const int64_t s = colptr[c], e = colptr[c + 1];
-    const int64_t r0 = nptr[c / P];
-    double acc = 0.0;
-    for (int64_t k = s + lane; k < e; k += 32) {
-      const int64_t loc = k - s;
-      acc = __fma_rn(nz[k], x[(int64_t)P * nadj[r0 + loc / P] + loc % P], acc);
+  (void)colptr;
+  constexpr int NPW = 32 / SPMV_G;  // nodes per warp
+  const int lane = threadIdx.x & 31, g = lane % SPMV_G, wpb = blockDim.x >> 5;
+  const int64_t non = ndof / P;
+  const int64_t stride = (int64_t)gridDim.x * wpb * NPW;
+  for (int64_t B0 = ((int64_t)blockIdx.x * wpb + (threadIdx.x >> 5)) * NPW; B0 < non; B0 += stride) {
+    const int64_t B = B0 + lane / SPMV_G;
+    double acc[P];
+    node_columns<P>(nz, nptr, nadj, x, B, B < non, g, acc);
+    if (B < non && g < P) {
+      double v = acc[0];
+#pragma unroll
+      for (int j = 1; j < P; ++j) v = g == j ? acc[j] : v;
+      y[P * B + g] = v;
     }
-    acc = warp_sum(acc);
-    if (lane == 0) y[c] = acc;
   }
 }
 
@@ -274,31 +324,17 @@ __global__ void __launch_bounds__(CG_THREADS)
 k_seg_spmv(Seg S, const double *__restrict__ nz, const int64_t *__restrict__ nptr,
            const int32_t *__restrict__ nadj, const double *__restrict__ u,
            const uint8_t *__restrict__ fixed, double *__restrict__ c, double *__restrict__ part) {
-  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, w = threadIdx.x >> 5;
+  constexpr int NPW = 32 / SPMV_G;  // nodes per warp
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, w = threadIdx.x >> 5, g = lane % SPMV_G;
   for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
     if (S.st[S.cseg[ch]].done) continue;
     double dot = 0.0;
     const int64_t B1 = S.cend[ch] / P;
-    for (int64_t B = S.cbeg[ch] / P + w; B < B1; B += wpb) {
-      const int64_t r0 = nptr[B];
-      const int deg = (int)(nptr[B + 1] - r0);
-      const double *col = nz + (int64_t)P * P * r0;  // column (B,j): col[(j*deg + t)*P + i]
+    for (int64_t B0 = S.cbeg[ch] / P + (int64_t)w * NPW; B0 < B1; B0 += (int64_t)wpb * NPW) {
+      const int64_t B = B0 + lane / SPMV_G;
       double acc[P];
-#pragma unroll
-      for (int j = 0; j < P; ++j) acc[j] = 0.0;
-      for (int t = lane; t < deg; t += 32) {
-        const int64_t A = nadj[r0 + t];
-        double xa[P];
-#pragma unroll
-        for (int i = 0; i < P; ++i) xa[i] = u[P * A + i];
-#pragma unroll
-        for (int j = 0; j < P; ++j)
-#pragma unroll
-          for (int i = 0; i < P; ++i) acc[j] = __fma_rn(col[((size_t)j * deg + t) * P + i], xa[i], acc[j]);
-      }
-#pragma unroll
-      for (int j = 0; j < P; ++j) acc[j] = warp_sum(acc[j]);
-      if (lane == 0) {
+      node_columns<P>(nz, nptr, nadj, u, B, B < B1, g, acc);
+      if (B < B1 && g == 0) {
 #pragma unroll
         for (int j = 0; j < P; ++j) {
           const int64_t d = P * B + j;
