@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--workers", type=int, default=4, help="serving: server workers")
     ap.add_argument("--no-peak", action="store_true", help="skip the DGEMM FP64 reference rate")
     ap.add_argument("--no-other-form", action="store_true", help="skip the second arithmetic form")
+    ap.add_argument("--no-plain", action="store_true", help="batched: skip the one-at-a-time plain arm")
     ap.add_argument("--precond", default=None, choices=["jacobi", "bjacobi", "ic0", "auto"],
                     help="CG preconditioner (defaults: ic0 for batched, bjacobi for tl, auto for serving: "
                          "IC(0) from 50,000 nodes, Jacobi below)")
@@ -249,6 +250,31 @@ def run_batched(args, llf):
         Ai = A[a:b, a:b].tocsc()[fr][:, fr]
         ud = spla.spsolve(Ai.tocsc(), f.a[a:b, 0][fr])
         errs.append(float(np.linalg.norm(u.a[a:b, 0][fr] - ud) / np.linalg.norm(ud)))
+    # the plain GPU form: every instance on its own, FP64 assembly and
+    # Jacobi-PCG to the same tolerance, one after the other (patterns built
+    # before the timed loop, as for the batch)
+    plain = None
+    if not args.no_plain:
+        singles = []
+        for i, (m, E, nu) in enumerate(inst):
+            Pi = llf.Problem([llf.Material("body", E=E, nu=nu)], type="Solid", mesh=m)
+            Pi.pattern()
+            singles.append((Pi, llf.loadVector(Pi, [llf.load("right", fx=1.0)]),
+                            [llf.displacementConstraint("left", ux=0, uy=0, uz=0)]))
+        def solve_one(Pi, fi, si):
+            Ki = llf.stiffnessMatrix(Pi)
+            return llf.solveField(Ki, fi, support=si, iterative=True, preconditioner="jacobi", reltol=1e-12,
+                                  maxiter=20 * 3 * Pi.non)
+        solve_one(*singles[int(np.argmin([m.nel for m, _, _ in inst]))])   # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for Pi, fi, si in singles:
+            solve_one(Pi, fi, si)
+        torch.cuda.synchronize()
+        tp = time.perf_counter() - t0
+        plain = {"value": len(inst) / tp, "unit": "solves/s", "seconds": tp,
+                 "form": "one instance at a time: FP64 assembly + Jacobi-PCG to 1e-12",
+                 "speedup_of_batched": (len(inst) / t) / (len(inst) / tp)}
     nel = sum(m.nel for m, _, _ in inst)
     return {"metric": "batched assemble+solve (independent tet10 systems / s)", "value": len(inst) / t,
             "unit": "solves/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
@@ -259,7 +285,7 @@ def run_batched(args, llf):
                        "reltol": 1e-12},
             "cg_iterations": {"min": int(np.min(u.iterations)), "median": float(np.median(u.iterations)),
                               "max": int(np.max(u.iterations))},
-            "rel_err_vs_direct": errs}
+            "rel_err_vs_direct": errs, "plain_gpu": plain}
 
 
 def run_serving(args, llf):
