@@ -233,7 +233,29 @@ struct Seg {
   int nseg;
   SegState *st;
   int *active;
+  int *arrive;                 // 3*nseg arrival counters of the fused reductions (zero between uses;
+                               // [nseg, 2nseg) the update's, [2nseg, 3nseg) the IC(0) z.r's)
 };
+
+// Last-block-done segment reduction: after a chunk's partial is written,
+// thread 0 fences and counts the chunk in; the block that brings in the
+// segment's last chunk sees every partial (fence, then L2 loads) and sums
+// them in chunk order — the same order and result as a separate reduction
+// kernel.  Block-uniform; the counter is reset by that last block.
+__device__ __forceinline__ bool arrive_last(int *cnt, int64_t nch) {
+  __shared__ int last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = (int64_t)atomicAdd(cnt, 1) == nch - 1;
+    if (last) {
+      __threadfence();
+      *cnt = 0;
+    }
+  }
+  __syncthreads();
+  return last != 0;
+}
 
 // y = fixed ? 0 : b - A x_c; r = y; x = 0; u = 0; partial r.r per chunk.
 __global__ void __launch_bounds__(CG_THREADS)
@@ -258,6 +280,40 @@ __device__ __forceinline__ double seg_total(const Seg &S, int s, const double *p
   double v = 0.0;
   for (int64_t ch = S.sfirst[s] + threadIdx.x; ch < S.sfirst[s + 1]; ch += blockDim.x) v = __dadd_rn(v, part[ch]);
   return block_sum(v);
+}
+
+// The same sum read through L2 (partials written by other blocks of the
+// same launch).
+__device__ __forceinline__ double seg_total_l2(const Seg &S, int s, const double *part) {
+  double v = 0.0;
+  for (int64_t ch = S.sfirst[s] + threadIdx.x; ch < S.sfirst[s + 1]; ch += blockDim.x)
+    v = __dadd_rn(v, __ldcg(part + ch));
+  return block_sum(v);
+}
+
+// Segment state after the alpha reduction (u.c) / the residual reduction.
+__device__ __forceinline__ void seg_set_alpha(const Seg &S, int s, double uc) {
+  SegState &q = S.st[s];
+  if (!(uc > 0.0) || !isfinite(uc)) {
+    q.breakdown = 1;
+    q.done = 1;
+    q.alpha = 0.0;
+    atomicSub(S.active, 1);
+  } else {
+    q.alpha = q.rho / uc;
+  }
+}
+__device__ __forceinline__ bool seg_set_finish(const Seg &S, int s, double rr) {
+  SegState &q = S.st[s];
+  q.res = sqrt(rr);
+  q.rho_prev = q.rho;
+  q.it += 1;
+  if (q.res <= q.tol || q.it >= q.maxiter) {
+    q.done = 1;
+    atomicSub(S.active, 1);
+    return true;
+  }
+  return false;
 }
 
 __global__ void k_seg_start(Seg S, const double *part, double reltol, long long maxiter) {
@@ -353,17 +409,7 @@ __global__ void k_seg_alpha(Seg S, const double *part) {
   for (int s = blockIdx.x; s < S.nseg; s += gridDim.x) {
     if (S.st[s].done) continue;
     double uc = seg_total(S, s, part);
-    if (threadIdx.x == 0) {
-      SegState &q = S.st[s];
-      if (!(uc > 0.0) || !isfinite(uc)) {
-        q.breakdown = 1;
-        q.done = 1;
-        q.alpha = 0.0;
-        atomicSub(S.active, 1);
-      } else {
-        q.alpha = q.rho / uc;
-      }
-    }
+    if (threadIdx.x == 0) seg_set_alpha(S, s, uc);
   }
 }
 
@@ -383,6 +429,52 @@ k_seg_update(Seg S, double *__restrict__ xw, double *__restrict__ r, const doubl
     }
     double s = block_sum(rr);
     if (threadIdx.x == 0) part[ch] = s;
+  }
+}
+
+// x += alpha u, r -= alpha c and the residual check; with a local
+// preconditioner (mode NONE, JACOBI, BJACOBI) also z = M^-1 r and rho = z.r
+// for the next iteration — one launch where there were four.
+template <int P>
+__global__ void __launch_bounds__(CG_THREADS)
+k_seg_update_fused(Seg S, double *__restrict__ xw, double *__restrict__ r, const double *__restrict__ u,
+                   const double *__restrict__ c, double *__restrict__ part, double *__restrict__ part2,
+                   const double *__restrict__ pinv, int mode, bool local_prec, const uint8_t *__restrict__ fixed,
+                   double *__restrict__ z) {
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    const int sg = S.cseg[ch];
+    const SegState &q = S.st[sg];
+    if (q.done) continue;
+    const double alpha = q.alpha;
+    double rr = 0.0, zr = 0.0;
+    for (int64_t i = S.cbeg[ch] + threadIdx.x; i < S.cend[ch]; i += blockDim.x) {
+      xw[i] = __fma_rn(alpha, u[i], xw[i]);
+      const double ri = __fma_rn(-alpha, c[i], r[i]);
+      r[i] = ri;
+      rr = __fma_rn(ri, ri, rr);
+    }
+    if (local_prec) {  // the block-Jacobi blocks stay within the chunk (whole nodes): own r only
+      __syncthreads();
+      for (int64_t i = S.cbeg[ch] + threadIdx.x; i < S.cend[ch]; i += blockDim.x) {
+        const double zi = fixed[i] ? 0.0 : apply_prec<P>(pinv, mode, r, i);
+        z[i] = zi;
+        zr = __fma_rn(zi, r[i], zr);
+      }
+    }
+    const double s1 = block_sum(rr);
+    const double s2 = local_prec ? block_sum(zr) : 0.0;
+    if (threadIdx.x == 0) {
+      part[ch] = s1;
+      if (local_prec) part2[ch] = s2;
+    }
+    if (arrive_last(S.arrive + S.nseg + sg, S.sfirst[sg + 1] - S.sfirst[sg])) {
+      const double trr = seg_total_l2(S, sg, part);
+      const double tzr = local_prec ? seg_total_l2(S, sg, part2) : 0.0;
+      if (threadIdx.x == 0) {
+        const bool done = seg_set_finish(S, sg, trr);
+        if (local_prec && !done) S.st[sg].rho = tzr;
+      }
+    }
   }
 }
 
@@ -536,6 +628,11 @@ k_seg_zr(Seg S, const float *__restrict__ zf, const double *__restrict__ r, doub
     }
     double s = block_sum(zr);
     if (threadIdx.x == 0) part[ch] = s;
+    const int sg = S.cseg[ch];
+    if (arrive_last(S.arrive + 2 * S.nseg + sg, S.sfirst[sg + 1] - S.sfirst[sg])) {  // rho = z.r
+      const double t = seg_total_l2(S, sg, part);
+      if (threadIdx.x == 0) S.st[sg].rho = t;
+    }
   }
 }
 
@@ -573,32 +670,44 @@ void enqueue_ic0(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const IcApply 
   { KernelScope k(ctx, "k_seg_zr"); k_seg_zr<<<gch, CG_THREADS, 0, s>>>(S, ic.zf, r, z, part); }
 }
 
+// z = M^-1 r and rho = z.r of the first iteration.
+template <int P>
+void enqueue_first_prec(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const double *pinv, int precond,
+                        double *r, double *z, const uint8_t *fixed, double *part, unsigned gch, unsigned gseg,
+                        const IcApply &ic) {
+  cudaStream_t s = ctx->stream;
+  if (precond == LLF_PRECOND_IC0) {
+    enqueue_ic0<P>(ctx, S, m, ic, r, z, part, gch);  // its z.r sets rho
+    return;
+  }
+  { KernelScope k(ctx, "k_seg_prec"); k_seg_prec<P><<<gch, CG_THREADS, 0, s>>>(S, pinv, precond, r, fixed, z, part); }
+  { KernelScope k(ctx, "k_seg_rho"); k_seg_rho<<<gseg, CG_THREADS, 0, s>>>(S, part); }
+}
+
+// One CG iteration: u = z + beta u; c = A u; alpha; x, r updated with the
+// residual check, then the next z and rho (fused for the local
+// preconditioners, the IC(0) sweeps after the update otherwise).
 template <int P>
 void enqueue_iteration(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const double *pinv, int precond,
                        double *r, double *z, double *u, double *c, double *xw, const uint8_t *fixed,
-                       double *part, unsigned gch, unsigned gseg, const IcApply &ic) {
+                       double *part, double *part2, unsigned gch, unsigned gseg, const IcApply &ic) {
   const llf_pattern *pat = m->pat;
   cudaStream_t s = ctx->stream;
-  if (precond == LLF_PRECOND_IC0) {
-    enqueue_ic0<P>(ctx, S, m, ic, r, z, part, gch);
-  } else {
-    KernelScope k(ctx, "k_seg_prec");
-    k_seg_prec<P><<<gch, CG_THREADS, 0, s>>>(S, pinv, precond, r, fixed, z, part);
-  }
-  { KernelScope k(ctx, "k_seg_rho"); k_seg_rho<<<gseg, CG_THREADS, 0, s>>>(S, part); }
+  const bool local = precond != LLF_PRECOND_IC0;
   { KernelScope k(ctx, "k_seg_dir"); k_seg_dir<<<gch, CG_THREADS, 0, s>>>(S, z, u); }
   { KernelScope k(ctx, "k_seg_spmv");
     k_seg_spmv<P><<<gch, CG_THREADS, 0, s>>>(S, m->d_nz, pat->d_nptr, pat->d_nadj, u, fixed, c, part); }
   { KernelScope k(ctx, "k_seg_alpha"); k_seg_alpha<<<gseg, CG_THREADS, 0, s>>>(S, part); }
-  { KernelScope k(ctx, "k_seg_update"); k_seg_update<<<gch, CG_THREADS, 0, s>>>(S, xw, r, u, c, part); }
-  { KernelScope k(ctx, "k_seg_finish"); k_seg_finish<<<gseg, CG_THREADS, 0, s>>>(S, part); }
+  { KernelScope k(ctx, "k_seg_update");
+    k_seg_update_fused<P><<<gch, CG_THREADS, 0, s>>>(S, xw, r, u, c, part, part2, pinv, precond, local, fixed, z); }
+  if (!local) enqueue_ic0<P>(ctx, S, m, ic, r, z, part, gch);
 }
 
 template <int P>
 int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
              const Seg &S, double *r, double *z, double *u, double *c, double *xw, double *pinv,
-             double *part, int precond, double reltol, int64_t maxiter, bool use_graph, SegState *hst,
-             const IcApply &ic = IcApply());
+             double *part, double *part2, int precond, double reltol, int64_t maxiter, bool use_graph,
+             SegState *hst, const IcApply &ic = IcApply());
 int pcg_outcome(llf_ctx *ctx, int nseg, const SegState *hst, int64_t *iters, double *relres);
 
 // Buffers, chunking and preconditioner of the segmented PCG for one matrix
@@ -613,6 +722,8 @@ struct PcgPlan {
   int *d_active = nullptr;
   SegState *d_st = nullptr;
   double *r = nullptr, *z = nullptr, *u = nullptr, *c = nullptr, *xw = nullptr, *pinv = nullptr, *part = nullptr;
+  double *part2 = nullptr;
+  int *d_arrive = nullptr;
   Ic0Factor icf;
   IcApply ic;
   int32_t *d_node_seg = nullptr;
@@ -652,6 +763,9 @@ struct PcgPlan {
     LLF_CUDA_TRY(ctx, dalloc(ctx, &xw, n));
     LLF_CUDA_TRY(ctx, dalloc(ctx, &pinv, precond == LLF_PRECOND_BJACOBI ? n * P : n));
     LLF_CUDA_TRY(ctx, dalloc(ctx, &part, nch));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &part2, nch));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_arrive, 3 * (int64_t)nseg));
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_arrive, 0, sizeof(int) * 3 * nseg, s));
     if (nch) {
       LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_cb, cb.data(), sizeof(int64_t) * nch, cudaMemcpyHostToDevice, s));
       LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_ce, ce.data(), sizeof(int64_t) * nch, cudaMemcpyHostToDevice, s));
@@ -659,7 +773,7 @@ struct PcgPlan {
     }
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_sf, sf.data(), sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, s));
     LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_active, 0, sizeof(int), s));
-    S = Seg{d_cb, d_ce, d_cs, d_sf, nch, nseg, d_st, d_active};
+    S = Seg{d_cb, d_ce, d_cs, d_sf, nch, nseg, d_st, d_active, d_arrive};
     hst.assign(nseg, SegState{});
     // IC(0): factor of A with the fixed DoFs as identity rows, node -> system map
     if (precond == LLF_PRECOND_IC0) {
@@ -685,8 +799,8 @@ struct PcgPlan {
 
   int solve(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
             double reltol, int64_t maxiter, int64_t *iters, double *relres) {
-    int rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, precond, reltol, maxiter,
-                         !ctx->profiling, hst.data(), ic);
+    int rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, part2, precond, reltol,
+                         maxiter, !ctx->profiling, hst.data(), ic);
     if (rc != LLF_OK) return rc;
     return pcg_outcome(ctx, nseg, hst.data(), iters, relres);
   }
@@ -699,7 +813,7 @@ struct PcgPlan {
     }
     dfree(ctx, d_cb); dfree(ctx, d_ce); dfree(ctx, d_cs); dfree(ctx, d_sf); dfree(ctx, d_active);
     dfree(ctx, d_st); dfree(ctx, r); dfree(ctx, z); dfree(ctx, u); dfree(ctx, c); dfree(ctx, xw);
-    dfree(ctx, pinv); dfree(ctx, part);
+    dfree(ctx, pinv); dfree(ctx, part); dfree(ctx, part2); dfree(ctx, d_arrive);
   }
 };
 
@@ -722,8 +836,8 @@ int pcg_segments(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d
 template <int P>
 int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
              const Seg &S, double *r, double *z, double *u, double *c, double *xw, double *pinv,
-             double *part, int precond, double reltol, int64_t maxiter, bool use_graph, SegState *hst,
-             const IcApply &ic) {
+             double *part, double *part2, int precond, double reltol, int64_t maxiter, bool use_graph,
+             SegState *hst, const IcApply &ic) {
   const llf_pattern *pat = m->pat;
   const int64_t n = pat->ndof;
   const int64_t nch = S.nchunks;
@@ -743,6 +857,7 @@ int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, 
   { KernelScope k(ctx, "k_spmv"); k_spmv<P><<<gv, CG_THREADS, 0, s>>>(m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, xw, c, n); }
   { KernelScope k(ctx, "k_seg_init"); k_seg_init<<<gch, CG_THREADS, 0, s>>>(S, d_b, c, d_fixed, r, xw, u, part); }
   { KernelScope k(ctx, "k_seg_start"); k_seg_start<<<gseg, CG_THREADS, 0, s>>>(S, part, reltol, (long long)maxiter); }
+  enqueue_first_prec<P>(ctx, S, m, pinv, precond, r, z, d_fixed, part, gch, gseg, ic);
   LLF_CUDA_TRY(ctx, cudaGetLastError());
 
   // capture a run of iterations once, replay until every segment is done
@@ -754,7 +869,7 @@ int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, 
     cudaGraph_t graph = nullptr;
     if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       const long long saved = ctx->launches;
-      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, gch, gseg, ic);
+      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, part2, gch, gseg, ic);
       launches_per_graph = ctx->launches - saved;
       ctx->launches = saved;
       if (cudaStreamEndCapture(s, &graph) != cudaSuccess ||
@@ -773,7 +888,7 @@ int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, 
       LLF_CUDA_TRY(ctx, cudaGraphLaunch(exec, s));
       ctx->launches += launches_per_graph;
     } else {
-      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, gch, gseg, ic);
+      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, part2, gch, gseg, ic);
     }
     LLF_CUDA_TRY(ctx, cudaGetLastError());
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(h_active, d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -831,8 +946,9 @@ constexpr size_t NA_OFF_CE = NA_OFF_CB + na_round(sizeof(int64_t) * NA_CH);
 constexpr size_t NA_OFF_SF = NA_OFF_CE + na_round(sizeof(int64_t) * NA_CH);
 constexpr size_t NA_OFF_CS = NA_OFF_SF + na_round(sizeof(int64_t) * 2);
 constexpr size_t NA_OFF_ST = NA_OFF_CS + na_round(sizeof(int32_t) * NA_CH);
-constexpr size_t NA_OFF_ACT = NA_OFF_ST + na_round(sizeof(SegState));
-constexpr size_t NA_BYTES = NA_OFF_ACT + 256;
+constexpr size_t NA_OFF_ACT = NA_OFF_ST + na_round(sizeof(SegState));  // active counter, then 3 arrival counters
+constexpr size_t NA_OFF_PART2 = NA_OFF_ACT + 256;
+constexpr size_t NA_BYTES = NA_OFF_PART2 + na_round(sizeof(double) * NA_CH);
 
 }  // namespace
 
@@ -892,16 +1008,19 @@ int pcg_noalloc_typed(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doub
   int32_t *cs = (int32_t *)(base + NA_OFF_CS);
   SegState *st = (SegState *)(base + NA_OFF_ST);
   int *active = (int *)(base + NA_OFF_ACT);
+  int *arrive = active + 1;
+  double *part2 = (double *)(base + NA_OFF_PART2);
   const int64_t nch = (n + CHUNK - 1) / CHUNK;
   // the array keeps the previous call's contents: the active-system counter
-  // must start at zero; every other region is written before it is read
-  LLF_CUDA_TRY(ctx, cudaMemsetAsync(active, 0, sizeof(int), ctx->stream));
+  // and the three arrival counters must start at zero; every other region
+  // is written before it is read
+  LLF_CUDA_TRY(ctx, cudaMemsetAsync(active, 0, sizeof(int) * 4, ctx->stream));
   k_na_chunks<<<1, 64, 0, ctx->stream>>>(cb, ce, cs, sf, n, nch);
   ctx->launches++;
   LLF_CUDA_TRY(ctx, cudaGetLastError());
-  Seg S{cb, ce, cs, sf, nch, 1, st, active};
+  Seg S{cb, ce, cs, sf, nch, 1, st, active, arrive};
   SegState hst[1];
-  rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, precond, reltol, maxiter,
+  rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, part2, precond, reltol, maxiter,
                    false, hst);
   if (rc != LLF_OK) return rc;
   return pcg_outcome(ctx, 1, hst, iters, relres);
