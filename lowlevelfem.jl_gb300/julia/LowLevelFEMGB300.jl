@@ -344,6 +344,31 @@ function solveTemperature(problem; heatFlux=LoadCondition[], temperatureConstrai
     return solveField(K, q; support=temperatureConstraint, kw...)
 end
 
+# FDM (src/heat.jl:1466-1616): the whole theta-method loop on the device.
+# K and C re-enter through the problem's pattern; a lumped C (diagonal only)
+# keeps its diagonal in the structural values.
+function FDM(K::SystemMatrix, C::SystemMatrix, q::ScalarField, bc, TT0::ScalarField, n::Int, Δt::Float64; ϑ=0.5)
+    problem = K.model
+    nd = problem.pdim * problem.non
+    T = zeros(nd, n)
+    T[:, 1] .= TT0.a[:, 1]
+    TT = ScalarField([], T, collect(0:Δt:(n-1)*Δt), [], n, :scalar, problem)
+    LowLevelFEM.applyBoundaryConditions!(TT, bc)
+    fixed = zeros(UInt8, nd)
+    fixed[LowLevelFEM.constrainedDoFs(problem, bc)] .= 1
+    hK = upload(K); hC = upload(C)
+    qa = Matrix{Float64}(q.a)
+    its = Ref{Int64}(0)
+    st = ccall((:llf_heat_fdm, LIB), Cint,
+               (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Cint, Ptr{Float64}, Ptr{UInt8}, Int64, Float64,
+                Float64, Cint, Float64, Int64, Ref{Int64}),
+               ctx(), hK, hC, qa, size(qa, 2), TT.a, fixed, n, Δt, ϑ, 2, 1e-13, 20nd, its)
+    ccall((:llf_matrix_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), hK)
+    ccall((:llf_matrix_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), hC)
+    check(st)
+    return TT
+end
+
 # A host SystemMatrix re-enters the device through the structural pattern of
 # its problem: the values are scattered by row/column search on the host
 # side of Julia and uploaded as structural values.
