@@ -285,12 +285,15 @@ struct Ic0Factor {
   double *Lcol = nullptr;           // L_jk with node k's list  (nnzb * P * P)
   double *Ldinv = nullptr;          // L_jj^-1 per node          (non * P * P)
   double shift = 0.0;               // diagonal shift the factorisation needed
-  // FP32 factor for the solves: node j's earlier neighbours fk[fptr[j]..] with
-  // blocks Lf (L_jk), later neighbours bk[bptr[j]..] with blocks Lb (L_kj),
-  // and L_jj^-1 (Ldf); the index arrays belong to the pattern's colouring
+  // FP32 factor for the solves, indexed by a node's position t in d_nodes
+  // (colour order): the earlier neighbours fk[fptr[t]..] with blocks Lf
+  // (L_jk), the later neighbours bk[bptr[t]..] with blocks Lb (L_kj),
+  // L_jj^-1 (Ldf) and the node's system (segc); the index arrays belong to
+  // the pattern's colouring
   const int64_t *fptr = nullptr, *bptr = nullptr;
   const int32_t *fk = nullptr, *bk = nullptr;
   float *Lf = nullptr, *Lb = nullptr, *Ldf = nullptr;
+  int32_t *segc = nullptr;
 };
 // seg_nodes: first node of each independent system (+ node count), d_node_seg:
 // system of every node; a system's colouring and factor do not depend on the

@@ -282,11 +282,13 @@ k_ic0_factor(const int32_t *__restrict__ nodes, int count, int color_c, const in
   }
 }
 
-// Earlier / later neighbour counts of every node (thread per node).
-__global__ void k_ic0_count(const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
-                            const int16_t *__restrict__ color, int64_t non, int64_t *__restrict__ fcnt,
-                            int64_t *__restrict__ bcnt) {
-  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < non; j += (int64_t)gridDim.x * blockDim.x) {
+// Earlier / later neighbour counts of every node, in colour order (thread
+// per position of the colour-sorted node list).
+__global__ void k_ic0_count(const int32_t *__restrict__ nodes, const int64_t *__restrict__ nptr,
+                            const int32_t *__restrict__ nadj, const int16_t *__restrict__ color, int64_t non,
+                            int64_t *__restrict__ fcnt, int64_t *__restrict__ bcnt) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < non; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = nodes[t];
     const int16_t cj = color[j];
     int64_t f = 0, b = 0;
     for (int64_t q = nptr[j]; q < nptr[j + 1]; ++q) {
@@ -294,21 +296,24 @@ __global__ void k_ic0_count(const int64_t *__restrict__ nptr, const int32_t *__r
       f += ck < cj;
       b += ck > cj;
     }
-    fcnt[j] = f;
-    bcnt[j] = b;
+    fcnt[t] = f;
+    bcnt[t] = b;
   }
 }
 
-// Packed neighbour lists: for node j its earlier neighbours (forward solve)
-// and later neighbours (backward solve), each with the position of the
-// block in the node's adjacency list.
-__global__ void k_ic0_lists(const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
-                            const int16_t *__restrict__ color, int64_t non, const int64_t *__restrict__ fptr,
-                            const int64_t *__restrict__ bptr, int32_t *__restrict__ fk, int32_t *__restrict__ fsrc,
-                            int32_t *__restrict__ bk, int32_t *__restrict__ bsrc) {
-  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < non; j += (int64_t)gridDim.x * blockDim.x) {
+// Packed neighbour lists in colour order: for the node at position t of the
+// colour-sorted list, its earlier neighbours (forward solve) and later
+// neighbours (backward solve), each with the position of the block in the
+// node's adjacency list.  One colour's lists are then one contiguous run.
+__global__ void k_ic0_lists(const int32_t *__restrict__ nodes, const int64_t *__restrict__ nptr,
+                            const int32_t *__restrict__ nadj, const int16_t *__restrict__ color, int64_t non,
+                            const int64_t *__restrict__ fptr, const int64_t *__restrict__ bptr,
+                            int32_t *__restrict__ fk, int32_t *__restrict__ fsrc, int32_t *__restrict__ bk,
+                            int32_t *__restrict__ bsrc) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < non; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = nodes[t];
     const int16_t cj = color[j];
-    int64_t f = fptr[j], b = bptr[j];
+    int64_t f = fptr[t], b = bptr[t];
     for (int64_t q = nptr[j]; q < nptr[j + 1]; ++q) {
       const int32_t k = nadj[q];
       const int16_t ck = color[k];
@@ -321,6 +326,13 @@ __global__ void k_ic0_lists(const int64_t *__restrict__ nptr, const int32_t *__r
       }
     }
   }
+}
+
+// out[t] = v[nodes[t]]: a per-node int32 array in colour order.
+__global__ void k_ic0_by_color(const int32_t *__restrict__ nodes, const int32_t *__restrict__ v, int64_t non,
+                               int32_t *__restrict__ out) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < non; t += (int64_t)gridDim.x * blockDim.x)
+    out[t] = v[nodes[t]];
 }
 
 // FP32 copies of the factor in packed order (blocks of L with the forward
@@ -344,7 +356,8 @@ struct IcColoring {
   std::vector<int64_t> ptr;      // colour c: nodes [ptr[c], ptr[c+1]) of d_nodes
   int16_t *d_color = nullptr;    // non
   int32_t *d_nodes = nullptr;    // non, sorted by (colour, index)
-  // packed neighbour lists: earlier (f) and later (b) neighbours of every node
+  // packed neighbour lists: earlier (f) and later (b) neighbours of every
+  // node, indexed by the node's position in d_nodes (colour order)
   int64_t *d_fptr = nullptr, *d_bptr = nullptr;     // non + 1
   int32_t *d_fk = nullptr, *d_fsrc = nullptr;       // neighbour, position in the adjacency
   int32_t *d_bk = nullptr, *d_bsrc = nullptr;
@@ -443,7 +456,7 @@ static int ic0_coloring(llf_ctx *ctx, llf_pattern *pat, const std::vector<int64_
   LLF_CUDA_TRY(ctx, cudaMemsetAsync(fcnt + non, 0, sizeof(int64_t), s));
   LLF_CUDA_TRY(ctx, cudaMemsetAsync(bcnt + non, 0, sizeof(int64_t), s));
   const unsigned gt = (unsigned)std::max<int64_t>(1, std::min<int64_t>((non + 127) / 128, (int64_t)ctx->num_sms * 16));
-  k_ic0_count<<<gt, 128, 0, s>>>(pat->d_nptr, pat->d_nadj, cl->d_color, non, fcnt, bcnt);
+  k_ic0_count<<<gt, 128, 0, s>>>(cl->d_nodes, pat->d_nptr, pat->d_nadj, cl->d_color, non, fcnt, bcnt);
   LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_fptr, non + 1));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_bptr, non + 1));
   LLF_CUDA_TRY(ctx, exclusive_scan_i64(ctx, fcnt, cl->d_fptr, non + 1, &cl->nf));
@@ -454,8 +467,8 @@ static int ic0_coloring(llf_ctx *ctx, llf_pattern *pat, const std::vector<int64_
   LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_fsrc, cl->nf));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_bk, cl->nb));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_bsrc, cl->nb));
-  k_ic0_lists<<<gt, 128, 0, s>>>(pat->d_nptr, pat->d_nadj, cl->d_color, non, cl->d_fptr, cl->d_bptr, cl->d_fk,
-                                 cl->d_fsrc, cl->d_bk, cl->d_bsrc);
+  k_ic0_lists<<<gt, 128, 0, s>>>(cl->d_nodes, pat->d_nptr, pat->d_nadj, cl->d_color, non, cl->d_fptr, cl->d_bptr,
+                                 cl->d_fk, cl->d_fsrc, cl->d_bk, cl->d_bsrc);
   LLF_CUDA_TRY(ctx, cudaGetLastError());
   *out = cl;
   return LLF_OK;
@@ -509,12 +522,14 @@ static int ic0_factor_t(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixe
   LLF_CUDA_TRY(ctx, dalloc(ctx, &f->Lf, (size_t)cl->nf * P * P));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &f->Lb, (size_t)cl->nb * P * P));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &f->Ldf, (size_t)non * P * P));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &f->segc, non));
   const unsigned gp = (unsigned)(ctx->num_sms * 16);
   {
     KernelScope ks(ctx, "k_ic0_pack");
     k_ic0_pack<<<gp, 256, 0, s>>>(f->Lrow, cl->d_fsrc, cl->nf, P * P, f->Lf);
     k_ic0_pack<<<gp, 256, 0, s>>>(f->Lcol, cl->d_bsrc, cl->nb, P * P, f->Lb);
-    k_ic0_pack<<<gp, 256, 0, s>>>(f->Ldinv, nullptr, non, P * P, f->Ldf);
+    k_ic0_pack<<<gp, 256, 0, s>>>(f->Ldinv, cl->d_nodes, non, P * P, f->Ldf);
+    k_ic0_by_color<<<gp, 256, 0, s>>>(cl->d_nodes, d_node_seg, non, f->segc);
   }
   LLF_CUDA_TRY(ctx, cudaGetLastError());
   dfree(ctx, f->Lrow);
@@ -540,4 +555,5 @@ void ic0_release(llf_ctx *ctx, Ic0Factor *f) {
   dfree(ctx, f->Lf);
   dfree(ctx, f->Lb);
   dfree(ctx, f->Ldf);
+  dfree(ctx, f->segc);
 }

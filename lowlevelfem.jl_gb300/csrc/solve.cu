@@ -512,14 +512,21 @@ __global__ void k_keep_fixed(const double *__restrict__ x, const uint8_t *__rest
 // IC(0) application z = (L L^T)^-1 r in FP32, one colour per launch, eight
 // lanes per node over the node's packed neighbour list; nodes of converged
 // systems are skipped.  y and z share one FP32 vector (the backward sweep
-// overwrites y_i by z_i once every later z_j is known).
+// overwrites y_i by z_i once every later z_j is known).  The factor, its
+// list pointers, L_jj^-1 and the node -> system map are in colour order, so
+// a launch reads one contiguous run of each; lane g of a node takes list
+// positions g, g + 8, ... two at a time (the same order as one at a time,
+// so the sums do not change).
 constexpr int IC_G = 8;  // lanes per node
 
-template <int P>
+// The forward sweep of one colour (t: position in colour order, first = the
+// colour's first position).  LAST: the last colour, whose backward step
+// z_j = L_jj^-T y_j needs no later neighbour and is done here as well.
+template <int P, bool LAST>
 __global__ void __launch_bounds__(CG_THREADS)
-k_ic0_forward(const int32_t *__restrict__ nodes, int count, const int64_t *__restrict__ fptr,
+k_ic0_forward(const int32_t *__restrict__ nodes, int64_t first, int count, const int64_t *__restrict__ fptr,
               const int32_t *__restrict__ fk, const float *__restrict__ Lf, const float *__restrict__ Ldf,
-              const int32_t *__restrict__ node_seg, const SegState *__restrict__ st,
+              const int32_t *__restrict__ segc, const SegState *__restrict__ st,
               const double *__restrict__ r, float *__restrict__ y) {
   constexpr int PP = P * P;
   const int lane = threadIdx.x & 31, gl = lane & (IC_G - 1);
@@ -528,30 +535,53 @@ k_ic0_forward(const int32_t *__restrict__ nodes, int count, const int64_t *__res
   const int stride = gridDim.x * (blockDim.x >> 5) * per_warp;
   for (int base = wg; base < count; base += stride) {
     const int idx = base + (lane / IC_G);
-    int64_t j = -1;
+    const int64_t t = first + idx;
+    int64_t j = -1, q0 = 0, q1 = 0;
     if (idx < count) {
-      j = nodes[idx];
-      if (st[node_seg[j]].done) j = -1;
+      j = nodes[t];
+      q0 = fptr[t];
+      q1 = fptr[t + 1];
+      if (st[segc[t]].done) j = -1;
     }
     float acc[P];
 #pragma unroll
     for (int a = 0; a < P; ++a) acc[a] = 0.f;
     if (j >= 0)
-      for (int64_t q = fptr[j] + gl; q < fptr[j + 1]; q += IC_G) {
-        const int64_t k = fk[q];
-        const float *L = Lf + q * PP;
+      for (int64_t q = q0 + gl; q < q1; q += 2 * IC_G) {
+        const int64_t q2 = q + IC_G;
+        const bool two = q2 < q1;
+        const int64_t k1 = fk[q], k2 = two ? fk[q2] : k1;
+        float L1[PP], L2[PP], y1[P], y2[P];
+#pragma unroll
+        for (int e = 0; e < PP; ++e) L1[e] = Lf[q * PP + e];
+        if (two) {
+#pragma unroll
+          for (int e = 0; e < PP; ++e) L2[e] = Lf[q2 * PP + e];
+        }
+#pragma unroll
+        for (int m = 0; m < P; ++m) {
+          y1[m] = y[P * k1 + m];
+          y2[m] = y[P * k2 + m];
+        }
 #pragma unroll
         for (int a = 0; a < P; ++a)
 #pragma unroll
-          for (int m = 0; m < P; ++m) acc[a] = fmaf(L[a * P + m], y[P * k + m], acc[a]);
+          for (int m = 0; m < P; ++m) acc[a] = fmaf(L1[a * P + m], y1[m], acc[a]);
+        if (two) {
+#pragma unroll
+          for (int a = 0; a < P; ++a)
+#pragma unroll
+            for (int m = 0; m < P; ++m) acc[a] = fmaf(L2[a * P + m], y2[m], acc[a]);
+        }
       }
 #pragma unroll
     for (int a = 0; a < P; ++a)
 #pragma unroll
       for (int off = IC_G / 2; off > 0; off >>= 1) acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], off);
     if (j >= 0 && gl == 0) {
-      const float *D = Ldf + j * PP;
-      float v[P];
+      float D[PP], v[P], w[P];
+#pragma unroll
+      for (int e = 0; e < PP; ++e) D[e] = Ldf[t * PP + e];
 #pragma unroll
       for (int a = 0; a < P; ++a) v[a] = (float)r[P * j + a] - acc[a];
 #pragma unroll
@@ -559,17 +589,30 @@ k_ic0_forward(const int32_t *__restrict__ nodes, int count, const int64_t *__res
         float s = 0.f;
 #pragma unroll
         for (int m = 0; m <= a; ++m) s = fmaf(D[a * P + m], v[m], s);
-        y[P * j + a] = s;
+        w[a] = s;
       }
+      if (LAST) {  // y_j - 0 then L_jj^-T, as the backward sweep would
+#pragma unroll
+        for (int b = 0; b < P; ++b) v[b] = w[b] - 0.f;
+#pragma unroll
+        for (int b = 0; b < P; ++b) {
+          float s = 0.f;
+#pragma unroll
+          for (int m = b; m < P; ++m) s = fmaf(D[m * P + b], v[m], s);
+          w[b] = s;
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < P; ++a) y[P * j + a] = w[a];
     }
   }
 }
 
 template <int P>
 __global__ void __launch_bounds__(CG_THREADS)
-k_ic0_backward(const int32_t *__restrict__ nodes, int count, const int64_t *__restrict__ bptr,
+k_ic0_backward(const int32_t *__restrict__ nodes, int64_t first, int count, const int64_t *__restrict__ bptr,
                const int32_t *__restrict__ bk, const float *__restrict__ Lb, const float *__restrict__ Ldf,
-               const int32_t *__restrict__ node_seg, const SegState *__restrict__ st, float *__restrict__ z) {
+               const int32_t *__restrict__ segc, const SegState *__restrict__ st, float *__restrict__ z) {
   constexpr int PP = P * P;
   const int lane = threadIdx.x & 31, gl = lane & (IC_G - 1);
   const int per_warp = 32 / IC_G;
@@ -577,32 +620,55 @@ k_ic0_backward(const int32_t *__restrict__ nodes, int count, const int64_t *__re
   const int stride = gridDim.x * (blockDim.x >> 5) * per_warp;
   for (int base = wg; base < count; base += stride) {
     const int idx = base + (lane / IC_G);
-    int64_t i = -1;
+    const int64_t t = first + idx;
+    int64_t i = -1, q0 = 0, q1 = 0;
     if (idx < count) {
-      i = nodes[idx];
-      if (st[node_seg[i]].done) i = -1;
+      i = nodes[t];
+      q0 = bptr[t];
+      q1 = bptr[t + 1];
+      if (st[segc[t]].done) i = -1;
     }
     float acc[P];
 #pragma unroll
     for (int b = 0; b < P; ++b) acc[b] = 0.f;
     if (i >= 0)
-      for (int64_t q = bptr[i] + gl; q < bptr[i + 1]; q += IC_G) {
-        const int64_t jn = bk[q];
-        const float *L = Lb + q * PP;  // L_{jn,i}
+      for (int64_t q = q0 + gl; q < q1; q += 2 * IC_G) {
+        const int64_t q2 = q + IC_G;
+        const bool two = q2 < q1;
+        const int64_t j1 = bk[q], j2 = two ? bk[q2] : j1;
+        float L1[PP], L2[PP], z1[P], z2[P];  // L_{jn,i}
+#pragma unroll
+        for (int e = 0; e < PP; ++e) L1[e] = Lb[q * PP + e];
+        if (two) {
+#pragma unroll
+          for (int e = 0; e < PP; ++e) L2[e] = Lb[q2 * PP + e];
+        }
+#pragma unroll
+        for (int a = 0; a < P; ++a) {
+          z1[a] = z[P * j1 + a];
+          z2[a] = z[P * j2 + a];
+        }
 #pragma unroll
         for (int b = 0; b < P; ++b)
 #pragma unroll
-          for (int a = 0; a < P; ++a) acc[b] = fmaf(L[a * P + b], z[P * jn + a], acc[b]);
+          for (int a = 0; a < P; ++a) acc[b] = fmaf(L1[a * P + b], z1[a], acc[b]);
+        if (two) {
+#pragma unroll
+          for (int b = 0; b < P; ++b)
+#pragma unroll
+            for (int a = 0; a < P; ++a) acc[b] = fmaf(L2[a * P + b], z2[a], acc[b]);
+        }
       }
 #pragma unroll
     for (int b = 0; b < P; ++b)
 #pragma unroll
       for (int off = IC_G / 2; off > 0; off >>= 1) acc[b] += __shfl_xor_sync(0xffffffffu, acc[b], off);
     if (i >= 0 && gl == 0) {
-      const float *D = Ldf + i * PP;
-      float v[P];
+      float D[PP], v[P];
 #pragma unroll
-      for (int b = 0; b < P; ++b) v[b] = z[P * i + b] - acc[b];
+      for (int e = 0; e < PP; ++e) D[e] = Ldf[t * PP + e];
+#pragma unroll
+      for (int b = 0; b < P; ++b) v[b] = z[P * i + b] - acc[b];  // y_i, from an earlier launch
 #pragma unroll
       for (int b = 0; b < P; ++b) {
         float s = 0.f;
@@ -639,7 +705,6 @@ k_seg_zr(Seg S, const float *__restrict__ zf, const double *__restrict__ r, doub
 // IC(0) state of one solve: the factor and the node -> system map.
 struct IcApply {
   const Ic0Factor *f = nullptr;
-  const int32_t *node_seg = nullptr;
   float *zf = nullptr;  // FP32 work vector (ndof)
 };
 
@@ -653,19 +718,26 @@ void enqueue_ic0(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const IcApply 
     const int64_t warps = (count + 32 / IC_G - 1) / (32 / IC_G);
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)ctx->num_sms * 16));
   };
-  for (int c = 0; c < f.ncolors; ++c) {
+  // forward sweeps; the last colour's launch also does its backward step
+  const int C = f.ncolors;
+  for (int c = 0; c < C; ++c) {
     const int count = (int)(f.color_ptr[c + 1] - f.color_ptr[c]);
     if (!count) continue;
     KernelScope k(ctx, "k_ic0_forward");
-    k_ic0_forward<P><<<grid(count), CG_THREADS, 0, s>>>(f.d_nodes + f.color_ptr[c], count, f.fptr, f.fk, f.Lf,
-                                                        f.Ldf, ic.node_seg, S.st, r, ic.zf);
+    const int64_t t0 = f.color_ptr[c];
+    if (c == C - 1)
+      k_ic0_forward<P, true><<<grid(count), CG_THREADS, 0, s>>>(f.d_nodes, t0, count, f.fptr, f.fk, f.Lf, f.Ldf,
+                                                                f.segc, S.st, r, ic.zf);
+    else
+      k_ic0_forward<P, false><<<grid(count), CG_THREADS, 0, s>>>(f.d_nodes, t0, count, f.fptr, f.fk, f.Lf, f.Ldf,
+                                                                 f.segc, S.st, r, ic.zf);
   }
-  for (int c = f.ncolors - 1; c >= 0; --c) {
+  for (int c = C - 2; c >= 0; --c) {
     const int count = (int)(f.color_ptr[c + 1] - f.color_ptr[c]);
     if (!count) continue;
     KernelScope k(ctx, "k_ic0_backward");
-    k_ic0_backward<P><<<grid(count), CG_THREADS, 0, s>>>(f.d_nodes + f.color_ptr[c], count, f.bptr, f.bk, f.Lb,
-                                                         f.Ldf, ic.node_seg, S.st, ic.zf);
+    k_ic0_backward<P><<<grid(count), CG_THREADS, 0, s>>>(f.d_nodes, f.color_ptr[c], count, f.bptr, f.bk, f.Lb,
+                                                         f.Ldf, f.segc, S.st, ic.zf);
   }
   { KernelScope k(ctx, "k_seg_zr"); k_seg_zr<<<gch, CG_THREADS, 0, s>>>(S, ic.zf, r, z, part); }
 }
@@ -792,7 +864,6 @@ struct PcgPlan {
       if (dalloc(ctx, &ic.zf, n) != cudaSuccess)
         return llf_fail(ctx, LLF_ERR_CUDA, "pcg: out of device memory for the IC(0) work vector");
       ic.f = &icf;
-      ic.node_seg = d_node_seg;
     }
     return LLF_OK;
   }
