@@ -6,7 +6,8 @@
 // Ordering.  The node graph of the pattern is coloured once per pattern
 // (Jones-Plassmann rounds with hashed priorities, first-fit colours: nodes
 // coloured in one round are pairwise non-adjacent), and the unknowns are
-// ordered colour by colour.  Within a colour no two nodes are coupled, so
+// ordered colour by colour (within a colour by decreasing degree, which no
+// result depends on).  Within a colour no two nodes are coupled, so
 // every step of the factorisation and of both triangular solves is
 // parallel over the nodes of one colour.
 //
@@ -355,7 +356,7 @@ struct IcColoring {
   int ncolors = 0;
   std::vector<int64_t> ptr;      // colour c: nodes [ptr[c], ptr[c+1]) of d_nodes
   int16_t *d_color = nullptr;    // non
-  int32_t *d_nodes = nullptr;    // non, sorted by (colour, index)
+  int32_t *d_nodes = nullptr;    // non, sorted by (colour, decreasing degree, index)
   // packed neighbour lists: earlier (f) and later (b) neighbours of every
   // node, indexed by the node's position in d_nodes (colour order)
   int64_t *d_fptr = nullptr, *d_bptr = nullptr;     // non + 1
@@ -425,7 +426,9 @@ static int ic0_coloring(llf_ctx *ctx, llf_pattern *pat, const std::vector<int64_
     return rc == LLF_ERR_LIMIT ? rc : llf_fail(ctx, LLF_ERR_LIMIT, "IC(0): more than 256 colours needed");
   }
   std::vector<int16_t> h(non);
+  std::vector<int64_t> hptr(non + 1);
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), ca, sizeof(int16_t) * non, cudaMemcpyDeviceToHost, s));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(hptr.data(), pat->d_nptr, sizeof(int64_t) * (non + 1), cudaMemcpyDeviceToHost, s));
   LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
   IcColoring *cl = new IcColoring;
   cl->seg_nodes = seg_nodes;
@@ -433,9 +436,17 @@ static int ic0_coloring(llf_ctx *ctx, llf_pattern *pat, const std::vector<int64_
   cl->ptr.assign(cl->ncolors + 1, 0);
   for (int64_t i = 0; i < non; ++i) cl->ptr[h[i] + 1]++;
   for (int c = 0; c < cl->ncolors; ++c) cl->ptr[c + 1] += cl->ptr[c];
-  std::vector<int32_t> nodes(non);
+  // within a colour, nodes by decreasing degree (then index): the rows that
+  // one warp of a sweep serves have lists of similar length
+  int64_t maxdeg = 0;
+  for (int64_t i = 0; i < non; ++i) maxdeg = std::max(maxdeg, hptr[i + 1] - hptr[i]);
+  std::vector<int64_t> dcnt(maxdeg + 2, 0);
+  for (int64_t i = 0; i < non; ++i) dcnt[maxdeg - (hptr[i + 1] - hptr[i]) + 1]++;
+  for (int64_t d = 0; d <= maxdeg; ++d) dcnt[d + 1] += dcnt[d];
+  std::vector<int32_t> bydeg(non), nodes(non);
+  for (int64_t i = 0; i < non; ++i) bydeg[dcnt[maxdeg - (hptr[i + 1] - hptr[i])]++] = (int32_t)i;
   std::vector<int64_t> fill(cl->ptr.begin(), cl->ptr.end() - 1);
-  for (int64_t i = 0; i < non; ++i) nodes[fill[h[i]]++] = (int32_t)i;
+  for (int64_t i : bydeg) nodes[fill[h[i]]++] = (int32_t)i;
   cl->d_color = ca;
   cudaError_t e = dalloc(ctx, &cl->d_nodes, non);
   if (e == cudaSuccess)

@@ -513,10 +513,11 @@ __global__ void k_keep_fixed(const double *__restrict__ x, const uint8_t *__rest
 // lanes per node over the node's packed neighbour list; nodes of converged
 // systems are skipped.  y and z share one FP32 vector (the backward sweep
 // overwrites y_i by z_i once every later z_j is known).  The factor, its
-// list pointers, L_jj^-1 and the node -> system map are in colour order, so
-// a launch reads one contiguous run of each; lane g of a node takes list
-// positions g, g + 8, ... two at a time (the same order as one at a time,
-// so the sums do not change).
+// list pointers, L_jj^-1 and the node -> system map are in colour order (a
+// colour's nodes by decreasing degree), so a launch reads one contiguous run
+// of each and the four nodes of a warp have lists of similar length; lane g
+// of a node takes list positions g, g + 8, ... two at a time (the same order
+// as one at a time, so the sums do not change).
 constexpr int IC_G = 8;  // lanes per node
 
 // The forward sweep of one colour (t: position in colour order, first = the
