@@ -37,6 +37,8 @@ namespace {
 
 constexpr int CG_THREADS = 256;
 constexpr int CHUNK = 768;  // DoFs per reduction chunk (a multiple of every pdim: chunks hold whole nodes)
+constexpr int CHUNK_PER_THREAD = CHUNK / CG_THREADS;  // a chunk's DoFs per thread of its block
+static_assert(CHUNK % CG_THREADS == 0, "a chunk is whole rounds of a block");
 
 struct SegState {
   double rho_prev, rho, alpha, res, res0, tol;
@@ -237,6 +239,12 @@ struct Seg {
                                // [nseg, 2nseg) the update's, [2nseg, 3nseg) the IC(0) z.r's)
 };
 
+// One block per chunk for the kernels of a CG iteration (direction, product,
+// update, z.r): a chunk is three DoFs per thread, so its state and data
+// loads are latency that only more chunks in flight hide, and the block
+// scheduler balances the products' uneven chunks.
+inline unsigned chunk_grid(const Seg &S) { return (unsigned)std::max<int64_t>(1, S.nchunks); }
+
 // Last-block-done segment reduction: after a chunk's partial is written,
 // thread 0 fences and counts the chunk in; the block that brings in the
 // segment's last chunk sees every partial (fence, then L2 loads) and sums
@@ -366,8 +374,12 @@ __global__ void k_seg_dir(Seg S, const double *__restrict__ z, double *__restric
     const SegState &q = S.st[S.cseg[ch]];
     if (q.done) continue;
     const double beta = q.rho / q.rho_prev;
-    for (int64_t i = S.cbeg[ch] + threadIdx.x; i < S.cend[ch]; i += blockDim.x)
-      u[i] = __fma_rn(beta, u[i], z[i]);
+    const int64_t b = S.cbeg[ch], e = S.cend[ch];
+#pragma unroll
+    for (int k = 0; k < CHUNK_PER_THREAD; ++k) {
+      const int64_t i = b + threadIdx.x + (int64_t)k * CG_THREADS;
+      if (i < e) u[i] = __fma_rn(beta, u[i], z[i]);
+    }
   }
 }
 
@@ -447,11 +459,16 @@ k_seg_update_fused(Seg S, double *__restrict__ xw, double *__restrict__ r, const
     if (q.done) continue;
     const double alpha = q.alpha;
     double rr = 0.0, zr = 0.0;
-    for (int64_t i = S.cbeg[ch] + threadIdx.x; i < S.cend[ch]; i += blockDim.x) {
-      xw[i] = __fma_rn(alpha, u[i], xw[i]);
-      const double ri = __fma_rn(-alpha, c[i], r[i]);
-      r[i] = ri;
-      rr = __fma_rn(ri, ri, rr);
+    const int64_t b = S.cbeg[ch], e = S.cend[ch];
+#pragma unroll
+    for (int k = 0; k < CHUNK_PER_THREAD; ++k) {
+      const int64_t i = b + threadIdx.x + (int64_t)k * CG_THREADS;
+      if (i < e) {
+        xw[i] = __fma_rn(alpha, u[i], xw[i]);
+        const double ri = __fma_rn(-alpha, c[i], r[i]);
+        r[i] = ri;
+        rr = __fma_rn(ri, ri, rr);
+      }
     }
     if (local_prec) {  // the block-Jacobi blocks stay within the chunk (whole nodes): own r only
       __syncthreads();
@@ -688,10 +705,15 @@ k_seg_zr(Seg S, const float *__restrict__ zf, const double *__restrict__ r, doub
   for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
     if (S.st[S.cseg[ch]].done) continue;
     double zr = 0.0;
-    for (int64_t i = S.cbeg[ch] + threadIdx.x; i < S.cend[ch]; i += blockDim.x) {
-      const double zi = (double)zf[i];
-      z[i] = zi;
-      zr = __fma_rn(zi, r[i], zr);
+    const int64_t b = S.cbeg[ch], e = S.cend[ch];
+#pragma unroll
+    for (int k = 0; k < CHUNK_PER_THREAD; ++k) {
+      const int64_t i = b + threadIdx.x + (int64_t)k * CG_THREADS;
+      if (i < e) {
+        const double zi = (double)zf[i];
+        z[i] = zi;
+        zr = __fma_rn(zi, r[i], zr);
+      }
     }
     double s = block_sum(zr);
     if (threadIdx.x == 0) part[ch] = s;
@@ -740,7 +762,7 @@ void enqueue_ic0(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const IcApply 
     k_ic0_backward<P><<<grid(count), CG_THREADS, 0, s>>>(f.d_nodes, f.color_ptr[c], count, f.bptr, f.bk, f.Lb,
                                                          f.Ldf, f.segc, S.st, ic.zf);
   }
-  { KernelScope k(ctx, "k_seg_zr"); k_seg_zr<<<gch, CG_THREADS, 0, s>>>(S, ic.zf, r, z, part); }
+  { KernelScope k(ctx, "k_seg_zr"); k_seg_zr<<<chunk_grid(S), CG_THREADS, 0, s>>>(S, ic.zf, r, z, part); }
 }
 
 // z = M^-1 r and rho = z.r of the first iteration.
@@ -767,12 +789,13 @@ void enqueue_iteration(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const do
   const llf_pattern *pat = m->pat;
   cudaStream_t s = ctx->stream;
   const bool local = precond != LLF_PRECOND_IC0;
-  { KernelScope k(ctx, "k_seg_dir"); k_seg_dir<<<gch, CG_THREADS, 0, s>>>(S, z, u); }
+  { KernelScope k(ctx, "k_seg_dir"); k_seg_dir<<<chunk_grid(S), CG_THREADS, 0, s>>>(S, z, u); }
   { KernelScope k(ctx, "k_seg_spmv");
-    k_seg_spmv<P><<<gch, CG_THREADS, 0, s>>>(S, m->d_nz, pat->d_nptr, pat->d_nadj, u, fixed, c, part); }
+    k_seg_spmv<P><<<chunk_grid(S), CG_THREADS, 0, s>>>(S, m->d_nz, pat->d_nptr, pat->d_nadj, u, fixed, c, part); }
   { KernelScope k(ctx, "k_seg_alpha"); k_seg_alpha<<<gseg, CG_THREADS, 0, s>>>(S, part); }
   { KernelScope k(ctx, "k_seg_update");
-    k_seg_update_fused<P><<<gch, CG_THREADS, 0, s>>>(S, xw, r, u, c, part, part2, pinv, precond, local, fixed, z); }
+    k_seg_update_fused<P><<<chunk_grid(S), CG_THREADS, 0, s>>>(S, xw, r, u, c, part, part2, pinv, precond, local,
+                                                               fixed, z); }
   if (!local) enqueue_ic0<P>(ctx, S, m, ic, r, z, part, gch);
 }
 
