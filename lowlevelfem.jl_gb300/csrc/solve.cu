@@ -537,6 +537,41 @@ __global__ void k_keep_fixed(const double *__restrict__ x, const uint8_t *__rest
 // as one at a time, so the sums do not change).
 constexpr int IC_G = 8;  // lanes per node
 
+// Programmatic dependent launch: a sweep launched with programmatic stream
+// serialisation starts while the previous sweep finishes, loads what no
+// sweep writes (node data, lists, factor blocks, system states), then waits
+// for the previous grid before it reads y / z.  It releases its own
+// dependent only after that wait, so a launch never overlaps more than its
+// predecessor.  Without the launch attribute both instructions are no-ops.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_release() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+// The next two list positions of a lane (q and q + IC_G, both before q1):
+// neighbour indices and blocks, loaded ahead of the products that need them.
+template <int P>
+struct IcPair {
+  bool one = false, two = false;
+  int64_t k1 = 0, k2 = 0;
+  float L1[P * P], L2[P * P];
+  __device__ __forceinline__ void load(bool live, int64_t q, int64_t q1, const int32_t *__restrict__ lk,
+                                       const float *__restrict__ Lv) {
+    constexpr int PP = P * P;
+    one = live && q < q1;
+    two = one && q + IC_G < q1;
+    if (one) {
+      k1 = lk[q];
+#pragma unroll
+      for (int e = 0; e < PP; ++e) L1[e] = Lv[q * PP + e];
+    }
+    k2 = k1;
+    if (two) {
+      k2 = lk[q + IC_G];
+#pragma unroll
+      for (int e = 0; e < PP; ++e) L2[e] = Lv[(q + IC_G) * PP + e];
+    }
+  }
+};
+
 // The forward sweep of one colour (t: position in colour order, first = the
 // colour's first position).  LAST: the last colour, whose backward step
 // z_j = L_jj^-T y_j needs no later neighbour and is done here as well.
@@ -551,6 +586,7 @@ k_ic0_forward(const int32_t *__restrict__ nodes, int64_t first, int count, const
   const int per_warp = 32 / IC_G;
   const int wg = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * per_warp;
   const int stride = gridDim.x * (blockDim.x >> 5) * per_warp;
+  bool waited = false;
   for (int base = wg; base < count; base += stride) {
     const int idx = base + (lane / IC_G);
     const int64_t t = first + idx;
@@ -564,34 +600,34 @@ k_ic0_forward(const int32_t *__restrict__ nodes, int64_t first, int count, const
     float acc[P];
 #pragma unroll
     for (int a = 0; a < P; ++a) acc[a] = 0.f;
-    if (j >= 0)
-      for (int64_t q = q0 + gl; q < q1; q += 2 * IC_G) {
-        const int64_t q2 = q + IC_G;
-        const bool two = q2 < q1;
-        const int64_t k1 = fk[q], k2 = two ? fk[q2] : k1;
-        float L1[PP], L2[PP], y1[P], y2[P];
+    IcPair<P> pr;
+    int64_t q = q0 + gl;
+    pr.load(j >= 0, q, q1, fk, Lf);
+    if (!waited) {  // y of earlier colours: written by the previous launches
+      grid_dep_wait();
+      grid_dep_release();
+      waited = true;
+    }
+    while (pr.one) {
+      float y1[P], y2[P];
 #pragma unroll
-        for (int e = 0; e < PP; ++e) L1[e] = Lf[q * PP + e];
-        if (two) {
+      for (int m = 0; m < P; ++m) {
+        y1[m] = y[P * pr.k1 + m];
+        y2[m] = y[P * pr.k2 + m];
+      }
 #pragma unroll
-          for (int e = 0; e < PP; ++e) L2[e] = Lf[q2 * PP + e];
-        }
+      for (int a = 0; a < P; ++a)
 #pragma unroll
-        for (int m = 0; m < P; ++m) {
-          y1[m] = y[P * k1 + m];
-          y2[m] = y[P * k2 + m];
-        }
+        for (int m = 0; m < P; ++m) acc[a] = fmaf(pr.L1[a * P + m], y1[m], acc[a]);
+      if (pr.two) {
 #pragma unroll
         for (int a = 0; a < P; ++a)
 #pragma unroll
-          for (int m = 0; m < P; ++m) acc[a] = fmaf(L1[a * P + m], y1[m], acc[a]);
-        if (two) {
-#pragma unroll
-          for (int a = 0; a < P; ++a)
-#pragma unroll
-            for (int m = 0; m < P; ++m) acc[a] = fmaf(L2[a * P + m], y2[m], acc[a]);
-        }
+          for (int m = 0; m < P; ++m) acc[a] = fmaf(pr.L2[a * P + m], y2[m], acc[a]);
       }
+      q += 2 * IC_G;
+      pr.load(true, q, q1, fk, Lf);
+    }
 #pragma unroll
     for (int a = 0; a < P; ++a)
 #pragma unroll
@@ -636,6 +672,7 @@ k_ic0_backward(const int32_t *__restrict__ nodes, int64_t first, int count, cons
   const int per_warp = 32 / IC_G;
   const int wg = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * per_warp;
   const int stride = gridDim.x * (blockDim.x >> 5) * per_warp;
+  bool waited = false;
   for (int base = wg; base < count; base += stride) {
     const int idx = base + (lane / IC_G);
     const int64_t t = first + idx;
@@ -649,34 +686,34 @@ k_ic0_backward(const int32_t *__restrict__ nodes, int64_t first, int count, cons
     float acc[P];
 #pragma unroll
     for (int b = 0; b < P; ++b) acc[b] = 0.f;
-    if (i >= 0)
-      for (int64_t q = q0 + gl; q < q1; q += 2 * IC_G) {
-        const int64_t q2 = q + IC_G;
-        const bool two = q2 < q1;
-        const int64_t j1 = bk[q], j2 = two ? bk[q2] : j1;
-        float L1[PP], L2[PP], z1[P], z2[P];  // L_{jn,i}
+    IcPair<P> pr;  // blocks L_{jn,i}
+    int64_t q = q0 + gl;
+    pr.load(i >= 0, q, q1, bk, Lb);
+    if (!waited) {  // z of later colours: written by the previous launches
+      grid_dep_wait();
+      grid_dep_release();
+      waited = true;
+    }
+    while (pr.one) {
+      float z1[P], z2[P];
 #pragma unroll
-        for (int e = 0; e < PP; ++e) L1[e] = Lb[q * PP + e];
-        if (two) {
+      for (int a = 0; a < P; ++a) {
+        z1[a] = z[P * pr.k1 + a];
+        z2[a] = z[P * pr.k2 + a];
+      }
 #pragma unroll
-          for (int e = 0; e < PP; ++e) L2[e] = Lb[q2 * PP + e];
-        }
+      for (int b = 0; b < P; ++b)
 #pragma unroll
-        for (int a = 0; a < P; ++a) {
-          z1[a] = z[P * j1 + a];
-          z2[a] = z[P * j2 + a];
-        }
+        for (int a = 0; a < P; ++a) acc[b] = fmaf(pr.L1[a * P + b], z1[a], acc[b]);
+      if (pr.two) {
 #pragma unroll
         for (int b = 0; b < P; ++b)
 #pragma unroll
-          for (int a = 0; a < P; ++a) acc[b] = fmaf(L1[a * P + b], z1[a], acc[b]);
-        if (two) {
-#pragma unroll
-          for (int b = 0; b < P; ++b)
-#pragma unroll
-            for (int a = 0; a < P; ++a) acc[b] = fmaf(L2[a * P + b], z2[a], acc[b]);
-        }
+          for (int a = 0; a < P; ++a) acc[b] = fmaf(pr.L2[a * P + b], z2[a], acc[b]);
       }
+      q += 2 * IC_G;
+      pr.load(true, q, q1, bk, Lb);
+    }
 #pragma unroll
     for (int b = 0; b < P; ++b)
 #pragma unroll
@@ -741,26 +778,45 @@ void enqueue_ic0(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const IcApply 
     const int64_t warps = (count + 32 / IC_G - 1) / (32 / IC_G);
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)ctx->num_sms * 16));
   };
-  // forward sweeps; the last colour's launch also does its backward step
+  // forward sweeps; the last colour's launch also does its backward step.
+  // Every sweep but the first follows another sweep and starts early (PDL).
   const int C = f.ncolors;
+  bool after_sweep = false;
+  auto launch = [&](auto kern, int count, auto... args) {
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid(count));
+    cfg.blockDim = dim3(CG_THREADS);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = after_sweep ? 1 : 0;
+    after_sweep = true;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+  };
   for (int c = 0; c < C; ++c) {
     const int count = (int)(f.color_ptr[c + 1] - f.color_ptr[c]);
     if (!count) continue;
     KernelScope k(ctx, "k_ic0_forward");
     const int64_t t0 = f.color_ptr[c];
     if (c == C - 1)
-      k_ic0_forward<P, true><<<grid(count), CG_THREADS, 0, s>>>(f.d_nodes, t0, count, f.fptr, f.fk, f.Lf, f.Ldf,
-                                                                f.segc, S.st, r, ic.zf);
+      launch(k_ic0_forward<P, true>, count, (const int32_t *)f.d_nodes, t0, count,
+             (const int64_t *)f.fptr, (const int32_t *)f.fk, (const float *)f.Lf, (const float *)f.Ldf,
+             (const int32_t *)f.segc, (const SegState *)S.st, r, ic.zf);
     else
-      k_ic0_forward<P, false><<<grid(count), CG_THREADS, 0, s>>>(f.d_nodes, t0, count, f.fptr, f.fk, f.Lf, f.Ldf,
-                                                                 f.segc, S.st, r, ic.zf);
+      launch(k_ic0_forward<P, false>, count, (const int32_t *)f.d_nodes, t0, count,
+             (const int64_t *)f.fptr, (const int32_t *)f.fk, (const float *)f.Lf, (const float *)f.Ldf,
+             (const int32_t *)f.segc, (const SegState *)S.st, r, ic.zf);
   }
   for (int c = C - 2; c >= 0; --c) {
     const int count = (int)(f.color_ptr[c + 1] - f.color_ptr[c]);
     if (!count) continue;
     KernelScope k(ctx, "k_ic0_backward");
-    k_ic0_backward<P><<<grid(count), CG_THREADS, 0, s>>>(f.d_nodes, f.color_ptr[c], count, f.bptr, f.bk, f.Lb,
-                                                         f.Ldf, f.segc, S.st, ic.zf);
+    launch(k_ic0_backward<P>, count, (const int32_t *)f.d_nodes, (int64_t)f.color_ptr[c], count,
+           (const int64_t *)f.bptr, (const int32_t *)f.bk, (const float *)f.Lb, (const float *)f.Ldf,
+           (const int32_t *)f.segc, (const SegState *)S.st, ic.zf);
   }
   { KernelScope k(ctx, "k_seg_zr"); k_seg_zr<<<chunk_grid(S), CG_THREADS, 0, s>>>(S, ic.zf, r, z, part); }
 }
