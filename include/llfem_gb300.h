@@ -464,7 +464,7 @@ int llf_heat_fdm(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C,
  * d_fixed, each of the matrix's DoF count — and the call allocates nothing:
  * no cudaMalloc, cudaMallocAsync or cudaFree, no library allocator.  The CG
  * work vectors live in one fixed array compiled into the library
- * (about 8.4 MB for LLF_NOALLOC_MAX_DOFS = 131072 unknowns), which every GPU
+ * (about 8.7 MB for LLF_NOALLOC_MAX_DOFS = 131072 unknowns), which every GPU
  * that loads the library holds until the process exits.
  *
  * Same algorithm and results as llf_pcg (IterativeSolvers.cg recurrence and

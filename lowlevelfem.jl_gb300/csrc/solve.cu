@@ -79,14 +79,13 @@ __device__ __forceinline__ double block_sum(double v) {
 constexpr int SPMV_G = 4;
 
 template <int P>
-__device__ __forceinline__ void node_columns(const double *__restrict__ nz, const int64_t *__restrict__ nptr,
-                                             const int32_t *__restrict__ nadj, const double *__restrict__ x,
-                                             int64_t B, bool valid, int g, double (&acc)[P]) {
+__device__ __forceinline__ void node_columns_at(const double *__restrict__ nz, const int32_t *__restrict__ nadj,
+                                                const double *__restrict__ x, int64_t r0, int64_t r1, bool valid,
+                                                int g, double (&acc)[P]) {
 #pragma unroll
   for (int j = 0; j < P; ++j) acc[j] = 0.0;
   if (valid) {
-    const int64_t r0 = nptr[B];
-    const int n = (int)(nptr[B + 1] - r0) * P;  // entries per column
+    const int n = (int)(r1 - r0) * P;  // entries per column
     const double *col = nz + (int64_t)P * r0 * P;
     int k = g;
     for (; k + SPMV_G < n; k += 2 * SPMV_G) {
@@ -112,6 +111,15 @@ __device__ __forceinline__ void node_columns(const double *__restrict__ nz, cons
   for (int off = SPMV_G / 2; off > 0; off >>= 1)
 #pragma unroll
     for (int j = 0; j < P; ++j) acc[j] = __dadd_rn(acc[j], __shfl_xor_sync(0xffffffffu, acc[j], off));
+}
+
+// The same for node B, whose row nodes are nadj[nptr[B] .. nptr[B+1]).
+template <int P>
+__device__ __forceinline__ void node_columns(const double *__restrict__ nz, const int64_t *__restrict__ nptr,
+                                             const int32_t *__restrict__ nadj, const double *__restrict__ x,
+                                             int64_t B, bool valid, int g, double (&acc)[P]) {
+  const int64_t r0 = valid ? nptr[B] : 0, r1 = valid ? nptr[B + 1] : 0;
+  node_columns_at<P>(nz, nadj, x, r0, r1, valid, g, acc);
 }
 
 // y = A x for all columns (plain product, llf_matrix_spmv), SPMV_G lanes per
@@ -237,6 +245,7 @@ struct Seg {
   int *active;
   int *arrive;                 // 3*nseg arrival counters of the fused reductions (zero between uses;
                                // [nseg, 2nseg) the update's, [2nseg, 3nseg) the IC(0) z.r's)
+  const int16_t *perm;         // per node position: the product's node order within its chunk (or null)
 };
 
 // One block per chunk for the kernels of a CG iteration (direction, product,
@@ -383,10 +392,12 @@ __global__ void k_seg_dir(Seg S, const double *__restrict__ z, double *__restric
   }
 }
 
-// c = A u on the chunk's columns (masked) and partial u.c.  One warp per
-// node column B (chunks start and end on node boundaries): lanes take the
-// column's row nodes, read each row node's P values of u once and apply the
-// P x P block of all P DoF columns of B.
+// c = A u on the chunk's columns (masked) and partial u.c.  SPMV_G lanes per
+// node column B (chunks start and end on node boundaries), the chunk's nodes
+// taken in the order S.perm gives (decreasing degree: the eight nodes of a
+// warp have lists of similar length, so few lanes idle in the FP64 products).
+// A column's sums do not depend on the order; the partial u.c takes its
+// nodes in that fixed order.
 template <int P>
 __global__ void __launch_bounds__(CG_THREADS)
 k_seg_spmv(Seg S, const double *__restrict__ nz, const int64_t *__restrict__ nptr,
@@ -397,12 +408,23 @@ k_seg_spmv(Seg S, const double *__restrict__ nz, const int64_t *__restrict__ npt
   for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
     if (S.st[S.cseg[ch]].done) continue;
     double dot = 0.0;
-    const int64_t B1 = S.cend[ch] / P;
-    for (int64_t B0 = S.cbeg[ch] / P + (int64_t)w * NPW; B0 < B1; B0 += (int64_t)wpb * NPW) {
-      const int64_t B = B0 + lane / SPMV_G;
+    const int64_t b0 = S.cbeg[ch] / P;
+    const int nb = (int)(S.cend[ch] / P - b0);
+    const int step = wpb * NPW;
+    // this lane group's node of the round and of the next one, with its row
+    // range loaded a round ahead
+    auto node_of = [&](int r) -> int64_t { return b0 + (r < nb ? (S.perm ? (int)S.perm[b0 + r] : r) : 0); };
+    int r = w * NPW + lane / SPMV_G;
+    int64_t B = node_of(r);
+    int64_t q0 = r < nb ? nptr[B] : 0, q1 = r < nb ? nptr[B + 1] : 0;
+    for (int r0 = w * NPW; r0 < nb; r0 += step, r += step) {
+      const bool valid = r < nb;
+      const int64_t Bn = node_of(r + step);
+      const bool vn = r + step < nb;
+      const int64_t q0n = vn ? nptr[Bn] : 0, q1n = vn ? nptr[Bn + 1] : 0;
       double acc[P];
-      node_columns<P>(nz, nptr, nadj, u, B, B < B1, g, acc);
-      if (B < B1 && g == 0) {
+      node_columns_at<P>(nz, nadj, u, q0, q1, valid, g, acc);
+      if (valid && g == 0) {
 #pragma unroll
         for (int j = 0; j < P; ++j) {
           const int64_t d = P * B + j;
@@ -411,9 +433,34 @@ k_seg_spmv(Seg S, const double *__restrict__ nz, const int64_t *__restrict__ npt
           dot = __fma_rn(u[d], v, dot);
         }
       }
+      B = Bn;
+      q0 = q0n;
+      q1 = q1n;
     }
     double s = block_sum(dot);
     if (threadIdx.x == 0) part[ch] = s;
+  }
+}
+
+// The product's node order of every chunk: decreasing degree, then index.
+// perm[b0 + r] = offset in the chunk (first node b0) of its r-th node.  A
+// block ranks one chunk's degrees in shared memory (a chunk has at most
+// CHUNK nodes).
+__global__ void __launch_bounds__(CG_THREADS)
+k_chunk_perm(Seg S, const int64_t *__restrict__ nptr, int P, int16_t *__restrict__ perm) {
+  __shared__ int deg[CHUNK];
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    const int64_t b0 = S.cbeg[ch] / P;
+    const int nb = (int)(S.cend[ch] / P - b0);
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) deg[i] = (int)(nptr[b0 + i + 1] - nptr[b0 + i]);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+      const int di = deg[i];
+      int rank = 0;
+      for (int k = 0; k < nb; ++k) rank += deg[k] > di || (deg[k] == di && k < i);
+      perm[b0 + rank] = (int16_t)i;
+    }
+    __syncthreads();
   }
 }
 
@@ -876,6 +923,7 @@ struct PcgPlan {
   double *r = nullptr, *z = nullptr, *u = nullptr, *c = nullptr, *xw = nullptr, *pinv = nullptr, *part = nullptr;
   double *part2 = nullptr;
   int *d_arrive = nullptr;
+  int16_t *d_perm = nullptr;
   Ic0Factor icf;
   IcApply ic;
   int32_t *d_node_seg = nullptr;
@@ -925,7 +973,12 @@ struct PcgPlan {
     }
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_sf, sf.data(), sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, s));
     LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_active, 0, sizeof(int), s));
-    S = Seg{d_cb, d_ce, d_cs, d_sf, nch, nseg, d_st, d_active, d_arrive};
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_perm, pat->mesh->non));
+    S = Seg{d_cb, d_ce, d_cs, d_sf, nch, nseg, d_st, d_active, d_arrive, d_perm};
+    if (nch) {
+      KernelScope k(ctx, "k_chunk_perm");
+      k_chunk_perm<<<chunk_grid(S), CG_THREADS, 0, s>>>(S, pat->d_nptr, P, d_perm);
+    }
     hst.assign(nseg, SegState{});
     // IC(0): factor of A with the fixed DoFs as identity rows, node -> system map
     if (precond == LLF_PRECOND_IC0) {
@@ -964,7 +1017,7 @@ struct PcgPlan {
     }
     dfree(ctx, d_cb); dfree(ctx, d_ce); dfree(ctx, d_cs); dfree(ctx, d_sf); dfree(ctx, d_active);
     dfree(ctx, d_st); dfree(ctx, r); dfree(ctx, z); dfree(ctx, u); dfree(ctx, c); dfree(ctx, xw);
-    dfree(ctx, pinv); dfree(ctx, part); dfree(ctx, part2); dfree(ctx, d_arrive);
+    dfree(ctx, pinv); dfree(ctx, part); dfree(ctx, part2); dfree(ctx, d_arrive); dfree(ctx, d_perm);
   }
 };
 
@@ -1099,7 +1152,8 @@ constexpr size_t NA_OFF_CS = NA_OFF_SF + na_round(sizeof(int64_t) * 2);
 constexpr size_t NA_OFF_ST = NA_OFF_CS + na_round(sizeof(int32_t) * NA_CH);
 constexpr size_t NA_OFF_ACT = NA_OFF_ST + na_round(sizeof(SegState));  // active counter, then 3 arrival counters
 constexpr size_t NA_OFF_PART2 = NA_OFF_ACT + 256;
-constexpr size_t NA_BYTES = NA_OFF_PART2 + na_round(sizeof(double) * NA_CH);
+constexpr size_t NA_OFF_PERM = NA_OFF_PART2 + na_round(sizeof(double) * NA_CH);
+constexpr size_t NA_BYTES = NA_OFF_PERM + na_round(sizeof(int16_t) * NA_N);  // the product's node order (<= NA_N nodes)
 
 }  // namespace
 
@@ -1161,6 +1215,7 @@ int pcg_noalloc_typed(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doub
   int *active = (int *)(base + NA_OFF_ACT);
   int *arrive = active + 1;
   double *part2 = (double *)(base + NA_OFF_PART2);
+  int16_t *perm = (int16_t *)(base + NA_OFF_PERM);
   const int64_t nch = (n + CHUNK - 1) / CHUNK;
   // the array keeps the previous call's contents: the active-system counter
   // and the three arrival counters must start at zero; every other region
@@ -1169,7 +1224,12 @@ int pcg_noalloc_typed(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doub
   k_na_chunks<<<1, 64, 0, ctx->stream>>>(cb, ce, cs, sf, n, nch);
   ctx->launches++;
   LLF_CUDA_TRY(ctx, cudaGetLastError());
-  Seg S{cb, ce, cs, sf, nch, 1, st, active, arrive};
+  Seg S{cb, ce, cs, sf, nch, 1, st, active, arrive, perm};
+  if (nch) {  // the same node order as llf_pcg's plan, so the same sums
+    KernelScope k(ctx, "k_chunk_perm");
+    k_chunk_perm<<<chunk_grid(S), CG_THREADS, 0, ctx->stream>>>(S, m->pat->d_nptr, P, perm);
+  }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
   SegState hst[1];
   rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, part2, precond, reltol, maxiter,
                    false, hst);
