@@ -127,81 +127,121 @@ __device__ __forceinline__ double a_prime(const double *__restrict__ nz, int64_t
   return nz[(size_t)P * P * ci0 + (size_t)cc * P * degi + (size_t)P * ti + r];
 }
 
-// Factorisation of the nodes of one colour (warp per node).
+// Factorisation of the nodes of one colour, a warp per node j.  The blocks
+// L_ji of row j are made in colour order of i (L_ji needs the L_jk of
+// colours before i's), a group of up to IcFac<P>::SLOTS neighbours i of one
+// colour at a time:
+//   1. all lanes go over j's list: the common neighbours k of j and i of an
+//      earlier colour than i (and j's place in i's list) are found by binary
+//      search in i's list and kept, in j's list order, in shared memory;
+//   2. lane (slot, a, b) sums entry (a, b) of S = sum_k L_jk L_ik^T over
+//      them (the FMA order of a lane doing all P*P entries), forms
+//      A'_ji - S and, with the other lanes of its row a, entry (a, b) of
+//      (A'_ji - S) L_ii^-T.
+// Every lane of a slot takes the same path, so the FP64 instructions run
+// with P*P lanes per pair (the GB300's FP64 pipe is spent per warp
+// instruction, however few lanes take part).
+template <int P>
+struct IcFac {
+  static constexpr int PP = P * P;
+  static constexpr int SLOTS = 32 / PP < 8 ? 32 / PP : 8;  // pairs per group
+};
+
 template <int P>
 __global__ void __launch_bounds__(IC_THREADS)
-k_ic0_factor(const int32_t *__restrict__ nodes, int count, int color_c, const int64_t *__restrict__ nptr,
-             const int32_t *__restrict__ nadj, const int32_t *__restrict__ diagpos,
-             const int16_t *__restrict__ color, const double *__restrict__ nz,
+k_ic0_factor(const int32_t *__restrict__ nodes, const int64_t *__restrict__ fptr, const int32_t *__restrict__ fk,
+             const int32_t *__restrict__ fsrc, const int32_t *__restrict__ fcol, int count, int max_deg,
+             const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
+             const int32_t *__restrict__ diagpos, const int16_t *__restrict__ color, const double *__restrict__ nz,
              const uint8_t *__restrict__ fixed, double shift, double *__restrict__ Lrow,
              double *__restrict__ Lcol, double *__restrict__ Ldinv, int *fail) {
-  constexpr int PP = P * P;
-  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-  for (int w = blockIdx.x * wpb + (threadIdx.x >> 5); w < count; w += gridDim.x * wpb) {
+  constexpr int PP = P * P, NS = IcFac<P>::SLOTS;
+  extern __shared__ int16_t ic_fac_smem[];  // per warp: NS lists of max_deg (u, v) pairs
+  __shared__ int s_nm[IC_THREADS / 32][NS], s_tj[IC_THREADS / 32][NS];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  int16_t *mu = ic_fac_smem + (size_t)wib * NS * max_deg * 2, *mv = mu + (size_t)NS * max_deg;
+  const int slot = lane / PP, e = lane % PP, ea = e / P, eb = e % P;
+  for (int w = blockIdx.x * wpb + wib; w < count; w += gridDim.x * wpb) {
     const int64_t j = nodes[w];
     const int64_t c0 = nptr[j];
     const int deg = (int)(nptr[j + 1] - c0);
     const int32_t *rj = nadj + c0;
-    // off-diagonal blocks of row j, one earlier colour at a time
-    for (int cp = 0; cp < color_c; ++cp) {
-      for (int t = lane; t < deg; t += 32) {
-        const int64_t i = rj[t];
-        if (color[i] != cp) continue;
+    const int cj = color[j];
+    const int64_t pe = fptr[w + 1];
+    for (int64_t p = fptr[w]; p < pe;) {
+      const int cp = color[fk[fcol[p]]];
+      int n = 1;
+      while (n < NS && p + n < pe && color[fk[fcol[p + n]]] == cp) ++n;
+      // 1. common neighbours of an earlier colour, in j's list order
+      for (int sl = 0; sl < n; ++sl) {
+        const int64_t i = fk[fcol[p + sl]];
         const int64_t ci0 = nptr[i];
         const int degi = (int)(nptr[i + 1] - ci0);
         const int32_t *ri = nadj + ci0;
-        double S[P][P];
-#pragma unroll
-        for (int a = 0; a < P; ++a)
-#pragma unroll
-          for (int b = 0; b < P; ++b) S[a][b] = 0.0;
-        for (int u = 0; u < deg; ++u) {
-          const int32_t k = rj[u];
-          if (color[k] >= cp) continue;
-          const int pk = bsearch_row(ri, degi, k);
-          if (pk < 0) continue;
-          const double *Ljk = Lrow + (size_t)(c0 + u) * PP;
-          const double *Lik = Lrow + (size_t)(ci0 + pk) * PP;
-#pragma unroll
-          for (int a = 0; a < P; ++a)
-#pragma unroll
-            for (int b = 0; b < P; ++b)
-#pragma unroll
-              for (int m = 0; m < P; ++m) S[a][b] = __fma_rn(Ljk[a * P + m], Lik[b * P + m], S[a][b]);
-        }
-        const int tj = bsearch_row(ri, degi, (int32_t)j);  // j in i's list
-        if (tj < 0) {  // the node pattern is symmetric; a miss means corrupt input
-          atomicOr((unsigned *)fail, 2u);
-          continue;
-        }
-        double Bm[P][P];
-#pragma unroll
-        for (int a = 0; a < P; ++a)
-#pragma unroll
-          for (int b = 0; b < P; ++b)
-            Bm[a][b] = __dsub_rn(a_prime<P>(nz, ci0, degi, tj, a, b, j, i, fixed), S[a][b]);
-        const double *Di = Ldinv + (size_t)i * PP;  // L_ii^-1, lower
-        double X[P][P];
-#pragma unroll
-        for (int a = 0; a < P; ++a)
-#pragma unroll
-          for (int b = 0; b < P; ++b) {
-            double acc = 0.0;
-#pragma unroll
-            for (int m = 0; m < P; ++m) acc = __fma_rn(Bm[a][m], Di[b * P + m], acc);
-            X[a][b] = acc;
+        int cnt = 0, tj = -1;
+        for (int ub = 0; ub < deg; ub += 32) {
+          const int u = ub + lane;
+          int v = -1;
+          bool self = false;
+          if (u < deg) {
+            const int32_t k = rj[u];
+            self = k == (int32_t)j;
+            if (self || color[k] < cp) v = bsearch_row(ri, degi, k);
           }
-        double *lr = Lrow + (size_t)(c0 + t) * PP;
-        double *lc = Lcol + (size_t)(ci0 + tj) * PP;
-#pragma unroll
-        for (int a = 0; a < P; ++a)
-#pragma unroll
-          for (int b = 0; b < P; ++b) {
-            lr[a * P + b] = X[a][b];
-            lc[a * P + b] = X[a][b];
+          const bool hit = v >= 0 && !self;
+          const unsigned bh = __ballot_sync(0xffffffffu, hit);
+          if (hit) {
+            const int at = cnt + __popc(bh & ((1u << lane) - 1u));
+            mu[sl * max_deg + at] = (int16_t)u;
+            mv[sl * max_deg + at] = (int16_t)v;
           }
+          cnt += __popc(bh);
+          const unsigned bj = __ballot_sync(0xffffffffu, self && v >= 0);
+          if (bj) tj = __shfl_sync(0xffffffffu, v, __ffs(bj) - 1);
+        }
+        if (lane == 0) {
+          s_nm[wib][sl] = cnt;
+          s_tj[wib][sl] = tj;
+        }
       }
       __syncwarp();
+      // 2. entry (ea, eb) of pair `slot`
+      const bool act = slot < n;
+      int64_t i = 0, ci0 = 0;
+      int degi = 0, tj = -1, t = 0;
+      double S = 0.0;
+      if (act) {
+        const int32_t q = fcol[p + slot];
+        i = fk[q];
+        t = (int)(fsrc[q] - c0);
+        ci0 = nptr[i];
+        degi = (int)(nptr[i + 1] - ci0);
+        tj = s_tj[wib][slot];
+        const int nm = s_nm[wib][slot];
+        for (int h = 0; h < nm; ++h) {
+          const double *Ljk = Lrow + (size_t)(c0 + mu[slot * max_deg + h]) * PP + ea * P;
+          const double *Lik = Lrow + (size_t)(ci0 + mv[slot * max_deg + h]) * PP + eb * P;
+#pragma unroll
+          for (int m = 0; m < P; ++m) S = __fma_rn(Ljk[m], Lik[m], S);
+        }
+      }
+      const double Bm = act && tj >= 0 ? __dsub_rn(a_prime<P>(nz, ci0, degi, tj, ea, eb, j, i, fixed), S) : 0.0;
+      double X = 0.0;
+#pragma unroll
+      for (int m = 0; m < P; ++m) {
+        const double bm = __shfl_sync(0xffffffffu, Bm, (slot * PP + ea * P + m) & 31);  // entry (ea, m)
+        if (act) X = __fma_rn(bm, Ldinv[(size_t)i * PP + eb * P + m], X);
+      }
+      if (act) {
+        if (tj < 0) {  // the node pattern is symmetric; a miss means corrupt input
+          if (e == 0) atomicOr((unsigned *)fail, 2u);
+        } else {
+          Lrow[(size_t)(c0 + t) * PP + e] = X;
+          Lcol[(size_t)(ci0 + tj) * PP + e] = X;
+        }
+      }
+      __syncwarp();
+      p += n;
     }
     // diagonal block
     double D[P][P];
@@ -211,7 +251,7 @@ k_ic0_factor(const int32_t *__restrict__ nodes, int count, int color_c, const in
       for (int b = 0; b < P; ++b) D[a][b] = 0.0;
     for (int t = lane; t < deg; t += 32) {
       const int32_t k = rj[t];
-      if (color[k] >= color_c) continue;
+      if (color[k] >= cj) continue;
       const double *Ljk = Lrow + (size_t)(c0 + t) * PP;
 #pragma unroll
       for (int a = 0; a < P; ++a)
@@ -306,11 +346,13 @@ __global__ void k_ic0_count(const int32_t *__restrict__ nodes, const int64_t *__
 // colour-sorted list, its earlier neighbours (forward solve) and later
 // neighbours (backward solve), each with the position of the block in the
 // node's adjacency list.  One colour's lists are then one contiguous run.
+// fcol orders each node's forward list by the neighbours' colour (then list
+// order): the factorisation takes the blocks of row t in that order.
 __global__ void k_ic0_lists(const int32_t *__restrict__ nodes, const int64_t *__restrict__ nptr,
                             const int32_t *__restrict__ nadj, const int16_t *__restrict__ color, int64_t non,
                             const int64_t *__restrict__ fptr, const int64_t *__restrict__ bptr,
                             int32_t *__restrict__ fk, int32_t *__restrict__ fsrc, int32_t *__restrict__ bk,
-                            int32_t *__restrict__ bsrc) {
+                            int32_t *__restrict__ bsrc, int32_t *__restrict__ fcol) {
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < non; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = nodes[t];
     const int16_t cj = color[j];
@@ -326,6 +368,10 @@ __global__ void k_ic0_lists(const int32_t *__restrict__ nodes, const int64_t *__
         bsrc[b++] = (int32_t)q;
       }
     }
+    int64_t o = fptr[t];
+    for (int16_t cc = 0; cc < cj; ++cc)
+      for (int64_t u = fptr[t]; u < f; ++u)
+        if (color[fk[u]] == cc) fcol[o++] = (int32_t)u;
   }
 }
 
@@ -362,6 +408,7 @@ struct IcColoring {
   int64_t *d_fptr = nullptr, *d_bptr = nullptr;     // non + 1
   int32_t *d_fk = nullptr, *d_fsrc = nullptr;       // neighbour, position in the adjacency
   int32_t *d_bk = nullptr, *d_bsrc = nullptr;
+  int32_t *d_fcol = nullptr;                        // forward-list positions by colour (factorisation order)
   int64_t nf = 0, nb = 0;
 };
 
@@ -373,6 +420,7 @@ void ic0_coloring_free(llf_ctx *ctx, llf_pattern *pat) {
   dfree(ctx, cl->d_fptr); dfree(ctx, cl->d_bptr);
   dfree(ctx, cl->d_fk); dfree(ctx, cl->d_fsrc);
   dfree(ctx, cl->d_bk); dfree(ctx, cl->d_bsrc);
+  dfree(ctx, cl->d_fcol);
   delete cl;
   pat->ic_coloring = nullptr;
 }
@@ -478,8 +526,9 @@ static int ic0_coloring(llf_ctx *ctx, llf_pattern *pat, const std::vector<int64_
   LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_fsrc, cl->nf));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_bk, cl->nb));
   LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_bsrc, cl->nb));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &cl->d_fcol, cl->nf));
   k_ic0_lists<<<gt, 128, 0, s>>>(cl->d_nodes, pat->d_nptr, pat->d_nadj, cl->d_color, non, cl->d_fptr, cl->d_bptr,
-                                 cl->d_fk, cl->d_fsrc, cl->d_bk, cl->d_bsrc);
+                                 cl->d_fk, cl->d_fsrc, cl->d_bk, cl->d_bsrc, cl->d_fcol);
   LLF_CUDA_TRY(ctx, cudaGetLastError());
   *out = cl;
   return LLF_OK;
@@ -503,6 +552,13 @@ static int ic0_factor_t(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixe
   LLF_CUDA_TRY(ctx, dalloc(ctx, &f->Ldinv, (size_t)non * P * P));
   int *d_fail = nullptr;
   LLF_CUDA_TRY(ctx, dalloc(ctx, &d_fail, 1));
+  // the factorisation's per-warp match lists: NS x max_deg (u, v) pairs of int16
+  const int md = std::max(1, pat->max_deg);
+  if (md > 32767) return llf_fail(ctx, LLF_ERR_LIMIT, "IC(0): a node has more than 32767 neighbours");
+  const size_t per_warp = (size_t)IcFac<P>::SLOTS * md * 2 * sizeof(int16_t);
+  const int fwpb = (int)std::min<size_t>(IC_THREADS / 32, (48 * 1024) / per_warp);
+  if (fwpb < 1) return llf_fail(ctx, LLF_ERR_LIMIT, "IC(0): node degree too large for the factorisation");
+  const size_t fsmem = per_warp * fwpb;
   const double shifts[] = {0.0, 1e-4, 1e-3, 1e-2, 1e-1, 1.0};
   int fail = 1;
   for (double shift : shifts) {
@@ -512,11 +568,13 @@ static int ic0_factor_t(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixe
     for (int c = 0; c < cl->ncolors; ++c) {
       const int count = (int)(cl->ptr[c + 1] - cl->ptr[c]);
       if (count == 0) continue;
-      const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((count + 7) / 8, (int64_t)ctx->num_sms * 16));
+      const unsigned grid = (unsigned)std::max<int64_t>(
+          1, std::min<int64_t>((count + fwpb - 1) / fwpb, (int64_t)ctx->num_sms * 32));
       KernelScope ks(ctx, "k_ic0_factor");
-      k_ic0_factor<P><<<grid, IC_THREADS, 0, s>>>(cl->d_nodes + cl->ptr[c], count, c, pat->d_nptr, pat->d_nadj,
-                                                  pat->d_diagpos, cl->d_color, m->d_nz, d_fixed, shift, f->Lrow,
-                                                  f->Lcol, f->Ldinv, d_fail);
+      k_ic0_factor<P><<<grid, 32 * fwpb, fsmem, s>>>(cl->d_nodes + cl->ptr[c], cl->d_fptr + cl->ptr[c], cl->d_fk,
+                                                     cl->d_fsrc, cl->d_fcol, count, md, pat->d_nptr, pat->d_nadj,
+                                                     pat->d_diagpos, cl->d_color, m->d_nz, d_fixed, shift, f->Lrow,
+                                                     f->Lcol, f->Ldinv, d_fail);
     }
     LLF_CUDA_TRY(ctx, cudaGetLastError());
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&fail, d_fail, sizeof(int), cudaMemcpyDeviceToHost, s));
