@@ -88,21 +88,26 @@ __device__ __forceinline__ void node_columns_at(const double *__restrict__ nz, c
     const int n = (int)(r1 - r0) * P;  // entries per column
     const double *col = nz + (int64_t)P * r0 * P;
     int k = g;
+    // the row nodes of the step's two entries, loaded a step ahead so that
+    // only the gather of x waits on a load
+    int32_t ra = k < n ? nadj[r0 + k / P] : 0, rb = k + SPMV_G < n ? nadj[r0 + (k + SPMV_G) / P] : 0;
     for (; k + SPMV_G < n; k += 2 * SPMV_G) {
-      const int k2 = k + SPMV_G;
+      const int k2 = k + SPMV_G, kn = k + 2 * SPMV_G;
       double v[P], v2[P];
 #pragma unroll
       for (int j = 0; j < P; ++j) {
         v[j] = col[(int64_t)j * n + k];
         v2[j] = col[(int64_t)j * n + k2];
       }
-      const double xa = x[(int64_t)P * nadj[r0 + k / P] + k % P];
-      const double xb = x[(int64_t)P * nadj[r0 + k2 / P] + k2 % P];
+      const double xa = x[(int64_t)P * ra + k % P];
+      const double xb = x[(int64_t)P * rb + k2 % P];
+      ra = kn < n ? nadj[r0 + kn / P] : 0;
+      rb = kn + SPMV_G < n ? nadj[r0 + (kn + SPMV_G) / P] : 0;
 #pragma unroll
       for (int j = 0; j < P; ++j) acc[j] = __fma_rn(v2[j], xb, __fma_rn(v[j], xa, acc[j]));
     }
     if (k < n) {
-      const double xa = x[(int64_t)P * nadj[r0 + k / P] + k % P];
+      const double xa = x[(int64_t)P * ra + k % P];
 #pragma unroll
       for (int j = 0; j < P; ++j) acc[j] = __fma_rn(col[(int64_t)j * n + k], xa, acc[j]);
     }
