@@ -4,7 +4,7 @@
 // src/poisson.jl:1432-1546).
 //
 // Ordering.  The node graph of the pattern is coloured once per pattern
-// (Jones-Plassmann rounds with hashed priorities, first-fit colours: nodes
+// (Jones-Plassmann rounds with degree-then-hash priorities, first-fit colours: nodes
 // coloured in one round are pairwise non-adjacent), and the unknowns are
 // ordered colour by colour (within a colour by decreasing degree, which no
 // result depends on).  Within a colour no two nodes are coupled, so
@@ -46,10 +46,12 @@ __device__ __forceinline__ uint32_t jp_hash(uint32_t x) {
   return x;
 }
 
-// One Jones-Plassmann round: an uncoloured node whose priority (hash of its
-// index within its system, then that index) is the largest among its
-// uncoloured neighbours takes the smallest colour none of its coloured
-// neighbours has.  Priorities relative to the system's first node make the
+// One Jones-Plassmann round: an uncoloured node whose priority (its degree,
+// then the hash of its index within its system, then that index) is the
+// largest among its uncoloured neighbours takes the smallest colour none of
+// its coloured neighbours has.  Degree first (largest-degree-first) needs
+// fewer colours than the hash alone (tet10: 15 against 18), so the sweeps
+// make fewer launches.  Priorities relative to the system's first node make the
 // colouring of a system the same alone and inside a batch.  Reads cin,
 // writes cout (a copy of cin plus this round's colours); counts the nodes
 // left uncoloured.
@@ -80,7 +82,8 @@ __global__ void k_jp_round(const int64_t *__restrict__ nptr, const int32_t *__re
         used[ca >> 5] |= 1u << (ca & 31);
       } else {
         const uint32_t la = (uint32_t)(A - base), ha = jp_hash(la);  // A is in B's system
-        if (ha > hb || (ha == hb && la > lb)) beaten = true;
+        const int dega = (int)(nptr[A + 1] - nptr[A]);
+        if (dega > deg || (dega == deg && (ha > hb || (ha == hb && la > lb)))) beaten = true;
       }
     }
     beaten = __any_sync(0xffffffffu, beaten);
