@@ -249,7 +249,8 @@ struct Seg {
   SegState *st;
   int *active;
   int *arrive;                 // 3*nseg arrival counters of the fused reductions (zero between uses;
-                               // [nseg, 2nseg) the update's, [2nseg, 3nseg) the IC(0) z.r's)
+                               // [0, nseg) the product's u.c, [nseg, 2nseg) the update's,
+                               // [2nseg, 3nseg) the IC(0) z.r's)
   const int16_t *perm;         // per node position: the product's node order within its chunk (or null)
 };
 
@@ -402,7 +403,8 @@ __global__ void k_seg_dir(Seg S, const double *__restrict__ z, double *__restric
 // taken in the order S.perm gives (decreasing degree: the eight nodes of a
 // warp have lists of similar length, so few lanes idle in the FP64 products).
 // A column's sums do not depend on the order; the partial u.c takes its
-// nodes in that fixed order.
+// nodes in that fixed order.  The block that brings in a segment's last
+// chunk sums the partials (chunk order) and sets alpha = rho / u.c.
 template <int P>
 __global__ void __launch_bounds__(CG_THREADS)
 k_seg_spmv(Seg S, const double *__restrict__ nz, const int64_t *__restrict__ nptr,
@@ -444,6 +446,11 @@ k_seg_spmv(Seg S, const double *__restrict__ nz, const int64_t *__restrict__ npt
     }
     double s = block_sum(dot);
     if (threadIdx.x == 0) part[ch] = s;
+    const int sg = S.cseg[ch];
+    if (arrive_last(S.arrive + sg, S.sfirst[sg + 1] - S.sfirst[sg])) {
+      const double uc = seg_total_l2(S, sg, part);
+      if (threadIdx.x == 0) seg_set_alpha(S, sg, uc);
+    }
   }
 }
 
@@ -469,32 +476,7 @@ k_chunk_perm(Seg S, const int64_t *__restrict__ nptr, int P, int16_t *__restrict
   }
 }
 
-__global__ void k_seg_alpha(Seg S, const double *part) {
-  for (int s = blockIdx.x; s < S.nseg; s += gridDim.x) {
-    if (S.st[s].done) continue;
-    double uc = seg_total(S, s, part);
-    if (threadIdx.x == 0) seg_set_alpha(S, s, uc);
-  }
-}
 
-__global__ void __launch_bounds__(CG_THREADS)
-k_seg_update(Seg S, double *__restrict__ xw, double *__restrict__ r, const double *__restrict__ u,
-             const double *__restrict__ c, double *__restrict__ part) {
-  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
-    const SegState &q = S.st[S.cseg[ch]];
-    if (q.done) continue;
-    const double alpha = q.alpha;
-    double rr = 0.0;
-    for (int64_t i = S.cbeg[ch] + threadIdx.x; i < S.cend[ch]; i += blockDim.x) {
-      xw[i] = __fma_rn(alpha, u[i], xw[i]);
-      double ri = __fma_rn(-alpha, c[i], r[i]);
-      r[i] = ri;
-      rr = __fma_rn(ri, ri, rr);
-    }
-    double s = block_sum(rr);
-    if (threadIdx.x == 0) part[ch] = s;
-  }
-}
 
 // x += alpha u, r -= alpha c and the residual check; with a local
 // preconditioner (mode NONE, JACOBI, BJACOBI) also z = M^-1 r and rho = z.r
@@ -547,22 +529,6 @@ k_seg_update_fused(Seg S, double *__restrict__ xw, double *__restrict__ r, const
   }
 }
 
-__global__ void k_seg_finish(Seg S, const double *part) {
-  for (int s = blockIdx.x; s < S.nseg; s += gridDim.x) {
-    if (S.st[s].done) continue;
-    double rr = seg_total(S, s, part);
-    if (threadIdx.x == 0) {
-      SegState &q = S.st[s];
-      q.res = sqrt(rr);
-      q.rho_prev = q.rho;
-      q.it += 1;
-      if (q.res <= q.tol || q.it >= q.maxiter) {
-        q.done = 1;
-        atomicSub(S.active, 1);
-      }
-    }
-  }
-}
 
 __global__ void k_cg_merge(const double *__restrict__ xw, const uint8_t *__restrict__ fixed,
                            double *__restrict__ x, int64_t n) {
@@ -887,20 +853,20 @@ void enqueue_first_prec(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const d
   { KernelScope k(ctx, "k_seg_rho"); k_seg_rho<<<gseg, CG_THREADS, 0, s>>>(S, part); }
 }
 
-// One CG iteration: u = z + beta u; c = A u; alpha; x, r updated with the
-// residual check, then the next z and rho (fused for the local
-// preconditioners, the IC(0) sweeps after the update otherwise).
+// One CG iteration: u = z + beta u; c = A u with alpha = rho / u.c made by
+// each segment's last product block (u.c partials in part3); x and r
+// updated with the residual check, then the next z and rho (fused for the
+// local preconditioners, the IC(0) sweeps after the update otherwise).
 template <int P>
 void enqueue_iteration(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const double *pinv, int precond,
                        double *r, double *z, double *u, double *c, double *xw, const uint8_t *fixed,
-                       double *part, double *part2, unsigned gch, unsigned gseg, const IcApply &ic) {
+                       double *part, double *part2, double *part3, unsigned gch, unsigned gseg, const IcApply &ic) {
   const llf_pattern *pat = m->pat;
   cudaStream_t s = ctx->stream;
   const bool local = precond != LLF_PRECOND_IC0;
   { KernelScope k(ctx, "k_seg_dir"); k_seg_dir<<<chunk_grid(S), CG_THREADS, 0, s>>>(S, z, u); }
   { KernelScope k(ctx, "k_seg_spmv");
-    k_seg_spmv<P><<<chunk_grid(S), CG_THREADS, 0, s>>>(S, m->d_nz, pat->d_nptr, pat->d_nadj, u, fixed, c, part); }
-  { KernelScope k(ctx, "k_seg_alpha"); k_seg_alpha<<<gseg, CG_THREADS, 0, s>>>(S, part); }
+    k_seg_spmv<P><<<chunk_grid(S), CG_THREADS, 0, s>>>(S, m->d_nz, pat->d_nptr, pat->d_nadj, u, fixed, c, part3); }
   { KernelScope k(ctx, "k_seg_update");
     k_seg_update_fused<P><<<chunk_grid(S), CG_THREADS, 0, s>>>(S, xw, r, u, c, part, part2, pinv, precond, local,
                                                                fixed, z); }
@@ -910,7 +876,7 @@ void enqueue_iteration(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const do
 template <int P>
 int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
              const Seg &S, double *r, double *z, double *u, double *c, double *xw, double *pinv,
-             double *part, double *part2, int precond, double reltol, int64_t maxiter, bool use_graph,
+             double *part, double *part2, double *part3, int precond, double reltol, int64_t maxiter, bool use_graph,
              SegState *hst, const IcApply &ic = IcApply());
 int pcg_outcome(llf_ctx *ctx, int nseg, const SegState *hst, int64_t *iters, double *relres);
 
@@ -926,7 +892,7 @@ struct PcgPlan {
   int *d_active = nullptr;
   SegState *d_st = nullptr;
   double *r = nullptr, *z = nullptr, *u = nullptr, *c = nullptr, *xw = nullptr, *pinv = nullptr, *part = nullptr;
-  double *part2 = nullptr;
+  double *part2 = nullptr, *part3 = nullptr;
   int *d_arrive = nullptr;
   int16_t *d_perm = nullptr;
   Ic0Factor icf;
@@ -969,6 +935,7 @@ struct PcgPlan {
     LLF_CUDA_TRY(ctx, dalloc(ctx, &pinv, precond == LLF_PRECOND_BJACOBI ? n * P : n));
     LLF_CUDA_TRY(ctx, dalloc(ctx, &part, nch));
     LLF_CUDA_TRY(ctx, dalloc(ctx, &part2, nch));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &part3, nch));
     LLF_CUDA_TRY(ctx, dalloc(ctx, &d_arrive, 3 * (int64_t)nseg));
     LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_arrive, 0, sizeof(int) * 3 * nseg, s));
     if (nch) {
@@ -1008,7 +975,7 @@ struct PcgPlan {
 
   int solve(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
             double reltol, int64_t maxiter, int64_t *iters, double *relres) {
-    int rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, part2, precond, reltol,
+    int rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, part2, part3, precond, reltol,
                          maxiter, !ctx->profiling, hst.data(), ic);
     if (rc != LLF_OK) return rc;
     return pcg_outcome(ctx, nseg, hst.data(), iters, relres);
@@ -1022,7 +989,8 @@ struct PcgPlan {
     }
     dfree(ctx, d_cb); dfree(ctx, d_ce); dfree(ctx, d_cs); dfree(ctx, d_sf); dfree(ctx, d_active);
     dfree(ctx, d_st); dfree(ctx, r); dfree(ctx, z); dfree(ctx, u); dfree(ctx, c); dfree(ctx, xw);
-    dfree(ctx, pinv); dfree(ctx, part); dfree(ctx, part2); dfree(ctx, d_arrive); dfree(ctx, d_perm);
+    dfree(ctx, pinv); dfree(ctx, part); dfree(ctx, part2); dfree(ctx, part3); dfree(ctx, d_arrive);
+    dfree(ctx, d_perm);
   }
 };
 
@@ -1045,7 +1013,7 @@ int pcg_segments(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d
 template <int P>
 int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
              const Seg &S, double *r, double *z, double *u, double *c, double *xw, double *pinv,
-             double *part, double *part2, int precond, double reltol, int64_t maxiter, bool use_graph,
+             double *part, double *part2, double *part3, int precond, double reltol, int64_t maxiter, bool use_graph,
              SegState *hst, const IcApply &ic) {
   const llf_pattern *pat = m->pat;
   const int64_t n = pat->ndof;
@@ -1078,7 +1046,7 @@ int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, 
     cudaGraph_t graph = nullptr;
     if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       const long long saved = ctx->launches;
-      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, part2, gch, gseg, ic);
+      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, part2, part3, gch, gseg, ic);
       launches_per_graph = ctx->launches - saved;
       ctx->launches = saved;
       if (cudaStreamEndCapture(s, &graph) != cudaSuccess ||
@@ -1097,7 +1065,7 @@ int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, 
       LLF_CUDA_TRY(ctx, cudaGraphLaunch(exec, s));
       ctx->launches += launches_per_graph;
     } else {
-      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, part2, gch, gseg, ic);
+      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, part2, part3, gch, gseg, ic);
     }
     LLF_CUDA_TRY(ctx, cudaGetLastError());
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(h_active, d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1157,7 +1125,8 @@ constexpr size_t NA_OFF_CS = NA_OFF_SF + na_round(sizeof(int64_t) * 2);
 constexpr size_t NA_OFF_ST = NA_OFF_CS + na_round(sizeof(int32_t) * NA_CH);
 constexpr size_t NA_OFF_ACT = NA_OFF_ST + na_round(sizeof(SegState));  // active counter, then 3 arrival counters
 constexpr size_t NA_OFF_PART2 = NA_OFF_ACT + 256;
-constexpr size_t NA_OFF_PERM = NA_OFF_PART2 + na_round(sizeof(double) * NA_CH);
+constexpr size_t NA_OFF_PART3 = NA_OFF_PART2 + na_round(sizeof(double) * NA_CH);
+constexpr size_t NA_OFF_PERM = NA_OFF_PART3 + na_round(sizeof(double) * NA_CH);
 constexpr size_t NA_BYTES = NA_OFF_PERM + na_round(sizeof(int16_t) * NA_N);  // the product's node order (<= NA_N nodes)
 
 }  // namespace
@@ -1219,7 +1188,7 @@ int pcg_noalloc_typed(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doub
   SegState *st = (SegState *)(base + NA_OFF_ST);
   int *active = (int *)(base + NA_OFF_ACT);
   int *arrive = active + 1;
-  double *part2 = (double *)(base + NA_OFF_PART2);
+  double *part2 = (double *)(base + NA_OFF_PART2), *part3 = (double *)(base + NA_OFF_PART3);
   int16_t *perm = (int16_t *)(base + NA_OFF_PERM);
   const int64_t nch = (n + CHUNK - 1) / CHUNK;
   // the array keeps the previous call's contents: the active-system counter
@@ -1236,7 +1205,7 @@ int pcg_noalloc_typed(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doub
   }
   LLF_CUDA_TRY(ctx, cudaGetLastError());
   SegState hst[1];
-  rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, part2, precond, reltol, maxiter,
+  rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, part2, part3, precond, reltol, maxiter,
                    false, hst);
   if (rc != LLF_OK) return rc;
   return pcg_outcome(ctx, 1, hst, iters, relres);
