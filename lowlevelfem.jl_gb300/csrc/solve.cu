@@ -788,7 +788,7 @@ struct IcApply {
 
 template <int P>
 void enqueue_ic0(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const IcApply &ic, const double *r, double *z,
-                 double *part, unsigned gch) {
+                 double *part) {
   const Ic0Factor &f = *ic.f;
   cudaStream_t s = ctx->stream;
   (void)m;
@@ -846,7 +846,7 @@ void enqueue_first_prec(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const d
                         const IcApply &ic) {
   cudaStream_t s = ctx->stream;
   if (precond == LLF_PRECOND_IC0) {
-    enqueue_ic0<P>(ctx, S, m, ic, r, z, part, gch);  // its z.r sets rho
+    enqueue_ic0<P>(ctx, S, m, ic, r, z, part);  // its z.r sets rho
     return;
   }
   { KernelScope k(ctx, "k_seg_prec"); k_seg_prec<P><<<gch, CG_THREADS, 0, s>>>(S, pinv, precond, r, fixed, z, part); }
@@ -860,7 +860,7 @@ void enqueue_first_prec(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const d
 template <int P>
 void enqueue_iteration(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const double *pinv, int precond,
                        double *r, double *z, double *u, double *c, double *xw, const uint8_t *fixed,
-                       double *part, double *part2, double *part3, unsigned gch, unsigned gseg, const IcApply &ic) {
+                       double *part, double *part2, double *part3, const IcApply &ic) {
   const llf_pattern *pat = m->pat;
   cudaStream_t s = ctx->stream;
   const bool local = precond != LLF_PRECOND_IC0;
@@ -870,7 +870,7 @@ void enqueue_iteration(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const do
   { KernelScope k(ctx, "k_seg_update");
     k_seg_update_fused<P><<<chunk_grid(S), CG_THREADS, 0, s>>>(S, xw, r, u, c, part, part2, pinv, precond, local,
                                                                fixed, z); }
-  if (!local) enqueue_ic0<P>(ctx, S, m, ic, r, z, part, gch);
+  if (!local) enqueue_ic0<P>(ctx, S, m, ic, r, z, part);
 }
 
 template <int P>
@@ -1046,7 +1046,7 @@ int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, 
     cudaGraph_t graph = nullptr;
     if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       const long long saved = ctx->launches;
-      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, part2, part3, gch, gseg, ic);
+      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, part2, part3, ic);
       launches_per_graph = ctx->launches - saved;
       ctx->launches = saved;
       if (cudaStreamEndCapture(s, &graph) != cudaSuccess ||
@@ -1065,7 +1065,7 @@ int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, 
       LLF_CUDA_TRY(ctx, cudaGraphLaunch(exec, s));
       ctx->launches += launches_per_graph;
     } else {
-      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, part2, part3, gch, gseg, ic);
+      for (int k = 0; k < per_graph; ++k) enqueue_iteration<P>(ctx, S, m, pinv, precond, r, z, u, c, xw, d_fixed, part, part2, part3, ic);
     }
     LLF_CUDA_TRY(ctx, cudaGetLastError());
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(h_active, d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
