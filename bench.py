@@ -214,8 +214,9 @@ def _pct(v, q):
 
 def run_batched(args, llf):
     """Batched configuration: independent tet10 boxes assembled in one launch
-    and solved by one segmented Jacobi-PCG (CUDA graph).  Solves/s and the
-    relative displacement error of sample instances against a direct solve."""
+    and solved by one segmented PCG (IC(0) by default; CUDA graph).  Solves/s
+    and the relative displacement error of sample instances against a direct
+    solve."""
     import numpy as np
     import torch
     from llfem_gb300 import workloads as wl
