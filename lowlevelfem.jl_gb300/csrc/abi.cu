@@ -502,6 +502,7 @@ int llf_pattern_destroy(llf_ctx *ctx, llf_pattern *p) {
     dfree(ctx, p->d_n2e_ptr); dfree(ctx, p->d_n2e); dfree(ctx, p->d_nptr);
     dfree(ctx, p->d_nadj); dfree(ctx, p->d_diagpos); dfree(ctx, p->d_colptr);
     dfree(ctx, p->d_pos);
+    dfree(ctx, p->d_gather_nodes);
     ic0_coloring_free(ctx, p);
     cudaStreamSynchronize(ctx->stream);
   }

@@ -123,6 +123,13 @@ struct llf_pattern {
   uint16_t *d_pos = nullptr;
   int conn_version = 0;           // mesh connectivity the pattern was built from
   void *ic_coloring = nullptr;    // node colouring of the IC(0) preconditioner (ic0.cu), on first use
+  // the gather's column nodes in two degree classes (assemble.cu, on first
+  // use): d_gather_nodes holds the nodes of degree <= gather_md_low, then
+  // the others; each class runs with a buffer sized for its own degrees
+  int32_t *d_gather_nodes = nullptr;
+  int64_t gather_n_low = 0;
+  int gather_md_low = 0;
+  bool gather_split_done = false;
   // per column slab of the to-host assembly: one past the largest element
   // index that a node of this or an earlier slab touches (assemble.cu)
   std::vector<int64_t> slab_elem_end;
