@@ -415,8 +415,9 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
   double *acc = cg_smem + (size_t)wib * max_deg * P * P;
   unsigned char *has = reinterpret_cast<unsigned char *>(cg_smem + (size_t)wpb * max_deg * P * P) +
                        (size_t)wib * ((max_deg + 7) & ~7);
-  for (int64_t w = (int64_t)blockIdx.x * wpb + wib; w < non; w += (int64_t)gridDim.x * wpb) {
-    const int64_t B = list ? (int64_t)list[w] : w;  // column node (non: nodes of the list)
+  const int nw = (int)non, wstride = (int)gridDim.x * wpb;  // node counts fit int32 (nadj holds int32 nodes)
+  for (int w = (int)blockIdx.x * wpb + wib; w < nw; w += wstride) {
+    const int64_t B = list ? (int64_t)__ldg(list + w) : (int64_t)w;  // column node (non: nodes of the list)
     const int64_t c0 = nptr[B];
     const int deg = (int)(nptr[B + 1] - c0);
     const int64_t s = n2e_ptr[B];
