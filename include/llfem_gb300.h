@@ -125,6 +125,11 @@ int llf_profile_enable(llf_ctx *ctx, int on);
 int llf_profile_reset(llf_ctx *ctx);
 int llf_profile_report(llf_ctx *ctx, char *buf, int64_t len, int64_t *needed);
 int llf_launch_count(llf_ctx *ctx, int64_t *launches);
+/* Device allocations the context has made since it was created (every
+ * stream-ordered allocation of an entry point counts once).  A diagnostic
+ * counter with no reference counterpart: a caller can check that a call
+ * allocated nothing by reading it before and after. */
+int llf_alloc_count(llf_ctx *ctx, int64_t *allocs);
 
 /* ======================================================================== */
 /* Built-in quadrature and shape tables (host only, no GPU needed)          */
@@ -468,14 +473,24 @@ int llf_heat_fdm(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C,
  * that loads the library holds until the process exits.
  *
  * Same algorithm and results as llf_pcg (IterativeSolvers.cg recurrence and
- * stopping rule, Dirichlet masking); systems above LLF_NOALLOC_MAX_DOFS are
- * rejected with LLF_ERR_LIMIT.  The first call on a device looks up the
- * array's device address for that device (make that first call before any
- * stream capture).  All calls share the one array and it keeps the previous
- * call's contents; each call clears on its own stream what has to start at
- * zero (the count of unconverged systems) and writes every other work
- * vector before reading it.  Calls whose work overlaps on the GPU (two
- * contexts or threads at once) race on the array: serialise them. */
+ * stopping rule, Dirichlet masking) with the preconditioners none, Jacobi
+ * and block Jacobi; IC(0) is not available here (its factor and colouring
+ * need memory sized by the matrix) and is refused with LLF_ERR_UNSUPPORTED.
+ * Systems above LLF_NOALLOC_MAX_DOFS are rejected with LLF_ERR_LIMIT.  The
+ * first call on a device looks up the array's device address for that
+ * device, with that device made current for the lookup and the caller's
+ * current device restored afterwards (make that first call before any
+ * stream capture).  The address is kept for the life of the process: a
+ * cudaDeviceReset, or any other teardown of the device's primary context,
+ * invalidates it, so do not call this entry point after one.  All calls
+ * share the one array and it keeps the previous call's contents; each call
+ * clears on its own stream what has to start at zero (the count of
+ * unconverged systems and the three arrival counters of the chunk
+ * reductions: the product's u.c for alpha, the update's residual norm and
+ * z.r after a sweep preconditioner)
+ * and writes every other work vector before reading it.  Calls whose work
+ * overlaps on the GPU (two contexts or threads at once) race on the array:
+ * serialise them. */
 int llf_pcg_noalloc(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                     const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
                     int64_t *iters, double *relres);

@@ -59,6 +59,7 @@ SIGNATURES = {
     "llf_profile_reset": (i32, [vp]),
     "llf_profile_report": (i32, [vp, C.c_char_p, i64, P_i64]),
     "llf_launch_count": (i32, [vp, P_i64]),
+    "llf_alloc_count": (i32, [vp, P_i64]),
     "llf_mesh_upload": (i32, [vp, i32, i64, P_dbl, i64, i32, P_i64, i32, i32, PP]),
     "llf_mesh_update": (i32, [vp, vp, P_dbl, P_i64]),
     "llf_mesh_set_materials": (i32, [vp, vp, P_i32]),
@@ -200,6 +201,12 @@ class Context:
     def launches(self) -> int:
         n = C.c_int64(0)
         self.check(lib().llf_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def allocs(self) -> int:
+        """Device allocations the context has made so far."""
+        n = C.c_int64(0)
+        self.check(lib().llf_alloc_count(self.h, C.byref(n)))
         return n.value
 
     def close(self):

@@ -294,6 +294,12 @@ int llf_launch_count(llf_ctx *ctx, int64_t *launches) {
   return LLF_OK;
 }
 
+int llf_alloc_count(llf_ctx *ctx, int64_t *allocs) {
+  if (!ctx || !allocs) return LLF_ERR_ARG;
+  *allocs = ctx->allocs;
+  return LLF_OK;
+}
+
 int llf_builtin_rule(int family, int order, int *nip, int *npe, double *xi, double *w,
                      double *N, double *dN, double *node_ref) {
   llf::Rule r;
@@ -1066,6 +1072,10 @@ int llf_pcg_noalloc(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double
   if (!ctx) return LLF_ERR_ARG;
   if (!m || !d_b || !d_x || !d_fixed)
     return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_noalloc: null argument");
+  if (precond == LLF_PRECOND_IC0)
+    return llf_fail(ctx, LLF_ERR_UNSUPPORTED,
+                    "llf_pcg_noalloc: IC(0) is not supported on the allocation-free path (its factor and colouring "
+                    "need device memory sized by the matrix); use none, Jacobi or block Jacobi, or llf_pcg");
   if (precond < LLF_PRECOND_NONE || precond > LLF_PRECOND_BJACOBI)
     return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_noalloc: unknown preconditioner");
   int64_t it = 0;

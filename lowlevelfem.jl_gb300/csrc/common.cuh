@@ -48,6 +48,7 @@ struct llf_ctx {
   int num_sms = 0;
   bool profiling = false;
   long long launches = 0;
+  long long allocs = 0;           // device allocations made through the context
   std::vector<ProfPending> pending;
   std::vector<std::pair<std::string, ProfAcc>> prof;
 };
@@ -168,6 +169,7 @@ template <class T>
 cudaError_t dalloc(llf_ctx *ctx, T **p, size_t count) {
   *p = nullptr;
   if (count == 0) count = 1;
+  ctx->allocs++;
   return cudaMallocAsync((void **)p, count * sizeof(T), ctx->stream);
 }
 template <class T>

@@ -62,8 +62,10 @@ __global__ void k_scan_add(int64_t *__restrict__ out, int64_t n,
   }
 }
 
-cudaError_t scan_rec(cudaStream_t s, const int64_t *in, int64_t *out, int64_t n,
+cudaError_t scan_rec(llf_ctx *ctx, const int64_t *in, int64_t *out, int64_t n,
                      int64_t *d_total) {
+  cudaStream_t s = ctx->stream;
+  ctx->allocs += 2;
   int64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
   if (tiles < 1) tiles = 1;
   int64_t *totals = nullptr, *offs = nullptr;
@@ -73,7 +75,7 @@ cudaError_t scan_rec(cudaStream_t s, const int64_t *in, int64_t *out, int64_t n,
   if (e != cudaSuccess) return e;
   k_scan_tiles<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, out, n, totals);
   if (tiles > 1) {
-    e = scan_rec(s, totals, offs, tiles, d_total);
+    e = scan_rec(ctx, totals, offs, tiles, d_total);
     if (e != cudaSuccess) return e;
     k_scan_add<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(out, n, offs);
   } else {
@@ -91,7 +93,7 @@ cudaError_t scan_rec(cudaStream_t s, const int64_t *in, int64_t *out, int64_t n,
 cudaError_t exclusive_scan_i64_dev(llf_ctx *ctx, const int64_t *in, int64_t *out, int64_t n, int64_t *d_total) {
   cudaError_t e = cudaMemsetAsync(d_total, 0, sizeof(int64_t), ctx->stream);
   if (e != cudaSuccess) return e;
-  if (n > 0) return scan_rec(ctx->stream, in, out, n, d_total);
+  if (n > 0) return scan_rec(ctx, in, out, n, d_total);
   return cudaGetLastError();
 }
 
@@ -100,11 +102,12 @@ cudaError_t exclusive_scan_i64_dev(llf_ctx *ctx, const int64_t *in, int64_t *out
 cudaError_t exclusive_scan_i64(llf_ctx *ctx, const int64_t *in, int64_t *out,
                                int64_t n, int64_t *total_host) {
   int64_t *d_total = nullptr;
+  ctx->allocs++;
   cudaError_t e = cudaMallocAsync((void **)&d_total, sizeof(int64_t), ctx->stream);
   if (e != cudaSuccess) return e;
   cudaMemsetAsync(d_total, 0, sizeof(int64_t), ctx->stream);
   if (n > 0) {
-    e = scan_rec(ctx->stream, in, out, n, d_total);
+    e = scan_rec(ctx, in, out, n, d_total);
     if (e != cudaSuccess) return e;
   }
   if (total_host) {

@@ -1158,12 +1158,20 @@ int noalloc_scratch(llf_ctx *ctx, unsigned char **out) {
   if (ctx->device < 0 || ctx->device >= 128) return llf_fail(ctx, LLF_ERR_ARG, "device index");
   std::lock_guard<std::mutex> lock(g_na_mutex);
   if (!g_na_ptr[ctx->device]) {
+    // the lookup needs the context's device current; the caller's current
+    // device is put back afterwards, on the error path too
+    int prev = -1;
+    LLF_CUDA_TRY(ctx, cudaGetDevice(&prev));
     LLF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    cudaError_t e2 = cudaSetDevice(prev);
     if (e != cudaSuccess || !p)
       return llf_fail(ctx, LLF_ERR_CUDA, std::string("llf_pcg_noalloc: cudaGetSymbolAddress of the scratch array failed: ") +
                                              cudaGetErrorString(e));
+    if (e2 != cudaSuccess)
+      return llf_fail(ctx, LLF_ERR_CUDA, std::string("llf_pcg_noalloc: restoring the current device failed: ") +
+                                             cudaGetErrorString(e2));
     g_na_ptr[ctx->device] = (unsigned char *)p;
   }
   *out = g_na_ptr[ctx->device];

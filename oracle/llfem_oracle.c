@@ -1598,3 +1598,170 @@ int orc_tl_internal_force(int mode, int64_t non, const double *xyz, int64_t nel,
   free(X); free(fe);
   return rc;
 }
+
+/* ------------------------------------------------------------------------ */
+/* The reference's own element arithmetic for stiffnessMatrix, threaded:    */
+/* the CPU baseline of the benchmark (not a checker of the GPU bits).       */
+/*                                                                          */
+/* Per element and integration point q (src/linear.jl:190-330):             */
+/*   J from the element's coordinates, J = sum_a x_a (x) dN_a(xi_q)          */
+/*   (compute_element_geometry!, src/multifield.jl:1666-1743, standing in   */
+/*   for gmsh getJacobians); dh[:,a] = inv(J)^T dN_ref[a];                  */
+/*   B1 filled as fill_B_matrix! does (src/linear.jl:125-151): rows         */
+/*   xx, yy, zz, xy, yz, zx (2D: xx, yy, xy), DoF columns interleaved;      */
+/*   K1 += (((B1^T D) B1) b) detJ w, left to right, with D of               */
+/*   constitutive_matrix (src/linear.jl:154-188).                           */
+/* Global placement is the reference's transposed one (entry (nn2[l],       */
+/* nn2[k]) receives K1[k,l]) scattered straight into the structural CSC     */
+/* through one binary search per node pair, into one buffer per thread,     */
+/* the buffers summed at the end: the reference's threaded direct-CSC       */
+/* assembly (assemble_csc_worker! / reduce_csc_buffers!,                    */
+/* src/multifield.jl:2394-2499, :2345-2380).  Values agree with             */
+/* orc_assemble to rounding, not bit for bit.  Returns elapsed seconds.     */
+/* ------------------------------------------------------------------------ */
+static void orc_constitutive(int ptype, int dim, double E, double nu, double *D, int *rows) {
+  int r = dim == 3 ? 6 : 3;
+  *rows = r;
+  for (int i = 0; i < r * r; ++i) D[i] = 0.0;
+  if (dim == 3) {
+    double c = E / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) D[i * 6 + j] = c * (i == j ? 1.0 - nu : nu);
+    for (int i = 3; i < 6; ++i) D[i * 6 + i] = c * ((1.0 - 2.0 * nu) / 2.0);
+  } else if (ptype == PT_PLANE_STRESS) {
+    double c = E / (1.0 - nu * nu);
+    D[0] = c; D[1] = c * nu; D[3] = c * nu; D[4] = c; D[8] = c * ((1.0 - nu) / 2.0);
+  } else {
+    double c = E / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    D[0] = c * (1.0 - nu); D[1] = c * nu; D[3] = c * nu; D[4] = c * (1.0 - nu);
+    D[8] = c * ((1.0 - 2.0 * nu) / 2.0);
+  }
+}
+
+double orc_assemble_bdb_threaded(int ptype, int dim, const double *xyz, int64_t nel, int npe,
+                                 const int32_t *conn, int nip, const double *w, const double *dN,
+                                 double E, double nu, double thickness, orc_csc *pat, int nthreads,
+                                 int chunk) {
+  const int64_t nnz = pat->nnz;
+  const int pdim = dim;
+  const int nd = pdim * npe;
+  double D[36];
+  int rows = 0;
+  orc_constitutive(ptype, dim, E, nu, D, &rows);
+  const double b = (dim == 2 && ptype == PT_PLANE_STRESS) ? thickness : 1.0;
+  int T = nthreads > 0 ? nthreads : 1;
+#ifdef _OPENMP
+  double t0 = omp_get_wtime();
+#else
+  double t0 = 0;
+#endif
+  double **bufs = (double **)malloc(sizeof(double *) * T);
+#pragma omp parallel num_threads(T)
+  {
+#ifdef _OPENMP
+    int tid = omp_get_thread_num();
+#else
+    int tid = 0;
+#endif
+    double *nz = (double *)calloc(nnz + 1, sizeof(double));
+    bufs[tid] = nz;
+    double *X = (double *)malloc(sizeof(double) * npe * 3);
+    double *dh = (double *)malloc(sizeof(double) * 3 * npe);
+    double *B1 = (double *)malloc(sizeof(double) * rows * nd);
+    double *BtD = (double *)malloc(sizeof(double) * nd * rows);
+    double *K1 = (double *)malloc(sizeof(double) * nd * nd);
+    int64_t nchunks = (nel + chunk - 1) / chunk;
+    for (int64_t ch = tid; ch < nchunks; ch += T) {
+      int64_t e0 = ch * chunk, e1 = e0 + chunk < nel ? e0 + chunk : nel;
+      for (int64_t e = e0; e < e1; ++e) {
+        for (int a = 0; a < npe; ++a)
+          for (int i = 0; i < 3; ++i) X[3 * a + i] = xyz[3 * (int64_t)conn[e * npe + a] + i];
+        memset(K1, 0, sizeof(double) * nd * nd);
+        for (int q = 0; q < nip; ++q) {
+          const double *dq = dN + (size_t)q * npe * 3;
+          double J[3][3] = {{0}};
+          for (int i = 0; i < dim; ++i)
+            for (int j = 0; j < dim; ++j) {
+              double acc = 0.0;
+              for (int a = 0; a < npe; ++a) acc += X[3 * a + i] * dq[3 * a + j];
+              J[i][j] = acc;
+            }
+          double iJ[9], det;
+          if (dim == 3) {
+            det = orc_inv3(J, iJ);
+          } else {
+            det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+            iJ[0] = J[1][1] / det; iJ[1] = -J[0][1] / det; iJ[3] = -J[1][0] / det; iJ[4] = J[0][0] / det;
+          }
+          det = fabs(det);
+          /* dh[i][a] = sum_j inv(J)^T[i][j] dN[a][j] = sum_j iJ[j][i] dN[a][j] */
+          for (int a = 0; a < npe; ++a)
+            for (int i = 0; i < dim; ++i) {
+              double acc = 0.0;
+              for (int j = 0; j < dim; ++j) acc += iJ[j * 3 + i] * dq[3 * a + j];
+              dh[i * npe + a] = acc;
+            }
+          memset(B1, 0, sizeof(double) * rows * nd);
+          for (int l = 0; l < npe; ++l) {
+            const double h1 = dh[l], h2 = dh[npe + l];
+            if (dim == 3) {
+              const double h3 = dh[2 * npe + l];
+              const int cx = 3 * l, cy = 3 * l + 1, cz = 3 * l + 2;
+              B1[0 * nd + cx] = h1; B1[1 * nd + cy] = h2; B1[2 * nd + cz] = h3;
+              B1[3 * nd + cx] = h2; B1[3 * nd + cy] = h1;
+              B1[4 * nd + cy] = h3; B1[4 * nd + cz] = h2;
+              B1[5 * nd + cx] = h3; B1[5 * nd + cz] = h1;
+            } else {
+              const int cx = 2 * l, cy = 2 * l + 1;
+              B1[0 * nd + cx] = h1; B1[1 * nd + cy] = h2;
+              B1[2 * nd + cx] = h2; B1[2 * nd + cy] = h1;
+            }
+          }
+          /* (B1^T D): nd x rows */
+          for (int k = 0; k < nd; ++k)
+            for (int c = 0; c < rows; ++c) {
+              double acc = 0.0;
+              for (int r = 0; r < rows; ++r) acc += B1[r * nd + k] * D[r * rows + c];
+              BtD[k * rows + c] = acc;
+            }
+          /* ((B1^T D) B1) b detJ w, added to K1 */
+          const double wq = w[q];
+          for (int k = 0; k < nd; ++k)
+            for (int l = 0; l < nd; ++l) {
+              double acc = 0.0;
+              for (int r = 0; r < rows; ++r) acc += BtD[k * rows + r] * B1[r * nd + l];
+              K1[k * nd + l] += ((acc * b) * det) * wq;
+            }
+        }
+        /* transposed placement: column nn2[k], row nn2[l] <- K1[k][l] */
+        for (int bn = 0; bn < npe; ++bn) {
+          int64_t Bnode = conn[e * npe + bn];
+          int64_t col0 = Bnode * pdim;
+          for (int an = 0; an < npe; ++an) {
+            int64_t A = conn[e * npe + an];
+            int64_t p0 = find_pos(pat->rowval, pat->colptr[col0], pat->colptr[col0 + 1], A * pdim);
+            int64_t off = p0 - pat->colptr[col0];
+            for (int j = 0; j < pdim; ++j) {
+              int64_t base = pat->colptr[col0 + j] + off;
+              for (int i = 0; i < pdim; ++i) nz[base + i] += K1[((size_t)bn * pdim + j) * nd + an * pdim + i];
+            }
+          }
+        }
+      }
+    }
+    free(X); free(dh); free(B1); free(BtD); free(K1);
+  }
+#pragma omp parallel for num_threads(T) schedule(static)
+  for (int64_t k = 0; k < nnz; ++k) {
+    double s = 0.0;
+    for (int t = 0; t < T; ++t) s += bufs[t][k];
+    pat->nzval[k] = s;
+  }
+  for (int t = 0; t < T; ++t) free(bufs[t]);
+  free(bufs);
+#ifdef _OPENMP
+  return omp_get_wtime() - t0;
+#else
+  return 0.0;
+#endif
+}

@@ -53,6 +53,9 @@ def lib():
         L.orc_assemble_csc_threaded.restype = dbl
         L.orc_assemble_csc_threaded.argtypes = [i32, i32, i32, i32, Pd, i64, i32, Pi32, i32, Pd, Pd,
                                                 Pd, Pd, dbl, vp, i32, i32, Pd]
+        L.orc_assemble_bdb_threaded.restype = dbl
+        L.orc_assemble_bdb_threaded.argtypes = [i32, i32, Pd, i64, i32, Pi32, i32, Pd, Pd, dbl, dbl, dbl, vp,
+                                                i32, i32]
         L.orc_free.argtypes = [vp]
         L.orc_n.restype = i64
         L.orc_n.argtypes = [vp]
@@ -209,6 +212,21 @@ def assemble_threaded(kind, ptype, dim, pdim, xyz, conn, rule, params, pat: CSC,
                                            float(thickness), pat.h, T, chunk,
                                            _p(np.ascontiguousarray(rule["node_ref"], dtype=np.float64), C.c_double)
                                            if affine else None)
+
+
+def assemble_bdb_threaded(ptype, dim, xyz, conn, rule, E, nu, pat: CSC, thickness=1.0, nthreads=None,
+                          chunk=64):
+    """CPU baseline: the reference's per-point B^T D B element arithmetic
+    (src/linear.jl:190-330) with the threaded direct-CSC scatter of
+    src/multifield.jl:2394-2499, into `pat` (overwritten).  Returns seconds."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    conn0 = _conn0(conn)
+    w = np.ascontiguousarray(rule["w"], dtype=np.float64)
+    dN = np.ascontiguousarray(rule["dN"], dtype=np.float64)
+    T = nthreads or lib().orc_num_threads()
+    return lib().orc_assemble_bdb_threaded(ptype, dim, _p(xyz, C.c_double), conn0.shape[0], conn0.shape[1],
+                                           _p(conn0, C.c_int32), len(w), _p(w, C.c_double), _p(dN, C.c_double),
+                                           float(E), float(nu), float(thickness), pat.h, T, chunk)
 
 
 def element_matrix(kind, dim, pdim, X, rule, c1, c2=0.0):

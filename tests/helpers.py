@@ -31,3 +31,23 @@ def assert_csc_identical(got, ref, what=""):
     if not np.array_equal(gv, rv):
         d = np.abs(gv - rv).max() / max(np.abs(rv).max(), 1e-300)
         raise AssertionError(f"{what}: nzval not bit-identical (max rel diff {d:.3e})")
+
+
+def benchmark_msh_mesh(llf):
+    """The reference's elasticity_benchmark.msh (unit cube, 30^3 hex8, MSH node
+    numbering and element order), rebuilt bit for bit from the committed
+    fixture tests/golden/elasticity_benchmark_msh.npz, and made current."""
+    import os
+    import sys
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    if here not in sys.path:
+        sys.path.insert(0, here)
+    from make_msh_fixture import FACES, decode
+    xyz, conn, faces = decode()
+    groups = {}
+    for name in FACES:
+        c = faces[name]
+        groups[name] = llf.Group(name, 2, np.unique(c), llf.QUAD, 1, c)
+    groups["body"] = llf.Group("body", 3, np.arange(1, xyz.shape[0] + 1, dtype=np.int64), llf.HEX, 1, conn,
+                               np.arange(conn.shape[0]))
+    return llf.set_current(llf.Mesh(3, llf.HEX, 1, xyz, conn, groups, name="elasticity_benchmark.msh"))

@@ -256,23 +256,29 @@ def test_c1_quad4_full_size_properties(llf, orc):
     assert_csc_identical(K.csc(), ref.julia(), "C1 quad4 200x100")
 
 
-def test_c2_hex27_full_size_properties(llf):
+def test_c2_hex27_full_size_bit_identical(llf, orc):
+    """Config 2 at full size, the bench's headline workload: hex27 40^3
+    (531,441 nodes, 64,000 elements, 297,685,449 structural entries), K and
+    the consistent M against the oracle's serial restatement of the
+    reference's COO assembly + sparse + dropzeros!, bit for bit.  This is the
+    case with two degree-class gather launches, 64,000-element persistent
+    grids and row positions up to degree 125."""
     m = llf.structured_box_mesh(n=40, order=2)
-    mat = llf.Material("body", E=2.1e5, nu=0.3)
+    mat = llf.Material("body", E=2.1e5, nu=0.3, rho=7.85e-9)
     p = llf.Problem([mat], type="Solid")
     assert p.pattern().nnz == 297685449
     K = llf.stiffnessMatrix(p)
-    c, r, v = K.csc()
-    n = 3 * m.non
-    assert len(c) == n + 1 and c[-1] - 1 == len(v)
-    # rigid translations are in the kernel: K t = 0
-    for comp in range(3):
-        t = np.zeros(n); t[comp::3] = 1.0
-        assert np.abs(K * t).max() <= 1e-10 * np.abs(v).max()
-    # symmetry of the stored values through y = K x vs x' K
-    x = np.random.default_rng(2).standard_normal(n)
-    z = np.random.default_rng(3).standard_normal(n)
-    assert abs(z @ (K * x) - x @ (K * z)) <= 1e-12 * np.abs(K * x).sum()
+    got = K.csc()
+    K.dm = None
+    ref = oracle_operator(llf, orc, m, "stiffness", 0, mat)
+    assert_csc_identical(got, ref.julia(), "C2 K hex27 40^3")
+    del got, ref
+    M = llf.massMatrix(p, lumped=False)
+    got = M.csc()
+    M.dm = None
+    ref = oracle_operator(llf, orc, m, "mass", 0, mat)
+    assert_csc_identical(got, ref.julia(), "C2 consistent M hex27 40^3")
+    assert len(got[2]) == 99228483   # same-component couplings only (the survey's count)
 
 
 def test_connectivity_change_requires_new_pattern(llf, orc):
@@ -344,3 +350,50 @@ def test_larger_meshes_bit_identical(llf, orc, case):
     H = llf.heatConductionMatrix(ph)
     refh = oracle_operator(llf, orc, m, "heat", PT[ph.type], mat)
     assert_csc_identical(H.csc(), refh.julia(), f"conduction {kind} n{n} p{order}")
+
+
+# ------------------------------------------------------- caller-supplied tables
+def _permuted_rule(rule, scale=1.0):
+    """The built-in rule with its points in reverse order and its weights
+    scaled: what a caller passing gmsh's own getIntegrationPoints /
+    getBasisFunctions output (src/linear.jl:235-243) may hand over, in
+    another point order and normalisation."""
+    q = np.arange(rule["nip"])[::-1]
+    return {"nip": rule["nip"], "npe": rule["npe"], "w": rule["w"][q] * scale,
+            "N": np.ascontiguousarray(rule["N"][q]), "dN": np.ascontiguousarray(rule["dN"][q]),
+            "node_ref": None}
+
+
+@pytest.mark.parametrize("case", [("box", 2, 2, False, "Solid"), ("box", 2, 2, True, "Solid"),
+                                  ("rect", 3, 3, False, "PlaneStrain"), ("rect", 2, 2, True, "PlaneStress")],
+                         ids=["hex27", "tet10", "quad16", "tri6"])
+@pytest.mark.parametrize("scale", [1.0, 0.5])
+def test_tables_upload_bit_identical(llf, orc, case, scale):
+    """llf_tables_upload (the path the Julia shim takes with gmsh's tables):
+    K, M and the conduction matrix from caller-supplied tables equal the
+    oracle fed the same tables bit for bit, with the table layout
+    N[q*npe+a], dN[(q*npe+a)*3+j]; scale 1 agrees with the built-in rule to
+    rounding (only the point order differs)."""
+    kind, n, order, simplex, ptype = case
+    m = make_mesh(llf, kind, n, order, simplex)
+    mat = llf.Material("body", E=2.1e5, nu=0.3, rho=7.85e-9, k=45.0)
+    rule = _permuted_rule(llf._lib.builtin_rule(m.family, m.order), scale)
+    p = llf.Problem([mat], type=ptype, thickness=0.7)
+    p.device_mesh().set_tables(rule["w"], rule["N"], rule["dN"])
+    K = llf.stiffnessMatrix(p)
+    ref = orc.assemble(orc.ELASTIC, PT[ptype], m.dim, m.dim, m.xyz, m.conn, rule, [mat.E, mat.nu], 0.7,
+                       affine=False)
+    assert_csc_identical(K.csc(), ref.julia(), f"K from uploaded tables {kind} p{order}")
+    M = llf.massMatrix(p, lumped=False)
+    refm = orc.assemble(orc.MASS, PT[ptype], m.dim, m.dim, m.xyz, m.conn, rule, [mat.rho], 0.7, affine=False)
+    assert_csc_identical(M.csc(), refm.julia(), f"M from uploaded tables {kind} p{order}")
+    pt = "HeatConduction" if m.dim == 3 else "PlaneHeatConduction"
+    ph = llf.Problem([mat], type=pt, thickness=0.7)
+    ph.device_mesh().set_tables(rule["w"], rule["N"], rule["dN"])
+    H = llf.heatConductionMatrix(ph)
+    refh = orc.assemble(orc.HEAT, PT[pt], m.dim, 1, m.xyz, m.conn, rule, [mat.k], 0.7, affine=False)
+    assert_csc_identical(H.csc(), refh.julia(), f"conduction from uploaded tables {kind} p{order}")
+    if scale == 1.0:
+        Kb = oracle_operator(llf, orc, m, "stiffness", PT[ptype], mat, thickness=0.7).scipy()
+        d = abs(K.A - Kb).max() / abs(Kb).max()
+        assert d <= 1e-13, d

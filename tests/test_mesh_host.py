@@ -6,7 +6,8 @@ import pytest
 
 from conftest import REFERENCE
 
-MSH = os.path.join(REFERENCE, "examples/dev/compare_LLFEM_Ferrite_dealII_Gridap/elasticity_benchmark.msh")
+MSH = os.path.join(REFERENCE, "examples/dev/compare_LLFEM_Ferrite_dealII_Gridap/elasticity_benchmark.msh") \
+    if REFERENCE else ""
 
 
 def test_config_sizes(llf):
@@ -22,9 +23,11 @@ def test_d_is_min_dx_dy(llf):
     assert m.nel == 400 * 200
 
 
-@pytest.mark.skipif(not os.path.exists(MSH), reason="reference mesh fixture not available")
 def test_generator_matches_reference_msh(llf):
-    ref = llf.read_msh(MSH)
+    """The structured generator and the reference's elasticity_benchmark.msh
+    (rebuilt from tests/golden/) hold the same node set and group sizes."""
+    from helpers import benchmark_msh_mesh
+    ref = benchmark_msh_mesh(llf)
     gen = llf.structured_box_mesh(n=30)
     assert ref.nel == gen.nel == 27000 and ref.non == gen.non == 29791
     a = np.round(np.sort(ref.xyz.view([("", float)] * 3), axis=0).view(float).reshape(-1, 3), 12)
@@ -69,3 +72,12 @@ def test_problem_type_errors(llf):
         llf.Problem(llf.Material("body"), type="PlaneStress")
     with pytest.raises(ValueError):
         llf.Problem([llf.Material("body")], type="Solid")  # 3D problem on a 2D mesh
+
+
+@pytest.mark.skipif(not MSH or not os.path.exists(MSH), reason="set LLF_REFERENCE_DIR to a reference checkout")
+def test_msh_reader_matches_fixture(llf):
+    """read_msh on the reference's file gives the committed fixture bit for bit."""
+    from helpers import benchmark_msh_mesh
+    fx = benchmark_msh_mesh(llf)
+    m = llf.read_msh(MSH)
+    assert np.array_equal(m.xyz.view(np.int64), fx.xyz.view(np.int64)) and np.array_equal(m.conn, fx.conn)

@@ -35,9 +35,12 @@ def _noalloc(llf, K, b, x0, fixed, precond, reltol, maxiter):
     torch.cuda.synchronize()
     it, rr = C.c_int64(0), C.c_double(0.0)
     L = llf._lib.lib()
+    allocs0 = K.dm.ctx.allocs()
     rc = L.llf_pcg_noalloc(K.dm.ctx.h, K.dm.h, C.c_void_p(db.data_ptr()), C.c_void_p(dx.data_ptr()),
                            C.c_void_p(dfx.data_ptr()), precond, reltol, maxiter, C.byref(it), C.byref(rr))
     K.dm.ctx.check(rc, "llf_pcg_noalloc")
+    # the library's own allocation counter: the call made no device allocation
+    assert K.dm.ctx.allocs() == allocs0, "llf_pcg_noalloc allocated device memory"
     torch.cuda.synchronize()
     return dx.cpu().numpy(), it.value, rr.value
 
@@ -73,3 +76,11 @@ def test_noalloc_rejects_oversized_system(llf):
     assert len(f) > 131072
     with pytest.raises(llf.LLFError, match="at most 131072"):
         _noalloc(llf, K, f, np.zeros_like(f), fixed, 1, 1e-8, 10)
+
+
+def test_noalloc_refuses_ic0(llf):
+    """IC(0) needs a factor sized by the matrix, so this path refuses it with
+    a message that says so (not as an unknown preconditioner)."""
+    _, K, f, fixed = _system(llf, 2, order=1)
+    with pytest.raises(llf.LLFError, match="IC\\(0\\) is not supported"):
+        _noalloc(llf, K, f, np.zeros_like(f), fixed, 3, 1e-8, 10)
