@@ -415,17 +415,6 @@ int llf_matrix_spmv(llf_ctx *ctx, const llf_matrix *m, const double *x,
 
 int llf_matrix_destroy(llf_ctx *ctx, llf_matrix *m);
 
-/* Make the node-block structural values the solvers read (no reference
- * counterpart; an internal form).  An assembly (llf_assemble_stiffness,
- * _mass with lumped = 0, _heat, _form without accumulation) gathers straight
- * into the stored CSC and keeps one bit per structural entry saying whether
- * it was stored; the structural values are expanded from these on first use
- * by every entry point that needs them (an allocation of 8 bytes per
- * structural entry).  Call this to do that step at a time of your choosing,
- * e.g. before llf_pcg_noalloc, which never allocates and so refuses a
- * matrix whose structural values are not made yet. */
-int llf_matrix_prepare(llf_ctx *ctx, const llf_matrix *m);
-
 /* ======================================================================== */
 /* Solve                                                                    */
 /* ======================================================================== */
@@ -482,10 +471,6 @@ int llf_heat_fdm(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C,
  * work vectors live in one fixed array compiled into the library
  * (about 8.7 MB for LLF_NOALLOC_MAX_DOFS = 131072 unknowns), which every GPU
  * that loads the library holds until the process exits.
- *
- * The matrix's structural values must already exist (llf_matrix_prepare,
- * or any earlier llf_pcg / llf_matrix_spmv on it, makes them); otherwise the
- * call returns LLF_ERR_STATE instead of allocating them.
  *
  * Same algorithm and results as llf_pcg (IterativeSolvers.cg recurrence and
  * stopping rule, Dirichlet masking) with the preconditioners none, Jacobi

@@ -50,11 +50,11 @@ int llf_check_status(llf_ctx *ctx, const char *what) {
   std::string w(what);
   if (st & ST_BAD_NODE) return llf_fail(ctx, LLF_ERR_MESH, w + ": connectivity refers to a node tag outside 1..non");
   if (st & ST_BAD_JACOBIAN) return llf_fail(ctx, LLF_ERR_MESH, w + ": non-positive Jacobian determinant (inverted or degenerate element)");
-  if (st & ST_CAPACITY) return llf_fail(ctx, LLF_ERR_LIMIT, w + ": a node neighbourhood or an output exceeds its buffer");
+  if (st & ST_CAPACITY) return llf_fail(ctx, LLF_ERR_LIMIT, w + ": node neighbourhood exceeds the pattern buffer");
   if (st & ST_NONFINITE) return llf_fail(ctx, LLF_ERR_NUMERIC, w + ": NaN or Inf in an input array");
   if (st & ST_PATTERN) return llf_fail(ctx, LLF_ERR_STATE, w + ": pattern entry without a contributing element (mesh and pattern disagree)");
   if (st & ST_BREAKDOWN) return llf_fail(ctx, LLF_ERR_NUMERIC, w + ": breakdown");
-  if (st & ST_TIMEOUT) return llf_fail(ctx, LLF_ERR_CUDA, w + ": a bounded device wait timed out (tensor-core pipeline or gather look-back)");
+  if (st & ST_TIMEOUT) return llf_fail(ctx, LLF_ERR_CUDA, w + ": a bounded wait on the tensor cores timed out");
   return llf_fail(ctx, LLF_ERR_CUDA, w + ": unknown device status");
 }
 
@@ -639,10 +639,6 @@ int llf_assemble_form(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int form_k
   } else {
     return llf_fail(ctx, LLF_ERR_ARG, "llf_assemble_form: form_kind");
   }
-  if (accumulate && accumulate->pat == pat && !accumulate->diagonal_only) {
-    int rc0 = matrix_need_nz(ctx, accumulate);
-    if (rc0 != LLF_OK) return rc0;
-  }
   if (accumulate && (accumulate->pat != pat || accumulate->diagonal_only || !accumulate->d_nz))
     return llf_fail(ctx, LLF_ERR_STATE, "llf_assemble_form: csc_matrix must be a full matrix on the same pattern");
   llf_matrix *m;
@@ -941,8 +937,6 @@ int llf_matrix_copy_structural(llf_ctx *ctx, const llf_matrix *m, double *nzval)
   if (!ctx || !m || !nzval) return LLF_ERR_ARG;
   if (m->diagonal_only)
     return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "lumped matrix has no structural values");
-  int rc = matrix_need_nz(ctx, m);
-  if (rc != LLF_OK) return rc;
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(nzval, m->d_nz, sizeof(double) * m->pat->nnz,
                                     cudaMemcpyDeviceToHost, ctx->stream));
   LLF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -998,20 +992,11 @@ int llf_matrix_destroy(llf_ctx *ctx, llf_matrix *m) {
   if (!m) return LLF_OK;
   if (ctx) {
     dfree(ctx, m->d_nz); dfree(ctx, m->d_diag); dfree(ctx, m->d_colptr_s);
-    dfree(ctx, m->d_rowval_s); dfree(ctx, m->d_nzval_s); dfree(ctx, m->d_keep);
+    dfree(ctx, m->d_rowval_s); dfree(ctx, m->d_nzval_s);
     cudaStreamSynchronize(ctx->stream);
   }
   delete m;
   return LLF_OK;
-}
-
-int llf_matrix_prepare(llf_ctx *ctx, const llf_matrix *m) {
-  if (!ctx) return LLF_ERR_ARG;
-  if (!m) return llf_fail(ctx, LLF_ERR_ARG, "llf_matrix_prepare: null matrix");
-  if (m->diagonal_only) return llf_ok(ctx);
-  int rc = matrix_need_nz(ctx, m);
-  if (rc == LLF_OK) LLF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  return rc == LLF_OK ? llf_ok(ctx) : rc;
 }
 
 int llf_pcg(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x, const uint8_t *fixed,

@@ -385,103 +385,22 @@ __device__ __forceinline__ int nonzero_bits(double v) {
   return ((unsigned long long)__double_as_longlong(v) << 1) != 0ull;
 }
 
-// Accumulation of one column node B by one warp (shared by both gathers).
-// The accumulator (deg*P*P doubles) lives in shared memory, starting at
-// -0.0 (the identity of IEEE addition).  The elements of B are walked in
-// ascending order; lane a reads block (a, b) of the element's column
-// b = local(B) (one contiguous run of npe blocks, 16-byte padded) and the
-// block's row position from the pattern's element-to-column map, both
-// prefetched one element ahead, and adds the block into the accumulator.  A
-// byte per row position records whether the position has a value yet: the
-// first block that reaches a position is stored, later ones are added, and
-// positions that no element reaches are written as -0.0.  Every entry thus
-// equals the reference's combination of its triplets (first value, then
-// + each later one), signed zeros included, with one FP64 addition per
+// Column-node gather.  One warp per column node B: its accumulator
+// (deg*P*P doubles) lives in shared memory, starting at -0.0 (the identity
+// of IEEE addition).  The elements of B are walked in ascending order; lane
+// a reads block (a, b) of the element's column b = local(B) (one contiguous
+// run of npe blocks, 16-byte padded) and the block's row position from the
+// pattern's element-to-column map, both prefetched one element ahead, and
+// adds the block into the accumulator.  A byte per row position records
+// whether the position has a value yet: the first block that reaches a
+// position is stored, later ones are added, and positions that no element
+// reaches are written as -0.0 (the identity of IEEE addition).  Every entry
+// thus equals the reference's combination of its triplets (first value,
+// then + each later one), signed zeros included, with one FP64 addition per
 // contribution after the first only.  With init (values to accumulate into)
-// the accumulator starts from them and every block is added.
-template <int P, bool BLOCKVAL, class T>
-__device__ __forceinline__ void colgather_accumulate(double *acc, unsigned char *has, int lane, int64_t c0, int deg,
-                                                     int64_t s, int nb, const int2 *__restrict__ n2e,
-                                                     const uint16_t *__restrict__ pos, const T *__restrict__ Kf,
-                                                     int64_t cs, int npe, const double *__restrict__ init) {
-  constexpr int BS = BLOCKVAL ? P * P : 1;
-  constexpr int BSTR = kf_bstride(P, BLOCKVAL, (int)sizeof(T));  // stored block stride
-  constexpr bool VEC = sizeof(T) == 4 && BSTR % 4 == 0;           // 16-byte block loads
-  if (init) {  // accumulate into existing structural values (same layout as the output)
-    const double *src = init + (size_t)P * P * c0;
-    for (int idx = lane; idx < deg * P * P; idx += 32) {
-      const int j = idx / (P * deg), r = idx - j * P * deg;
-      acc[(size_t)(r / P) * P * P + j * P + r % P] = src[idx];
-    }
-  } else {
-    for (int t = lane; t < deg; t += 32) has[t] = 0;
-  }
-  const bool store_first = init == nullptr;
-  __syncwarp();
-  if (npe <= 32) {
-    const bool act = lane < npe;
-    T cur[BSTR], nxt[BSTR];
-    unsigned tc = 0xffffu, tn = 0xffffu;
-    auto load_block = [&](const T *v, T *dst) {
-      if constexpr (VEC) {
-#pragma unroll
-        for (int m = 0; m < BSTR; m += 4) {
-          const float4 f = __ldg(reinterpret_cast<const float4 *>(v + m));
-          dst[m] = f.x; dst[m + 1] = f.y; dst[m + 2] = f.z; dst[m + 3] = f.w;
-        }
-      } else {
-#pragma unroll
-        for (int m = 0; m < BS; ++m) dst[m] = v[m];
-      }
-    };
-    if (nb > 0 && act) {
-      const int2 el = n2e[s];
-      load_block(Kf + ((size_t)el.x * npe + el.y) * cs + (size_t)lane * BSTR, cur);
-      tc = pos[s * npe + lane];
-    }
-    for (int k = 0; k < nb; ++k) {  // elements of B, ascending
-      if (k + 1 < nb && act) {
-        const int2 el = n2e[s + k + 1];
-        load_block(Kf + ((size_t)el.x * npe + el.y) * cs + (size_t)lane * BSTR, nxt);
-        tn = pos[(s + k + 1) * npe + lane];
-      }
-      if (act && tc != 0xffffu) {  // the lanes of one element hold distinct positions
-        if (store_first && !has[tc]) {
-          add_block<P, BLOCKVAL, true>(acc, (int)tc, cur);
-          has[tc] = 1;
-        } else {
-          add_block<P, BLOCKVAL, false>(acc, (int)tc, cur);
-        }
-      }
-      __syncwarp();
-#pragma unroll
-      for (int m = 0; m < BSTR; ++m) cur[m] = nxt[m];
-      tc = tn;
-    }
-  } else {
-    for (int k = 0; k < nb; ++k) {
-      const int2 el = n2e[s + k];
-      const T *col = Kf + ((size_t)el.x * npe + el.y) * cs;
-      for (int a = lane; a < npe; a += 32) {
-        const unsigned t = pos[(s + k) * npe + a];
-        if (t != 0xffffu) {
-          if (store_first && !has[t]) {
-            add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BSTR);
-            has[t] = 1;
-          } else {
-            add_block<P, BLOCKVAL, false>(acc, (int)t, col + (size_t)a * BSTR);
-          }
-        }
-      }
-      __syncwarp();
-    }
-  }
-}
-
-// Column-node gather into the structural values.  One warp per column node
-// B (colgather_accumulate); the column is written out coalesced with its
-// non-zero count: column (B,j) holds the entries (row node t, component i)
-// at P*t + i.
+// the accumulator starts from them and every block is added.  The column is
+// written out coalesced with its non-zero count: column (B,j) holds the
+// entries (row node t, component i) at P*t + i.
 template <int P, bool BLOCKVAL, class T>
 __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__restrict__ n2e_ptr,
                             const int2 *__restrict__ n2e, const uint16_t *__restrict__ pos,
@@ -490,6 +409,9 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
                             int64_t *__restrict__ cnt, const int32_t *__restrict__ list) {
   extern __shared__ double cg_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  constexpr int BS = BLOCKVAL ? P * P : 1;
+  constexpr int BSTR = kf_bstride(P, BLOCKVAL, (int)sizeof(T));  // stored block stride
+  constexpr bool VEC = sizeof(T) == 4 && BSTR % 4 == 0;           // 16-byte block loads
   double *acc = cg_smem + (size_t)wib * max_deg * P * P;
   unsigned char *has = reinterpret_cast<unsigned char *>(cg_smem + (size_t)wpb * max_deg * P * P) +
                        (size_t)wib * ((max_deg + 7) & ~7);
@@ -500,8 +422,75 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
     const int deg = (int)(nptr[B + 1] - c0);
     const int64_t s = n2e_ptr[B];
     const int nb = (int)(n2e_ptr[B + 1] - s);
-    colgather_accumulate<P, BLOCKVAL, T>(acc, has, lane, c0, deg, s, nb, n2e, pos, Kf, cs, npe, init);
+    if (init) {  // accumulate into existing structural values (same layout as the output)
+      const double *src = init + (size_t)P * P * c0;
+      for (int idx = lane; idx < deg * P * P; idx += 32) {
+        const int j = idx / (P * deg), r = idx - j * P * deg;
+        acc[(size_t)(r / P) * P * P + j * P + r % P] = src[idx];
+      }
+    } else {
+      for (int t = lane; t < deg; t += 32) has[t] = 0;
+    }
     const bool store_first = init == nullptr;
+    __syncwarp();
+    if (npe <= 32) {
+      const bool act = lane < npe;
+      T cur[BSTR], nxt[BSTR];
+      unsigned tc = 0xffffu, tn = 0xffffu;
+      auto load_block = [&](const T *v, T *dst) {
+        if constexpr (VEC) {
+#pragma unroll
+          for (int m = 0; m < BSTR; m += 4) {
+            const float4 f = __ldg(reinterpret_cast<const float4 *>(v + m));
+            dst[m] = f.x; dst[m + 1] = f.y; dst[m + 2] = f.z; dst[m + 3] = f.w;
+          }
+        } else {
+#pragma unroll
+          for (int m = 0; m < BS; ++m) dst[m] = v[m];
+        }
+      };
+      if (nb > 0 && act) {
+        const int2 el = n2e[s];
+        load_block(Kf + ((size_t)el.x * npe + el.y) * cs + (size_t)lane * BSTR, cur);
+        tc = pos[s * npe + lane];
+      }
+      for (int k = 0; k < nb; ++k) {  // elements of B, ascending
+        if (k + 1 < nb && act) {
+          const int2 el = n2e[s + k + 1];
+          load_block(Kf + ((size_t)el.x * npe + el.y) * cs + (size_t)lane * BSTR, nxt);
+          tn = pos[(s + k + 1) * npe + lane];
+        }
+        if (act && tc != 0xffffu) {  // the lanes of one element hold distinct positions
+          if (store_first && !has[tc]) {
+            add_block<P, BLOCKVAL, true>(acc, (int)tc, cur);
+            has[tc] = 1;
+          } else {
+            add_block<P, BLOCKVAL, false>(acc, (int)tc, cur);
+          }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int m = 0; m < BSTR; ++m) cur[m] = nxt[m];
+        tc = tn;
+      }
+    } else {
+      for (int k = 0; k < nb; ++k) {
+        const int2 el = n2e[s + k];
+        const T *col = Kf + ((size_t)el.x * npe + el.y) * cs;
+        for (int a = lane; a < npe; a += 32) {
+          const unsigned t = pos[(s + k) * npe + a];
+          if (t != 0xffffu) {
+            if (store_first && !has[t]) {
+              add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BSTR);
+              has[t] = 1;
+            } else {
+              add_block<P, BLOCKVAL, false>(acc, (int)t, col + (size_t)a * BSTR);
+            }
+          }
+        }
+        __syncwarp();
+      }
+    }
 #pragma unroll
     for (int j = 0; j < P; ++j) {
       double *out = nz + (size_t)P * P * c0 + (size_t)j * P * deg;
@@ -517,159 +506,6 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
       if (lane == 0 && cnt) cnt[B * P + j] = n;
     }
     __syncwarp();
-  }
-}
-
-// ------------------------------------------------------ gather -> stored CSC
-// The column gather fused with dropzeros!: each warp sums its column node as
-// k_colgather does and writes the node's P stored columns (1-based rowval,
-// nzval, 1-based colptr) straight from shared memory, together with one bit
-// per structural entry that says whether the entry was stored.  The stored
-// offset of node B is the number of stored entries of nodes 0..B-1, found by
-// a decoupled look-back over a per-node state word: a warp publishes its own
-// count as soon as its sums are done, then walks back over its predecessors,
-// 32 at a time, until it meets one whose inclusive prefix is published, and
-// publishes its own.  Nodes are taken in ascending order from a ticket
-// counter, so every node a warp waits for belongs to a warp that is already
-// running and waits only for smaller nodes: the waits always end.  Each wait
-// is bounded all the same; a warp that gives up sets ST_TIMEOUT and writes
-// nothing.
-constexpr unsigned long long LB_AGG = 1ull << 62, LB_INC = 2ull << 62, LB_VAL = (1ull << 62) - 1;
-constexpr int LB_SPIN_MAX = 1 << 20;
-
-__device__ __forceinline__ void lb_store(unsigned long long *p, unsigned long long v) {
-  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ unsigned long long lb_load(const unsigned long long *p) {
-  unsigned long long v;
-  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-
-template <int P, bool BLOCKVAL, class T>
-__global__ void k_colgather_csc(const int64_t *__restrict__ nptr, const int64_t *__restrict__ n2e_ptr,
-                                const int2 *__restrict__ n2e, const uint16_t *__restrict__ pos,
-                                const T *__restrict__ Kf, int64_t cs, int npe, int64_t non, int max_deg,
-                                const int32_t *__restrict__ nadj, unsigned long long *lb, unsigned *ticket,
-                                int64_t cap, int64_t *__restrict__ colptr_s, int64_t *__restrict__ rowval_s,
-                                double *__restrict__ nzval_s, unsigned *__restrict__ keep, unsigned *status) {
-  extern __shared__ double cg_smem[];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-  double *acc = cg_smem + (size_t)wib * max_deg * P * P;
-  unsigned char *has = reinterpret_cast<unsigned char *>(cg_smem + (size_t)wpb * max_deg * P * P) +
-                       (size_t)wib * ((max_deg + 7) & ~7);
-  const unsigned lt = (1u << lane) - 1u;
-  for (;;) {
-    unsigned tk = 0;
-    if (lane == 0) tk = atomicAdd(ticket, 1u);
-    const int64_t B = (int64_t)__shfl_sync(0xffffffffu, tk, 0);
-    if (B >= non) break;
-    const int64_t c0 = nptr[B];
-    const int deg = (int)(nptr[B + 1] - c0);
-    const int64_t s = n2e_ptr[B];
-    const int nb = (int)(n2e_ptr[B + 1] - s);
-    colgather_accumulate<P, BLOCKVAL, T>(acc, has, lane, c0, deg, s, nb, n2e, pos, Kf, cs, npe, nullptr);
-    __syncwarp();
-    // stored entries of the node
-    int total = 0;
-    for (int idx = lane; idx < P * P * deg; idx += 32) {
-      const int j = idx / (P * deg), r = idx - j * P * deg, t = r / P, i = r - t * P;
-      total += has[t] ? nonzero_bits(acc[(size_t)t * P * P + j * P + i]) : 0;
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) total += __shfl_xor_sync(0xffffffffu, total, off);
-    if (lane == 0) lb_store(lb + B, LB_AGG | (unsigned long long)total);
-    // decoupled look-back for the stored entries of nodes 0..B-1
-    long long excl = 0;
-    bool ok = true;
-    int64_t look = B - 1;
-    int spins = 0;
-    while (look >= 0) {
-      const int64_t q = look - lane;
-      const unsigned long long st = q >= 0 ? lb_load(lb + q) : LB_INC;
-      const unsigned flag = (unsigned)(st >> 62);
-      const unsigned inc = __ballot_sync(0xffffffffu, flag == 2u);
-      const unsigned empty = __ballot_sync(0xffffffffu, flag == 0u);
-      const int p = inc ? __ffs(inc) - 1 : 31;             // nearest inclusive predecessor (or the window's end)
-      const unsigned upto = p >= 31 ? 0xffffffffu : ((2u << p) - 1u);
-      if (empty & upto) {                                    // a predecessor has not published yet
-        if (++spins > LB_SPIN_MAX) {
-          ok = false;
-          break;
-        }
-        __nanosleep(100);
-        continue;
-      }
-      long long v = lane <= p ? (long long)(st & LB_VAL) : 0;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-      excl += v;
-      if (inc) break;
-      look -= 32;
-    }
-    if (!ok) {
-      if (lane == 0) atomicOr(status, ST_TIMEOUT);
-      continue;
-    }
-    if (lane == 0) lb_store(lb + B, LB_INC | (unsigned long long)(excl + total));
-    if (excl + total > cap) {
-      if (lane == 0) atomicOr(status, ST_CAPACITY);
-      continue;
-    }
-    // the node's stored columns, straight from the accumulator
-    int64_t o = excl;
-    const int64_t sbase = (int64_t)P * P * c0;
-#pragma unroll
-    for (int j = 0; j < P; ++j) {
-      if (lane == 0) colptr_s[B * P + j] = o + 1;
-      const int64_t s0 = sbase + (int64_t)j * P * deg;
-      for (int l0 = 0; l0 < P * deg; l0 += 32) {
-        const int idx = l0 + lane;
-        const int t = idx / P, i = idx - t * P;
-        double v = 0.0;
-        bool kp = false;
-        if (idx < P * deg && has[t]) {
-          v = acc[(size_t)t * P * P + j * P + i];
-          kp = nonzero_bits(v);
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, kp);
-        if (kp) {
-          const int64_t d = o + __popc(bal & lt);
-          rowval_s[d] = (int64_t)P * nadj[c0 + t] + i + 1;
-          nzval_s[d] = v;
-        }
-        o += __popc(bal);
-        if (lane == 0 && bal) {
-          const int64_t sidx = s0 + l0;
-          const int sh = (int)(sidx & 31);
-          atomicOr(keep + (sidx >> 5), bal << sh);
-          if (sh) atomicOr(keep + (sidx >> 5) + 1, bal >> (32 - sh));
-        }
-      }
-    }
-    if (B == non - 1 && lane == 0) colptr_s[non * P] = o + 1;
-    __syncwarp();
-  }
-}
-
-// Structural values from the stored CSC and its keep bits: one warp per DoF
-// column, dropped entries as +0.0.
-__global__ void k_expand_stored(const int64_t *__restrict__ colptr, const int64_t *__restrict__ colptr_s,
-                                const double *__restrict__ nzval_s, const unsigned *__restrict__ keep,
-                                int64_t ndof, double *__restrict__ nz) {
-  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int64_t c = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5); c < ndof; c += (int64_t)gridDim.x * wpb) {
-    const int64_t s = colptr[c], e = colptr[c + 1];
-    int64_t o = colptr_s[c] - 1;
-    for (int64_t k0 = s; k0 < e; k0 += 32) {
-      const int64_t k = k0 + lane;
-      bool kp = false;
-      if (k < e) kp = (keep[k >> 5] >> (k & 31)) & 1u;
-      const unsigned bal = __ballot_sync(0xffffffffu, kp);
-      if (k < e) nz[k] = kp ? nzval_s[o + __popc(bal & lt)] : 0.0;
-      o += __popc(bal);
-    }
   }
 }
 
@@ -928,98 +764,6 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const 
   return launch(md, nullptr, B0, nB);
 }
 
-// Fused gather + dropzeros! into m's stored CSC (k_colgather_csc): the
-// stored arrays are allocated at the structural size (an upper bound), the
-// look-back state and the ticket counter cleared, one launch over all
-// column nodes in ascending order, then the stored count read back.
-template <int P, bool BV, class T>
-int run_colgather_csc(llf_ctx *ctx, llf_pattern *pat, const T *Kf, int64_t cs, llf_matrix *m) {
-  if (pat->conn_version != pat->mesh->conn_version)
-    return llf_fail(ctx, LLF_ERR_STATE, "the mesh connectivity changed after the pattern was built; rebuild it");
-  const int64_t non = pat->mesh->non, ndof = pat->ndof, nnz = pat->nnz;
-  cudaStream_t s = ctx->stream;
-  const int64_t nwords = nnz / 32 + 2;
-  unsigned long long *lb = nullptr;
-  unsigned *ticket = nullptr;
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_colptr_s, ndof + 1));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_rowval_s, nnz));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nzval_s, nnz));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_keep, nwords));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &lb, non + 1));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &ticket, 1));
-  LLF_CUDA_TRY(ctx, cudaMemsetAsync(m->d_keep, 0, sizeof(unsigned) * nwords, s));
-  LLF_CUDA_TRY(ctx, cudaMemsetAsync(lb, 0, sizeof(unsigned long long) * (non + 1), s));
-  LLF_CUDA_TRY(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), s));
-  if (non == 0) {
-    const int64_t one = 1;
-    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_colptr_s, &one, sizeof(int64_t), cudaMemcpyHostToDevice, s));
-  } else {
-    auto fn = k_colgather_csc<P, BV, T>;
-    const int md = pat->max_deg > 0 ? pat->max_deg : 1;
-    const size_t per_warp = (size_t)md * P * P * sizeof(double) + (size_t)((md + 7) & ~7);
-    int wpb = (int)std::min<size_t>(4, (200 * 1024) / per_warp);
-    if (wpb < 1) wpb = 1;
-    const size_t smem = (size_t)wpb * per_warp;
-    if (smem > 200 * 1024)
-      return llf_fail(ctx, LLF_ERR_LIMIT, "a column node has too many neighbours for the gather buffer");
-    if (smem > 48 * 1024)
-      LLF_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 1;
-    LLF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, wpb * 32, smem));
-    // every CTA resident at once (the look-back waits only for running warps,
-    // but a resident grid also keeps the ticket order close to the node order)
-    int64_t grid = (int64_t)ctx->num_sms * (per_sm < 1 ? 1 : per_sm);
-    const int64_t need = (non + wpb - 1) / wpb;
-    if (grid > need) grid = need;
-    KernelScope ks(ctx, "k_colgather_csc");
-    fn<<<(unsigned)grid, wpb * 32, smem, s>>>(pat->d_nptr, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, Kf, cs,
-                                              pat->mesh->npe, non, md, pat->d_nadj, lb, ticket, nnz,
-                                              m->d_colptr_s, m->d_rowval_s, m->d_nzval_s, m->d_keep, ctx->d_status);
-    LLF_CUDA_TRY(ctx, cudaGetLastError());
-  }
-  int64_t last = 0;
-  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&last, m->d_colptr_s + ndof, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-  dfree(ctx, lb);
-  dfree(ctx, ticket);
-  LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
-  int rc = llf_check_status(ctx, "gather");
-  if (rc != LLF_OK) return rc;
-  if (last < 1 || last - 1 > nnz) return llf_fail(ctx, LLF_ERR_CUDA, "gather: stored entry count out of range");
-  m->nnz_s = last - 1;
-  return LLF_OK;
-}
-
-// The assembly's gather for a matrix that keeps the reference's stored CSC
-// only (stiffness, consistent mass, conduction): the element kernels, then
-// the fused gather; the structural values are made later if a solver needs
-// them (matrix_need_nz).
-struct CscSink : GatherSink {
-  llf_matrix *m = nullptr;
-  explicit CscSink(llf_matrix *mm) : m(mm) {}
-  template <class T>
-  int run(llf_ctx *ctx, llf_pattern *pat, const T *Kf, int64_t cs, bool blockval, const ElemLauncher &elems) {
-    int rc = elems(0, pat->mesh->nel);
-    if (rc != LLF_OK) return rc;
-    switch (pat->pdim * 2 + (blockval ? 1 : 0)) {
-      case 2: return run_colgather_csc<1, false, T>(ctx, pat, Kf, cs, m);
-      case 3: return run_colgather_csc<1, true, T>(ctx, pat, Kf, cs, m);
-      case 4: return run_colgather_csc<2, false, T>(ctx, pat, Kf, cs, m);
-      case 5: return run_colgather_csc<2, true, T>(ctx, pat, Kf, cs, m);
-      case 6: return run_colgather_csc<3, false, T>(ctx, pat, Kf, cs, m);
-      case 7: return run_colgather_csc<3, true, T>(ctx, pat, Kf, cs, m);
-    }
-    return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
-  }
-  int gather(llf_ctx *ctx, llf_pattern *pat, const double *Kf, int64_t cs, bool blockval,
-             const ElemLauncher &elems) override {
-    return run<double>(ctx, pat, Kf, cs, blockval, elems);
-  }
-  int gather(llf_ctx *ctx, llf_pattern *pat, const float *Kf, int64_t cs, bool blockval,
-             const ElemLauncher &elems) override {
-    return run<float>(ctx, pat, Kf, cs, blockval, elems);
-  }
-};
-
 }  // namespace
 
 // ------------------------------------------------------------------ host
@@ -1117,29 +861,10 @@ int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts) {
   return LLF_OK;
 }
 
-int matrix_need_nz(llf_ctx *ctx, const llf_matrix *cm) {
-  llf_matrix *m = const_cast<llf_matrix *>(cm);
-  if (m->d_nz || m->diagonal_only) return LLF_OK;
-  if (!m->d_keep || !m->d_colptr_s)
-    return llf_fail(ctx, LLF_ERR_STATE, "matrix has neither structural values nor a stored form");
-  const llf_pattern *pat = m->pat;
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nz, pat->nnz));
-  KernelScope ks(ctx, "k_expand_stored");
-  k_expand_stored<<<grid_1d(pat->ndof * 32, 256, ctx->num_sms), 256, 0, ctx->stream>>>(
-      pat->d_colptr, m->d_colptr_s, m->d_nzval_s, m->d_keep, pat->ndof, m->d_nz);
-  LLF_CUDA_TRY(ctx, cudaGetLastError());
-  return LLF_OK;
-}
-
 int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int ptype,
                   const double *c1, const double *c2, int nmat, int form, int lumped,
                   llf_matrix *m, const double *init, GatherSink *sink) {
   (void)ptype;
-  // a plain assembly (no accumulation, dropzeros!, not lumped) gathers
-  // straight into the stored CSC
-  CscSink csc(m);
-  const bool fused = !sink && !init && !m->keep_pattern && !(kind == KIND_MASS && lumped);
-  if (fused) sink = &csc;
   const int dim = mesh->dim;
   const int npe = mesh->npe;
   const int P = pat->pdim;
@@ -1275,12 +1000,6 @@ int matrix_axpby_impl(llf_ctx *ctx, double a, const llf_matrix *A, double b,
                       const llf_matrix *B, llf_matrix *C) {
   if (A->pat != B->pat)
     return llf_fail(ctx, LLF_ERR_STATE, "axpby: matrices live on different patterns");
-  for (const llf_matrix *X : {A, B}) {
-    if (!X->diagonal_only) {
-      int rc = matrix_need_nz(ctx, X);
-      if (rc != LLF_OK) return rc;
-    }
-  }
   C->pat = A->pat;
   if (A->diagonal_only && B->diagonal_only) {  // both lumped: a lumped result
     const int64_t n = A->pat->ndof;

@@ -138,9 +138,7 @@ struct llf_pattern {
 
 struct llf_matrix {
   llf_pattern *pat = nullptr;
-  double *d_nz = nullptr;         // structural values (pattern->nnz); made from the
-                                  // stored form on first use when d_keep is set
-  unsigned *d_keep = nullptr;     // one bit per structural entry: stored (not dropped)
+  double *d_nz = nullptr;         // structural values (pattern->nnz)
   bool diagonal_only = false;     // lumped mass: values live on the diagonal
   bool keep_pattern = false;      // stored form keeps every structural entry (no dropzeros!)
   double *d_diag = nullptr;       // ndof (diagonal_only)
@@ -227,10 +225,6 @@ int assemble_to_host_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int ki
 // dropzeros -> stored form; counts (non-zeros per DoF column) may come from
 // the gather, else they are counted here
 int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts);
-// The structural values the solvers and matrix algebra read.  An assembly
-// through the fused gather keeps only the stored CSC and its keep bits; the
-// structural values are made from them here on first use (an allocation).
-int matrix_need_nz(llf_ctx *ctx, const llf_matrix *m);
 // assemble_fp32.cu: precision form (FP32 quadrature, FP64 accumulation) into nz
 // aflag/ageo: per-element affine flag and invJ/det (null: quadrature form only)
 int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,

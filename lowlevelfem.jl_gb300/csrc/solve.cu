@@ -1232,10 +1232,6 @@ int pcg_noalloc_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doubl
                                             " unknowns; the fixed scratch array holds at most " +
                                             std::to_string((long long)LLF_NOALLOC_MAX_DOFS) +
                                             " (use llf_pcg for larger systems)");
-  if (!m->d_nz)
-    return llf_fail(ctx, LLF_ERR_STATE,
-                    "llf_pcg_noalloc: the matrix's solver values are not made yet (an assembly keeps only its stored "
-                    "CSC); call llf_matrix_prepare once beforehand, outside the allocation-free section");
   switch (m->pat->pdim) {
     case 1: return pcg_noalloc_typed<1>(ctx, m, d_b, d_x, d_fixed, precond, reltol, maxiter, iters, relres);
     case 2: return pcg_noalloc_typed<2>(ctx, m, d_b, d_x, d_fixed, precond, reltol, maxiter, iters, relres);
@@ -1246,10 +1242,6 @@ int pcg_noalloc_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doubl
 
 int spmv_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_x, double *d_y) {
   const int64_t n = m->pat->ndof;
-  if (!m->diagonal_only) {
-    int rc = matrix_need_nz(ctx, m);
-    if (rc != LLF_OK) return rc;
-  }
   const unsigned grid = (unsigned)(ctx->num_sms * 4);
   if (m->diagonal_only) {
     KernelScope ks(ctx, "k_diag_scale");
@@ -1273,8 +1265,6 @@ int pcg_batched_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doubl
                      double reltol, int64_t maxiter, int64_t *iters, double *relres) {
   if (m->diagonal_only)
     return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pcg on a lumped (diagonal) matrix");
-  int rc = matrix_need_nz(ctx, m);
-  if (rc != LLF_OK) return rc;
   switch (m->pat->pdim) {
     case 1: return pcg_segments<1>(ctx, m, d_b, d_x, d_fixed, nseg, seg_off, precond, reltol, maxiter, iters, relres);
     case 2: return pcg_segments<2>(ctx, m, d_b, d_x, d_fixed, nseg, seg_off, precond, reltol, maxiter, iters, relres);
@@ -1346,7 +1336,7 @@ __global__ void k_fdm_check_diag(const double *__restrict__ d, const uint8_t *__
 
 void free_matrix_arrays(llf_ctx *ctx, llf_matrix *m) {
   dfree(ctx, m->d_nz); dfree(ctx, m->d_diag); dfree(ctx, m->d_colptr_s);
-  dfree(ctx, m->d_rowval_s); dfree(ctx, m->d_nzval_s); dfree(ctx, m->d_keep);
+  dfree(ctx, m->d_rowval_s); dfree(ctx, m->d_nzval_s);
 }
 
 template <int P>
@@ -1430,12 +1420,6 @@ int fdm_typed(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C, const doub
 int heat_fdm_impl(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C, const double *d_q, int nq, double *d_T,
                   const uint8_t *d_fixed, int64_t nsteps, double dt, double theta, int precond, double reltol,
                   int64_t maxiter, int64_t *iters_total) {
-  for (const llf_matrix *X : {K, C}) {
-    if (X && !X->diagonal_only) {
-      int rc = matrix_need_nz(ctx, X);
-      if (rc != LLF_OK) return rc;
-    }
-  }
   switch (K->pat->pdim) {
     case 1: return fdm_typed<1>(ctx, K, C, d_q, nq, d_T, d_fixed, nsteps, dt, theta, precond, reltol, maxiter, iters_total);
     case 2: return fdm_typed<2>(ctx, K, C, d_q, nq, d_T, d_fixed, nsteps, dt, theta, precond, reltol, maxiter, iters_total);

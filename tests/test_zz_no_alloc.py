@@ -84,17 +84,3 @@ def test_noalloc_refuses_ic0(llf):
     _, K, f, fixed = _system(llf, 2, order=1)
     with pytest.raises(llf.LLFError, match="IC\\(0\\) is not supported"):
         _noalloc(llf, K, f, np.zeros_like(f), fixed, 3, 1e-8, 10)
-
-
-def test_noalloc_needs_prepared_matrix(llf):
-    """A fresh assembly keeps only its stored CSC; the allocation-free call
-    refuses to make the solver's values itself (that would allocate) until
-    llf_matrix_prepare has made them, after which it runs without
-    allocating and agrees with llf_pcg."""
-    _, K, f, fixed = _system(llf, 3, order=2)
-    with pytest.raises(llf.LLFError, match="llf_matrix_prepare"):
-        _noalloc(llf, K, f, np.zeros_like(f), fixed, 1, 1e-10, 20 * len(f))
-    K.dm.prepare()
-    got, _, _ = _noalloc(llf, K, f, np.zeros_like(f), fixed, 1, 1e-10, 20 * len(f))
-    ref, _, _ = K.dm.pcg(f, np.zeros_like(f), fixed, precond=1, reltol=1e-10, maxiter=20 * len(f))
-    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-14 * np.abs(ref).max())
