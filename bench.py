@@ -56,7 +56,12 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="assembly", choices=["assembly", "batched", "serving", "tl"])
-    ap.add_argument("--instances", type=int, default=64, help="batched: instances (a seeded sample of 512)")
+    ap.add_argument("--instances", type=int, default=512, help="batched: instances (the first k of the seeded 512)")
+    ap.add_argument("--batched-form", default="fp32q", choices=["fp64", "fp32q"], help="batched: assembly form")
+    ap.add_argument("--batched-solve", default="mixed", choices=["fp64", "mixed"], help="batched: CG precision")
+    ap.add_argument("--batched-reltol", type=float, default=1e-10, help="batched: CG relative residual")
+    ap.add_argument("--group-nnz", type=float, default=1.5e9,
+                    help="batched: structural entries admitted to the GPU at a time")
     ap.add_argument("--requests", type=int, default=200, help="serving: requests of the Poisson stream")
     ap.add_argument("--workers", type=int, default=8,
                     help="serving: server workers (200 requests: 4 -> 40.6, 8 -> 43.0, 16 -> 34.0 solves/s)")
@@ -266,60 +271,118 @@ def _pct(v, q):
     return v[min(len(v) - 1, int(math.ceil(q / 100.0 * len(v))) - 1)] if v else None
 
 
+NNZ_PER_DOF_TET10 = 83   # structural entries per DoF of the tet10 boxes (the 16-instance sample: 82.8)
+
+
+def batched_groups(inst, budget_nnz):
+    """Instances in order, grouped so that each group's structural entries
+    (estimated from its DoFs) stay within budget_nnz: the batch is admitted
+    to HBM a group at a time (about 60 device bytes per entry: values, the
+    stored CSC, the FP32 copy, the IC(0) factor)."""
+    groups, cur, acc = [], [], 0
+    for k, (m, _, _) in enumerate(inst):
+        est = NNZ_PER_DOF_TET10 * 3 * m.non
+        if cur and acc + est > budget_nnz:
+            groups.append(cur)
+            cur, acc = [], 0
+        cur.append(k)
+        acc += est
+    if cur:
+        groups.append(cur)
+    return groups
+
+
 def run_batched(args, llf):
-    """Batched configuration: independent tet10 boxes assembled in one launch
-    and solved by one segmented PCG (IC(0) by default; CUDA graph).  Solves/s
-    and the relative displacement error of sample instances against a direct
-    solve."""
+    """Batched configuration: independent tet10 boxes (element counts
+    log-uniform 1e3-2e5, seeded), admitted to the GPU in groups by their
+    footprint; per group one assembly launch (FP32 quadrature, FP64
+    accumulation by default) and one segmented mixed-precision PCG (FP32
+    iterations, FP64 reliable updates, IC(0); CUDA graph) to an FP64
+    relative residual.  Solves/s over all instances, the relative
+    displacement error of sample instances against a direct solve of the
+    FP64-assembled matrix, and the plain GPU form (each instance alone, FP64
+    assembly + FP64 Jacobi-PCG) on the same instances."""
     import numpy as np
     import torch
     from llfem_gb300 import workloads as wl
     rng = np.random.default_rng(wl.SEED)
     inst = [wl.batched_instance(rng) for _ in range(args.instances)]
-    batch, noff = llf.concat_meshes([m for m, _, _ in inst])
-    mats = [llf.Material(f"body#{i}", E=E, nu=nu) for i, (_, E, nu) in enumerate(inst)]
-    P = llf.Problem(mats, type="Solid", mesh=batch)
-    loads = [llf.load(f"right#{i}", fx=1.0) for i in range(len(inst))]
-    sup = [llf.displacementConstraint(f"left#{i}", ux=0, uy=0, uz=0) for i in range(len(inst))]
-    f = llf.loadVector(P, loads)
-    P.pattern()
     prec = args.precond or "ic0"
+    form = args.batched_form
+    mixed = args.batched_solve == "mixed"
+    reltol = args.batched_reltol
+    groups = batched_groups(inst, args.group_nnz)
+    built = []
+    for g in groups:
+        batch, noff = llf.concat_meshes([inst[k][0] for k in g])
+        mats = [llf.Material(f"body#{i}", E=inst[k][1], nu=inst[k][2]) for i, k in enumerate(g)]
+        P = llf.Problem(mats, type="Solid", mesh=batch)
+        f = llf.loadVector(P, [llf.load(f"right#{i}", fx=1.0) for i in range(len(g))])
+        sup = [llf.displacementConstraint(f"left#{i}", ux=0, uy=0, uz=0) for i in range(len(g))]
+        P.pattern()
+        built.append((g, P, f, sup, noff))
+
+    def one_pass(keep=False):
+        out = []
+        for g, P, f, sup, noff in built:
+            K = llf.stiffnessMatrix(P, precision=form)
+            u = llf.solveFieldBatched(K, f, support=sup, node_offsets=noff, preconditioner=prec, reltol=reltol,
+                                      precision="mixed" if mixed else "fp64")
+            out.append((u, K if keep else None))
+            del K
+        return out
+
     times = []
+    res = None
     for rep in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        K = llf.stiffnessMatrix(P)
-        u = llf.solveFieldBatched(K, f, support=sup, node_offsets=noff, preconditioner=prec, reltol=1e-12)
+        res = one_pass()
         torch.cuda.synchronize()
         if rep >= args.warmup:
             times.append(time.perf_counter() - t0)
     t = statistics.median(times)
-    # accuracy against a direct solve of the two smallest instances
+    its = np.concatenate([u.iterations for u, _ in res])
+    # accuracy: the smallest instance of every group and the largest overall,
+    # against a direct solve of the instance's FP64-assembled matrix (the
+    # plain form's matrix, bit-identical to the oracle's)
     import scipy.sparse.linalg as spla
     errs = []
-    A = K.A
-    fixed = np.zeros(A.shape[0], bool)
-    fixed[llf.constrainedDoFs(P, sup) - 1] = True
-    for i in np.argsort(np.diff(noff))[:2]:
+    sizes = [inst[k][0].non for k in range(len(inst))]
+    check = sorted({min(g, key=lambda k: sizes[k]) for g in groups} | {int(np.argmax(sizes))})[:6]
+    for k in check:
+        gi = next(ix for ix, (g, *_rest) in enumerate(built) if k in g)
+        g, P, f, sup, noff = built[gi]
+        i = g.index(k)
         a, b = 3 * noff[i], 3 * noff[i + 1]
-        fr = ~fixed[a:b]
-        Ai = A[a:b, a:b].tocsc()[fr][:, fr]
-        ud = spla.spsolve(Ai.tocsc(), f.a[a:b, 0][fr])
-        errs.append(float(np.linalg.norm(u.a[a:b, 0][fr] - ud) / np.linalg.norm(ud)))
+        m, E, nu = inst[k]
+        llf.set_current(m)
+        Pi = llf.Problem([llf.Material("body", E=E, nu=nu)], type="Solid", mesh=m)
+        Ki = llf.stiffnessMatrix(Pi).A
+        fi = f.a[a:b, 0]
+        fixed = np.zeros(b - a, bool)
+        fixed[llf.constrainedDoFs(Pi, [llf.displacementConstraint("left", ux=0, uy=0, uz=0)]) - 1] = True
+        fr = ~fixed
+        ud = np.zeros(b - a)
+        ud[fr] = spla.spsolve(Ki.tocsc()[fr][:, fr].tocsc(), fi[fr])
+        errs.append({"instance": int(k), "dofs": int(b - a),
+                     "rel_err": float(np.linalg.norm(res[gi][0].a[a:b, 0] - ud) / np.linalg.norm(ud))})
     # the plain GPU form: every instance on its own, FP64 assembly and
-    # Jacobi-PCG to the same tolerance, one after the other (patterns built
-    # before the timed loop, as for the batch)
+    # Jacobi-PCG (FP64) to the same tolerance, one after the other (patterns
+    # built before the timed loop, as for the batch)
     plain = None
     if not args.no_plain:
         singles = []
         for i, (m, E, nu) in enumerate(inst):
+            llf.set_current(m)
             Pi = llf.Problem([llf.Material("body", E=E, nu=nu)], type="Solid", mesh=m)
             Pi.pattern()
             singles.append((Pi, llf.loadVector(Pi, [llf.load("right", fx=1.0)]),
                             [llf.displacementConstraint("left", ux=0, uy=0, uz=0)]))
+
         def solve_one(Pi, fi, si):
             Ki = llf.stiffnessMatrix(Pi)
-            return llf.solveField(Ki, fi, support=si, iterative=True, preconditioner="jacobi", reltol=1e-12,
+            return llf.solveField(Ki, fi, support=si, iterative=True, preconditioner="jacobi", reltol=reltol,
                                   maxiter=20 * 3 * Pi.non)
         solve_one(*singles[int(np.argmin([m.nel for m, _, _ in inst]))])   # warm-up
         torch.cuda.synchronize()
@@ -329,19 +392,22 @@ def run_batched(args, llf):
         torch.cuda.synchronize()
         tp = time.perf_counter() - t0
         plain = {"value": len(inst) / tp, "unit": "solves/s", "seconds": tp,
-                 "form": "one instance at a time: FP64 assembly + Jacobi-PCG to 1e-12",
+                 "form": f"one instance at a time: FP64 assembly + FP64 Jacobi-PCG to {reltol:g}",
                  "speedup_of_batched": (len(inst) / t) / (len(inst) / tp)}
     nel = sum(m.nel for m, _, _ in inst)
     return {"metric": "batched assemble+solve (independent tet10 systems / s)", "value": len(inst) / t,
             "unit": "solves/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic: seeded sample of the 512-instance tet10 workload",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": ("f32-quadrature/f64-accumulate" if form == "fp32q" else "f64") + " assembly, "
+                     + ("f32 iterations/f64 reliable updates" if mixed else "f64") + " CG",
+            "data": f"synthetic: seeded tet10 boxes ({len(inst)} of the 512-instance workload)",
             "config": {"workload": f"batched-tet10-{len(inst)}", "instances": len(inst), "elements": nel,
-                       "dofs": 3 * batch.non, "structural_nnz": P.pattern().nnz, "precond": prec,
-                       "reltol": 1e-12},
-            "cg_iterations": {"min": int(np.min(u.iterations)), "median": float(np.median(u.iterations)),
-                              "max": int(np.max(u.iterations))},
-            "rel_err_vs_direct": errs, "plain_gpu": plain}
+                       "dofs": int(3 * sum(sizes)), "groups": len(groups), "group_nnz_budget": args.group_nnz,
+                       "structural_nnz": int(sum(P.pattern().nnz for _, P, *_ in built)), "precond": prec,
+                       "reltol": reltol, "assembly": form, "solve": args.batched_solve},
+            "cg_iterations": {"min": int(its.min()), "median": float(np.median(its)), "max": int(its.max())},
+            "rel_err_vs_direct": errs, "max_rel_err_vs_direct": max(e["rel_err"] for e in errs),
+            "plain_gpu": plain}
 
 
 def run_serving(args, llf):
@@ -723,10 +789,12 @@ def main():
         samples = {}
         try:
             bargs = _ap.Namespace(**{**vars(args), "instances": 16, "steps": 1, "warmup": 1, "no_plain": False,
-                                     "precond": None})
+                                     "precond": None, "batched_form": "fp32q", "batched_solve": "mixed",
+                                     "batched_reltol": 1e-10, "group_nnz": 1.5e9})
             r = run_batched(bargs, llf)
-            samples["batched"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "config", "cg_iterations",
-                                                    "rel_err_vs_direct", "plain_gpu") if k in r}
+            samples["batched"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "dtype", "config", "cg_iterations",
+                                                    "rel_err_vs_direct", "max_rel_err_vs_direct", "plain_gpu")
+                                  if k in r}
         except Exception as ex:
             samples["batched"] = {"error": str(ex)}
         try:

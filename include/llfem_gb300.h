@@ -507,6 +507,22 @@ int llf_pcg_batched(llf_ctx *ctx, const llf_matrix *m, const double *b, double *
                     int precond, double reltol, int64_t maxiter, int64_t *iters,
                     double *relres);
 
+/* Mixed-precision form of llf_pcg_batched (nseg = 1: a single system),
+ * replacing the same cg(K.A[free,free], ...) call (src/linear.jl:3827-3828).
+ * The iterations run in FP32: an FP32 copy of the matrix values, FP32
+ * vectors and products, the preconditioner (Jacobi, block Jacobi or IC(0))
+ * applied into FP32.  The solution is accumulated in FP64 and the residual
+ * is replaced by the true residual b - A x of the FP64 matrix whenever the
+ * FP32 one has fallen 100-fold since the last replacement, at the
+ * tolerance and at maxiter; a system stops only when that true FP64
+ * residual meets ||r|| <= reltol ||r0||, so relres[] is an FP64 residual.
+ * iters[] counts FP32 products.  Each system runs its own CG, and its
+ * result is the same alone and in a batch. */
+int llf_pcg_mixed(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x,
+                  const uint8_t *fixed, int nseg, const int64_t *seg_off,
+                  int precond, double reltol, int64_t maxiter, int64_t *iters,
+                  double *relres);
+
 /* ======================================================================== */
 /* Serving                                                                  */
 /* ======================================================================== */

@@ -97,6 +97,7 @@ SIGNATURES = {
     "llf_matrix_destroy": (i32, [vp, vp]),
     "llf_pcg": (i32, [vp, vp, P_dbl, P_dbl, P_u8, i32, dbl, i64, P_i64, P_dbl]),
     "llf_pcg_batched": (i32, [vp, vp, P_dbl, P_dbl, P_u8, i32, P_i64, i32, dbl, i64, P_i64, P_dbl]),
+    "llf_pcg_mixed": (i32, [vp, vp, P_dbl, P_dbl, P_u8, i32, P_i64, i32, dbl, i64, P_i64, P_dbl]),
     "llf_pcg_noalloc": (i32, [vp, vp, vp, vp, vp, i32, dbl, i64, P_i64, P_dbl]),
     "llf_server_create": (i32, [i32, i32, i64, PP]),
     "llf_server_submit_heat": (i32, [vp, i32, i64, P_dbl, i64, i32, P_i64, i32, i32, dbl, dbl, P_dbl, P_dbl, P_u8,
@@ -402,8 +403,9 @@ class DeviceMatrix:
         return x, it.value, rr.value
 
     def pcg_batched(self, b, x0, fixed, seg_off, precond=PRECOND_NONE, reltol=1.4901161193847656e-08,
-                    maxiter=None, raise_on_fail=True):
-        """Independent CG per block-diagonal segment [seg_off[g], seg_off[g+1])."""
+                    maxiter=None, raise_on_fail=True, mixed=False):
+        """Independent CG per block-diagonal segment [seg_off[g], seg_off[g+1]);
+        mixed: FP32 iterations with FP64 reliable updates (llf_pcg_mixed)."""
         b, x = f64(b), f64(x0).copy()
         fx = np.ascontiguousarray(fixed, dtype=np.uint8)
         so = i64a(seg_off)
@@ -411,9 +413,10 @@ class DeviceMatrix:
         its = np.zeros(nseg, dtype=np.int64)
         rr = np.zeros(nseg)
         maxiter = self.n if maxiter is None else int(maxiter)
-        rc = lib().llf_pcg_batched(self.ctx.h, self.h, ptr(b, C.c_double), ptr(x, C.c_double), ptr(fx, C.c_uint8),
-                                   nseg, ptr(so, C.c_int64), int(precond), float(reltol), maxiter,
-                                   ptr(its, C.c_int64), ptr(rr, C.c_double))
+        fn = lib().llf_pcg_mixed if mixed else lib().llf_pcg_batched
+        rc = fn(self.ctx.h, self.h, ptr(b, C.c_double), ptr(x, C.c_double), ptr(fx, C.c_uint8),
+                nseg, ptr(so, C.c_int64), int(precond), float(reltol), maxiter,
+                ptr(its, C.c_int64), ptr(rr, C.c_double))
         if rc != LLF_OK and (raise_on_fail or rc != -4):
             self.ctx.check(rc, "pcg_batched")
         return x, its, rr

@@ -814,15 +814,20 @@ def solveField(K: SystemMatrix, f, support=(), iterative=False, reltol=SQRT_EPS,
 
 
 def solveFieldBatched(K: SystemMatrix, f, support=(), node_offsets=None, iterative=True, reltol=SQRT_EPS,
-                      maxiter=None, preconditioner="jacobi"):
+                      maxiter=None, preconditioner="jacobi", precision="fp64"):
     """Many independent systems at once: K is the block-diagonal matrix of a
-    batch (concat_meshes), instance i owning nodes node_offsets[i]..[i+1]-1.
-    Every instance runs its own CG (own scalars and stopping rule) inside the
-    same launches; instance i's result is bit-identical to solving it alone.
-    Returns the field and per-instance iteration counts / residuals."""
+    batch (concat_meshes), instance i owning nodes node_offsets[i]..[i+1]-1
+    (node_offsets=None: one system).  Every instance runs its own CG (own
+    scalars and stopping rule) inside the same launches; instance i's result
+    is bit-identical to solving it alone.  precision="mixed" runs the
+    iterations in FP32 with FP64 reliable updates (llf_pcg_mixed): the
+    stopping test is still on the FP64 residual.  Returns the field and
+    per-instance iteration counts / residuals."""
     problem = K.model
     if node_offsets is None:
-        raise ValueError("solveFieldBatched: node_offsets required")
+        node_offsets = [0, problem.non]
+    if precision not in ("fp64", "mixed"):
+        raise ValueError(f"solveFieldBatched: precision {precision!r} (fp64 or mixed)")
     u = _field_for(problem, np.zeros(problem.pdim * problem.non))
     applyBoundaryConditions_(u, list(support))
     fixed = np.zeros(problem.pdim * problem.non, dtype=np.uint8)
@@ -835,7 +840,7 @@ def solveFieldBatched(K: SystemMatrix, f, support=(), node_offsets=None, iterati
     seg = np.asarray(node_offsets, dtype=np.int64) * problem.pdim
     maxiter = problem.non * problem.dim if maxiter is None else maxiter
     x, its, rr = K.dm.pcg_batched(fa, u.a[:, 0], fixed, seg, precond=prec, reltol=reltol, maxiter=maxiter,
-                                  raise_on_fail=not iterative)
+                                  raise_on_fail=not iterative, mixed=precision == "mixed")
     u.a[:, 0] = x
     u.iterations, u.relres = its, rr
     return u

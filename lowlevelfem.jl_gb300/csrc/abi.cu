@@ -1086,20 +1086,20 @@ int llf_pcg_noalloc(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double
   return rc == LLF_OK ? llf_ok(ctx) : rc;
 }
 
-int llf_pcg_batched(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x, const uint8_t *fixed,
-                    int nseg, const int64_t *seg_off, int precond, double reltol, int64_t maxiter,
-                    int64_t *iters, double *relres) {
+static int pcg_batched_host(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x, const uint8_t *fixed,
+                            int nseg, const int64_t *seg_off, int precond, double reltol, int64_t maxiter,
+                            int64_t *iters, double *relres, bool mixed) {
   if (!ctx) return LLF_ERR_ARG;
   if (!m || !b || !x || !fixed || !seg_off || !iters || !relres || nseg < 1)
-    return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched: null argument or nseg < 1");
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched/llf_pcg_mixed: null argument or nseg < 1");
   if (precond < LLF_PRECOND_NONE || precond > LLF_PRECOND_IC0)
-    return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched: unknown preconditioner");
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched/llf_pcg_mixed: unknown preconditioner");
   const int64_t n = m->pat->ndof;
   if (seg_off[0] != 0 || seg_off[nseg] != n)
-    return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched: seg_off must run from 0 to the DoF count");
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched/llf_pcg_mixed: seg_off must run from 0 to the DoF count");
   for (int g = 0; g < nseg; ++g)
     if (seg_off[g + 1] < seg_off[g] || (seg_off[g] % m->pat->pdim) != 0)
-      return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched: seg_off must be non-decreasing node boundaries");
+      return llf_fail(ctx, LLF_ERR_ARG, "llf_pcg_batched/llf_pcg_mixed: seg_off must be non-decreasing node boundaries");
   double *db = nullptr, *dx = nullptr;
   uint8_t *df = nullptr;
   LLF_CUDA_TRY(ctx, dalloc(ctx, &db, n));
@@ -1108,7 +1108,7 @@ int llf_pcg_batched(llf_ctx *ctx, const llf_matrix *m, const double *b, double *
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(db, b, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(df, fixed, n, cudaMemcpyHostToDevice, ctx->stream));
-  int rc = pcg_batched_impl(ctx, m, db, dx, df, nseg, seg_off, precond, reltol, maxiter, iters, relres);
+  int rc = pcg_batched_impl(ctx, m, db, dx, df, nseg, seg_off, precond, reltol, maxiter, iters, relres, mixed);
   if (rc == LLF_OK || rc == LLF_ERR_NOT_CONVERGED) {
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
     LLF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1118,6 +1118,18 @@ int llf_pcg_batched(llf_ctx *ctx, const llf_matrix *m, const double *b, double *
   dfree(ctx, df);
   cudaStreamSynchronize(ctx->stream);
   return rc == LLF_OK ? llf_ok(ctx) : rc;
+}
+
+int llf_pcg_batched(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x, const uint8_t *fixed,
+                    int nseg, const int64_t *seg_off, int precond, double reltol, int64_t maxiter,
+                    int64_t *iters, double *relres) {
+  return pcg_batched_host(ctx, m, b, x, fixed, nseg, seg_off, precond, reltol, maxiter, iters, relres, false);
+}
+
+int llf_pcg_mixed(llf_ctx *ctx, const llf_matrix *m, const double *b, double *x, const uint8_t *fixed,
+                  int nseg, const int64_t *seg_off, int precond, double reltol, int64_t maxiter,
+                  int64_t *iters, double *relres) {
+  return pcg_batched_host(ctx, m, b, x, fixed, nseg, seg_off, precond, reltol, maxiter, iters, relres, true);
 }
 
 }  // extern "C"

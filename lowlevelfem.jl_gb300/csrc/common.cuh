@@ -280,9 +280,10 @@ int pcg_noalloc_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doubl
 int heat_fdm_impl(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C, const double *d_q, int nq, double *d_T,
                   const uint8_t *d_fixed, int64_t nsteps, double dt, double theta, int precond, double reltol,
                   int64_t maxiter, int64_t *iters_total);
+// mixed: FP32 iterations with FP64 reliable updates (solve.cu, pcg_mixed_core)
 int pcg_batched_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                      const uint8_t *d_fixed, int nseg, const int64_t *seg_off, int precond,
-                     double reltol, int64_t maxiter, int64_t *iters, double *relres);
+                     double reltol, int64_t maxiter, int64_t *iters, double *relres, bool mixed = false);
 
 // ic0.cu: multicolour node-block IC(0)
 struct Ic0Factor {

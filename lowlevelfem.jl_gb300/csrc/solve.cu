@@ -40,10 +40,19 @@ constexpr int CHUNK = 768;  // DoFs per reduction chunk (a multiple of every pdi
 constexpr int CHUNK_PER_THREAD = CHUNK / CG_THREADS;  // a chunk's DoFs per thread of its block
 static_assert(CHUNK % CG_THREADS == 0, "a chunk is whole rounds of a block");
 
+// Work vectors of the mixed-precision CG (FP32 matrix copy and vectors, the
+// FP64 right-hand side minus the prescribed values' product).
+struct MixedBufs {
+  float *nz32 = nullptr, *r = nullptr, *z = nullptr, *u = nullptr, *c = nullptr;
+  double *rb = nullptr;
+};
+
 struct SegState {
   double rho_prev, rho, alpha, res, res0, tol;
   long long it, maxiter;
   int done, breakdown;
+  double rmax;  // mixed precision: true residual at the last reliable update
+  int upd, pad;  // mixed precision: a reliable update is due
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -353,6 +362,8 @@ __global__ void k_seg_start(Seg S, const double *part, double reltol, long long 
       q.it = 0;
       q.maxiter = maxiter;
       q.breakdown = 0;
+      q.rmax = q.res0;
+      q.upd = 0;
       q.done = (q.res <= q.tol) || (maxiter <= 0);
       if (!q.done) atomicAdd(S.active, 1);
     }
@@ -593,12 +604,12 @@ struct IcPair {
 // The forward sweep of one colour (t: position in colour order, first = the
 // colour's first position).  LAST: the last colour, whose backward step
 // z_j = L_jj^-T y_j needs no later neighbour and is done here as well.
-template <int P, bool LAST>
+template <int P, bool LAST, class RT>
 __global__ void __launch_bounds__(CG_THREADS)
 k_ic0_forward(const int32_t *__restrict__ nodes, int64_t first, int count, const int64_t *__restrict__ fptr,
               const int32_t *__restrict__ fk, const float *__restrict__ Lf, const float *__restrict__ Ldf,
               const int32_t *__restrict__ segc, const SegState *__restrict__ st,
-              const double *__restrict__ r, float *__restrict__ y) {
+              const RT *__restrict__ r, float *__restrict__ y) {
   constexpr int PP = P * P;
   const int lane = threadIdx.x & 31, gl = lane & (IC_G - 1);
   const int per_warp = 32 / IC_G;
@@ -786,12 +797,11 @@ struct IcApply {
   float *zf = nullptr;  // FP32 work vector (ndof)
 };
 
-template <int P>
-void enqueue_ic0(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const IcApply &ic, const double *r, double *z,
-                 double *part) {
+// The colour sweeps of one IC(0) application, z (in ic.zf, FP32) from r.
+template <int P, class RT>
+void enqueue_ic0_sweeps(llf_ctx *ctx, const Seg &S, const IcApply &ic, const RT *r) {
   const Ic0Factor &f = *ic.f;
   cudaStream_t s = ctx->stream;
-  (void)m;
   auto grid = [&](int count) {
     const int64_t warps = (count + 32 / IC_G - 1) / (32 / IC_G);
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)ctx->num_sms * 16));
@@ -820,11 +830,11 @@ void enqueue_ic0(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const IcApply 
     KernelScope k(ctx, "k_ic0_forward");
     const int64_t t0 = f.color_ptr[c];
     if (c == C - 1)
-      launch(k_ic0_forward<P, true>, count, (const int32_t *)f.d_nodes, t0, count,
+      launch(k_ic0_forward<P, true, RT>, count, (const int32_t *)f.d_nodes, t0, count,
              (const int64_t *)f.fptr, (const int32_t *)f.fk, (const float *)f.Lf, (const float *)f.Ldf,
              (const int32_t *)f.segc, (const SegState *)S.st, r, ic.zf);
     else
-      launch(k_ic0_forward<P, false>, count, (const int32_t *)f.d_nodes, t0, count,
+      launch(k_ic0_forward<P, false, RT>, count, (const int32_t *)f.d_nodes, t0, count,
              (const int64_t *)f.fptr, (const int32_t *)f.fk, (const float *)f.Lf, (const float *)f.Ldf,
              (const int32_t *)f.segc, (const SegState *)S.st, r, ic.zf);
   }
@@ -836,7 +846,14 @@ void enqueue_ic0(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const IcApply 
            (const int64_t *)f.bptr, (const int32_t *)f.bk, (const float *)f.Lb, (const float *)f.Ldf,
            (const int32_t *)f.segc, (const SegState *)S.st, ic.zf);
   }
-  { KernelScope k(ctx, "k_seg_zr"); k_seg_zr<<<chunk_grid(S), CG_THREADS, 0, s>>>(S, ic.zf, r, z, part); }
+}
+
+template <int P>
+void enqueue_ic0(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const IcApply &ic, const double *r, double *z,
+                 double *part) {
+  (void)m;
+  enqueue_ic0_sweeps<P, double>(ctx, S, ic, r);
+  { KernelScope k(ctx, "k_seg_zr"); k_seg_zr<<<chunk_grid(S), CG_THREADS, 0, ctx->stream>>>(S, ic.zf, r, z, part); }
 }
 
 // z = M^-1 r and rho = z.r of the first iteration.
@@ -879,6 +896,11 @@ int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, 
              double *part, double *part2, double *part3, int precond, double reltol, int64_t maxiter, bool use_graph,
              SegState *hst, const IcApply &ic = IcApply());
 int pcg_outcome(llf_ctx *ctx, int nseg, const SegState *hst, int64_t *iters, double *relres);
+template <int P>
+int pcg_mixed_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
+                   const Seg &S, const MixedBufs &B, double *xw, double *tmp, double *pinv, double *part,
+                   double *part2, double *part3, int precond, double reltol, int64_t maxiter, bool use_graph,
+                   SegState *hst, const IcApply &ic);
 
 // Buffers, chunking and preconditioner of the segmented PCG for one matrix
 // and one set of fixed DoFs, built once and reused by every solve with them
@@ -899,13 +921,16 @@ struct PcgPlan {
   IcApply ic;
   int32_t *d_node_seg = nullptr;
   int precond = 0, nseg = 0;
+  bool mixed = false;  // FP32 iterations with FP64 reliable updates (pcg_mixed_core)
+  MixedBufs mb;
   Seg S{};
   std::vector<SegState> hst;
 
   int create(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixed, int nseg_, const int64_t *seg_off,
-             int precond_) {
+             int precond_, bool mixed_ = false) {
     precond = precond_;
     nseg = nseg_;
+    mixed = mixed_;
     const llf_pattern *pat = m->pat;
     const int64_t n = pat->ndof;
     cudaStream_t s = ctx->stream;
@@ -927,9 +952,18 @@ struct PcgPlan {
     LLF_CUDA_TRY(ctx, dalloc(ctx, &d_sf, nseg + 1));
     LLF_CUDA_TRY(ctx, dalloc(ctx, &d_active, 1));
     LLF_CUDA_TRY(ctx, dalloc(ctx, &d_st, nseg));
-    LLF_CUDA_TRY(ctx, dalloc(ctx, &r, n));
-    LLF_CUDA_TRY(ctx, dalloc(ctx, &z, n));
-    LLF_CUDA_TRY(ctx, dalloc(ctx, &u, n));
+    if (mixed) {
+      LLF_CUDA_TRY(ctx, dalloc(ctx, &mb.nz32, pat->nnz));
+      LLF_CUDA_TRY(ctx, dalloc(ctx, &mb.r, n));
+      LLF_CUDA_TRY(ctx, dalloc(ctx, &mb.z, n));
+      LLF_CUDA_TRY(ctx, dalloc(ctx, &mb.u, n));
+      LLF_CUDA_TRY(ctx, dalloc(ctx, &mb.c, n));
+      LLF_CUDA_TRY(ctx, dalloc(ctx, &mb.rb, n));
+    } else {
+      LLF_CUDA_TRY(ctx, dalloc(ctx, &r, n));
+      LLF_CUDA_TRY(ctx, dalloc(ctx, &z, n));
+      LLF_CUDA_TRY(ctx, dalloc(ctx, &u, n));
+    }
     LLF_CUDA_TRY(ctx, dalloc(ctx, &c, n));
     LLF_CUDA_TRY(ctx, dalloc(ctx, &xw, n));
     LLF_CUDA_TRY(ctx, dalloc(ctx, &pinv, precond == LLF_PRECOND_BJACOBI ? n * P : n));
@@ -975,8 +1009,10 @@ struct PcgPlan {
 
   int solve(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
             double reltol, int64_t maxiter, int64_t *iters, double *relres) {
-    int rc = pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, part2, part3, precond, reltol,
-                         maxiter, !ctx->profiling, hst.data(), ic);
+    int rc = mixed ? pcg_mixed_core<P>(ctx, m, d_b, d_x, d_fixed, S, mb, xw, c, pinv, part, part2, part3, precond,
+                                       reltol, maxiter, !ctx->profiling, hst.data(), ic)
+                   : pcg_core<P>(ctx, m, d_b, d_x, d_fixed, S, r, z, u, c, xw, pinv, part, part2, part3, precond,
+                                 reltol, maxiter, !ctx->profiling, hst.data(), ic);
     if (rc != LLF_OK) return rc;
     return pcg_outcome(ctx, nseg, hst.data(), iters, relres);
   }
@@ -991,15 +1027,16 @@ struct PcgPlan {
     dfree(ctx, d_st); dfree(ctx, r); dfree(ctx, z); dfree(ctx, u); dfree(ctx, c); dfree(ctx, xw);
     dfree(ctx, pinv); dfree(ctx, part); dfree(ctx, part2); dfree(ctx, part3); dfree(ctx, d_arrive);
     dfree(ctx, d_perm);
+    dfree(ctx, mb.nz32); dfree(ctx, mb.r); dfree(ctx, mb.z); dfree(ctx, mb.u); dfree(ctx, mb.c); dfree(ctx, mb.rb);
   }
 };
 
 template <int P>
 int pcg_segments(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                  const uint8_t *d_fixed, int nseg, const int64_t *seg_off, int precond,
-                 double reltol, int64_t maxiter, int64_t *iters, double *relres) {
+                 double reltol, int64_t maxiter, int64_t *iters, double *relres, bool mixed = false) {
   PcgPlan<P> plan;
-  int rc = plan.create(ctx, m, d_fixed, nseg, seg_off, precond);
+  int rc = plan.create(ctx, m, d_fixed, nseg, seg_off, precond, mixed);
   if (rc == LLF_OK) rc = plan.solve(ctx, m, d_b, d_x, d_fixed, reltol, maxiter, iters, relres);
   plan.destroy(ctx);
   return rc;
@@ -1069,6 +1106,451 @@ int pcg_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, 
     }
     LLF_CUDA_TRY(ctx, cudaGetLastError());
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(h_active, d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    active = *h_active;
+  }
+  *h_active = 0;
+  if (exec) cudaGraphExecDestroy(exec);
+  { KernelScope k(ctx, "k_cg_merge"); k_cg_merge<<<gv, CG_THREADS, 0, s>>>(xw, d_fixed, d_x, n); }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(hst, S.st, sizeof(SegState) * nseg, cudaMemcpyDeviceToHost, s));
+  LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  return LLF_OK;
+}
+
+
+// ---------------------------------------------------------------- mixed CG
+// Mixed-precision PCG: the iterations run in FP32 — an FP32 copy of the
+// matrix values, FP32 vectors, FP32 products on the FP32 pipe, the
+// preconditioner applied into FP32 — while the solution is accumulated in
+// FP64 and the residual is replaced by the true FP64 residual
+// r = (b - A x_c) - A x of the FP64 matrix whenever the FP32 recurrence
+// residual has fallen by MX_DELTA since the last replacement, when it meets
+// the tolerance, and at maxiter (reliable updates; the search direction is
+// kept across a replacement).  A system is done only when its true FP64
+// residual meets ||r|| <= reltol ||r0||.  Scalars (rho, alpha, the dot
+// products) are FP64.  Every system of a batch still runs its own CG and
+// reductions per chunk and then per system in chunk order, so a system
+// gives the same result alone and in a batch.
+constexpr double MX_DELTA = 1e-2;
+
+__global__ void k_f64_to_f32(const double *__restrict__ a, float *__restrict__ b, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = __double2float_rn(a[i]);
+}
+
+// FP32 products of the P columns of a node (node_columns_at in FP32).
+template <int P>
+__device__ __forceinline__ void node_columns32_at(const float *__restrict__ nz, const int32_t *__restrict__ nadj,
+                                                  const float *__restrict__ x, int64_t r0, int64_t r1, bool valid,
+                                                  int g, float (&acc)[P]) {
+#pragma unroll
+  for (int j = 0; j < P; ++j) acc[j] = 0.f;
+  if (valid) {
+    const int n = (int)(r1 - r0) * P;
+    const float *col = nz + (int64_t)P * r0 * P;
+    int k = g;
+    int32_t ra = k < n ? nadj[r0 + k / P] : 0, rb = k + SPMV_G < n ? nadj[r0 + (k + SPMV_G) / P] : 0;
+    for (; k + SPMV_G < n; k += 2 * SPMV_G) {
+      const int k2 = k + SPMV_G, kn = k + 2 * SPMV_G;
+      float v[P], v2[P];
+#pragma unroll
+      for (int j = 0; j < P; ++j) {
+        v[j] = col[(int64_t)j * n + k];
+        v2[j] = col[(int64_t)j * n + k2];
+      }
+      const float xa = x[(int64_t)P * ra + k % P];
+      const float xb = x[(int64_t)P * rb + k2 % P];
+      ra = kn < n ? nadj[r0 + kn / P] : 0;
+      rb = kn + SPMV_G < n ? nadj[r0 + (kn + SPMV_G) / P] : 0;
+#pragma unroll
+      for (int j = 0; j < P; ++j) acc[j] = fmaf(v2[j], xb, fmaf(v[j], xa, acc[j]));
+    }
+    if (k < n) {
+      const float xa = x[(int64_t)P * ra + k % P];
+#pragma unroll
+      for (int j = 0; j < P; ++j) acc[j] = fmaf(col[(int64_t)j * n + k], xa, acc[j]);
+    }
+  }
+#pragma unroll
+  for (int off = SPMV_G / 2; off > 0; off >>= 1)
+#pragma unroll
+    for (int j = 0; j < P; ++j) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], off);
+}
+
+// z_c = M^-1 r at DoF c with an FP32 residual (FP64 arithmetic, FP32 result).
+template <int P>
+__device__ __forceinline__ float apply_prec32(const double *__restrict__ pinv, int mode, const float *__restrict__ r,
+                                              int64_t c) {
+  if (mode == LLF_PRECOND_BJACOBI) {
+    const int64_t B = c / P;
+    const int i = (int)(c % P);
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j < P; ++j) acc = __fma_rn(pinv[(size_t)B * P * P + i * P + j], (double)r[P * B + j], acc);
+    return __double2float_rn(acc);
+  }
+  return __double2float_rn(__dmul_rn(pinv[c], (double)r[c]));
+}
+
+// rb = r64 = fixed ? 0 : b - A x_c; r = (float) r64; x = 0; u = 0; partial r.r.
+__global__ void __launch_bounds__(CG_THREADS)
+k_mx_init(Seg S, const double *__restrict__ b, const double *__restrict__ y, const uint8_t *__restrict__ fixed,
+          double *__restrict__ rb, float *__restrict__ r, double *__restrict__ xw, float *__restrict__ u,
+          double *__restrict__ part) {
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    double rr = 0.0;
+    for (int64_t i = S.cbeg[ch] + threadIdx.x; i < S.cend[ch]; i += blockDim.x) {
+      const double ri = fixed[i] ? 0.0 : __dsub_rn(b[i], y[i]);
+      rb[i] = ri;
+      r[i] = __double2float_rn(ri);
+      xw[i] = 0.0;
+      u[i] = 0.f;
+      rr = __fma_rn(ri, ri, rr);
+    }
+    const double sm = block_sum(rr);
+    if (threadIdx.x == 0) part[ch] = sm;
+  }
+}
+
+// First z = M^-1 r (local preconditioners) and partial z.r.
+template <int P>
+__global__ void __launch_bounds__(CG_THREADS)
+k_mx_prec(Seg S, const double *__restrict__ pinv, int mode, const float *__restrict__ r,
+          const uint8_t *__restrict__ fixed, float *__restrict__ z, double *__restrict__ part) {
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    if (S.st[S.cseg[ch]].done) continue;
+    double zr = 0.0;
+    for (int64_t i = S.cbeg[ch] + threadIdx.x; i < S.cend[ch]; i += blockDim.x) {
+      const float zi = fixed[i] ? 0.f : apply_prec32<P>(pinv, mode, r, i);
+      z[i] = zi;
+      zr = __fma_rn((double)zi, (double)r[i], zr);
+    }
+    const double sm = block_sum(zr);
+    if (threadIdx.x == 0) part[ch] = sm;
+  }
+}
+
+__global__ void __launch_bounds__(CG_THREADS) k_mx_dir(Seg S, const float *__restrict__ z, float *__restrict__ u) {
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    const SegState &q = S.st[S.cseg[ch]];
+    if (q.done) continue;
+    const float beta = __double2float_rn(q.rho / q.rho_prev);
+    const int64_t b = S.cbeg[ch], e = S.cend[ch];
+#pragma unroll
+    for (int k = 0; k < CHUNK_PER_THREAD; ++k) {
+      const int64_t i = b + threadIdx.x + (int64_t)k * CG_THREADS;
+      if (i < e) u[i] = fmaf(beta, u[i], z[i]);
+    }
+  }
+}
+
+// c = A32 u (masked) and alpha = rho / u.c (u.c in FP64) — k_seg_spmv in FP32.
+template <int P>
+__global__ void __launch_bounds__(CG_THREADS)
+k_mx_spmv(Seg S, const float *__restrict__ nz, const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
+          const float *__restrict__ u, const uint8_t *__restrict__ fixed, float *__restrict__ c,
+          double *__restrict__ part) {
+  constexpr int NPW = 32 / SPMV_G;
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, w = threadIdx.x >> 5, g = lane % SPMV_G;
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    if (S.st[S.cseg[ch]].done) continue;
+    double dot = 0.0;
+    const int64_t b0 = S.cbeg[ch] / P;
+    const int nb = (int)(S.cend[ch] / P - b0);
+    const int step = wpb * NPW;
+    auto node_of = [&](int rr) -> int64_t { return b0 + (rr < nb ? (S.perm ? (int)S.perm[b0 + rr] : rr) : 0); };
+    int rr = w * NPW + lane / SPMV_G;
+    int64_t B = node_of(rr);
+    int64_t q0 = rr < nb ? nptr[B] : 0, q1 = rr < nb ? nptr[B + 1] : 0;
+    for (int r0 = w * NPW; r0 < nb; r0 += step, rr += step) {
+      const bool valid = rr < nb;
+      const int64_t Bn = node_of(rr + step);
+      const bool vn = rr + step < nb;
+      const int64_t q0n = vn ? nptr[Bn] : 0, q1n = vn ? nptr[Bn + 1] : 0;
+      float acc[P];
+      node_columns32_at<P>(nz, nadj, u, q0, q1, valid, g, acc);
+      if (valid && g == 0) {
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+          const int64_t d = P * B + j;
+          const float v = fixed[d] ? 0.f : acc[j];
+          c[d] = v;
+          dot = __fma_rn((double)u[d], (double)v, dot);
+        }
+      }
+      B = Bn;
+      q0 = q0n;
+      q1 = q1n;
+    }
+    const double sm = block_sum(dot);
+    if (threadIdx.x == 0) part[ch] = sm;
+    const int sg = S.cseg[ch];
+    if (arrive_last(S.arrive + sg, S.sfirst[sg + 1] - S.sfirst[sg])) {
+      const double uc = seg_total_l2(S, sg, part);
+      if (threadIdx.x == 0) seg_set_alpha(S, sg, uc);
+    }
+  }
+}
+
+// x += alpha u (FP64), r -= alpha c (FP32), with a local preconditioner the
+// next z and z.r; the segment's last block decides whether a reliable update
+// is due (recurrence residual below MX_DELTA of the last true one, at the
+// tolerance, or at maxiter) and otherwise moves rho on.
+template <int P>
+__global__ void __launch_bounds__(CG_THREADS)
+k_mx_update(Seg S, double *__restrict__ xw, float *__restrict__ r, const float *__restrict__ u,
+            const float *__restrict__ c, double *__restrict__ part, double *__restrict__ part2,
+            const double *__restrict__ pinv, int mode, bool local_prec, const uint8_t *__restrict__ fixed,
+            float *__restrict__ z) {
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    const int sg = S.cseg[ch];
+    const SegState &q = S.st[sg];
+    if (q.done) continue;
+    const double alpha = q.alpha;
+    const float af = __double2float_rn(alpha);
+    double rr = 0.0, zr = 0.0;
+    const int64_t b = S.cbeg[ch], e = S.cend[ch];
+#pragma unroll
+    for (int k = 0; k < CHUNK_PER_THREAD; ++k) {
+      const int64_t i = b + threadIdx.x + (int64_t)k * CG_THREADS;
+      if (i < e) {
+        xw[i] = __fma_rn(alpha, (double)u[i], xw[i]);
+        const float ri = fmaf(-af, c[i], r[i]);
+        r[i] = ri;
+        rr = __fma_rn((double)ri, (double)ri, rr);
+      }
+    }
+    if (local_prec) {
+      __syncthreads();
+      for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        const float zi = fixed[i] ? 0.f : apply_prec32<P>(pinv, mode, r, i);
+        z[i] = zi;
+        zr = __fma_rn((double)zi, (double)r[i], zr);
+      }
+    }
+    const double s1 = block_sum(rr);
+    const double s2 = local_prec ? block_sum(zr) : 0.0;
+    if (threadIdx.x == 0) {
+      part[ch] = s1;
+      if (local_prec) part2[ch] = s2;
+    }
+    if (arrive_last(S.arrive + S.nseg + sg, S.sfirst[sg + 1] - S.sfirst[sg])) {
+      const double trr = seg_total_l2(S, sg, part);
+      const double tzr = local_prec ? seg_total_l2(S, sg, part2) : 0.0;
+      if (threadIdx.x == 0) {
+        SegState &w = S.st[sg];
+        const double res32 = sqrt(trr);
+        w.it += 1;
+        w.rho_prev = w.rho;
+        if (res32 <= w.tol || res32 <= MX_DELTA * w.rmax || w.it >= w.maxiter || !isfinite(res32)) {
+          w.upd = 1;
+        } else if (local_prec) {
+          w.rho = tzr;
+        }
+      }
+    }
+  }
+}
+
+// Reliable update of the systems that asked for one: r64 = rb - A64 x (FP64
+// product, masked), r = (float) r64, with a local preconditioner z = M^-1 r
+// and z.r; the system's last block takes the true residual: done when it
+// meets the tolerance (or at maxiter), otherwise it becomes the new
+// reference of the update test.
+template <int P>
+__global__ void __launch_bounds__(CG_THREADS)
+k_mx_true(Seg S, const double *__restrict__ nz, const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
+          const double *__restrict__ xw, const double *__restrict__ rb, const uint8_t *__restrict__ fixed,
+          float *__restrict__ r, const double *__restrict__ pinv, int mode, bool local_prec, float *__restrict__ z,
+          double *__restrict__ part, double *__restrict__ part2) {
+  constexpr int NPW = 32 / SPMV_G;
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, w = threadIdx.x >> 5, g = lane % SPMV_G;
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    const int sg = S.cseg[ch];
+    {
+      const SegState &q = S.st[sg];
+      if (q.done || !q.upd) continue;
+    }
+    double rr = 0.0, zr = 0.0;
+    const int64_t b0 = S.cbeg[ch] / P;
+    const int nb = (int)(S.cend[ch] / P - b0);
+    for (int r0 = w * NPW; r0 < nb; r0 += wpb * NPW) {
+      const int rr_idx = r0 + lane / SPMV_G;
+      const bool valid = rr_idx < nb;
+      const int64_t B = b0 + (valid ? rr_idx : 0);
+      double acc[P];
+      node_columns<P>(nz, nptr, nadj, xw, B, valid, g, acc);
+      if (valid && g == 0) {
+        float rn[P];
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+          const int64_t d = P * B + j;
+          const double v = fixed[d] ? 0.0 : __dsub_rn(rb[d], acc[j]);
+          rn[j] = __double2float_rn(v);
+          r[d] = rn[j];
+          rr = __fma_rn(v, v, rr);
+        }
+        if (local_prec) {
+#pragma unroll
+          for (int j = 0; j < P; ++j) {
+            const int64_t d = P * B + j;
+            float zi = 0.f;
+            if (!fixed[d]) {
+              if (mode == LLF_PRECOND_BJACOBI) {
+                double a = 0.0;
+#pragma unroll
+                for (int k = 0; k < P; ++k) a = __fma_rn(pinv[(size_t)B * P * P + j * P + k], (double)rn[k], a);
+                zi = __double2float_rn(a);
+              } else {
+                zi = __double2float_rn(__dmul_rn(pinv[d], (double)rn[j]));
+              }
+            }
+            z[d] = zi;
+            zr = __fma_rn((double)zi, (double)rn[j], zr);
+          }
+        }
+      }
+    }
+    const double s1 = block_sum(rr);
+    const double s2 = local_prec ? block_sum(zr) : 0.0;
+    if (threadIdx.x == 0) {
+      part[ch] = s1;
+      if (local_prec) part2[ch] = s2;
+    }
+    if (arrive_last(S.arrive + 2 * S.nseg + sg, S.sfirst[sg + 1] - S.sfirst[sg])) {
+      const double trr = seg_total_l2(S, sg, part);
+      const double tzr = local_prec ? seg_total_l2(S, sg, part2) : 0.0;
+      if (threadIdx.x == 0) {
+        SegState &q = S.st[sg];
+        q.res = sqrt(trr);
+        q.upd = 0;
+        if (q.res <= q.tol || q.it >= q.maxiter || !isfinite(q.res)) {
+          if (!isfinite(q.res)) q.breakdown = 1;
+          q.done = 1;
+          atomicSub(S.active, 1);
+        } else {
+          q.rmax = q.res;
+          if (local_prec) q.rho = tzr;
+        }
+      }
+    }
+  }
+}
+
+// z.r after an IC(0) application in the mixed CG (z in FP32).
+__global__ void __launch_bounds__(CG_THREADS)
+k_mx_zr(Seg S, const float *__restrict__ zf, const float *__restrict__ r, double *__restrict__ part) {
+  for (int64_t ch = blockIdx.x; ch < S.nchunks; ch += gridDim.x) {
+    if (S.st[S.cseg[ch]].done) continue;
+    double zr = 0.0;
+    const int64_t b = S.cbeg[ch], e = S.cend[ch];
+#pragma unroll
+    for (int k = 0; k < CHUNK_PER_THREAD; ++k) {
+      const int64_t i = b + threadIdx.x + (int64_t)k * CG_THREADS;
+      if (i < e) zr = __fma_rn((double)zf[i], (double)r[i], zr);
+    }
+    const double sm = block_sum(zr);
+    if (threadIdx.x == 0) part[ch] = sm;
+    const int sg = S.cseg[ch];
+    if (arrive_last(S.arrive + 2 * S.nseg + sg, S.sfirst[sg + 1] - S.sfirst[sg])) {
+      const double t = seg_total_l2(S, sg, part);
+      if (threadIdx.x == 0) S.st[sg].rho = t;
+    }
+  }
+}
+
+
+template <int P>
+void enqueue_iteration_mixed(llf_ctx *ctx, const Seg &S, const llf_matrix *m, const double *pinv, int precond,
+                             const MixedBufs &B, double *xw, const uint8_t *fixed, double *part, double *part2,
+                             double *part3, const IcApply &ic) {
+  const llf_pattern *pat = m->pat;
+  cudaStream_t s = ctx->stream;
+  const bool local = precond != LLF_PRECOND_IC0;
+  float *z = local ? B.z : ic.zf;
+  { KernelScope k(ctx, "k_mx_dir"); k_mx_dir<<<chunk_grid(S), CG_THREADS, 0, s>>>(S, z, B.u); }
+  { KernelScope k(ctx, "k_mx_spmv");
+    k_mx_spmv<P><<<chunk_grid(S), CG_THREADS, 0, s>>>(S, B.nz32, pat->d_nptr, pat->d_nadj, B.u, fixed, B.c, part3); }
+  { KernelScope k(ctx, "k_mx_update");
+    k_mx_update<P><<<chunk_grid(S), CG_THREADS, 0, s>>>(S, xw, B.r, B.u, B.c, part, part2, pinv, precond, local,
+                                                        fixed, z); }
+  { KernelScope k(ctx, "k_mx_true");
+    k_mx_true<P><<<chunk_grid(S), CG_THREADS, 0, s>>>(S, m->d_nz, pat->d_nptr, pat->d_nadj, xw, B.rb, fixed, B.r,
+                                                      pinv, precond, local, z, part, part2); }
+  if (!local) {
+    enqueue_ic0_sweeps<P, float>(ctx, S, ic, B.r);
+    { KernelScope k(ctx, "k_mx_zr"); k_mx_zr<<<chunk_grid(S), CG_THREADS, 0, s>>>(S, ic.zf, B.r, part); }
+  }
+}
+
+// The mixed CG of every segment of S to completion (caller's buffers; no
+// allocation); the final per-segment states go to hst.
+template <int P>
+int pcg_mixed_core(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x, const uint8_t *d_fixed,
+                   const Seg &S, const MixedBufs &B, double *xw, double *tmp, double *pinv, double *part,
+                   double *part2, double *part3, int precond, double reltol, int64_t maxiter, bool use_graph,
+                   SegState *hst, const IcApply &ic) {
+  const llf_pattern *pat = m->pat;
+  const int64_t n = pat->ndof;
+  const int64_t nch = S.nchunks;
+  const int nseg = S.nseg;
+  cudaStream_t s = ctx->stream;
+  const unsigned gch = (unsigned)std::max<int64_t>(1, std::min<int64_t>(nch, (int64_t)ctx->num_sms * 8));
+  const unsigned gseg = (unsigned)std::max(1, std::min(nseg, ctx->num_sms * 8));
+  const unsigned gv = (unsigned)(ctx->num_sms * 4);
+  const bool local = precond != LLF_PRECOND_IC0;
+  if (local) {
+    KernelScope k(ctx, "k_precond_setup");
+    k_precond_setup<P><<<(unsigned)((pat->mesh->non + 127) / 128), 128, 0, s>>>(
+        m->d_nz, pat->d_colptr, pat->d_diagpos, d_fixed, pat->mesh->non, precond, pinv);
+  }
+  { KernelScope k(ctx, "k_f64_to_f32");
+    k_f64_to_f32<<<(unsigned)(ctx->num_sms * 8), CG_THREADS, 0, s>>>(m->d_nz, B.nz32, pat->nnz); }
+  { KernelScope k(ctx, "k_keep_fixed"); k_keep_fixed<<<gv, CG_THREADS, 0, s>>>(d_x, d_fixed, xw, n); }
+  { KernelScope k(ctx, "k_spmv"); k_spmv<P><<<gv, CG_THREADS, 0, s>>>(m->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, xw, tmp, n); }
+  { KernelScope k(ctx, "k_mx_init"); k_mx_init<<<gch, CG_THREADS, 0, s>>>(S, d_b, tmp, d_fixed, B.rb, B.r, xw, B.u, part); }
+  { KernelScope k(ctx, "k_seg_start"); k_seg_start<<<gseg, CG_THREADS, 0, s>>>(S, part, reltol, (long long)maxiter); }
+  if (local) {
+    { KernelScope k(ctx, "k_mx_prec"); k_mx_prec<P><<<gch, CG_THREADS, 0, s>>>(S, pinv, precond, B.r, d_fixed, B.z, part); }
+    { KernelScope k(ctx, "k_seg_rho"); k_seg_rho<<<gseg, CG_THREADS, 0, s>>>(S, part); }
+  } else {
+    enqueue_ic0_sweeps<P, float>(ctx, S, ic, B.r);
+    { KernelScope k(ctx, "k_mx_zr"); k_mx_zr<<<chunk_grid(S), CG_THREADS, 0, s>>>(S, ic.zf, B.r, part); }
+  }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  const int per_graph = 16;
+  long long launches_per_graph = 0;
+  cudaGraphExec_t exec = nullptr;
+  bool graph_ok = use_graph;
+  if (graph_ok) {
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const long long saved = ctx->launches;
+      for (int k = 0; k < per_graph; ++k)
+        enqueue_iteration_mixed<P>(ctx, S, m, pinv, precond, B, xw, d_fixed, part, part2, part3, ic);
+      launches_per_graph = ctx->launches - saved;
+      ctx->launches = saved;
+      if (cudaStreamEndCapture(s, &graph) != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+        graph_ok = false;
+      if (graph) cudaGraphDestroy(graph);
+    } else {
+      graph_ok = false;
+    }
+    cudaGetLastError();
+  }
+  int active = 1;
+  int *h_active = (int *)ctx->h_status;
+  while (active > 0) {
+    if (graph_ok) {
+      LLF_CUDA_TRY(ctx, cudaGraphLaunch(exec, s));
+      ctx->launches += launches_per_graph;
+    } else {
+      for (int k = 0; k < per_graph; ++k)
+        enqueue_iteration_mixed<P>(ctx, S, m, pinv, precond, B, xw, d_fixed, part, part2, part3, ic);
+    }
+    LLF_CUDA_TRY(ctx, cudaGetLastError());
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(h_active, S.active, sizeof(int), cudaMemcpyDeviceToHost, s));
     LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     active = *h_active;
   }
@@ -1262,13 +1744,13 @@ int spmv_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_x, double *d_y)
 
 int pcg_batched_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                      const uint8_t *d_fixed, int nseg, const int64_t *seg_off, int precond,
-                     double reltol, int64_t maxiter, int64_t *iters, double *relres) {
+                     double reltol, int64_t maxiter, int64_t *iters, double *relres, bool mixed) {
   if (m->diagonal_only)
     return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pcg on a lumped (diagonal) matrix");
   switch (m->pat->pdim) {
-    case 1: return pcg_segments<1>(ctx, m, d_b, d_x, d_fixed, nseg, seg_off, precond, reltol, maxiter, iters, relres);
-    case 2: return pcg_segments<2>(ctx, m, d_b, d_x, d_fixed, nseg, seg_off, precond, reltol, maxiter, iters, relres);
-    case 3: return pcg_segments<3>(ctx, m, d_b, d_x, d_fixed, nseg, seg_off, precond, reltol, maxiter, iters, relres);
+    case 1: return pcg_segments<1>(ctx, m, d_b, d_x, d_fixed, nseg, seg_off, precond, reltol, maxiter, iters, relres, mixed);
+    case 2: return pcg_segments<2>(ctx, m, d_b, d_x, d_fixed, nseg, seg_off, precond, reltol, maxiter, iters, relres, mixed);
+    case 3: return pcg_segments<3>(ctx, m, d_b, d_x, d_fixed, nseg, seg_off, precond, reltol, maxiter, iters, relres, mixed);
   }
   return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
 }
