@@ -72,6 +72,7 @@ def parse():
     ap.add_argument("--no-samples", action="store_true",
                     help="assembly line: skip the short batched and serving samples")
     ap.add_argument("--no-plain", action="store_true", help="batched: skip the one-at-a-time plain arm")
+    ap.add_argument("--profile", action="store_true", help="batched: add a traced pass's kernel time breakdown")
     ap.add_argument("--precond", default=None, choices=["jacobi", "bjacobi", "ic0", "auto"],
                     help="CG preconditioner (defaults: ic0 for batched, bjacobi for tl, auto for serving: "
                          "Jacobi for its scalar heat requests)")
@@ -277,12 +278,17 @@ NNZ_PER_DOF_TET10 = 83   # structural entries per DoF of the tet10 boxes (the 16
 
 
 def batched_groups(inst, budget_nnz):
-    """Instances in order, grouped so that each group's structural entries
-    (estimated from its DoFs) stay within budget_nnz: the batch is admitted
-    to HBM a group at a time (about 60 device bytes per entry: values, the
-    stored CSC, the FP32 copy, the IC(0) factor)."""
+    """Instances grouped so that each group's structural entries (estimated
+    from its DoFs) stay within budget_nnz: the batch is admitted to HBM a
+    group at a time (about 60 device bytes per entry: values, the stored
+    CSC, the IC(0) factor).  Instances are taken by size, so a group holds
+    instances of similar size, which need similar CG iteration counts: a
+    group's CG runs until its slowest system converges, and systems that
+    converged early only idle through the tail."""
     groups, cur, acc = [], [], 0
-    for k, (m, _, _) in enumerate(inst):
+    order = sorted(range(len(inst)), key=lambda k: inst[k][0].non)
+    for k in order:
+        m = inst[k][0]
         est = NNZ_PER_DOF_TET10 * 3 * m.non
         if cur and acc + est > budget_nnz:
             groups.append(cur)
@@ -344,6 +350,17 @@ def run_batched(args, llf):
         if rep >= args.warmup:
             times.append(time.perf_counter() - t0)
     t = statistics.median(times)
+    kernels_ms = None
+    if args.profile:
+        # one more pass with the library's per-launch event tracing (graph
+        # replay off while tracing): the kernel time breakdown of a pass
+        ctx = built[0][1]._ctx
+        ctx.profile_reset()
+        ctx.profile(True)
+        one_pass()
+        torch.cuda.synchronize()
+        ctx.profile(False)
+        kernels_ms = {k: round(v["ms"], 3) for k, v in sorted(ctx.profile_report().items(), key=lambda kv: -kv[1]["ms"])}
     its = np.concatenate([u.iterations for u, _ in res])
     # accuracy against the FP64-assembled matrix of each checked instance (the
     # plain form's matrix, bit-identical to the oracle's): a direct solve for
@@ -418,7 +435,7 @@ def run_batched(args, llf):
                        "reltol": reltol, "assembly": form, "solve": args.batched_solve},
             "cg_iterations": {"min": int(its.min()), "median": float(np.median(its)), "max": int(its.max())},
             "rel_err_vs_direct": errs, "max_rel_err_vs_direct": max(e["rel_err"] for e in errs),
-            "plain_gpu": plain}
+            "plain_gpu": plain, "kernels_ms_traced_pass": kernels_ms}
 
 
 def run_serving(args, llf):
