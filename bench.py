@@ -66,7 +66,10 @@ def parse():
                     help="batched: structural entries admitted to the GPU at a time")
     ap.add_argument("--requests", type=int, default=200, help="serving: requests of the Poisson stream")
     ap.add_argument("--workers", type=int, default=8,
-                    help="serving: server workers (200 requests: 4 -> 40.6, 8 -> 43.0, 16 -> 34.0 solves/s)")
+                    help="serving: preparation threads (engine) or solver workers (pool)")
+    ap.add_argument("--server", default="engine", choices=["engine", "pool"],
+                    help="serving: continuous-batching engine or the worker pool")
+    ap.add_argument("--max-systems", type=int, default=256, help="serving: engine slots")
     ap.add_argument("--no-peak", action="store_true", help="skip the DGEMM FP64 reference rate")
     ap.add_argument("--no-other-form", action="store_true", help="skip the second arithmetic form")
     ap.add_argument("--no-samples", action="store_true",
@@ -476,7 +479,8 @@ def run_serving(args, llf):
         one.wait(submit(one, r))
     t_single = time.perf_counter() - t0
     one.close()
-    srv = llf._lib.Server(workers=args.workers, budget_bytes=120 << 30)
+    srv = llf._lib.Server(workers=args.workers, budget_bytes=120 << 30, batched=args.server == "engine",
+                          max_systems=args.max_systems)
     for t in [submit(srv, r) for r in warm]:   # every worker has created its context
         srv.wait(t)
     tickets = [None] * len(reqs)
@@ -509,6 +513,7 @@ def run_serving(args, llf):
             "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic heat requests (seeded)",
             "config": {"workload": f"serving-heat-{len(reqs)}", "requests": len(reqs), "workers": args.workers,
+                       "server": args.server, "max_systems": args.max_systems,
                        "dofs_median": float(np.median(dofs)), "dofs_max": int(max(dofs)), "reltol": 1e-10,
                        "precond": args.precond or "auto"},
             "latency_s": {"p50": _pct(lat, 50), "p99": _pct(lat, 99), "max": max(lat)},
@@ -826,7 +831,8 @@ def main():
         except Exception as ex:
             samples["batched"] = {"error": str(ex)}
         try:
-            sargs = _ap.Namespace(**{**vars(args), "requests": 100, "precond": None})
+            sargs = _ap.Namespace(**{**vars(args), "requests": 100, "precond": None, "server": "engine",
+                                     "max_systems": 256})
             r = run_serving(sargs, llf)
             samples["serving"] = {k: r[k] for k in ("value", "unit", "config", "latency_s",
                                                     "one_at_a_time_solves_per_s", "cg_iterations_median") if k in r}

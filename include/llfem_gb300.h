@@ -540,6 +540,22 @@ typedef struct llf_server llf_server;
 int llf_server_create(int device, int nworkers, int64_t mem_budget_bytes,
                       llf_server **out);
 
+/* The continuous-batching form of the same server.  nprep preparation
+ * threads (each with its own context) take requests in arrival order as the
+ * memory budget allows, upload the mesh, build the pattern, assemble K and
+ * run the first CG steps.  One engine thread then runs the CG iterations of
+ * every prepared request together: the requests occupy slots (at most
+ * max_systems) of a device-resident table, and one captured CUDA graph of 16
+ * iterations is replayed over the table; between replays converged requests
+ * are retired (result to the host, memory released) and newly prepared ones
+ * admitted, so requests that arrive while others iterate join the next
+ * replay.  Preconditioners: none, Jacobi, block Jacobi (IC(0) is refused per
+ * request).  Each result equals that of a lone llf_pcg solve of the request
+ * bit for bit.  Submission, waiting, statistics and destruction are the
+ * calls below. */
+int llf_server_create_batched(int device, int nprep, int max_systems,
+                              int64_t mem_budget_bytes, llf_server **out);
+
 /* Copy one request into the server; *ticket identifies it. x0[non] holds the
  * prescribed temperatures on fixed[non] != 0 (other entries ignored); rhs
  * (may be NULL = 0) the nodal heat loads.  maxiter <= 0 means 20*non. */

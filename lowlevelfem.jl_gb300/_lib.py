@@ -100,6 +100,7 @@ SIGNATURES = {
     "llf_pcg_mixed": (i32, [vp, vp, P_dbl, P_dbl, P_u8, i32, P_i64, i32, dbl, i64, P_i64, P_dbl]),
     "llf_pcg_noalloc": (i32, [vp, vp, vp, vp, vp, i32, dbl, i64, P_i64, P_dbl]),
     "llf_server_create": (i32, [i32, i32, i64, PP]),
+    "llf_server_create_batched": (i32, [i32, i32, i32, i64, PP]),
     "llf_server_submit_heat": (i32, [vp, i32, i64, P_dbl, i64, i32, P_i64, i32, i32, dbl, dbl, P_dbl, P_dbl, P_u8,
                                      i32, dbl, i64, P_i64]),
     "llf_server_wait": (i32, [vp, i64, dbl, P_dbl, P_i64, P_dbl, P_dbl, P_dbl, C.c_char_p, i64]),
@@ -226,9 +227,16 @@ class Server:
     """Request server of the library (llf_server): worker threads with their
     own streams, admission by device-memory budget."""
 
-    def __init__(self, device: int = 0, workers: int = 4, budget_bytes: int = 64 << 30):
+    def __init__(self, device: int = 0, workers: int = 4, budget_bytes: int = 64 << 30, batched: bool = False,
+                 max_systems: int = 256):
+        """batched=True: continuous batching (llf_server_create_batched), with
+        `workers` preparation threads and one engine iterating every prepared
+        request in shared launches; otherwise a pool of `workers` solvers."""
         h = C.c_void_p()
-        rc = lib().llf_server_create(device, workers, int(budget_bytes), C.byref(h))
+        if batched:
+            rc = lib().llf_server_create_batched(device, workers, int(max_systems), int(budget_bytes), C.byref(h))
+        else:
+            rc = lib().llf_server_create(device, workers, int(budget_bytes), C.byref(h))
         if rc != LLF_OK:
             raise LLFError(rc, "llf_server_create failed")
         self.h = h

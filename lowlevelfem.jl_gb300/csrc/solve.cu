@@ -28,6 +28,7 @@
 // Iterations after a segment converged are no-ops for that segment, so every
 // segment stops exactly where IterativeSolvers would.
 #include "common.cuh"
+#include "engine.h"
 
 #include <algorithm>
 #include <cmath>
@@ -1909,3 +1910,534 @@ int heat_fdm_impl(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C, const 
   }
   return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
 }
+
+// ---------------------------------------------------------------- engine
+// Device-resident continuous batching (engine.h): the CG iterations of many
+// independent systems, each with its own matrix and vectors, in the same
+// launches.  A slot describes one admitted system; the chunk table lists the
+// chunks of all admitted systems, each system's chunks contiguous and in its
+// own DoF order.  The kernels loop over the table (its length is read from
+// device memory), so one captured graph serves whatever is admitted.
+#include "engine.h"
+
+namespace {
+
+struct EngSlot {
+  const double *nz;
+  const int64_t *nptr;
+  const int32_t *nadj;
+  const uint8_t *fixed;
+  const int16_t *perm;
+  const double *pinv;
+  double *xw, *r, *z, *u, *c;
+  int mode, pad;
+};
+
+struct EngTab {
+  const EngSlot *slot;
+  SegState *st;
+  int *arrive;                 // 2 per slot: product, update
+  const int32_t *cslot;        // per chunk: slot
+  const int64_t *cbeg, *cend;  // per chunk: DoF range within its system
+  const int64_t *sfirst;       // per slot: first chunk in the table
+  const int64_t *snch;         // per slot: chunk count
+  const int64_t *nchunks;      // chunks in the table (device)
+  double *part, *part2, *part3;
+};
+
+__device__ __forceinline__ double eng_total(const EngTab &T, int sl, const double *part) {
+  double v = 0.0;
+  const int64_t f = T.sfirst[sl], n = T.snch[sl];
+  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) v = __dadd_rn(v, __ldcg(part + f + k));
+  return block_sum(v);
+}
+
+// u = z + beta u (k_seg_dir on a slot's vectors).
+__global__ void __launch_bounds__(CG_THREADS) k_eng_dir(EngTab T) {
+  const int64_t nch = *T.nchunks;
+  for (int64_t ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+    const int sl = T.cslot[ch];
+    const SegState &q = T.st[sl];
+    if (q.done) continue;
+    const EngSlot &S = T.slot[sl];
+    const double beta = q.rho / q.rho_prev;
+    const int64_t b = T.cbeg[ch], e = T.cend[ch];
+#pragma unroll
+    for (int k = 0; k < CHUNK_PER_THREAD; ++k) {
+      const int64_t i = b + threadIdx.x + (int64_t)k * CG_THREADS;
+      if (i < e) S.u[i] = __fma_rn(beta, S.u[i], S.z[i]);
+    }
+  }
+}
+
+// c = A u and alpha (k_seg_spmv on a slot's matrix and vectors).
+template <int P>
+__global__ void __launch_bounds__(CG_THREADS) k_eng_spmv(EngTab T) {
+  constexpr int NPW = 32 / SPMV_G;
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, w = threadIdx.x >> 5, g = lane % SPMV_G;
+  const int64_t nch = *T.nchunks;
+  for (int64_t ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+    const int sl = T.cslot[ch];
+    if (T.st[sl].done) continue;
+    const EngSlot &S = T.slot[sl];
+    double dot = 0.0;
+    const int64_t b0 = T.cbeg[ch] / P;
+    const int nb = (int)(T.cend[ch] / P - b0);
+    const int step = wpb * NPW;
+    auto node_of = [&](int r) -> int64_t { return b0 + (r < nb ? (int)S.perm[b0 + r] : 0); };
+    int r = w * NPW + lane / SPMV_G;
+    int64_t B = node_of(r);
+    int64_t q0 = r < nb ? S.nptr[B] : 0, q1 = r < nb ? S.nptr[B + 1] : 0;
+    for (int r0 = w * NPW; r0 < nb; r0 += step, r += step) {
+      const bool valid = r < nb;
+      const int64_t Bn = node_of(r + step);
+      const bool vn = r + step < nb;
+      const int64_t q0n = vn ? S.nptr[Bn] : 0, q1n = vn ? S.nptr[Bn + 1] : 0;
+      double acc[P];
+      node_columns_at<P>(S.nz, S.nadj, S.u, q0, q1, valid, g, acc);
+      if (valid && g == 0) {
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+          const int64_t d = P * B + j;
+          const double v = S.fixed[d] ? 0.0 : acc[j];
+          S.c[d] = v;
+          dot = __fma_rn(S.u[d], v, dot);
+        }
+      }
+      B = Bn;
+      q0 = q0n;
+      q1 = q1n;
+    }
+    const double s = block_sum(dot);
+    if (threadIdx.x == 0) T.part3[ch] = s;
+    if (arrive_last(T.arrive + 2 * sl, T.snch[sl])) {
+      const double uc = eng_total(T, sl, T.part3);
+      if (threadIdx.x == 0) {
+        SegState &q = T.st[sl];
+        if (!(uc > 0.0) || !isfinite(uc)) {
+          q.breakdown = 1;
+          q.done = 1;
+          q.alpha = 0.0;
+        } else {
+          q.alpha = q.rho / uc;
+        }
+      }
+    }
+  }
+}
+
+// x += alpha u, r -= alpha c, the residual check, the next z and rho
+// (k_seg_update_fused with a local preconditioner on a slot's vectors).
+template <int P>
+__global__ void __launch_bounds__(CG_THREADS) k_eng_update(EngTab T) {
+  const int64_t nch = *T.nchunks;
+  for (int64_t ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+    const int sl = T.cslot[ch];
+    const SegState &q = T.st[sl];
+    if (q.done) continue;
+    const EngSlot &S = T.slot[sl];
+    const double alpha = q.alpha;
+    double rr = 0.0, zr = 0.0;
+    const int64_t b = T.cbeg[ch], e = T.cend[ch];
+#pragma unroll
+    for (int k = 0; k < CHUNK_PER_THREAD; ++k) {
+      const int64_t i = b + threadIdx.x + (int64_t)k * CG_THREADS;
+      if (i < e) {
+        S.xw[i] = __fma_rn(alpha, S.u[i], S.xw[i]);
+        const double ri = __fma_rn(-alpha, S.c[i], S.r[i]);
+        S.r[i] = ri;
+        rr = __fma_rn(ri, ri, rr);
+      }
+    }
+    __syncthreads();
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+      const double zi = S.fixed[i] ? 0.0 : apply_prec<P>(S.pinv, S.mode, S.r, i);
+      S.z[i] = zi;
+      zr = __fma_rn(zi, S.r[i], zr);
+    }
+    const double s1 = block_sum(rr);
+    const double s2 = block_sum(zr);
+    if (threadIdx.x == 0) {
+      T.part[ch] = s1;
+      T.part2[ch] = s2;
+    }
+    if (arrive_last(T.arrive + 2 * sl + 1, T.snch[sl])) {
+      const double trr = eng_total(T, sl, T.part);
+      const double tzr = eng_total(T, sl, T.part2);
+      if (threadIdx.x == 0) {
+        SegState &w = T.st[sl];
+        w.res = sqrt(trr);
+        w.rho_prev = w.rho;
+        w.it += 1;
+        if (w.res <= w.tol || w.it >= w.maxiter) w.done = 1;
+        else w.rho = tzr;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+namespace llf_engine {
+
+struct System {
+  const llf_matrix *K = nullptr;
+  int P = 1, precond = 0;
+  int64_t ndof = 0, nch = 0;
+  double *b = nullptr, *x = nullptr, *xw = nullptr, *r = nullptr, *z = nullptr, *u = nullptr, *c = nullptr;
+  double *pinv = nullptr;
+  uint8_t *fixed = nullptr;
+  int16_t *perm = nullptr;
+  SegState st{};
+};
+
+struct Engine {
+  llf_ctx *ctx = nullptr;
+  int max_systems = 0;
+  int64_t max_chunks = 0;
+  std::vector<System *> sys;      // per slot (nullptr: free)
+  std::vector<int64_t> tag;
+  EngSlot *d_slot = nullptr;
+  SegState *d_st = nullptr;
+  int *d_arrive = nullptr;
+  int32_t *d_cslot = nullptr;
+  int64_t *d_cbeg = nullptr, *d_cend = nullptr, *d_sfirst = nullptr, *d_snch = nullptr, *d_nch = nullptr;
+  double *d_part = nullptr, *d_part2 = nullptr, *d_part3 = nullptr;
+  std::vector<SegState> hst;
+  cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};  // per P
+  long long launches_per_graph = 0;
+  bool table_dirty = true;
+};
+
+namespace {
+
+template <int P>
+int prepare_t(llf_ctx *ctx, const llf_matrix *K, const double *hb, const double *hx0, const uint8_t *hfixed,
+              int precond, double reltol, int64_t maxiter, System *sy) {
+  const llf_pattern *pat = K->pat;
+  const int64_t n = pat->ndof, non = pat->mesh->non;
+  cudaStream_t s = ctx->stream;
+  sy->P = P;
+  sy->precond = precond;
+  sy->ndof = n;
+  const int64_t nch = (n + CHUNK - 1) / CHUNK;
+  sy->nch = nch;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &sy->b, n));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &sy->x, n));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &sy->xw, n));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &sy->r, n));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &sy->z, n));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &sy->u, n));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &sy->c, n));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &sy->pinv, precond == LLF_PRECOND_BJACOBI ? n * P : n));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &sy->fixed, n));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &sy->perm, non));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(sy->b, hb, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(sy->x, hx0, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(sy->fixed, hfixed, n, cudaMemcpyHostToDevice, s));
+  // the first steps of pcg_core on a one-system chunking (the same chunks,
+  // kernels and node order as llf_pcg)
+  std::vector<int64_t> cb(nch), ce(nch), sf{0, nch};
+  std::vector<int32_t> cs(nch, 0);
+  for (int64_t k = 0; k < nch; ++k) {
+    cb[k] = k * CHUNK;
+    ce[k] = std::min<int64_t>((k + 1) * CHUNK, n);
+  }
+  int64_t *d_cb = nullptr, *d_ce = nullptr, *d_sf = nullptr;
+  int32_t *d_cs = nullptr;
+  int *d_active = nullptr, *d_arrive = nullptr;
+  SegState *d_st = nullptr;
+  double *part = nullptr;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_cb, nch));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_ce, nch));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_cs, nch));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_sf, 2));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_active, 1));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_arrive, 3));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &d_st, 1));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &part, nch));
+  if (nch) {
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_cb, cb.data(), sizeof(int64_t) * nch, cudaMemcpyHostToDevice, s));
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_ce, ce.data(), sizeof(int64_t) * nch, cudaMemcpyHostToDevice, s));
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_cs, cs.data(), sizeof(int32_t) * nch, cudaMemcpyHostToDevice, s));
+  }
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_sf, sf.data(), sizeof(int64_t) * 2, cudaMemcpyHostToDevice, s));
+  LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_active, 0, sizeof(int), s));
+  LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_arrive, 0, sizeof(int) * 3, s));
+  Seg S{d_cb, d_ce, d_cs, d_sf, nch, 1, d_st, d_active, d_arrive, sy->perm};
+  const unsigned gch = (unsigned)std::max<int64_t>(1, std::min<int64_t>(nch, (int64_t)ctx->num_sms * 8));
+  const unsigned gv = (unsigned)(ctx->num_sms * 4);
+  if (nch) {
+    KernelScope k(ctx, "k_chunk_perm");
+    k_chunk_perm<<<chunk_grid(S), CG_THREADS, 0, s>>>(S, pat->d_nptr, P, sy->perm);
+  }
+  { KernelScope k(ctx, "k_precond_setup");
+    k_precond_setup<P><<<(unsigned)((non + 127) / 128), 128, 0, s>>>(K->d_nz, pat->d_colptr, pat->d_diagpos, sy->fixed,
+                                                                     non, precond, sy->pinv); }
+  { KernelScope k(ctx, "k_keep_fixed"); k_keep_fixed<<<gv, CG_THREADS, 0, s>>>(sy->x, sy->fixed, sy->xw, n); }
+  { KernelScope k(ctx, "k_spmv");
+    k_spmv<P><<<gv, CG_THREADS, 0, s>>>(K->d_nz, pat->d_colptr, pat->d_nptr, pat->d_nadj, sy->xw, sy->c, n); }
+  { KernelScope k(ctx, "k_seg_init"); k_seg_init<<<gch, CG_THREADS, 0, s>>>(S, sy->b, sy->c, sy->fixed, sy->r, sy->xw, sy->u, part); }
+  { KernelScope k(ctx, "k_seg_start"); k_seg_start<<<1, CG_THREADS, 0, s>>>(S, part, reltol, (long long)maxiter); }
+  { KernelScope k(ctx, "k_seg_prec"); k_seg_prec<P><<<gch, CG_THREADS, 0, s>>>(S, sy->pinv, precond, sy->r, sy->fixed, sy->z, part); }
+  { KernelScope k(ctx, "k_seg_rho"); k_seg_rho<<<1, CG_THREADS, 0, s>>>(S, part); }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&sy->st, d_st, sizeof(SegState), cudaMemcpyDeviceToHost, s));
+  LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  dfree(ctx, d_cb); dfree(ctx, d_ce); dfree(ctx, d_cs); dfree(ctx, d_sf); dfree(ctx, d_active);
+  dfree(ctx, d_arrive); dfree(ctx, d_st); dfree(ctx, part);
+  return LLF_OK;
+}
+
+template <int P>
+void enqueue_engine_iteration(Engine *e, const EngTab &T) {
+  cudaStream_t s = e->ctx->stream;
+  const unsigned grid = (unsigned)(e->ctx->num_sms * 8);
+  { KernelScope k(e->ctx, "k_eng_dir"); k_eng_dir<<<grid, CG_THREADS, 0, s>>>(T); }
+  { KernelScope k(e->ctx, "k_eng_spmv"); k_eng_spmv<P><<<grid, CG_THREADS, 0, s>>>(T); }
+  { KernelScope k(e->ctx, "k_eng_update"); k_eng_update<P><<<grid, CG_THREADS, 0, s>>>(T); }
+}
+
+EngTab tab_of(Engine *e) {
+  return EngTab{e->d_slot, e->d_st, e->d_arrive, e->d_cslot, e->d_cbeg, e->d_cend, e->d_sfirst, e->d_snch,
+                e->d_nch, e->d_part, e->d_part2, e->d_part3};
+}
+
+// Chunk table of the admitted systems (slot order), uploaded on the stream.
+int upload_table(Engine *e) {
+  llf_ctx *ctx = e->ctx;
+  std::vector<int32_t> cslot;
+  std::vector<int64_t> cbeg, cend, sfirst(e->max_systems, 0), snch(e->max_systems, 0);
+  for (int sl = 0; sl < e->max_systems; ++sl) {
+    System *sy = e->sys[sl];
+    if (!sy) continue;
+    sfirst[sl] = (int64_t)cslot.size();
+    snch[sl] = sy->nch;
+    for (int64_t k = 0; k < sy->nch; ++k) {
+      cslot.push_back(sl);
+      cbeg.push_back(k * CHUNK);
+      cend.push_back(std::min<int64_t>((k + 1) * CHUNK, sy->ndof));
+    }
+  }
+  const int64_t nch = (int64_t)cslot.size();
+  cudaStream_t s = ctx->stream;
+  if (nch) {
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(e->d_cslot, cslot.data(), sizeof(int32_t) * nch, cudaMemcpyHostToDevice, s));
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(e->d_cbeg, cbeg.data(), sizeof(int64_t) * nch, cudaMemcpyHostToDevice, s));
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(e->d_cend, cend.data(), sizeof(int64_t) * nch, cudaMemcpyHostToDevice, s));
+  }
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(e->d_sfirst, sfirst.data(), sizeof(int64_t) * e->max_systems,
+                                    cudaMemcpyHostToDevice, s));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(e->d_snch, snch.data(), sizeof(int64_t) * e->max_systems, cudaMemcpyHostToDevice, s));
+  // the host vectors must outlive the copies
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(e->d_nch, &nch, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  e->table_dirty = false;
+  return LLF_OK;
+}
+
+int64_t chunks_in_use(const Engine *e) {
+  int64_t n = 0;
+  for (System *sy : e->sys)
+    if (sy) n += sy->nch;
+  return n;
+}
+
+}  // namespace
+
+int prepare(llf_ctx *ctx, const llf_matrix *K, const double *b, const double *x0, const uint8_t *fixed,
+            int precond, double reltol, int64_t maxiter, System **out) {
+  if (!ctx || !K || !b || !x0 || !fixed || !out) return LLF_ERR_ARG;
+  if (K->diagonal_only) return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "engine: lumped (diagonal) matrix");
+  if (precond < LLF_PRECOND_NONE || precond > LLF_PRECOND_BJACOBI)
+    return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "engine: preconditioner must be none, Jacobi or block Jacobi");
+  auto *sy = new System();
+  sy->K = K;
+  int rc = LLF_ERR_UNSUPPORTED;
+  switch (K->pat->pdim) {
+    case 1: rc = prepare_t<1>(ctx, K, b, x0, fixed, precond, reltol, maxiter, sy); break;
+    case 2: rc = prepare_t<2>(ctx, K, b, x0, fixed, precond, reltol, maxiter, sy); break;
+    case 3: rc = prepare_t<3>(ctx, K, b, x0, fixed, precond, reltol, maxiter, sy); break;
+  }
+  if (rc != LLF_OK) {
+    release(ctx, sy);
+    return rc;
+  }
+  *out = sy;
+  return LLF_OK;
+}
+
+void release(llf_ctx *ctx, System *sy) {
+  if (!sy) return;
+  dfree(ctx, sy->b); dfree(ctx, sy->x); dfree(ctx, sy->xw); dfree(ctx, sy->r); dfree(ctx, sy->z);
+  dfree(ctx, sy->u); dfree(ctx, sy->c); dfree(ctx, sy->pinv); dfree(ctx, sy->fixed); dfree(ctx, sy->perm);
+  delete sy;
+}
+
+int create(llf_ctx *ctx, int max_systems, int64_t max_chunks, Engine **out) {
+  if (!ctx || !out || max_systems < 1 || max_chunks < 1) return LLF_ERR_ARG;
+  auto *e = new Engine();
+  e->ctx = ctx;
+  e->max_systems = max_systems;
+  e->max_chunks = max_chunks;
+  e->sys.assign(max_systems, nullptr);
+  e->tag.assign(max_systems, 0);
+  e->hst.assign(max_systems, SegState{});
+  cudaStream_t s = ctx->stream;
+  auto fail = [&](cudaError_t err) {
+    destroy(e);
+    return llf_fail(ctx, LLF_ERR_CUDA, std::string("engine: ") + cudaGetErrorString(err));
+  };
+  cudaError_t err = dalloc(ctx, &e->d_slot, max_systems);
+  if (err == cudaSuccess) err = dalloc(ctx, &e->d_st, max_systems);
+  if (err == cudaSuccess) err = dalloc(ctx, &e->d_arrive, 2 * (int64_t)max_systems);
+  if (err == cudaSuccess) err = dalloc(ctx, &e->d_cslot, max_chunks);
+  if (err == cudaSuccess) err = dalloc(ctx, &e->d_cbeg, max_chunks);
+  if (err == cudaSuccess) err = dalloc(ctx, &e->d_cend, max_chunks);
+  if (err == cudaSuccess) err = dalloc(ctx, &e->d_sfirst, max_systems);
+  if (err == cudaSuccess) err = dalloc(ctx, &e->d_snch, max_systems);
+  if (err == cudaSuccess) err = dalloc(ctx, &e->d_nch, 1);
+  if (err == cudaSuccess) err = dalloc(ctx, &e->d_part, max_chunks);
+  if (err == cudaSuccess) err = dalloc(ctx, &e->d_part2, max_chunks);
+  if (err == cudaSuccess) err = dalloc(ctx, &e->d_part3, max_chunks);
+  if (err == cudaSuccess) err = cudaMemsetAsync(e->d_arrive, 0, sizeof(int) * 2 * max_systems, s);
+  if (err == cudaSuccess) err = cudaMemsetAsync(e->d_st, 0, sizeof(SegState) * max_systems, s);
+  if (err == cudaSuccess) err = cudaMemsetAsync(e->d_slot, 0, sizeof(EngSlot) * max_systems, s);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+  if (err != cudaSuccess) return fail(err);
+  int rc = upload_table(e);
+  if (rc != LLF_OK) {
+    destroy(e);
+    return rc;
+  }
+  *out = e;
+  return LLF_OK;
+}
+
+void destroy(Engine *e) {
+  if (!e) return;
+  llf_ctx *ctx = e->ctx;
+  for (int sl = 0; sl < e->max_systems; ++sl)
+    if (e->sys[sl]) release(ctx, e->sys[sl]);
+  for (auto &x : e->exec)
+    if (x) cudaGraphExecDestroy(x);
+  dfree(ctx, e->d_slot); dfree(ctx, e->d_st); dfree(ctx, e->d_arrive); dfree(ctx, e->d_cslot);
+  dfree(ctx, e->d_cbeg); dfree(ctx, e->d_cend); dfree(ctx, e->d_sfirst); dfree(ctx, e->d_snch);
+  dfree(ctx, e->d_nch); dfree(ctx, e->d_part); dfree(ctx, e->d_part2); dfree(ctx, e->d_part3);
+  cudaStreamSynchronize(ctx->stream);
+  delete e;
+}
+
+int admitted(const Engine *e) {
+  int n = 0;
+  for (System *sy : e->sys) n += sy != nullptr;
+  return n;
+}
+
+int admit(Engine *e, System *sy, int64_t tag) {
+  llf_ctx *ctx = e->ctx;
+  if (!sy) return llf_fail(ctx, LLF_ERR_ARG, "engine: null system");
+  for (int sl = 0; sl < e->max_systems; ++sl)
+    if (e->sys[sl] && e->sys[sl]->P != sy->P)
+      return llf_fail(ctx, LLF_ERR_STATE, "engine: all admitted systems must have the same DoFs per node");
+  if (chunks_in_use(e) + sy->nch > e->max_chunks) return 0;
+  int sl = -1;
+  for (int k = 0; k < e->max_systems; ++k)
+    if (!e->sys[k]) { sl = k; break; }
+  if (sl < 0) return 0;
+  const llf_pattern *pat = sy->K->pat;
+  EngSlot d{sy->K->d_nz, pat->d_nptr, pat->d_nadj, sy->fixed, sy->perm, sy->pinv,
+            sy->xw, sy->r, sy->z, sy->u, sy->c, sy->precond, 0};
+  cudaStream_t s = ctx->stream;
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(e->d_slot + sl, &d, sizeof(EngSlot), cudaMemcpyHostToDevice, s));
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(e->d_st + sl, &sy->st, sizeof(SegState), cudaMemcpyHostToDevice, s));
+  LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  e->sys[sl] = sy;
+  e->tag[sl] = tag;
+  e->hst[sl] = sy->st;
+  e->table_dirty = true;
+  return 1;
+}
+
+int step(Engine *e) {
+  llf_ctx *ctx = e->ctx;
+  if (e->table_dirty) {
+    int rc = upload_table(e);
+    if (rc != LLF_OK) return rc;
+  }
+  int P = 0;
+  for (System *sy : e->sys)
+    if (sy) { P = sy->P; break; }
+  if (!P) return LLF_OK;
+  cudaStream_t s = ctx->stream;
+  const EngTab T = tab_of(e);
+  const int per_graph = 16;
+  auto enqueue = [&]() {
+    for (int k = 0; k < per_graph; ++k) {
+      if (P == 1) enqueue_engine_iteration<1>(e, T);
+      else if (P == 2) enqueue_engine_iteration<2>(e, T);
+      else enqueue_engine_iteration<3>(e, T);
+    }
+  };
+  cudaGraphExec_t &exec = e->exec[P - 1];
+  if (!exec && !ctx->profiling) {
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const long long saved = ctx->launches;
+      enqueue();
+      e->launches_per_graph = ctx->launches - saved;
+      ctx->launches = saved;
+      if (cudaStreamEndCapture(s, &graph) != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+        exec = nullptr;
+      if (graph) cudaGraphDestroy(graph);
+    }
+    cudaGetLastError();
+  }
+  if (exec && !ctx->profiling) {
+    LLF_CUDA_TRY(ctx, cudaGraphLaunch(exec, s));
+    ctx->launches += e->launches_per_graph;
+  } else {
+    enqueue();
+  }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(e->hst.data(), e->d_st, sizeof(SegState) * e->max_systems,
+                                    cudaMemcpyDeviceToHost, s));
+  LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  return LLF_OK;
+}
+
+int collect(Engine *e, std::vector<Done> &out) {
+  llf_ctx *ctx = e->ctx;
+  cudaStream_t s = ctx->stream;
+  const unsigned gv = (unsigned)(ctx->num_sms * 4);
+  std::vector<int> fin;
+  for (int sl = 0; sl < e->max_systems; ++sl)
+    if (e->sys[sl] && e->hst[sl].done) fin.push_back(sl);
+  if (fin.empty()) return LLF_OK;
+  const size_t base = out.size();
+  for (int sl : fin) {
+    System *sy = e->sys[sl];
+    Done d;
+    d.tag = e->tag[sl];
+    d.x.resize(sy->ndof);
+    { KernelScope k(ctx, "k_cg_merge"); k_cg_merge<<<gv, CG_THREADS, 0, s>>>(sy->xw, sy->fixed, sy->x, sy->ndof); }
+    LLF_CUDA_TRY(ctx, cudaGetLastError());
+    LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d.x.data(), sy->x, sizeof(double) * sy->ndof, cudaMemcpyDeviceToHost, s));
+    out.push_back(std::move(d));
+  }
+  LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  for (size_t k = 0; k < fin.size(); ++k) {
+    const int sl = fin[k];
+    const SegState &q = e->hst[sl];
+    Done &d = out[base + k];
+    d.iters = q.it;
+    d.relres = q.res0 > 0 ? q.res / q.res0 : 0.0;
+    d.status = q.breakdown ? LLF_ERR_NUMERIC : (q.res <= q.tol ? LLF_OK : LLF_ERR_NOT_CONVERGED);
+    release(ctx, e->sys[sl]);
+    e->sys[sl] = nullptr;
+    e->table_dirty = true;
+  }
+  return LLF_OK;
+}
+
+}  // namespace llf_engine
