@@ -506,6 +506,7 @@ def run_serving(args, llf):
         done_at = max(done_at, time.perf_counter())
     th.join()
     stats = srv.stats()
+    timing = srv.timing()
     srv.close()
     span = done_at - start
     dofs = [m.non for m, _, _, _ in reqs]
@@ -518,7 +519,8 @@ def run_serving(args, llf):
                        "precond": args.precond or "auto"},
             "latency_s": {"p50": _pct(lat, 50), "p99": _pct(lat, 99), "max": max(lat)},
             "one_at_a_time_solves_per_s": len(reqs) / t_single,
-            "cg_iterations_median": float(np.median(iters)), "peak_device_bytes": stats["peak_bytes"]}
+            "cg_iterations_median": float(np.median(iters)), "peak_device_bytes": stats["peak_bytes"],
+            "server_timing": timing}
 
 
 def run_tl(args, llf):

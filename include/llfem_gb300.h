@@ -579,6 +579,13 @@ int llf_server_wait(llf_server *s, int64_t ticket, double timeout_s, double *x,
 int llf_server_stats(llf_server *s, int64_t *queued, int64_t *served,
                      int64_t *bytes_in_use, int64_t *peak_bytes);
 
+/* Where a continuous-batching server's time went (no reference
+ * counterpart; a diagnostic): seconds summed over the preparation threads,
+ * the engine's replays, its retirements and its idle waits, the replay
+ * count and the mean number of requests admitted per replay. */
+int llf_server_timing(llf_server *s, double *prep_s, double *step_s, double *collect_s,
+                      double *idle_s, int64_t *replays, double *mean_admitted);
+
 /* Drains the queue, joins the workers and frees the server. */
 int llf_server_destroy(llf_server *s);
 

@@ -101,6 +101,7 @@ SIGNATURES = {
     "llf_pcg_noalloc": (i32, [vp, vp, vp, vp, vp, i32, dbl, i64, P_i64, P_dbl]),
     "llf_server_create": (i32, [i32, i32, i64, PP]),
     "llf_server_create_batched": (i32, [i32, i32, i32, i64, PP]),
+    "llf_server_timing": (i32, [vp, P_dbl, P_dbl, P_dbl, P_dbl, P_i64, P_dbl]),
     "llf_server_submit_heat": (i32, [vp, i32, i64, P_dbl, i64, i32, P_i64, i32, i32, dbl, dbl, P_dbl, P_dbl, P_u8,
                                      i32, dbl, i64, P_i64]),
     "llf_server_wait": (i32, [vp, i64, dbl, P_dbl, P_i64, P_dbl, P_dbl, P_dbl, C.c_char_p, i64]),
@@ -272,6 +273,13 @@ class Server:
         q, s, b, p = C.c_int64(0), C.c_int64(0), C.c_int64(0), C.c_int64(0)
         lib().llf_server_stats(self.h, C.byref(q), C.byref(s), C.byref(b), C.byref(p))
         return {"queued": q.value, "served": s.value, "bytes_in_use": b.value, "peak_bytes": p.value}
+
+    def timing(self) -> dict:
+        v = [C.c_double(0) for _ in range(4)]
+        n, a = C.c_int64(0), C.c_double(0)
+        lib().llf_server_timing(self.h, *[C.byref(x) for x in v], C.byref(n), C.byref(a))
+        return {"prep_s": v[0].value, "engine_step_s": v[1].value, "engine_collect_s": v[2].value,
+                "engine_idle_s": v[3].value, "replays": n.value, "mean_admitted": a.value}
 
     def close(self):
         if getattr(self, "h", None):

@@ -96,6 +96,9 @@ struct llf_server {
   int preparing = 0;                // requests taken by preparation threads, not yet handed over
   std::deque<std::unique_ptr<Job>> ready;
   std::thread engine;
+  // where the time goes (seconds summed over threads)
+  double t_prep = 0.0, t_step = 0.0, t_collect = 0.0, t_idle = 0.0;
+  int64_t replays = 0, admitted_sum = 0;
 };
 
 namespace {
@@ -209,6 +212,7 @@ void prep_main(llf_server *s) {
     {
       std::lock_guard<std::mutex> lock(s->mu);
       s->preparing--;
+      s->t_prep += std::chrono::duration<double>(Clock::now() - job->started).count();
       s->ready.push_back(std::move(job));
     }
     s->cv_engine.notify_all();
@@ -240,6 +244,7 @@ void engine_main(llf_server *s) {
   for (;;) {
     {
       std::unique_lock<std::mutex> lock(s->mu);
+      const auto w0 = Clock::now();
       for (;;) {
         while (!s->ready.empty()) {
           pending.push_back(std::move(s->ready.front()));
@@ -249,6 +254,7 @@ void engine_main(llf_server *s) {
         if (s->stopping && s->queue.empty() && s->preparing == 0) break;
         s->cv_engine.wait(lock);
       }
+      s->t_idle += std::chrono::duration<double>(Clock::now() - w0).count();
       if (pending.empty() && inflight.empty()) break;
     }
     if (crc != LLF_OK) {
@@ -274,8 +280,18 @@ void engine_main(llf_server *s) {
     }
     if (inflight.empty()) continue;
     std::vector<llf_engine::Done> done;
+    const auto t0 = Clock::now();
+    const int nadm = llf_engine::admitted(eng);
     int rc = llf_engine::step(eng);
+    const auto t1 = Clock::now();
     if (rc == LLF_OK) rc = llf_engine::collect(eng, done);
+    {
+      std::lock_guard<std::mutex> lock(s->mu);
+      s->t_step += std::chrono::duration<double>(t1 - t0).count();
+      s->t_collect += std::chrono::duration<double>(Clock::now() - t1).count();
+      s->replays++;
+      s->admitted_sum += nadm;
+    }
     if (rc != LLF_OK) {  // a device error: fail everything in flight and start a fresh engine
       const std::string msg = llf_last_error(ctx);
       llf_engine::destroy(eng);
@@ -441,6 +457,19 @@ int llf_server_stats(llf_server *s, int64_t *queued, int64_t *served, int64_t *b
   if (served) *served = s->served;
   if (bytes_in_use) *bytes_in_use = s->in_use;
   if (peak_bytes) *peak_bytes = s->peak_in_use;
+  return LLF_OK;
+}
+
+int llf_server_timing(llf_server *s, double *prep_s, double *step_s, double *collect_s, double *idle_s,
+                      int64_t *replays, double *mean_admitted) {
+  if (!s) return LLF_ERR_ARG;
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (prep_s) *prep_s = s->t_prep;
+  if (step_s) *step_s = s->t_step;
+  if (collect_s) *collect_s = s->t_collect;
+  if (idle_s) *idle_s = s->t_idle;
+  if (replays) *replays = s->replays;
+  if (mean_admitted) *mean_admitted = s->replays ? (double)s->admitted_sum / (double)s->replays : 0.0;
   return LLF_OK;
 }
 
