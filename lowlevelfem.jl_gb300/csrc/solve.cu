@@ -1952,10 +1952,22 @@ __device__ __forceinline__ double eng_total(const EngTab &T, int sl, const doubl
   return block_sum(v);
 }
 
+// The chunks of a launch are handed out in table order from a counter (one
+// per launch, cleared at the start of every replay): the systems' chunks
+// differ in cost by more than an order of magnitude (P1 triangles to P4
+// tetrahedra), so a fixed assignment would leave blocks idle.
+__device__ __forceinline__ int64_t eng_next(unsigned *ctr) {
+  __shared__ unsigned long long s_ch;
+  __syncthreads();
+  if (threadIdx.x == 0) s_ch = atomicAdd(ctr, 1u);
+  __syncthreads();
+  return (int64_t)s_ch;
+}
+
 // u = z + beta u (k_seg_dir on a slot's vectors).
-__global__ void __launch_bounds__(CG_THREADS) k_eng_dir(EngTab T) {
+__global__ void __launch_bounds__(CG_THREADS) k_eng_dir(EngTab T, unsigned *ctr) {
   const int64_t nch = *T.nchunks;
-  for (int64_t ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+  for (int64_t ch = eng_next(ctr); ch < nch; ch = eng_next(ctr)) {
     const int sl = T.cslot[ch];
     const SegState &q = T.st[sl];
     if (q.done) continue;
@@ -1972,11 +1984,11 @@ __global__ void __launch_bounds__(CG_THREADS) k_eng_dir(EngTab T) {
 
 // c = A u and alpha (k_seg_spmv on a slot's matrix and vectors).
 template <int P>
-__global__ void __launch_bounds__(CG_THREADS) k_eng_spmv(EngTab T) {
+__global__ void __launch_bounds__(CG_THREADS) k_eng_spmv(EngTab T, unsigned *ctr) {
   constexpr int NPW = 32 / SPMV_G;
   const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, w = threadIdx.x >> 5, g = lane % SPMV_G;
   const int64_t nch = *T.nchunks;
-  for (int64_t ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+  for (int64_t ch = eng_next(ctr); ch < nch; ch = eng_next(ctr)) {
     const int sl = T.cslot[ch];
     if (T.st[sl].done) continue;
     const EngSlot &S = T.slot[sl];
@@ -2029,9 +2041,9 @@ __global__ void __launch_bounds__(CG_THREADS) k_eng_spmv(EngTab T) {
 // x += alpha u, r -= alpha c, the residual check, the next z and rho
 // (k_seg_update_fused with a local preconditioner on a slot's vectors).
 template <int P>
-__global__ void __launch_bounds__(CG_THREADS) k_eng_update(EngTab T) {
+__global__ void __launch_bounds__(CG_THREADS) k_eng_update(EngTab T, unsigned *ctr) {
   const int64_t nch = *T.nchunks;
-  for (int64_t ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+  for (int64_t ch = eng_next(ctr); ch < nch; ch = eng_next(ctr)) {
     const int sl = T.cslot[ch];
     const SegState &q = T.st[sl];
     if (q.done) continue;
@@ -2103,6 +2115,7 @@ struct Engine {
   int32_t *d_cslot = nullptr;
   int64_t *d_cbeg = nullptr, *d_cend = nullptr, *d_sfirst = nullptr, *d_snch = nullptr, *d_nch = nullptr;
   double *d_part = nullptr, *d_part2 = nullptr, *d_part3 = nullptr;
+  unsigned *d_ctr = nullptr;       // chunk counters, 3 per iteration of a replay
   std::vector<SegState> hst;
   cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};  // per P
   long long launches_per_graph = 0;
@@ -2190,12 +2203,12 @@ int prepare_t(llf_ctx *ctx, const llf_matrix *K, const double *hb, const double 
 }
 
 template <int P>
-void enqueue_engine_iteration(Engine *e, const EngTab &T) {
+void enqueue_engine_iteration(Engine *e, const EngTab &T, unsigned *ctr) {
   cudaStream_t s = e->ctx->stream;
   const unsigned grid = (unsigned)(e->ctx->num_sms * 8);
-  { KernelScope k(e->ctx, "k_eng_dir"); k_eng_dir<<<grid, CG_THREADS, 0, s>>>(T); }
-  { KernelScope k(e->ctx, "k_eng_spmv"); k_eng_spmv<P><<<grid, CG_THREADS, 0, s>>>(T); }
-  { KernelScope k(e->ctx, "k_eng_update"); k_eng_update<P><<<grid, CG_THREADS, 0, s>>>(T); }
+  { KernelScope k(e->ctx, "k_eng_dir"); k_eng_dir<<<grid, CG_THREADS, 0, s>>>(T, ctr); }
+  { KernelScope k(e->ctx, "k_eng_spmv"); k_eng_spmv<P><<<grid, CG_THREADS, 0, s>>>(T, ctr + 1); }
+  { KernelScope k(e->ctx, "k_eng_update"); k_eng_update<P><<<grid, CG_THREADS, 0, s>>>(T, ctr + 2); }
 }
 
 EngTab tab_of(Engine *e) {
@@ -2300,6 +2313,7 @@ int create(llf_ctx *ctx, int max_systems, int64_t max_chunks, Engine **out) {
   if (err == cudaSuccess) err = dalloc(ctx, &e->d_part, max_chunks);
   if (err == cudaSuccess) err = dalloc(ctx, &e->d_part2, max_chunks);
   if (err == cudaSuccess) err = dalloc(ctx, &e->d_part3, max_chunks);
+  if (err == cudaSuccess) err = dalloc(ctx, &e->d_ctr, 3 * 16);
   if (err == cudaSuccess) err = cudaMemsetAsync(e->d_arrive, 0, sizeof(int) * 2 * max_systems, s);
   if (err == cudaSuccess) err = cudaMemsetAsync(e->d_st, 0, sizeof(SegState) * max_systems, s);
   if (err == cudaSuccess) err = cudaMemsetAsync(e->d_slot, 0, sizeof(EngSlot) * max_systems, s);
@@ -2324,6 +2338,7 @@ void destroy(Engine *e) {
   dfree(ctx, e->d_slot); dfree(ctx, e->d_st); dfree(ctx, e->d_arrive); dfree(ctx, e->d_cslot);
   dfree(ctx, e->d_cbeg); dfree(ctx, e->d_cend); dfree(ctx, e->d_sfirst); dfree(ctx, e->d_snch);
   dfree(ctx, e->d_nch); dfree(ctx, e->d_part); dfree(ctx, e->d_part2); dfree(ctx, e->d_part3);
+  dfree(ctx, e->d_ctr);
   cudaStreamSynchronize(ctx->stream);
   delete e;
 }
@@ -2373,10 +2388,12 @@ int step(Engine *e) {
   const EngTab T = tab_of(e);
   const int per_graph = 16;
   auto enqueue = [&]() {
+    cudaMemsetAsync(e->d_ctr, 0, sizeof(unsigned) * 3 * per_graph, s);
     for (int k = 0; k < per_graph; ++k) {
-      if (P == 1) enqueue_engine_iteration<1>(e, T);
-      else if (P == 2) enqueue_engine_iteration<2>(e, T);
-      else enqueue_engine_iteration<3>(e, T);
+      unsigned *ctr = e->d_ctr + 3 * k;
+      if (P == 1) enqueue_engine_iteration<1>(e, T, ctr);
+      else if (P == 2) enqueue_engine_iteration<2>(e, T, ctr);
+      else enqueue_engine_iteration<3>(e, T, ctr);
     }
   };
   cudaGraphExec_t &exec = e->exec[P - 1];
