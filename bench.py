@@ -70,6 +70,9 @@ def parse():
     ap.add_argument("--server", default="engine", choices=["engine", "pool"],
                     help="serving: continuous-batching engine or the worker pool")
     ap.add_argument("--max-systems", type=int, default=256, help="serving: engine slots")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: offered requests per second (Poisson)")
+    ap.add_argument("--one-sample", type=int, default=0,
+                    help="serving: the one-at-a-time arm on the first k requests (0: all)")
     ap.add_argument("--no-peak", action="store_true", help="skip the DGEMM FP64 reference rate")
     ap.add_argument("--no-other-form", action="store_true", help="skip the second arithmetic form")
     ap.add_argument("--no-samples", action="store_true",
@@ -449,8 +452,9 @@ def run_serving(args, llf):
     import threading
     from llfem_gb300 import workloads as wl
     rng = np.random.default_rng(wl.SEED)
-    reqs = [wl.heat_request(rng) for _ in range(args.requests)]
-    arrivals = np.cumsum(rng.exponential(1.0 / 200.0, size=len(reqs)))
+    meshes = {}
+    reqs = [wl.heat_request(rng, cache=meshes) for _ in range(args.requests)]
+    arrivals = np.cumsum(rng.exponential(1.0, size=len(reqs))) / args.rate
 
     def precond(m):
         mode = args.precond or "auto"
@@ -474,8 +478,9 @@ def run_serving(args, llf):
     warm = [wl.heat_request(np.random.default_rng(1), dofs_max=5e3) for _ in range(2 * args.workers)]
     one = llf._lib.Server(workers=1)
     one.wait(submit(one, warm[0]))
+    n_one = len(reqs) if args.one_sample <= 0 else min(len(reqs), args.one_sample)
     t0 = time.perf_counter()
-    for r in reqs:
+    for r in reqs[:n_one]:
         one.wait(submit(one, r))
     t_single = time.perf_counter() - t0
     one.close()
@@ -510,7 +515,7 @@ def run_serving(args, llf):
     srv.close()
     span = done_at - start
     dofs = [m.non for m, _, _, _ in reqs]
-    return {"metric": "served steady-heat solves / s (Poisson 200 req/s)", "value": len(reqs) / span,
+    return {"metric": f"served steady-heat solves / s (Poisson {args.rate:g} req/s)", "value": len(reqs) / span,
             "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic heat requests (seeded)",
             "config": {"workload": f"serving-heat-{len(reqs)}", "requests": len(reqs), "workers": args.workers,
@@ -518,7 +523,8 @@ def run_serving(args, llf):
                        "dofs_median": float(np.median(dofs)), "dofs_max": int(max(dofs)), "reltol": 1e-10,
                        "precond": args.precond or "auto"},
             "latency_s": {"p50": _pct(lat, 50), "p99": _pct(lat, 99), "max": max(lat)},
-            "one_at_a_time_solves_per_s": len(reqs) / t_single,
+            "offered_req_per_s": args.rate, "stream_s": float(arrivals[-1]),
+            "one_at_a_time_solves_per_s": n_one / t_single, "one_at_a_time_sample": n_one,
             "cg_iterations_median": float(np.median(iters)), "peak_device_bytes": stats["peak_bytes"],
             "server_timing": timing}
 
@@ -834,10 +840,11 @@ def main():
             samples["batched"] = {"error": str(ex)}
         try:
             sargs = _ap.Namespace(**{**vars(args), "requests": 100, "precond": None, "server": "engine",
-                                     "max_systems": 256})
+                                     "max_systems": 256, "rate": 200.0, "one_sample": 0})
             r = run_serving(sargs, llf)
-            samples["serving"] = {k: r[k] for k in ("value", "unit", "config", "latency_s",
-                                                    "one_at_a_time_solves_per_s", "cg_iterations_median") if k in r}
+            samples["serving"] = {k: r[k] for k in ("metric", "value", "unit", "config", "latency_s",
+                                                    "one_at_a_time_solves_per_s", "cg_iterations_median",
+                                                    "offered_req_per_s") if k in r}
         except Exception as ex:
             samples["serving"] = {"error": str(ex)}
 

@@ -32,18 +32,25 @@ def batched_instance(rng: np.random.Generator, ne_min=1e3, ne_max=2e5):
     return m, E, nu
 
 
-def heat_request(rng: np.random.Generator, dofs_min=1e3, dofs_max=1e6, orders=(1, 2, 3, 4)):
+def heat_request(rng: np.random.Generator, dofs_min=1e3, dofs_max=1e6, orders=(1, 2, 3, 4), cache=None):
+    """One request (mesh, k, fixed, x0).  cache (a dict, optional) shares
+    meshes between requests of the same shape (dimension, cells per edge,
+    order); the random draws are the same with or without it."""
     dofs = math.exp(rng.uniform(math.log(dofs_min), math.log(dofs_max)))
     p = int(rng.choice(orders))
     three_d = bool(rng.integers(0, 2))
     if three_d:
         n = max(1, int(round((dofs ** (1.0 / 3.0) - 1.0) / p)))
-        m = _mesh.structured_box_mesh(n=n, order=p, simplex=True)
-        faces = ("left", "right")
     else:
         n = max(1, int(round((math.sqrt(dofs) - 1.0) / p)))
-        m = _mesh.structured_rect_mesh(n=n, order=p, simplex=True)
-        faces = ("left", "right")
+    key = (three_d, n, p)
+    m = cache.get(key) if cache is not None else None
+    if m is None:
+        m = (_mesh.structured_box_mesh(n=n, order=p, simplex=True) if three_d
+             else _mesh.structured_rect_mesh(n=n, order=p, simplex=True))
+        if cache is not None:
+            cache[key] = m
+    faces = ("left", "right")
     k = float(math.exp(rng.normal(0.0, 1.0)))
     fixed = np.zeros(m.non, dtype=np.uint8)
     x0 = np.zeros(m.non)
