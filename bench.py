@@ -75,6 +75,7 @@ def parse():
                     help="serving: the one-at-a-time arm on the first k requests (0: all)")
     ap.add_argument("--no-peak", action="store_true", help="skip the DGEMM FP64 reference rate")
     ap.add_argument("--no-other-form", action="store_true", help="skip the second arithmetic form")
+    ap.add_argument("--no-tune", action="store_true", help="assembly: skip the schedule autotuner")
     ap.add_argument("--no-samples", action="store_true",
                     help="assembly line: skip the short batched and serving samples")
     ap.add_argument("--no-plain", action="store_true", help="batched: skip the one-at-a-time plain arm")
@@ -640,6 +641,23 @@ def main():
     nnz = pat.nnz
     Ea, nua = L.f64([E]), L.f64([NU])
 
+    # the assembly's launch schedule, tuned on this mesh before the timed
+    # region (llf_autotune_stiffness; no choice changes a result bit)
+    tuned = {}
+    if not args.no_tune:
+        for fm_name, fm in (("fp64", L.FP64), ("fp32q", L.FP32Q)):
+            if args.no_other_form and fm != form:
+                continue
+            t_tune = time.perf_counter()
+            buf = L.C.create_string_buffer(1 << 16)
+            need = L.C.c_int64(0)
+            ctx.check(L.lib().llf_autotune_stiffness(ctx.h, dm.h, pat.h, L.SOLID, L.ptr(Ea, L.C.c_double),
+                                                      L.ptr(nua, L.C.c_double), 1, 1.0, fm, 2, buf, 1 << 16,
+                                                      L.C.byref(need)))
+            rep = json.loads(buf.value.decode())
+            tuned[fm_name] = {"chosen": rep["chosen"], "ms": rep["ms"], "candidates": len(rep["trials"]),
+                              "default_ms": rep["trials"][0]["ms"], "tuning_s": time.perf_counter() - t_tune}
+
     def assemble(fm=form):
         h = L.C.c_void_p()
         ctx.check(L.lib().llf_assemble_stiffness(ctx.h, dm.h, pat.h, L.SOLID, L.ptr(Ea, L.C.c_double),
@@ -864,7 +882,7 @@ def main():
                "dtype": "f64" if form == L.FP64 else "f32-quadrature/f64-accumulate",
                "data": "synthetic structured mesh (unit cube)",
                "config": workload_config(args.n, args.form),
-               "stored_nnz": stored, "pattern_build_s": pattern_s,
+               "stored_nnz": stored, "pattern_build_s": pattern_s, "autotune": tuned,
                "parallelism": "replicas" if world > 1 else "single",
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                "clocks": clocks, "other_form": other, "precision_form_error": precision, "samples": samples}

@@ -223,6 +223,24 @@ int llf_assemble_stiffness(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
                            int nmat, double thickness, int form,
                            llf_matrix **out);
 
+/* Tune the launch schedule of llf_assemble_stiffness for this mesh and
+ * pattern (the reference leaves its threaded assembly's element chunk size
+ * to an automatic choice, src/multifield.jl:2645, :3029-3033): the element
+ * kernels' CTAs per SM, the gather's degree-class threshold and warps per
+ * CTA, chosen one knob at a time from timed assemblies (best of `trials`
+ * each, after a warm one).  No choice changes a result bit, and every
+ * candidate's stored CSC is checked against the first one's.  The choice is
+ * kept on the pattern and reused for every pattern of the same shape
+ * (family, order, nodes per element, DoFs per node, operator, form, log2
+ * of the element count) in this process, and across processes when the
+ * environment variable LLF_TUNE_FILE names a file.  report (may be NULL)
+ * receives a JSON text of the candidates and their times; *needed its
+ * length. */
+int llf_autotune_stiffness(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int ptype,
+                           const double *E, const double *nu, int nmat, double thickness,
+                           int form, int trials, char *report, int64_t report_len,
+                           int64_t *needed);
+
 /* stiffnessMatrix straight into the host arrays of a
  * SparseMatrixCSC{Float64,Int64} — the same result, bit for bit, as
  * llf_assemble_stiffness followed by llf_matrix_copy_csc, in one call whose

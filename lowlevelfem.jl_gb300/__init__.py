@@ -14,7 +14,7 @@ from .mesh import (Mesh, Group, structured_rect_mesh, structured_box_mesh, read_
 from .api import (Material, material, elastic_constants, Problem, Field, SystemMatrix, VectorField,
                   ScalarField, TensorField, BoundaryCondition, LoadCondition, displacementConstraint,
                   temperatureConstraint, load, heatFlux, elasticSupport, heatConvection, constrainedDoFs,
-                  allDoFs, freeDoFs, applyBoundaryConditions_, loadVector, stiffnessMatrix, massMatrix,
+                  allDoFs, freeDoFs, applyBoundaryConditions_, loadVector, stiffnessMatrix, autotune, massMatrix,
                   heatConductionMatrix, heatCapacityMatrix, elasticSupportMatrix, heatConvectionMatrix,
                   heatConvectionVector, applyElasticSupport_, applyHeatConvection_, externalTangentFollower,
                   elementsToNodes, isElementwise, solveDisplacement,

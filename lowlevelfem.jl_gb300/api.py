@@ -313,6 +313,25 @@ def stiffnessMatrix(problem: Problem, elements=(), forceOneThread=True, precisio
     return SystemMatrix(_lib.DeviceMatrix(ctx, h, pat), problem)
 
 
+def autotune(problem: Problem, precision="fp64", trials=3) -> dict:
+    """Tune the launch schedule of stiffnessMatrix(problem) on this problem's
+    mesh and pattern (llf_autotune_stiffness): the chosen schedule is kept
+    for every later assembly of this shape; results do not change.  Returns
+    the tuner's report (candidates, times, the choice)."""
+    import json
+    ctx = problem._ctx
+    E = np.array([m.E for m in problem.material])
+    nu = np.array([m.nu for m in problem.material])
+    dm, pat = problem.device_mesh(), problem.pattern()
+    need = _lib.C.c_int64(0)
+    buf = _lib.C.create_string_buffer(1 << 16)
+    ctx.check(_lib.lib().llf_autotune_stiffness(ctx.h, dm.h, pat.h, problem.ptype, _lib.ptr(E, _lib.C.c_double),
+                                                _lib.ptr(nu, _lib.C.c_double), len(E), problem.thickness,
+                                                _form(precision), int(trials), buf, 1 << 16,
+                                                _lib.C.byref(need)), "autotune")
+    return json.loads(buf.value.decode())
+
+
 def massMatrix(problem: Problem, lumped=True, precision="fp64") -> SystemMatrix:
     """M = ρ b Σ HᵀH detJ w, consistent or row-sum lumped (src/linear.jl:1843-2004)."""
     if problem.type not in ("Solid", "PlaneStress", "PlaneStrain"):

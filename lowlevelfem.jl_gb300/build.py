@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libllfem_gb300.so")
 
-CU_SOURCES = ["abi.cu", "scan.cu", "pattern.cu", "assemble.cu", "assemble_fp32.cu", "solve.cu", "ic0.cu", "tl.cu", "field.cu"]
+CU_SOURCES = ["abi.cu", "scan.cu", "pattern.cu", "assemble.cu", "assemble_fp32.cu", "solve.cu", "ic0.cu", "tl.cu", "field.cu", "autotune.cu"]
 CXX_SOURCES = ["tables.cpp", "serve.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

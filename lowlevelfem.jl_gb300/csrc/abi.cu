@@ -555,6 +555,31 @@ int llf_assemble_stiffness(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int p
   return finish_matrix(ctx, rc, m, out);
 }
 
+int llf_autotune_stiffness(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int ptype, const double *E,
+                           const double *nu, int nmat, double thickness, int form, int trials, char *report,
+                           int64_t report_len, int64_t *needed) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!valid_ptype(ptype) || ptype == LLF_HEAT_CONDUCTION || ptype == LLF_PLANE_HEAT_CONDUCTION)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_autotune_stiffness: ptype must be SOLID, PLANE_STRESS or PLANE_STRAIN");
+  int rc = pattern_dim_check(ctx, mesh, pat, ptype);
+  if (rc) return rc;
+  if (pat->pdim != mesh->dim) return llf_fail(ctx, LLF_ERR_STATE, "stiffness needs a pattern with pdim == dim");
+  if (!E || !nu || nmat < 1) return llf_fail(ctx, LLF_ERR_ARG, "material arrays");
+  if (form != LLF_FP64 && form != LLF_FP32Q) return llf_fail(ctx, LLF_ERR_ARG, "form");
+  std::vector<double> c1(nmat), c2(nmat);
+  for (int i = 0; i < nmat; ++i) lame(ptype, E[i], nu[i], thickness, &c1[i], &c2[i]);
+  std::string rep;
+  rc = autotune_impl(ctx, mesh, pat, KIND_ELASTIC, ptype, c1.data(), c2.data(), nmat, form, trials, &rep);
+  if (rc != LLF_OK) return rc;
+  if (needed) *needed = (int64_t)rep.size();
+  if (report && report_len > 0) {
+    const size_t n = std::min((size_t)(report_len - 1), rep.size());
+    std::memcpy(report, rep.data(), n);
+    report[n] = 0;
+  }
+  return llf_ok(ctx);
+}
+
 int llf_assemble_stiffness_csc(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int ptype, const double *E,
                                const double *nu, int nmat, double thickness, int form, int64_t capacity,
                                int64_t *colptr, int64_t *rowval, double *nzval, int64_t *nnz) {

@@ -51,6 +51,7 @@ struct ElemArgs {
   // symmetric [0,NS) and antisymmetric [6,6+NA) parts of R_ab, and Mref_ab
   const uint8_t *aflag;
   const double *ageo, *Rp, *Mp;
+  int cta_cap;               // host side: CTAs per SM at most (0: as many as fit)
 };
 
 __device__ __forceinline__ int pair_offset(int a, int npe) {
@@ -661,6 +662,7 @@ int run_elem(llf_ctx *ctx, ElemArgs a) {
                           &per_sm, k_elem_fp64<KIND, DIM, false>, ELEM_THREADS, smem));
   }
   if (per_sm < 1) per_sm = 1;
+  if (a.cta_cap > 0 && per_sm > a.cta_cap) per_sm = a.cta_cap;
   int64_t grid = (int64_t)ctx->num_sms * per_sm;
   if (grid > a.nel) grid = a.nel > 0 ? a.nel : 1;
   double *scratch = nullptr;
@@ -687,7 +689,8 @@ static int gather_split(llf_ctx *ctx, llf_pattern *pat) {
   if (pat->gather_split_done) return LLF_OK;
   pat->gather_split_done = true;
   const int64_t non = pat->mesh->non;
-  if (non < 1024 || pat->max_deg < 16) return LLF_OK;
+  const int thr = pat->tune.gather_thr;   // percent of the largest degree
+  if (non < 1024 || pat->max_deg < 16 || thr <= 0) return LLF_OK;
   std::vector<int64_t> h(non + 1);
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), pat->d_nptr, sizeof(int64_t) * (non + 1), cudaMemcpyDeviceToHost,
                                     ctx->stream));
@@ -700,7 +703,7 @@ static int gather_split(llf_ctx *ctx, llf_pattern *pat) {
     acc += hist[d];
     if (acc >= (non * 6 + 9) / 10) { md_low = d; break; }
   }
-  if (md_low < 1 || md_low * 10 > pat->max_deg * 7) return LLF_OK;
+  if (md_low < 1 || md_low * 100 > pat->max_deg * thr) return LLF_OK;
   std::vector<int32_t> order;
   order.reserve(non);
   for (int64_t b = 0; b < non; ++b)
@@ -732,7 +735,7 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const 
   auto launch = [&](int md, const int32_t *list, int64_t b0, int64_t count) -> int {
     if (count <= 0) return LLF_OK;
     const size_t per_warp = (size_t)md * P * P * sizeof(double) + (size_t)((md + 7) & ~7);
-    int wpb = (int)std::min<size_t>(4, (200 * 1024) / per_warp);
+    int wpb = (int)std::min<size_t>(pat->tune.gather_wpb > 0 ? pat->tune.gather_wpb : 4, (200 * 1024) / per_warp);
     if (wpb < 1) wpb = 1;
     size_t smem = (size_t)wpb * per_warp;
     if (smem > 200 * 1024)
@@ -865,6 +868,7 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
                   const double *c1, const double *c2, int nmat, int form, int lumped,
                   llf_matrix *m, const double *init, GatherSink *sink) {
   (void)ptype;
+  if (!pat->tune.from_tuner) tune_lookup(pat, kind, form);
   const int dim = mesh->dim;
   const int npe = mesh->npe;
   const int P = pat->pdim;
@@ -924,6 +928,7 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
     a.ageo = ageo;
     a.Rp = mesh->d_Rp;
     a.Mp = mesh->d_Mp;
+    a.cta_cap = pat->tune.elem_cap;
     // element range [e0, e1): the element-indexed arrays are offset
     auto elems = [&](int64_t e0, int64_t e1) -> int {
       ElemArgs b = a;

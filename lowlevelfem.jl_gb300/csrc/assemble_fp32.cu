@@ -36,6 +36,7 @@ struct Elem32Args {
   // per affine element its FP32 coefficients (k_affine_coeff32), CW floats
   const float *coef;
   int affine_elsewhere;  // affine elements are left to k_affine_fp32
+  int cta_cap;           // host side: CTAs per SM at most (0: as many as fit)
 };
 
 constexpr int CW = 48;  // coefficient floats per element (W 36 + U 9, padded)
@@ -493,6 +494,7 @@ int run_affine32(llf_ctx *ctx, const Elem32Args &a) {
     LLF_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 1;
   LLF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, E32_THREADS, smem));
+  if (a.cta_cap > 0 && per_sm > a.cta_cap) per_sm = a.cta_cap;
   int64_t grid = (int64_t)ctx->num_sms * (per_sm < 1 ? 1 : per_sm);
   if (grid > a.nel) grid = a.nel > 0 ? a.nel : 1;
   KernelScope ks(ctx, "k_affine_fp32");
@@ -515,6 +517,7 @@ int run_elem32(llf_ctx *ctx, Elem32Args a) {
     LLF_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 1;
   LLF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, E32_THREADS, smem));
+  if (a.cta_cap > 0 && per_sm > a.cta_cap) per_sm = a.cta_cap;
   int64_t grid = (int64_t)ctx->num_sms * (per_sm < 1 ? 1 : per_sm);
   if (grid > a.nel) grid = a.nel > 0 ? a.nel : 1;
   KernelScope ks(ctx, "k_elem_fp32");
@@ -580,6 +583,7 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
   const size_t af_smem = kind == KIND_MASS ? affine_fp32_smem<KIND_MASS>(a.npairs)
                                            : affine_fp32_smem<KIND_ELASTIC>(a.npairs);
   a.affine_elsewhere = (aflag && af_smem <= 96 * 1024) ? 1 : 0;
+  a.cta_cap = pat->tune.elem_cap;
   // element range [e0, e1): the element-indexed arrays are offset
   auto elems = [&](int64_t e0, int64_t e1) -> int {
     Elem32Args b = a;

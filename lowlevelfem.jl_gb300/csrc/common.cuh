@@ -131,6 +131,16 @@ struct llf_pattern {
   int64_t gather_n_low = 0;
   int gather_md_low = 0;
   bool gather_split_done = false;
+  // launch schedule of this pattern's assemblies (autotune.cu picks it;
+  // every choice gives the same bits): element kernels' CTAs per SM
+  // (0: as many as fit), the gather's degree-class threshold in percent of
+  // the largest degree (0: one class) and its warps per CTA
+  struct Tune {
+    int elem_cap = 0;
+    int gather_thr = 70;
+    int gather_wpb = 4;
+    bool from_tuner = false;
+  } tune;
   // per column slab of the to-host assembly: one past the largest element
   // index that a node of this or an earlier slab touches (assemble.cu)
   std::vector<int64_t> slab_elem_end;
@@ -222,6 +232,13 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
 int assemble_to_host_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, const double *c1,
                           const double *c2, int nmat, int form, int64_t capacity, int64_t *colptr,
                           int64_t *rowval, double *nzval, int64_t *nnz);
+// autotune.cu: the tuned schedule for a pattern's shape, if one is known
+// (in this process, or in the file LLF_TUNE_FILE names); applied at the
+// pattern's first assembly
+void tune_lookup(llf_pattern *pat, int kind, int form);
+void tune_reset_split(llf_ctx *ctx, llf_pattern *pat);
+int autotune_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int ptype, const double *c1,
+                  const double *c2, int nmat, int form, int trials, std::string *report);
 // dropzeros -> stored form; counts (non-zeros per DoF column) may come from
 // the gather, else they are counted here
 int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts);
