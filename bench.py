@@ -76,6 +76,8 @@ def parse():
     ap.add_argument("--no-peak", action="store_true", help="skip the DGEMM FP64 reference rate")
     ap.add_argument("--no-other-form", action="store_true", help="skip the second arithmetic form")
     ap.add_argument("--no-tune", action="store_true", help="assembly: skip the schedule autotuner")
+    ap.add_argument("--no-c4b", action="store_true", help="tl: skip the hex125 12^3 Newton solve")
+    ap.add_argument("--c4b-fp64", action="store_true", help="tl: also run the hex125 Newton with the FP64 tangent")
     ap.add_argument("--no-samples", action="store_true",
                     help="assembly line: skip the short batched and serving samples")
     ap.add_argument("--no-plain", action="store_true", help="batched: skip the one-at-a-time plain arm")
@@ -589,6 +591,29 @@ def run_tl(args, llf):
     dtc = float(np.abs(ktc.dm.copy_structural() - k64).max() / np.abs(k64).max())
     gemm4 = 2 * 375 ** 2 * (15 * 125) * m4.nel
     tc_ms = prof_tc.get("k_tl_tangent_tc", 0.0)
+    # the order-4 variant's Newton solve: hex125 12^3, 30% stretch in 10
+    # steps, FP64 residuals, the tangent on the tensor cores (and optionally
+    # the FP64 tangent for comparison)
+    newton4 = {}
+    forms4 = [] if args.no_c4b else (["tf32x3", "fp64"] if args.c4b_fp64 else ["tf32x3"])
+    for tform in forms4:
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        u4 = llf.solveDeformation(P4, support=sup, params=prm, steps=10, tol=1e-8,
+                                  preconditioner=args.precond or "bjacobi", tangent=tform)
+        torch.cuda.synchronize()
+        tn4 = time.perf_counter() - t1
+        last = {}
+        for h in u4.history:
+            last[h["step"]] = h
+        newton4[tform] = {"s": tn4, "newton_iterations": len(u4.history),
+                          "cg_iterations": int(sum(h.get("cg_iterations", 0) for h in u4.history)),
+                          "steps_converged": int(sum("cg_iterations" not in h for h in last.values())),
+                          "final_residual": u4.history[-1]["residual"],
+                          "u_norm": float(np.linalg.norm(u4.a))}
+    if len(newton4) == 2:
+        newton4["u_rel_diff_tf32x3_vs_fp64"] = abs(newton4["tf32x3"]["u_norm"] - newton4["fp64"]["u_norm"]) / \
+            newton4["fp64"]["u_norm"]
     return {"metric": "TL Newton iteration time (hex8 48^3, 30% stretch, 10 steps)", "value": t_newton / max(its, 1) * 1e3,
             "unit": "ms/iteration", "n_gpus": 1, "steps": its, "warmup": 0, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic unit cube",
@@ -604,7 +629,8 @@ def run_tl(args, llf):
                                                     "gemm_flops": gemm4,
                                                     "tensor_tflops_per_split": gemm4 / (tc_ms * 1e-3) / 1e12 if tc_ms else None,
                                                     "tensor_tflops_issued": 3 * gemm4 / (tc_ms * 1e-3) / 1e12 if tc_ms else None,
-                                                    "max_rel_diff_vs_fp64": dtc}}}
+                                                    "max_rel_diff_vs_fp64": dtc}},
+            "hex125_newton": newton4}
 
 
 def main():
@@ -800,12 +826,48 @@ def main():
         te = time_e2e(to_host_fused)
         assert got.value == nnz_s
         te2 = time_e2e(to_host_two_calls)
-        e2e = {"value": nnz / te / 1e9, "unit": "GNNZ/s", "ms_per_step": te * 1e3,
+        full = {"value": nnz / te / 1e9, "unit": "GNNZ/s", "ms_per_step": te * 1e3,
+                "h2d_bytes_per_step": xyz_h.numel() * 8 + conn_h.numel() * 8,
+                "d2h_bytes_per_step": colptr_h.numel() * 8 + 2 * nnz_s * 8,
+                "call": "llf_mesh_update + llf_assemble_stiffness_csc (pinned host arrays)",
+                "two_call_ms_per_step": te2 * 1e3,
+                "two_call": "llf_mesh_update + llf_assemble_stiffness + llf_matrix_copy_csc"}
+        # values against the pattern the caller holds: colptr, nzval and one
+        # keep bit per structural entry come back; the caller's rowval (the
+        # structural rowval filtered by the bits, llf_rowval_from_keep) is
+        # rebuilt inside the timed region whenever the bits differ from the
+        # previous call's, and the bits are compared every call
+        import numpy as np
+        _, srow = pat.copy()
+        nw = (pat.nnz + 31) // 32
+        keep_h = torch.empty(nw, dtype=torch.int32).pin_memory()
+        keep_prev = np.zeros(nw, dtype=np.uint32)
+        rows_h = torch.empty(pat.nnz, dtype=torch.int64).pin_memory()
+        rebuilt = [0]
+
+        def to_host_values():
+            ctx.check(L.lib().llf_assemble_stiffness_values(
+                ctx.h, dm.h, pat.h, L.SOLID, L.ptr(Ea, L.C.c_double), L.ptr(nua, L.C.c_double), 1, 1.0, form,
+                pat.nnz, P(colptr_h, L.C.c_int64), P(nzval_h, L.C.c_double), P(keep_h, L.C.c_uint32),
+                L.C.byref(got)))
+            kb = keep_h.numpy().view(np.uint32)
+            if not np.array_equal(kb, keep_prev):
+                n_rows = L.lib().llf_rowval_from_keep(pat.nnz, L.ptr(srow, L.C.c_int64), P(keep_h, L.C.c_uint32),
+                                                      P(rows_h, L.C.c_int64))
+                assert n_rows == got.value
+                keep_prev[:] = kb
+                rebuilt[0] += 1
+
+        tv = time_e2e(to_host_values)
+        assert got.value == nnz_s
+        assert torch.equal(rows_h[:nnz_s], rowval_h[:nnz_s])   # the caller's rowval is the stored one
+        e2e = {"value": nnz / tv / 1e9, "unit": "GNNZ/s", "ms_per_step": tv * 1e3,
                "h2d_bytes_per_step": xyz_h.numel() * 8 + conn_h.numel() * 8,
-               "d2h_bytes_per_step": colptr_h.numel() * 8 + 2 * nnz_s * 8,
-               "call": "llf_mesh_update + llf_assemble_stiffness_csc (pinned host arrays)",
-               "two_call_ms_per_step": te2 * 1e3,
-               "two_call": "llf_mesh_update + llf_assemble_stiffness + llf_matrix_copy_csc"}
+               "d2h_bytes_per_step": colptr_h.numel() * 8 + nnz_s * 8 + nw * 4,
+               "call": "llf_mesh_update + llf_assemble_stiffness_values (pinned host arrays) + keep-bit compare "
+                       "(+ llf_rowval_from_keep when the bits change)",
+               "rowval_rebuilds": rebuilt[0],
+               "full_csc": full}
 
     # the other arithmetic form on the same workload (reported beside the headline)
     other = None

@@ -256,6 +256,30 @@ int llf_assemble_stiffness_csc(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
                                int64_t capacity, int64_t *colptr,
                                int64_t *rowval, double *nzval, int64_t *nnz);
 
+/* stiffnessMatrix as values against a pattern the caller already holds
+ * (no counterpart in the reference; its stiffnessMatrix returns a fresh
+ * SparseMatrixCSC each call).  The same assembly and column-slab copies as
+ * llf_assemble_stiffness_csc, but rowval, which the pattern fixes up to
+ * the entries dropzeros! removes, is not copied: colptr[ndof+1] (1-based)
+ * and nzval[capacity >= structural nnz] receive the stored CSC, and
+ * keep[(structural nnz + 31)/32] one bit per structural entry (bit k of
+ * word k/32: entry k of llf_pattern_copy's rowval is stored).  The stored
+ * rowval is the structural rowval filtered by keep (llf_rowval_from_keep);
+ * a caller that re-assembles the same operator keeps its previous rowval
+ * while the keep bits do not change, so each call moves about half the
+ * bytes of llf_assemble_stiffness_csc. */
+int llf_assemble_stiffness_values(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
+                                  int ptype, const double *E, const double *nu,
+                                  int nmat, double thickness, int form,
+                                  int64_t capacity, int64_t *colptr, double *nzval,
+                                  uint32_t *keep, int64_t *nnz);
+
+/* Host only: the stored rowval from the structural rowval and the keep bits
+ * of llf_assemble_stiffness_values; returns the stored count (or a negative
+ * status). */
+int64_t llf_rowval_from_keep(int64_t nnz_structural, const int64_t *rowval_structural,
+                             const uint32_t *keep, int64_t *rowval);
+
 /* M = rho b sum H^T H detJ w, consistent (lumped == 0) or row-sum lumped —
  * massMatrix / massMatrixSolid, src/linear.jl:1843-2004. */
 int llf_assemble_mass(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,

@@ -953,7 +953,8 @@ def tangentMatrix(problem: Problem, F, energy="NeoHookeCompressible", params=Non
 
 
 def solveDeformation(problem: Problem, support=(), load=(), energy="NeoHookeCompressible", params=None,
-                     steps=10, tol=1e-8, maxit=25, reltol=1e-10, preconditioner="bjacobi", callback=None):
+                     steps=10, tol=1e-8, maxit=25, reltol=1e-10, preconditioner="bjacobi", callback=None,
+                     tangent="fp64"):
     """Total Lagrangian Newton solution in `steps` proportional load steps:
     prescribed displacements and external loads are ramped linearly; every
     Newton iteration evaluates F = I + u∘∇, f_int and the consistent tangent on
@@ -961,7 +962,10 @@ def solveDeformation(problem: Problem, support=(), load=(), energy="NeoHookeComp
     prescribed values on the constrained DoFs.  Converged when the FP64
     residual on the free DoFs drops below tol times its value at the start of
     the step (or below tol times |f_ext| when that is larger).  Returns u and
-    per-iteration records (step, iteration, residual norm, CG iterations)."""
+    per-iteration records (step, iteration, residual norm, CG iterations).
+    tangent="tf32x3" assembles the tangent on the tensor cores (split TF32
+    products): the residual and the update stay FP64, so the iteration still
+    converges to the FP64 tolerance, a little less than quadratically."""
     n = problem.pdim * problem.non
     u = _field_for(problem, np.zeros(n))
     target = _field_for(problem, np.zeros(n))
@@ -989,7 +993,7 @@ def solveDeformation(problem: Problem, support=(), load=(), energy="NeoHookeComp
                     res0 = max(rn, float(np.linalg.norm(fext)), 1e-300)
                 if rn <= tol * res0:
                     break
-            K = tangentMatrix(problem, F, energy=energy, params=params)
+            K = tangentMatrix(problem, F, energy=energy, params=params, precision=tangent)
             x, cg_it, _ = K.dm.pcg(r, du_fixed, fixed, precond=prec, reltol=reltol, maxiter=20 * n,
                                    raise_on_fail=True)
             history[-1]["cg_iterations"] = cg_it

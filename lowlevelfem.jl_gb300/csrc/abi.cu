@@ -601,6 +601,50 @@ int llf_assemble_stiffness_csc(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, i
   return rc == LLF_OK ? llf_ok(ctx) : rc;
 }
 
+int llf_assemble_stiffness_values(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int ptype, const double *E,
+                                  const double *nu, int nmat, double thickness, int form, int64_t capacity,
+                                  int64_t *colptr, double *nzval, uint32_t *keep, int64_t *nnz) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!valid_ptype(ptype) || ptype == LLF_HEAT_CONDUCTION || ptype == LLF_PLANE_HEAT_CONDUCTION)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_assemble_stiffness_values: ptype must be SOLID, PLANE_STRESS or PLANE_STRAIN");
+  int rc = pattern_dim_check(ctx, mesh, pat, ptype);
+  if (rc) return rc;
+  if (pat->pdim != mesh->dim) return llf_fail(ctx, LLF_ERR_STATE, "stiffness needs a pattern with pdim == dim");
+  if (!E || !nu || nmat < 1) return llf_fail(ctx, LLF_ERR_ARG, "material arrays");
+  if (form != LLF_FP64 && form != LLF_FP32Q) return llf_fail(ctx, LLF_ERR_ARG, "form");
+  if (!colptr || !nzval || !keep || !nnz)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_assemble_stiffness_values: null output");
+  if (capacity < pat->nnz)
+    return llf_fail(ctx, LLF_ERR_ARG, "llf_assemble_stiffness_values: capacity must be at least the structural nnz");
+  std::vector<double> c1(nmat), c2(nmat);
+  for (int i = 0; i < nmat; ++i) lame(ptype, E[i], nu[i], thickness, &c1[i], &c2[i]);
+  rc = assemble_to_host_impl(ctx, mesh, pat, KIND_ELASTIC, c1.data(), c2.data(), nmat, form, capacity, colptr,
+                             nullptr, nzval, nnz, keep);
+  return rc == LLF_OK ? llf_ok(ctx) : rc;
+}
+
+int64_t llf_rowval_from_keep(int64_t nnz_structural, const int64_t *rowval_structural, const uint32_t *keep,
+                             int64_t *rowval) {
+  if (nnz_structural < 0 || !rowval_structural || !keep || !rowval) return LLF_ERR_ARG;
+  int64_t o = 0;
+  for (int64_t w = 0; w * 32 < nnz_structural; ++w) {
+    uint32_t bits = keep[w];
+    const int64_t base = w * 32;
+    if (bits == 0xffffffffu && base + 32 <= nnz_structural) {
+      std::memcpy(rowval + o, rowval_structural + base, sizeof(int64_t) * 32);
+      o += 32;
+      continue;
+    }
+    while (bits) {
+      const int b = __builtin_ctz(bits);
+      if (base + b >= nnz_structural) break;
+      rowval[o++] = rowval_structural[base + b];
+      bits &= bits - 1u;
+    }
+  }
+  return o;
+}
+
 int llf_assemble_mass(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int ptype,
                       const double *rho, int nmat, double thickness, int lumped, int form,
                       llf_matrix **out) {

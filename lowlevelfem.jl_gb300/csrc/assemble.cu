@@ -533,11 +533,16 @@ __global__ void k_count_nz(const double *__restrict__ nz, const int64_t *__restr
 
 // One warp per DoF column; four 32-entry chunks loaded (values and row
 // nodes) before their ballots so that each warp keeps 2 KB in flight.
+// rowval_s may be null (values only); keepbits (or null) receives one bit
+// per structural entry, set when the entry is stored (the array must start
+// zeroed; chunk boundaries do not fall on word boundaries, so the words are
+// or-ed in).
 template <int P, bool KEEP>
 __global__ void k_compact(const double *__restrict__ nz, const int64_t *__restrict__ colptr,
                           const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
                           int64_t ndof, const int64_t *__restrict__ outptr,
-                          int64_t *__restrict__ rowval_s, double *__restrict__ nzval_s) {
+                          int64_t *__restrict__ rowval_s, double *__restrict__ nzval_s,
+                          unsigned *__restrict__ keepbits = nullptr) {
   constexpr int U = 4;
   const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
   for (int64_t c = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5); c < ndof;
@@ -561,8 +566,14 @@ __global__ void k_compact(const double *__restrict__ nz, const int64_t *__restri
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
         if (keep) {
           const int off = __popc(bal & ((1u << lane) - 1u));
-          rowval_s[o + off] = row[u] + 1;
+          if (rowval_s) rowval_s[o + off] = row[u] + 1;
           nzval_s[o + off] = v[u];
+        }
+        if (keepbits && lane == 0 && bal) {
+          const int64_t sidx = s + l0 + u * 32;
+          const int sh = (int)(sidx & 31);
+          atomicOr(keepbits + (sidx >> 5), bal << sh);
+          if (sh) atomicOr(keepbits + (sidx >> 5) + 1, bal >> (32 - sh));
         }
         o += __popc(bal);
       }
@@ -1080,6 +1091,7 @@ struct HostSlabSink : GatherSink {
   int64_t capacity = 0;
   int64_t *h_colptr = nullptr, *h_rowval = nullptr;
   double *h_nzval = nullptr;
+  unsigned *h_keep = nullptr;   // values-only form: keep bits instead of rowval
   int64_t nnz = 0;
 
   template <class T>
@@ -1093,11 +1105,15 @@ struct HostSlabSink : GatherSink {
     cudaStream_t cp = nullptr;
     cudaEvent_t ev[NSLAB] = {}, done[NSLAB] = {};
     int rc = LLF_OK;
+    unsigned *keep = nullptr;
+    const int64_t nwords = pat->nnz / 32 + 2;
     cudaError_t e = dalloc(ctx, &nz, pat->nnz);
+    if (e == cudaSuccess && h_keep) e = dalloc(ctx, &keep, nwords);
+    if (e == cudaSuccess && h_keep) e = cudaMemsetAsync(keep, 0, sizeof(unsigned) * nwords, s);
     if (e == cudaSuccess) e = dalloc(ctx, &cnt, ndof + 1);
     if (e == cudaSuccess) e = dalloc(ctx, &outptr, ndof + 1);
     if (e == cudaSuccess) e = dalloc(ctx, &colptr, ndof + 1);
-    if (e == cudaSuccess) e = dalloc(ctx, &rowval, pat->nnz);
+    if (e == cudaSuccess && !h_keep) e = dalloc(ctx, &rowval, pat->nnz);
     if (e == cudaSuccess) e = dalloc(ctx, &nzval, pat->nnz);
     if (e == cudaSuccess) e = dalloc(ctx, &carry, NSLAB + 1);
     if (e == cudaSuccess) e = dalloc(ctx, &totals, NSLAB);
@@ -1148,7 +1164,7 @@ struct HostSlabSink : GatherSink {
         KernelScope ks(ctx, "k_compact");
 #define LLF_SLAB_COMPACT(PP) \
   k_compact<PP, false><<<g, 256, 0, s>>>(nz, pat->d_colptr + c0, pat->d_nptr + B0, pat->d_nadj, nc, outptr + c0, \
-                                          rowval, nzval)
+                                          rowval, nzval, keep)
         if (P == 1) LLF_SLAB_COMPACT(1); else if (P == 2) LLF_SLAB_COMPACT(2); else LLF_SLAB_COMPACT(3);
 #undef LLF_SLAB_COMPACT
         k_colptr_1based<<<grid_1d(nc, 256, ctx->num_sms), 256, 0, s>>>(outptr + c0, nc, colptr + c0);
@@ -1170,11 +1186,18 @@ struct HostSlabSink : GatherSink {
       e = cudaStreamWaitEvent(cp, ev[k], 0);
       if (e == cudaSuccess && nc > 0)
         e = cudaMemcpyAsync(h_colptr + c0, colptr + c0, sizeof(int64_t) * nc, cudaMemcpyDeviceToHost, cp);
-      if (e == cudaSuccess && o1 > o0)
+      if (e == cudaSuccess && o1 > o0 && !h_keep)
         e = cudaMemcpyAsync(h_rowval + o0, rowval + o0, sizeof(int64_t) * (o1 - o0), cudaMemcpyDeviceToHost, cp);
       if (e == cudaSuccess && o1 > o0)
         e = cudaMemcpyAsync(h_nzval + o0, nzval + o0, sizeof(double) * (o1 - o0), cudaMemcpyDeviceToHost, cp);
       if (e == cudaSuccess) e = cudaEventRecord(done[k], cp);
+      if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+    }
+    // the keep bits once every slab is compacted (the words at slab edges
+    // take bits from both neighbours)
+    if (rc == LLF_OK && h_keep) {
+      e = cudaMemcpyAsync(h_keep, keep, sizeof(unsigned) * ((pat->nnz + 31) / 32), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
       if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
     }
     if (cp) {
@@ -1193,6 +1216,7 @@ struct HostSlabSink : GatherSink {
     dfree(ctx, nzval);
     dfree(ctx, carry);
     dfree(ctx, totals);
+    dfree(ctx, keep);
     cudaStreamSynchronize(s);
     for (int k = 0; k < NSLAB; ++k) {
       if (ev[k]) cudaEventDestroy(ev[k]);
@@ -1237,12 +1261,13 @@ struct HostSlabSink : GatherSink {
 
 int assemble_to_host_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, const double *c1,
                           const double *c2, int nmat, int form, int64_t capacity, int64_t *colptr,
-                          int64_t *rowval, double *nzval, int64_t *nnz) {
+                          int64_t *rowval, double *nzval, int64_t *nnz, unsigned *keep) {
   HostSlabSink sink;
   sink.capacity = capacity;
   sink.h_colptr = colptr;
   sink.h_rowval = rowval;
   sink.h_nzval = nzval;
+  sink.h_keep = keep;
   llf_matrix scratch;
   scratch.pat = pat;
   int rc = assemble_impl(ctx, mesh, pat, kind, LLF_SOLID, c1, c2, nmat, form, 0, &scratch, nullptr, &sink);

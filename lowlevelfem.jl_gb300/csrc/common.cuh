@@ -231,7 +231,7 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
 // next slab is gathered and compacted (assemble.cu)
 int assemble_to_host_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, const double *c1,
                           const double *c2, int nmat, int form, int64_t capacity, int64_t *colptr,
-                          int64_t *rowval, double *nzval, int64_t *nnz);
+                          int64_t *rowval, double *nzval, int64_t *nnz, unsigned *keep = nullptr);
 // autotune.cu: the tuned schedule for a pattern's shape, if one is known
 // (in this process, or in the file LLF_TUNE_FILE names); applied at the
 // pattern's first assembly

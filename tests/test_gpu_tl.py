@@ -190,3 +190,26 @@ def test_tensor_core_tangent_within_tf32x3_tolerance(llf, case):
     err = np.abs(a - b).max() / scale
     assert err <= 5e-5, err
     assert err > 0.0  # the tensor-core path really ran (TF32 splits are not bit-exact)
+
+
+@pytest.mark.parametrize("order,n", [(3, 2), (4, 2)], ids=["hex64", "hex125"])
+def test_newton_converges_with_tensor_core_tangent(llf, order, n):
+    """The order-3/4 hexahedra of the hyperelastic configuration with the
+    tangent assembled on the tensor cores (tf32x3): f_int and the update stay
+    FP64, so Newton reaches the same FP64 residual tolerance as with the FP64
+    tangent and the same displacement, at most a few iterations later."""
+    llf.structured_box_mesh(n=n, order=order)
+    p = llf.Problem([llf.Material("body")], type="Solid")
+    sup = [llf.displacementConstraint("left", ux=0.0), llf.displacementConstraint("right", ux=0.3),
+           llf.displacementConstraint("bottom", uy=0.0), llf.displacementConstraint("rear", uz=0.0)]
+    prm = {"mu": 1.0, "lambda": 10.0}
+    u64 = llf.solveDeformation(p, support=sup, params=prm, steps=3, tol=1e-8)
+    utc = llf.solveDeformation(p, support=sup, params=prm, steps=3, tol=1e-8, tangent="tf32x3")
+    for step in (1, 2, 3):
+        # a step that converged ends with a residual record and no solve after it
+        last = [h for h in utc.history if h["step"] == step][-1]
+        assert "cg_iterations" not in last, (step, last)
+    it64, ittc = len(u64.history), len(utc.history)
+    assert ittc <= it64 + 6, (it64, ittc)
+    d = np.linalg.norm(utc.a - u64.a) / np.linalg.norm(u64.a)
+    assert d <= 1e-7, d

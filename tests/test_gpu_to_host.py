@@ -51,3 +51,45 @@ def test_to_host_capacity_is_checked(llf):
     assert rc == -1   # LLF_ERR_ARG
     rc, c, r, v = _to_host(llf, p, llf._lib.FP64)
     assert rc == 0 and len(v) == llf.stiffnessMatrix(p).nnz()
+
+
+def _values(llf, p, form):
+    L = llf._lib
+    ctx, dm, pat = p._ctx, p.device_mesh(), p.pattern()
+    E = np.array([m.E for m in p.material])
+    nu = np.array([m.nu for m in p.material])
+    colptr = np.zeros(pat.ndof + 1, dtype=np.int64)
+    nzval = np.zeros(pat.nnz)
+    keep = np.zeros((pat.nnz + 31) // 32, dtype=np.uint32)
+    nnz = L.C.c_int64(0)
+    rc = L.lib().llf_assemble_stiffness_values(ctx.h, dm.h, pat.h, p.ptype, L.ptr(E, L.C.c_double),
+                                               L.ptr(nu, L.C.c_double), len(E), p.thickness, form, pat.nnz,
+                                               L.ptr(colptr, L.C.c_int64), L.ptr(nzval, L.C.c_double),
+                                               L.ptr(keep, L.C.c_uint32), L.C.byref(nnz))
+    return rc, colptr, nzval[:nnz.value], keep
+
+
+@pytest.mark.parametrize("case", [("box", 3, 2, False, "Solid"), ("box", 4, 2, True, "Solid"),
+                                  ("rect", 20, 1, False, "PlaneStrain"), ("box", 17, 1, False, "Solid")],
+                         ids=["hex27", "tet10", "quad4", "hex8-4913"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_values_and_keep_bits_give_the_csc(llf, case, precision):
+    """llf_assemble_stiffness_values: colptr and nzval of the stored CSC plus
+    one bit per structural entry; the structural rowval (llf_pattern_copy)
+    filtered by the bits (llf_rowval_from_keep) is the stored rowval."""
+    L = llf._lib
+    kind, n, order, simplex, pt = case
+    make_mesh(llf, kind, n, order, simplex)
+    p = llf.Problem([llf.Material("body", E=2.1e5, nu=0.3)], type=pt, thickness=0.5)
+    form = L.FP64 if precision == "fp64" else L.FP32Q
+    sc, sr = p.pattern().copy()
+    for _ in range(2):
+        rc, c, v, keep = _values(llf, p, form)
+        assert rc == 0
+        gc, gr, gv = llf.stiffnessMatrix(p, precision=precision).csc()
+        assert np.array_equal(c, gc) and np.array_equal(v, gv)
+        rows = np.zeros(len(sr), dtype=np.int64)
+        got = L.lib().llf_rowval_from_keep(len(sr), L.ptr(sr, L.C.c_int64), L.ptr(keep, L.C.c_uint32),
+                                           L.ptr(rows, L.C.c_int64))
+        assert got == len(gv) and np.array_equal(rows[:got], gr)
+        assert int(np.unpackbits(keep.view(np.uint8)).sum()) == len(gv)
