@@ -106,25 +106,64 @@ function pattern(problem, pdim::Int=problem.pdim)
     return d[pdim] = h[]
 end
 
-# device matrix -> SparseMatrixCSC{Float64,Int64} (two-phase copy), then free
-function fetch(hm::Ptr{Cvoid}, n::Int)
+# Matrices assembled here stay on the device until the SparseMatrixCSC that
+# was returned for them is collected: solveField / FDM use the device copy
+# instead of uploading the host arrays again, as long as those arrays still
+# hold what was returned (same arrays, same sum of values; a caller that
+# edits K.A in place gets a fresh upload).
+struct DevCopy
+    h::Ptr{Cvoid}
+    pat::Ptr{Cvoid}
+    nnz::Int
+    checksum::Float64
+end
+const DEVICE = WeakKeyDict{SparseMatrixCSC{Float64,Int64},DevCopy}()
+
+function keep_on_device!(A::SparseMatrixCSC{Float64,Int64}, hm::Ptr{Cvoid}, pat::Ptr{Cvoid})
+    DEVICE[A] = DevCopy(hm, pat, nnz(A), sum(nonzeros(A)))
+    finalizer(A) do _
+        ccall((:llf_matrix_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), hm)
+    end
+    return A
+end
+
+# The device matrix of K if K.A is unchanged since it was returned, else
+# nothing.
+function device_copy(K::SystemMatrix, pat::Ptr{Cvoid})
+    d = get(DEVICE, K.A, nothing)
+    d === nothing && return nothing
+    (d.pat == pat && d.nnz == nnz(K.A) && d.checksum == sum(nonzeros(K.A))) || return nothing
+    return d.h
+end
+
+# device matrix -> SparseMatrixCSC{Float64,Int64} (two-phase copy); the
+# device matrix is kept for the solves (keep_on_device!)
+function fetch(hm::Ptr{Cvoid}, n::Int, pat::Ptr{Cvoid})
     nnz = Ref{Int64}(0)
     check(ccall((:llf_matrix_nnz, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ref{Int64}), ctx(), hm, nnz))
     colptr = Vector{Int64}(undef, n + 1); rowval = Vector{Int64}(undef, nnz[]); nzval = Vector{Float64}(undef, nnz[])
     check(ccall((:llf_matrix_copy_csc, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}),
                 ctx(), hm, colptr, rowval, nzval))
-    ccall((:llf_matrix_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), hm)
-    return SparseMatrixCSC(n, n, colptr, rowval, nzval)
+    return keep_on_device!(SparseMatrixCSC(n, n, colptr, rowval, nzval), hm, pat)
 end
 
 # ---------------------------------------------------------------- assembly
-# One call straight into the SparseMatrixCSC arrays: rowval/nzval sized by the
-# structural nnz, filled while the assembly runs, then resize!d to the
-# stored count.
-function stiffnessMatrix(problem; elements=[], forceOneThread=true)
+# stiffnessMatrix: assembled on the device, the stored CSC copied into the
+# SparseMatrixCSC arrays, the device matrix kept for the solves.  With
+# keep_device=false: one call straight into the host arrays
+# (llf_assemble_stiffness_csc, the device work hidden behind the copy).
+function stiffnessMatrix(problem; elements=[], forceOneThread=true, keep_device=true)
     m = device_mesh(problem); pat = pattern(problem)
     E = Float64[mat.E for mat in problem.material]; ν = Float64[mat.ν for mat in problem.material]
     n = problem.pdim * problem.non
+    if keep_device
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:llf_assemble_stiffness, LIB), Cint,
+                    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Cint, Float64, Cint,
+                     Ref{Ptr{Cvoid}}),
+                    ctx(), m.h, pat, ptype(problem), E, ν, length(E), problem.thickness, 0, h))
+        return SystemMatrix(fetch(h[], n, pat), problem)
+    end
     snnz = Ref{Int64}(0); ndof = Ref{Int64}(0); pd = Ref{Cint}(0)
     ccall((:llf_pattern_info, LIB), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}, Ref{Cint}), pat, ndof, snnz, pd)
     colptr = Vector{Int64}(undef, n + 1); rowval = Vector{Int64}(undef, snnz[]); nzval = Vector{Float64}(undef, snnz[])
@@ -145,7 +184,7 @@ function massMatrix(problem; lumped=true)
     check(ccall((:llf_assemble_mass, LIB), Cint,
                 (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Float64, Cint, Cint, Ref{Ptr{Cvoid}}),
                 ctx(), m.h, pat, ptype(problem), ρ, length(ρ), problem.thickness, lumped ? 1 : 0, 0, h))
-    return SystemMatrix(fetch(h[], problem.pdim * problem.non), problem)
+    return SystemMatrix(fetch(h[], problem.pdim * problem.non, pat), problem)
 end
 
 function heatConductionMatrix(problem; elements=[])
@@ -155,7 +194,7 @@ function heatConductionMatrix(problem; elements=[])
     check(ccall((:llf_assemble_heat, LIB), Cint,
                 (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Float64, Cint, Ref{Ptr{Cvoid}}),
                 ctx(), m.h, pat, ptype(problem), k, length(k), problem.thickness, 0, h))
-    return SystemMatrix(fetch(h[], problem.non), problem)
+    return SystemMatrix(fetch(h[], problem.non, pat), problem)
 end
 
 function heatCapacityMatrix(problem; elements=[], lumped=false)
@@ -165,7 +204,7 @@ function heatCapacityMatrix(problem; elements=[], lumped=false)
     check(ccall((:llf_assemble_mass, LIB), Cint,
                 (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Float64, Cint, Cint, Ref{Ptr{Cvoid}}),
                 ctx(), m.h, pat, ptype(problem), cρ, length(cρ), 1.0, lumped ? 1 : 0, 0, h))
-    return SystemMatrix(fetch(h[], problem.non), problem)
+    return SystemMatrix(fetch(h[], problem.non, pat), problem)
 end
 
 # Boundary elements of the conditions' physical groups, in condition order,
@@ -222,7 +261,7 @@ function support_matrix(problem, conds, keys)
                ctx(), pat, bm, ke, C_NULL, problem.dim == 2 ? problem.thickness : 1.0, h)
     ccall((:llf_mesh_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), bm)
     check(st)
-    return SystemMatrix(fetch(h[], pd * problem.non), problem)
+    return SystemMatrix(fetch(h[], pd * problem.non, pat), problem)
 end
 
 elasticSupportMatrix(problem, elSupports) = support_matrix(problem, elSupports, (:kx, :ky, :kz))
@@ -246,7 +285,7 @@ function externalTangentFollower(problem, loads; F)
                ctx(), pat, bm, Fn, te, C_NULL, h)
     ccall((:llf_mesh_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), bm)
     check(st)
-    return SystemMatrix(fetch(h[], 3problem.non), problem)
+    return SystemMatrix(fetch(h[], 3problem.non, pat), problem)
 end
 
 # energy: pass :NeoHookeCompressible or :StVenantKirchhoff; params = (μ=.., λ=..)
@@ -265,7 +304,7 @@ function materialTangentMatrix(problem; F, C=nothing, energy=nothing, params=not
     check(ccall((:llf_tl_material_tangent, LIB), Cint,
                 (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Cint, Ptr{Float64}, Cint, Ref{Ptr{Cvoid}}),
                 ctx(), m.h, pat, Fe, lw, prm, length(prm), h))
-    return SystemMatrix(fetch(h[], 3problem.non), problem)
+    return SystemMatrix(fetch(h[], 3problem.non, pat), problem)
 end
 
 function initialStressMatrix(problem; S=nothing, energy=nothing, params=nothing, C=nothing)
@@ -283,7 +322,7 @@ function initialStressMatrix(problem; S=nothing, energy=nothing, params=nothing,
                     (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Cint, Ptr{Float64}, Cint, Ref{Ptr{Cvoid}}),
                     ctx(), m.h, pat, C_NULL, Ce, law(energy), prm, length(prm), h))
     end
-    return SystemMatrix(fetch(h[], 3problem.non), problem)
+    return SystemMatrix(fetch(h[], 3problem.non, pat), problem)
 end
 
 function internalForceVector(problem; P=nothing, F=nothing, energy=nothing, params=nothing)
@@ -317,14 +356,14 @@ function solveField(K::SystemMatrix, f; support=BoundaryCondition[], iterative=f
     LowLevelFEM.applyBoundaryConditions!(u, support)
     fixed = zeros(UInt8, n)
     fixed[LowLevelFEM.constrainedDoFs(problem, support)] .= 1
-    hm = upload(K)
+    hm, owned = device_matrix(K)
     x = vec(u.a[:, 1]); its = Ref{Int64}(0); rr = Ref{Float64}(0.0)
     prec = iterative ? (preconditioner === nothing ? 0 : 1) : 2
     tol = iterative ? reltol : 1e-13
     st = ccall((:llf_pcg, LIB), Cint,
                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{UInt8}, Cint, Float64, Int64, Ref{Int64}, Ref{Float64}),
                ctx(), hm, vec(f.a[:, 1]), x, fixed, prec, tol, iterative ? maxiter : 20n, its, rr)
-    ccall((:llf_matrix_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), hm)
+    owned && ccall((:llf_matrix_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), hm)
     (st == 0 || (iterative && st == -4)) || check(st)
     u.a[:, 1] .= x
     return u
@@ -356,37 +395,62 @@ function FDM(K::SystemMatrix, C::SystemMatrix, q::ScalarField, bc, TT0::ScalarFi
     LowLevelFEM.applyBoundaryConditions!(TT, bc)
     fixed = zeros(UInt8, nd)
     fixed[LowLevelFEM.constrainedDoFs(problem, bc)] .= 1
-    hK = upload(K); hC = upload(C)
+    (hK, oK) = device_matrix(K); (hC, oC) = device_matrix(C)
     qa = Matrix{Float64}(q.a)
     its = Ref{Int64}(0)
     st = ccall((:llf_heat_fdm, LIB), Cint,
                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Cint, Ptr{Float64}, Ptr{UInt8}, Int64, Float64,
                 Float64, Cint, Float64, Int64, Ref{Int64}),
                ctx(), hK, hC, qa, size(qa, 2), TT.a, fixed, n, Δt, ϑ, 2, 1e-13, 20nd, its)
-    ccall((:llf_matrix_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), hK)
-    ccall((:llf_matrix_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), hC)
+    oK && ccall((:llf_matrix_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), hK)
+    oC && ccall((:llf_matrix_destroy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx(), hC)
     check(st)
     return TT
 end
 
+# The device matrix of a SystemMatrix: the one kept when it was assembled
+# here (and is unchanged), else an upload.  Returns (handle, owned): an
+# owned handle is the caller's to destroy.
+function device_matrix(K::SystemMatrix)
+    pat = pattern(K.model, size(K.A, 1) == K.model.non ? 1 : K.model.pdim)
+    h = device_copy(K, pat)
+    h === nothing || return (h, false)
+    return (upload(K, pat), true)
+end
+
 # A host SystemMatrix re-enters the device through the structural pattern of
-# its problem: the values are scattered by row/column search on the host
-# side of Julia and uploaded as structural values.
-function upload(K::SystemMatrix)
-    problem = K.model
-    pat = pattern(problem)
-    nnz = Ref{Int64}(0); ndof = Ref{Int64}(0); pd = Ref{Cint}(0)
-    ccall((:llf_pattern_info, LIB), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}, Ref{Cint}), pat, ndof, nnz, pd)
-    colptr = Vector{Int64}(undef, ndof[] + 1); rowval = Vector{Int64}(undef, nnz[])
-    check(ccall((:llf_pattern_copy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Int64}, Ptr{Int64}), ctx(), pat, colptr, rowval))
-    S = SparseMatrixCSC(ndof[], ndof[], colptr, rowval, zeros(nnz[]))
+# its problem: per column, the stored rows (a sorted subset of the
+# structural rows, or the same set) are merged into the structural rows in
+# one pass, and the values go up as structural values.
+const STRUCT_ROWS = IdDict{Ptr{Cvoid},Tuple{Vector{Int64},Vector{Int64}}}()
+
+function upload(K::SystemMatrix, pat::Ptr{Cvoid})
+    colptr, rowval = get!(STRUCT_ROWS, pat) do
+        nnz = Ref{Int64}(0); ndof = Ref{Int64}(0); pd = Ref{Cint}(0)
+        ccall((:llf_pattern_info, LIB), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}, Ref{Cint}), pat, ndof, nnz, pd)
+        c = Vector{Int64}(undef, ndof[] + 1); r = Vector{Int64}(undef, nnz[])
+        check(ccall((:llf_pattern_copy, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Int64}, Ptr{Int64}), ctx(), pat, c, r))
+        (c, r)
+    end
     A = K.A
-    for j in 1:size(A, 2), p in nzrange(A, j)
-        S[rowvals(A)[p], j] = nonzeros(A)[p]
+    size(A, 2) == length(colptr) - 1 || error("LowLevelFEMGB300: matrix size does not match the problem's pattern")
+    vals = zeros(length(rowval))
+    Ar, Av, Ac = rowvals(A), nonzeros(A), SparseArrays.getcolptr(A)
+    @inbounds for j in 1:size(A, 2)
+        q = colptr[j]; qe = colptr[j+1]
+        for p in Ac[j]:(Ac[j+1]-1)
+            r = Ar[p]
+            while q < qe && rowval[q] < r
+                q += 1
+            end
+            (q < qe && rowval[q] == r) ||
+                error("LowLevelFEMGB300: entry ($r, $j) is outside the problem's structural pattern")
+            vals[q] = Av[p]
+        end
     end
     h = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:llf_matrix_from_structural, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ref{Ptr{Cvoid}}),
-                ctx(), pat, nonzeros(S), h))
+                ctx(), pat, vals, h))
     return h[]
 end
 
