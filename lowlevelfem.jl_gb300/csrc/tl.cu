@@ -814,6 +814,41 @@ int tl_tangent_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double
 
 // Tensor-core form of the consistent tangent (k_tl_points_tc + k_tl_tangent_tc,
 // then the FP32 element matrices summed in FP64 by the gather).
+namespace {
+// Exact symmetry of the tensor-core element matrices: the tiles above and
+// below the diagonal round their FP32 sums differently, so block (b,a) is
+// not quite block (a,b)^T.  Each mirrored pair of entries is replaced by
+// their mean, so the gathered tangent is symmetric bit for bit (CG relies
+// on it; unsymmetric rounding cost it about twice the iterations).  One
+// thread per element and node pair a <= b.
+__global__ void k_tc_symmetrize(float *__restrict__ Kf, int64_t nel, int npe, int64_t cs) {
+  constexpr int BSTR = kf_bstride(3, true, 4);
+  const int64_t npairs = (int64_t)npe * (npe + 1) / 2;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nel * npairs;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = t / npairs;
+    int p = (int)(t - e * npairs);
+    int a = 0;
+    while (p >= npe - a) {  // pair index -> (a, b >= a), row by row
+      p -= npe - a;
+      ++a;
+    }
+    const int b = a + p;
+    float *X = Kf + ((size_t)e * npe + b) * cs + (size_t)a * BSTR;  // block (a, b)
+    float *Y = Kf + ((size_t)e * npe + a) * cs + (size_t)b * BSTR;  // block (b, a)
+#pragma unroll
+    for (int ci = 0; ci < 3; ++ci)
+#pragma unroll
+      for (int cj = 0; cj < 3; ++cj) {
+        if (a == b && cj <= ci) continue;
+        const float m = (X[ci * 3 + cj] + Y[cj * 3 + ci]) * 0.5f;
+        X[ci * 3 + cj] = m;
+        Y[cj * 3 + ci] = m;
+      }
+  }
+}
+}  // namespace
+
 int tl_tangent_tc_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const double *d_F, int law,
                        const double *params, int nparams, llf_matrix *m) {
   if (mesh->dim != 3 || pat->pdim != 3)
@@ -872,6 +907,12 @@ int tl_tangent_tc_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, const dou
       e = cudaGetLastError();
       if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
     }
+  }
+  if (rc == LLF_OK && mesh->nel > 0) {
+    KernelScope ks(ctx, "k_tc_symmetrize");
+    k_tc_symmetrize<<<(unsigned)(ctx->num_sms * 16), 256, 0, s>>>(Kf, mesh->nel, npe, cs);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
   }
   if (rc == LLF_OK) {
     cudaError_t e = dalloc(ctx, &m->d_nz, pat->nnz);

@@ -190,6 +190,9 @@ def test_tensor_core_tangent_within_tf32x3_tolerance(llf, case):
     err = np.abs(a - b).max() / scale
     assert err <= 5e-5, err
     assert err > 0.0  # the tensor-core path really ran (TF32 splits are not bit-exact)
+    # mirrored entries are made equal, so the tangent is symmetric bit for bit
+    A = Ktc.A
+    assert abs(A - A.T).max() == 0.0
 
 
 @pytest.mark.parametrize("order,n", [(3, 2), (4, 2)], ids=["hex64", "hex125"])
