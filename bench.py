@@ -43,6 +43,7 @@ def workload_name(n):
 # k_colgather 338.2 MB, k_compact 417.5 MB
 NNZ_16CUBE = 19320201
 DRAM_BYTES_16CUBE = (1.324032 + 6.096128 + 158.8992 + 224.209664 + 114.00704 + 165.33248 + 252.210688) * 1e6
+DRAM_BYTES_ELEM_16CUBE = (6.096128 + 158.8992) * 1e6   # k_elem_fp64 alone
 
 
 def parse():
@@ -767,16 +768,24 @@ def main():
 
     # DRAM traffic of one FP64 assembly from ncu captures of its kernels on
     # hex27 16^3 (profiles/k_*_hex27_16cube.md), scaled by structural nnz
-    traffic = None
+    traffic = traffic_k = None
     if form == L.FP64 and ORDER == 2:
         traffic = DRAM_BYTES_16CUBE * nnz / NNZ_16CUBE
-    roofline = {"bound": "hbm", "kernel": "assembly (all kernels of one llf_assemble_stiffness)",
-                "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "peak_source": peak_kind, "traffic": traffic,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_affine_geometry, "
-                                  "k_elem_fp64, k_colgather, k_compact on hex27 16^3, scaled by structural nnz"
-                                  if traffic else None,
+        traffic_k = DRAM_BYTES_ELEM_16CUBE * nnz / NNZ_16CUBE if kname == "k_elem_fp64" else None
+    # the contract's figure: the assembly's algorithmic bytes over the
+    # dominant kernel's average launch; the whole assembly's figure beside it
+    achieved_k = bytes_alg / (k_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": kname,
+                "achieved": achieved_k, "peak": hbm_peak, "unit": "GB/s", "frac": achieved_k / hbm_peak,
+                "peak_source": peak_kind, "traffic": traffic_k,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_elem_fp64 on hex27 16^3 "
+                                  "(profiles/k_elem_fp64_hex27_16cube.md), scaled by structural nnz" if traffic_k else None,
                 "algorithmic_bytes": bytes_alg, "dominant_kernel": kname, "dominant_ms": k_ms,
+                "note": "the dominant kernel is bound by the FP64 pipe, not HBM: see fp64",
+                "assembly": {"kernels": "all kernels of one llf_assemble_stiffness", "ms": asm_ms,
+                             "achieved": achieved, "frac": achieved / hbm_peak, "traffic": traffic,
+                             "traffic_source": "ncu dram bytes of k_affine_geometry, k_elem_fp64, k_colgather, "
+                                               "k_compact on hex27 16^3, scaled by structural nnz" if traffic else None},
                 "per_kernel": per_kernel,
                 "fp64": {"element_kernel_flops": flops, "achieved_tflops": fp64_achieved,
                          "dgemm_peak_tflops_measured": fp64_peak,
