@@ -267,12 +267,14 @@ int llf_assemble_stiffness_csc(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
  * rowval is the structural rowval filtered by keep (llf_rowval_from_keep);
  * a caller that re-assembles the same operator keeps its previous rowval
  * while the keep bits do not change, so each call moves about half the
- * bytes of llf_assemble_stiffness_csc. */
+ * bytes of llf_assemble_stiffness_csc.  *keep_changed (may be NULL)
+ * receives 0 when the bits equal those of the previous values call on the
+ * same pattern (compared on the device), else 1. */
 int llf_assemble_stiffness_values(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat,
                                   int ptype, const double *E, const double *nu,
                                   int nmat, double thickness, int form,
                                   int64_t capacity, int64_t *colptr, double *nzval,
-                                  uint32_t *keep, int64_t *nnz);
+                                  uint32_t *keep, int64_t *nnz, int *keep_changed);
 
 /* Host only: the stored rowval from the structural rowval and the keep bits
  * of llf_assemble_stiffness_values; returns the stored count (or a negative

@@ -71,7 +71,7 @@ SIGNATURES = {
     "llf_pattern_destroy": (i32, [vp, vp]),
     "llf_autotune_stiffness": (i32, [vp, vp, vp, i32, P_dbl, P_dbl, i32, dbl, i32, i32, C.c_char_p, i64, P_i64]),
     "llf_assemble_stiffness_values": (i32, [vp, vp, vp, i32, P_dbl, P_dbl, i32, dbl, i32, i64, P_i64, P_dbl,
-                                            C.POINTER(C.c_uint32), P_i64]),
+                                            C.POINTER(C.c_uint32), P_i64, C.POINTER(i32)]),
     "llf_rowval_from_keep": (i64, [i64, P_i64, C.POINTER(C.c_uint32), P_i64]),
     "llf_assemble_stiffness": (i32, [vp, vp, vp, i32, P_dbl, P_dbl, i32, dbl, i32, PP]),
     "llf_assemble_mass": (i32, [vp, vp, vp, i32, P_dbl, i32, dbl, i32, i32, PP]),

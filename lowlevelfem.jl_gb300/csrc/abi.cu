@@ -509,6 +509,7 @@ int llf_pattern_destroy(llf_ctx *ctx, llf_pattern *p) {
     dfree(ctx, p->d_nadj); dfree(ctx, p->d_diagpos); dfree(ctx, p->d_colptr);
     dfree(ctx, p->d_pos);
     dfree(ctx, p->d_gather_nodes);
+    dfree(ctx, p->d_keep_prev);
     ic0_coloring_free(ctx, p);
     cudaStreamSynchronize(ctx->stream);
   }
@@ -603,7 +604,8 @@ int llf_assemble_stiffness_csc(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, i
 
 int llf_assemble_stiffness_values(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int ptype, const double *E,
                                   const double *nu, int nmat, double thickness, int form, int64_t capacity,
-                                  int64_t *colptr, double *nzval, uint32_t *keep, int64_t *nnz) {
+                                  int64_t *colptr, double *nzval, uint32_t *keep, int64_t *nnz,
+                                  int *keep_changed) {
   if (!ctx) return LLF_ERR_ARG;
   if (!valid_ptype(ptype) || ptype == LLF_HEAT_CONDUCTION || ptype == LLF_PLANE_HEAT_CONDUCTION)
     return llf_fail(ctx, LLF_ERR_ARG, "llf_assemble_stiffness_values: ptype must be SOLID, PLANE_STRESS or PLANE_STRAIN");
@@ -619,7 +621,7 @@ int llf_assemble_stiffness_values(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat
   std::vector<double> c1(nmat), c2(nmat);
   for (int i = 0; i < nmat; ++i) lame(ptype, E[i], nu[i], thickness, &c1[i], &c2[i]);
   rc = assemble_to_host_impl(ctx, mesh, pat, KIND_ELASTIC, c1.data(), c2.data(), nmat, form, capacity, colptr,
-                             nullptr, nzval, nnz, keep);
+                             nullptr, nzval, nnz, keep, keep_changed);
   return rc == LLF_OK ? llf_ok(ctx) : rc;
 }
 

@@ -581,6 +581,15 @@ __global__ void k_compact(const double *__restrict__ nz, const int64_t *__restri
   }
 }
 
+// Number of differing 32-bit words of two arrays (device counter).
+__global__ void k_words_differ(const unsigned *__restrict__ a, const unsigned *__restrict__ b, int64_t n,
+                               unsigned long long *cnt) {
+  unsigned long long c = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    c += a[i] != b[i];
+  if (c) atomicAdd(cnt, c);
+}
+
 __global__ void k_colptr_1based(const int64_t *__restrict__ in, int64_t n,
                                 int64_t *__restrict__ out) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -1092,6 +1101,7 @@ struct HostSlabSink : GatherSink {
   int64_t *h_colptr = nullptr, *h_rowval = nullptr;
   double *h_nzval = nullptr;
   unsigned *h_keep = nullptr;   // values-only form: keep bits instead of rowval
+  int keep_changed = 1;         // values-only form: the bits differ from the last call's on the pattern
   int64_t nnz = 0;
 
   template <class T>
@@ -1196,9 +1206,31 @@ struct HostSlabSink : GatherSink {
     // the keep bits once every slab is compacted (the words at slab edges
     // take bits from both neighbours)
     if (rc == LLF_OK && h_keep) {
-      e = cudaMemcpyAsync(h_keep, keep, sizeof(unsigned) * ((pat->nnz + 31) / 32), cudaMemcpyDeviceToHost, s);
+      const int64_t nw = (pat->nnz + 31) / 32;
+      unsigned long long *ndiff = nullptr;
+      unsigned long long hdiff = 1;
+      e = cudaMemcpyAsync(h_keep, keep, sizeof(unsigned) * nw, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess && pat->d_keep_prev) {   // compare with the last call's bits on the device
+        e = dalloc(ctx, &ndiff, 1);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ndiff, 0, sizeof(unsigned long long), s);
+        if (e == cudaSuccess) {
+          KernelScope ks(ctx, "k_words_differ");
+          k_words_differ<<<grid_1d(nw, 256, ctx->num_sms), 256, 0, s>>>(keep, pat->d_keep_prev, nw, ndiff);
+          e = cudaGetLastError();
+        }
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(&hdiff, ndiff, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+      }
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-      if (e != cudaSuccess) rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+      dfree(ctx, ndiff);
+      if (e != cudaSuccess) {
+        rc = llf_fail(ctx, LLF_ERR_CUDA, cudaGetErrorString(e));
+      } else {
+        keep_changed = hdiff != 0;
+        dfree(ctx, pat->d_keep_prev);   // this call's bits become the pattern's reference
+        pat->d_keep_prev = keep;
+        keep = nullptr;
+      }
     }
     if (cp) {
       cudaError_t e2 = cudaStreamSynchronize(cp);
@@ -1261,16 +1293,18 @@ struct HostSlabSink : GatherSink {
 
 int assemble_to_host_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, const double *c1,
                           const double *c2, int nmat, int form, int64_t capacity, int64_t *colptr,
-                          int64_t *rowval, double *nzval, int64_t *nnz, unsigned *keep) {
+                          int64_t *rowval, double *nzval, int64_t *nnz, unsigned *keep, int *keep_changed) {
   HostSlabSink sink;
   sink.capacity = capacity;
   sink.h_colptr = colptr;
   sink.h_rowval = rowval;
   sink.h_nzval = nzval;
   sink.h_keep = keep;
+  if (keep_changed) *keep_changed = 1;
   llf_matrix scratch;
   scratch.pat = pat;
   int rc = assemble_impl(ctx, mesh, pat, kind, LLF_SOLID, c1, c2, nmat, form, 0, &scratch, nullptr, &sink);
   if (rc == LLF_OK) *nnz = sink.nnz;
+  if (rc == LLF_OK && keep_changed) *keep_changed = sink.keep_changed;
   return rc;
 }

@@ -144,6 +144,9 @@ struct llf_pattern {
   // per column slab of the to-host assembly: one past the largest element
   // index that a node of this or an earlier slab touches (assemble.cu)
   std::vector<int64_t> slab_elem_end;
+  // keep bits of the last values-only assembly on this pattern (assemble.cu):
+  // the next one reports whether its bits differ
+  unsigned *d_keep_prev = nullptr;
 };
 
 struct llf_matrix {
@@ -231,7 +234,8 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
 // next slab is gathered and compacted (assemble.cu)
 int assemble_to_host_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, const double *c1,
                           const double *c2, int nmat, int form, int64_t capacity, int64_t *colptr,
-                          int64_t *rowval, double *nzval, int64_t *nnz, unsigned *keep = nullptr);
+                          int64_t *rowval, double *nzval, int64_t *nnz, unsigned *keep = nullptr,
+                          int *keep_changed = nullptr);
 // autotune.cu: the tuned schedule for a pattern's shape, if one is known
 // (in this process, or in the file LLF_TUNE_FILE names); applied at the
 // pattern's first assembly

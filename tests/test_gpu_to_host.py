@@ -62,11 +62,12 @@ def _values(llf, p, form):
     nzval = np.zeros(pat.nnz)
     keep = np.zeros((pat.nnz + 31) // 32, dtype=np.uint32)
     nnz = L.C.c_int64(0)
+    changed = L.C.c_int(-1)
     rc = L.lib().llf_assemble_stiffness_values(ctx.h, dm.h, pat.h, p.ptype, L.ptr(E, L.C.c_double),
                                                L.ptr(nu, L.C.c_double), len(E), p.thickness, form, pat.nnz,
                                                L.ptr(colptr, L.C.c_int64), L.ptr(nzval, L.C.c_double),
-                                               L.ptr(keep, L.C.c_uint32), L.C.byref(nnz))
-    return rc, colptr, nzval[:nnz.value], keep
+                                               L.ptr(keep, L.C.c_uint32), L.C.byref(nnz), L.C.byref(changed))
+    return rc, colptr, nzval[:nnz.value], keep, changed.value
 
 
 @pytest.mark.parametrize("case", [("box", 3, 2, False, "Solid"), ("box", 4, 2, True, "Solid"),
@@ -83,9 +84,10 @@ def test_values_and_keep_bits_give_the_csc(llf, case, precision):
     p = llf.Problem([llf.Material("body", E=2.1e5, nu=0.3)], type=pt, thickness=0.5)
     form = L.FP64 if precision == "fp64" else L.FP32Q
     sc, sr = p.pattern().copy()
-    for _ in range(2):
-        rc, c, v, keep = _values(llf, p, form)
+    for call in range(2):
+        rc, c, v, keep, changed = _values(llf, p, form)
         assert rc == 0
+        assert changed == (1 if call == 0 else 0)   # the second call's bits equal the first's
         gc, gr, gv = llf.stiffnessMatrix(p, precision=precision).csc()
         assert np.array_equal(c, gc) and np.array_equal(v, gv)
         rows = np.zeros(len(sr), dtype=np.int64)
