@@ -312,9 +312,11 @@ struct Ic0Factor {
   std::vector<int64_t> color_ptr;   // host: colour c = nodes [color_ptr[c], color_ptr[c+1]) of d_nodes
   const int16_t *d_color = nullptr; // per node (owned by the pattern)
   const int32_t *d_nodes = nullptr; // nodes sorted by colour (owned by the pattern)
-  double *Lrow = nullptr;           // L_jk with node j's list  (nnzb * P * P), FP64, during the factorisation
-  double *Lcol = nullptr;           // L_jk with node k's list  (nnzb * P * P)
-  double *Ldinv = nullptr;          // L_jj^-1 per node          (non * P * P)
+  // during the factorisation, in FP64 or (fp32) FP32:
+  void *Lrow = nullptr;             // L_jk with node j's list  (nnzb * P * P)
+  void *Lcol = nullptr;             // L_jk with node k's list  (nnzb * P * P)
+  void *Ldinv = nullptr;            // L_jj^-1 per node          (non * P * P)
+  bool fp32 = false;
   double shift = 0.0;               // diagonal shift the factorisation needed
   // FP32 factor for the solves, indexed by a node's position t in d_nodes
   // (colour order): the earlier neighbours fk[fptr[t]..] with blocks Lf

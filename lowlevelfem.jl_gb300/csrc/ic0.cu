@@ -30,6 +30,7 @@
 #include "common.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 namespace {
@@ -130,6 +131,21 @@ __device__ __forceinline__ double a_prime(const double *__restrict__ nz, int64_t
   return nz[(size_t)P * P * ci0 + (size_t)cc * P * degi + (size_t)P * ti + r];
 }
 
+// The factorisation's arithmetic in FT (FP64, or FP32 for the FP32 factor):
+// correctly rounded IEEE operations, no contraction.
+__device__ __forceinline__ double xfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float xfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double xsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float xsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double xmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double xsqrt(double a) { return __dsqrt_rn(a); }
+__device__ __forceinline__ float xsqrt(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ double xrcp(double a) { return __drcp_rn(a); }
+__device__ __forceinline__ float xrcp(float a) { return __frcp_rn(a); }
+
 // Factorisation of the nodes of one colour, a warp per node j.  The blocks
 // L_ji of row j are made in colour order of i (L_ji needs the L_jk of
 // colours before i's), a group of up to IcFac<P>::SLOTS neighbours i of one
@@ -150,14 +166,14 @@ struct IcFac {
   static constexpr int SLOTS = 32 / PP < 8 ? 32 / PP : 8;  // pairs per group
 };
 
-template <int P>
+template <int P, class FT>
 __global__ void __launch_bounds__(IC_THREADS)
 k_ic0_factor(const int32_t *__restrict__ nodes, const int64_t *__restrict__ fptr, const int32_t *__restrict__ fk,
              const int32_t *__restrict__ fsrc, const int32_t *__restrict__ fcol, int count, int max_deg,
              const int64_t *__restrict__ nptr, const int32_t *__restrict__ nadj,
              const int32_t *__restrict__ diagpos, const int16_t *__restrict__ color, const double *__restrict__ nz,
-             const uint8_t *__restrict__ fixed, double shift, double *__restrict__ Lrow,
-             double *__restrict__ Lcol, double *__restrict__ Ldinv, int *fail) {
+             const uint8_t *__restrict__ fixed, double shift, FT *__restrict__ Lrow,
+             FT *__restrict__ Lcol, FT *__restrict__ Ldinv, int *fail) {
   constexpr int PP = P * P, NS = IcFac<P>::SLOTS;
   extern __shared__ int16_t ic_fac_smem[];  // per warp: NS lists of max_deg (u, v) pairs
   __shared__ int s_nm[IC_THREADS / 32][NS], s_tj[IC_THREADS / 32][NS];
@@ -212,7 +228,7 @@ k_ic0_factor(const int32_t *__restrict__ nodes, const int64_t *__restrict__ fptr
       const bool act = slot < n;
       int64_t i = 0, ci0 = 0;
       int degi = 0, tj = -1, t = 0;
-      double S = 0.0;
+      FT S = 0;
       if (act) {
         const int32_t q = fcol[p + slot];
         i = fk[q];
@@ -222,18 +238,18 @@ k_ic0_factor(const int32_t *__restrict__ nodes, const int64_t *__restrict__ fptr
         tj = s_tj[wib][slot];
         const int nm = s_nm[wib][slot];
         for (int h = 0; h < nm; ++h) {
-          const double *Ljk = Lrow + (size_t)(c0 + mu[slot * max_deg + h]) * PP + ea * P;
-          const double *Lik = Lrow + (size_t)(ci0 + mv[slot * max_deg + h]) * PP + eb * P;
+          const FT *Ljk = Lrow + (size_t)(c0 + mu[slot * max_deg + h]) * PP + ea * P;
+          const FT *Lik = Lrow + (size_t)(ci0 + mv[slot * max_deg + h]) * PP + eb * P;
 #pragma unroll
-          for (int m = 0; m < P; ++m) S = __fma_rn(Ljk[m], Lik[m], S);
+          for (int m = 0; m < P; ++m) S = xfma(Ljk[m], Lik[m], S);
         }
       }
-      const double Bm = act && tj >= 0 ? __dsub_rn(a_prime<P>(nz, ci0, degi, tj, ea, eb, j, i, fixed), S) : 0.0;
-      double X = 0.0;
+      const FT Bm = act && tj >= 0 ? xsub((FT)a_prime<P>(nz, ci0, degi, tj, ea, eb, j, i, fixed), S) : (FT)0;
+      FT X = 0;
 #pragma unroll
       for (int m = 0; m < P; ++m) {
-        const double bm = __shfl_sync(0xffffffffu, Bm, (slot * PP + ea * P + m) & 31);  // entry (ea, m)
-        if (act) X = __fma_rn(bm, Ldinv[(size_t)i * PP + eb * P + m], X);
+        const FT bm = __shfl_sync(0xffffffffu, Bm, (slot * PP + ea * P + m) & 31);  // entry (ea, m)
+        if (act) X = xfma(bm, Ldinv[(size_t)i * PP + eb * P + m], X);
       }
       if (act) {
         if (tj < 0) {  // the node pattern is symmetric; a miss means corrupt input
@@ -247,76 +263,76 @@ k_ic0_factor(const int32_t *__restrict__ nodes, const int64_t *__restrict__ fptr
       p += n;
     }
     // diagonal block
-    double D[P][P];
+    FT D[P][P];
 #pragma unroll
     for (int a = 0; a < P; ++a)
 #pragma unroll
-      for (int b = 0; b < P; ++b) D[a][b] = 0.0;
+      for (int b = 0; b < P; ++b) D[a][b] = 0;
     for (int t = lane; t < deg; t += 32) {
       const int32_t k = rj[t];
       if (color[k] >= cj) continue;
-      const double *Ljk = Lrow + (size_t)(c0 + t) * PP;
+      const FT *Ljk = Lrow + (size_t)(c0 + t) * PP;
 #pragma unroll
       for (int a = 0; a < P; ++a)
 #pragma unroll
         for (int b = 0; b < P; ++b)
 #pragma unroll
-          for (int m = 0; m < P; ++m) D[a][b] = __fma_rn(Ljk[a * P + m], Ljk[b * P + m], D[a][b]);
+          for (int m = 0; m < P; ++m) D[a][b] = xfma(Ljk[a * P + m], Ljk[b * P + m], D[a][b]);
     }
 #pragma unroll
     for (int a = 0; a < P; ++a)
 #pragma unroll
       for (int b = 0; b < P; ++b)
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) D[a][b] = __dadd_rn(D[a][b], __shfl_xor_sync(0xffffffffu, D[a][b], off));
+        for (int off = 16; off > 0; off >>= 1) D[a][b] = xadd(D[a][b], __shfl_xor_sync(0xffffffffu, D[a][b], off));
     if (lane == 0) {
       const int dp = diagpos[j];
-      double Aj[P][P];
+      FT Aj[P][P];
 #pragma unroll
       for (int a = 0; a < P; ++a)
 #pragma unroll
         for (int b = 0; b < P; ++b) {
-          double v = dp >= 0 ? a_prime<P>(nz, c0, deg, dp, a, b, j, j, fixed) : (a == b ? 1.0 : 0.0);
-          if (a == b) v = __dmul_rn(v, 1.0 + shift);
-          Aj[a][b] = __dsub_rn(v, D[a][b]);
+          FT v = (FT)(dp >= 0 ? a_prime<P>(nz, c0, deg, dp, a, b, j, j, fixed) : (a == b ? 1.0 : 0.0));
+          if (a == b) v = xmul(v, (FT)(1.0 + shift));
+          Aj[a][b] = xsub(v, D[a][b]);
         }
       // Cholesky Aj = L L^T, then L^-1 (both lower)
-      double L[P][P], Li[P][P];
+      FT L[P][P], Li[P][P];
       bool ok = true;
 #pragma unroll
       for (int a = 0; a < P; ++a)
 #pragma unroll
-        for (int b = 0; b < P; ++b) { L[a][b] = 0.0; Li[a][b] = 0.0; }
+        for (int b = 0; b < P; ++b) { L[a][b] = 0; Li[a][b] = 0; }
 #pragma unroll
       for (int b = 0; b < P; ++b) {
-        double d = Aj[b][b];
+        FT d = Aj[b][b];
 #pragma unroll
-        for (int m = 0; m < b; ++m) d = __fma_rn(-L[b][m], L[b][m], d);
-        if (!(d > 0.0)) { ok = false; d = 1.0; }
-        const double lb = __dsqrt_rn(d);
+        for (int m = 0; m < b; ++m) d = xfma(-L[b][m], L[b][m], d);
+        if (!(d > (FT)0)) { ok = false; d = 1; }
+        const FT lb = xsqrt(d);
         L[b][b] = lb;
-        const double rl = __drcp_rn(lb);
+        const FT rl = xrcp(lb);
 #pragma unroll
         for (int a = b + 1; a < P; ++a) {
-          double v = Aj[a][b];
+          FT v = Aj[a][b];
 #pragma unroll
-          for (int m = 0; m < b; ++m) v = __fma_rn(-L[a][m], L[b][m], v);
-          L[a][b] = __dmul_rn(v, rl);
+          for (int m = 0; m < b; ++m) v = xfma(-L[a][m], L[b][m], v);
+          L[a][b] = xmul(v, rl);
         }
       }
 #pragma unroll
       for (int b = 0; b < P; ++b) {
-        Li[b][b] = __drcp_rn(L[b][b]);
+        Li[b][b] = xrcp(L[b][b]);
 #pragma unroll
         for (int a = b + 1; a < P; ++a) {
-          double v = 0.0;
+          FT v = 0;
 #pragma unroll
-          for (int m = b; m < a; ++m) v = __fma_rn(L[a][m], Li[m][b], v);
-          Li[a][b] = __dmul_rn(-v, __drcp_rn(L[a][a]));
+          for (int m = b; m < a; ++m) v = xfma(L[a][m], Li[m][b], v);
+          Li[a][b] = xmul(-v, xrcp(L[a][a]));
         }
       }
       if (!ok) atomicOr((unsigned *)fail, 1u);
-      double *ld = Ldinv + (size_t)j * PP;
+      FT *ld = Ldinv + (size_t)j * PP;
 #pragma unroll
       for (int a = 0; a < P; ++a)
 #pragma unroll
@@ -387,7 +403,8 @@ __global__ void k_ic0_by_color(const int32_t *__restrict__ nodes, const int32_t 
 
 // FP32 copies of the factor in packed order (blocks of L with the forward
 // and backward lists, and L_jj^-1).
-__global__ void k_ic0_pack(const double *__restrict__ src, const int32_t *__restrict__ idx, int64_t count, int pp,
+template <class FT>
+__global__ void k_ic0_pack(const FT *__restrict__ src, const int32_t *__restrict__ idx, int64_t count, int pp,
                            float *__restrict__ dst) {
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < count * pp;
        t += (int64_t)gridDim.x * blockDim.x) {
@@ -537,8 +554,8 @@ static int ic0_coloring(llf_ctx *ctx, llf_pattern *pat, const std::vector<int64_
   return LLF_OK;
 }
 
-template <int P>
-static int ic0_factor_t(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixed,
+template <int P, class FT>
+static int ic0_factor_tt(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixed,
                         const std::vector<int64_t> &seg_nodes, const int32_t *d_node_seg, Ic0Factor *f) {
   const llf_pattern *pat = m->pat;
   const int64_t non = pat->mesh->non;
@@ -550,9 +567,14 @@ static int ic0_factor_t(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixe
   f->color_ptr = cl->ptr;
   f->d_color = cl->d_color;
   f->d_nodes = cl->d_nodes;
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &f->Lrow, (size_t)pat->nnzb * P * P));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &f->Lcol, (size_t)pat->nnzb * P * P));
-  LLF_CUDA_TRY(ctx, dalloc(ctx, &f->Ldinv, (size_t)non * P * P));
+  FT *Lrow = nullptr, *Lcol = nullptr, *Ldinv = nullptr;
+  f->fp32 = sizeof(FT) == sizeof(float);
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &Lrow, (size_t)pat->nnzb * P * P));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &Lcol, (size_t)pat->nnzb * P * P));
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &Ldinv, (size_t)non * P * P));
+  f->Lrow = Lrow;
+  f->Lcol = Lcol;
+  f->Ldinv = Ldinv;
   int *d_fail = nullptr;
   LLF_CUDA_TRY(ctx, dalloc(ctx, &d_fail, 1));
   // the factorisation's per-warp match lists: NS x max_deg (u, v) pairs of int16
@@ -566,18 +588,18 @@ static int ic0_factor_t(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixe
   int fail = 1;
   for (double shift : shifts) {
     LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_fail, 0, sizeof(int), s));
-    LLF_CUDA_TRY(ctx, cudaMemsetAsync(f->Lrow, 0, sizeof(double) * pat->nnzb * P * P, s));
-    LLF_CUDA_TRY(ctx, cudaMemsetAsync(f->Lcol, 0, sizeof(double) * pat->nnzb * P * P, s));
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(Lrow, 0, sizeof(FT) * pat->nnzb * P * P, s));
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(Lcol, 0, sizeof(FT) * pat->nnzb * P * P, s));
     for (int c = 0; c < cl->ncolors; ++c) {
       const int count = (int)(cl->ptr[c + 1] - cl->ptr[c]);
       if (count == 0) continue;
       const unsigned grid = (unsigned)std::max<int64_t>(
           1, std::min<int64_t>((count + fwpb - 1) / fwpb, (int64_t)ctx->num_sms * 32));
       KernelScope ks(ctx, "k_ic0_factor");
-      k_ic0_factor<P><<<grid, 32 * fwpb, fsmem, s>>>(cl->d_nodes + cl->ptr[c], cl->d_fptr + cl->ptr[c], cl->d_fk,
+      k_ic0_factor<P, FT><<<grid, 32 * fwpb, fsmem, s>>>(cl->d_nodes + cl->ptr[c], cl->d_fptr + cl->ptr[c], cl->d_fk,
                                                      cl->d_fsrc, cl->d_fcol, count, md, pat->d_nptr, pat->d_nadj,
-                                                     pat->d_diagpos, cl->d_color, m->d_nz, d_fixed, shift, f->Lrow,
-                                                     f->Lcol, f->Ldinv, d_fail);
+                                                     pat->d_diagpos, cl->d_color, m->d_nz, d_fixed, shift, Lrow,
+                                                     Lcol, Ldinv, d_fail);
     }
     LLF_CUDA_TRY(ctx, cudaGetLastError());
     LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&fail, d_fail, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -598,24 +620,37 @@ static int ic0_factor_t(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixe
   const unsigned gp = (unsigned)(ctx->num_sms * 16);
   {
     KernelScope ks(ctx, "k_ic0_pack");
-    k_ic0_pack<<<gp, 256, 0, s>>>(f->Lrow, cl->d_fsrc, cl->nf, P * P, f->Lf);
-    k_ic0_pack<<<gp, 256, 0, s>>>(f->Lcol, cl->d_bsrc, cl->nb, P * P, f->Lb);
-    k_ic0_pack<<<gp, 256, 0, s>>>(f->Ldinv, cl->d_nodes, non, P * P, f->Ldf);
+    k_ic0_pack<FT><<<gp, 256, 0, s>>>(Lrow, cl->d_fsrc, cl->nf, P * P, f->Lf);
+    k_ic0_pack<FT><<<gp, 256, 0, s>>>(Lcol, cl->d_bsrc, cl->nb, P * P, f->Lb);
+    k_ic0_pack<FT><<<gp, 256, 0, s>>>(Ldinv, cl->d_nodes, non, P * P, f->Ldf);
     k_ic0_by_color<<<gp, 256, 0, s>>>(cl->d_nodes, d_node_seg, non, f->segc);
   }
   LLF_CUDA_TRY(ctx, cudaGetLastError());
-  dfree(ctx, f->Lrow);
-  dfree(ctx, f->Lcol);
-  dfree(ctx, f->Ldinv);
+  dfree(ctx, Lrow);
+  dfree(ctx, Lcol);
+  dfree(ctx, Ldinv);
+  f->Lrow = f->Lcol = f->Ldinv = nullptr;
   return LLF_OK;
+}
+
+// The factor's arithmetic: FP64, or FP32 when LLF_IC0_FP32=1 (the factor is
+// applied in FP32 in either case; the FP32 factorisation runs on the FP32
+// pipe instead of GB300's narrow FP64 one).
+static bool ic0_fp32_factor() {
+  const char *e = getenv("LLF_IC0_FP32");
+  return e && e[0] == '1';
 }
 
 int ic0_factor(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixed, const std::vector<int64_t> &seg_nodes,
                const int32_t *d_node_seg, Ic0Factor *f) {
-  switch (m->pat->pdim) {
-    case 1: return ic0_factor_t<1>(ctx, m, d_fixed, seg_nodes, d_node_seg, f);
-    case 2: return ic0_factor_t<2>(ctx, m, d_fixed, seg_nodes, d_node_seg, f);
-    case 3: return ic0_factor_t<3>(ctx, m, d_fixed, seg_nodes, d_node_seg, f);
+  const bool f32 = ic0_fp32_factor();
+  switch (m->pat->pdim * 2 + (f32 ? 1 : 0)) {
+    case 2: return ic0_factor_tt<1, double>(ctx, m, d_fixed, seg_nodes, d_node_seg, f);
+    case 3: return ic0_factor_tt<1, float>(ctx, m, d_fixed, seg_nodes, d_node_seg, f);
+    case 4: return ic0_factor_tt<2, double>(ctx, m, d_fixed, seg_nodes, d_node_seg, f);
+    case 5: return ic0_factor_tt<2, float>(ctx, m, d_fixed, seg_nodes, d_node_seg, f);
+    case 6: return ic0_factor_tt<3, double>(ctx, m, d_fixed, seg_nodes, d_node_seg, f);
+    case 7: return ic0_factor_tt<3, float>(ctx, m, d_fixed, seg_nodes, d_node_seg, f);
   }
   return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
 }
