@@ -64,7 +64,8 @@ def parse():
                     help="batched: CG precision (mixed: FP32 iterations, 1.1-1.7x the FP64 products here)")
     ap.add_argument("--batched-reltol", type=float, default=1e-10, help="batched: CG relative residual")
     ap.add_argument("--group-nnz", type=float, default=1.5e9,
-                    help="batched: structural entries admitted to the GPU at a time")
+                    help="batched: structural entries of one group")
+    ap.add_argument("--streams", type=int, default=2, help="batched: groups in flight (one CUDA stream each)")
     ap.add_argument("--requests", type=int, default=200, help="serving: requests of the Poisson stream")
     ap.add_argument("--workers", type=int, default=8,
                     help="serving: preparation threads (engine) or solver workers (pool)")
@@ -334,21 +335,31 @@ def run_batched(args, llf):
     for g in groups:
         batch, noff = llf.concat_meshes([inst[k][0] for k in g])
         mats = [llf.Material(f"body#{i}", E=inst[k][1], nu=inst[k][2]) for i, k in enumerate(g)]
-        P = llf.Problem(mats, type="Solid", mesh=batch)
+        # each group on a context (CUDA stream) of its own, so that groups on
+        # different streams overlap (one group's assembly and factorisation
+        # with another's CG)
+        P = llf.Problem(mats, type="Solid", mesh=batch, device=0 if args.streams > 1 else None)
         f = llf.loadVector(P, [llf.load(f"right#{i}", fx=1.0) for i in range(len(g))])
         sup = [llf.displacementConstraint(f"left#{i}", ux=0, uy=0, uz=0) for i in range(len(g))]
         P.pattern()
         built.append((g, P, f, sup, noff))
 
+    def run_group(item):
+        g, P, f, sup, noff = item
+        K = llf.stiffnessMatrix(P, precision=form)
+        u = llf.solveFieldBatched(K, f, support=sup, node_offsets=noff, preconditioner=prec, reltol=reltol,
+                                  precision="mixed" if mixed else "fp64")
+        del K
+        return (u, None)
+
     def one_pass(keep=False):
-        out = []
-        for g, P, f, sup, noff in built:
-            K = llf.stiffnessMatrix(P, precision=form)
-            u = llf.solveFieldBatched(K, f, support=sup, node_offsets=noff, preconditioner=prec, reltol=reltol,
-                                      precision="mixed" if mixed else "fp64")
-            out.append((u, K if keep else None))
-            del K
-        return out
+        if args.streams <= 1:
+            return [run_group(item) for item in built]
+        # args.streams groups in flight, each on its own stream (threads: the
+        # library calls release the interpreter)
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(max_workers=args.streams) as ex:
+            return list(ex.map(run_group, built))
 
     times = []
     res = None
@@ -441,6 +452,7 @@ def run_batched(args, llf):
             "data": f"synthetic: seeded tet10 boxes ({len(inst)} of the 512-instance workload)",
             "config": {"workload": f"batched-tet10-{len(inst)}", "instances": len(inst), "elements": nel,
                        "dofs": int(3 * sum(sizes)), "groups": len(groups), "group_nnz_budget": args.group_nnz,
+                       "groups_in_flight": args.streams,
                        "structural_nnz": int(sum(P.pattern().nnz for _, P, *_ in built)), "precond": prec,
                        "reltol": reltol, "assembly": form, "solve": args.batched_solve},
             "cg_iterations": {"min": int(its.min()), "median": float(np.median(its)), "max": int(its.max())},
@@ -919,7 +931,7 @@ def main():
         try:
             bargs = _ap.Namespace(**{**vars(args), "instances": 16, "steps": 1, "warmup": 1, "no_plain": False,
                                      "precond": None, "batched_form": "fp64", "batched_solve": "fp64",
-                                     "batched_reltol": 1e-10, "group_nnz": 1.5e9})
+                                     "batched_reltol": 1e-10, "group_nnz": 1.5e9, "streams": 2})
             r = run_batched(bargs, llf)
             samples["batched"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "dtype", "config", "cg_iterations",
                                                     "rel_err_vs_direct", "max_rel_err_vs_direct", "plain_gpu")

@@ -633,12 +633,13 @@ static int ic0_factor_tt(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fix
   return LLF_OK;
 }
 
-// The factor's arithmetic: FP64, or FP32 when LLF_IC0_FP32=1 (the factor is
-// applied in FP32 in either case; the FP32 factorisation runs on the FP32
-// pipe instead of GB300's narrow FP64 one).
+// The factor's arithmetic: FP32 (FP64 when LLF_IC0_FP32=0).  The factor is
+// applied in FP32 either way; the FP32 factorisation runs on the FP32 pipe
+// instead of GB300's narrow FP64 one (the 512-instance batch: the same CG
+// iteration counts, 22.5 -> 22.8 solves/s).
 static bool ic0_fp32_factor() {
   const char *e = getenv("LLF_IC0_FP32");
-  return e && e[0] == '1';
+  return !(e && e[0] == '0');
 }
 
 int ic0_factor(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixed, const std::vector<int64_t> &seg_nodes,
