@@ -63,9 +63,9 @@ def parse():
     ap.add_argument("--batched-solve", default="fp64", choices=["fp64", "mixed"],
                     help="batched: CG precision (mixed: FP32 iterations, 1.1-1.7x the FP64 products here)")
     ap.add_argument("--batched-reltol", type=float, default=1e-10, help="batched: CG relative residual")
-    ap.add_argument("--group-nnz", type=float, default=1.5e9,
+    ap.add_argument("--group-nnz", type=float, default=1.0e9,
                     help="batched: structural entries of one group")
-    ap.add_argument("--streams", type=int, default=2, help="batched: groups in flight (one CUDA stream each)")
+    ap.add_argument("--streams", type=int, default=3, help="batched: groups in flight (one CUDA stream each)")
     ap.add_argument("--requests", type=int, default=200, help="serving: requests of the Poisson stream")
     ap.add_argument("--workers", type=int, default=8,
                     help="serving: preparation threads (engine) or solver workers (pool)")
@@ -931,7 +931,7 @@ def main():
         try:
             bargs = _ap.Namespace(**{**vars(args), "instances": 16, "steps": 1, "warmup": 1, "no_plain": False,
                                      "precond": None, "batched_form": "fp64", "batched_solve": "fp64",
-                                     "batched_reltol": 1e-10, "group_nnz": 1.5e9, "streams": 2})
+                                     "batched_reltol": 1e-10, "group_nnz": 1.0e9, "streams": 3})
             r = run_batched(bargs, llf)
             samples["batched"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "dtype", "config", "cg_iterations",
                                                     "rel_err_vs_direct", "max_rel_err_vs_direct", "plain_gpu")
