@@ -62,8 +62,11 @@ __host__ __device__ constexpr int sym_l(int n) {
 // oracle's orc_is_affine / orc_geom at point 0): J0 = fma chain over nodes of
 // X_a,i dN0_a,j; s = max |X|; the element is affine when every node satisfies
 // |X_a - X_0 - J0 (xi_a - xi_0)| <= 2^-46 s componentwise (fma chain over j)
-// and s > 0.  For affine elements geo[e*10 + 0..8] = invJ (row-major) and
-// geo[e*10 + 9] = det; flag[e] = 1.  Elements with a negative material index
+// and s > 0.  When every off-diagonal entry of J0 is within the same
+// tolerance the element is an axis-aligned brick and those entries are set
+// to +0.0 before the inverse (oracle: orc_geom_affine).  For affine elements
+// geo[e*10 + 0..8] = invJ (row-major) and geo[e*10 + 9] = det; flag[e] = 2
+// for axis-aligned ones, else 1.  Elements with a negative material index
 // get flag 0.
 template <int DIM>
 __global__ void k_affine_geometry(const double *__restrict__ xyz, const int32_t *__restrict__ conn,
@@ -100,12 +103,28 @@ __global__ void k_affine_geometry(const double *__restrict__ xyz, const int32_t 
         }
       }
       if (ok) {
+        // axis-aligned up to the rounding of the sums: the off-diagonal
+        // entries become +0.0, so every coefficient mixing two axes is an
+        // exact zero (flag 2 selects the element kernels' reduced form)
+        bool aligned = true;
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j)
+            if (i != j && !(fabs(J[i][j]) <= tol)) aligned = false;
+        if (aligned) {
+#pragma unroll
+          for (int i = 0; i < DIM; ++i)
+#pragma unroll
+            for (int j = 0; j < DIM; ++j)
+              if (i != j) J[i][j] = 0.0;
+        }
         double inv[9];
         const double det = jac_inverse<DIM>(J, inv);
 #pragma unroll
         for (int k = 0; k < 9; ++k) geo[e * 10 + k] = inv[k];
         geo[e * 10 + 9] = det;
-        f = 1;
+        f = aligned ? 2 : 1;
       }
     }
     flag[e] = f;

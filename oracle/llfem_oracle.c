@@ -228,11 +228,46 @@ void orc_affine_split(int dim, const double *Rab, double *sv, double *av) {
   }
 }
 
+/* Geometry of an affine element: J0 as the geometry contract at point 0;
+ * when every off-diagonal entry of J0 is within the affinity tolerance
+ * (|J0_ij| <= 64 eps s, s the largest |X| of the element) the element is an
+ * axis-aligned brick up to the rounding of the sums, and those entries are
+ * set to +0.0 before the inverse, so that invJ and every coefficient below
+ * that mixes two axes are exact zeros.  Returns det. */
+static double orc_geom_affine(int dim, int npe, const double *X, const double *dN0, double inv[9]) {
+  double J[3][3] = {{0}};
+  for (int i = 0; i < dim; ++i)
+    for (int j = 0; j < dim; ++j) {
+      double acc = 0.0;
+      for (int a = 0; a < npe; ++a) acc = fma(X[3 * a + i], dN0[3 * a + j], acc);
+      J[i][j] = acc;
+    }
+  double s = 0.0;
+  for (int a = 0; a < npe; ++a)
+    for (int i = 0; i < dim; ++i) s = fmax(s, fabs(X[3 * a + i]));
+  const double tol = 64.0 * 2.220446049250313e-16 * s;
+  int al = 1;
+  for (int i = 0; i < dim; ++i)
+    for (int j = 0; j < dim; ++j)
+      if (i != j && !(fabs(J[i][j]) <= tol)) al = 0;
+  if (al)
+    for (int i = 0; i < dim; ++i)
+      for (int j = 0; j < dim; ++j)
+        if (i != j) J[i][j] = 0.0;
+  if (dim == 3) return orc_inv3(J, inv);
+  double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+  double rdet = 1.0 / det;
+  inv[0] = J[1][1] * rdet;   inv[1] = -J[0][1] * rdet; inv[2] = 0.0;
+  inv[3] = -J[1][0] * rdet;  inv[4] = J[0][0] * rdet;  inv[5] = 0.0;
+  inv[6] = 0.0; inv[7] = 0.0; inv[8] = 0.0;
+  return det;
+}
+
 static int orc_element_affine(int kind, int dim, int pdim, int npe, const double *dN0, const double *X,
                               const double *R, const double *Mref, double c1, double c2, double *Ke) {
   size_t nd = (size_t)pdim * npe;
   double inv[9];
-  double det = orc_geom(dim, npe, X, dN0, inv);
+  double det = orc_geom_affine(dim, npe, X, dN0, inv);
   if (!(det > 0.0)) return -1;
   const int ns = dim == 3 ? 6 : 3, na = dim == 3 ? 3 : 1;
   const int(*sym)[2] = dim == 3 ? ORC_SYM3 : ORC_SYM2;

@@ -221,6 +221,54 @@ def test_distorted_mesh_bit_identical(llf, orc, case, part):
                          f"H {_ids(case)} {part}")
 
 
+def _turned(xyz, d, angle):
+    """xyz turned by angle about (1, 2, 3) (3D) or the z axis (2D) through
+    the centre of the unit cell."""
+    if d == 3:
+        ax = np.array([1.0, 2.0, 3.0]) / np.sqrt(14.0)
+        K = np.array([[0, -ax[2], ax[1]], [ax[2], 0, -ax[0]], [-ax[1], ax[0], 0]])
+        R = np.eye(3) + np.sin(angle) * K + (1 - np.cos(angle)) * (K @ K)
+    else:
+        c, s = np.cos(angle), np.sin(angle)
+        R = np.array([[c, -s, 0.0], [s, c, 0.0], [0.0, 0.0, 1.0]])
+    out = (xyz - 0.5) @ R.T + 0.5
+    if d == 2:
+        out[:, 2] = xyz[:, 2]
+    return out
+
+
+AFFINE_CASES = [("box", 2, 2, False, "Solid"), ("box", 2, 1, True, "Solid"), ("rect", 3, 3, False, "PlaneStrain"),
+                ("rect", 2, 2, True, "PlaneStress")]
+
+
+@pytest.mark.parametrize("case", AFFINE_CASES, ids=_ids)
+@pytest.mark.parametrize("geometry", ["turned", "turned-1e-9", "turned-1e-15", "stretched"])
+def test_affine_geometry_forms_bit_identical(llf, orc, case, geometry):
+    """Affine elements that are axis-aligned bricks (stretched, or turned by
+    less than the rounding of their Jacobian) take the reduced node-pair
+    form, the others the full one; both are the oracle's bit for bit."""
+    kind, n, order, simplex, ptype = case
+    m = make_mesh(llf, kind, n, order, simplex)
+    d = m.dim
+    if geometry == "stretched":
+        m.xyz[:, :d] *= np.array([2.5, 0.75, 1.3])[:d]
+    else:
+        m.xyz[:] = _turned(m.xyz, d, {"turned": 0.3, "turned-1e-9": 1e-9, "turned-1e-15": 1e-15}[geometry])
+    mat = llf.Material("body", E=2.1e5, nu=0.3, rho=7.85e-9, k=45.0)
+    p = llf.Problem([mat], type=ptype, thickness=0.7)
+    assert_csc_identical(llf.stiffnessMatrix(p).csc(),
+                         oracle_operator(llf, orc, m, "stiffness", PT[ptype], mat, thickness=0.7).julia(),
+                         f"K {_ids(case)} {geometry}")
+    assert_csc_identical(llf.massMatrix(p, lumped=False).csc(),
+                         oracle_operator(llf, orc, m, "mass", PT[ptype], mat, thickness=0.7).julia(),
+                         f"M {_ids(case)} {geometry}")
+    hp = "HeatConduction" if d == 3 else "PlaneHeatConduction"
+    ph = llf.Problem([mat], type=hp, thickness=0.7)
+    assert_csc_identical(llf.heatConductionMatrix(ph).csc(),
+                         oracle_operator(llf, orc, m, "heat", PT[hp], mat, thickness=0.7).julia(),
+                         f"H {_ids(case)} {geometry}")
+
+
 # ---------------------------------------------------------------- error paths
 def test_inverted_element_is_an_error(llf):
     m = llf.structured_box_mesh(n=2, order=1)
