@@ -39,11 +39,12 @@ def workload_name(n):
     """The workload label for n cells per edge (the headline case is 40)."""
     return f"hooke3d-unit-cube-hex27-{n}x{n}x{n}"
 # ncu DRAM bytes (read + write) of one FP64 assembly of hex27 16^3 (19,320,201
-# structural nnz): k_affine_geometry 1.3 MB, k_elem_fp64 165.0 MB,
-# k_colgather 338.2 MB, k_compact 417.5 MB
+# structural nnz): k_affine_geometry 1.3 MB, k_elem_affine 153.8 MB (the
+# general-geometry k_elem_fp64 165.0 MB), k_colgather 338.2 MB, k_compact 417.5 MB
 NNZ_16CUBE = 19320201
-DRAM_BYTES_16CUBE = (1.324032 + 6.096128 + 158.8992 + 224.209664 + 114.00704 + 165.33248 + 252.210688) * 1e6
-DRAM_BYTES_ELEM_16CUBE = (6.096128 + 158.8992) * 1e6   # k_elem_fp64 alone
+KERNEL_DRAM_BYTES_16CUBE = {"k_affine_geometry": 1.324032e6, "k_elem_fp64": (6.096128 + 158.8992) * 1e6,
+                            "k_elem_affine": (0.392704 + 153.449984) * 1e6,
+                            "k_colgather": (224.209664 + 114.00704) * 1e6, "k_compact": (165.33248 + 252.210688) * 1e6}
 
 
 def parse():
@@ -165,22 +166,30 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------- workload
-def algorithmic(mesh, nnz):
+def algorithmic(mesh, nnz, aligned=True):
     """Algorithmic bytes of one assembly (structural nnz values written, node
     coordinates and connectivity read) and FP64 operations of the element
     kernel under the arithmetic contract (FMA = 2 flops).  Every element of
     the structured mesh passes the affinity test, so the count is the affine
     form's: affinity test, Jacobian inverse and per-element coefficients,
     then per node pair Ksym = W S (ns x ns FMA), Kanti = U A (na x na FMA,
-    a != b) and the 2 na additions that form the two off-diagonal halves."""
+    a != b) and the 2 na additions that form the two off-diagonal halves.
+    Its elements are axis-aligned bricks (aligned=True): W is then zero
+    outside its d x d diagonal-component block and its mixed diagonal, U is
+    diagonal, and the kernel performs d x d FMA plus 2 na products per pair
+    (the coefficients: 2 ns + 3 d + d (d - 1) + 2 na + d + 1 operations)."""
     npe, d = mesh.npe, 3
     ns, na = (6, 3) if d == 3 else (3, 1)
     bytes_ = 8 * nnz + 24 * mesh.non + 4 * npe * mesh.nel
     npairs = npe * (npe + 1) // 2
     test = 2 * d * d * npe + npe * d * (1 + 3 * d)
     inverse = 42
-    coeffs = 3 * ns * ns + (2 + 1) * ns * ns + d * ns * 2 + 5 * na * na + ns + 1
-    pairs = (npairs - npe) * (2 * ns * ns + 2 * na * na + 2 * na) + npe * 2 * ns * ns
+    if aligned:
+        coeffs = 2 * ns + 3 * d + d * (d - 1) + 2 * na + d + 1
+        pairs = (npairs - npe) * (2 * d * d + 2 * na + 2 * na) + npe * (2 * d * d + na)
+    else:
+        coeffs = 3 * ns * ns + (2 + 1) * ns * ns + d * ns * 2 + 5 * na * na + ns + 1
+        pairs = (npairs - npe) * (2 * ns * ns + 2 * na * na + 2 * na) + npe * 2 * ns * ns
     flops = mesh.nel * (test + inverse + coeffs + pairs)
     return bytes_, flops
 
@@ -752,7 +761,10 @@ def main():
     hbm_peak, peak_kind = peaks()
     # dominant kernel by summed device time in the timed region
     kname, kstat = max(prof.items(), key=lambda kv: kv[1]["ms"])
-    k_ms = kstat["ms"] / max(kstat["launches"], 1)
+    # per assembly: a kernel may launch more than once in one assembly (the
+    # gather runs one launch per column-degree class)
+    k_ms = kstat["ms"] / args.steps
+    k_launches = kstat["launches"] / args.steps
     per_kernel = {k: {"launches": v["launches"], "ms_per_launch": v["ms"] / max(v["launches"], 1),
                       "share": v["ms"] / sum(x["ms"] for x in prof.values())} for k, v in prof.items()}
     asm_ms = sum(v["ms"] for v in prof.values()) / args.steps
@@ -775,28 +787,36 @@ def main():
         del x
     except Exception:
         pass
-    elem_ms = prof.get("k_elem_fp64", {}).get("ms", 0.0) / max(prof.get("k_elem_fp64", {}).get("launches", 1), 1)
+    ek = prof.get("k_elem_affine") or prof.get("k_elem_fp64") or {}
+    elem_ms = ek.get("ms", 0.0) / max(ek.get("launches", 1), 1)
     fp64_achieved = flops / (elem_ms * 1e-3) / 1e12 if elem_ms > 0 else None
 
     # DRAM traffic of one FP64 assembly from ncu captures of its kernels on
     # hex27 16^3 (profiles/k_*_hex27_16cube.md), scaled by structural nnz
     traffic = traffic_k = None
     if form == L.FP64 and ORDER == 2:
-        traffic = DRAM_BYTES_16CUBE * nnz / NNZ_16CUBE
-        traffic_k = DRAM_BYTES_ELEM_16CUBE * nnz / NNZ_16CUBE if kname == "k_elem_fp64" else None
+        elem_k = "k_elem_affine" if "k_elem_affine" in prof else "k_elem_fp64"
+        known = [k for k in ("k_affine_geometry", elem_k, "k_colgather", "k_compact") if k in KERNEL_DRAM_BYTES_16CUBE]
+        if len(known) == 4:
+            traffic = sum(KERNEL_DRAM_BYTES_16CUBE[k] for k in known) * nnz / NNZ_16CUBE
+        if kname in KERNEL_DRAM_BYTES_16CUBE:
+            traffic_k = KERNEL_DRAM_BYTES_16CUBE[kname] * nnz / NNZ_16CUBE
     # the contract's figure: the assembly's algorithmic bytes over the
     # dominant kernel's average launch; the whole assembly's figure beside it
     achieved_k = bytes_alg / (k_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "kernel": kname,
                 "achieved": achieved_k, "peak": hbm_peak, "unit": "GB/s", "frac": achieved_k / hbm_peak,
                 "peak_source": peak_kind, "traffic": traffic_k,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_elem_fp64 on hex27 16^3 "
-                                  "(profiles/k_elem_fp64_hex27_16cube.md), scaled by structural nnz" if traffic_k else None,
+                "traffic_source": f"ncu dram__bytes_read.sum + dram__bytes_write.sum of {kname} on hex27 16^3 "
+                                  f"(profiles/{kname}*_hex27_16cube.md), scaled by structural nnz" if traffic_k else None,
                 "algorithmic_bytes": bytes_alg, "dominant_kernel": kname, "dominant_ms": k_ms,
-                "note": "the dominant kernel is bound by the FP64 pipe, not HBM: see fp64",
+                "dominant_launches_per_assembly": k_launches,
+                "note": ("the element kernel is bound by the FP64 pipe, not HBM: see fp64" if kname.startswith("k_elem")
+                         else "achieved = the assembly's algorithmic bytes over this kernel's time per assembly "
+                              "(all its launches); the element kernel's FP64 rate is under fp64"),
                 "assembly": {"kernels": "all kernels of one llf_assemble_stiffness", "ms": asm_ms,
                              "achieved": achieved, "frac": achieved / hbm_peak, "traffic": traffic,
-                             "traffic_source": "ncu dram bytes of k_affine_geometry, k_elem_fp64, k_colgather, "
+                             "traffic_source": "ncu dram bytes of k_affine_geometry, the element kernel, k_colgather, "
                                                "k_compact on hex27 16^3, scaled by structural nnz" if traffic else None},
                 "per_kernel": per_kernel,
                 "fp64": {"element_kernel_flops": flops, "achieved_tflops": fp64_achieved,

@@ -67,12 +67,13 @@ __host__ __device__ constexpr int sym_l(int n) {
 // to +0.0 before the inverse (oracle: orc_geom_affine).  For affine elements
 // geo[e*10 + 0..8] = invJ (row-major) and geo[e*10 + 9] = det; flag[e] = 2
 // for axis-aligned ones, else 1.  Elements with a negative material index
-// get flag 0.
+// get flag 0; the others with flag 0 are counted in *nonaffine (if given).
 template <int DIM>
 __global__ void k_affine_geometry(const double *__restrict__ xyz, const int32_t *__restrict__ conn,
                                   const int32_t *__restrict__ emat, int64_t nel, int npe,
                                   const double *__restrict__ dN0, const double *__restrict__ nref,
-                                  double *__restrict__ geo, uint8_t *__restrict__ flag) {
+                                  double *__restrict__ geo, uint8_t *__restrict__ flag,
+                                  unsigned long long *__restrict__ nonaffine) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nel;
        e += (int64_t)gridDim.x * blockDim.x) {
     uint8_t f = 0;
@@ -125,6 +126,8 @@ __global__ void k_affine_geometry(const double *__restrict__ xyz, const int32_t 
         for (int k = 0; k < 9; ++k) geo[e * 10 + k] = inv[k];
         geo[e * 10 + 9] = det;
         f = aligned ? 2 : 1;
+      } else if (nonaffine) {
+        atomicAdd(nonaffine, 1ull);
       }
     }
     flag[e] = f;
@@ -142,9 +145,8 @@ __device__ __forceinline__ void affine_stage(const double *geo_e, double c1, dou
 // W = Lame combination of V, U (antisymmetric congruence times c1 - c2),
 // c1*trV (heat) and c1*det (mass).
 template <int DIM>
-__device__ __forceinline__ void affine_coefficients(double *sAff, double c1, double c2) {
+__device__ __forceinline__ void affine_coefficients(double *sAff, double c1, double c2, int lane) {
   constexpr int NS = DIM == 3 ? 6 : 3, NA = DIM == 3 ? 3 : 1;
-  const int lane = threadIdx.x;
   const double *inv = sAff + AF_INV;
   const double det = sAff[AF_DET];
   for (int t = lane; t < NS * NS; t += 32) {
@@ -227,11 +229,48 @@ __device__ __forceinline__ void affine_coefficients32(const double *geo_e, doubl
 
 template <int DIM>
 __device__ __forceinline__ void affine_stage(const double *geo_e, double c1, double c2, double *sAff,
-                                             unsigned *status) {
-  if (threadIdx.x < 10) sAff[AF_INV + threadIdx.x] = geo_e[threadIdx.x];
+                                             unsigned *status, int lane) {
+  if (lane < 10) sAff[AF_INV + lane] = geo_e[lane];
   __syncwarp();
-  if (threadIdx.x == 0 && !(sAff[AF_DET] > 0.0)) atomicOr(status, ST_BAD_JACOBIAN);
-  affine_coefficients<DIM>(sAff, c1, c2);
+  if (lane == 0 && !(sAff[AF_DET] > 0.0)) atomicOr(status, ST_BAD_JACOBIAN);
+  affine_coefficients<DIM>(sAff, c1, c2, lane);
+}
+
+// The coefficients of an axis-aligned element (flag 2: invJ diagonal, its
+// other entries exact zeros; d_k = invJ[k][k]), by one warp (contract of
+// the oracle's orc_element_aligned): V_n = det (d_k d_l) for the symmetric
+// component n = (k,l); elasticity alpha_i = cp V_i, beta_i = c2 V_i (at
+// AF_W + i and AF_W + DIM + i), a_m = cp V_m, b_m = cm V_m for the mixed
+// components (at AF_W + 2 DIM + m and AF_W + 2 DIM + NA + m); heat
+// c1 trV_n = c1 V_n (n < DIM, the general form's value bit for bit: the
+// other terms of trV are exact zeros); mass c1 det.
+template <int DIM>
+__device__ __forceinline__ void affine_stage_aligned(const double *geo_e, double c1, double c2, double *sAff,
+                                                     unsigned *status, int lane) {
+  constexpr int NS = DIM == 3 ? 6 : 3, NA = DIM == 3 ? 3 : 1;
+  const double det = geo_e[9];
+  if (lane == 0) {
+    sAff[AF_DET] = det;
+    if (!(det > 0.0)) atomicOr(status, ST_BAD_JACOBIAN);
+  }
+  double *Vd = sAff + AF_V;   // V_n, n < NS
+  if (lane < NS) {
+    const int k = sym_k<DIM>(lane), l = sym_l<DIM>(lane);
+    Vd[lane] = __dmul_rn(det, __dmul_rn(geo_e[k * 3 + k], geo_e[l * 3 + l]));
+  }
+  __syncwarp();
+  const double cp = __dadd_rn(c1, c2), cm = __dsub_rn(c1, c2);
+  if (lane < DIM) {
+    sAff[AF_W + lane] = __dmul_rn(cp, Vd[lane]);
+    sAff[AF_W + DIM + lane] = __dmul_rn(c2, Vd[lane]);
+    sAff[AF_Q + lane] = __dmul_rn(c1, Vd[lane]);
+  } else if (lane < DIM + NA) {
+    const int m = lane - DIM;
+    sAff[AF_W + 2 * DIM + m] = __dmul_rn(cp, Vd[DIM + m]);
+    sAff[AF_W + 2 * DIM + NA + m] = __dmul_rn(cm, Vd[DIM + m]);
+  } else if (lane == DIM + NA) {
+    sAff[AF_M] = __dmul_rn(c1, det);
+  }
 }
 
 }  // namespace

@@ -52,6 +52,7 @@ struct ElemArgs {
   const uint8_t *aflag;
   const double *ageo, *Rp, *Mp;
   int cta_cap;               // host side: CTAs per SM at most (0: as many as fit)
+  bool all_affine;           // host side: k_affine_geometry counted no non-affine element
 };
 
 __device__ __forceinline__ int pair_offset(int a, int npe) {
@@ -107,17 +108,25 @@ __device__ __forceinline__ void store_pair(double *Ke, int64_t cs, int a, int b,
 // the symmetric part S (NS values) and antisymmetric part A (NA values) of
 // R_ab; elasticity Ksym = W S, Kanti = U A (a != b), heat (c1 trV) . S, mass
 // (c1 det) Mref_ab.
-// ALIGNED (axis-aligned elements, flag 2 of k_affine_geometry): W is zero
-// outside its diagonal-component block and its mixed diagonal, U and the
-// mixed part of c1 trV are zero or diagonal, all as exact zeros, and the
-// terms with a zero coefficient are left out of the fma chains.  A left-out
-// fma(+-0, s, acc) returns acc whenever acc is non-zero, so every block
-// value is the full chain's bit for bit, up to the sign of a zero result;
-// zeros are dropped from the stored CSC and add nothing to a non-zero sum,
-// so the stored matrix is the same.  Elasticity: 21 FP64 operations per
-// node pair in 3D instead of 51.
-template <int KIND, int DIM, int P, int BS, bool ALIGNED>
-__device__ __forceinline__ void affine_pairs(const ElemArgs &A, const double *sAff, double *Ke) {
+// ALIGNED (axis-aligned elements, flag 2 of k_affine_geometry, whose
+// coefficients affine_stage_aligned forms): elasticity through the
+// collapsed Lame combination of the oracle's orc_element_aligned, 15 FP64
+// operations per node pair in 3D instead of 51; heat leaves the mixed
+// components, whose coefficients are exact zeros there, out of its fma
+// chain (a left-out fma(+-0, s, acc) returns acc whenever acc is non-zero,
+// so the value is the full chain's up to the sign of a zero result, and
+// zeros are dropped from the stored CSC and add nothing to a non-zero sum).
+// Rp, Mp: the pair tables in global memory (read through the read-only
+// path) or, with TAB_SMEM, in shared memory.
+template <bool TAB_SMEM>
+__device__ __forceinline__ double ld_tab(const double *p) {
+  if (TAB_SMEM) return *p;
+  return __ldg(p);
+}
+
+template <int KIND, int DIM, int P, int BS, bool ALIGNED, bool TAB_SMEM = false>
+__device__ __forceinline__ void affine_pairs(const ElemArgs &A, const double *sAff, double *Ke,
+                                             const double *Rp, const double *Mp) {
   constexpr int NS = DIM == 3 ? 6 : 3, NA = DIM == 3 ? 3 : 1;
   const int npe = A.npe;
   if (KIND == KIND_MASS) {
@@ -126,22 +135,67 @@ __device__ __forceinline__ void affine_pairs(const ElemArgs &A, const double *sA
       int a, b;
       pair_decode(pi, npe, a, b);
       double blk[BS];
-      blk[0] = __dmul_rn(cm, __ldg(A.Mp + pi));
+      blk[0] = __dmul_rn(cm, ld_tab<TAB_SMEM>(Mp + pi));
       store_pair<P, BS>(Ke, A.colstride, a, b, blk);
     }
   } else if (KIND == KIND_HEAT) {
     double Q[NS];
 #pragma unroll
-    for (int n = 0; n < NS; ++n) Q[n] = sAff[AF_Q + n];
+    for (int n = 0; n < NS; ++n) Q[n] = (!ALIGNED || n < DIM) ? sAff[AF_Q + n] : 0.0;
     for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
       int a, b;
       pair_decode(pi, npe, a, b);
-      const double *sp = A.Rp + (size_t)pi * 9;
+      const double *sp = Rp + (size_t)pi * 9;
       double acc = 0.0;
 #pragma unroll
-      for (int n = 0; n < (ALIGNED ? DIM : NS); ++n) acc = __fma_rn(Q[n], __ldg(sp + n), acc);
+      for (int n = 0; n < (ALIGNED ? DIM : NS); ++n) acc = __fma_rn(Q[n], ld_tab<TAB_SMEM>(sp + n), acc);
       double blk[BS];
       blk[0] = acc;
+      store_pair<P, BS>(Ke, A.colstride, a, b, blk);
+    }
+  } else if (ALIGNED) {
+    // axis-aligned elasticity (contract of the oracle's orc_element_aligned):
+    // g = sum beta_n S_n, K_ii = fma(alpha_i, S_i, g), h = b_m A_m,
+    // K_ij = fma(a_m, S_m, h), K_ji = fma(a_m, S_m, -h); a == b: a_m S_m
+    double al[DIM], be[DIM], am[NA], bm[NA];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      al[i] = sAff[AF_W + i];
+      be[i] = sAff[AF_W + DIM + i];
+    }
+#pragma unroll
+    for (int m = 0; m < NA; ++m) {
+      am[m] = sAff[AF_W + 2 * DIM + m];
+      bm[m] = sAff[AF_W + 2 * DIM + NA + m];
+    }
+    for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
+      int a, b;
+      pair_decode(pi, npe, a, b);
+      const double *sp = Rp + (size_t)pi * 9;
+      double sv[NS], av[NA];
+#pragma unroll
+      for (int n = 0; n < NS; ++n) sv[n] = ld_tab<TAB_SMEM>(sp + n);
+#pragma unroll
+      for (int n = 0; n < NA; ++n) av[n] = ld_tab<TAB_SMEM>(sp + 6 + n);
+      double g = __dmul_rn(be[0], sv[0]);
+#pragma unroll
+      for (int n = 1; n < DIM; ++n) g = __fma_rn(be[n], sv[n], g);
+      double blk[BS];
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) blk[i * DIM + i] = __fma_rn(al[i], sv[i], g);
+#pragma unroll
+      for (int m = 0; m < NA; ++m) {
+        const int i = sym_k<DIM>(DIM + m), j = sym_l<DIM>(DIM + m);
+        if (a != b) {
+          const double h = __dmul_rn(bm[m], av[m]);
+          blk[i * DIM + j] = __fma_rn(am[m], sv[DIM + m], h);
+          blk[j * DIM + i] = __fma_rn(am[m], sv[DIM + m], -h);
+        } else {
+          const double v = __dmul_rn(am[m], sv[DIM + m]);
+          blk[i * DIM + j] = v;
+          blk[j * DIM + i] = v;
+        }
+      }
       store_pair<P, BS>(Ke, A.colstride, a, b, blk);
     }
   } else {
@@ -153,22 +207,18 @@ __device__ __forceinline__ void affine_pairs(const ElemArgs &A, const double *sA
     for (int pi = threadIdx.x; pi < A.npairs; pi += blockDim.x) {
       int a, b;
       pair_decode(pi, npe, a, b);
-      const double *sp = A.Rp + (size_t)pi * 9;
+      const double *sp = Rp + (size_t)pi * 9;
       double sv[NS], av[NA];
 #pragma unroll
-      for (int n = 0; n < NS; ++n) sv[n] = __ldg(sp + n);
+      for (int n = 0; n < NS; ++n) sv[n] = ld_tab<TAB_SMEM>(sp + n);
 #pragma unroll
-      for (int n = 0; n < NA; ++n) av[n] = __ldg(sp + 6 + n);
+      for (int n = 0; n < NA; ++n) av[n] = ld_tab<TAB_SMEM>(sp + 6 + n);
       double ks[NS];
 #pragma unroll
       for (int m = 0; m < NS; ++m) {
         double acc = 0.0;
-        if (ALIGNED && m >= DIM) {
-          acc = __dmul_rn(W[m * NS + m], sv[m]);
-        } else {
 #pragma unroll
-          for (int n = 0; n < (ALIGNED ? DIM : NS); ++n) acc = __fma_rn(W[m * NS + n], sv[n], acc);
-        }
+        for (int n = 0; n < NS; ++n) acc = __fma_rn(W[m * NS + n], sv[n], acc);
         ks[m] = acc;
       }
       double blk[BS];
@@ -178,12 +228,8 @@ __device__ __forceinline__ void affine_pairs(const ElemArgs &A, const double *sA
 #pragma unroll
         for (int m = 0; m < NA; ++m) {
           double acc = 0.0;
-          if (ALIGNED) {
-            acc = __dmul_rn(U[m * NA + m], av[m]);
-          } else {
 #pragma unroll
-            for (int n = 0; n < NA; ++n) acc = __fma_rn(U[m * NA + n], av[n], acc);
-          }
+          for (int n = 0; n < NA; ++n) acc = __fma_rn(U[m * NA + n], av[n], acc);
           const int i = sym_k<DIM>(DIM + m), j = sym_l<DIM>(DIM + m);
           blk[i * DIM + j] = __dadd_rn(ks[DIM + m], acc);
           blk[j * DIM + i] = __dsub_rn(ks[DIM + m], acc);
@@ -247,12 +293,18 @@ k_elem_fp64(ElemArgs A) {
     const double c2 = (KIND == KIND_ELASTIC) ? A.c2[mat] : 0.0;
     double *Ke = A.Kf + (size_t)e * npe * A.colstride;
     if (A.aflag && A.aflag[e]) {  // uniform across the CTA
-      if (threadIdx.x < 32) affine_stage<DIM>(A.ageo + (size_t)e * 10, c1, c2, sAff, A.status);
+      const bool aligned = A.aflag[e] == 2;   // uniform across the CTA
+      if (threadIdx.x < 32) {
+        if (aligned)
+          affine_stage_aligned<DIM>(A.ageo + (size_t)e * 10, c1, c2, sAff, A.status, threadIdx.x);
+        else
+          affine_stage<DIM>(A.ageo + (size_t)e * 10, c1, c2, sAff, A.status, threadIdx.x);
+      }
       __syncthreads();
-      if (A.aflag[e] == 2)
-        affine_pairs<KIND, DIM, P, BS, true>(A, sAff, Ke);
+      if (aligned)
+        affine_pairs<KIND, DIM, P, BS, true>(A, sAff, Ke, A.Rp, A.Mp);
       else
-        affine_pairs<KIND, DIM, P, BS, false>(A, sAff, Ke);
+        affine_pairs<KIND, DIM, P, BS, false>(A, sAff, Ke, A.Rp, A.Mp);
     } else {
       for (int t = threadIdx.x; t < npe * DIM; t += blockDim.x) {
         int a = t / DIM, i = t % DIM;
@@ -359,6 +411,114 @@ k_elem_fp64(ElemArgs A) {
     }
     __syncthreads();
   }
+}
+
+// Affine-element kernel with staged stores, for meshes whose elements are
+// all affine (k_affine_geometry counted no other): one CTA per element at a
+// time (grid-stride, persistent).  The pair table (the parts of R_ab, or
+// Mref_ab) is copied into shared memory once per CTA by a bulk copy
+// (cp.async.bulk completing on an mbarrier; a bounded wait).  Each element
+// matrix is built in a shared-memory image of its Kf run (the same layout,
+// column padding included) and leaves with one bulk store (cp.async.bulk
+// global <- shared), which drains while the CTA forms the next element's
+// coefficients; the warp that forms them rotates from element to element.
+// The arithmetic is affine_pairs', so Kf holds what k_elem_fp64 writes.
+// Shared memory: image [npe * colstride] | table [tab_n, even] | sAff |
+// mbarrier.
+__device__ __forceinline__ uint32_t sh_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t now_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait on an mbarrier phase (2 s); false on timeout.
+__device__ __forceinline__ bool bar_wait(uint64_t *bar, unsigned parity) {
+  const uint64_t t0 = now_ns();
+  for (;;) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok) : "r"(sh_addr(bar)), "r"(parity) : "memory");
+    if (ok) return true;
+    if (now_ns() - t0 > 2000000000ull) return false;
+  }
+}
+
+constexpr int AFFK_MAX_THREADS = 256;
+
+template <int KIND, int DIM>
+__global__ void __launch_bounds__(AFFK_MAX_THREADS)
+k_elem_affine(ElemArgs A, int tab_n) {
+  extern __shared__ __align__(128) double smem_a[];
+  constexpr int BS = (KIND == KIND_ELASTIC) ? DIM * DIM : 1;
+  constexpr int P = (KIND == KIND_ELASTIC) ? DIM : 1;
+  const int64_t kelems = (int64_t)A.npe * A.colstride;
+  const unsigned ke_bytes = (unsigned)(kelems * 8);
+  double *sKe = smem_a;
+  double *sTab = sKe + kelems;
+  double *sAff = sTab + ((tab_n + 1) & ~1);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sAff + AFF_DOUBLES);
+  const double *gTab = KIND == KIND_MASS ? A.Mp : A.Rp;
+  const unsigned tab_bytes = (unsigned)tab_n * 8u;
+  if ((tab_bytes & 15u) == 0 && ((uintptr_t)gTab & 15u) == 0) {
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sh_addr(bar)), "r"(1u) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sh_addr(bar)), "r"(tab_bytes)
+                   : "memory");
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                   ::"r"(sh_addr(sTab)), "l"(gTab), "r"(tab_bytes), "r"(sh_addr(bar))
+                   : "memory");
+    }
+    const bool ok = bar_wait(bar, 0);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicOr(A.status, ST_TIMEOUT);
+      return;
+    }
+  } else {
+    for (int t = threadIdx.x; t < tab_n; t += blockDim.x) sTab[t] = gTab[t];
+    __syncthreads();
+  }
+  const int nwarps = (int)(blockDim.x >> 5);
+  unsigned iter = 0;
+  for (int64_t e = blockIdx.x; e < A.nel; e += gridDim.x, ++iter) {
+    const int mat = A.emat ? A.emat[e] : 0;
+    if (mat < 0) continue;  // uniform across the CTA
+    const double c1 = A.c1[mat];
+    const double c2 = (KIND == KIND_ELASTIC) ? A.c2[mat] : 0.0;
+    const bool aligned = A.aflag[e] == 2;
+    if ((int)(threadIdx.x >> 5) == (int)((blockIdx.x + iter) % (unsigned)nwarps)) {
+      const int lane = threadIdx.x & 31;
+      if (aligned)
+        affine_stage_aligned<DIM>(A.ageo + (size_t)e * 10, c1, c2, sAff, A.status, lane);
+      else
+        affine_stage<DIM>(A.ageo + (size_t)e * 10, c1, c2, sAff, A.status, lane);
+    }
+    // the previous element's store has read the image
+    if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    __syncthreads();
+    if (aligned)
+      affine_pairs<KIND, DIM, P, BS, true, true>(A, sAff, sKe, sTab, sTab);
+    else
+      affine_pairs<KIND, DIM, P, BS, false, true>(A, sAff, sKe, sTab, sTab);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double *Ke = A.Kf + (size_t)e * kelems;
+      asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(Ke), "r"(sh_addr(sKe)),
+                   "r"(ke_bytes)
+                   : "memory");
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    }
+  }
+  if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
 // Column-node gather.  T = double (FP64 form) or float (precision form);
@@ -674,8 +834,43 @@ int launch_elem(llf_ctx *ctx, const ElemArgs &a, size_t smem, unsigned grid) {
   return LLF_OK;
 }
 
+// The staged affine kernel when every element is affine, the element has
+// enough node pairs to fill a CTA and two CTAs fit on an SM; *done = false
+// otherwise.  Threads: the node pairs in as few rounds of at most 256 as
+// possible, rounded up to whole warps (hex27: 378 pairs, 2 rounds of 192).
+template <int KIND, int DIM>
+int run_elem_affine(llf_ctx *ctx, const ElemArgs &a, bool *done) {
+  *done = false;
+  const int npairs = a.npairs;
+  if (!a.all_affine || !a.aflag || npairs < 32) return LLF_OK;
+  const int tab_n = KIND == KIND_MASS ? npairs : npairs * 9;
+  const size_t smem = sizeof(double) * ((size_t)a.npe * a.colstride + ((tab_n + 1) & ~1) + AFF_DOUBLES) + 16;
+  if (smem > 110 * 1024) return LLF_OK;
+  const int rounds = (npairs + AFFK_MAX_THREADS - 1) / AFFK_MAX_THREADS;
+  const int threads = ((npairs + rounds - 1) / rounds + 31) / 32 * 32;
+  auto fn = k_elem_affine<KIND, DIM>;
+  if (smem > 48 * 1024)
+    LLF_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  LLF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+  if (per_sm < 1) return LLF_OK;
+  if (a.cta_cap > 0 && per_sm > a.cta_cap) per_sm = a.cta_cap;
+  int64_t grid = (int64_t)ctx->num_sms * per_sm;
+  if (grid > a.nel) grid = a.nel;
+  KernelScope ks(ctx, "k_elem_affine");
+  fn<<<(unsigned)grid, threads, smem, ctx->stream>>>(a, tab_n);
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  *done = true;
+  return LLF_OK;
+}
+
 template <int KIND, int DIM>
 int run_elem(llf_ctx *ctx, ElemArgs a) {
+  {
+    bool done = false;
+    const int rc = run_elem_affine<KIND, DIM>(ctx, a, &done);
+    if (rc != LLF_OK || done) return rc;
+  }
   const int npe = a.npe, nip = a.nip;
   const int gsw = (KIND == KIND_MASS) ? 1 : DIM;
   const size_t tables = sizeof(double) * ((size_t)nip * npe * DIM + nip +
@@ -928,18 +1123,30 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
   // affine geometry of every element (built-in tables only)
   uint8_t *aflag = nullptr;
   double *ageo = nullptr;
+  unsigned long long *nonaff = nullptr;   // elements in use that are not affine
+  bool all_affine = false;
   if (mesh->d_Rp) {
     LLF_CUDA_TRY(ctx, dalloc(ctx, &aflag, mesh->nel));
     LLF_CUDA_TRY(ctx, dalloc(ctx, &ageo, (size_t)mesh->nel * 10));
-    KernelScope ks(ctx, "k_affine_geometry");
-    const unsigned g = grid_1d(mesh->nel, 128, ctx->num_sms);
-    if (dim == 3)
-      k_affine_geometry<3><<<g, 128, 0, s>>>(mesh->d_xyz, mesh->d_conn, mesh->d_emat, mesh->nel, npe,
-                                             mesh->d_dN, mesh->d_nref, ageo, aflag);
-    else
-      k_affine_geometry<2><<<g, 128, 0, s>>>(mesh->d_xyz, mesh->d_conn, mesh->d_emat, mesh->nel, npe,
-                                             mesh->d_dN, mesh->d_nref, ageo, aflag);
-    LLF_CUDA_TRY(ctx, cudaGetLastError());
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &nonaff, 1));
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(nonaff, 0, sizeof(unsigned long long), s));
+    {
+      KernelScope ks(ctx, "k_affine_geometry");
+      const unsigned g = grid_1d(mesh->nel, 128, ctx->num_sms);
+      if (dim == 3)
+        k_affine_geometry<3><<<g, 128, 0, s>>>(mesh->d_xyz, mesh->d_conn, mesh->d_emat, mesh->nel, npe,
+                                               mesh->d_dN, mesh->d_nref, ageo, aflag, nonaff);
+      else
+        k_affine_geometry<2><<<g, 128, 0, s>>>(mesh->d_xyz, mesh->d_conn, mesh->d_emat, mesh->nel, npe,
+                                               mesh->d_dN, mesh->d_nref, ageo, aflag, nonaff);
+      LLF_CUDA_TRY(ctx, cudaGetLastError());
+    }
+    if (form != LLF_FP32Q) {
+      unsigned long long h = 1;
+      LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&h, nonaff, sizeof(h), cudaMemcpyDeviceToHost, s));
+      LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+      all_affine = h == 0;
+    }
   }
   int rc = LLF_OK;
   if (form == LLF_FP32Q) {
@@ -969,6 +1176,7 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
     a.Rp = mesh->d_Rp;
     a.Mp = mesh->d_Mp;
     a.cta_cap = pat->tune.elem_cap;
+    a.all_affine = all_affine;
     // element range [e0, e1): the element-indexed arrays are offset
     auto elems = [&](int64_t e0, int64_t e1) -> int {
       ElemArgs b = a;
@@ -1000,6 +1208,7 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
   dfree(ctx, d_c2);
   dfree(ctx, aflag);
   dfree(ctx, ageo);
+  dfree(ctx, nonaff);
   if (rc == LLF_OK) rc = llf_check_status(ctx, "assembly");
   if (sink) {
     dfree(ctx, cnt);

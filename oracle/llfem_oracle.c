@@ -233,8 +233,9 @@ void orc_affine_split(int dim, const double *Rab, double *sv, double *av) {
  * (|J0_ij| <= 64 eps s, s the largest |X| of the element) the element is an
  * axis-aligned brick up to the rounding of the sums, and those entries are
  * set to +0.0 before the inverse, so that invJ and every coefficient below
- * that mixes two axes are exact zeros.  Returns det. */
-static double orc_geom_affine(int dim, int npe, const double *X, const double *dN0, double inv[9]) {
+ * that mixes two axes are exact zeros.  Returns det; *aligned = 1 then. */
+static double orc_geom_affine(int dim, int npe, const double *X, const double *dN0, double inv[9],
+                              int *aligned) {
   double J[3][3] = {{0}};
   for (int i = 0; i < dim; ++i)
     for (int j = 0; j < dim; ++j) {
@@ -254,6 +255,7 @@ static double orc_geom_affine(int dim, int npe, const double *X, const double *d
     for (int i = 0; i < dim; ++i)
       for (int j = 0; j < dim; ++j)
         if (i != j) J[i][j] = 0.0;
+  *aligned = al;
   if (dim == 3) return orc_inv3(J, inv);
   double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
   double rdet = 1.0 / det;
@@ -263,12 +265,72 @@ static double orc_geom_affine(int dim, int npe, const double *X, const double *d
   return det;
 }
 
+/* Elasticity on an axis-aligned affine element (invJ diagonal: d_k =
+ * invJ[k][k]).  With V_n = det (d_k d_l) for the symmetric component
+ * n = (k,l), the Lame combination collapses to
+ *   K_ii = (c1 + c2) V_i S_i + c2 sum_n<dim V_n S_n,
+ *   K_ij = (c1 + c2) V_m S_m + (c1 - c2) V_m A_m,  K_ji = (c1 + c2) V_m S_m - (c1 - c2) V_m A_m
+ * (m = (i,j) mixed; A = 0 when a == b).  Contract: alpha_i = cp V_i,
+ * beta_i = c2 V_i, a_m = cp V_m, b_m = cm V_m; per pair
+ * g = fma chain over n < dim of beta_n S_n (from beta_0 S_0),
+ * K_ii = fma(alpha_i, S_i, g), h_m = b_m A_m, K_ij = fma(a_m, S_m, h_m),
+ * K_ji = fma(a_m, S_m, -h_m); a == b: K_ij = K_ji = a_m S_m.
+ * 15 FP64 operations per node pair in 3D. */
+static int orc_element_aligned(int dim, int npe, const double *inv, double det, const double *R, double c1,
+                               double c2, double *Ke) {
+  const int ns = dim == 3 ? 6 : 3, na = dim == 3 ? 3 : 1;
+  const int(*sym)[2] = dim == 3 ? ORC_SYM3 : ORC_SYM2;
+  const size_t nd = (size_t)dim * npe;
+  double V[6], alpha[3], beta[3], am[3], bm[3];
+  for (int n = 0; n < ns; ++n) {
+    int k = sym[n][0], l = sym[n][1];
+    V[n] = det * (inv[k * 3 + k] * inv[l * 3 + l]);
+  }
+  const double cp = c1 + c2, cm = c1 - c2;
+  for (int i = 0; i < dim; ++i) {
+    alpha[i] = cp * V[i];
+    beta[i] = c2 * V[i];
+  }
+  for (int m = 0; m < na; ++m) {
+    am[m] = cp * V[dim + m];
+    bm[m] = cm * V[dim + m];
+  }
+  memset(Ke, 0, sizeof(double) * nd * nd);
+  for (int a = 0; a < npe; ++a)
+    for (int b = a; b < npe; ++b) {
+      double sv[6], av[3], blk[9] = {0};
+      orc_affine_split(dim, R + ((size_t)a * npe + b) * 9, sv, av);
+      double g = beta[0] * sv[0];
+      for (int n = 1; n < dim; ++n) g = fma(beta[n], sv[n], g);
+      for (int i = 0; i < dim; ++i) blk[i * dim + i] = fma(alpha[i], sv[i], g);
+      for (int m = 0; m < na; ++m) {
+        int i = sym[dim + m][0], j = sym[dim + m][1];
+        if (a != b) {
+          double h = bm[m] * av[m];
+          blk[i * dim + j] = fma(am[m], sv[dim + m], h);
+          blk[j * dim + i] = fma(am[m], sv[dim + m], -h);
+        } else {
+          blk[i * dim + j] = blk[j * dim + i] = am[m] * sv[dim + m];
+        }
+      }
+      for (int i = 0; i < dim; ++i)
+        for (int j = 0; j < dim; ++j) {
+          double v = blk[i * dim + j];
+          Ke[((size_t)a * dim + i) * nd + (size_t)b * dim + j] = v;
+          Ke[((size_t)b * dim + j) * nd + (size_t)a * dim + i] = v;
+        }
+    }
+  return 0;
+}
+
 static int orc_element_affine(int kind, int dim, int pdim, int npe, const double *dN0, const double *X,
                               const double *R, const double *Mref, double c1, double c2, double *Ke) {
   size_t nd = (size_t)pdim * npe;
   double inv[9];
-  double det = orc_geom_affine(dim, npe, X, dN0, inv);
+  int aligned = 0;
+  double det = orc_geom_affine(dim, npe, X, dN0, inv, &aligned);
   if (!(det > 0.0)) return -1;
+  if (aligned && kind == ORC_ELASTIC) return orc_element_aligned(dim, npe, inv, det, R, c1, c2, Ke);
   const int ns = dim == 3 ? 6 : 3, na = dim == 3 ? 3 : 1;
   const int(*sym)[2] = dim == 3 ? ORC_SYM3 : ORC_SYM2;
   double V[6][6], trV[6], W[6][6], U[3][3], Qh[6];
