@@ -919,6 +919,21 @@ def main():
                  "roofline_frac": bytes_alg / (sum(v["ms"] for v in oprof.values()) / args.steps * 1e-3) / 1e9 / hbm_peak,
                  "per_kernel_ms": {k: v["ms"] / max(v["launches"], 1) for k, v in oprof.items()}}
 
+    # the same assembly with stored-layout reuse off: every step counts the
+    # non-zeros, scans and compacts, as the first assembly on a pattern does
+    first = None
+    if not args.no_other_form and rank == 0:
+        os.environ["LLF_STORED_LAYOUT"] = "0"
+        try:
+            fms, fprof, _, fstored, _ = measure(form, args.steps, args.warmup)
+        finally:
+            del os.environ["LLF_STORED_LAYOUT"]
+        first = {"what": "the headline assembly without the stored layout of the previous assembly on the pattern "
+                         "(count, scan and compaction every step, as on a pattern's first assembly)",
+                 "value": world * nnz / (fms * 1e-3) / 1e9, "unit": "GNNZ/s", "ms_per_step": fms,
+                 "stored_nnz": fstored,
+                 "per_kernel_ms": {k: v["ms"] / max(v["launches"], 1) for k, v in fprof.items()}}
+
     # the FP64 form on the same mesh turned about a skew axis through its
     # centre: every element stays affine but none is axis-aligned, so the
     # element kernel runs the full 51-operation node-pair form instead of the
@@ -1007,7 +1022,7 @@ def main():
                "stored_nnz": stored, "pattern_build_s": pattern_s, "autotune": tuned,
                "parallelism": "replicas" if world > 1 else "single",
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-               "clocks": clocks, "other_form": other, "general_geometry": general,
+               "clocks": clocks, "other_form": other, "without_layout_reuse": first, "general_geometry": general,
                "precision_form_error": precision, "samples": samples}
         print(json.dumps(out), flush=True)
     if world > 1:

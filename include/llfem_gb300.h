@@ -213,7 +213,21 @@ int llf_pattern_destroy(llf_ctx *ctx, llf_pattern *pat);
 /* ======================================================================== */
 /* All assembly calls create a new device matrix on the pattern, fill the
  * structural values, then apply dropzeros!.  Material arrays hold one value
- * per material index (nmat entries). `form` is LLF_FP64 or LLF_FP32Q. */
+ * per material index (nmat entries). `form` is LLF_FP64 or LLF_FP32Q.
+ *
+ * Stored layouts.  A pattern keeps the stored (dropzeros'ed) column layout
+ * of its last assembly of each operator and form (stiffness, mass, heat; a
+ * few at a time).  The next such assembly on the pattern writes its stored
+ * CSC straight from the gather into that layout and checks every column's
+ * non-zero count; if a count differs, the assembly counts and compacts the
+ * usual way and keeps the new layout.  The arrays returned are the same
+ * either way.  A matrix assembled into a kept layout holds the stored CSC
+ * only; its structural values (the solvers' format) are expanded from it on
+ * the first call that needs them (llf_pcg*, llf_matrix_spmv,
+ * llf_matrix_copy_structural, llf_matrix_axpby, llf_heat_fdm, or
+ * llf_matrix_prepare), except llf_pcg_noalloc, which refuses such a matrix.
+ * LLF_STORED_LAYOUT=0 in the environment turns the reuse off.  Not used for
+ * lumped mass matrices, nor for assemblies that accumulate into a matrix. */
 
 /* K = sum_e sum_q B^T D B b detJ w — stiffnessMatrix / stiffnessMatrixSolid,
  * src/linear.jl:70-87, :154-188, :190-330.  ptype LLF_SOLID,
@@ -435,6 +449,12 @@ int llf_matrix_nnz(llf_ctx *ctx, const llf_matrix *m, int64_t *nnz);
 int llf_matrix_copy_csc(llf_ctx *ctx, const llf_matrix *m, int64_t *colptr,
                         int64_t *rowval, double *nzval);
 
+/* Make the matrix's structural values resident: expands them from the
+ * stored CSC when its assembly wrote the stored CSC only (allocates the
+ * structural array), else does nothing.  Call it before llf_pcg_noalloc on
+ * a matrix assembled into a kept stored layout. */
+int llf_matrix_prepare(llf_ctx *ctx, llf_matrix *m);
+
 /* Structural values (length = structural nnz of the pattern) to host. */
 int llf_matrix_copy_structural(llf_ctx *ctx, const llf_matrix *m,
                                double *nzval);
@@ -534,7 +554,9 @@ int llf_heat_fdm(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C,
  * z.r after a sweep preconditioner)
  * and writes every other work vector before reading it.  Calls whose work
  * overlaps on the GPU (two contexts or threads at once) race on the array:
- * serialise them. */
+ * serialise them.  The matrix's structural values must be resident (see
+ * llf_matrix_prepare); a matrix that holds its stored CSC only is refused
+ * with LLF_ERR_STATE. */
 int llf_pcg_noalloc(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                     const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
                     int64_t *iters, double *relres);

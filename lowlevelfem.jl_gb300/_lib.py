@@ -95,6 +95,7 @@ SIGNATURES = {
     "llf_matrix_nnz": (i32, [vp, vp, P_i64]),
     "llf_matrix_copy_csc": (i32, [vp, vp, P_i64, P_i64, P_dbl]),
     "llf_matrix_copy_structural": (i32, [vp, vp, P_dbl]),
+    "llf_matrix_prepare": (i32, [vp, vp]),
     "llf_matrix_axpby": (i32, [vp, dbl, vp, dbl, vp, PP]),
     "llf_matrix_from_structural": (i32, [vp, vp, P_dbl, PP]),
     "llf_matrix_spmv": (i32, [vp, vp, P_dbl, P_dbl]),
@@ -393,6 +394,10 @@ class DeviceMatrix:
         self.ctx.check(lib().llf_matrix_copy_csc(self.ctx.h, self.h, ptr(colptr, C.c_int64),
                                                  ptr(rowval, C.c_int64), ptr(nzval, C.c_double)))
         return colptr, rowval, nzval
+
+    def prepare(self):
+        """Make the structural values resident (llf_matrix_prepare)."""
+        self.ctx.check(lib().llf_matrix_prepare(self.ctx.h, self.h))
 
     def copy_structural(self):
         nz = np.zeros(self.pattern.nnz)

@@ -510,6 +510,7 @@ int llf_pattern_destroy(llf_ctx *ctx, llf_pattern *p) {
     dfree(ctx, p->d_pos);
     dfree(ctx, p->d_gather_nodes);
     dfree(ctx, p->d_keep_prev);
+    pattern_free_layouts(ctx, p);
     ic0_coloring_free(ctx, p);
     cudaStreamSynchronize(ctx->stream);
   }
@@ -709,6 +710,10 @@ int llf_assemble_form(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int form_k
     kind = KIND_MASS;
   } else {
     return llf_fail(ctx, LLF_ERR_ARG, "llf_assemble_form: form_kind");
+  }
+  if (accumulate && accumulate->pat == pat && !accumulate->diagonal_only) {
+    const int rc = matrix_ensure_nz(ctx, accumulate);
+    if (rc != LLF_OK) return rc;
   }
   if (accumulate && (accumulate->pat != pat || accumulate->diagonal_only || !accumulate->d_nz))
     return llf_fail(ctx, LLF_ERR_STATE, "llf_assemble_form: csc_matrix must be a full matrix on the same pattern");
@@ -1004,10 +1009,21 @@ int llf_matrix_copy_csc(llf_ctx *ctx, const llf_matrix *m, int64_t *colptr, int6
   return llf_ok(ctx);
 }
 
+int llf_matrix_prepare(llf_ctx *ctx, llf_matrix *m) {
+  if (!ctx) return LLF_ERR_ARG;
+  if (!m) return llf_fail(ctx, LLF_ERR_ARG, "llf_matrix_prepare: null matrix");
+  const int rc = matrix_ensure_nz(ctx, m);
+  return rc == LLF_OK ? llf_ok(ctx) : rc;
+}
+
 int llf_matrix_copy_structural(llf_ctx *ctx, const llf_matrix *m, double *nzval) {
   if (!ctx || !m || !nzval) return LLF_ERR_ARG;
   if (m->diagonal_only)
     return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "lumped matrix has no structural values");
+  {
+    const int rc = matrix_ensure_nz(ctx, m);
+    if (rc != LLF_OK) return rc;
+  }
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(nzval, m->d_nz, sizeof(double) * m->pat->nnz,
                                     cudaMemcpyDeviceToHost, ctx->stream));
   LLF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

@@ -582,12 +582,18 @@ __device__ __forceinline__ int nonzero_bits(double v) {
 // the accumulator starts from them and every block is added.  The column is
 // written out coalesced with its non-zero count: column (B,j) holds the
 // entries (row node t, component i) at P*t + i.
+// With spec.ptr0 the column is compacted (dropzeros!) straight into the
+// stored CSC at the layout of an earlier assembly: each DoF column's
+// non-zeros go, in row order, to [ptr0[c], ptr0[c+1]) (writes stay inside
+// that range), and a column whose count differs sets *spec.mismatch; the
+// structural values are then written only if nz is given.
 template <int P, bool BLOCKVAL, class T>
 __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__restrict__ n2e_ptr,
                             const int2 *__restrict__ n2e, const uint16_t *__restrict__ pos,
                             const T *__restrict__ Kf, int64_t cs, int npe, int64_t non, int max_deg,
                             const double *__restrict__ init, double *__restrict__ nz,
-                            int64_t *__restrict__ cnt, const int32_t *__restrict__ list) {
+                            int64_t *__restrict__ cnt, const int32_t *__restrict__ list,
+                            const int32_t *__restrict__ nadj, StoredSpec spec) {
   extern __shared__ double cg_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   constexpr int BS = BLOCKVAL ? P * P : 1;
@@ -674,17 +680,44 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
     }
 #pragma unroll
     for (int j = 0; j < P; ++j) {
-      double *out = nz + (size_t)P * P * c0 + (size_t)j * P * deg;
-      int n = 0;
-      for (int idx = lane; idx < P * deg; idx += 32) {
-        const int t = idx / P, i = idx % P;
-        const double v = (!store_first || has[t]) ? acc[(size_t)t * P * P + j * P + i] : -0.0;
-        out[idx] = v;
-        n += nonzero_bits(v);
-      }
+      double *out = nz ? nz + (size_t)P * P * c0 + (size_t)j * P * deg : nullptr;
+      if (spec.ptr0) {
+        const int64_t o = spec.ptr0[B * P + j], oend = spec.ptr0[B * P + j + 1];
+        const int32_t *rn = nadj + c0;
+        int64_t run = 0;
+        for (int i0 = 0; i0 < P * deg; i0 += 32) {  // warp-uniform chunks
+          const int idx = i0 + lane;
+          const bool valid = idx < P * deg;
+          const int t = idx / P, i = idx % P;
+          double v = 0.0;
+          if (valid) {
+            v = (!store_first || has[t]) ? acc[(size_t)t * P * P + j * P + i] : -0.0;
+            if (nz) out[idx] = v;
+          }
+          const bool keep = valid && nonzero_bits(v);
+          const unsigned bal = __ballot_sync(0xffffffffu, keep);
+          if (keep) {
+            const int64_t at = o + run + __popc(bal & ((1u << lane) - 1u));
+            if (at < oend) {
+              spec.rowval_s[at] = (int64_t)P * rn[t] + i + 1;
+              spec.nzval_s[at] = v;
+            }
+          }
+          run += __popc(bal);
+        }
+        if (lane == 0 && run != oend - o) atomicOr(spec.mismatch, 1u);
+      } else {
+        int n = 0;
+        for (int idx = lane; idx < P * deg; idx += 32) {
+          const int t = idx / P, i = idx % P;
+          const double v = (!store_first || has[t]) ? acc[(size_t)t * P * P + j * P + i] : -0.0;
+          out[idx] = v;
+          n += nonzero_bits(v);
+        }
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) n += __shfl_xor_sync(0xffffffffu, n, off);
-      if (lane == 0 && cnt) cnt[B * P + j] = n;
+        for (int off = 16; off > 0; off >>= 1) n += __shfl_xor_sync(0xffffffffu, n, off);
+        if (lane == 0 && cnt) cnt[B * P + j] = n;
+      }
     }
     __syncwarp();
   }
@@ -958,7 +991,8 @@ static int gather_split(llf_ctx *ctx, llf_pattern *pat) {
 template <int P, bool BV, class T>
 int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,
                   int npe, const T *Kf, int64_t cs, const double *init, double *nz, int64_t *cnt,
-                  int64_t B0 = 0, int64_t nB = -1) {
+                  int64_t B0 = 0, int64_t nB = -1, const StoredSpec *spec = nullptr) {
+  const StoredSpec sp = spec ? *spec : StoredSpec{};
   // column nodes [B0, B0 + nB): the node-indexed arrays are offset, the
   // offsets they hold (into n2e, pos, nz) stay absolute
   if (nB < 0) nB = pat->mesh->non - B0;
@@ -984,7 +1018,8 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const 
     if (grid > need) grid = need > 0 ? need : 1;
     KernelScope ks(ctx, "k_colgather");
     fn<<<(unsigned)grid, wpb * 32, smem, ctx->stream>>>(pat->d_nptr + b0, n2e_ptr + b0, n2e, pos, Kf, cs, npe, count,
-                                                        md, init, nz, cnt ? cnt + b0 * P : nullptr, list);
+                                                        md, init, nz, cnt ? cnt + b0 * P : nullptr, list,
+                                                        pat->d_nadj, sp);
     LLF_CUDA_TRY(ctx, cudaGetLastError());
     return LLF_OK;
   };
@@ -1007,25 +1042,50 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const 
 // ------------------------------------------------------------------ host
 template <class T>
 int gather_full_t(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,
-                  int npe, const T *Kf, int64_t cs, bool blockval, const double *init, double *nz, int64_t *cnt) {
+                  int npe, const T *Kf, int64_t cs, bool blockval, const double *init, double *nz, int64_t *cnt,
+                  StoredSpec *spec = nullptr);
+
+// The gather into a kept stored layout; if a column's count differs, the
+// usual gather (structural values and counts) follows.
+template <class T>
+int gather_spec_t(llf_ctx *ctx, llf_pattern *pat, const T *Kf, int64_t cs, bool blockval, StoredSpec *spec) {
+  int rc = gather_full_t<T>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, cs, blockval,
+                            nullptr, nullptr, nullptr, spec);
+  if (rc != LLF_OK) return rc;
+  unsigned mis = 1;
+  LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&mis, spec->mismatch, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+  LLF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (mis == 0) return LLF_OK;
+  spec->fell_back = true;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, spec->nz_slot, pat->nnz));
+  return gather_full_t<T>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, cs, blockval,
+                          nullptr, *spec->nz_slot, spec->cnt_fallback, nullptr);
+}
+
+template <class T>
+int gather_full_t(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,
+                  int npe, const T *Kf, int64_t cs, bool blockval, const double *init, double *nz, int64_t *cnt,
+                  StoredSpec *spec) {
   switch (pat->pdim * 2 + (blockval ? 1 : 0)) {
-    case 2: return run_colgather<1, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt);
-    case 3: return run_colgather<1, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt);
-    case 4: return run_colgather<2, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt);
-    case 5: return run_colgather<2, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt);
-    case 6: return run_colgather<3, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt);
-    case 7: return run_colgather<3, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt);
+    case 2: return run_colgather<1, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt, 0, -1, spec);
+    case 3: return run_colgather<1, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt, 0, -1, spec);
+    case 4: return run_colgather<2, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt, 0, -1, spec);
+    case 5: return run_colgather<2, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt, 0, -1, spec);
+    case 6: return run_colgather<3, false, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt, 0, -1, spec);
+    case 7: return run_colgather<3, true, T>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, cs, init, nz, cnt, 0, -1, spec);
   }
   return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
 }
 
 int gather_full(llf_ctx *ctx, llf_pattern *pat, const double *Kf, int64_t colstride, bool blockval,
-                double *nz, int64_t *cnt, const double *init) {
+                double *nz, int64_t *cnt, const double *init, StoredSpec *spec) {
+  if (spec) return gather_spec_t<double>(ctx, pat, Kf, colstride, blockval, spec);
   return gather_full_t<double>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, colstride,
                                blockval, init, nz, cnt);
 }
 int gather_full32(llf_ctx *ctx, llf_pattern *pat, const float *Kf, int64_t colstride, bool blockval,
-                  double *nz, int64_t *cnt, const double *init) {
+                  double *nz, int64_t *cnt, const double *init, StoredSpec *spec) {
+  if (spec) return gather_spec_t<float>(ctx, pat, Kf, colstride, blockval, spec);
   return gather_full_t<float>(ctx, pat, pat->d_n2e_ptr, pat->d_n2e, pat->d_pos, pat->mesh->npe, Kf, colstride,
                               blockval, init, nz, cnt);
 }
@@ -1034,7 +1094,64 @@ int gather_full_ext(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, cons
   return gather_full_t<double>(ctx, pat, n2e_ptr, n2e, pos, npe, Kf, colstride, blockval, nullptr, nz, cnt);
 }
 
-int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts) {
+// Structural values from the stored CSC, one warp per DoF column: the
+// column's structural entries are zeroed, then each stored entry finds its
+// structural position (its row node by binary search in the column's node
+// list, sorted) and is written there.
+template <int P>
+__global__ void k_expand_nz(const int64_t *__restrict__ colptr, const int64_t *__restrict__ nptr,
+                            const int32_t *__restrict__ nadj, int64_t ndof, const int64_t *__restrict__ colptr_s,
+                            const int64_t *__restrict__ rowval_s, const double *__restrict__ nzval_s,
+                            double *__restrict__ nz, unsigned *__restrict__ status) {
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  for (int64_t c = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5); c < ndof; c += (int64_t)gridDim.x * wpb) {
+    const int64_t s = colptr[c], len = colptr[c + 1] - s;
+    const int64_t c0 = nptr[c / P];
+    const int deg = (int)(nptr[c / P + 1] - c0);
+    for (int64_t l = lane; l < len; l += 32) nz[s + l] = 0.0;
+    __syncwarp();
+    const int64_t o0 = colptr_s[c] - 1, o1 = colptr_s[c + 1] - 1;
+    for (int64_t k = o0 + lane; k < o1; k += 32) {
+      const int64_t r = rowval_s[k] - 1;
+      const int32_t node = (int32_t)(r / P);
+      int lo = 0, hi = deg - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (nadj[c0 + mid] < node) lo = mid + 1; else hi = mid;
+      }
+      if (deg > 0 && nadj[c0 + lo] == node) {
+        nz[s + (int64_t)P * lo + r % P] = nzval_s[k];
+      } else {
+        atomicOr(status, ST_PATTERN);
+      }
+    }
+  }
+}
+
+int matrix_ensure_nz(llf_ctx *ctx, const llf_matrix *cm) {
+  llf_matrix *m = const_cast<llf_matrix *>(cm);
+  if (m->d_nz || m->diagonal_only) return LLF_OK;
+  if (!m->d_colptr_s) return llf_fail(ctx, LLF_ERR_STATE, "matrix has neither structural nor stored values");
+  llf_pattern *pat = m->pat;
+  const int64_t n = pat->ndof;
+  LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nz, pat->nnz > 0 ? pat->nnz : 1));
+  unsigned g = grid_1d(n * 32, 256, ctx->num_sms);
+  KernelScope ks(ctx, "k_expand_nz");
+  switch (pat->pdim) {
+#define LLF_EXPAND(PP)                                                                                          \
+  k_expand_nz<PP><<<g, 256, 0, ctx->stream>>>(pat->d_colptr, pat->d_nptr, pat->d_nadj, n, m->d_colptr_s,       \
+                                              m->d_rowval_s, m->d_nzval_s, m->d_nz, ctx->d_status)
+    case 1: LLF_EXPAND(1); break;
+    case 2: LLF_EXPAND(2); break;
+    case 3: LLF_EXPAND(3); break;
+#undef LLF_EXPAND
+    default: return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pdim must be 1, 2 or 3");
+  }
+  LLF_CUDA_TRY(ctx, cudaGetLastError());
+  return llf_check_status(ctx, "structural values from the stored CSC");
+}
+
+int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts, int64_t **ptr0_out) {
   llf_pattern *pat = m->pat;
   const int64_t n = pat->ndof;
   cudaStream_t s = ctx->stream;
@@ -1095,8 +1212,57 @@ int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts) {
   }
   LLF_CUDA_TRY(ctx, cudaGetLastError());
   if (cnt != counts) dfree(ctx, cnt);
-  dfree(ctx, ptr0);
+  if (ptr0_out) {
+    *ptr0_out = ptr0;
+  } else {
+    dfree(ctx, ptr0);
+  }
   return LLF_OK;
+}
+
+// ------------------------------------------------------- stored layouts
+namespace {
+
+llf_pattern::StoredLayout *layout_find(llf_pattern *pat, int kind, int form) {
+  for (auto &l : pat->layouts)
+    if (l.d_ptr0 && l.kind == kind && l.form == form) return &l;
+  return nullptr;
+}
+
+// Keep ptr0 (ndof + 1, taken over) as the layout of (kind, form): in the
+// slot of the same operator and form, else an empty one, else the least
+// recently used.
+void layout_store(llf_ctx *ctx, llf_pattern *pat, int kind, int form, int64_t *ptr0, int64_t total) {
+  llf_pattern::StoredLayout *slot = layout_find(pat, kind, form);
+  if (!slot)
+    for (auto &l : pat->layouts)
+      if (!l.d_ptr0) { slot = &l; break; }
+  if (!slot) {
+    slot = &pat->layouts[0];
+    for (auto &l : pat->layouts)
+      if (l.used < slot->used) slot = &l;
+  }
+  dfree(ctx, slot->d_ptr0);
+  slot->kind = kind;
+  slot->form = form;
+  slot->total = total;
+  slot->d_ptr0 = ptr0;
+  slot->used = ++pat->layout_clock;
+}
+
+// Stored-layout reuse is on unless LLF_STORED_LAYOUT=0.
+bool layout_reuse_enabled() {
+  const char *v = getenv("LLF_STORED_LAYOUT");
+  return !(v && v[0] == '0');
+}
+
+}  // namespace
+
+void pattern_free_layouts(llf_ctx *ctx, llf_pattern *pat) {
+  for (auto &l : pat->layouts) {
+    dfree(ctx, l.d_ptr0);
+    l = llf_pattern::StoredLayout{};
+  }
 }
 
 int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int ptype,
@@ -1119,7 +1285,29 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_c1, c1, sizeof(double) * nmat, cudaMemcpyHostToDevice, s));
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(d_c2, c2 ? c2 : c1, sizeof(double) * nmat,
                                     cudaMemcpyHostToDevice, s));
-  if (!sink) LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nz, pat->nnz));
+  // the stored layout of the last assembly of this operator and form on
+  // the pattern: the gather then writes the stored CSC itself, and the
+  // structural values are left to matrix_ensure_nz
+  const bool reuse = !sink && !init && !(kind == KIND_MASS && lumped) && !m->keep_pattern && layout_reuse_enabled();
+  llf_pattern::StoredLayout *lay = reuse ? layout_find(pat, kind, form) : nullptr;
+  StoredSpec spec;
+  unsigned *d_mis = nullptr;
+  if (lay) {
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_rowval_s, lay->total > 0 ? lay->total : 1));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nzval_s, lay->total > 0 ? lay->total : 1));
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &d_mis, 1));
+    LLF_CUDA_TRY(ctx, cudaMemsetAsync(d_mis, 0, sizeof(unsigned), s));
+    spec.ptr0 = lay->d_ptr0;
+    spec.rowval_s = m->d_rowval_s;
+    spec.nzval_s = m->d_nzval_s;
+    spec.mismatch = d_mis;
+    spec.nz_slot = &m->d_nz;
+    spec.cnt_fallback = cnt;
+  } else if (!sink) {
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nz, pat->nnz));
+  }
+  StoredSpec *sp = lay ? &spec : nullptr;
+  int64_t *ptr0 = nullptr;   // the stored layout of this assembly, kept on the pattern
   // affine geometry of every element (built-in tables only)
   uint8_t *aflag = nullptr;
   double *ageo = nullptr;
@@ -1150,7 +1338,7 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
   }
   int rc = LLF_OK;
   if (form == LLF_FP32Q) {
-    rc = assemble_fp32_impl(ctx, mesh, pat, kind, d_c1, d_c2, aflag, ageo, m->d_nz, cnt, init, sink);
+    rc = assemble_fp32_impl(ctx, mesh, pat, kind, d_c1, d_c2, aflag, ageo, m->d_nz, cnt, init, sink, sp);
   } else {
     double *Kf = nullptr;
     const int64_t cs = kf_colstride(npe, BS, (int)sizeof(double));
@@ -1200,7 +1388,7 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
       rc = sink->gather(ctx, pat, Kf, cs, kind == KIND_ELASTIC, elems);
     } else {
       rc = elems(0, mesh->nel);
-      if (rc == LLF_OK) rc = gather_full(ctx, pat, Kf, cs, kind == KIND_ELASTIC, m->d_nz, cnt, init);
+      if (rc == LLF_OK) rc = gather_full(ctx, pat, Kf, cs, kind == KIND_ELASTIC, m->d_nz, cnt, init, sp);
     }
     dfree(ctx, Kf);
   }
@@ -1224,7 +1412,31 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
                                                                    pat->ndof, m->d_diag);
     }
   }
-  if (rc == LLF_OK) rc = matrix_finalize(ctx, m, (kind == KIND_MASS && lumped) ? nullptr : cnt);
+  if (lay && rc == LLF_OK) {
+    dfree(ctx, d_mis);
+    if (!spec.fell_back) {  // every column's count matched: the stored CSC is complete
+      m->nnz_s = lay->total;
+      LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_colptr_s, pat->ndof + 1));
+      {
+        KernelScope ks(ctx, "k_colptr_1based");
+        k_colptr_1based<<<grid_1d(pat->ndof + 1, 256, ctx->num_sms), 256, 0, s>>>(lay->d_ptr0, pat->ndof + 1,
+                                                                                 m->d_colptr_s);
+      }
+      LLF_CUDA_TRY(ctx, cudaGetLastError());
+      lay->used = ++pat->layout_clock;
+      dfree(ctx, cnt);
+      return LLF_OK;
+    }
+    // a column's count differed: the gather ran again the usual way
+    dfree(ctx, m->d_rowval_s);
+    dfree(ctx, m->d_nzval_s);
+    rc = matrix_finalize(ctx, m, cnt, reuse ? &ptr0 : nullptr);
+  } else {
+    dfree(ctx, d_mis);
+    if (rc == LLF_OK)
+      rc = matrix_finalize(ctx, m, (kind == KIND_MASS && lumped) ? nullptr : cnt, reuse ? &ptr0 : nullptr);
+  }
+  if (rc == LLF_OK && ptr0) layout_store(ctx, pat, kind, form, ptr0, m->nnz_s);
   dfree(ctx, cnt);
   return rc;
 }
@@ -1252,6 +1464,14 @@ __global__ void k_scale(double a, const double *__restrict__ x, double *__restri
 
 int matrix_axpby_impl(llf_ctx *ctx, double a, const llf_matrix *A, double b,
                       const llf_matrix *B, llf_matrix *C) {
+  if (!A->diagonal_only) {
+    const int rc = matrix_ensure_nz(ctx, A);
+    if (rc != LLF_OK) return rc;
+  }
+  if (!B->diagonal_only) {
+    const int rc = matrix_ensure_nz(ctx, B);
+    if (rc != LLF_OK) return rc;
+  }
   if (A->pat != B->pat)
     return llf_fail(ctx, LLF_ERR_STATE, "axpby: matrices live on different patterns");
   C->pat = A->pat;

@@ -532,7 +532,7 @@ int run_elem32(llf_ctx *ctx, Elem32Args a) {
 // per-column non-zero counts into cnt).
 int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, const double *d_c1,
                        const double *d_c2, const uint8_t *aflag, const double *ageo, double *nz,
-                       int64_t *cnt, const double *init, GatherSink *sink) {
+                       int64_t *cnt, const double *init, GatherSink *sink, StoredSpec *spec) {
   const int npe = mesh->npe, P = pat->pdim;
   float *Kf = nullptr;
   const int64_t cs = kf_colstride(npe, kf_bstride(P, kind == KIND_ELASTIC, (int)sizeof(float)), (int)sizeof(float));
@@ -616,7 +616,7 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
     rc = sink->gather(ctx, pat, Kf, cs, kind == KIND_ELASTIC, elems);
   } else {
     rc = elems(0, mesh->nel);
-    if (rc == LLF_OK) rc = gather_full32(ctx, pat, Kf, cs, kind == KIND_ELASTIC, nz, cnt, init);
+    if (rc == LLF_OK) rc = gather_full32(ctx, pat, Kf, cs, kind == KIND_ELASTIC, nz, cnt, init, spec);
   }
   dfree(ctx, coef);
   dfree(ctx, Kf);

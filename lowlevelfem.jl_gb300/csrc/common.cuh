@@ -147,11 +147,42 @@ struct llf_pattern {
   // keep bits of the last values-only assembly on this pattern (assemble.cu):
   // the next one reports whether its bits differ
   unsigned *d_keep_prev = nullptr;
+  // stored layouts of recent assemblies on this pattern (assemble.cu), one
+  // per operator and arithmetic form: the 0-based start of every stored
+  // (dropzeros'ed) column.  The next assembly of the same operator and form
+  // writes its stored CSC straight from the gather into this layout and
+  // checks every column's count; a column whose count differs sends the
+  // assembly through the counting compaction instead.
+  struct StoredLayout {
+    int kind = -1, form = -1;
+    int64_t total = 0;
+    int64_t *d_ptr0 = nullptr;   // ndof + 1
+    uint64_t used = 0;
+  };
+  StoredLayout layouts[4];
+  uint64_t layout_clock = 0;
+};
+
+// The stored layout an assembly's gather writes into (assemble.cu).  When
+// a column's count differs, the gather is run again the usual way: the
+// structural values go to *nz_slot (allocated then) and the column counts
+// to cnt_fallback, and fell_back is set.
+struct StoredSpec {
+  const int64_t *ptr0 = nullptr;   // 0-based stored column starts, ndof + 1
+  int64_t *rowval_s = nullptr;     // 1-based rows, total entries
+  double *nzval_s = nullptr;
+  unsigned *mismatch = nullptr;    // device: set when a column's stored count differs
+  double **nz_slot = nullptr;
+  int64_t *cnt_fallback = nullptr;
+  bool fell_back = false;
 };
 
 struct llf_matrix {
   llf_pattern *pat = nullptr;
-  double *d_nz = nullptr;         // structural values (pattern->nnz)
+  // structural values (pattern->nnz).  An assembly that wrote its stored
+  // CSC straight into a kept layout leaves them to matrix_ensure_nz, which
+  // expands them from the stored CSC on the first use that needs them.
+  double *d_nz = nullptr;
   bool diagonal_only = false;     // lumped mass: values live on the diagonal
   bool keep_pattern = false;      // stored form keeps every structural entry (no dropzeros!)
   double *d_diag = nullptr;       // ndof (diagonal_only)
@@ -245,23 +276,32 @@ int autotune_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
                   const double *c2, int nmat, int form, int trials, std::string *report);
 // dropzeros -> stored form; counts (non-zeros per DoF column) may come from
 // the gather, else they are counted here
-int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts);
+int matrix_finalize(llf_ctx *ctx, llf_matrix *m, int64_t *counts, int64_t **ptr0_out = nullptr);
+// frees the pattern's stored layouts (assemble.cu)
+void pattern_free_layouts(llf_ctx *ctx, llf_pattern *pat);
+// The structural values of m, expanded from its stored CSC if the assembly
+// left them out (assemble.cu): the stored entries at their structural
+// positions, +0.0 at the others.  Allocates; a no-op when they exist.
+int matrix_ensure_nz(llf_ctx *ctx, const llf_matrix *m);
 // assemble_fp32.cu: precision form (FP32 quadrature, FP64 accumulation) into nz
 // aflag/ageo: per-element affine flag and invJ/det (null: quadrature form only)
 int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
                        const double *d_c1, const double *d_c2, const uint8_t *aflag,
                        const double *ageo, double *nz, int64_t *cnt, const double *init = nullptr,
-                       GatherSink *sink = nullptr);
+                       GatherSink *sink = nullptr, StoredSpec *spec = nullptr);
 // Element-ordered column-node gather of whole element matrices laid out as
 // Kf[element][column node][row node][block] (blockval: pdim x pdim blocks,
 // entry (i,j) at i*pdim+j; otherwise one scalar per node pair placed on the
 // component diagonal).  Column (e, b) starts at Kf + (e*npe + b)*colstride
 // (colstride >= npe*block size, in elements).  Writes the structural values
 // and, if cnt != NULL, the non-zero count of every DoF column.
+// With spec, the gather writes the stored CSC into spec's layout instead
+// (and no structural values), checking every column's count against it; see
+// StoredSpec for a count that differs.
 int gather_full(llf_ctx *ctx, llf_pattern *pat, const double *Kf, int64_t colstride, bool blockval,
-                double *nz, int64_t *cnt, const double *init = nullptr);
+                double *nz, int64_t *cnt, const double *init = nullptr, StoredSpec *spec = nullptr);
 int gather_full32(llf_ctx *ctx, llf_pattern *pat, const float *Kf, int64_t colstride, bool blockval,
-                  double *nz, int64_t *cnt, const double *init = nullptr);
+                  double *nz, int64_t *cnt, const double *init = nullptr, StoredSpec *spec = nullptr);
 // The same gather for another element set on the pattern's nodes (e.g.
 // boundary faces): its node -> element lists, element-to-column map and npe.
 int gather_full_ext(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,

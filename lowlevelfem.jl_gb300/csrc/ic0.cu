@@ -644,6 +644,10 @@ static bool ic0_fp32_factor() {
 
 int ic0_factor(llf_ctx *ctx, const llf_matrix *m, const uint8_t *d_fixed, const std::vector<int64_t> &seg_nodes,
                const int32_t *d_node_seg, Ic0Factor *f) {
+  {
+    const int rc = matrix_ensure_nz(ctx, m);
+    if (rc != LLF_OK) return rc;
+  }
   const bool f32 = ic0_fp32_factor();
   switch (m->pat->pdim * 2 + (f32 ? 1 : 0)) {
     case 2: return ic0_factor_tt<1, double>(ctx, m, d_fixed, seg_nodes, d_node_seg, f);

@@ -1707,6 +1707,10 @@ int pcg_noalloc_typed(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doub
 int pcg_noalloc_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                      const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
                      int64_t *iters, double *relres) {
+  if (!m->d_nz && !m->diagonal_only)
+    return llf_fail(ctx, LLF_ERR_STATE,
+                    "llf_pcg_noalloc: the matrix's structural values are not expanded yet (its assembly wrote the "
+                    "stored CSC only); run llf_pcg or llf_matrix_spmv on it once first");
   if (m->diagonal_only)
     return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "llf_pcg_noalloc: lumped (diagonal) matrix");
   const int64_t n = m->pat->ndof;
@@ -1724,6 +1728,10 @@ int pcg_noalloc_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doubl
 }
 
 int spmv_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_x, double *d_y) {
+  {
+    const int rc = matrix_ensure_nz(ctx, m);
+    if (rc != LLF_OK) return rc;
+  }
   const int64_t n = m->pat->ndof;
   const unsigned grid = (unsigned)(ctx->num_sms * 4);
   if (m->diagonal_only) {
@@ -1746,6 +1754,10 @@ int spmv_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_x, double *d_y)
 int pcg_batched_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
                      const uint8_t *d_fixed, int nseg, const int64_t *seg_off, int precond,
                      double reltol, int64_t maxiter, int64_t *iters, double *relres, bool mixed) {
+  {
+    const int rc = matrix_ensure_nz(ctx, m);
+    if (rc != LLF_OK) return rc;
+  }
   if (m->diagonal_only)
     return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "pcg on a lumped (diagonal) matrix");
   switch (m->pat->pdim) {
@@ -1759,6 +1771,10 @@ int pcg_batched_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, doubl
 int pcg_impl(llf_ctx *ctx, const llf_matrix *m, const double *d_b, double *d_x,
              const uint8_t *d_fixed, int precond, double reltol, int64_t maxiter,
              int64_t *iters, double *relres) {
+  {
+    const int rc = matrix_ensure_nz(ctx, m);
+    if (rc != LLF_OK) return rc;
+  }
   const int64_t off[2] = {0, m->pat->ndof};
   return pcg_batched_impl(ctx, m, d_b, d_x, d_fixed, 1, off, precond, reltol, maxiter, iters, relres);
 }
@@ -1903,6 +1919,11 @@ int fdm_typed(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C, const doub
 int heat_fdm_impl(llf_ctx *ctx, const llf_matrix *K, const llf_matrix *C, const double *d_q, int nq, double *d_T,
                   const uint8_t *d_fixed, int64_t nsteps, double dt, double theta, int precond, double reltol,
                   int64_t maxiter, int64_t *iters_total) {
+  {
+    int rc = matrix_ensure_nz(ctx, K);
+    if (rc == LLF_OK) rc = matrix_ensure_nz(ctx, C);
+    if (rc != LLF_OK) return rc;
+  }
   switch (K->pat->pdim) {
     case 1: return fdm_typed<1>(ctx, K, C, d_q, nq, d_T, d_fixed, nsteps, dt, theta, precond, reltol, maxiter, iters_total);
     case 2: return fdm_typed<2>(ctx, K, C, d_q, nq, d_T, d_fixed, nsteps, dt, theta, precond, reltol, maxiter, iters_total);
@@ -2262,6 +2283,10 @@ int prepare(llf_ctx *ctx, const llf_matrix *K, const double *b, const double *x0
             int precond, double reltol, int64_t maxiter, System **out) {
   if (!ctx || !K || !b || !x0 || !fixed || !out) return LLF_ERR_ARG;
   if (K->diagonal_only) return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "engine: lumped (diagonal) matrix");
+  {
+    const int rc = matrix_ensure_nz(ctx, K);
+    if (rc != LLF_OK) return rc;
+  }
   if (precond < LLF_PRECOND_NONE || precond > LLF_PRECOND_BJACOBI)
     return llf_fail(ctx, LLF_ERR_UNSUPPORTED, "engine: preconditioner must be none, Jacobi or block Jacobi");
   auto *sy = new System();

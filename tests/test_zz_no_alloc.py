@@ -84,3 +84,19 @@ def test_noalloc_refuses_ic0(llf):
     _, K, f, fixed = _system(llf, 2, order=1)
     with pytest.raises(llf.LLFError, match="IC\\(0\\) is not supported"):
         _noalloc(llf, K, f, np.zeros_like(f), fixed, 3, 1e-8, 10)
+
+
+def test_noalloc_after_layout_reuse_needs_prepare(llf):
+    """A matrix assembled into the stored layout its pattern kept holds the
+    stored CSC only: llf_pcg_noalloc refuses it until llf_matrix_prepare has
+    expanded its structural values; then it solves as llf_pcg does."""
+    P, K1, f, fixed = _system(llf, 3, order=2)
+    K = llf.stiffnessMatrix(P)   # second assembly on the pattern: the kept layout
+    x0 = np.zeros_like(f)
+    with pytest.raises(llf.LLFError, match="not expanded"):
+        _noalloc(llf, K, f, x0, fixed, 1, 1e-10, 20 * len(f))
+    K.dm.prepare()
+    got, it, _ = _noalloc(llf, K, f, x0, fixed, 1, 1e-10, 20 * len(f))
+    ref, it_ref, _ = K1.dm.pcg(f, x0, fixed, precond=1, reltol=1e-10, maxiter=20 * len(f))
+    assert it == it_ref
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-14 * np.abs(ref).max())
