@@ -469,6 +469,52 @@ def run_batched(args, llf):
             "plain_gpu": plain, "kernels_ms_traced_pass": kernels_ms}
 
 
+def run_c2_solve(llf, n, reltol=1e-10):
+    """Config 2 end to end through the public API (the reference's
+    stiffnessMatrix, massMatrix, loadVector and solveDisplacement,
+    src/linear.jl:70-87, :1843-2004, :3088-3434, :3711-3870): hex27 n^3 unit
+    cube, E = 2.1e5, nu = 0.3, rho = 7.85e-9; K and the consistent M in FP64;
+    face x = 0 clamped, face x = 1 under a uniform traction of 1 along x;
+    IC(0)-preconditioned CG to a relative residual of reltol.  The solution's
+    true residual on the free DoFs is measured with the library's product,
+    and M's entries must sum to 3 rho V (V = 1)."""
+    import numpy as np
+    llf.structured_box_mesh(n=n, order=ORDER)
+    mat = llf.Material("body", E=E, nu=NU, rho=7.85e-9)
+    P = llf.Problem([mat], type="Solid")
+    P.device_mesh()
+    P.pattern()
+    ctx = P._ctx
+    ts = {}
+    t0 = time.perf_counter()
+    K = llf.stiffnessMatrix(P)
+    ctx.sync()
+    ts["stiffness_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    M = llf.massMatrix(P, lumped=False)
+    ctx.sync()
+    ts["mass_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    f = llf.loadVector(P, [llf.load("right", fx=1.0)])
+    ts["load_s"] = time.perf_counter() - t0
+    sup = [llf.displacementConstraint("left", ux=0, uy=0, uz=0)]
+    t0 = time.perf_counter()
+    u = llf.solveDisplacement(K, f, support=sup, iterative=True, reltol=reltol, preconditioner="ic0",
+                              maxiter=20 * P.non)
+    ts["solve_s"] = time.perf_counter() - t0
+    fixed = np.zeros(3 * P.non, dtype=bool)
+    fixed[llf.constrainedDoFs(P, sup) - 1] = True
+    fa = f.a[:, 0]
+    r = (fa - K.dm.spmv(u.a[:, 0]))[~fixed]
+    msum = float(M.dm.copy_csc()[2].sum())
+    return {"workload": workload_name(n) + "-clamped-traction", "dofs": 3 * P.non, "stored_nnz_K": K.nnz(),
+            "stored_nnz_M": M.nnz(), "precond": "ic0", "reltol": reltol, "cg_iterations": int(u.iterations),
+            "relres_reported": float(u.relres),
+            "true_relres_free": float(np.linalg.norm(r) / np.linalg.norm(fa[~fixed])),
+            "mass_sum_rel_err": abs(msum - 3 * 7.85e-9) / (3 * 7.85e-9),
+            **ts, "total_s": sum(ts.values())}
+
+
 def run_serving(args, llf):
     """Serving configuration: a Poisson stream (200 req/s) of steady heat
     requests through llf_server; p50/p99 latency and solves/s, against the same
@@ -993,6 +1039,10 @@ def main():
                                   if k in r}
         except Exception as ex:
             samples["batched"] = {"error": str(ex)}
+        try:
+            samples["c2_solve"] = run_c2_solve(llf, args.n)
+        except Exception as ex:
+            samples["c2_solve"] = {"error": str(ex)}
         try:
             sargs = _ap.Namespace(**{**vars(args), "requests": 100, "precond": None, "server": "engine",
                                      "max_systems": 256, "rate": 200.0, "one_sample": 0})
