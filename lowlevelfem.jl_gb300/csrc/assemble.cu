@@ -549,15 +549,18 @@ __device__ __forceinline__ double widen(float f) {
   return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) | bits));
 }
 
+// The accumulator holds P planes, one per DoF column j of the column node,
+// ps doubles apart; plane j holds the column's entries (row node t,
+// component i) at P*t + i, the order they are written out in.
 template <int P, bool BLOCKVAL, bool FIRST, class T>
-__device__ __forceinline__ void add_block(double *acc, int t, const T *v) {
-  double *dst = acc + (size_t)t * P * P;  // [t][j][i]
+__device__ __forceinline__ void add_block(double *acc, int t, const T *v, int ps) {
+  double *dst = acc + (size_t)t * P;
 #pragma unroll
   for (int i = 0; i < P; ++i)
 #pragma unroll
     for (int j = 0; j < P; ++j) {
       double x = BLOCKVAL ? widen(v[i * P + j]) : (i == j ? widen(v[0]) : 0.0);
-      dst[j * P + i] = FIRST ? x : __dadd_rn(dst[j * P + i], x);
+      dst[j * ps + i] = FIRST ? x : __dadd_rn(dst[j * ps + i], x);
     }
 }
 
@@ -582,6 +585,9 @@ __device__ __forceinline__ int nonzero_bits(double v) {
 // the accumulator starts from them and every block is added.  The column is
 // written out coalesced with its non-zero count: column (B,j) holds the
 // entries (row node t, component i) at P*t + i.
+// all_touched: every row position of a column receives a block (a gather
+// over the pattern's own element lists), so the marks are not read when the
+// column is written out.
 // With spec.ptr0 the column is compacted (dropzeros!) straight into the
 // stored CSC at the layout of an earlier assembly: each DoF column's
 // non-zeros go, in row order, to [ptr0[c], ptr0[c+1]) (writes stay inside
@@ -593,13 +599,14 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
                             const T *__restrict__ Kf, int64_t cs, int npe, int64_t non, int max_deg,
                             const double *__restrict__ init, double *__restrict__ nz,
                             int64_t *__restrict__ cnt, const int32_t *__restrict__ list,
-                            const int32_t *__restrict__ nadj, StoredSpec spec) {
+                            const int32_t *__restrict__ nadj, StoredSpec spec, int all_touched) {
   extern __shared__ double cg_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   constexpr int BS = BLOCKVAL ? P * P : 1;
   constexpr int BSTR = kf_bstride(P, BLOCKVAL, (int)sizeof(T));  // stored block stride
   constexpr bool VEC = sizeof(T) == 4 && BSTR % 4 == 0;           // 16-byte block loads
   double *acc = cg_smem + (size_t)wib * max_deg * P * P;
+  const int ps = max_deg * P;  // accumulator plane stride
   unsigned char *has = reinterpret_cast<unsigned char *>(cg_smem + (size_t)wpb * max_deg * P * P) +
                        (size_t)wib * ((max_deg + 7) & ~7);
   const int nw = (int)non, wstride = (int)gridDim.x * wpb;  // node counts fit int32 (nadj holds int32 nodes)
@@ -613,7 +620,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
       const double *src = init + (size_t)P * P * c0;
       for (int idx = lane; idx < deg * P * P; idx += 32) {
         const int j = idx / (P * deg), r = idx - j * P * deg;
-        acc[(size_t)(r / P) * P * P + j * P + r % P] = src[idx];
+        acc[(size_t)j * ps + r] = src[idx];
       }
     } else {
       for (int t = lane; t < deg; t += 32) has[t] = 0;
@@ -649,10 +656,10 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
         }
         if (act && tc != 0xffffu) {  // the lanes of one element hold distinct positions
           if (store_first && !has[tc]) {
-            add_block<P, BLOCKVAL, true>(acc, (int)tc, cur);
+            add_block<P, BLOCKVAL, true>(acc, (int)tc, cur, ps);
             has[tc] = 1;
           } else {
-            add_block<P, BLOCKVAL, false>(acc, (int)tc, cur);
+            add_block<P, BLOCKVAL, false>(acc, (int)tc, cur, ps);
           }
         }
         __syncwarp();
@@ -668,10 +675,10 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
           const unsigned t = pos[(s + k) * npe + a];
           if (t != 0xffffu) {
             if (store_first && !has[t]) {
-              add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BSTR);
+              add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BSTR, ps);
               has[t] = 1;
             } else {
-              add_block<P, BLOCKVAL, false>(acc, (int)t, col + (size_t)a * BSTR);
+              add_block<P, BLOCKVAL, false>(acc, (int)t, col + (size_t)a * BSTR, ps);
             }
           }
         }
@@ -691,7 +698,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
           const int t = idx / P, i = idx % P;
           double v = 0.0;
           if (valid) {
-            v = (!store_first || has[t]) ? acc[(size_t)t * P * P + j * P + i] : -0.0;
+            v = (!store_first || all_touched || has[t]) ? acc[(size_t)j * ps + idx] : -0.0;
             if (nz) out[idx] = v;
           }
           const bool keep = valid && nonzero_bits(v);
@@ -710,7 +717,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
         int n = 0;
         for (int idx = lane; idx < P * deg; idx += 32) {
           const int t = idx / P, i = idx % P;
-          const double v = (!store_first || has[t]) ? acc[(size_t)t * P * P + j * P + i] : -0.0;
+          const double v = (!store_first || all_touched || has[t]) ? acc[(size_t)j * ps + idx] : -0.0;
           out[idx] = v;
           n += nonzero_bits(v);
         }
@@ -1019,7 +1026,7 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const 
     KernelScope ks(ctx, "k_colgather");
     fn<<<(unsigned)grid, wpb * 32, smem, ctx->stream>>>(pat->d_nptr + b0, n2e_ptr + b0, n2e, pos, Kf, cs, npe, count,
                                                         md, init, nz, cnt ? cnt + b0 * P : nullptr, list,
-                                                        pat->d_nadj, sp);
+                                                        pat->d_nadj, sp, n2e_ptr == pat->d_n2e_ptr ? 1 : 0);
     LLF_CUDA_TRY(ctx, cudaGetLastError());
     return LLF_OK;
   };
