@@ -378,6 +378,7 @@ int llf_mesh_upload(llf_ctx *ctx, int dim, int64_t non, const double *xyz, int64
 
 int llf_mesh_update(llf_ctx *ctx, llf_mesh *m, const double *xyz, const int64_t *conn) {
   if (!ctx || !m || !xyz) return LLF_ERR_ARG;
+  m->geo_version++;
   LLF_CUDA_TRY(ctx, cudaMemcpyAsync(m->d_xyz, xyz, sizeof(double) * 3 * m->non,
                                     cudaMemcpyHostToDevice, ctx->stream));
   if (conn) {
@@ -399,6 +400,7 @@ int llf_mesh_update(llf_ctx *ctx, llf_mesh *m, const double *xyz, const int64_t 
 
 int llf_mesh_set_materials(llf_ctx *ctx, llf_mesh *m, const int32_t *elem_mat) {
   if (!ctx || !m) return LLF_ERR_ARG;
+  m->geo_version++;
   dfree(ctx, m->d_emat);
   if (elem_mat) {
     LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_emat, m->nel));
@@ -424,6 +426,7 @@ int llf_mesh_destroy(llf_ctx *ctx, llf_mesh *m) {
     dfree(ctx, m->d_nref); dfree(ctx, m->d_Rp); dfree(ctx, m->d_Mp);
     dfree(ctx, m->d_Rpf); dfree(ctx, m->d_Mpf);
     dfree(ctx, m->d_wf); dfree(ctx, m->d_Nf); dfree(ctx, m->d_dNf);
+    dfree(ctx, m->d_aflag); dfree(ctx, m->d_ageo);
     cudaStreamSynchronize(ctx->stream);
   }
   delete m;

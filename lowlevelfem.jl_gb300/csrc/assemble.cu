@@ -1315,33 +1315,44 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
   }
   StoredSpec *sp = lay ? &spec : nullptr;
   int64_t *ptr0 = nullptr;   // the stored layout of this assembly, kept on the pattern
-  // affine geometry of every element (built-in tables only)
+  // affine geometry of every element (built-in tables only), kept on the
+  // mesh until its coordinates, connectivity, materials or tables change
   uint8_t *aflag = nullptr;
   double *ageo = nullptr;
-  unsigned long long *nonaff = nullptr;   // elements in use that are not affine
   bool all_affine = false;
   if (mesh->d_Rp) {
-    LLF_CUDA_TRY(ctx, dalloc(ctx, &aflag, mesh->nel));
-    LLF_CUDA_TRY(ctx, dalloc(ctx, &ageo, (size_t)mesh->nel * 10));
-    LLF_CUDA_TRY(ctx, dalloc(ctx, &nonaff, 1));
-    LLF_CUDA_TRY(ctx, cudaMemsetAsync(nonaff, 0, sizeof(unsigned long long), s));
-    {
-      KernelScope ks(ctx, "k_affine_geometry");
-      const unsigned g = grid_1d(mesh->nel, 128, ctx->num_sms);
-      if (dim == 3)
-        k_affine_geometry<3><<<g, 128, 0, s>>>(mesh->d_xyz, mesh->d_conn, mesh->d_emat, mesh->nel, npe,
-                                               mesh->d_dN, mesh->d_nref, ageo, aflag, nonaff);
-      else
-        k_affine_geometry<2><<<g, 128, 0, s>>>(mesh->d_xyz, mesh->d_conn, mesh->d_emat, mesh->nel, npe,
-                                               mesh->d_dN, mesh->d_nref, ageo, aflag, nonaff);
-      LLF_CUDA_TRY(ctx, cudaGetLastError());
-    }
-    if (form != LLF_FP32Q) {
+    if (mesh->geo_cached != mesh->geo_version || mesh->geo_cached_tables != mesh->tables_version ||
+        !mesh->d_aflag) {
+      mesh->geo_cached = -1;
+      if (!mesh->d_aflag) {
+        LLF_CUDA_TRY(ctx, dalloc(ctx, &mesh->d_aflag, mesh->nel));
+        LLF_CUDA_TRY(ctx, dalloc(ctx, &mesh->d_ageo, (size_t)mesh->nel * 10));
+      }
+      unsigned long long *nonaff = nullptr;   // elements in use that are not affine
+      LLF_CUDA_TRY(ctx, dalloc(ctx, &nonaff, 1));
+      LLF_CUDA_TRY(ctx, cudaMemsetAsync(nonaff, 0, sizeof(unsigned long long), s));
+      {
+        KernelScope ks(ctx, "k_affine_geometry");
+        const unsigned g = grid_1d(mesh->nel, 128, ctx->num_sms);
+        if (dim == 3)
+          k_affine_geometry<3><<<g, 128, 0, s>>>(mesh->d_xyz, mesh->d_conn, mesh->d_emat, mesh->nel, npe,
+                                                 mesh->d_dN, mesh->d_nref, mesh->d_ageo, mesh->d_aflag, nonaff);
+        else
+          k_affine_geometry<2><<<g, 128, 0, s>>>(mesh->d_xyz, mesh->d_conn, mesh->d_emat, mesh->nel, npe,
+                                                 mesh->d_dN, mesh->d_nref, mesh->d_ageo, mesh->d_aflag, nonaff);
+        LLF_CUDA_TRY(ctx, cudaGetLastError());
+      }
       unsigned long long h = 1;
       LLF_CUDA_TRY(ctx, cudaMemcpyAsync(&h, nonaff, sizeof(h), cudaMemcpyDeviceToHost, s));
       LLF_CUDA_TRY(ctx, cudaStreamSynchronize(s));
-      all_affine = h == 0;
+      dfree(ctx, nonaff);
+      mesh->geo_all_affine = h == 0;
+      mesh->geo_cached = mesh->geo_version;
+      mesh->geo_cached_tables = mesh->tables_version;
     }
+    aflag = mesh->d_aflag;
+    ageo = mesh->d_ageo;
+    all_affine = mesh->geo_all_affine;
   }
   int rc = LLF_OK;
   if (form == LLF_FP32Q) {
@@ -1401,9 +1412,6 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
   }
   dfree(ctx, d_c1);
   dfree(ctx, d_c2);
-  dfree(ctx, aflag);
-  dfree(ctx, ageo);
-  dfree(ctx, nonaff);
   if (rc == LLF_OK) rc = llf_check_status(ctx, "assembly");
   if (sink) {
     dfree(ctx, cnt);

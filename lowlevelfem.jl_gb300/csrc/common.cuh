@@ -94,6 +94,14 @@ struct llf_mesh {
   float *d_wf = nullptr, *d_Nf = nullptr, *d_dNf = nullptr;
   int tables_version = 0;
   int conn_version = 0;           // bumped when llf_mesh_update changes the connectivity
+  int geo_version = 0;            // bumped by every coordinate, connectivity or material upload
+  // affine geometry of the elements (assemble.cu), kept for the geometry
+  // version and tables it was computed from: per element the flag and
+  // J^-1, det (k_affine_geometry), and whether every element in use is affine
+  uint8_t *d_aflag = nullptr;
+  double *d_ageo = nullptr;
+  int geo_cached = -1, geo_cached_tables = -1;
+  bool geo_all_affine = false;
   // affine-element tables (built-in rules, whose node coordinates are known;
   // null after llf_tables_upload): reference node coordinates [npe*3] and,
   // per upper-triangle node pair (a <= b, a-major), R_ab [9] and Mref_ab

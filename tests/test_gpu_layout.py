@@ -103,3 +103,22 @@ def test_reused_matrix_solves_like_a_fresh_one(llf):
     u1, it1, _ = K1.dm.pcg(f, x0, fixed, precond=1, reltol=1e-10, maxiter=20 * n)
     u2, it2, _ = K2.dm.pcg(f, x0, fixed, precond=1, reltol=1e-10, maxiter=20 * n)
     assert it1 == it2 and np.array_equal(u1, u2)
+
+
+def test_geometry_kept_until_the_mesh_changes(llf, orc):
+    """The affine geometry is kept on the device mesh between assemblies and
+    recomputed after a coordinate upload: turning the mesh and turning it
+    back gives the oracle's matrices each time."""
+    m = llf.structured_box_mesh(n=3, order=2)
+    mat = llf.Material("body", E=2.1e5, nu=0.3)
+    p = llf.Problem([mat], type="Solid")
+    rule = llf._lib.builtin_rule(m.family, m.order)
+    xyz0 = m.xyz.copy()
+    c, s_ = np.cos(0.4), np.sin(0.4)
+    turned = (xyz0 - 0.5) @ np.array([[c, -s_, 0], [s_, c, 0], [0, 0, 1.0]]).T + 0.5
+    dm = p.device_mesh()
+    for xyz in (xyz0, turned, turned, xyz0, xyz0):
+        dm.update(xyz, m.conn)
+        K = llf.stiffnessMatrix(p)
+        ref = orc.assemble(orc.ELASTIC, 0, 3, 3, xyz, m.conn, rule, [mat.E, mat.nu])
+        assert_csc_identical(K.csc(), ref.julia(), "after a coordinate upload")
