@@ -599,7 +599,8 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
                             const T *__restrict__ Kf, int64_t cs, int npe, int64_t non, int max_deg,
                             const double *__restrict__ init, double *__restrict__ nz,
                             int64_t *__restrict__ cnt, const int32_t *__restrict__ list,
-                            const int32_t *__restrict__ nadj, StoredSpec spec, int all_touched) {
+                            const int32_t *__restrict__ nadj, StoredSpec spec, int all_touched,
+                            int first_marked) {
   extern __shared__ double cg_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   constexpr int BS = BLOCKVAL ? P * P : 1;
@@ -622,7 +623,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
         const int j = idx / (P * deg), r = idx - j * P * deg;
         acc[(size_t)j * ps + r] = src[idx];
       }
-    } else {
+    } else if (!first_marked) {
       for (int t = lane; t < deg; t += 32) has[t] = 0;
     }
     const bool store_first = init == nullptr;
@@ -655,7 +656,12 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
           tn = pos[(s + k + 1) * npe + lane];
         }
         if (act && tc != 0xffffu) {  // the lanes of one element hold distinct positions
-          if (store_first && !has[tc]) {
+          if (first_marked) {  // the map marks each position's first block
+            if (store_first && (tc & 0x8000u))
+              add_block<P, BLOCKVAL, true>(acc, (int)(tc & 0x7fffu), cur, ps);
+            else
+              add_block<P, BLOCKVAL, false>(acc, (int)(tc & 0x7fffu), cur, ps);
+          } else if (store_first && !has[tc]) {
             add_block<P, BLOCKVAL, true>(acc, (int)tc, cur, ps);
             has[tc] = 1;
           } else {
@@ -672,9 +678,15 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
         const int2 el = n2e[s + k];
         const T *col = Kf + ((size_t)el.x * npe + el.y) * cs;
         for (int a = lane; a < npe; a += 32) {
-          const unsigned t = pos[(s + k) * npe + a];
-          if (t != 0xffffu) {
-            if (store_first && !has[t]) {
+          const unsigned raw = pos[(s + k) * npe + a];
+          const unsigned t = (first_marked && raw != 0xffffu) ? (raw & 0x7fffu) : raw;
+          if (raw != 0xffffu) {
+            if (first_marked) {
+              if (store_first && (raw & 0x8000u))
+                add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BSTR, ps);
+              else
+                add_block<P, BLOCKVAL, false>(acc, (int)t, col + (size_t)a * BSTR, ps);
+            } else if (store_first && !has[t]) {
               add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BSTR, ps);
               has[t] = 1;
             } else {
@@ -995,6 +1007,36 @@ static int gather_split(llf_ctx *ctx, llf_pattern *pat) {
   return LLF_OK;
 }
 
+// Marks, once per pattern, the first block of every row position in the
+// pattern's element-to-column map: per column node B (a warp each), its
+// elements in ascending order, and the first element whose block reaches a
+// row position gets bit 15 of that map entry (positions fit 15 bits).  The
+// gather then stores that block and adds the later ones without keeping
+// per-position marks of its own.
+__global__ void k_mark_first(const int64_t *__restrict__ nptr, const int64_t *__restrict__ n2e_ptr,
+                             uint16_t *__restrict__ pos, int npe, int64_t non, int max_deg) {
+  extern __shared__ unsigned char mf_has[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  unsigned char *has = mf_has + (size_t)wib * ((max_deg + 7) & ~7);
+  for (int64_t B = (int64_t)blockIdx.x * wpb + wib; B < non; B += (int64_t)gridDim.x * wpb) {
+    const int deg = (int)(nptr[B + 1] - nptr[B]);
+    const int64_t s = n2e_ptr[B];
+    const int nb = (int)(n2e_ptr[B + 1] - s);
+    for (int t = lane; t < deg; t += 32) has[t] = 0;
+    __syncwarp();
+    for (int k = 0; k < nb; ++k) {
+      for (int a = lane; a < npe; a += 32) {  // the lanes of one element hold distinct positions
+        const unsigned raw = pos[(s + k) * npe + a];
+        if (raw < 0x8000u && !has[raw]) {
+          has[raw] = 1;
+          pos[(s + k) * npe + a] = (uint16_t)(raw | 0x8000u);
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
 template <int P, bool BV, class T>
 int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const int2 *n2e, const uint16_t *pos,
                   int npe, const T *Kf, int64_t cs, const double *init, double *nz, int64_t *cnt,
@@ -1005,6 +1047,22 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const 
   if (nB < 0) nB = pat->mesh->non - B0;
   if (pat->conn_version != pat->mesh->conn_version)
     return llf_fail(ctx, LLF_ERR_STATE, "the mesh connectivity changed after the pattern was built; rebuild it");
+  // the pattern's own map: each position's first block marked (once)
+  bool first_marked = false;
+  const int mdm = pat->max_deg > 0 ? pat->max_deg : 1;
+  if (pos == pat->d_pos && mdm < 0x7fff) {
+    if (!pat->pos_first) {
+      const int mw = 4;
+      const size_t msm = (size_t)mw * ((mdm + 7) & ~7);
+      KernelScope ks(ctx, "k_mark_first");
+      k_mark_first<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((pat->mesh->non + mw - 1) / mw,
+                                                                    (int64_t)ctx->num_sms * 8)),
+                     mw * 32, msm, ctx->stream>>>(pat->d_nptr, pat->d_n2e_ptr, pat->d_pos, npe, pat->mesh->non, mdm);
+      LLF_CUDA_TRY(ctx, cudaGetLastError());
+      pat->pos_first = true;
+    }
+    first_marked = true;
+  }
   auto fn = k_colgather<P, BV, T>;
   // one launch over `count` column nodes (the list's, or [B0, B0 + count))
   // with an accumulator of md row positions per warp
@@ -1026,7 +1084,8 @@ int run_colgather(llf_ctx *ctx, llf_pattern *pat, const int64_t *n2e_ptr, const 
     KernelScope ks(ctx, "k_colgather");
     fn<<<(unsigned)grid, wpb * 32, smem, ctx->stream>>>(pat->d_nptr + b0, n2e_ptr + b0, n2e, pos, Kf, cs, npe, count,
                                                         md, init, nz, cnt ? cnt + b0 * P : nullptr, list,
-                                                        pat->d_nadj, sp, n2e_ptr == pat->d_n2e_ptr ? 1 : 0);
+                                                        pat->d_nadj, sp, n2e_ptr == pat->d_n2e_ptr ? 1 : 0,
+                                                        first_marked ? 1 : 0);
     LLF_CUDA_TRY(ctx, cudaGetLastError());
     return LLF_OK;
   };

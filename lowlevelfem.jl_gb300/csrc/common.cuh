@@ -130,6 +130,9 @@ struct llf_pattern {
   // node a, the position of node conn[e][a] in B's row-node list,
   // d_pos[(n2e_ptr[B] + k) * npe + a] (0xffff: not in the pattern)
   uint16_t *d_pos = nullptr;
+  // bit 15 of a d_pos entry marks the first block of its row position in the
+  // column's element order (assemble.cu, set by the first gather)
+  bool pos_first = false;
   int conn_version = 0;           // mesh connectivity the pattern was built from
   void *ic_coloring = nullptr;    // node colouring of the IC(0) preconditioner (ic0.cu), on first use
   // the gather's column nodes in two degree classes (assemble.cu, on first
