@@ -845,8 +845,9 @@ def main():
     if form == L.FP64 and ORDER == 2:
         elem_k = "k_elem_affine" if "k_elem_affine" in prof else "k_elem_fp64"
         layout = "k_compact" not in prof   # every timed assembly wrote into the kept stored layout
-        parts = ("k_affine_geometry", elem_k, "k_colgather_layout") if layout else \
-            ("k_affine_geometry", elem_k, "k_colgather", "k_compact")
+        parts = [elem_k, "k_colgather_layout"] if layout else [elem_k, "k_colgather", "k_compact"]
+        if "k_affine_geometry" in prof:    # (kept on the mesh after the first assembly)
+            parts.insert(0, "k_affine_geometry")
         if all(k in KERNEL_DRAM_BYTES_16CUBE for k in parts):
             traffic = sum(KERNEL_DRAM_BYTES_16CUBE[k] for k in parts) * nnz / NNZ_16CUBE
         kkey = "k_colgather_layout" if (layout and kname == "k_colgather") else kname
@@ -868,8 +869,9 @@ def main():
                               "(all its launches); the element kernel's FP64 rate is under fp64"),
                 "assembly": {"kernels": "all kernels of one llf_assemble_stiffness", "ms": asm_ms,
                              "achieved": achieved, "frac": achieved / hbm_peak, "traffic": traffic,
-                             "traffic_source": "ncu dram bytes of k_affine_geometry, the element kernel, k_colgather, "
-                                               "k_compact on hex27 16^3, scaled by structural nnz" if traffic else None},
+                             "traffic_source": "ncu dram bytes of " + ", ".join(parts) + " on hex27 16^3 "
+                                               "(profiles/*_hex27_16cube.md), scaled by structural nnz"
+                                               if traffic else None},
                 "per_kernel": per_kernel,
                 "fp64": {"element_kernel_flops": flops, "achieved_tflops": fp64_achieved,
                          "dgemm_peak_tflops_measured": fp64_peak,
