@@ -1415,7 +1415,7 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
   }
   int rc = LLF_OK;
   if (form == LLF_FP32Q) {
-    rc = assemble_fp32_impl(ctx, mesh, pat, kind, d_c1, d_c2, aflag, ageo, m->d_nz, cnt, init, sink, sp);
+    rc = assemble_fp32_impl(ctx, mesh, pat, kind, d_c1, d_c2, aflag, ageo, m->d_nz, cnt, init, sink, sp, all_affine);
   } else {
     double *Kf = nullptr;
     const int64_t cs = kf_colstride(npe, BS, (int)sizeof(double));

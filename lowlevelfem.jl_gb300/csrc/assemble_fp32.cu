@@ -532,7 +532,7 @@ int run_elem32(llf_ctx *ctx, Elem32Args a) {
 // per-column non-zero counts into cnt).
 int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, const double *d_c1,
                        const double *d_c2, const uint8_t *aflag, const double *ageo, double *nz,
-                       int64_t *cnt, const double *init, GatherSink *sink, StoredSpec *spec) {
+                       int64_t *cnt, const double *init, GatherSink *sink, StoredSpec *spec, bool all_affine) {
   const int npe = mesh->npe, P = pat->pdim;
   float *Kf = nullptr;
   const int64_t cs = kf_colstride(npe, kf_bstride(P, kind == KIND_ELASTIC, (int)sizeof(float)), (int)sizeof(float));
@@ -604,6 +604,7 @@ int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
         r = kind == KIND_ELASTIC ? run_affine32<KIND_ELASTIC, 2>(ctx, b)
                                  : (kind == KIND_HEAT ? run_affine32<KIND_HEAT, 2>(ctx, b) : run_affine32<KIND_MASS, 2>(ctx, b));
       if (r != LLF_OK) return r;
+      if (all_affine) return LLF_OK;   // no element left for the general kernel
     }
     if (mesh->dim == 3)
       return kind == KIND_ELASTIC ? run_elem32<KIND_ELASTIC, 3>(ctx, b)

@@ -295,11 +295,13 @@ void pattern_free_layouts(llf_ctx *ctx, llf_pattern *pat);
 // positions, +0.0 at the others.  Allocates; a no-op when they exist.
 int matrix_ensure_nz(llf_ctx *ctx, const llf_matrix *m);
 // assemble_fp32.cu: precision form (FP32 quadrature, FP64 accumulation) into nz
-// aflag/ageo: per-element affine flag and invJ/det (null: quadrature form only)
+// aflag/ageo: per-element affine flag and invJ/det (null: quadrature form
+// only); all_affine: every element in use is affine, so the quadrature
+// kernel is not launched
 int assemble_fp32_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind,
                        const double *d_c1, const double *d_c2, const uint8_t *aflag,
                        const double *ageo, double *nz, int64_t *cnt, const double *init = nullptr,
-                       GatherSink *sink = nullptr, StoredSpec *spec = nullptr);
+                       GatherSink *sink = nullptr, StoredSpec *spec = nullptr, bool all_affine = false);
 // Element-ordered column-node gather of whole element matrices laid out as
 // Kf[element][column node][row node][block] (blockval: pdim x pdim blocks,
 // entry (i,j) at i*pdim+j; otherwise one scalar per node pair placed on the
