@@ -1,26 +1,39 @@
 // Element-operator assembly into the reference's CSC layout.
 //
 // Pipeline (one call of llf_assemble_*):
-//   k_elem_fp64   one CTA per element at a time (grid-stride, persistent):
-//                 element node coordinates gathered into shared memory, the
-//                 reference shape gradients staged in shared memory for the
-//                 CTA's lifetime (read from global memory for elements whose
-//                 tables do not fit), Jacobian / inverse / physical gradients
-//                 per integration point, then the upper-triangle node-pair
-//                 blocks of the element matrix, each written twice (block and
-//                 mirror) so the element matrix leaves the kernel whole in the
-//                 layout Kf[element][column node b][row node a][block];
+//   geometry      k_affine_geometry, once per mesh geometry (kept on the
+//                 device mesh): which elements are affine images of the
+//                 reference element (and which of those are axis-aligned
+//                 bricks), with their J^-1 and det;
+//   k_elem_affine meshes whose elements are all affine: one CTA per element
+//                 at a time (persistent), the node-pair blocks formed from
+//                 the reference pair tables into a shared-memory image of the
+//                 element matrix, which one bulk store writes out;
+//   k_elem_fp64   other meshes: one CTA per element at a time, element node
+//                 coordinates gathered into shared memory, the reference
+//                 shape gradients staged in shared memory for the CTA's
+//                 lifetime (read from global memory for elements whose tables
+//                 do not fit), Jacobian / inverse / physical gradients per
+//                 integration point (the affine form for affine elements),
+//                 then the upper-triangle node-pair blocks, each written
+//                 twice (block and mirror).  Both kernels leave the element
+//                 matrix whole in the layout Kf[element][column node b][row
+//                 node a][block];
 //   k_colgather   one warp per column node B: walks the elements around B in
 //                 ascending order; for each, the lanes read the element's
 //                 column b = local(B) — one contiguous run of npe blocks — and
 //                 add every block into a shared-memory accumulator of the
-//                 column (row position found by binary search in the column's
-//                 node list).  Each entry is thus summed over its elements in
+//                 column at the row position the pattern's element-to-column
+//                 map gives.  Each entry is thus summed over its elements in
 //                 element order, the order SparseArrays.sparse combines the
 //                 reference's triplets (src/linear.jl:314-323).  The column is
-//                 written out coalesced together with its non-zero count;
-//   finalize      dropzeros! (src/linear.jl:324): scan of the counts, then
-//                 compaction into 1-based Int64 SparseMatrixCSC arrays.
+//                 written out coalesced together with its non-zero count, or,
+//                 when the pattern kept the stored layout of an earlier
+//                 assembly of the same operator and form, compacted straight
+//                 into it (dropzeros!, every column's count checked);
+//   finalize      otherwise dropzeros! (src/linear.jl:324): scan of the
+//                 counts, then compaction into 1-based Int64 SparseMatrixCSC
+//                 arrays, whose column starts the pattern keeps.
 // Every floating-point operation of the FP64 form is an explicit IEEE
 // intrinsic (__dmul_rn, __dadd_rn, __fma_rn, __drcp_rn), so no contraction
 // or reassociation can move the result away from the CPU oracle's.
