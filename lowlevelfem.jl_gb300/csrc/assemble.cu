@@ -1382,6 +1382,15 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
     spec.mismatch = d_mis;
     spec.nz_slot = &m->d_nz;
     spec.cnt_fallback = cnt;
+    // the column pointers follow from the layout alone (recomputed if a
+    // column's count turns out to differ)
+    LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_colptr_s, pat->ndof + 1));
+    {
+      KernelScope ks(ctx, "k_colptr_1based");
+      k_colptr_1based<<<grid_1d(pat->ndof + 1, 256, ctx->num_sms), 256, 0, s>>>(lay->d_ptr0, pat->ndof + 1,
+                                                                               m->d_colptr_s);
+    }
+    LLF_CUDA_TRY(ctx, cudaGetLastError());
   } else if (!sink) {
     LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_nz, pat->nnz));
   }
@@ -1503,13 +1512,6 @@ int assemble_impl(llf_ctx *ctx, llf_mesh *mesh, llf_pattern *pat, int kind, int 
     dfree(ctx, d_mis);
     if (!spec.fell_back) {  // every column's count matched: the stored CSC is complete
       m->nnz_s = lay->total;
-      LLF_CUDA_TRY(ctx, dalloc(ctx, &m->d_colptr_s, pat->ndof + 1));
-      {
-        KernelScope ks(ctx, "k_colptr_1based");
-        k_colptr_1based<<<grid_1d(pat->ndof + 1, 256, ctx->num_sms), 256, 0, s>>>(lay->d_ptr0, pat->ndof + 1,
-                                                                                 m->d_colptr_s);
-      }
-      LLF_CUDA_TRY(ctx, cudaGetLastError());
       lay->used = ++pat->layout_clock;
       dfree(ctx, cnt);
       return LLF_OK;

@@ -9,7 +9,7 @@ import os
 import numpy as np
 import pytest
 
-from helpers import assert_csc_identical
+from helpers import PT, assert_csc_identical, make_mesh, oracle_operator
 
 pytestmark = pytest.mark.gpu
 
@@ -122,3 +122,24 @@ def test_geometry_kept_until_the_mesh_changes(llf, orc):
         K = llf.stiffnessMatrix(p)
         ref = orc.assemble(orc.ELASTIC, 0, 3, 3, xyz, m.conn, rule, [mat.E, mat.nu])
         assert_csc_identical(K.csc(), ref.julia(), "after a coordinate upload")
+
+
+@pytest.mark.parametrize("case", [("rect", 6, 2, False), ("rect", 4, 1, True), ("box", 3, 2, True)],
+                         ids=["quad9", "tri3", "tet10"])
+def test_scalar_and_plane_operators_reuse(llf, orc, case):
+    """Conduction and plane-strain stiffness assembled three times on one
+    pattern (the second and third into the kept layout): the oracle's
+    matrices each time."""
+    kind, n, order, simplex = case
+    m = make_mesh(llf, kind, n, order, simplex)
+    mat = llf.Material("body", E=2.1e5, nu=0.3, k=45.0)
+    d = m.dim
+    hp = "HeatConduction" if d == 3 else "PlaneHeatConduction"
+    ph = llf.Problem([mat], type=hp, thickness=0.5)
+    sp_ = "Solid" if d == 3 else "PlaneStrain"
+    ps = llf.Problem([mat], type=sp_, thickness=0.5)
+    refH = oracle_operator(llf, orc, m, "heat", PT[hp], mat, thickness=0.5).julia()
+    refK = oracle_operator(llf, orc, m, "stiffness", PT[sp_], mat, thickness=0.5).julia()
+    for _ in range(3):
+        assert_csc_identical(llf.heatConductionMatrix(ph).csc(), refH, f"H {case}")
+        assert_csc_identical(llf.stiffnessMatrix(ps).csc(), refK, f"K {case}")
