@@ -717,25 +717,35 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
         const int64_t o = spec.ptr0[B * P + j], oend = spec.ptr0[B * P + j + 1];
         const int32_t *rn = nadj + c0;
         int64_t run = 0;
-        for (int i0 = 0; i0 < P * deg; i0 += 32) {  // warp-uniform chunks
-          const int idx = i0 + lane;
-          const bool valid = idx < P * deg;
-          const int t = idx / P, i = idx % P;
-          double v = 0.0;
-          if (valid) {
-            v = (!store_first || all_touched || has[t]) ? acc[(size_t)j * ps + idx] : -0.0;
-            if (nz) out[idx] = v;
+        const unsigned below = (1u << lane) - 1u;
+        // warp-uniform chunks of 64 entries, two consecutive ones per lane
+        for (int i0 = 0; i0 < P * deg; i0 += 64) {
+          const int idx = i0 + 2 * lane;
+          double v[2] = {0.0, 0.0};
+          bool keep[2];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const bool valid = idx + h < P * deg;
+            if (valid) {
+              v[h] = (!store_first || all_touched || has[(idx + h) / P]) ? acc[(size_t)j * ps + idx + h] : -0.0;
+              if (nz) out[idx + h] = v[h];
+            }
+            keep[h] = valid && nonzero_bits(v[h]);
           }
-          const bool keep = valid && nonzero_bits(v);
-          const unsigned bal = __ballot_sync(0xffffffffu, keep);
-          if (keep) {
-            const int64_t at = o + run + __popc(bal & ((1u << lane) - 1u));
-            if (at < oend) {
-              spec.rowval_s[at] = (int64_t)P * rn[t] + i + 1;
-              spec.nzval_s[at] = v;
+          const unsigned b0 = __ballot_sync(0xffffffffu, keep[0]), b1 = __ballot_sync(0xffffffffu, keep[1]);
+          int64_t at = o + run + __popc(b0 & below) + __popc(b1 & below);   // the lanes before, both entries
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            if (keep[h]) {
+              if (at < oend) {
+                const int t = (idx + h) / P, i = (idx + h) % P;
+                spec.rowval_s[at] = (int64_t)P * rn[t] + i + 1;
+                spec.nzval_s[at] = v[h];
+              }
+              ++at;
             }
           }
-          run += __popc(bal);
+          run += __popc(b0) + __popc(b1);
         }
         if (lane == 0 && run != oend - o) atomicOr(spec.mismatch, 1u);
       } else {
