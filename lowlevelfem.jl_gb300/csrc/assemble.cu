@@ -542,6 +542,16 @@ k_elem_affine(ElemArgs A, int tab_n) {
 // NaN keep their payload): the precision form's gather widens every element
 // value, and GB300's FP64 pipe is kept for the additions.
 __device__ __forceinline__ double widen(double x) { return x; }
+__device__ __forceinline__ double widen(unsigned long long b) { return __longlong_as_double((long long)b); }
+// The gather holds FP64 values it only moves as their bit patterns (64-bit
+// integers), so that moving, selecting and storing them takes no FP64
+// instruction: GB300 spends its FP64 pipe per warp instruction.
+template <class T> struct GatherWord { using type = T; };
+template <> struct GatherWord<double> { using type = unsigned long long; };
+__device__ __forceinline__ unsigned long long value_bits(unsigned long long b) { return b; }
+__device__ __forceinline__ unsigned long long value_bits(float f) {
+  return (unsigned long long)__double_as_longlong(widen(f));
+}
 __device__ __forceinline__ double widen(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
@@ -565,15 +575,20 @@ __device__ __forceinline__ double widen(float f) {
 // The accumulator holds P planes, one per DoF column j of the column node,
 // ps doubles apart; plane j holds the column's entries (row node t,
 // component i) at P*t + i, the order they are written out in.
-template <int P, bool BLOCKVAL, bool FIRST, class T>
-__device__ __forceinline__ void add_block(double *acc, int t, const T *v, int ps) {
+template <int P, bool BLOCKVAL, bool FIRST, class W>
+__device__ __forceinline__ void add_block(double *acc, int t, const W *v, int ps) {
   double *dst = acc + (size_t)t * P;
+  unsigned long long *dstb = reinterpret_cast<unsigned long long *>(dst);
 #pragma unroll
   for (int i = 0; i < P; ++i)
 #pragma unroll
     for (int j = 0; j < P; ++j) {
-      double x = BLOCKVAL ? widen(v[i * P + j]) : (i == j ? widen(v[0]) : 0.0);
-      dst[j * ps + i] = FIRST ? x : __dadd_rn(dst[j * ps + i], x);
+      if (FIRST) {  // the first block of the position: its bits
+        dstb[j * ps + i] = BLOCKVAL ? value_bits(v[i * P + j]) : (i == j ? value_bits(v[0]) : 0ull);
+      } else {
+        const double x = BLOCKVAL ? widen(v[i * P + j]) : (i == j ? widen(v[0]) : 0.0);
+        dst[j * ps + i] = __dadd_rn(dst[j * ps + i], x);
+      }
     }
 }
 
@@ -619,7 +634,9 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
   constexpr int BS = BLOCKVAL ? P * P : 1;
   constexpr int BSTR = kf_bstride(P, BLOCKVAL, (int)sizeof(T));  // stored block stride
   constexpr bool VEC = sizeof(T) == 4 && BSTR % 4 == 0;           // 16-byte block loads
+  using W = typename GatherWord<T>::type;
   double *acc = cg_smem + (size_t)wib * max_deg * P * P;
+  unsigned long long *accb = reinterpret_cast<unsigned long long *>(acc);
   const int ps = max_deg * P;  // accumulator plane stride
   unsigned char *has = reinterpret_cast<unsigned char *>(cg_smem + (size_t)wpb * max_deg * P * P) +
                        (size_t)wib * ((max_deg + 7) & ~7);
@@ -634,7 +651,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
       const double *src = init + (size_t)P * P * c0;
       for (int idx = lane; idx < deg * P * P; idx += 32) {
         const int j = idx / (P * deg), r = idx - j * P * deg;
-        acc[(size_t)j * ps + r] = src[idx];
+        accb[(size_t)j * ps + r] = reinterpret_cast<const unsigned long long *>(src)[idx];
       }
     } else if (!first_marked) {
       for (int t = lane; t < deg; t += 32) has[t] = 0;
@@ -643,9 +660,9 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
     __syncwarp();
     if (npe <= 32) {
       const bool act = lane < npe;
-      T cur[BSTR], nxt[BSTR];
+      W cur[BSTR], nxt[BSTR];
       unsigned tc = 0xffffu, tn = 0xffffu;
-      auto load_block = [&](const T *v, T *dst) {
+      auto load_block = [&](const T *v, W *dst) {
         if constexpr (VEC) {
 #pragma unroll
           for (int m = 0; m < BSTR; m += 4) {
@@ -653,8 +670,9 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
             dst[m] = f.x; dst[m + 1] = f.y; dst[m + 2] = f.z; dst[m + 3] = f.w;
           }
         } else {
+          const W *vw = reinterpret_cast<const W *>(v);
 #pragma unroll
-          for (int m = 0; m < BS; ++m) dst[m] = v[m];
+          for (int m = 0; m < BS; ++m) dst[m] = vw[m];
         }
       };
       if (nb > 0 && act) {
@@ -696,14 +714,14 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
           if (raw != 0xffffu) {
             if (first_marked) {
               if (store_first && (raw & 0x8000u))
-                add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BSTR, ps);
+                add_block<P, BLOCKVAL, true>(acc, (int)t, reinterpret_cast<const W *>(col + (size_t)a * BSTR), ps);
               else
-                add_block<P, BLOCKVAL, false>(acc, (int)t, col + (size_t)a * BSTR, ps);
+                add_block<P, BLOCKVAL, false>(acc, (int)t, reinterpret_cast<const W *>(col + (size_t)a * BSTR), ps);
             } else if (store_first && !has[t]) {
-              add_block<P, BLOCKVAL, true>(acc, (int)t, col + (size_t)a * BSTR, ps);
+              add_block<P, BLOCKVAL, true>(acc, (int)t, reinterpret_cast<const W *>(col + (size_t)a * BSTR), ps);
               has[t] = 1;
             } else {
-              add_block<P, BLOCKVAL, false>(acc, (int)t, col + (size_t)a * BSTR, ps);
+              add_block<P, BLOCKVAL, false>(acc, (int)t, reinterpret_cast<const W *>(col + (size_t)a * BSTR), ps);
             }
           }
         }
@@ -721,16 +739,17 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
         // warp-uniform chunks of 64 entries, two consecutive ones per lane
         for (int i0 = 0; i0 < P * deg; i0 += 64) {
           const int idx = i0 + 2 * lane;
-          double v[2] = {0.0, 0.0};
+          unsigned long long v[2] = {0ull, 0ull};   // value bits
           bool keep[2];
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
             const bool valid = idx + h < P * deg;
             if (valid) {
-              v[h] = (!store_first || all_touched || has[(idx + h) / P]) ? acc[(size_t)j * ps + idx + h] : -0.0;
-              if (nz) out[idx + h] = v[h];
+              v[h] = (!store_first || all_touched || has[(idx + h) / P]) ? accb[(size_t)j * ps + idx + h]
+                                                                         : 0x8000000000000000ull;   // -0.0
+              if (nz) reinterpret_cast<unsigned long long *>(out)[idx + h] = v[h];
             }
-            keep[h] = valid && nonzero_bits(v[h]);
+            keep[h] = valid && (v[h] << 1) != 0ull;
           }
           const unsigned b0 = __ballot_sync(0xffffffffu, keep[0]), b1 = __ballot_sync(0xffffffffu, keep[1]);
           int64_t at = o + run + __popc(b0 & below) + __popc(b1 & below);   // the lanes before, both entries
@@ -740,7 +759,7 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
               if (at < oend) {
                 const int t = (idx + h) / P, i = (idx + h) % P;
                 spec.rowval_s[at] = (int64_t)P * rn[t] + i + 1;
-                spec.nzval_s[at] = v[h];
+                reinterpret_cast<unsigned long long *>(spec.nzval_s)[at] = v[h];
               }
               ++at;
             }
@@ -752,9 +771,10 @@ __global__ void k_colgather(const int64_t *__restrict__ nptr, const int64_t *__r
         int n = 0;
         for (int idx = lane; idx < P * deg; idx += 32) {
           const int t = idx / P, i = idx % P;
-          const double v = (!store_first || all_touched || has[t]) ? acc[(size_t)j * ps + idx] : -0.0;
-          out[idx] = v;
-          n += nonzero_bits(v);
+          const unsigned long long v =
+              (!store_first || all_touched || has[t]) ? accb[(size_t)j * ps + idx] : 0x8000000000000000ull;
+          reinterpret_cast<unsigned long long *>(out)[idx] = v;
+          n += (v << 1) != 0ull;
         }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) n += __shfl_xor_sync(0xffffffffu, n, off);
