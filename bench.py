@@ -12,6 +12,14 @@ contract: value (device-resident inputs, CUDA events on the launching
 stream), e2e (through the C-ABI from pinned host buffers: mesh upload +
 assembly + CSC copy-back), roofline of the dominant kernel, cpu_baseline,
 clocks sampled during the timed region, gpu_launches.
+
+The timed steps repeat the assembly of the same operator on the same mesh:
+the mesh's affine geometry and the pattern's stored layout come from the
+warm-up (every value and row index is computed again, and every column's
+count is checked against the layout).  without_layout_reuse times the same
+steps with LLF_STORED_LAYOUT=0; other_form, general_geometry (the mesh
+turned off its axes), precision_form_error and samples (batched, serving,
+the config-2 end-to-end solve) are reported beside the headline.
 """
 from __future__ import annotations
 
