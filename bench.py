@@ -108,6 +108,25 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float, device="cuda") -> float:
+    """The largest x over the job's ranks (the job's step time is its
+    slowest rank's); x itself without a process group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world: int, units: float, ms_step: float) -> float:
+    """Whole-job rate in units / ns (GNNZ/s for structural entries): every
+    rank assembles its own replica of the workload ("replicas only", weak
+    scaling), so the job moves world * units per step of the slowest rank."""
+    return world * units / (ms_step * 1e-3) / 1e9
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -803,16 +822,12 @@ def main():
         prof = ctx.profile_report()
         launches = ctx.launches()
         ms = [a.elapsed_time(b) for a, b in evs]
-        ms_step = sum(ms) / len(ms)
-        if world > 1:
-            t = torch.tensor([ms_step], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms_step = float(t.item())
+        ms_step = max_over_ranks(sum(ms) / len(ms))
         measure.last_steps_ms = ms   # the individual steps of this call
         return ms_step, prof, launches, stored, clk.summary()
 
     ms_step, prof, launches, stored, clocks = measure(form, args.steps, args.warmup)
-    value = world * nnz / (ms_step * 1e-3) / 1e9
+    value = job_rate(world, nnz, ms_step)
 
     bytes_alg, flops = algorithmic(mesh, nnz)
     hbm_peak, peak_kind = peaks()
