@@ -455,7 +455,9 @@ int llf_matrix_copy_csc(llf_ctx *ctx, const llf_matrix *m, int64_t *colptr,
  * a matrix assembled into a kept stored layout. */
 int llf_matrix_prepare(llf_ctx *ctx, llf_matrix *m);
 
-/* Structural values (length = structural nnz of the pattern) to host. */
+/* Structural values (length = structural nnz of the pattern) to host.  For
+ * a matrix assembled into a kept stored layout they are expanded from its
+ * stored CSC first; the entries dropzeros! removed then read +0.0. */
 int llf_matrix_copy_structural(llf_ctx *ctx, const llf_matrix *m,
                                double *nzval);
 
