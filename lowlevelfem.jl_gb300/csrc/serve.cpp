@@ -103,12 +103,13 @@ struct llf_server {
 
 namespace {
 
-// Device bytes of one request: mesh, pattern (node adjacency bounded by
-// nel*npe^2 blocks), values, stored form and the CG vectors.
+// Device bytes of one request: mesh (with the affine geometry kept on it,
+// 81 bytes per element), pattern (node adjacency bounded by nel*npe^2
+// blocks, and its stored layout), values, stored form and the CG vectors.
 int64_t estimate_footprint(const Request &r) {
   const int64_t nnz_bound = std::min<int64_t>(r.nel * (int64_t)r.npe * r.npe, r.non * r.non);
-  return r.non * 24 + r.nel * r.npe * 16 + nnz_bound * (4 + 8 + 16 + 8) + r.nel * (int64_t)r.npe * r.npe * 8 +
-         r.non * 8 * 12 + (64 << 20);
+  return r.non * 24 + r.nel * r.npe * 16 + r.nel * 88 + nnz_bound * (4 + 8 + 16 + 8) +
+         r.nel * (int64_t)r.npe * r.npe * 8 + r.non * 8 * 13 + (64 << 20);
 }
 
 void finish(llf_server *s, int64_t ticket, Result &&res, int64_t footprint) {
